@@ -1,0 +1,358 @@
+// Plain FP64 / complex<double> assembly.
+//
+// K1-K3 + K5 (element kernel, one warp per element): for each quadrature
+// point the warp forms the Jacobian, its inverse and determinant (gmsh
+// getJacobians, src/term/Assembler.cpp:131-139), evaluates the coefficient
+// programs at the physical point (EquationEvaluator::initialize,
+// src/term/evaluator/EquationEvaluator.h:155-168), maps the reference
+// gradients with J^-T (FieldEvaluator<Form1>, src/term/evaluator/FieldEvaluator.h:67-70)
+// and accumulates Ke += w det (c L)^T conj(R) (BilinearTerm::evaluate,
+// src/term/BilinearTerm.cpp:314-326) with the AFrequency factors
+// (src/term/Assembler.cpp:283-295), and b_e += w det conj(phi) f
+// (LinearTerm::evaluate, src/term/LinearTerm.cpp:182-191). Ke is symmetric
+// for these terms, so each lane owns upper-triangle entries.
+//
+// K4 (gather kernel, one warp per CSR row): walks the row's (element, local
+// test index) list in element order and adds each element row into a shared
+// accumulator at the precomputed column slots, then writes the row once.
+// This replaces MatrixFactory::addValues' binary search and atomics
+// (src/system/MatrixFactory.cpp:233-448) with a fixed-order sum, and applies
+// the Dirichlet lifting of VectorFactory::addValuesDC
+// (src/system/VectorFactory.cpp:178-210, which reads values[j*n + i], the
+// transposed element entry) and the element right-hand sides
+// (VectorFactory::addValues, :122-145).
+#include "common.cuh"
+
+namespace femg {
+
+constexpr int kWarpsPerBlockElem = 4;
+
+struct ElemWarpSmem {
+  double X[kMaxNodes * 3];
+  double J[9], Jinv[9];
+  double det;
+  double2 a, b, s;  // w det c_gradgrad, w det c_mass, w det f
+  double G[3][kMaxDofs];
+  double phi[kMaxDofs];
+  double Gs[2][3][kMaxDofs];
+  double phis[2][kMaxDofs];
+};
+
+template <int MAXENT, bool CPLX>
+__global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
+    k_element_fp64(const PlanDev p, const DevTerms terms, double *__restrict__ ke, double2 *__restrict__ be) {
+  __shared__ ElemWarpSmem smem[kWarpsPerBlockElem];
+  __shared__ uint8_t pairI[kMaxDofs * (kMaxDofs + 1) / 2], pairJ[kMaxDofs * (kMaxDofs + 1) / 2];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int n = p.nb;  // scalar field here: n == nb
+  const int nEnt = n * (n + 1) / 2;
+  for (int k = threadIdx.x; k < nEnt; k += blockDim.x) {
+    // k -> (i, j), i <= j, row-major over the upper triangle
+    int i = 0, rem = k;
+    while (rem >= n - i) {
+      rem -= n - i;
+      ++i;
+    }
+    pairI[k] = (uint8_t)i;
+    pairJ[k] = (uint8_t)(i + rem);
+  }
+  __syncthreads();
+  ElemWarpSmem &S = smem[warp];
+  const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlockElem;
+  for (int64_t e = (int64_t)blockIdx.x * kWarpsPerBlockElem + warp; e < p.E; e += stride) {
+    const int o = p.orient ? p.orient[e] : 0;
+    for (int t = lane; t < p.nn * 3; t += 32) S.X[t] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + t / 3] + t % 3];
+    __syncwarp();
+    double accR[MAXENT], accI[MAXENT];
+#pragma unroll
+    for (int m = 0; m < MAXENT; ++m) {
+      accR[m] = 0.0;
+      accI[m] = 0.0;
+    }
+    double2 bacc[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+    for (int q = 0; q < p.nq; ++q) {
+      if (lane == 0) {
+        if (q == 0 || !p.affine) {
+          S.det = jacobian(p.dim, p.nn, S.X, p.geoGrad + (size_t)q * p.nn * 3, S.J);
+          jacobianInverse(S.J, S.det, S.Jinv);
+        }
+        double xq[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < p.nn; ++k) {
+          const double g = p.geoVal[q * p.nn + k];
+          xq[0] += g * S.X[3 * k];
+          xq[1] += g * S.X[3 * k + 1];
+          xq[2] += g * S.X[3 * k + 2];
+        }
+        double2 cgg = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0), f = make_double2(0.0, 0.0);
+        for (int t = 0; t < terms.n; ++t) {
+          const DevTerm &T = terms.t[t];
+          const double2 v = evalExpr(T.coef, e, xq);
+          if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, v));
+          else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, v));
+          else if (T.kind == FG_TERM_SOURCE) f = cadd(f, v);
+        }
+        const double wd = p.w[q] * S.det;
+        S.a = make_double2(wd * cgg.x, wd * cgg.y);
+        S.b = make_double2(wd * cm.x, wd * cm.y);
+        S.s = make_double2(wd * f.x, wd * f.y);
+      }
+      __syncwarp();
+      const size_t base = ((size_t)o * p.nq + q) * p.nb;
+      for (int i = lane; i < n; i += 32) {
+        const double g0 = p.bgrad[3 * (base + i)], g1 = p.bgrad[3 * (base + i) + 1], g2 = p.bgrad[3 * (base + i) + 2];
+        const double ph = p.bval[base + i];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          const double G = S.Jinv[r] * g0 + S.Jinv[3 + r] * g1 + S.Jinv[6 + r] * g2;
+          S.G[r][i] = G;
+          S.Gs[0][r][i] = S.a.x * G;
+          if (CPLX) S.Gs[1][r][i] = S.a.y * G;
+        }
+        S.phi[i] = ph;
+        S.phis[0][i] = S.b.x * ph;
+        if (CPLX) S.phis[1][i] = S.b.y * ph;
+        // b_e[i] += w det conj(phi_i) f
+        const int slot = i >> 5;
+        bacc[slot].x += S.s.x * ph;
+        bacc[slot].y += S.s.y * ph;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int m = 0; m < MAXENT; ++m) {
+        const int k = lane + 32 * m;
+        if (k < nEnt) {
+          const int i = pairI[k], j = pairJ[k];
+          accR[m] += S.G[0][i] * S.Gs[0][0][j] + S.G[1][i] * S.Gs[0][1][j] + S.G[2][i] * S.Gs[0][2][j] + S.phi[i] * S.phis[0][j];
+          if (CPLX)
+            accI[m] += S.G[0][i] * S.Gs[1][0][j] + S.G[1][i] * S.Gs[1][1][j] + S.G[2][i] * S.Gs[1][2][j] + S.phi[i] * S.phis[1][j];
+        }
+      }
+      __syncwarp();
+    }
+    // Ke layout [E][ncomp][n][n], row = local test index, column = local unknown index
+    const int ncomp = CPLX ? 2 : 1;
+    double *K = ke + (size_t)e * ncomp * n * n;
+#pragma unroll
+    for (int m = 0; m < MAXENT; ++m) {
+      const int k = lane + 32 * m;
+      if (k < nEnt) {
+        const int i = pairI[k], j = pairJ[k];
+        K[i * n + j] = accR[m];
+        K[j * n + i] = accR[m];
+        if (CPLX) {
+          K[n * n + i * n + j] = accI[m];
+          K[n * n + j * n + i] = accI[m];
+        }
+      }
+    }
+    if (be)
+      for (int i = lane; i < n; i += 32) be[(size_t)e * n + i] = bacc[i >> 5];
+    __syncwarp();
+  }
+}
+
+int launchElementFp64(fg_plan *plan, const DevTerms &terms, double *ke, double *be, cudaStream_t s) {
+  const PlanDev &p = plan->d;
+  if (p.mult != 1 || terms.hasElastic) {
+    setLastError("FP64 element kernel: compound fields go through the elastic kernel");
+    return FG_ERR_UNSUPPORTED;
+  }
+  const int nEnt = p.nb * (p.nb + 1) / 2;
+  const int perLane = (nEnt + 31) / 32;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t blocks = (p.E + kWarpsPerBlockElem - 1) / kWarpsPerBlockElem;
+  blocks = std::min<int64_t>(blocks, (int64_t)sms * 64);
+  if (blocks < 1) blocks = 1;
+  const bool cplx = terms.complexKe != 0;
+  double2 *be2 = (double2 *)be;
+#define FG_LAUNCH_ELEM(M)                                                                                   \
+  do {                                                                                                      \
+    if (cplx) k_element_fp64<M, true><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, terms, ke, be2); \
+    else k_element_fp64<M, false><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, terms, ke, be2);  \
+  } while (0)
+  if (perLane <= 1) FG_LAUNCH_ELEM(1);
+  else if (perLane <= 8) FG_LAUNCH_ELEM(8);
+  else if (perLane <= 20) FG_LAUNCH_ELEM(20);
+  else {
+    setLastError("FP64 element kernel: more than 35 basis functions per element");
+    return FG_ERR_UNSUPPORTED;
+  }
+#undef FG_LAUNCH_ELEM
+  countLaunch();
+  FG_CUDA(cudaGetLastError());
+  return FG_OK;
+}
+
+// ------------------------------------------------------------------ gather
+
+template <typename SlotT, bool KCPLX, typename KT>
+__global__ void __launch_bounds__(256)
+    k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
+             double2 *__restrict__ values, double2 *__restrict__ rhs, int warpsPerBlock) {
+  extern __shared__ double2 acc[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  double2 *A = acc + (size_t)warp * p.maxRowLen;
+  const SlotT *slot = (const SlotT *)p.slot;
+  const SlotT kFixed = (SlotT)(sizeof(SlotT) == 1 ? 0xFF : kSlotFixed);
+  const SlotT kIgnore = (SlotT)(sizeof(SlotT) == 1 ? 0xFE : kSlotIgnore);
+  const int n = p.n;
+  const size_t nn2 = (size_t)n * n;
+  const int64_t stride = (int64_t)gridDim.x * warpsPerBlock;
+  for (int64_t row = (int64_t)blockIdx.x * warpsPerBlock + warp; row < (int64_t)p.nRows; row += stride) {
+    const uint64_t start = p.ai[row];
+    const int len = (int)(p.ai[row + 1] - start);
+    for (int s = lane; s < len; s += 32) A[s] = make_double2(0.0, 0.0);
+    __syncwarp();
+    double2 bsum = make_double2(0.0, 0.0);
+    double2 dc = make_double2(0.0, 0.0);
+    const uint64_t r0 = p.rowPtr[row], r1 = p.rowPtr[row + 1];
+    for (uint64_t r = r0; r < r1; ++r) {
+      const uint32_t packed = p.rowElem[r];
+      const int64_t e = packed >> 6;
+      const int i = packed & 63;
+      const KT *K = ke + (size_t)e * (KCPLX ? 2 : 1) * nn2;
+      const SlotT *sl = slot + ((size_t)e * n + i) * n;
+      for (int j = lane; j < n; j += 32) {
+        const SlotT sv = sl[j];
+        if (sv == kIgnore) continue;
+        if (sv != kFixed) {
+          double2 v = make_double2((double)K[i * n + j], KCPLX ? (double)K[nn2 + i * n + j] : 0.0);
+          A[sv].x += v.x;
+          A[sv].y += v.y;
+        } else {
+          // VectorFactory::addValuesDC: values[j*n + i] * valuesDC[J]
+          const double2 v = make_double2((double)K[j * n + i], KCPLX ? (double)K[nn2 + j * n + i] : 0.0);
+          dc = cadd(dc, cmul(v, uD[p.edof[e * n + j]]));
+        }
+      }
+      if (be) bsum = cadd(bsum, be[e * n + i]);
+      __syncwarp();
+    }
+    for (int s = lane; s < len; s += 32) values[start + s] = A[s];
+    if (rhs) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        dc.x += __shfl_down_sync(0xffffffffu, dc.x, off);
+        dc.y += __shfl_down_sync(0xffffffffu, dc.y, off);
+      }
+      if (lane == 0) rhs[row] = cadd(bsum, dc);
+    }
+    __syncwarp();
+  }
+}
+
+int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, const double *be, const double *dirichletDev,
+                 double *values, double *rhs, cudaStream_t s) {
+  const PlanDev &p = plan->d;
+  if (p.nRows == 0) return FG_OK;
+  const size_t rowBytes = (size_t)std::max(p.maxRowLen, 1) * sizeof(double2);
+  int wpb = (int)std::min<size_t>(8, (200 * 1024) / rowBytes);
+  if (wpb < 1) {
+    setLastError("gather: CSR row too long for shared memory");
+    return FG_ERR_UNSUPPORTED;
+  }
+  const size_t smem = rowBytes * wpb;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t blocks = ((int64_t)p.nRows + wpb - 1) / wpb;
+  blocks = std::min<int64_t>(blocks, (int64_t)sms * 32);
+  const double2 *be2 = (const double2 *)be;
+  const double2 *uD = (const double2 *)dirichletDev;
+  double2 *v2 = (double2 *)values;
+  double2 *r2 = (double2 *)rhs;
+#define FG_GATHER(SLOT, CPLX, KT)                                                                                 \
+  do {                                                                                                            \
+    auto kern = k_gather<SLOT, CPLX, KT>;                                                                         \
+    FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                  \
+    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be2, uD, v2, r2, wpb);                      \
+  } while (0)
+  if (p.slotBytes == 1) {
+    if (keIsFloat) {
+      if (keComplex) FG_GATHER(uint8_t, true, float); else FG_GATHER(uint8_t, false, float);
+    } else {
+      if (keComplex) FG_GATHER(uint8_t, true, double); else FG_GATHER(uint8_t, false, double);
+    }
+  } else {
+    if (keIsFloat) {
+      if (keComplex) FG_GATHER(uint16_t, true, float); else FG_GATHER(uint16_t, false, float);
+    } else {
+      if (keComplex) FG_GATHER(uint16_t, true, double); else FG_GATHER(uint16_t, false, double);
+    }
+  }
+#undef FG_GATHER
+  countLaunch();
+  FG_CUDA(cudaGetLastError());
+  return FG_OK;
+}
+
+// outputs: device pointers used in place, host pointers staged through the plan
+struct Outputs {
+  double *values = nullptr, *rhs = nullptr;
+  bool hostValues = false, hostRhs = false;
+};
+
+int prepareOutputs(fg_plan *plan, double *csr_values, double *rhs, Outputs *o) {
+  if (!csr_values) {
+    setLastError("csr_values must not be NULL");
+    return FG_ERR_ARG;
+  }
+  o->hostValues = !isDevicePointer(csr_values);
+  o->values = csr_values;
+  if (o->hostValues) {
+    int st = ensureDevice((void **)&plan->values, &plan->valuesBytes, plan->d.nnz * 16);
+    if (st) return st;
+    o->values = plan->values;
+  }
+  o->rhs = rhs;
+  if (rhs) {
+    o->hostRhs = !isDevicePointer(rhs);
+    if (o->hostRhs) {
+      int st = ensureDevice((void **)&plan->rhs, &plan->rhsBytes, plan->d.nRows * 16);
+      if (st) return st;
+      o->rhs = plan->rhs;
+    }
+  }
+  return FG_OK;
+}
+
+int finishOutputs(fg_plan *plan, const Outputs &o, double *csr_values, double *rhs, cudaStream_t s) {
+  if (o.hostValues) FG_CUDA(cudaMemcpyAsync(csr_values, o.values, plan->d.nnz * 16, cudaMemcpyDeviceToHost, s));
+  if (rhs && o.hostRhs) FG_CUDA(cudaMemcpyAsync(rhs, o.rhs, plan->d.nRows * 16, cudaMemcpyDeviceToHost, s));
+  if (o.hostValues || (rhs && o.hostRhs)) FG_CUDA(cudaStreamSynchronize(s));
+  return FG_OK;
+}
+
+}  // namespace femg
+
+using namespace femg;
+
+extern "C" int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency, const double *dirichlet,
+                                double *csr_values, double *rhs, void *stream) {
+  if (!plan) return FG_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  DevTerms dt;
+  int st = resolveTerms(plan, terms, n_terms, frequency, &dt);
+  if (st) return st;
+  const double *uD = nullptr;
+  if ((st = uploadDirichlet(plan, dirichlet, &uD, s))) return st;
+  Outputs o;
+  if ((st = prepareOutputs(plan, csr_values, rhs, &o))) return st;
+  const PlanDev &p = plan->d;
+  const int ncomp = dt.complexKe ? 2 : 1;
+  if ((st = ensureDevice((void **)&plan->ke, &plan->keBytes, (size_t)p.E * ncomp * p.n * p.n * sizeof(double)))) return st;
+  double *be = nullptr;
+  if (dt.hasSource && rhs) {
+    if ((st = ensureDevice((void **)&plan->be, &plan->beBytes, (size_t)p.E * p.n * 16))) return st;
+    be = plan->be;
+  }
+  if (p.E > 0) {
+    if ((st = launchElementFp64(plan, dt, plan->ke, be, s))) return st;
+  }
+  if ((st = launchGather(plan, plan->ke, dt.complexKe, 0, be, uD, o.values, o.rhs, s))) return st;
+  return finishOutputs(plan, o, csr_values, rhs, s);
+}

@@ -1,0 +1,216 @@
+// Shared declarations of the GB300 assembly kernels: the device-resident plan,
+// device term descriptors, error plumbing and small device helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/fem_g_gb300.h"
+
+namespace femg {
+
+void setLastError(const std::string &msg);
+void countLaunch(int n = 1);
+
+#define FG_CUDA(call)                                                                          \
+  do {                                                                                         \
+    cudaError_t _e = (call);                                                                   \
+    if (_e != cudaSuccess) {                                                                   \
+      ::femg::setLastError(std::string(#call) + ": " + cudaGetErrorString(_e));              \
+      return FG_ERR_CUDA;                                                                      \
+    }                                                                                          \
+  } while (0)
+
+constexpr int kMaxDofs = 64;         // element DOFs (basis x multiplicity) handled on device
+constexpr int kMaxNodes = 10;        // geometric nodes per element
+constexpr int kMaxTerms = 6;
+constexpr uint16_t kSlotFixed = 0xFFFF;   // column is a fixed DOF (Dirichlet lifting)
+constexpr uint16_t kSlotIgnore = 0xFFFE;  // column does not assemble (undefined type)
+
+// Device copy of an fg_expr with device array pointers and a precomputed class
+enum ExprClass { kExprConst = 0, kExprElem = 1, kExprPoint = 2 };
+struct DevExpr {
+  int32_t n_code;
+  int32_t cls;
+  double2 cval;  // value when cls == kExprConst
+  fg_instr code[FG_EXPR_MAX_CODE];
+  const double2 *arr[FG_EXPR_MAX_ARRAYS];
+};
+
+struct DevTerm {
+  int32_t kind;
+  int32_t dt;
+  double2 factor;  // module factor: 1, -omega^2 (dt2) or -i omega (dt1)
+  DevExpr coef, coef2;
+};
+
+struct DevTerms {
+  int32_t n;
+  int32_t complexKe;   // element matrices need an imaginary part
+  int32_t hasSource;
+  int32_t hasElastic;
+  DevTerm t[kMaxTerms];
+};
+
+// Device-resident data of one element bucket
+struct PlanDev {
+  int32_t dim, nn, nq, nb, mult, n, nOrient, affine;
+  int64_t E, nNodes;
+  uint64_t nRows, nnz, nFixed;
+  const double *xyz;      // [nNodes][3]
+  const int32_t *enodes;  // [E][nn]
+  const double *w;        // [nq]
+  const double *geoVal;   // [nq][nn]
+  const double *geoGrad;  // [nq][nn][3]
+  const double *bval;     // [nOrient][nq][nb]
+  const double *bgrad;    // [nOrient][nq][nb][3]
+  const int32_t *orient;  // [E] or null
+  const uint32_t *edof;   // [E][n]: row/column index, or fixed index for fixed DOFs
+  const uint8_t *etype;   // [E][n]: FG_AT_*
+  const uint64_t *ai;     // [nRows+1]
+  const uint64_t *rowPtr; // [nRows+1] into rowElem
+  const uint32_t *rowElem;// (e << 6) | i : element and local test index
+  const void *slot;       // [E][n][n] uint8 or uint16 position in the row
+  int32_t slotBytes;
+  int32_t maxRowLen;
+};
+
+}  // namespace femg
+
+struct fg_plan {
+  femg::PlanDev d;
+  // host copies needed by later calls
+  std::vector<uint64_t> hAi;
+  int64_t E = 0;
+  // owned device allocations
+  std::vector<void *> allocs;
+  // scratch (grown on demand)
+  double *ke = nullptr;
+  size_t keBytes = 0;
+  double *be = nullptr;
+  size_t beBytes = 0;
+  double *dirichlet = nullptr;
+  size_t dirichletBytes = 0;
+  double *values = nullptr;  // device CSR values when the caller passes host memory
+  size_t valuesBytes = 0;
+  double *rhs = nullptr;
+  size_t rhsBytes = 0;
+  std::vector<void *> termArrays;   // device copies of per-element coefficient arrays (per call)
+  std::vector<void *> boundArrays;  // ... of the terms bound by fg_plan_bind_terms
+  femg::DevTerms bound;
+  bool hasBound = false;
+  // mixed-precision state (reference tensors per orientation), see assemble_mixed.cu
+  void *mixed = nullptr;
+};
+
+namespace femg {
+
+// grow-only device scratch
+int ensureDevice(void **ptr, size_t *cap, size_t bytes);
+// upload a term list (copies per-element arrays)
+int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double frequency, DevTerms *out,
+                std::vector<void *> &arrays);
+// terms of a call: uploaded now, or the bound ones when terms == NULL
+int resolveTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double frequency, DevTerms *out);
+// copy the Dirichlet values; return device pointer (or null)
+int uploadDirichlet(fg_plan *plan, const double *dirichlet, const double **out, cudaStream_t s);
+bool isDevicePointer(const void *p);
+// FP64 gather of element matrices/vectors into CSR values and RHS
+int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, const double *be,
+                 const double *dirichletDev, double *values, double *rhs, cudaStream_t s);
+// FP64 element kernel (also used as the reference for the mixed error report)
+int launchElementFp64(fg_plan *plan, const DevTerms &terms, double *ke, double *be, cudaStream_t s);
+
+// ------------------------------------------------------------- device helpers
+
+__host__ __device__ inline double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ inline double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
+__device__ inline double2 cdiv(double2 a, double2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+// Evaluate a coefficient expression at element e and physical point x
+__device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x) {
+  if (ex.cls == kExprConst) return ex.cval;
+  double2 st[16];
+  int sp = 0;
+  for (int k = 0; k < ex.n_code; ++k) {
+    const fg_instr in = ex.code[k];
+    switch (in.op) {
+      case FG_OP_CONST: st[sp++] = make_double2(in.re, in.im); break;
+      case FG_OP_X: st[sp++] = make_double2(x[0], 0.0); break;
+      case FG_OP_Y: st[sp++] = make_double2(x[1], 0.0); break;
+      case FG_OP_Z: st[sp++] = make_double2(x[2], 0.0); break;
+      case FG_OP_ELEM: st[sp++] = ex.arr[in.arg][e]; break;
+      case FG_OP_NEG: st[sp - 1] = make_double2(-st[sp - 1].x, -st[sp - 1].y); break;
+      case FG_OP_HEAVISIDE: {
+        const double r = st[sp - 1].x;
+        st[sp - 1] = make_double2(r > 0.0 ? 1.0 : (r < 0.0 ? 0.0 : 0.5), 0.0);
+        break;
+      }
+      default: {
+        const double2 b = st[--sp];
+        const double2 a = st[sp - 1];
+        double2 r;
+        if (in.op == FG_OP_ADD) r = cadd(a, b);
+        else if (in.op == FG_OP_SUB) r = make_double2(a.x - b.x, a.y - b.y);
+        else if (in.op == FG_OP_MUL) r = cmul(a, b);
+        else r = cdiv(a, b);
+        st[sp - 1] = r;
+      }
+    }
+  }
+  return st[0];
+}
+
+// Jacobian at a quadrature point from the geometric nodes, stored column-major
+// like gmsh's getJacobians (J[3*c + r] = d x_r / d u_c); 2D elements get the
+// unit normal as third column. Returns det J.
+__device__ inline double jacobian(int dim, int nn, const double *X /*[nn][3]*/, const double *dN /*[nn][3]*/, double *J) {
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) J[3 * c + r] = 0.0;
+  const int nc = dim;
+  for (int k = 0; k < nn; ++k)
+    for (int c = 0; c < nc; ++c) {
+      const double g = dN[3 * k + c];
+      J[3 * c + 0] += X[3 * k + 0] * g;
+      J[3 * c + 1] += X[3 * k + 1] * g;
+      J[3 * c + 2] += X[3 * k + 2] * g;
+    }
+  if (dim == 2) {
+    const double nx = J[1] * J[5] - J[2] * J[4];
+    const double ny = J[2] * J[3] - J[0] * J[5];
+    const double nz = J[0] * J[4] - J[1] * J[3];
+    const double len = sqrt(nx * nx + ny * ny + nz * nz);
+    J[6] = nx / len;
+    J[7] = ny / len;
+    J[8] = nz / len;
+  }
+  // det of the column-major matrix
+  return J[0] * (J[4] * J[8] - J[7] * J[5]) - J[3] * (J[1] * J[8] - J[7] * J[2]) + J[6] * (J[1] * J[5] - J[4] * J[2]);
+}
+
+// inverse-transpose application data: Kinv[a][r] = (J^-1)[a][r], so that the
+// physical gradient is G_r = sum_a Kinv[a][r] * dphi/du_a  (J^-T grad)
+__device__ inline void jacobianInverse(const double *J, double det, double *Jinv /*row-major [a][r]*/) {
+  // J(r,c) = J[3c + r]
+  auto Jm = [&](int r, int c) { return J[3 * c + r]; };
+  const double id = 1.0 / det;
+  Jinv[0] = (Jm(1, 1) * Jm(2, 2) - Jm(1, 2) * Jm(2, 1)) * id;
+  Jinv[1] = (Jm(0, 2) * Jm(2, 1) - Jm(0, 1) * Jm(2, 2)) * id;
+  Jinv[2] = (Jm(0, 1) * Jm(1, 2) - Jm(0, 2) * Jm(1, 1)) * id;
+  Jinv[3] = (Jm(1, 2) * Jm(2, 0) - Jm(1, 0) * Jm(2, 2)) * id;
+  Jinv[4] = (Jm(0, 0) * Jm(2, 2) - Jm(0, 2) * Jm(2, 0)) * id;
+  Jinv[5] = (Jm(0, 2) * Jm(1, 0) - Jm(0, 0) * Jm(1, 2)) * id;
+  Jinv[6] = (Jm(1, 0) * Jm(2, 1) - Jm(1, 1) * Jm(2, 0)) * id;
+  Jinv[7] = (Jm(0, 1) * Jm(2, 0) - Jm(0, 0) * Jm(2, 1)) * id;
+  Jinv[8] = (Jm(0, 0) * Jm(1, 1) - Jm(0, 1) * Jm(1, 0)) * id;
+}
+
+}  // namespace femg

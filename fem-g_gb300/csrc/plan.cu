@@ -1,0 +1,527 @@
+// Plan creation: validation of the reference-side descriptors, upload of the
+// element bucket and construction of the element -> nonzero map used by the
+// deterministic CSR reduction.
+//
+// The map replaces the per-entry std::lower_bound of MatrixFactory::addValues
+// (src/system/MatrixFactory.cpp:267) and the index bucket of
+// FieldInterface::fillIndices (src/field/FieldInterface.cpp:1012-1076): for
+// every element e, local test DOF i and local unknown DOF j it stores the
+// position of column J inside the CSR row I, so the device never searches.
+// Each row also gets the list of (element, local index) pairs that touch it,
+// in element order; summing along that list is the fixed reduction order.
+#include <omp.h>
+
+#include <algorithm>
+#include <atomic>
+#include <complex>
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace femg {
+
+static thread_local std::string g_lastError;
+static std::atomic<int64_t> g_launches{0};
+
+void setLastError(const std::string &msg) { g_lastError = msg; }
+void countLaunch(int n) { g_launches += n; }
+
+int ensureDevice(void **ptr, size_t *cap, size_t bytes) {
+  if (bytes <= *cap && *ptr) return FG_OK;
+  if (*ptr) cudaFree(*ptr);
+  *ptr = nullptr;
+  *cap = 0;
+  if (bytes == 0) return FG_OK;
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    setLastError(std::string("device allocation of ") + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+    return FG_ERR_OOM;
+  }
+  *cap = bytes;
+  return FG_OK;
+}
+
+bool isDevicePointer(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+template <typename T>
+static int upload(fg_plan *plan, const T *host, size_t count, const T **dev) {
+  *dev = nullptr;
+  if (count == 0) return FG_OK;
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    setLastError(std::string("plan upload: ") + cudaGetErrorString(e));
+    return FG_ERR_OOM;
+  }
+  plan->allocs.push_back(p);
+  e = cudaMemcpy(p, host, count * sizeof(T), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    setLastError(std::string("plan upload copy: ") + cudaGetErrorString(e));
+    return FG_ERR_CUDA;
+  }
+  *dev = (const T *)p;
+  return FG_OK;
+}
+
+static bool isRow(int t) { return t == FG_AT_UNKNOWN || t == FG_AT_UNKNOWN_BUBBLE || t == FG_AT_UNKNOWN_GLOBAL; }
+
+static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_space_desc *space, const fg_system_desc *sys,
+                      fg_plan *plan) {
+  PlanDev &d = plan->d;
+  if (mesh->dim != 2 && mesh->dim != 3) {
+    setLastError("fg_plan_create: element dimension must be 2 or 3");
+    return FG_ERR_ARG;
+  }
+  if (mesh->nodes_per_element < mesh->dim + 1 || mesh->nodes_per_element > kMaxNodes) {
+    setLastError("fg_plan_create: unsupported nodes_per_element");
+    return FG_ERR_ARG;
+  }
+  const int n = space->n_basis * space->multiplicity;
+  if (space->n_basis <= 0 || space->multiplicity <= 0 || n > kMaxDofs) {
+    setLastError("fg_plan_create: element DOFs must be in [1, 64]");
+    return FG_ERR_UNSUPPORTED;
+  }
+  if (mesh->n_elements < 0 || mesh->n_elements >= (int64_t(1) << 26) || mesh->n_nodes >= (int64_t(1) << 31)) {
+    setLastError("fg_plan_create: element or node count out of range");
+    return FG_ERR_ARG;
+  }
+  if (rule->nq <= 0 || space->n_orientations <= 0) {
+    setLastError("fg_plan_create: empty rule or orientation table");
+    return FG_ERR_ARG;
+  }
+  const int64_t E = mesh->n_elements;
+  const int nn = mesh->nodes_per_element;
+  d.dim = mesh->dim;
+  d.nn = nn;
+  d.nq = rule->nq;
+  d.nb = space->n_basis;
+  d.mult = space->multiplicity;
+  d.n = n;
+  d.nOrient = space->n_orientations;
+  d.affine = (nn == mesh->dim + 1) ? 1 : 0;
+  d.E = E;
+  d.nNodes = mesh->n_nodes;
+  d.nRows = sys->n_rows;
+  d.nnz = sys->ai[sys->n_rows];
+  d.nFixed = sys->n_fixed;
+  plan->E = E;
+  plan->hAi.assign(sys->ai, sys->ai + sys->n_rows + 1);
+
+  // element nodes as int32, orientations checked
+  std::vector<int32_t> en((size_t)E * nn);
+  int bad = 0;
+#pragma omp parallel for reduction(+ : bad)
+  for (int64_t i = 0; i < E * nn; ++i) {
+    const int64_t v = mesh->elem_nodes[i];
+    if (v < 0 || v >= mesh->n_nodes) ++bad;
+    en[(size_t)i] = (int32_t)v;
+  }
+  if (bad) {
+    setLastError("fg_plan_create: element node index out of range");
+    return FG_ERR_INDEX;
+  }
+  if (space->n_orientations > 1) {
+    if (!space->elem_orientation) {
+      setLastError("fg_plan_create: elem_orientation required with several orientations");
+      return FG_ERR_ARG;
+    }
+    for (int64_t e = 0; e < E; ++e)
+      if (space->elem_orientation[e] < 0 || space->elem_orientation[e] >= space->n_orientations) {
+        setLastError("fg_plan_create: orientation index out of range");
+        return FG_ERR_INDEX;
+      }
+  }
+
+  // element DOF map: row/column index (or fixed index) and type
+  std::vector<uint32_t> edof((size_t)E * n);
+  std::vector<uint8_t> etype((size_t)E * n);
+#pragma omp parallel for reduction(+ : bad)
+  for (int64_t i = 0; i < E * n; ++i) {
+    const int t = sys->elem_dof_type[i];
+    const uint64_t v = sys->elem_dof_idx[i];
+    etype[(size_t)i] = (uint8_t)t;
+    edof[(size_t)i] = (uint32_t)v;
+    if (t == FG_AT_LINKED || t == FG_AT_LINKED_BUBBLE || t < 0 || t > FG_AT_LINKED_BUBBLE) ++bad;
+    else if (isRow(t) && v >= sys->n_rows) ++bad;
+    else if (t == FG_AT_FIXED && v >= sys->n_fixed) ++bad;
+  }
+  if (bad) {
+    setLastError("fg_plan_create: element DOF index/type out of range (linked DOFs are not supported)");
+    return FG_ERR_INDEX;
+  }
+
+  // row -> (element, local test index) lists, element order
+  std::vector<uint64_t> rowPtr(sys->n_rows + 1, 0);
+  for (int64_t i = 0; i < E * n; ++i)
+    if (isRow(etype[(size_t)i])) rowPtr[edof[(size_t)i] + 1]++;
+  for (uint64_t r = 0; r < sys->n_rows; ++r) rowPtr[r + 1] += rowPtr[r];
+  std::vector<uint32_t> rowElem(rowPtr[sys->n_rows]);
+  {
+    std::vector<uint64_t> fill(rowPtr.begin(), rowPtr.end() - 1);
+    for (int64_t e = 0; e < E; ++e)
+      for (int i = 0; i < n; ++i) {
+        const size_t k = (size_t)e * n + i;
+        if (isRow(etype[k])) rowElem[fill[edof[k]]++] = (uint32_t)((e << 6) | i);
+      }
+  }
+
+  // slots: position of each column inside its row
+  uint64_t maxLen = 0;
+  for (uint64_t r = 0; r < sys->n_rows; ++r) maxLen = std::max(maxLen, sys->ai[r + 1] - sys->ai[r]);
+  if (maxLen >= 0xFFFE) {
+    setLastError("fg_plan_create: CSR row longer than 65533 entries");
+    return FG_ERR_UNSUPPORTED;
+  }
+  d.maxRowLen = (int32_t)maxLen;
+  const bool narrow = maxLen < 0xFE;
+  d.slotBytes = narrow ? 1 : 2;
+  const size_t nSlots = (size_t)E * n * n;
+  std::vector<uint8_t> slot8;
+  std::vector<uint16_t> slot16;
+  if (narrow) slot8.assign(nSlots, 0xFF); else slot16.assign(nSlots, kSlotIgnore);
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : bad)
+  for (int64_t e = 0; e < E; ++e) {
+    for (int i = 0; i < n; ++i) {
+      const size_t ki = (size_t)e * n + i;
+      if (!isRow(etype[ki])) continue;
+      const uint64_t I = edof[ki];
+      const uint64_t *b = sys->aj + sys->ai[I];
+      const uint64_t *en2 = sys->aj + sys->ai[I + 1];
+      for (int j = 0; j < n; ++j) {
+        const size_t kj = (size_t)e * n + j;
+        const int t = etype[kj];
+        uint16_t s;
+        if (t == FG_AT_FIXED) s = kSlotFixed;
+        else if (!isRow(t)) s = kSlotIgnore;
+        else {
+          const uint64_t J = edof[kj];
+          const uint64_t *p = std::lower_bound(b, en2, J);
+          if (p == en2 || *p != J) {
+            ++bad;
+            s = kSlotIgnore;
+          } else {
+            s = (uint16_t)(p - b);
+          }
+        }
+        const size_t ks = ki * n + j;
+        if (narrow) slot8[ks] = s == kSlotFixed ? 0xFF : (s == kSlotIgnore ? 0xFE : (uint8_t)s);
+        else slot16[ks] = s;
+      }
+    }
+  }
+  if (bad) {
+    setLastError("fg_plan_create: an element DOF pair is missing from the CSR pattern");
+    return FG_ERR_INDEX;
+  }
+
+  int st;
+  if ((st = upload(plan, mesh->node_xyz, (size_t)mesh->n_nodes * 3, &d.xyz))) return st;
+  if ((st = upload(plan, en.data(), en.size(), &d.enodes))) return st;
+  if ((st = upload(plan, rule->weights, (size_t)rule->nq, &d.w))) return st;
+  if ((st = upload(plan, rule->geo_val, (size_t)rule->nq * nn, &d.geoVal))) return st;
+  if ((st = upload(plan, rule->geo_grad, (size_t)rule->nq * nn * 3, &d.geoGrad))) return st;
+  if ((st = upload(plan, space->basis_val, (size_t)space->n_orientations * rule->nq * space->n_basis, &d.bval))) return st;
+  if ((st = upload(plan, space->basis_grad, (size_t)space->n_orientations * rule->nq * space->n_basis * 3, &d.bgrad))) return st;
+  d.orient = nullptr;
+  if (space->n_orientations > 1)
+    if ((st = upload(plan, space->elem_orientation, (size_t)E, &d.orient))) return st;
+  if ((st = upload(plan, edof.data(), edof.size(), &d.edof))) return st;
+  if ((st = upload(plan, etype.data(), etype.size(), &d.etype))) return st;
+  if ((st = upload(plan, sys->ai, (size_t)sys->n_rows + 1, &d.ai))) return st;
+  if ((st = upload(plan, rowPtr.data(), rowPtr.size(), &d.rowPtr))) return st;
+  if ((st = upload(plan, rowElem.data(), rowElem.size(), &d.rowElem))) return st;
+  if (narrow) {
+    const uint8_t *p;
+    if ((st = upload(plan, slot8.data(), slot8.size(), &p))) return st;
+    d.slot = p;
+  } else {
+    const uint16_t *p;
+    if ((st = upload(plan, slot16.data(), slot16.size(), &p))) return st;
+    d.slot = p;
+  }
+  return FG_OK;
+}
+
+int uploadDirichlet(fg_plan *plan, const double *dirichlet, const double **out, cudaStream_t s) {
+  *out = nullptr;
+  if (plan->d.nFixed == 0) return FG_OK;
+  if (!dirichlet) {
+    setLastError("Dirichlet values required: the system has fixed DOFs");
+    return FG_ERR_ARG;
+  }
+  if (isDevicePointer(dirichlet)) {
+    *out = dirichlet;
+    return FG_OK;
+  }
+  int st = ensureDevice((void **)&plan->dirichlet, &plan->dirichletBytes, plan->d.nFixed * 16);
+  if (st) return st;
+  FG_CUDA(cudaMemcpyAsync(plan->dirichlet, dirichlet, plan->d.nFixed * 16, cudaMemcpyHostToDevice, s));
+  *out = plan->dirichlet;
+  return FG_OK;
+}
+
+static int classify(const fg_expr &ex) {
+  int cls = kExprConst;
+  for (int k = 0; k < ex.n_code; ++k) {
+    if (ex.code[k].op == FG_OP_X || ex.code[k].op == FG_OP_Y || ex.code[k].op == FG_OP_Z) return kExprPoint;
+    if (ex.code[k].op == FG_OP_ELEM) cls = kExprElem;
+  }
+  return cls;
+}
+
+static std::complex<double> evalConst(const fg_expr &ex) {
+  std::vector<std::complex<double>> st;
+  for (int k = 0; k < ex.n_code; ++k) {
+    const fg_instr &in = ex.code[k];
+    if (in.op == FG_OP_CONST) st.push_back({in.re, in.im});
+    else if (in.op == FG_OP_NEG) st.back() = -st.back();
+    else if (in.op == FG_OP_HEAVISIDE) {
+      const double r = st.back().real();
+      st.back() = r > 0 ? 1.0 : (r < 0 ? 0.0 : 0.5);
+    } else {
+      auto b = st.back();
+      st.pop_back();
+      auto &a = st.back();
+      if (in.op == FG_OP_ADD) a += b;
+      else if (in.op == FG_OP_SUB) a -= b;
+      else if (in.op == FG_OP_MUL) a *= b;
+      else a /= b;
+    }
+  }
+  return st.empty() ? 0.0 : st.back();
+}
+
+static int validateExpr(const fg_expr &ex) {
+  if (ex.n_code <= 0 || ex.n_code > FG_EXPR_MAX_CODE || ex.n_arrays < 0 || ex.n_arrays > FG_EXPR_MAX_ARRAYS) return 1;
+  int depth = 0;
+  for (int k = 0; k < ex.n_code; ++k) {
+    const int op = ex.code[k].op;
+    if (op <= FG_OP_ELEM) {
+      if (op == FG_OP_ELEM && (ex.code[k].arg < 0 || ex.code[k].arg >= ex.n_arrays || !ex.elem_values[ex.code[k].arg])) return 1;
+      if (++depth > 16) return 1;
+    } else if (op == FG_OP_NEG || op == FG_OP_HEAVISIDE) {
+      if (depth < 1) return 1;
+    } else if (op <= FG_OP_DIV) {
+      if (depth < 2) return 1;
+      --depth;
+    } else {
+      return 1;
+    }
+  }
+  return depth == 1 ? 0 : 1;
+}
+
+static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complexOut, std::vector<void *> &arrays) {
+  if (validateExpr(ex)) {
+    setLastError("invalid coefficient expression");
+    return FG_ERR_ARG;
+  }
+  std::memset(out, 0, sizeof(*out));
+  out->n_code = ex.n_code;
+  for (int k = 0; k < ex.n_code; ++k) {
+    out->code[k] = ex.code[k];
+    if (ex.code[k].op == FG_OP_CONST && ex.code[k].im != 0.0) *complexOut = true;
+  }
+  out->cls = classify(ex);
+  if (out->cls == kExprConst) {
+    auto v = evalConst(ex);
+    out->cval = make_double2(v.real(), v.imag());
+    if (v.imag() != 0.0) *complexOut = true;
+  }
+  for (int a = 0; a < ex.n_arrays; ++a) {
+    const size_t bytes = (size_t)plan->E * 16;
+    if (isDevicePointer(ex.elem_values[a])) {
+      out->arr[a] = (const double2 *)ex.elem_values[a];
+      *complexOut = true;  // cannot scan device data cheaply: assume complex
+      continue;
+    }
+    for (int64_t e = 0; e < plan->E; ++e)
+      if (ex.elem_values[a][2 * e + 1] != 0.0) {
+        *complexOut = true;
+        break;
+      }
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      setLastError("coefficient upload: out of device memory");
+      return FG_ERR_OOM;
+    }
+    arrays.push_back(p);
+    if (cudaMemcpy(p, ex.elem_values[a], bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+      setLastError("coefficient upload failed");
+      return FG_ERR_CUDA;
+    }
+    out->arr[a] = (const double2 *)p;
+  }
+  return FG_OK;
+}
+
+int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double frequency, DevTerms *out,
+                std::vector<void *> &arrays) {
+  for (void *p : arrays) cudaFree(p);
+  arrays.clear();
+  std::memset(out, 0, sizeof(*out));
+  if (nTerms <= 0 || nTerms > kMaxTerms || !terms) {
+    setLastError("term count must be in [1, 6]");
+    return FG_ERR_ARG;
+  }
+  bool anyDt = false;
+  for (int t = 0; t < nTerms; ++t) anyDt = anyDt || terms[t].dt != FG_DT_NONE;
+  bool cplx = false;
+  out->n = nTerms;
+  for (int t = 0; t < nTerms; ++t) {
+    const fg_term_desc &src = terms[t];
+    DevTerm &dt = out->t[t];
+    dt.kind = src.kind;
+    dt.dt = src.dt;
+    if (src.kind < FG_TERM_GRAD_GRAD || src.kind > FG_TERM_SOURCE) {
+      setLastError("unknown term kind");
+      return FG_ERR_ARG;
+    }
+    if (src.kind == FG_TERM_ELASTIC && plan->d.mult != 3) {
+      setLastError("the elastic (Tensor4) term needs a 3-component compound field");
+      return FG_ERR_UNSUPPORTED;
+    }
+    if (src.kind != FG_TERM_ELASTIC && plan->d.mult != 1 && src.kind != FG_TERM_MASS) {
+      setLastError("compound fields support the elastic and mass terms only");
+      return FG_ERR_UNSUPPORTED;
+    }
+    // AFrequency module factor (src/term/Assembler.cpp:283-295)
+    if (src.dt == FG_DT_2) dt.factor = make_double2(-frequency * frequency, 0.0);
+    else if (src.dt == FG_DT_1) {
+      dt.factor = make_double2(0.0, -frequency);
+      cplx = true;
+    } else dt.factor = make_double2(1.0, 0.0);
+    if (src.dt != FG_DT_NONE && src.kind == FG_TERM_SOURCE) {
+      setLastError("a linear term cannot carry a time derivative");
+      return FG_ERR_ARG;
+    }
+    bool sourceComplex = false;  // the right-hand side is always complex
+    int st = devExpr(plan, src.coef, &dt.coef, src.kind == FG_TERM_SOURCE ? &sourceComplex : &cplx, arrays);
+    if (st) return st;
+    if (src.kind == FG_TERM_ELASTIC) {
+      st = devExpr(plan, src.coef2, &dt.coef2, &cplx, arrays);
+      if (st) return st;
+      out->hasElastic = 1;
+    }
+    if (src.kind == FG_TERM_SOURCE) out->hasSource = 1;
+  }
+  (void)anyDt;
+  out->complexKe = cplx ? 1 : 0;
+  return FG_OK;
+}
+
+int resolveTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double frequency, DevTerms *out) {
+  if (!terms) {
+    if (!plan->hasBound) {
+      setLastError("no terms given and none bound to the plan");
+      return FG_ERR_ARG;
+    }
+    *out = plan->bound;
+    return FG_OK;
+  }
+  return uploadTerms(plan, terms, nTerms, frequency, out, plan->termArrays);
+}
+
+}  // namespace femg
+
+using namespace femg;
+
+extern "C" {
+
+int fg_plan_create(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_space_desc *space, const fg_system_desc *sys,
+                   fg_plan **out) {
+  if (!out) return FG_ERR_ARG;
+  *out = nullptr;
+  if (!mesh || !rule || !space || !sys || !mesh->node_xyz || !mesh->elem_nodes || !rule->weights || !rule->geo_val ||
+      !rule->geo_grad || !space->basis_val || !space->basis_grad || !sys->ai || !sys->aj || !sys->elem_dof_idx ||
+      !sys->elem_dof_type) {
+    setLastError("fg_plan_create: null descriptor field");
+    return FG_ERR_ARG;
+  }
+  int dev = 0;
+  if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) {
+    cudaGetLastError();
+    setLastError("fg_plan_create: no CUDA device");
+    return FG_ERR_NO_DEVICE;
+  }
+  fg_plan *plan = new (std::nothrow) fg_plan;
+  if (!plan) return FG_ERR_OOM;
+  int st;
+  try {
+    st = createPlan(mesh, rule, space, sys, plan);
+  } catch (const std::bad_alloc &) {
+    setLastError("fg_plan_create: host out of memory");
+    st = FG_ERR_OOM;
+  }
+  if (st != FG_OK) {
+    fg_plan_destroy(plan);
+    return st;
+  }
+  *out = plan;
+  return FG_OK;
+}
+
+void mixedDestroy(fg_plan *plan);
+
+void fg_plan_destroy(fg_plan *plan) {
+  if (!plan) return;
+  for (void *p : plan->allocs) cudaFree(p);
+  for (void *p : plan->termArrays) cudaFree(p);
+  for (void *p : plan->boundArrays) cudaFree(p);
+  if (plan->ke) cudaFree(plan->ke);
+  if (plan->be) cudaFree(plan->be);
+  if (plan->dirichlet) cudaFree(plan->dirichlet);
+  if (plan->values) cudaFree(plan->values);
+  if (plan->rhs) cudaFree(plan->rhs);
+  mixedDestroy(plan);
+  delete plan;
+}
+
+int fg_plan_info(const fg_plan *plan, int64_t *nnz, int64_t *n_elements, int32_t *n_dofs, int32_t *nq, int32_t *n_orient) {
+  if (!plan) return FG_ERR_ARG;
+  if (nnz) *nnz = (int64_t)plan->d.nnz;
+  if (n_elements) *n_elements = plan->d.E;
+  if (n_dofs) *n_dofs = plan->d.n;
+  if (nq) *nq = plan->d.nq;
+  if (n_orient) *n_orient = plan->d.nOrient;
+  return FG_OK;
+}
+
+int fg_plan_bind_terms(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency) {
+  if (!plan) return FG_ERR_ARG;
+  plan->hasBound = false;
+  int st = uploadTerms(plan, terms, n_terms, frequency, &plan->bound, plan->boundArrays);
+  if (st == FG_OK) plan->hasBound = true;
+  return st;
+}
+
+const char *fg_last_error(void) { return g_lastError.c_str(); }
+
+int64_t fg_launch_count(void) { return g_launches.load(); }
+
+int fg_host_alloc(void **ptr, size_t bytes) {
+  if (!ptr) return FG_ERR_ARG;
+  cudaError_t e = cudaMallocHost(ptr, bytes);
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    setLastError(std::string("fg_host_alloc: ") + cudaGetErrorString(e));
+    return FG_ERR_OOM;
+  }
+  return FG_OK;
+}
+
+void fg_host_free(void *ptr) {
+  if (ptr) cudaFreeHost(ptr);
+}
+
+}  // extern "C"

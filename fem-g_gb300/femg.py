@@ -1,0 +1,338 @@
+"""Python access to libfemg.so through its C ABI (ctypes only).
+
+The library is the product: CUDA kernels for sm_103a plus the host-side
+mirror of GmshFEM's Formulation interface. This module only binds the C
+entry points declared in include/fem_g_gb300.h and include/fem_g_gb300_host.h
+and converts arrays; it computes nothing itself. Loading fails loudly when
+the library is missing or was not built.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfemg.so")
+
+FG_OK, FG_ERR_ARG, FG_ERR_OOM, FG_ERR_CUDA, FG_ERR_INDEX, FG_ERR_TIMEOUT, FG_ERR_UNSUPPORTED, FG_ERR_NO_DEVICE = range(8)
+FG_TERM_GRAD_GRAD, FG_TERM_MASS, FG_TERM_ELASTIC, FG_TERM_SOURCE = range(4)
+FG_PROBLEM_HELMHOLTZ, FG_PROBLEM_NAVIER = range(2)
+FG_SPACE_LAGRANGE, FG_SPACE_HIERARCHICAL_H1 = range(2)
+FG_EXPR_MAX_CODE = 32
+FG_EXPR_MAX_ARRAYS = 4
+
+
+class FgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("status %d: %s" % (status, msg))
+        self.status = status
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("nodes_per_element", C.c_int32), ("n_nodes", C.c_int64),
+                ("node_xyz", C.POINTER(C.c_double)), ("n_elements", C.c_int64), ("elem_nodes", C.POINTER(C.c_int64))]
+
+
+class RuleDesc(C.Structure):
+    _fields_ = [("nq", C.c_int32), ("weights", C.POINTER(C.c_double)), ("geo_val", C.POINTER(C.c_double)),
+                ("geo_grad", C.POINTER(C.c_double))]
+
+
+class SpaceDesc(C.Structure):
+    _fields_ = [("n_basis", C.c_int32), ("multiplicity", C.c_int32), ("n_orientations", C.c_int32),
+                ("basis_val", C.POINTER(C.c_double)), ("basis_grad", C.POINTER(C.c_double)),
+                ("elem_orientation", C.POINTER(C.c_int32))]
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [("n_rows", C.c_uint64), ("ai", C.POINTER(C.c_uint64)), ("aj", C.POINTER(C.c_uint64)),
+                ("elem_dof_idx", C.POINTER(C.c_uint64)), ("elem_dof_type", C.POINTER(C.c_int32)), ("n_fixed", C.c_uint64)]
+
+
+class Instr(C.Structure):
+    _fields_ = [("op", C.c_int32), ("arg", C.c_int32), ("re", C.c_double), ("im", C.c_double)]
+
+
+class Expr(C.Structure):
+    _fields_ = [("n_code", C.c_int32), ("code", Instr * FG_EXPR_MAX_CODE), ("n_arrays", C.c_int32),
+                ("elem_values", C.POINTER(C.c_double) * FG_EXPR_MAX_ARRAYS)]
+
+
+class TermDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("dt", C.c_int32), ("coef", Expr), ("coef2", Expr)]
+
+
+class ErrReport(C.Structure):
+    _fields_ = [("max_elem_rel_fro", C.c_double), ("mean_elem_rel_fro", C.c_double), ("global_rel_fro", C.c_double)]
+
+
+class ProblemConfig(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("dim", C.c_int32), ("m", C.c_int32), ("mesh_order", C.c_int32),
+                ("space", C.c_int32), ("order", C.c_int32), ("gauss", C.c_int32), ("jitter", C.c_double),
+                ("seed", C.c_uint64), ("k", C.c_double), ("coef_mode", C.c_int32), ("dirichlet", C.c_int32),
+                ("dirichlet_value", C.c_double), ("source", C.c_int32), ("omega", C.c_double),
+                ("lame_sigma", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libfemg.so (build it first with build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libfemg.so is not built: run __graft_entry__.build()")
+    L = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    sig = {
+        "fg_plan_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(RuleDesc), C.POINTER(SpaceDesc), C.POINTER(SystemDesc), C.POINTER(P)]),
+        "fg_plan_destroy": (None, [P]),
+        "fg_plan_info": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+        "fg_plan_bind_terms": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_double]),
+        "fg_assemble_fp64": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_double, P, P, P, P]),
+        "fg_assemble_mixed": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_double, P, P, P, P, C.POINTER(ErrReport)]),
+        "fg_assemble_multi_freq": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, P, C.c_int32, C.c_int32, P, P]),
+        "fg_batch_create": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.POINTER(P)]),
+        "fg_batch_run": (C.c_int, [P, P, P, P]),
+        "fg_batch_destroy": (None, [P]),
+        "fg_last_error": (C.c_char_p, []),
+        "fg_launch_count": (C.c_int64, []),
+        "fg_host_alloc": (C.c_int, [C.POINTER(P), C.c_size_t]),
+        "fg_host_free": (None, [P]),
+        "fg_problem_create": (C.c_int, [C.POINTER(ProblemConfig), C.POINTER(P)]),
+        "fg_problem_destroy": (None, [P]),
+        "fg_problem_descs": (C.c_int, [P, C.POINTER(MeshDesc), C.POINTER(RuleDesc), C.POINTER(SpaceDesc), C.POINTER(SystemDesc),
+                                       C.POINTER(C.POINTER(TermDesc)), C.POINTER(C.c_int32), C.POINTER(C.POINTER(C.c_double))]),
+        "fg_problem_n_dofs": (C.c_int64, [P]),
+        "fg_problem_raw_dofs": (C.c_int, [P, P, P, P, P, P]),
+        "fg_problem_created_dofs": (C.c_int, [P, P, P, P, P]),
+        "fg_problem_bbox": (C.c_int, [P, P]),
+        "fg_problem_reserve_log": (C.c_int64, [P, P, P, C.c_int64]),
+        "fg_problem_pre_seconds": (C.c_double, [P]),
+        "fg_problem_assemble": (C.c_int, [P, C.c_int32, P, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def exported_symbols():
+    """Names bound above (the C ABI of both headers)."""
+    return [
+        "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_assemble_fp64", "fg_assemble_mixed",
+        "fg_assemble_multi_freq", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_last_error", "fg_launch_count",
+        "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
+        "fg_problem_raw_dofs", "fg_problem_created_dofs", "fg_problem_reserve_log", "fg_problem_bbox", "fg_problem_pre_seconds", "fg_problem_assemble",
+    ]
+
+
+def check(status):
+    if status != FG_OK:
+        raise FgError(status, lib().fg_last_error().decode())
+
+
+def _arr(ptr, count, dtype):
+    if count == 0:
+        return np.zeros(0, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(count,)).astype(dtype, copy=True)
+
+
+def config(kind=FG_PROBLEM_HELMHOLTZ, dim=2, m=4, mesh_order=2, space=FG_SPACE_LAGRANGE, order=1, gauss=4, jitter=0.2,
+           seed=1, k=10.0, coef_mode=0, dirichlet=0, dirichlet_value=0.0, source=0, omega=1.0, lame_sigma=0.5):
+    return ProblemConfig(kind, dim, m, mesh_order, space, order, gauss, jitter, seed, k, coef_mode, dirichlet,
+                         dirichlet_value, source, omega, lame_sigma)
+
+
+# The benchmark workloads (seeded synthetic inputs with the shapes of the
+# reference's configurations)
+def config_c1(m=64, seed=1):
+    """2D Helmholtz, P2 triangles, Gauss4, k=10, Dirichlet u=0, disk source."""
+    return config(dim=2, m=m, mesh_order=2, space=FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=seed, k=10.0,
+                  dirichlet=1, source=1)
+
+
+def config_c2(m=40, seed=2, order=3):
+    """3D Helmholtz, Kuhn tets, hierarchical H1 order 3, Gauss6, k=20."""
+    return config(dim=3, m=m, mesh_order=1, space=FG_SPACE_HIERARCHICAL_H1, order=order, gauss=6, jitter=0.15, seed=seed,
+                  k=20.0)
+
+
+def config_c3(m=40, seed=2, order=3):
+    """c2 mesh with per-tet coefficient -k^2 (1 + 0.3 xi), xi ~ N(0,1)."""
+    c = config_c2(m=m, seed=seed, order=order)
+    c.coef_mode = 1
+    return c
+
+
+def config_c5(m=60, seed=5, omega=5.0):
+    """3D Navier, 3-component hierarchical H1 order 2, Gauss4, lognormal Lame."""
+    return config(kind=FG_PROBLEM_NAVIER, dim=3, m=m, mesh_order=1, space=FG_SPACE_HIERARCHICAL_H1, order=2, gauss=4,
+                  jitter=0.15, seed=seed, omega=omega, lame_sigma=0.5)
+
+
+class Problem:
+    """A problem built by the host mirror (mesh, field, terms, pre())."""
+
+    def __init__(self, cfg):
+        L = lib()
+        self.ptr = C.c_void_p()
+        check(L.fg_problem_create(C.byref(cfg), C.byref(self.ptr)))
+        self.cfg = cfg
+        self.mesh, self.rule, self.space, self.sys = MeshDesc(), RuleDesc(), SpaceDesc(), SystemDesc()
+        self.terms_ptr = C.POINTER(TermDesc)()
+        self.n_terms = C.c_int32()
+        self.dir_ptr = C.POINTER(C.c_double)()
+        check(L.fg_problem_descs(self.ptr, C.byref(self.mesh), C.byref(self.rule), C.byref(self.space), C.byref(self.sys),
+                                 C.byref(self.terms_ptr), C.byref(self.n_terms), C.byref(self.dir_ptr)))
+
+    def close(self):
+        if self.ptr:
+            lib().fg_problem_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- arrays (copies)
+    @property
+    def E(self):
+        return self.mesh.n_elements
+
+    @property
+    def n(self):
+        return self.space.n_basis * self.space.multiplicity
+
+    @property
+    def nnz(self):
+        return int(self.ai[-1])
+
+    def arrays(self):
+        m, r, s, y = self.mesh, self.rule, self.space, self.sys
+        nq, nn, nb, no = r.nq, m.nodes_per_element, s.n_basis, s.n_orientations
+        out = dict(
+            dim=m.dim, nn=nn, nq=nq, nb=nb, mult=s.multiplicity, n_orient=no, E=m.n_elements,
+            xyz=_arr(m.node_xyz, 3 * m.n_nodes, np.float64).reshape(-1, 3),
+            enodes=_arr(m.elem_nodes, nn * m.n_elements, np.int64).reshape(-1, nn),
+            w=_arr(r.weights, nq, np.float64),
+            geo_val=_arr(r.geo_val, nq * nn, np.float64).reshape(nq, nn),
+            geo_grad=_arr(r.geo_grad, nq * nn * 3, np.float64).reshape(nq, nn, 3),
+            bval=_arr(s.basis_val, no * nq * nb, np.float64).reshape(no, nq, nb),
+            bgrad=_arr(s.basis_grad, no * nq * nb * 3, np.float64).reshape(no, nq, nb, 3),
+            orient=(_arr(s.elem_orientation, m.n_elements, np.int32) if no > 1 else np.zeros(m.n_elements, np.int32)),
+            n_rows=y.n_rows, ai=self.ai, aj=_arr(y.aj, int(self.ai[-1]), np.uint64),
+            edof=_arr(y.elem_dof_idx, self.n * m.n_elements, np.uint64).reshape(m.n_elements, self.n),
+            etype=_arr(y.elem_dof_type, self.n * m.n_elements, np.int32).reshape(m.n_elements, self.n),
+            n_fixed=y.n_fixed,
+            dirichlet=(_arr(self.dir_ptr, 2 * y.n_fixed, np.float64).view(np.complex128) if y.n_fixed else np.zeros(0, np.complex128)),
+        )
+        return out
+
+    @property
+    def ai(self):
+        return _arr(self.sys.ai, self.sys.n_rows + 1, np.uint64)
+
+    def terms(self):
+        return self.terms_ptr, self.n_terms.value
+
+    def raw_dofs(self):
+        L = lib()
+        n = L.fg_problem_n_dofs(self.ptr)
+        nt = np.zeros(n, np.uint64)
+        ent = np.zeros(n, np.uint64)
+        nd = np.zeros(n, np.uint64)
+        at = np.zeros(n, np.int32)
+        xyz = np.zeros((n, 3), np.float32)
+        check(L.fg_problem_raw_dofs(self.ptr, nt.ctypes.data, ent.ctypes.data, nd.ctypes.data, at.ctypes.data, xyz.ctypes.data))
+        return dict(num_type=nt, entity=ent, num_dof=nd, assemble_type=at, xyz=xyz)
+
+    def created_dofs(self):
+        L = lib()
+        n = L.fg_problem_n_dofs(self.ptr)
+        nt = np.zeros(n, np.uint64)
+        ent = np.zeros(n, np.uint64)
+        at = np.zeros(n, np.int32)
+        xyz = np.zeros((n, 3), np.float32)
+        check(L.fg_problem_created_dofs(self.ptr, nt.ctypes.data, ent.ctypes.data, at.ctypes.data, xyz.ctypes.data))
+        return dict(num_type=nt, entity=ent, assemble_type=at, xyz=xyz)
+
+    def reserve_log(self):
+        L = lib()
+        n = L.fg_problem_reserve_log(self.ptr, None, None, 0)
+        at = np.zeros(n, np.uint64)
+        arg = np.zeros(n, np.uint64)
+        L.fg_problem_reserve_log(self.ptr, at.ctypes.data, arg.ctypes.data, n)
+        return at, arg
+
+    def bbox(self):
+        b = np.zeros(6)
+        check(lib().fg_problem_bbox(self.ptr, b.ctypes.data))
+        return b
+
+    def pre_seconds(self):
+        return lib().fg_problem_pre_seconds(self.ptr)
+
+    def plan(self):
+        return Plan(self)
+
+
+class Plan:
+    """fg_plan over a Problem's descriptors (through the C ABI)."""
+
+    def __init__(self, prob):
+        L = lib()
+        self.prob = prob
+        self.ptr = C.c_void_p()
+        check(L.fg_plan_create(C.byref(prob.mesh), C.byref(prob.rule), C.byref(prob.space), C.byref(prob.sys), C.byref(self.ptr)))
+
+    def close(self):
+        if self.ptr:
+            lib().fg_plan_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        nnz, E = C.c_int64(), C.c_int64()
+        n, nq, no = C.c_int32(), C.c_int32(), C.c_int32()
+        check(lib().fg_plan_info(self.ptr, C.byref(nnz), C.byref(E), C.byref(n), C.byref(nq), C.byref(no)))
+        return dict(nnz=nnz.value, E=E.value, n=n.value, nq=nq.value, n_orient=no.value)
+
+    def bind_terms(self, frequency=0.0):
+        t, nt = self.prob.terms()
+        check(lib().fg_plan_bind_terms(self.ptr, t, nt, frequency))
+
+    def assemble(self, precision="fp64", values=None, rhs=None, bound=False, frequency=0.0, stream=None, report=False):
+        """Assemble into numpy arrays (host outputs) or raw device pointers
+        (ints); returns (values, rhs[, report])."""
+        L = lib()
+        p = self.prob
+        nnz = p.nnz
+        nrows = p.sys.n_rows
+        if values is None:
+            values = np.zeros(nnz, np.complex128)
+        if rhs is None:
+            rhs = np.zeros(nrows, np.complex128)
+        vptr = values if isinstance(values, int) else values.ctypes.data
+        rptr = rhs if isinstance(rhs, int) else (rhs.ctypes.data if rhs is not False else None)
+        t, nt = (None, 0) if bound else p.terms()
+        dptr = C.cast(p.dir_ptr, C.c_void_p) if p.sys.n_fixed else None
+        if precision == "fp64":
+            check(L.fg_assemble_fp64(self.ptr, t, nt, frequency, dptr, vptr, rptr, stream))
+            return values, rhs
+        rep = ErrReport()
+        check(L.fg_assemble_mixed(self.ptr, t, nt, frequency, dptr, vptr, rptr, stream, C.byref(rep) if report else None))
+        if report:
+            return values, rhs, dict(max_elem=rep.max_elem_rel_fro, mean_elem=rep.mean_elem_rel_fro, global_=rep.global_rel_fro)
+        return values, rhs

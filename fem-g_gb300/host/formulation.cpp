@@ -1,0 +1,532 @@
+#include "formulation.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+
+namespace femg {
+
+// ---------------------------------------------------------------- Domain
+
+Domain::Domain(const Mesh &mesh, const std::string &physical) {
+  auto it = mesh.physicals.find(physical);
+  if (it == mesh.physicals.end()) throw std::invalid_argument("unknown physical group " + physical);
+  entities = it->second;
+  std::sort(entities.begin(), entities.end());
+}
+
+int Domain::maxDim() const {
+  int d = 0;
+  for (auto &e : entities) d = std::max(d, e.first);
+  return d;
+}
+
+bool Domain::have(int dim, int tag) const {
+  return std::find(entities.begin(), entities.end(), std::make_pair(dim, tag)) != entities.end();
+}
+
+// --------------------------------------------------------- FunctionSpace
+
+int FunctionSpace::keysPerElement(int elementType) const {
+  if (type == SpaceType::Lagrange) return elementNodes(elementType);
+  const int dim = elementDim(elementType);
+  if (dim == 1) return 2 + (order - 1);
+  return hierarchicalCount(dim, order);
+}
+
+void FunctionSpace::getKeys(const Mesh &mesh, const ElementBlock &blk, bool withCoord, std::vector<int> &typeKeys,
+                            std::vector<uint64_t> &entityKeys, std::vector<double> &coord,
+                            std::vector<int> *infoDim) const {
+  typeKeys.clear();
+  entityKeys.clear();
+  coord.clear();
+  if (infoDim) infoDim->clear();
+  const int nn = blk.nodesPerElement;
+  const int dim = elementDim(blk.type);
+  const int nv = elementVertices(blk.type);
+  const int64_t E = blk.size();
+  const int nk = keysPerElement(blk.type);
+  typeKeys.reserve((size_t)E * nk);
+  entityKeys.reserve((size_t)E * nk);
+  if (withCoord) coord.reserve((size_t)E * nk * 3);
+  auto pushCoord = [&](const double *p) {
+    if (withCoord) coord.insert(coord.end(), p, p + 3);
+  };
+  if (type == SpaceType::Lagrange) {
+    for (int64_t e = 0; e < E; ++e)
+      for (int k = 0; k < nn; ++k) {
+        const int64_t node = blk.nodes[(size_t)(e * nn + k)];
+        typeKeys.push_back(0);
+        entityKeys.push_back((uint64_t)node + 1);
+        pushCoord(&mesh.xyz[3 * node]);
+        if (infoDim) infoDim->push_back(k < nv ? 0 : 1);
+      }
+    return;
+  }
+  const int p = order;
+  const int nf = (p - 1) * (p - 2) / 2;
+  const int ni3 = (p - 1) * (p - 2) * (p - 3) / 6;
+  for (int64_t e = 0; e < E; ++e) {
+    const int64_t *v = &blk.nodes[(size_t)(e * nn)];
+    double cen[3] = {0, 0, 0};
+    for (int a = 0; a < nv; ++a)
+      for (int c = 0; c < 3; ++c) cen[c] += mesh.xyz[3 * v[a] + c] / nv;
+    for (int a = 0; a < nv; ++a) {
+      typeKeys.push_back(0);
+      entityKeys.push_back((uint64_t)v[a] + 1);
+      pushCoord(&mesh.xyz[3 * v[a]]);
+      if (infoDim) infoDim->push_back(0);
+    }
+    for (auto &ed : simplexEdges(dim)) {
+      const int64_t tag = mesh.edgeTagOf(v[ed[0]], v[ed[1]]);
+      double mid[3];
+      for (int c = 0; c < 3; ++c) mid[c] = 0.5 * (mesh.xyz[3 * v[ed[0]] + c] + mesh.xyz[3 * v[ed[1]] + c]);
+      for (int k = 0; k <= p - 2; ++k) {
+        typeKeys.push_back(1 + k);
+        entityKeys.push_back((uint64_t)tag);
+        pushCoord(mid);
+        if (infoDim) infoDim->push_back(1);
+      }
+    }
+    if (dim == 2) {
+      for (int k = 0; k < nf; ++k) {
+        typeKeys.push_back(p + k);
+        entityKeys.push_back((uint64_t)blk.tags[(size_t)e]);
+        pushCoord(cen);
+        if (infoDim) infoDim->push_back(2);
+      }
+    } else if (dim == 3) {
+      for (auto &fc : simplexFaces(3)) {
+        const int64_t tag = mesh.faceTagOf(v[fc[0]], v[fc[1]], v[fc[2]]);
+        double fcen[3];
+        for (int c = 0; c < 3; ++c) fcen[c] = (mesh.xyz[3 * v[fc[0]] + c] + mesh.xyz[3 * v[fc[1]] + c] + mesh.xyz[3 * v[fc[2]] + c]) / 3.0;
+        for (int k = 0; k < nf; ++k) {
+          typeKeys.push_back(p + k);
+          entityKeys.push_back((uint64_t)tag);
+          pushCoord(fcen);
+          if (infoDim) infoDim->push_back(2);
+        }
+      }
+      for (int k = 0; k < ni3; ++k) {
+        typeKeys.push_back(p + nf + k);
+        entityKeys.push_back((uint64_t)blk.tags[(size_t)e]);
+        pushCoord(cen);
+        if (infoDim) infoDim->push_back(3);
+      }
+    }
+  }
+}
+
+int FunctionSpace::basisFunctions(bool derivative, const Mesh &mesh, const ElementBlock &blk, const QuadRule &rule,
+                                  std::vector<double> &table, std::vector<int32_t> &denseOrient, int &nOrient) const {
+  const int64_t E = blk.size();
+  const int ncomp = derivative ? 3 : 1;
+  denseOrient.assign((size_t)E, 0);
+  table.clear();
+  if (type == SpaceType::Lagrange) {
+    const int n = elementNodes(blk.type);
+    nOrient = 1;
+    std::vector<double> val(n), grad(3 * n);
+    for (int q = 0; q < rule.nq; ++q) {
+      lagrangeBasis(blk.type, &rule.points[3 * q], val.data(), grad.data());
+      for (int i = 0; i < n; ++i)
+        for (int c = 0; c < ncomp; ++c) table.push_back(derivative ? grad[3 * i + c] : val[i]);
+    }
+    return n;
+  }
+  const int dim = elementDim(blk.type);
+  const int n = hierarchicalCount(dim, order);
+  const int nn = blk.nodesPerElement;
+  const int nv = elementVertices(blk.type);
+  // raw orientation per element, then the dense numbering of first
+  // appearance (getDenseOrientations, src/field/FunctionSpaceInterface.cpp:495-519)
+  std::vector<int> unique;
+  std::map<int, int> denseOf;
+  for (int64_t e = 0; e < E; ++e) {
+    int64_t tags[4];
+    for (int a = 0; a < nv; ++a) tags[a] = blk.nodes[(size_t)(e * nn + a)] + 1;
+    const int code = orientationFree() ? 0 : hierarchicalOrientation(dim, tags);
+    auto it = denseOf.find(code);
+    if (it == denseOf.end()) {
+      it = denseOf.emplace(code, (int)unique.size()).first;
+      unique.push_back(code);
+    }
+    denseOrient[(size_t)e] = it->second;
+  }
+  nOrient = (int)unique.size();
+  std::vector<double> val(n), grad(3 * n);
+  for (int o = 0; o < nOrient; ++o)
+    for (int q = 0; q < rule.nq; ++q) {
+      hierarchicalBasis(dim, order, unique[o], &rule.points[3 * q], val.data(), grad.data());
+      for (int i = 0; i < n; ++i)
+        for (int c = 0; c < ncomp; ++c) table.push_back(derivative ? grad[3 * i + c] : val[i]);
+    }
+  (void)mesh;
+  return n;
+}
+
+// -------------------------------------------------------------- Function
+
+Function::Function(cplx v) { code.push_back({FG_OP_CONST, 0, v.real(), v.imag()}); }
+
+Function Function::x() {
+  Function f;
+  f.code = {{FG_OP_X, 0, 0.0, 0.0}};
+  return f;
+}
+Function Function::y() {
+  Function f;
+  f.code = {{FG_OP_Y, 0, 0.0, 0.0}};
+  return f;
+}
+Function Function::z() {
+  Function f;
+  f.code = {{FG_OP_Z, 0, 0.0, 0.0}};
+  return f;
+}
+
+Function Function::perElement(const std::vector<cplx> &values) {
+  Function f;
+  auto arr = std::make_shared<std::vector<double>>(2 * values.size());
+  for (size_t i = 0; i < values.size(); ++i) {
+    (*arr)[2 * i] = values[i].real();
+    (*arr)[2 * i + 1] = values[i].imag();
+  }
+  f.arrays = {arr};
+  f.code = {{FG_OP_ELEM, 0, 0.0, 0.0}};
+  return f;
+}
+
+bool Function::usesPoints() const {
+  for (auto &i : code)
+    if (i.op == FG_OP_X || i.op == FG_OP_Y || i.op == FG_OP_Z) return true;
+  return false;
+}
+
+bool Function::usesElements() const {
+  for (auto &i : code)
+    if (i.op == FG_OP_ELEM) return true;
+  return false;
+}
+
+cplx Function::constantValue() const {
+  if (!isConstant()) throw std::logic_error("not a constant function");
+  std::vector<cplx> st;
+  for (auto &in : code) {
+    if (in.op == FG_OP_CONST) {
+      st.push_back(cplx(in.re, in.im));
+      continue;
+    }
+    if (in.op == FG_OP_NEG) {
+      st.back() = -st.back();
+      continue;
+    }
+    if (in.op == FG_OP_HEAVISIDE) {
+      const double r = st.back().real();
+      st.back() = r > 0 ? 1.0 : (r < 0 ? 0.0 : 0.5);
+      continue;
+    }
+    cplx b = st.back();
+    st.pop_back();
+    cplx &a = st.back();
+    if (in.op == FG_OP_ADD) a += b;
+    else if (in.op == FG_OP_SUB) a -= b;
+    else if (in.op == FG_OP_MUL) a *= b;
+    else if (in.op == FG_OP_DIV) a /= b;
+  }
+  return st.back();
+}
+
+fg_expr Function::toExpr() const {
+  fg_expr e;
+  std::memset(&e, 0, sizeof(e));
+  if (code.size() > FG_EXPR_MAX_CODE) throw std::length_error("expression too long");
+  if (arrays.size() > FG_EXPR_MAX_ARRAYS) throw std::length_error("too many per-element arrays");
+  e.n_code = (int32_t)code.size();
+  for (size_t i = 0; i < code.size(); ++i) e.code[i] = code[i];
+  e.n_arrays = (int32_t)arrays.size();
+  for (size_t i = 0; i < arrays.size(); ++i) e.elem_values[i] = arrays[i]->data();
+  return e;
+}
+
+Function Function::binary(const Function &a, const Function &b, int op) {
+  Function r;
+  r.code = a.code;
+  r.arrays = a.arrays;
+  const int32_t shift = (int32_t)a.arrays.size();
+  for (auto in : b.code) {
+    if (in.op == FG_OP_ELEM) in.arg += shift;
+    r.code.push_back(in);
+  }
+  r.arrays.insert(r.arrays.end(), b.arrays.begin(), b.arrays.end());
+  r.code.push_back({op, 0, 0.0, 0.0});
+  return r;
+}
+
+Function operator+(const Function &a, const Function &b) { return Function::binary(a, b, FG_OP_ADD); }
+Function operator-(const Function &a, const Function &b) { return Function::binary(a, b, FG_OP_SUB); }
+Function operator*(const Function &a, const Function &b) { return Function::binary(a, b, FG_OP_MUL); }
+Function operator/(const Function &a, const Function &b) { return Function::binary(a, b, FG_OP_DIV); }
+Function operator-(const Function &a) {
+  Function r = a;
+  r.code.push_back({FG_OP_NEG, 0, 0.0, 0.0});
+  return r;
+}
+Function heaviside(const Function &a) {
+  Function r = a;
+  r.code.push_back({FG_OP_HEAVISIDE, 0, 0.0, 0.0});
+  return r;
+}
+
+// ------------------------------------------------------------ Field / DSL
+
+Field::Field(const std::string &n, const Domain &d, SpaceType t, int order, int mult, unsigned tg)
+    : name(n), domain(d), multiplicity(mult), tag(tg) {
+  fs.type = t;
+  fs.order = order;
+}
+
+Operand dof(Field &f) {
+  Operand o;
+  o.field = &f;
+  return o;
+}
+Operand tf(Field &f) {
+  Operand o;
+  o.field = &f;
+  o.test = true;
+  return o;
+}
+Operand dt_dof(Field &f) {
+  Operand o = dof(f);
+  o.dt = 1;
+  return o;
+}
+Operand dt2_dof(Field &f) {
+  Operand o = dof(f);
+  o.dt = 2;
+  return o;
+}
+Operand grad(Operand o) {
+  o.grad = true;
+  return o;
+}
+Operand operator*(const Function &c, Operand o) {
+  o.coef = c * o.coef;
+  return o;
+}
+Operand operator*(const Tensor4Isotropic &C, Operand o) {
+  o.tensor4 = true;
+  o.C = C;
+  return o;
+}
+
+// ----------------------------------------------------------- Formulation
+
+void Formulation::integral(const Operand &unknown, const Operand &test, const Domain &d, const std::string &gauss) {
+  if (unknown.test || !test.test) throw std::invalid_argument("integral(dof(...), tf(...)) expected");
+  bterms_.push_back({unknown, test, d, gauss});
+}
+
+void Formulation::integral(const Function &f, const Operand &test, const Domain &d, const std::string &gauss) {
+  if (!test.test) throw std::invalid_argument("integral(f, tf(...)) expected");
+  lterms_.push_back({f, test, d, gauss});
+}
+
+void Formulation::fillIndices(const Field &f, const ElementBlock &blk, std::vector<uint64_t> &idx, std::vector<int32_t> &type) const {
+  std::vector<int> typeKeys;
+  std::vector<uint64_t> entityKeys;
+  std::vector<double> coord;
+  f.fs.getKeys(*mesh, blk, false, typeKeys, entityKeys, coord, nullptr);
+  const size_t nk = typeKeys.size();
+  const int multi = f.multiplicity;
+  idx.assign(nk * multi, 0);
+  type.assign(nk * multi, 0);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < (int64_t)nk; ++i)
+    for (int j = 0; j < multi; ++j) {
+      const Dof *d = f.dofs.find((uint64_t)typeKeys[(size_t)i] + kDofFieldOffset * (f.tag + j), entityKeys[(size_t)i]);
+      if (d) {
+        idx[(size_t)i * multi + j] = d->numDof - 1;
+        type[(size_t)i * multi + j] = d->assembleType;
+      }
+    }
+}
+
+void Formulation::pre(const Mesh &m) {
+  auto t0 = std::chrono::steady_clock::now();
+  mesh = &m;
+  if (bterms_.empty()) throw std::invalid_argument("no bilinear term");
+  field = bterms_[0].unknown.field;
+  for (auto &t : bterms_)
+    if (t.unknown.field != field || t.test.field != field) throw std::invalid_argument("one field per formulation in this mirror");
+  for (auto &t : lterms_)
+    if (t.test.field != field) throw std::invalid_argument("one field per formulation in this mirror");
+  Field &f = *field;
+
+  // ---- DofsFactory::generate: fixed DOFs, then unknown DOFs
+  const int maxDim = f.domain.maxDim();
+  nFixed = nUnknown = nBubble = 0;
+  f.dofs = DofDictionary();
+  f.fixedValues.clear();
+  reserveLog.clear();
+  std::vector<int> typeKeys, info;
+  std::vector<uint64_t> entityKeys;
+  std::vector<double> coord;
+  for (auto &c : f.constraints) {
+    if (!f.fs.orientationFree() || f.multiplicity != 1)
+      throw std::invalid_argument("constraints need a Lagrange / order-1 scalar field in this mirror");
+    for (auto &de : c.domain.entities) {
+      const Entity *ent = m.find(de.first, de.second);
+      if (!ent) continue;
+      for (auto &blk : ent->blocks) {
+        f.fs.getKeys(m, blk, true, typeKeys, entityKeys, coord, nullptr);
+        reserveLog.push_back({f.dofs.size(), f.dofs.size() + typeKeys.size()});
+        f.dofs.reserve(f.dofs.size() + typeKeys.size());
+        for (size_t j = 0; j < typeKeys.size(); ++j) {
+          Dof d;
+          d.numType = (uint64_t)typeKeys[j] + kDofFieldOffset * f.tag;
+          d.entity = entityKeys[j];
+          d.assembleType = kAtFixed;
+          for (int k = 0; k < 3; ++k) d.xyz[k] = (float)coord[3 * j + k];
+          d.numDof = nFixed + 1;
+          if (f.dofs.insert(d)) {
+            ++nFixed;
+            f.fixedValues.push_back(c.value);
+          }
+        }
+      }
+    }
+  }
+  for (auto &de : f.domain.entities) {
+    const Entity *ent = m.find(de.first, de.second);
+    if (!ent) continue;
+    for (auto &blk : ent->blocks) {
+      const bool top = de.first == maxDim;
+      f.fs.getKeys(m, blk, true, typeKeys, entityKeys, coord, top ? &info : nullptr);
+      reserveLog.push_back({f.dofs.size(), f.dofs.size() + typeKeys.size() * f.multiplicity});
+      f.dofs.reserve(f.dofs.size() + typeKeys.size() * f.multiplicity);
+      for (size_t j = 0; j < typeKeys.size(); ++j)
+        for (int k = 0; k < f.multiplicity; ++k) {
+          const bool bubble = top && info[j] == maxDim;
+          Dof d;
+          d.numType = (uint64_t)typeKeys[j] + kDofFieldOffset * (f.tag + k);
+          d.entity = entityKeys[j];
+          d.assembleType = bubble ? kAtUnknownBubble : kAtUnknown;
+          for (int c = 0; c < 3; ++c) d.xyz[c] = (float)coord[3 * j + c];
+          d.numDof = nUnknown + 1;
+          if (f.dofs.insert(d)) {
+            ++nUnknown;
+            if (bubble) ++nBubble;
+          }
+        }
+    }
+  }
+  created = f.dofs.pool;
+
+  // ---- DofsManager::reorderWithHilbert(true)
+  if (m.dim == 2 || m.dim == 3) {
+    std::vector<DofDictionary *> fields = {&f.dofs};
+    reorderWithHilbert(m.dim, m.bbox, fields, nUnknown, nBubble);
+  }
+
+  // ---- pattern over the entities carrying bilinear terms
+  PatternBuilder pb;
+  pb.init(nUnknown);
+  bucket = nullptr;
+  for (auto &ent : m.entities) {
+    bool have = false;
+    for (auto &t : bterms_) have = have || t.domain.have(ent.dim, ent.tag);
+    if (!have) continue;
+    for (auto &blk : ent.blocks) {
+      if (bucket) throw std::invalid_argument("this mirror assembles a single element bucket");
+      bucket = &blk;
+      fillIndices(f, blk, elemDofIdx, elemDofType);
+      const int n = (int)(elemDofIdx.size() / blk.size());
+      pb.addElements(blk.size(), n, n, elemDofIdx.data(), elemDofType.data(), elemDofIdx.data(), elemDofType.data());
+    }
+  }
+  if (!bucket) throw std::invalid_argument("no element carries a bilinear term");
+  pb.finalize(ai, aj);
+
+  // ---- element bucket data (Assembler::assemblyInitialization)
+  std::string gauss = bterms_[0].gauss;
+  for (auto &t : bterms_)
+    if (t.gauss != gauss) throw std::invalid_argument("one integration type per formulation in this mirror");
+  for (auto &t : lterms_)
+    if (t.gauss != gauss) throw std::invalid_argument("one integration type per formulation in this mirror");
+  rule = gaussRule(gauss, bucket->type);
+  const int nn = bucket->nodesPerElement;
+  geoVal.assign((size_t)rule.nq * nn, 0.0);
+  geoGrad.assign((size_t)rule.nq * nn * 3, 0.0);
+  for (int q = 0; q < rule.nq; ++q) lagrangeBasis(bucket->type, &rule.points[3 * q], &geoVal[(size_t)q * nn], &geoGrad[(size_t)q * nn * 3]);
+  int no1 = 1, no2 = 1;
+  std::vector<int32_t> o2;
+  nBasis = f.fs.basisFunctions(false, m, *bucket, rule, basisVal, orient, no1);
+  f.fs.basisFunctions(true, m, *bucket, rule, basisGrad, o2, no2);
+  nOrient = no1;
+  dirichlet.assign(2 * nFixed, 0.0);
+  for (uint64_t i = 0; i < nFixed; ++i) {
+    dirichlet[2 * i] = f.fixedValues[i].real();
+    dirichlet[2 * i + 1] = f.fixedValues[i].imag();
+  }
+
+  // ---- terms for the C ABI
+  termDescs.clear();
+  for (auto &t : bterms_) {
+    fg_term_desc d;
+    std::memset(&d, 0, sizeof(d));
+    if (!t.test.coef.isConstant() || t.test.coef.constantValue() != cplx(1.0, 0.0))
+      throw std::invalid_argument("coefficients on the test function are not supported");
+    if (t.unknown.grad != t.test.grad) throw std::invalid_argument("mixed value/gradient terms are not supported");
+    d.dt = t.unknown.dt;
+    if (t.unknown.tensor4) {
+      if (!t.unknown.grad) throw std::invalid_argument("Tensor4 needs gradients");
+      d.kind = FG_TERM_ELASTIC;
+      d.coef = (t.unknown.coef * t.unknown.C.lambda).toExpr();
+      d.coef2 = (t.unknown.coef * t.unknown.C.mu).toExpr();
+    } else {
+      d.kind = t.unknown.grad ? FG_TERM_GRAD_GRAD : FG_TERM_MASS;
+      d.coef = t.unknown.coef.toExpr();
+    }
+    termDescs.push_back(d);
+  }
+  for (auto &t : lterms_) {
+    fg_term_desc d;
+    std::memset(&d, 0, sizeof(d));
+    if (t.test.grad) throw std::invalid_argument("gradient test functions in linear terms are not supported");
+    d.kind = FG_TERM_SOURCE;
+    d.coef = t.f.toExpr();
+    termDescs.push_back(d);
+  }
+  preSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void Formulation::descs(fg_mesh_desc *md, fg_rule_desc *rd, fg_space_desc *sd, fg_system_desc *sys) const {
+  md->dim = elementDim(bucket->type);
+  md->nodes_per_element = bucket->nodesPerElement;
+  md->n_nodes = mesh->nNodes();
+  md->node_xyz = mesh->xyz.data();
+  md->n_elements = bucket->size();
+  md->elem_nodes = bucket->nodes.data();
+  rd->nq = rule.nq;
+  rd->weights = rule.weights.data();
+  rd->geo_val = geoVal.data();
+  rd->geo_grad = geoGrad.data();
+  sd->n_basis = nBasis;
+  sd->multiplicity = field->multiplicity;
+  sd->n_orientations = nOrient;
+  sd->basis_val = basisVal.data();
+  sd->basis_grad = basisGrad.data();
+  sd->elem_orientation = nOrient > 1 ? orient.data() : nullptr;
+  sys->n_rows = nUnknown;
+  sys->ai = ai.data();
+  sys->aj = aj.data();
+  sys->elem_dof_idx = elemDofIdx.data();
+  sys->elem_dof_type = elemDofType.data();
+  sys->n_fixed = nFixed;
+}
+
+}  // namespace femg

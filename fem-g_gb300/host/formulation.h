@@ -1,0 +1,183 @@
+// Host-side mirror of the reference's user-facing assembly interface:
+// Domain, Field / CompoundField with a FunctionSpace, the equation DSL
+// (dof, tf, grad, dt_dof, dt2_dof), coefficient functions, and
+// Formulation::integral / pre / assemble.
+//
+// Reference interfaces mirrored:
+//   Formulation<T>::integral    src/problem/Formulation.cpp:219-746
+//   Formulation<T>::pre         src/problem/Formulation.cpp:897-1039
+//   Formulation<T>::assemble    src/problem/Formulation.cpp:1152-1215
+//   dof / tf / grad / dt_dof    src/equation/UnknownField.h:103-132
+//   Field<T, Form0>             src/field/Field.cpp:116-135
+//   FieldInterface::fillIndices src/field/FieldInterface.cpp:1012-1076
+//
+// assemble() is the GPU drop-in: it runs through the C ABI of
+// include/fem_g_gb300.h (fg_plan_create + fg_assemble_fp64/mixed).
+#pragma once
+#include <complex>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/fem_g_gb300.h"
+#include "dofs.h"
+#include "mesh.h"
+#include "refelem.h"
+
+namespace femg {
+
+using cplx = std::complex<double>;
+
+struct Domain {
+  std::vector<std::pair<int, int>> entities;  // (dim, tag), sorted
+  Domain() = default;
+  Domain(const Mesh &mesh, const std::string &physical);
+  int maxDim() const;
+  bool have(int dim, int tag) const;
+};
+
+enum class SpaceType { Lagrange = 0, HierarchicalH1 = 1 };
+
+class FunctionSpace {
+ public:
+  SpaceType type = SpaceType::Lagrange;
+  int order = 1;  // hierarchical order; Lagrange uses the mesh order
+
+  // "None" for Lagrange and hierarchical order 1, "HierarchicalSolin" otherwise
+  // (src/field/FunctionSpaceHierarchicalH1.cpp:44-50)
+  bool orientationFree() const { return type == SpaceType::Lagrange || order == 1; }
+  bool isConstantByElements() const { return type == SpaceType::Lagrange; }
+  int keysPerElement(int elementType) const;
+  // keys of all elements of a block in element order (gmsh getKeys semantics
+  // of this mirror): Lagrange -> (0, node tag) per element node; hierarchical
+  // -> vertices (0, node tag), edges (1+k, edge tag), faces (p+k, face tag),
+  // interior (p+nf+k, element tag). infoDim: dimension of the key's entity.
+  void getKeys(const Mesh &mesh, const ElementBlock &blk, bool withCoord, std::vector<int> &typeKeys,
+               std::vector<uint64_t> &entityKeys, std::vector<double> &coord, std::vector<int> *infoDim) const;
+  // basis tables: returns n; table [nOrient][nq][n][ncomp]; denseOrient per element
+  int basisFunctions(bool derivative, const Mesh &mesh, const ElementBlock &blk, const QuadRule &rule,
+                     std::vector<double> &table, std::vector<int32_t> &denseOrient, int &nOrient) const;
+};
+
+// Complex scalar coefficient: an expression in reverse Polish order
+class Function {
+ public:
+  std::vector<fg_instr> code;
+  std::vector<std::shared_ptr<std::vector<double>>> arrays;  // per element (re, im)
+
+  Function(double v = 0.0) : Function(cplx(v, 0.0)) {}
+  Function(cplx v);
+  static Function x();
+  static Function y();
+  static Function z();
+  static Function perElement(const std::vector<cplx> &values);
+
+  bool usesPoints() const;
+  bool usesElements() const;
+  bool isConstant() const { return !usesPoints() && !usesElements(); }
+  cplx constantValue() const;
+  fg_expr toExpr() const;
+
+  friend Function operator+(const Function &a, const Function &b);
+  friend Function operator-(const Function &a, const Function &b);
+  friend Function operator*(const Function &a, const Function &b);
+  friend Function operator/(const Function &a, const Function &b);
+  friend Function operator-(const Function &a);
+  friend Function heaviside(const Function &a);
+
+ private:
+  static Function binary(const Function &a, const Function &b, int op);
+};
+
+struct Tensor4Isotropic {  // C_ijkl = lambda d_ij d_kl + mu (d_ik d_jl + d_il d_jk)
+  Function lambda, mu;
+};
+
+class Field {
+ public:
+  Field(const std::string &name, const Domain &domain, SpaceType type, int order, int multiplicity, unsigned tag);
+  std::string name;
+  Domain domain;
+  FunctionSpace fs;
+  int multiplicity = 1;
+  unsigned tag = 0;
+  struct Constraint {
+    Domain domain;
+    cplx value;
+  };
+  std::vector<Constraint> constraints;
+  void addConstraint(const Domain &d, cplx value) { constraints.push_back({d, value}); }
+  DofDictionary dofs;
+  std::vector<cplx> fixedValues;  // by fixed numDof - 1
+};
+
+struct Operand {
+  Field *field = nullptr;
+  bool grad = false;
+  bool test = false;
+  int dt = 0;
+  Function coef = Function(1.0);
+  bool tensor4 = false;
+  Tensor4Isotropic C;
+};
+Operand dof(Field &f);
+Operand tf(Field &f);
+Operand dt_dof(Field &f);
+Operand dt2_dof(Field &f);
+Operand grad(Operand o);
+Operand operator*(const Function &c, Operand o);
+Operand operator*(const Tensor4Isotropic &C, Operand o);
+
+class Formulation {
+ public:
+  explicit Formulation(const std::string &name) : name_(name) {}
+  void integral(const Operand &unknown, const Operand &test, const Domain &d, const std::string &gauss);
+  void integral(const Function &f, const Operand &test, const Domain &d, const std::string &gauss);
+
+  // DOFs, Hilbert numbering, CSR pattern, element bucket data
+  void pre(const Mesh &mesh);
+
+  // results of pre()
+  uint64_t nUnknown = 0, nBubble = 0, nFixed = 0;
+  std::vector<uint64_t> ai, aj;
+  Field *field = nullptr;
+  const Mesh *mesh = nullptr;
+  const ElementBlock *bucket = nullptr;
+  QuadRule rule;
+  std::vector<double> geoVal, geoGrad;    // [nq][nn], [nq][nn][3]
+  std::vector<double> basisVal, basisGrad;
+  std::vector<int32_t> orient;
+  int nBasis = 0, nOrient = 1;
+  std::vector<uint64_t> elemDofIdx;
+  std::vector<int32_t> elemDofType;
+  std::vector<double> dirichlet;          // [nFixed][2]
+  std::vector<fg_term_desc> termDescs;    // C ABI terms
+  // reserve calls on the DOF dictionary: (DOFs created before the call, argument)
+  std::vector<std::pair<uint64_t, uint64_t>> reserveLog;
+  double preSeconds = 0.0;
+
+  // C ABI descriptors over the data above
+  void descs(fg_mesh_desc *m, fg_rule_desc *r, fg_space_desc *s, fg_system_desc *sys) const;
+
+  // created DOFs in creation order (before numbering), for numbering checks
+  std::vector<Dof> created;
+
+ private:
+  struct BTerm {
+    Operand unknown, test;
+    Domain domain;
+    std::string gauss;
+  };
+  struct LTerm {
+    Function f;
+    Operand test;
+    Domain domain;
+    std::string gauss;
+  };
+  std::string name_;
+  std::vector<BTerm> bterms_;
+  std::vector<LTerm> lterms_;
+  void fillIndices(const Field &f, const ElementBlock &blk, std::vector<uint64_t> &idx, std::vector<int32_t> &type) const;
+};
+
+}  // namespace femg

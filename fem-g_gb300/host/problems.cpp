@@ -1,0 +1,198 @@
+// C ABI of the host mirror (include/fem_g_gb300_host.h): builds the benchmark
+// problems the way a GmshFEM user program does (mesh, field, constraints,
+// Formulation::integral, pre) and hands their descriptors to the GPU plan.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/fem_g_gb300_host.h"
+#include "formulation.h"
+
+namespace femg {
+void setLastError(const std::string &msg);
+}
+
+struct fg_problem {
+  fg_problem_config cfg;
+  femg::Mesh mesh;
+  std::unique_ptr<femg::Field> u;
+  std::unique_ptr<femg::Formulation> form;
+  fg_plan *plan = nullptr;
+};
+
+using namespace femg;
+
+static void buildProblem(fg_problem *p) {
+  const fg_problem_config &c = p->cfg;
+  if (c.dim == 2)
+    p->mesh = makeSquareTri(c.m, c.mesh_order, c.jitter, c.seed);
+  else if (c.dim == 3)
+    p->mesh = makeCubeTet(c.m, c.mesh_order, c.jitter, c.seed);
+  else
+    throw std::invalid_argument("dim must be 2 or 3");
+  Domain omega(p->mesh, "omega");
+  const SpaceType st = c.space == FG_SPACE_LAGRANGE ? SpaceType::Lagrange : SpaceType::HierarchicalH1;
+  const int mult = c.kind == FG_PROBLEM_NAVIER ? 3 : 1;
+  p->u.reset(new Field("u", omega, st, c.order, mult, 0));
+  Field &u = *p->u;
+  p->form.reset(new Formulation(c.kind == FG_PROBLEM_NAVIER ? "navier" : "helmholtz"));
+  Formulation &f = *p->form;
+  const std::string gauss = "Gauss" + std::to_string(c.gauss);
+  const int64_t E = p->mesh.find(c.dim, 1)->blocks[0].size();
+  if (c.kind == FG_PROBLEM_HELMHOLTZ) {
+    if (c.dirichlet) {
+      if (c.dim != 2) throw std::invalid_argument("Dirichlet boundary only on the 2D square");
+      u.addConstraint(Domain(p->mesh, "gammaDir"), cplx(c.dirichlet_value, 0.0));
+    }
+    f.integral(grad(dof(u)), grad(tf(u)), omega, gauss);
+    if (c.coef_mode == FG_COEF_MODE_CONSTANT) {
+      f.integral(Function(-c.k * c.k) * dof(u), tf(u), omega, gauss);
+    } else {
+      // c_e = k^2 (1 + 0.3 xi_e), xi_e ~ N(0,1) per element in element order
+      Rng rng(c.seed + 1);
+      std::vector<cplx> ce((size_t)E);
+      for (int64_t e = 0; e < E; ++e) ce[(size_t)e] = cplx(-c.k * c.k * (1.0 + 0.3 * rng.normal()), 0.0);
+      f.integral(Function::perElement(ce) * dof(u), tf(u), omega, gauss);
+    }
+    if (c.source) {
+      Function x = Function::x(), y = Function::y();
+      Function fsrc = heaviside(Function(0.01) - (x - Function(0.5)) * (x - Function(0.5)) - (y - Function(0.5)) * (y - Function(0.5)));
+      f.integral(-fsrc, tf(u), omega, gauss);
+    }
+  } else if (c.kind == FG_PROBLEM_NAVIER) {
+    Rng rng(c.seed + 2);
+    std::vector<cplx> lam((size_t)E), mu((size_t)E);
+    for (int64_t e = 0; e < E; ++e) {
+      lam[(size_t)e] = std::exp(c.lame_sigma * rng.normal());
+      mu[(size_t)e] = std::exp(c.lame_sigma * rng.normal());
+    }
+    Tensor4Isotropic C{Function::perElement(lam), Function::perElement(mu)};
+    f.integral(C * grad(dof(u)), grad(tf(u)), omega, gauss);
+    f.integral(Function(-c.omega * c.omega) * dof(u), tf(u), omega, gauss);  // rho = 1
+  } else {
+    throw std::invalid_argument("unknown problem kind");
+  }
+  f.pre(p->mesh);
+}
+
+extern "C" {
+
+int fg_problem_create(const fg_problem_config *cfg, fg_problem **out) {
+  if (!cfg || !out) {
+    setLastError("fg_problem_create: null argument");
+    return FG_ERR_ARG;
+  }
+  *out = nullptr;
+  fg_problem *p = new (std::nothrow) fg_problem;
+  if (!p) return FG_ERR_OOM;
+  p->cfg = *cfg;
+  try {
+    buildProblem(p);
+  } catch (const std::bad_alloc &) {
+    delete p;
+    setLastError("fg_problem_create: out of memory");
+    return FG_ERR_OOM;
+  } catch (const std::exception &e) {
+    delete p;
+    setLastError(std::string("fg_problem_create: ") + e.what());
+    return FG_ERR_ARG;
+  }
+  *out = p;
+  return FG_OK;
+}
+
+void fg_problem_destroy(fg_problem *p) {
+  if (!p) return;
+  if (p->plan) fg_plan_destroy(p->plan);
+  delete p;
+}
+
+int fg_problem_descs(const fg_problem *p, fg_mesh_desc *mesh, fg_rule_desc *rule, fg_space_desc *space,
+                     fg_system_desc *sys, const fg_term_desc **terms, int32_t *n_terms, const double **dirichlet) {
+  if (!p) return FG_ERR_ARG;
+  fg_mesh_desc m;
+  fg_rule_desc r;
+  fg_space_desc s;
+  fg_system_desc y;
+  p->form->descs(&m, &r, &s, &y);
+  if (mesh) *mesh = m;
+  if (rule) *rule = r;
+  if (space) *space = s;
+  if (sys) *sys = y;
+  if (terms) *terms = p->form->termDescs.data();
+  if (n_terms) *n_terms = (int32_t)p->form->termDescs.size();
+  if (dirichlet) *dirichlet = p->form->nFixed ? p->form->dirichlet.data() : nullptr;
+  return FG_OK;
+}
+
+int64_t fg_problem_n_dofs(const fg_problem *p) { return p ? (int64_t)p->u->dofs.size() : -1; }
+
+int fg_problem_raw_dofs(const fg_problem *p, uint64_t *num_type, uint64_t *entity, uint64_t *num_dof, int32_t *assemble_type, float *xyz) {
+  if (!p) return FG_ERR_ARG;
+  const auto &dd = p->u->dofs;
+  size_t i = 0;
+  for (uint32_t id : dd.table.order()) {
+    const Dof &d = dd.pool[id];
+    if (num_type) num_type[i] = d.numType;
+    if (entity) entity[i] = d.entity;
+    if (num_dof) num_dof[i] = d.numDof;
+    if (assemble_type) assemble_type[i] = d.assembleType;
+    if (xyz)
+      for (int c = 0; c < 3; ++c) xyz[3 * i + c] = d.xyz[c];
+    ++i;
+  }
+  return FG_OK;
+}
+
+int fg_problem_created_dofs(const fg_problem *p, uint64_t *num_type, uint64_t *entity, int32_t *assemble_type, float *xyz) {
+  if (!p) return FG_ERR_ARG;
+  const auto &cr = p->form->created;
+  for (size_t i = 0; i < cr.size(); ++i) {
+    if (num_type) num_type[i] = cr[i].numType;
+    if (entity) entity[i] = cr[i].entity;
+    if (assemble_type) assemble_type[i] = cr[i].assembleType;
+    if (xyz)
+      for (int c = 0; c < 3; ++c) xyz[3 * i + c] = cr[i].xyz[c];
+  }
+  return FG_OK;
+}
+
+int64_t fg_problem_reserve_log(const fg_problem *p, uint64_t *at, uint64_t *arg, int64_t cap) {
+  if (!p) return -1;
+  const auto &log = p->form->reserveLog;
+  for (size_t i = 0; i < log.size() && (int64_t)i < cap; ++i) {
+    if (at) at[i] = log[i].first;
+    if (arg) arg[i] = log[i].second;
+  }
+  return (int64_t)log.size();
+}
+
+int fg_problem_bbox(const fg_problem *p, double *bbox) {
+  if (!p || !bbox) return FG_ERR_ARG;
+  std::memcpy(bbox, p->mesh.bbox, 6 * sizeof(double));
+  return FG_OK;
+}
+
+double fg_problem_pre_seconds(const fg_problem *p) { return p ? p->form->preSeconds : -1.0; }
+
+int fg_problem_assemble(fg_problem *p, int32_t precision, double *csr_values, double *rhs, void *stream) {
+  if (!p) return FG_ERR_ARG;
+  fg_mesh_desc m;
+  fg_rule_desc r;
+  fg_space_desc s;
+  fg_system_desc y;
+  p->form->descs(&m, &r, &s, &y);
+  if (!p->plan) {
+    int st = fg_plan_create(&m, &r, &s, &y, &p->plan);
+    if (st != FG_OK) return st;
+  }
+  const auto &t = p->form->termDescs;
+  const double *dir = p->form->nFixed ? p->form->dirichlet.data() : nullptr;
+  if (precision == 0) return fg_assemble_fp64(p->plan, t.data(), (int32_t)t.size(), 0.0, dir, csr_values, rhs, stream);
+  return fg_assemble_mixed(p->plan, t.data(), (int32_t)t.size(), 0.0, dir, csr_values, rhs, stream, nullptr);
+}
+
+}  // extern "C"

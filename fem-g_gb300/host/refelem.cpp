@@ -1,0 +1,260 @@
+#include "refelem.h"
+
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+
+#include "mesh.h"
+
+namespace femg {
+
+namespace {
+
+double factorial(int n) {
+  double f = 1.0;
+  for (int i = 2; i <= n; ++i) f *= i;
+  return f;
+}
+
+// Grundmann-Moller rule with index s on the n-simplex (n = 2, 3): degree 2s+1,
+// weights sum to the simplex volume 1/n!.
+QuadRule grundmannMoller(int n, int s) {
+  QuadRule r;
+  const int d = 2 * s + 1;
+  for (int i = 0; i <= s; ++i) {
+    const int rr = s - i;
+    const double D = d + n - 2 * i;
+    const double w = ((i % 2) ? -1.0 : 1.0) * std::ldexp(1.0, -2 * s) * std::pow(D, d) / (factorial(i) * factorial(d + n - i));
+    if (n == 2) {
+      for (int b1 = 0; b1 <= rr; ++b1)
+        for (int b2 = 0; b2 <= rr - b1; ++b2) {
+          r.points.push_back((2 * b1 + 1) / D);
+          r.points.push_back((2 * b2 + 1) / D);
+          r.points.push_back(0.0);
+          r.weights.push_back(w);
+        }
+    } else {
+      for (int b1 = 0; b1 <= rr; ++b1)
+        for (int b2 = 0; b2 <= rr - b1; ++b2)
+          for (int b3 = 0; b3 <= rr - b1 - b2; ++b3) {
+            r.points.push_back((2 * b1 + 1) / D);
+            r.points.push_back((2 * b2 + 1) / D);
+            r.points.push_back((2 * b3 + 1) / D);
+            r.weights.push_back(w);
+          }
+    }
+  }
+  r.nq = (int)r.weights.size();
+  return r;
+}
+
+QuadRule gaussLegendreLine(int npts) {
+  QuadRule r;
+  for (int i = 0; i < npts; ++i) {
+    double x = std::cos(M_PI * (i + 0.75) / (npts + 0.5));
+    for (int it = 0; it < 100; ++it) {
+      double p, dp;
+      legendre(npts, x, p, dp);
+      double dx = p / dp;
+      x -= dx;
+      if (std::fabs(dx) < 1e-16) break;
+    }
+    double p, dp;
+    legendre(npts, x, p, dp);
+    r.points.push_back(x);
+    r.points.push_back(0.0);
+    r.points.push_back(0.0);
+    r.weights.push_back(2.0 / ((1.0 - x * x) * dp * dp));
+  }
+  r.nq = npts;
+  return r;
+}
+
+struct VG {
+  double v;
+  double g[3];
+};
+
+inline VG mul(const VG &a, const VG &b) {
+  VG r;
+  r.v = a.v * b.v;
+  for (int c = 0; c < 3; ++c) r.g[c] = a.v * b.g[c] + b.v * a.g[c];
+  return r;
+}
+
+inline VG leg(int k, const VG &lo, const VG &hi) {
+  double p, dp;
+  legendre(k, hi.v - lo.v, p, dp);
+  VG r;
+  r.v = p;
+  for (int c = 0; c < 3; ++c) r.g[c] = dp * (hi.g[c] - lo.g[c]);
+  return r;
+}
+
+void barycentric(int dim, const double *uvw, VG *lam) {
+  for (int i = 0; i <= dim; ++i)
+    for (int c = 0; c < 3; ++c) lam[i].g[c] = 0.0;
+  if (dim == 1) {
+    lam[0].v = 0.5 * (1.0 - uvw[0]);
+    lam[1].v = 0.5 * (1.0 + uvw[0]);
+    lam[0].g[0] = -0.5;
+    lam[1].g[0] = 0.5;
+    return;
+  }
+  double s = 0.0;
+  for (int c = 0; c < dim; ++c) {
+    lam[c + 1].v = uvw[c];
+    lam[c + 1].g[c] = 1.0;
+    s += uvw[c];
+    lam[0].g[c] = -1.0;
+  }
+  lam[0].v = 1.0 - s;
+}
+
+const int kPerm3[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+
+}  // namespace
+
+void legendre(int k, double x, double &p, double &dp) {
+  double p0 = 1.0, p1 = x;
+  if (k == 0) {
+    p = 1.0;
+    dp = 0.0;
+    return;
+  }
+  for (int n = 1; n < k; ++n) {
+    double p2 = ((2 * n + 1) * x * p1 - n * p0) / (n + 1);
+    p0 = p1;
+    p1 = p2;
+  }
+  p = p1;
+  // derivative from (x^2-1) P_k' = k (x P_k - P_{k-1}); at |x| = 1 use k(k+1)/2 * x^(k+1)
+  if (std::fabs(std::fabs(x) - 1.0) < 1e-14)
+    dp = 0.5 * k * (k + 1) * ((x > 0 || (k % 2 == 1)) ? 1.0 : -1.0);
+  else
+    dp = k * (x * p1 - p0) / (x * x - 1.0);
+}
+
+QuadRule gaussRule(const std::string &integrationType, int elementType) {
+  if (integrationType.rfind("Gauss", 0) != 0) throw std::invalid_argument("unsupported integration type " + integrationType);
+  const int N = std::stoi(integrationType.substr(5));
+  const int dim = elementDim(elementType);
+  if (dim == 0) {
+    QuadRule r;
+    r.nq = 1;
+    r.points = {0, 0, 0};
+    r.weights = {1.0};
+    return r;
+  }
+  if (dim == 1) return gaussLegendreLine(std::max(1, (N + 2) / 2));
+  const int s = N <= 1 ? 0 : (N - 1 + 1) / 2;  // smallest s with 2s+1 >= N
+  return grundmannMoller(dim, s);
+}
+
+void lagrangeBasis(int type, const double *uvw, double *val, double *grad) {
+  const int dim = elementDim(type);
+  const int order = elementOrder(type);
+  const int nn = elementNodes(type);
+  for (int i = 0; i < nn * 3; ++i) grad[i] = 0.0;
+  if (dim == 0) {
+    val[0] = 1.0;
+    return;
+  }
+  VG lam[4];
+  barycentric(dim, uvw, lam);
+  const int nv = dim + 1;
+  if (order == 1) {
+    for (int i = 0; i < nv; ++i) {
+      val[i] = lam[i].v;
+      for (int c = 0; c < 3; ++c) grad[3 * i + c] = lam[i].g[c];
+    }
+    return;
+  }
+  for (int i = 0; i < nv; ++i) {
+    val[i] = lam[i].v * (2.0 * lam[i].v - 1.0);
+    for (int c = 0; c < 3; ++c) grad[3 * i + c] = (4.0 * lam[i].v - 1.0) * lam[i].g[c];
+  }
+  const auto &edges = simplexEdges(dim);
+  for (size_t e = 0; e < edges.size(); ++e) {
+    const VG &a = lam[edges[e][0]], &b = lam[edges[e][1]];
+    val[nv + e] = 4.0 * a.v * b.v;
+    for (int c = 0; c < 3; ++c) grad[3 * (nv + e) + c] = 4.0 * (a.v * b.g[c] + b.v * a.g[c]);
+  }
+}
+
+int hierarchicalCount(int dim, int p) {
+  if (dim == 2) return 3 + 3 * (p - 1) + (p - 1) * (p - 2) / 2;
+  if (dim == 3) return 4 + 6 * (p - 1) + 4 * ((p - 1) * (p - 2) / 2) + (p - 1) * (p - 2) * (p - 3) / 6;
+  throw std::invalid_argument("hierarchicalCount");
+}
+
+int hierarchicalOrientation(int dim, const int64_t *tags) {
+  const auto &edges = simplexEdges(dim);
+  int code = 0;
+  for (size_t e = 0; e < edges.size(); ++e)
+    if (tags[edges[e][0]] > tags[edges[e][1]]) code |= 1 << e;
+  if (dim == 3) {
+    int mult = 1 << edges.size();
+    for (auto &f : simplexFaces(3)) {
+      int digit = 0;
+      for (int q = 0; q < 6; ++q) {
+        const int *s = kPerm3[q];
+        if (tags[f[s[0]]] < tags[f[s[1]]] && tags[f[s[1]]] < tags[f[s[2]]]) {
+          digit = q;
+          break;
+        }
+      }
+      code += digit * mult;
+      mult *= 6;
+    }
+  }
+  return code;
+}
+
+void hierarchicalBasis(int dim, int p, int code, const double *uvw, double *val, double *grad) {
+  VG lam[4];
+  barycentric(dim, uvw, lam);
+  int idx = 0;
+  auto put = [&](const VG &f) {
+    val[idx] = f.v;
+    for (int c = 0; c < 3; ++c) grad[3 * idx + c] = f.g[c];
+    ++idx;
+  };
+  const int nv = dim + 1;
+  for (int i = 0; i < nv; ++i) put(lam[i]);
+  const auto &edges = simplexEdges(dim);
+  for (size_t e = 0; e < edges.size(); ++e) {
+    int a = edges[e][0], b = edges[e][1];
+    if ((code >> e) & 1) std::swap(a, b);
+    const VG ab = mul(lam[a], lam[b]);
+    for (int k = 0; k <= p - 2; ++k) put(mul(ab, leg(k, lam[a], lam[b])));
+  }
+  auto faceFns = [&](int s0, int s1, int s2) {
+    const VG abc = mul(mul(lam[s0], lam[s1]), lam[s2]);
+    for (int d = 0; d <= p - 3; ++d)
+      for (int i = d; i >= 0; --i) {
+        const int j = d - i;
+        put(mul(abc, mul(leg(i, lam[s0], lam[s1]), leg(j, lam[s1], lam[s2]))));
+      }
+  };
+  if (dim == 2) {
+    faceFns(0, 1, 2);
+    return;
+  }
+  int digits = code >> edges.size();
+  const auto &faces = simplexFaces(3);
+  for (size_t f = 0; f < faces.size(); ++f) {
+    const int *s = kPerm3[digits % 6];
+    digits /= 6;
+    faceFns(faces[f][s[0]], faces[f][s[1]], faces[f][s[2]]);
+  }
+  const VG abcd = mul(mul(lam[0], lam[1]), mul(lam[2], lam[3]));
+  for (int d = 0; d <= p - 4; ++d)
+    for (int i = d; i >= 0; --i)
+      for (int j = d - i; j >= 0; --j) {
+        const int k = d - i - j;
+        put(mul(abcd, mul(leg(i, lam[0], lam[1]), mul(leg(j, lam[1], lam[2]), leg(k, lam[2], lam[3])))));
+      }
+}
+
+}  // namespace femg

@@ -1,0 +1,51 @@
+// Reference-element data: quadrature rules, geometric (Lagrange) basis and the
+// hierarchical H1 basis with orientations.
+//
+// In the reference these come from gmsh:
+//  - quadrature: gmsh::model::mesh::getIntegrationPoints(type, "GaussN") via
+//    FunctionSpaceInterface::GetGaussInfo (src/field/FunctionSpaceInterface.cpp:470-481);
+//  - Lagrange basis: getBasisFunctions("Lagrange"/"GradLagrange")
+//    (src/field/FunctionSpaceLagrange.cpp:105-137);
+//  - hierarchical H1: getBasisFunctions("H1Legendre<p>"/"GradH1Legendre<p>")
+//    with per-element orientations (src/field/FunctionSpaceHierarchicalH1.cpp:83-109).
+// gmsh is absent, so the rules and bases below are written from the published
+// mathematics:
+//  - "GaussN" on a simplex is the Grundmann-Moller rule of odd degree
+//    2*ceil((N-1)/2)+1 >= N (A. Grundmann, H.M. Moller, SIAM J. Numer. Anal. 15,
+//    1978); on a line it is the Gauss-Legendre rule with ceil((N+1)/2) points;
+//  - the hierarchical basis is a Legendre-kernel family: vertex functions
+//    lambda_v, edge functions lambda_a lambda_b P_k(lambda_b - lambda_a), face
+//    and interior bubbles built the same way; edges and faces are oriented by
+//    the global node order so the basis is conforming across elements.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace femg {
+
+struct QuadRule {
+  int nq = 0;
+  std::vector<double> points;   // [nq][3] reference coordinates (u, v, w)
+  std::vector<double> weights;  // [nq]
+};
+
+// integrationType "GaussN" on an element type (gmsh codes)
+QuadRule gaussRule(const std::string &integrationType, int elementType);
+
+// Geometric Lagrange basis of an element type at a point: values [nn], reference
+// gradients [nn][3]
+void lagrangeBasis(int elementType, const double *uvw, double *val, double *grad);
+
+// Hierarchical H1 of order p on a simplex of dimension dim (2 or 3).
+int hierarchicalCount(int dim, int p);
+// Orientation code of an element from the global tags of its vertices: edge
+// reversal bits followed by base-6 face permutation digits (3D only).
+int hierarchicalOrientation(int dim, const int64_t *vertexTags);
+// Basis values [n] and reference gradients [n][3] for an orientation code.
+void hierarchicalBasis(int dim, int p, int orientationCode, const double *uvw, double *val, double *grad);
+
+// Legendre polynomial P_k and derivative
+void legendre(int k, double x, double &p, double &dp);
+
+}  // namespace femg

@@ -1,0 +1,232 @@
+/*
+ * fem-g GB300: C ABI of the GPU assembly path.
+ *
+ * The drop-in seam in the reference is the virtual
+ * gmshfem::problem::Formulation<T>::assemble (src/problem/Formulation.h:196-199,
+ * body src/problem/Formulation.cpp:1152-1215). A GPU formulation keeps the
+ * reference's own pre() (DOF dictionary, Hilbert numbering, CSR pattern) and
+ * replaces assemble() with the calls below:
+ *
+ *   fg_plan_create    replaces the per-bucket set-up of Formulation::_assembleDim
+ *                     (src/problem/Formulation.cpp:1418-1493) and
+ *                     Assembler::assemblyInitialization (src/term/Assembler.cpp:69-155):
+ *                     geometry, basis tables, element DOF map, element->nonzero map;
+ *   fg_assemble_fp64  replaces Assembler::assemble (src/term/Assembler.cpp:157-494):
+ *                     BilinearTerm::evaluate (src/term/BilinearTerm.cpp:304-343),
+ *                     LinearTerm::evaluate (src/term/LinearTerm.cpp:176-217),
+ *                     MatrixFactory::addValues (src/system/MatrixFactory.cpp:233-448),
+ *                     VectorFactory::addValues / addValuesDC
+ *                     (src/system/VectorFactory.cpp:122-210), in FP64;
+ *   fg_assemble_mixed same computation with FP64 geometry and a 3xTF32
+ *                     tensor-core element contraction accumulated in FP32;
+ *   fg_batch_*        many independent problems assembled in one persistent,
+ *                     graph-captured launch.
+ *
+ * Conventions: complex values are interleaved (re, im) doubles, the layout of
+ * std::complex<double>. CSR rows are test DOFs, columns unknown DOFs, as
+ * in MatrixFactory (row index = numDof-1 of the test function DOF). All calls
+ * return an FG_* status and never throw; fg_last_error() describes the last
+ * failure on the calling thread.
+ */
+#ifndef FEM_G_GB300_H
+#define FEM_G_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+enum {
+  FG_OK = 0,
+  FG_ERR_ARG = 1,         /* invalid argument or inconsistent descriptor */
+  FG_ERR_OOM = 2,         /* device or host allocation failed */
+  FG_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  FG_ERR_INDEX = 4,       /* an element DOF has no place in the CSR pattern */
+  FG_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  FG_ERR_UNSUPPORTED = 6, /* a term/space combination this build does not handle */
+  FG_ERR_NO_DEVICE = 7    /* no CUDA device */
+};
+
+/* DOF assemble types: same values as gmshfem::dofs::AssembleType (src/dofs/Dof.h:27-35) */
+enum {
+  FG_AT_UNDEFINED = 0,
+  FG_AT_FIXED = 1,
+  FG_AT_UNKNOWN = 2,
+  FG_AT_UNKNOWN_BUBBLE = 3,
+  FG_AT_UNKNOWN_GLOBAL = 4,
+  FG_AT_LINKED = 5,
+  FG_AT_LINKED_BUBBLE = 6
+};
+
+/* ---------------------------------------------------------------- inputs */
+
+/* One element bucket: the elements of one type on one entity (ElementBucket,
+ * src/problem/ElementBucket.h:20-43, built from gmsh nodes) */
+typedef struct {
+  int32_t dim;               /* topological dimension of the elements: 2 or 3 */
+  int32_t nodes_per_element; /* geometric nodes per element: 3, 6, 4 or 10 */
+  int64_t n_nodes;
+  const double *node_xyz;    /* [n_nodes][3] */
+  int64_t n_elements;
+  const int64_t *elem_nodes; /* [n_elements][nodes_per_element], 0-based */
+} fg_mesh_desc;
+
+/* Quadrature rule and the geometric basis on it (GetGaussInfo,
+ * src/field/FunctionSpaceInterface.cpp:470-481; gmsh getJacobians) */
+typedef struct {
+  int32_t nq;
+  const double *weights;  /* [nq] */
+  const double *geo_val;  /* [nq][nodes_per_element] */
+  const double *geo_grad; /* [nq][nodes_per_element][3] reference gradients */
+} fg_rule_desc;
+
+/* Function space on the bucket: reference basis per orientation, in the
+ * reference's layout bf[(o*nq + q)*ncomp*n + dof*ncomp + comp]
+ * (src/term/BilinearTerm.cpp:316) */
+typedef struct {
+  int32_t n_basis;      /* scalar basis functions per element */
+  int32_t multiplicity; /* 1 (Field) or 3 (CompoundField, DOF = basis*3 + component) */
+  int32_t n_orientations;
+  const double *basis_val;         /* [n_orientations][nq][n_basis] */
+  const double *basis_grad;        /* [n_orientations][nq][n_basis][3] */
+  const int32_t *elem_orientation; /* [n_elements] dense orientation, NULL if n_orientations == 1 */
+} fg_space_desc;
+
+/* Pattern and element DOF map produced by the reference's pre():
+ * MatrixFactory _ai/_aj (src/system/MatrixFactory.cpp:188-213) and the
+ * IndiceBucket of FieldInterface::fillIndices (src/field/FieldInterface.cpp:1012-1076) */
+typedef struct {
+  uint64_t n_rows;              /* unknown DOFs */
+  const uint64_t *ai;           /* [n_rows + 1] */
+  const uint64_t *aj;           /* [ai[n_rows]] */
+  const uint64_t *elem_dof_idx; /* [n_elements][n_basis*multiplicity]: numDof - 1 */
+  const int32_t *elem_dof_type; /* same shape: FG_AT_* */
+  uint64_t n_fixed;             /* fixed DOFs (size of the Dirichlet value array) */
+} fg_system_desc;
+
+/* Coefficient expression: a complex-valued program over the physical point
+ * (x, y, z) of a quadrature point and per-element arrays, in reverse Polish
+ * order. Mirrors the expression trees of src/function/ (ScalarFunction::evaluate,
+ * src/function/ScalarFunction.cpp:203-223) for the operators listed. */
+enum {
+  FG_OP_CONST = 0,     /* push (re, im) */
+  FG_OP_X = 1,         /* push x of the point */
+  FG_OP_Y = 2,
+  FG_OP_Z = 3,
+  FG_OP_ELEM = 4,      /* push elem_values[arg][element] */
+  FG_OP_ADD = 5,
+  FG_OP_SUB = 6,
+  FG_OP_MUL = 7,
+  FG_OP_DIV = 8,
+  FG_OP_NEG = 9,
+  FG_OP_HEAVISIDE = 10 /* 1 if Re>0, 0 if Re<0, 0.5 if Re==0 (unaryOperations.h:1008-1021) */
+};
+typedef struct {
+  int32_t op;
+  int32_t arg;
+  double re, im;
+} fg_instr;
+
+#define FG_EXPR_MAX_CODE 32
+#define FG_EXPR_MAX_ARRAYS 4
+typedef struct {
+  int32_t n_code;
+  fg_instr code[FG_EXPR_MAX_CODE];
+  int32_t n_arrays;
+  const double *elem_values[FG_EXPR_MAX_ARRAYS]; /* [n_elements][2] complex */
+} fg_expr;
+
+/* Terms of one formulation on the bucket (one field, one quadrature rule) */
+enum {
+  FG_TERM_GRAD_GRAD = 0, /* integral(c * grad(dof(u)), grad(tf(u))) */
+  FG_TERM_MASS = 1,      /* integral(c * dof(u), tf(u)) */
+  FG_TERM_ELASTIC = 2,   /* integral(C * grad(dof(u)), grad(tf(u))), C isotropic Tensor4 (lambda, mu) */
+  FG_TERM_SOURCE = 3     /* integral(f, tf(u)) : right-hand side */
+};
+enum { FG_DT_NONE = 0, FG_DT_1 = 1, FG_DT_2 = 2 }; /* dof, dt_dof, dt2_dof */
+
+typedef struct {
+  int32_t kind; /* FG_TERM_* */
+  int32_t dt;   /* FG_DT_*: with any dt term the AFrequency module applies */
+  fg_expr coef; /* c, f, or lambda for FG_TERM_ELASTIC */
+  fg_expr coef2; /* mu for FG_TERM_ELASTIC */
+} fg_term_desc;
+
+/* ------------------------------------------------------------- plan / run */
+
+typedef struct fg_plan fg_plan;
+
+/* Builds the device-resident plan for one element bucket: uploads geometry
+ * and basis tables, checks every element DOF against the pattern and builds
+ * the element->nonzero map used by the deterministic CSR reduction. */
+int fg_plan_create(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_space_desc *space,
+                   const fg_system_desc *sys, fg_plan **out);
+void fg_plan_destroy(fg_plan *plan);
+/* plan statistics: nnz, elements, element DOFs, quadrature points, orientations */
+int fg_plan_info(const fg_plan *plan, int64_t *nnz, int64_t *n_elements, int32_t *n_dofs, int32_t *nq, int32_t *n_orient);
+
+/* Error report of the mixed path (per element and global, against an FP64
+ * evaluation of the same element matrices on the device) */
+typedef struct {
+  double max_elem_rel_fro;  /* max over elements of ||Ke_mixed - Ke_fp64||_F / ||Ke_fp64||_F */
+  double mean_elem_rel_fro;
+  double global_rel_fro;    /* ||A_mixed - A_fp64||_F / ||A_fp64||_F over the CSR values */
+} fg_err_report;
+
+/* Upload the terms once (coefficient arrays copied to the device) so later
+ * assemble calls may pass terms == NULL and reuse them, like the reference's
+ * term initialisation (BilinearTerm::assemblyInitialization,
+ * src/term/BilinearTerm.cpp:156-273) followed by repeated assembly. */
+int fg_plan_bind_terms(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency);
+
+/* Assemble the system. csr_values ([nnz][2]) and rhs ([n_rows][2]) may be host
+ * or device pointers (detected); the values are overwritten (the reference
+ * adds into a zeroed module). dirichlet: [n_fixed][2] values of the fixed DOFs
+ * (may be NULL when n_fixed == 0). frequency: omega of the AFrequency module,
+ * used when a term has dt != 0. rhs may be NULL. stream: a cudaStream_t or NULL.
+ * terms == NULL uses the terms bound by fg_plan_bind_terms. With device
+ * outputs the call returns once the work is queued on the stream; with host
+ * outputs it returns after the results are copied back. */
+int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency,
+                     const double *dirichlet, double *csr_values, double *rhs, void *stream);
+/* Mixed precision: FP64 geometry, 3xTF32 tcgen05 contraction with FP32
+ * accumulation, FP64 CSR reduction. report may be NULL (no error report). */
+int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency,
+                      const double *dirichlet, double *csr_values, double *rhs, void *stream,
+                      fg_err_report *report);
+
+/* Several frequencies sharing K_e and M_e: values[f] = K - omega_f^2 * M
+ * assembled for n_freq frequencies in one pass (csr_values: [n_freq][nnz][2]). */
+int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, const double *omegas,
+                           int32_t n_freq, int32_t mixed, double *csr_values, void *stream);
+
+/* -------------------------------------------------------------- batching */
+
+typedef struct fg_batch fg_batch;
+/* A batch of independent plans assembled by one persistent kernel launch
+ * captured in a CUDA graph; tile shapes per (element type, order, rule) come
+ * from the built-in autotuner on the first run. */
+int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const *terms, const int32_t *n_terms,
+                    int32_t n_problems, int32_t mixed, fg_batch **out);
+/* values[p] / rhs[p]: device or host output arrays per problem (NULL rhs allowed) */
+int fg_batch_run(fg_batch *batch, double *const *csr_values, double *const *rhs, void *stream);
+void fg_batch_destroy(fg_batch *batch);
+
+/* ----------------------------------------------------------------- misc */
+
+const char *fg_last_error(void);
+/* number of kernel launches issued by this library since load (for the
+ * launch count a benchmark reports) */
+int64_t fg_launch_count(void);
+/* page-locked host buffers for end-to-end transfers */
+int fg_host_alloc(void **ptr, size_t bytes);
+void fg_host_free(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FEM_G_GB300_H */

@@ -1,0 +1,824 @@
+/*
+ * CPU oracle for the GmshFEM assembly path — TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's algorithms, used by the tests, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline legs as the checker.
+ * The product (libfemg.so) never links or calls this code.
+ *
+ * Each function cites the reference code it restates (paths inside the
+ * reference project GmshFEM 1.0.0, directory fem-master/).
+ *
+ * Parity pinning: the reference has no golden element matrices or CSR
+ * fixtures (its tests need gmsh + PETSc). The numbering pieces (robin-hood
+ * iteration order, Hilbert keys and sort) are pinned against the reference's
+ * own robin_hood.h and Hilbert.cpp compiled in oracle/_ref; the matrix
+ * pieces (evaluate, addValues, addValuesDC) are pinned against exact
+ * closed-form element matrices (P1 stiffness/mass) in the tests.
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef double complex cplx;
+
+/* ---------------------------------------------------------------- types */
+
+enum { AT_UNDEFINED = 0, AT_FIXED = 1, AT_UNKNOWN = 2, AT_UNKNOWN_BUBBLE = 3, AT_UNKNOWN_GLOBAL = 4 };
+enum { TERM_GRAD_GRAD = 0, TERM_MASS = 1, TERM_ELASTIC = 2, TERM_SOURCE = 3 };
+enum { OP_CONST = 0, OP_X, OP_Y, OP_Z, OP_ELEM, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_HEAVISIDE };
+
+/* same memory layout as fg_instr / fg_expr / fg_term_desc of the C ABI, so
+ * the tests can pass the product's term descriptors unchanged */
+typedef struct {
+  int32_t op, arg;
+  double re, im;
+} or_instr;
+typedef struct {
+  int32_t n_code;
+  or_instr code[32];
+  int32_t n_arrays;
+  const double *elem_values[4];
+} or_expr;
+typedef struct {
+  int32_t kind, dt;
+  or_expr coef, coef2;
+} or_term;
+
+typedef struct {
+  int dim, nn, nq, nb, mult;
+  int64_t E;
+  const double *xyz;      /* [nodes][3] */
+  const int64_t *enodes;  /* [E][nn] */
+  const double *w;        /* [nq] */
+  const double *geo_val;  /* [nq][nn] */
+  const double *geo_grad; /* [nq][nn][3] */
+  const double *bval;     /* [no][nq][nb] */
+  const double *bgrad;    /* [no][nq][nb][3] */
+  const int32_t *orient;  /* [E] (NULL: one table, Lagrange's isConstantByElements) */
+} or_bucket;
+
+/* -------------------------------------------------------- expressions */
+
+/* Function::evaluate for the operator subset of the ABI
+ * (src/function/ScalarFunction.cpp:203-223; nullary x/y/z/constant
+ * src/function/executionTree/nullaryOperations.h:284-345,1399-1484; heaviside
+ * src/function/executionTree/unaryOperations.h:1008-1021) */
+static cplx eval_expr(const or_expr *ex, int64_t e, const double *x) {
+  cplx st[16];
+  int sp = 0;
+  for (int k = 0; k < ex->n_code; ++k) {
+    const or_instr *in = &ex->code[k];
+    switch (in->op) {
+      case OP_CONST: st[sp++] = in->re + I * in->im; break;
+      case OP_X: st[sp++] = x[0]; break;
+      case OP_Y: st[sp++] = x[1]; break;
+      case OP_Z: st[sp++] = x[2]; break;
+      case OP_ELEM: st[sp++] = ex->elem_values[in->arg][2 * e] + I * ex->elem_values[in->arg][2 * e + 1]; break;
+      case OP_NEG: st[sp - 1] = -st[sp - 1]; break;
+      case OP_HEAVISIDE: {
+        double r = creal(st[sp - 1]);
+        st[sp - 1] = r > 0.0 ? 1.0 : (r < 0.0 ? 0.0 : 0.5);
+        break;
+      }
+      default: {
+        cplx b = st[--sp];
+        cplx a = st[sp - 1];
+        if (in->op == OP_ADD) a = a + b;
+        else if (in->op == OP_SUB) a = a - b;
+        else if (in->op == OP_MUL) a = a * b;
+        else a = a / b;
+        st[sp - 1] = a;
+      }
+    }
+  }
+  return st[0];
+}
+
+/* --------------------------------------------------------- geometry */
+
+/* gmsh getJacobians as consumed by the reference (src/term/Assembler.cpp:131-139,
+ * column-major 3x3 Map in src/term/evaluator/FieldEvaluator.h:69): J(r,c) =
+ * sum_k x_k[r] dN_k/du_c stored at J[3c + r]; 2D elements complete the third
+ * column with the unit normal. Returns det. */
+static double or_jacobian(const or_bucket *b, int64_t e, int q, double *J, double *xq) {
+  memset(J, 0, 9 * sizeof(double));
+  xq[0] = xq[1] = xq[2] = 0.0;
+  for (int k = 0; k < b->nn; ++k) {
+    const double *X = b->xyz + 3 * b->enodes[e * b->nn + k];
+    for (int c = 0; c < b->dim; ++c) {
+      double g = b->geo_grad[((size_t)q * b->nn + k) * 3 + c];
+      for (int r = 0; r < 3; ++r) J[3 * c + r] += X[r] * g;
+    }
+    double v = b->geo_val[(size_t)q * b->nn + k];
+    for (int r = 0; r < 3; ++r) xq[r] += v * X[r];
+  }
+  if (b->dim == 2) {
+    double nx = J[1] * J[5] - J[2] * J[4], ny = J[2] * J[3] - J[0] * J[5], nz = J[0] * J[4] - J[1] * J[3];
+    double l = sqrt(nx * nx + ny * ny + nz * nz);
+    J[6] = nx / l;
+    J[7] = ny / l;
+    J[8] = nz / l;
+  }
+#define M(r, c) J[3 * (c) + (r)]
+  return M(0, 0) * (M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1)) - M(0, 1) * (M(1, 0) * M(2, 2) - M(1, 2) * M(2, 0)) +
+         M(0, 2) * (M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0));
+#undef M
+}
+
+/* FieldEvaluator<Form1>: J^T.inverse() * bf (src/term/evaluator/FieldEvaluator.h:67-70);
+ * out G[3][nb] */
+static void or_form1(const double *J, const double *bf, int nb, double *G) {
+  /* K = J^T; Kinv = K^-1 by cofactors */
+  double K[3][3], Ki[3][3];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) K[r][c] = J[3 * r + c]; /* K(r,c) = J(c,r) */
+  double det = K[0][0] * (K[1][1] * K[2][2] - K[1][2] * K[2][1]) - K[0][1] * (K[1][0] * K[2][2] - K[1][2] * K[2][0]) +
+               K[0][2] * (K[1][0] * K[2][1] - K[1][1] * K[2][0]);
+  Ki[0][0] = (K[1][1] * K[2][2] - K[1][2] * K[2][1]) / det;
+  Ki[0][1] = (K[0][2] * K[2][1] - K[0][1] * K[2][2]) / det;
+  Ki[0][2] = (K[0][1] * K[1][2] - K[0][2] * K[1][1]) / det;
+  Ki[1][0] = (K[1][2] * K[2][0] - K[1][0] * K[2][2]) / det;
+  Ki[1][1] = (K[0][0] * K[2][2] - K[0][2] * K[2][0]) / det;
+  Ki[1][2] = (K[0][2] * K[1][0] - K[0][0] * K[1][2]) / det;
+  Ki[2][0] = (K[1][0] * K[2][1] - K[1][1] * K[2][0]) / det;
+  Ki[2][1] = (K[0][1] * K[2][0] - K[0][0] * K[2][1]) / det;
+  Ki[2][2] = (K[0][0] * K[1][1] - K[0][1] * K[1][0]) / det;
+  for (int d = 0; d < nb; ++d)
+    for (int r = 0; r < 3; ++r) G[r * nb + d] = Ki[r][0] * bf[3 * d] + Ki[r][1] * bf[3 * d + 1] + Ki[r][2] * bf[3 * d + 2];
+}
+
+/* -------------------------------------------------- element matrices */
+
+/* Element matrix of one element, A_e column-major (Eigen): Ae[j + i*n] = A_e(j, i)
+ * with j the unknown (lhs) index and i the test (rhs) index.
+ *   BilinearTerm::evaluate, Hermitian product (src/term/BilinearTerm.cpp:314-326):
+ *     A_e += w_q det_q * expressionLhs^T * conj(expressionRhs)
+ *   with expressionLhs = c(e,q) * field (EquationEvaluator Left scalar,
+ *   src/term/evaluator/EquationEvaluator.h:170-173), expressionRhs = field,
+ *   field = FieldEvaluator<Form0> (bf values) or <Form1> (J^-T grad bf);
+ *   the Tensor4 compound case (src/term/evaluator/EquationEvaluator.h:1222-1297,
+ *   CompoundFieldEvaluator<Form1,3> src/term/evaluator/FieldEvaluator.h:149-188)
+ *   for an isotropic C = lambda d_ij d_kl + mu (d_ik d_jl + d_il d_jk).
+ *   Module combination (src/term/Assembler.cpp:263-305): AModule adds every
+ *   term; AFrequency adds -w^2 * (dt2 terms) and -i w * (dt1 terms).
+ * Also the element right-hand side of LinearTerm::evaluate (Hermitian,
+ * src/term/LinearTerm.cpp:182-191): b_e += w det conj(phi) f(q). */
+static void or_element(const or_bucket *b, const or_term *terms, int nterms, double freq, int64_t e, cplx *Ae, cplx *be, cplx *tmp,
+                       double *G, double *phi, int bilinear) {
+  const int nb = b->nb, mult = b->mult, n = nb * mult, nq = b->nq;
+  const int o = b->orient ? b->orient[e] : 0;
+  int frequencyModule = 0;
+  for (int t = 0; t < nterms; ++t)
+    if (terms[t].dt) frequencyModule = 1;
+  for (int k = 0; k < n * n; ++k) Ae[k] = 0.0;
+  if (be)
+    for (int k = 0; k < n; ++k) be[k] = 0.0;
+  for (int t = 0; t < nterms; ++t) {
+    const or_term *T = &terms[t];
+    cplx *target = (frequencyModule && T->dt) ? tmp : Ae;
+    if (T->kind != TERM_SOURCE && !bilinear) continue;
+    if (T->kind == TERM_SOURCE) {
+      if (!be) continue;
+      for (int q = 0; q < nq; ++q) {
+        double J[9], xq[3];
+        double det = or_jacobian(b, e, q, J, xq);
+        cplx f = eval_expr(&T->coef, e, xq);
+        const double *bf = b->bval + ((size_t)o * nq + q) * nb;
+        for (int i = 0; i < nb; ++i)
+          for (int c = 0; c < mult; ++c) be[i * mult + c] += b->w[q] * det * conj(bf[i]) * f;
+      }
+      continue;
+    }
+    if (target == tmp)
+      for (int k = 0; k < n * n; ++k) tmp[k] = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      double J[9], xq[3];
+      double det = or_jacobian(b, e, q, J, xq);
+      const double wd = b->w[q] * det;
+      cplx c = eval_expr(&T->coef, e, xq);
+      if (T->kind == TERM_MASS) {
+        const double *bf = b->bval + ((size_t)o * nq + q) * nb;
+        for (int k = 0; k < nb; ++k) phi[k] = bf[k];
+        /* compound Form0: 3 x 3nb field, component c of dof i at row c */
+        for (int ii = 0; ii < n; ++ii)
+          for (int jj = 0; jj < n; ++jj) {
+            if (ii % mult != jj % mult) continue;
+            target[jj + ii * n] += wd * (c * phi[jj / mult]) * conj(phi[ii / mult]);
+          }
+      } else if (T->kind == TERM_GRAD_GRAD) {
+        or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
+        for (int ii = 0; ii < n; ++ii)
+          for (int jj = 0; jj < n; ++jj) {
+            if (ii % mult != jj % mult) continue;
+            const int i = ii / mult, j = jj / mult;
+            cplx s = 0.0;
+            for (int r = 0; r < 3; ++r) s += (c * G[r * nb + j]) * conj(G[r * nb + i]);
+            target[jj + ii * n] += wd * s;
+          }
+      } else if (T->kind == TERM_ELASTIC) {
+        /* (C : grad u) : grad v with grad u_{a,k} = d u_a / d x_k: for unknown
+         * DOF (j, beta) the field is the 3x3 matrix D with D[beta][k] = G[k][j];
+         * C : D = lambda tr(D) I + mu (D + D^T) */
+        cplx lam = c, mu = eval_expr(&T->coef2, e, xq);
+        or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
+        for (int ii = 0; ii < n; ++ii)
+          for (int jj = 0; jj < n; ++jj) {
+            const int i = ii / 3, al = ii % 3, j = jj / 3, be2 = jj % 3;
+            /* sum_{a,k} (C:Dj)[a][k] * Di[a][k], Di[a][k] = (a == al) G[k][i] */
+            cplx s = 0.0;
+            for (int k = 0; k < 3; ++k) {
+              /* (C:Dj)[al][k] = lambda tr(Dj) d(al,k) + mu (Dj[al][k] + Dj[k][al]) */
+              cplx trDj = G[be2 * nb + j];
+              cplx CD = (al == k ? lam * trDj : 0.0) + mu * ((al == be2 ? G[k * nb + j] : 0.0) + (k == be2 ? G[al * nb + j] : 0.0));
+              s += CD * G[k * nb + i];
+            }
+            target[jj + ii * n] += wd * s;
+          }
+      }
+    }
+    if (target == tmp) {
+      cplx factor = T->dt == 2 ? -freq * freq : -I * freq;
+      for (int k = 0; k < n * n; ++k) Ae[k] += factor * tmp[k];
+    }
+  }
+}
+
+/* Element matrices in the product's layout Ke[e][i][j] (i test, j unknown),
+ * for direct per-element comparison; be[e][i]. */
+int or_element_matrices(const or_bucket *b, const or_term *terms, int nterms, double freq, double *ke, double *be) {
+  const int n = b->nb * b->mult;
+#pragma omp parallel
+  {
+    cplx *Ae = malloc(sizeof(cplx) * n * n), *tmp = malloc(sizeof(cplx) * n * n), *bl = malloc(sizeof(cplx) * n);
+    double *G = malloc(sizeof(double) * 3 * b->nb), *phi = malloc(sizeof(double) * b->nb);
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < b->E; ++e) {
+      or_element(b, terms, nterms, freq, e, Ae, be ? bl : NULL, tmp, G, phi, 1);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          cplx v = Ae[j + i * n];
+          ke[2 * (((size_t)e * n + i) * n + j)] = creal(v);
+          ke[2 * (((size_t)e * n + i) * n + j) + 1] = cimag(v);
+        }
+      if (be)
+        for (int i = 0; i < n; ++i) {
+          be[2 * ((size_t)e * n + i)] = creal(bl[i]);
+          be[2 * ((size_t)e * n + i) + 1] = cimag(bl[i]);
+        }
+    }
+    free(Ae);
+    free(tmp);
+    free(bl);
+    free(G);
+    free(phi);
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------- scatter */
+
+static uint64_t lower_bound_u64(const uint64_t *a, uint64_t lo, uint64_t hi, uint64_t v) {
+  while (lo < hi) {
+    uint64_t mid = lo + (hi - lo) / 2;
+    if (a[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+static void atomic_add_c(double *p, cplx v) {
+#pragma omp atomic update
+  p[0] += creal(v);
+#pragma omp atomic update
+  p[1] += cimag(v);
+}
+
+/* Full assembly: Assembler::_assembleBilinear / _assembleLinear
+ * (src/term/Assembler.cpp:157-479) with
+ *   MatrixFactory::addValues (src/system/MatrixFactory.cpp:233-448): row =
+ *     test DOF, column = unknown DOF, values[i*n + j] = A_e(j, i), position by
+ *     std::lower_bound in the CSR row, Fixed columns flag the lifting;
+ *   VectorFactory::addValuesDC (src/system/VectorFactory.cpp:178-210):
+ *     b[row] += values[j*n + i] * valuesDC[fixed]  (note the transposed read);
+ *   VectorFactory::addValues (src/system/VectorFactory.cpp:122-145).
+ * values [nnz][2] and rhs [n_rows][2] are accumulated (zero them first). */
+int or_assemble(const or_bucket *b, const or_term *terms, int nterms, double freq, const uint64_t *ai, const uint64_t *aj,
+                const uint64_t *edof, const int32_t *etype, const double *dirichlet, double *values, double *rhs) {
+  const int n = b->nb * b->mult;
+  int hasSource = 0;
+  for (int t = 0; t < nterms; ++t)
+    if (terms[t].kind == TERM_SOURCE) hasSource = 1;
+  int err = 0;
+#pragma omp parallel
+  {
+    cplx *Ae = malloc(sizeof(cplx) * n * n), *tmp = malloc(sizeof(cplx) * n * n), *bl = malloc(sizeof(cplx) * n);
+    double *G = malloc(sizeof(double) * 3 * b->nb), *phi = malloc(sizeof(double) * b->nb);
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < b->E; ++e) {
+      /* _assembleBilinear: bilinear terms only */
+      or_element(b, terms, nterms, freq, e, Ae, NULL, tmp, G, phi, 1);
+      const uint64_t *idx = edof + (size_t)e * n;
+      const int32_t *typ = etype + (size_t)e * n;
+      int haveDC = 0;
+      for (int i = 0; i < n; ++i) {
+        const int ti = typ[i];
+        if (ti == AT_FIXED) {
+          haveDC = 1;
+          continue;
+        }
+        if (ti != AT_UNKNOWN && ti != AT_UNKNOWN_BUBBLE && ti != AT_UNKNOWN_GLOBAL) continue;
+        const uint64_t row = idx[i];
+        for (int j = 0; j < n; ++j) {
+          const int tj = typ[j];
+          if (tj == AT_FIXED) {
+            haveDC = 1;
+            continue;
+          }
+          if (tj != AT_UNKNOWN && tj != AT_UNKNOWN_BUBBLE && tj != AT_UNKNOWN_GLOBAL) continue;
+          const uint64_t pos = lower_bound_u64(aj, ai[row], ai[row + 1], idx[j]);
+          if (pos == ai[row + 1] || aj[pos] != idx[j]) {
+#pragma omp atomic write
+            err = 1;
+            continue;
+          }
+          atomic_add_c(values + 2 * pos, Ae[i * n + j]);
+        }
+      }
+      if (haveDC && rhs) {
+        for (int i = 0; i < n; ++i) {
+          if (typ[i] != AT_UNKNOWN && typ[i] != AT_UNKNOWN_BUBBLE && typ[i] != AT_UNKNOWN_GLOBAL) continue;
+          for (int j = 0; j < n; ++j)
+            if (typ[j] == AT_FIXED) {
+              cplx uD = dirichlet[2 * idx[j]] + I * dirichlet[2 * idx[j] + 1];
+              atomic_add_c(rhs + 2 * idx[i], Ae[j * n + i] * uD);
+            }
+        }
+      }
+    }
+    if (hasSource && rhs) {
+#pragma omp barrier
+#pragma omp for schedule(static)
+      for (int64_t e = 0; e < b->E; ++e) {
+        /* _assembleLinear: linear terms only */
+        or_element(b, terms, nterms, freq, e, Ae, bl, tmp, G, phi, 0);
+        const uint64_t *idx = edof + (size_t)e * n;
+        const int32_t *typ = etype + (size_t)e * n;
+        for (int i = 0; i < n; ++i)
+          if (typ[i] == AT_UNKNOWN || typ[i] == AT_UNKNOWN_BUBBLE || typ[i] == AT_UNKNOWN_GLOBAL) atomic_add_c(rhs + 2 * idx[i], bl[i]);
+      }
+    }
+    free(Ae);
+    free(tmp);
+    free(bl);
+    free(G);
+    free(phi);
+  }
+  return err;
+}
+
+/* --------------------------------------------------------------- pattern */
+
+/* MatrixFactory::addPattern (src/system/MatrixFactory.cpp:459-539) for a
+ * non-symmetric matrix, element by element in order (the reference builds
+ * rows under per-row locks; the resulting sorted sets do not depend on
+ * order), then finalizePattern (:188-213). Bubble rows of one element alias
+ * the first bubble row's column vector (:505-536).
+ * Output: ai [n_rows+1]; aj allocated here (free with or_free). */
+typedef struct {
+  uint64_t *v;
+  uint64_t n, cap;
+} u64vec;
+
+static void vec_insert_sorted(u64vec *r, uint64_t x) {
+  uint64_t pos = lower_bound_u64(r->v, 0, r->n, x);
+  if (pos < r->n && r->v[pos] == x) return;
+  if (r->n == r->cap) {
+    r->cap = r->cap ? 2 * r->cap : 16;
+    r->v = realloc(r->v, r->cap * sizeof(uint64_t));
+  }
+  memmove(r->v + pos + 1, r->v + pos, (r->n - pos) * sizeof(uint64_t));
+  r->v[pos] = x;
+  r->n++;
+}
+
+int or_pattern(int64_t E, int n, const uint64_t *edof, const int32_t *etype, uint64_t n_rows, uint64_t *ai, uint64_t **aj_out) {
+  u64vec *rows = calloc(n_rows, sizeof(u64vec));
+  int64_t *alias = malloc(n_rows * sizeof(int64_t));
+  for (uint64_t r = 0; r < n_rows; ++r) alias[r] = -1;
+  for (int64_t e = 0; e < E; ++e) {
+    const uint64_t *idx = edof + (size_t)e * n;
+    const int32_t *typ = etype + (size_t)e * n;
+    int64_t bubble = -1;
+    for (int i = 0; i < n; ++i) {
+      const int ti = typ[i];
+      if (ti != AT_UNKNOWN && ti != AT_UNKNOWN_GLOBAL && ti != AT_UNKNOWN_BUBBLE) continue;
+      const uint64_t Ir = idx[i];
+      if (ti == AT_UNKNOWN_BUBBLE) {
+        if (bubble >= 0) {
+          alias[Ir] = bubble;
+          continue;
+        }
+        bubble = (int64_t)Ir;
+      }
+      for (int j = 0; j < n; ++j) {
+        const int tj = typ[j];
+        if (tj != AT_UNKNOWN && tj != AT_UNKNOWN_GLOBAL && tj != AT_UNKNOWN_BUBBLE) continue;
+        vec_insert_sorted(&rows[Ir], idx[j]);
+      }
+    }
+  }
+  ai[0] = 0;
+  for (uint64_t r = 0; r < n_rows; ++r) ai[r + 1] = ai[r] + rows[alias[r] >= 0 ? alias[r] : (int64_t)r].n;
+  uint64_t *aj = malloc((ai[n_rows] ? ai[n_rows] : 1) * sizeof(uint64_t));
+  for (uint64_t r = 0; r < n_rows; ++r) {
+    const u64vec *src = &rows[alias[r] >= 0 ? alias[r] : (int64_t)r];
+    memcpy(aj + ai[r], src->v, src->n * sizeof(uint64_t));
+  }
+  for (uint64_t r = 0; r < n_rows; ++r) free(rows[r].v);
+  free(rows);
+  free(alias);
+  *aj_out = aj;
+  return 0;
+}
+
+void or_free(void *p) { free(p); }
+
+/* ----------------------------------------------------------- Hilbert */
+
+/* Hilbert<T_dim, T_N> (src/reorder/Hilbert.cpp:17-125 tables, :128-143 key,
+ * :174-288 apply): Gray-code state machine, key of the float coordinates
+ * scaled into 2^(bits-1) cells (unfused multiply-add, the x86 build's path
+ * without FP_FAST_FMAF), then a stable radix sort on the 64-bit key: top 11
+ * bits bucketed, then 7 byte passes inside each bucket. */
+typedef struct {
+  int dim, N;
+  uint8_t nextED[24][8];
+  uint8_t tiED[24][8];
+} or_hilbert_tables;
+
+static void or_hilbert_init(or_hilbert_tables *h, int dim) {
+  const int N = 1 << dim;
+  const unsigned mask = (~0u) ^ ((~0u) << dim);
+  uint8_t gray[8], tgc[8][3][8], inv[8], tinv[8][3][8], ee[8], dd[8], nE[8][3][8], nD[8][3][8];
+  h->dim = dim;
+  h->N = N;
+  for (int i = 0; i < N; ++i) gray[i] = (uint8_t)(i ^ (i >> 1));
+  for (int e = 0; e < N; ++e)
+    for (int d = 0; d < dim; ++d)
+      for (int i = 0; i < N; ++i) {
+        unsigned k = (unsigned)(i ^ e);
+        tgc[e][d][i] = (uint8_t)((k >> (d + 1)) | ((k << (dim - d - 1)) & mask));
+      }
+  inv[0] = 0;
+  for (int i = 1; i < N; ++i) {
+    inv[i] = (uint8_t)i;
+    for (int j = 1; j < dim; ++j) inv[i] ^= (uint8_t)(i >> j);
+  }
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < dim; ++j)
+      for (int k = 0; k < N; ++k) tinv[i][j][k] = inv[tgc[i][j][k]];
+  ee[0] = 0;
+  for (int i = 1; i < N; ++i) ee[i] = gray[2 * ((i - 1) / 2)];
+  dd[0] = 0;
+  for (int i = 1; i < N; ++i) {
+    if (i < N / 2) dd[i] = (i % 2 == 0) ? gray[i - 1] % dim : gray[i] % dim;
+    else dd[i] = dd[N - i - 1];
+  }
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < dim; ++j)
+      for (int k = 0; k < N; ++k) {
+        uint8_t l = ee[tinv[i][j][k]];
+        nE[i][j][k] = (uint8_t)(i ^ (((l << (j + 1)) & mask) | (l >> (dim - j - 1))));
+        nD[i][j][k] = (uint8_t)((j + dd[tinv[i][j][k]] + 1) % dim);
+      }
+  memset(h->nextED, 0, sizeof(h->nextED));
+  memset(h->tiED, 0, sizeof(h->tiED));
+  for (int i = 0; i < N * dim; ++i)
+    for (int j = 0; j < N; ++j) {
+      int e = i & (int)mask, d = i >> dim;
+      if (d >= dim) continue;
+      h->nextED[i][j] = (uint8_t)((nD[e][d][j] << dim) | nE[e][d][j]);
+      h->tiED[i][j] = tinv[e][d][j];
+    }
+}
+
+static uint64_t or_hilbert_index(const or_hilbert_tables *h, const uint32_t *el, int begBit) {
+  uint64_t key = 0;
+  uint8_t ed = 0;
+  for (int m = begBit; m >= 0; m--) {
+    uint8_t l = 0;
+    for (int n = h->dim - 1; n >= 0; n--) l ^= (uint8_t)(((el[n] >> m) & 0x1) << n);
+    key <<= h->dim;
+    key ^= h->tiED[ed][l];
+    ed = h->nextED[ed][l];
+  }
+  return key;
+}
+
+/* keys of n float points (dim 2 or 3) into out_keys */
+int or_hilbert_keys(int dim, int64_t n, const float *pts, const float *mn, const float *mx, uint64_t *out_keys) {
+  or_hilbert_tables h;
+  or_hilbert_init(&h, dim);
+  const unsigned nbrBits = (unsigned)floor(64.0 / dim);
+  const unsigned twoPow = 1u << (nbrBits - 1);
+  float scale[3], scaleMin[3];
+  for (int i = 0; i < dim; ++i) {
+    scale[i] = twoPow / (mx[i] - mn[i]);
+    scaleMin[i] = -mn[i] * scale[i];
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    uint32_t u[3];
+    for (int j = 0; j < dim; ++j) {
+      volatile float p = pts[i * dim + j] * scale[j];
+      u[j] = (uint32_t)(p + scaleMin[j]);
+    }
+    out_keys[i] = or_hilbert_index(&h, u, (int)nbrBits - 1);
+  }
+  return 0;
+}
+
+/* stable order of the keys: bucket by the top 11 bits, then 7 LSD byte passes
+ * (the radix sort of Hilbert::apply with one thread) */
+int or_hilbert_sort(int64_t n, const uint64_t *keys, uint32_t *perm) {
+  const int nb = 2048, shift = 64 - 11;
+  uint64_t *hist = calloc(nb + 1, sizeof(uint64_t));
+  uint32_t *a = malloc((n ? n : 1) * sizeof(uint32_t)), *c = malloc((n ? n : 1) * sizeof(uint32_t));
+  for (int64_t i = 0; i < n; ++i) hist[(keys[i] >> shift) + 1]++;
+  for (int b = 0; b < nb; ++b) hist[b + 1] += hist[b];
+  {
+    uint64_t *fill = malloc(nb * sizeof(uint64_t));
+    memcpy(fill, hist, nb * sizeof(uint64_t));
+    for (int64_t i = 0; i < n; ++i) c[fill[keys[i] >> shift]++] = (uint32_t)i;
+    free(fill);
+  }
+  uint64_t local[8 * 256];
+  for (int b = 0; b < nb; ++b) {
+    const uint64_t off = hist[b], cnt = hist[b + 1] - hist[b];
+    if (cnt == 0) continue;
+    uint32_t *src = c + off, *dst = a + off;
+    memset(local, 0, sizeof(local));
+    for (uint64_t j = 0; j < cnt; ++j)
+      for (int k = 0; k < 8; ++k) local[((keys[src[j]] >> (k * 8)) & 0xFF) + 256 * k]++;
+    uint64_t sum[8] = {0};
+    for (int j = 0; j < 256; ++j)
+      for (int k = 0; k < 8; ++k) {
+        uint64_t t = sum[k] + local[256 * k + j];
+        local[256 * k + j] = sum[k];
+        sum[k] = t;
+      }
+    for (int k = 0; k < 7; ++k) {
+      for (uint64_t j = 0; j < cnt; ++j) dst[local[((keys[src[j]] >> (k * 8)) & 0xFF) + 256 * k]++] = src[j];
+      uint32_t *t = src;
+      src = dst;
+      dst = t;
+    }
+    /* after 7 passes the sorted bucket sits in the buffer that started as the
+     * destination */
+    if (src != a + off) memcpy(a + off, src, cnt * sizeof(uint32_t));
+  }
+  memcpy(perm, a, n * sizeof(uint32_t));
+  free(hist);
+  free(a);
+  free(c);
+  return 0;
+}
+
+/* DofsManager::reorderWithHilbert(true) (src/dofs/DofsManager.cpp:118-241):
+ * DOFs given in dictionary iteration order (float coords, assemble types);
+ * unknown non-bubble DOFs get numDof 1.. in Hilbert order, bubbles last.
+ * num_dof is written for unknown DOFs only. */
+int or_reorder_hilbert(int dim, const double *bbox, int64_t n, const float *xyz, const int32_t *atype, uint64_t n_unknown,
+                       uint64_t n_bubble, uint64_t *num_dof) {
+  float mn[3], mx[3];
+  for (int c = 0; c < dim; ++c) {
+    mn[c] = (float)(bbox[c] - 0.000001 * fabs(bbox[c]));
+    mx[c] = (float)(bbox[3 + c] + 0.000001 * fabs(bbox[3 + c]));
+  }
+  for (int pass = 0; pass < 2; ++pass) {
+    const int want = pass == 0 ? AT_UNKNOWN : AT_UNKNOWN_BUBBLE;
+    int64_t cnt = 0;
+    for (int64_t i = 0; i < n; ++i)
+      if (atype[i] == want) ++cnt;
+    float *pts = malloc((cnt ? cnt : 1) * dim * sizeof(float));
+    int64_t *ids = malloc((cnt ? cnt : 1) * sizeof(int64_t));
+    uint64_t *keys = malloc((cnt ? cnt : 1) * sizeof(uint64_t));
+    uint32_t *perm = malloc((cnt ? cnt : 1) * sizeof(uint32_t));
+    int64_t k = 0;
+    for (int64_t i = 0; i < n; ++i)
+      if (atype[i] == want) {
+        for (int c = 0; c < dim; ++c) pts[k * dim + c] = xyz[3 * i + c];
+        ids[k++] = i;
+      }
+    or_hilbert_keys(dim, cnt, pts, mn, mx, keys);
+    or_hilbert_sort(cnt, keys, perm);
+    for (int64_t r = 0; r < cnt; ++r) num_dof[ids[perm[r]]] = pass == 0 ? (uint64_t)r + 1 : n_unknown - n_bubble + (uint64_t)r + 1;
+    free(pts);
+    free(ids);
+    free(keys);
+    free(perm);
+  }
+  return 0;
+}
+
+/* ----------------------------------------------------- robin-hood order */
+
+/* Slot order of robin_hood::unordered_map<Dof*, T> (vendored robin-hood
+ * 3.8.0: detail::Table doInsert, insert_move, shiftUp, increase_size,
+ * try_increase_info, reserve, iteration) keyed by Dof::hash
+ * (src/dofs/Dof.h:87-92). ops: a script of reserve(c) (op_kind 0, arg c) and
+ * insert(DOF arg) (op_kind 1) events; order_out receives the DOF ids in
+ * iteration order; returns the element count. */
+typedef struct {
+  uint32_t *keys;
+  uint64_t *hashes;
+  uint8_t *info;
+  size_t mask, num, maxAllowed;
+  uint32_t inc, shift;
+} or_rh;
+
+static uint64_t rh_rotr(uint64_t x, unsigned r) { return (x >> r) | (x << (64 - r)); }
+static uint64_t rh_mix(uint64_t x) {
+  uint64_t h1 = x * UINT64_C(0xA24BAED4963EE407);
+  uint64_t h2 = rh_rotr(x, 32) * UINT64_C(0x9FB21C651E98DF25);
+  return rh_rotr(h1 + h2, 32);
+}
+static size_t rh_max(size_t n) { return n * 80 / 100; }
+static size_t rh_buf(size_t n) { size_t m = rh_max(n); return n + (m < 0xFF ? m : 0xFF); }
+
+static void rh_init(or_rh *t, size_t maxElements) {
+  size_t nb = rh_buf(maxElements);
+  free(t->keys);
+  free(t->hashes);
+  free(t->info);
+  t->num = 0;
+  t->mask = maxElements - 1;
+  t->maxAllowed = rh_max(maxElements);
+  t->keys = calloc(nb, sizeof(uint32_t));
+  t->hashes = calloc(nb, sizeof(uint64_t));
+  t->info = calloc(nb + 8, 1);
+  t->info[nb] = 1;
+  t->inc = 32;
+  t->shift = 59;
+}
+
+static void rh_shift_up(or_rh *t, size_t start, size_t ins) {
+  for (size_t i = start; i != ins; --i) {
+    t->keys[i] = t->keys[i - 1];
+    t->hashes[i] = t->hashes[i - 1];
+  }
+  for (size_t i = start; i != ins; --i) {
+    t->info[i] = (uint8_t)(t->info[i - 1] + t->inc);
+    if (t->info[i] + t->inc > 0xFF) t->maxAllowed = 0;
+  }
+}
+
+static int rh_try_increase_info(or_rh *t) {
+  if (t->inc <= 2) return 0;
+  t->inc >>= 1;
+  ++t->shift;
+  size_t nb = rh_buf(t->mask + 1);
+  for (size_t i = 0; i < nb; i += 8)
+    for (size_t b = i; b < i + 8; ++b) t->info[b] >>= 1;
+  t->info[nb] = 1;
+  t->maxAllowed = rh_max(t->mask + 1);
+  return 1;
+}
+
+static void rh_insert_move(or_rh *t, uint32_t id, uint64_t hash) {
+  if (t->maxAllowed == 0) rh_try_increase_info(t);
+  uint64_t h = rh_mix(hash);
+  uint32_t info = t->inc + (uint32_t)(h >> t->shift);
+  size_t idx = (size_t)h & t->mask;
+  while (info <= t->info[idx]) {
+    ++idx;
+    info += t->inc;
+  }
+  size_t ins = idx;
+  uint8_t insInfo = (uint8_t)info;
+  if (insInfo + t->inc > 0xFF) t->maxAllowed = 0;
+  while (t->info[idx] != 0) {
+    ++idx;
+    info += t->inc;
+  }
+  if (idx != ins) rh_shift_up(t, idx, ins);
+  t->keys[ins] = id;
+  t->hashes[ins] = hash;
+  t->info[ins] = insInfo;
+  t->num++;
+}
+
+static void rh_rehash(or_rh *t, size_t nbk) {
+  size_t oldBuf = rh_buf(t->mask + 1);
+  uint32_t *ok = t->keys;
+  uint64_t *oh = t->hashes;
+  uint8_t *oi = t->info;
+  int had = ok != NULL;
+  t->keys = NULL;
+  t->hashes = NULL;
+  t->info = NULL;
+  rh_init(t, nbk);
+  if (had && oldBuf > 1)
+    for (size_t i = 0; i < oldBuf; ++i)
+      if (oi[i]) rh_insert_move(t, ok[i], oh[i]);
+  free(ok);
+  free(oh);
+  free(oi);
+}
+
+static void rh_increase(or_rh *t) {
+  if (t->keys == NULL) {
+    rh_init(t, 8);
+    return;
+  }
+  if (t->num < rh_max(t->mask + 1) && rh_try_increase_info(t)) return;
+  rh_rehash(t, (t->mask + 1) * 2);
+}
+
+static uint64_t dof_hash(uint64_t numType, uint64_t entity) {
+  uint64_t seed = entity + 0x9e3779b9ull;
+  seed ^= numType + 0x9e3779b9ull + (seed << 6) + (seed >> 2);
+  return seed;
+}
+
+int64_t or_robin_order(int64_t n_ops, const int32_t *op_kind, const uint64_t *op_arg, const uint64_t *num_type,
+                       const uint64_t *entity, uint32_t *order_out) {
+  or_rh t;
+  memset(&t, 0, sizeof(t));
+  static uint8_t dummy[8];
+  (void)dummy;
+  for (int64_t k = 0; k < n_ops; ++k) {
+    if (op_kind[k] == 0) {
+      size_t c = op_arg[k] > t.num ? op_arg[k] : t.num, ns = 8;
+      while (rh_max(ns) < c) ns *= 2;
+      rh_rehash(&t, ns);
+      continue;
+    }
+    const uint32_t id = (uint32_t)op_arg[k];
+    const uint64_t hsh = dof_hash(num_type[id], entity[id]);
+    for (;;) {
+      if (t.keys == NULL) {
+        rh_increase(&t);
+        continue;
+      }
+      uint64_t h = rh_mix(hsh);
+      uint32_t info = t.inc + (uint32_t)(h >> t.shift);
+      size_t idx = (size_t)h & t.mask;
+      while (info < t.info[idx]) {
+        ++idx;
+        info += t.inc;
+      }
+      int found = 0;
+      while (info == t.info[idx]) {
+        uint32_t o = t.keys[idx];
+        if (num_type[o] == num_type[id] && entity[o] == entity[id]) {
+          found = 1;
+          break;
+        }
+        ++idx;
+        info += t.inc;
+      }
+      if (found) break;
+      if (t.num >= t.maxAllowed) {
+        rh_increase(&t);
+        continue;
+      }
+      size_t ins = idx;
+      uint32_t insInfo = info;
+      if (insInfo + t.inc > 0xFF) t.maxAllowed = 0;
+      while (t.info[idx] != 0) {
+        ++idx;
+        info += t.inc;
+      }
+      if (idx != ins) rh_shift_up(&t, idx, ins);
+      t.keys[ins] = id;
+      t.hashes[ins] = hsh;
+      t.info[ins] = (uint8_t)insInfo;
+      t.num++;
+      break;
+    }
+  }
+  int64_t cnt = 0;
+  if (t.keys) {
+    size_t nb = rh_buf(t.mask + 1);
+    for (size_t i = 0; i < nb; ++i)
+      if (t.info[i]) order_out[cnt++] = t.keys[i];
+  }
+  free(t.keys);
+  free(t.hashes);
+  free(t.info);
+  return cnt;
+}
+
+int or_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
