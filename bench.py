@@ -1,0 +1,358 @@
+"""Benchmark of the GB300 assembly path (one JSON line on rank 0).
+
+Workload (default): the 3D Helmholtz system on the unit cube, 40^3 cubes x 6
+Kuhn tetrahedra = 384,000 tets, hierarchical H1 order 3 (20 DOFs per tet),
+Gauss6, k = 20, per-tet coefficient -k^2 (1 + 0.3 xi), xi ~ N(0,1): 84,640,201
+CSR nonzeros, 1,771,561 unknowns. Inputs are seeded synthetic data with the
+reference configuration's shapes.
+
+A step is one full assembly (every element matrix and vector, scatter into
+the CSR values and right-hand side) on inputs resident in HBM. The headline
+value is element matrices/s of the mixed-precision path (FP64 geometry,
+3xTF32 tensor-core contraction, FP64 CSR), with the plain FP64 path beside it
+and the relative Frobenius error between the two. The CSR output (1.35 GB)
+is larger than L2, so no flush is needed between steps.
+
+--impl reference times the reference algorithm on the host cores: the CPU
+oracle (a restatement of the reference's assemble; the reference itself does
+not build here: gmsh is absent), all threads, on a bounded sample of the
+same workload per step.
+
+Multi-GPU: every rank assembles its own replica of the workload (the path
+has no exchange step); value = all ranks' element matrices / max rank time.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "element matrices/s and CSR nnz/s: mixed vs FP64 GPU at <=1e-6 rel error, 1 GB300"
+
+
+def load_femg():
+    import __graft_entry__ as g
+    g.build()
+    return g._femg()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload_config(femg, name, m):
+    if name == "c3":
+        return femg.config_c3(m=m or 40), "helmholtz3d_tet_h1p3_%d3x6_gauss6_percell_coef" % (m or 40)
+    if name == "c2":
+        return femg.config_c2(m=m or 40), "helmholtz3d_tet_h1p3_%d3x6_gauss6_k20" % (m or 40)
+    if name == "c1":
+        return femg.config_c1(m=m or 64), "helmholtz2d_tri_p2_%d2x2_gauss4_k10_dirichlet" % (m or 64)
+    if name == "c5":
+        return femg.config_c5(m=m or 60), "navier3d_tet_h1p2x3_%d3x6_gauss4_lame" % (m or 60)
+    raise SystemExit("unknown workload " + name)
+
+
+def sub_arrays(a, S):
+    b = dict(a)
+    for k in ("enodes", "edof", "etype", "orient"):
+        b[k] = a[k][:S]
+    b["E"] = S
+    return b
+
+
+def cpu_rate(prob, a, target_s):
+    """Oracle assemble on the first S elements (all host threads): element
+    matrices/s. S grows until one run takes target_s seconds or covers the mesh."""
+    from oracle import oracle as O
+    t, nt = prob.terms()
+    S = min(2000, a["E"])
+    while True:
+        b = sub_arrays(a, S)
+        t0 = time.perf_counter()
+        O.assemble(b, t, nt)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or S >= a["E"]:
+            return S / dt, S, dt, O.num_threads()
+        S = int(min(a["E"], max(S * 2, S * target_s / max(dt, 1e-3) * 1.1)))
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    femg = load_femg()
+    cfg, wname = workload_config(femg, args.workload, args.m)
+    prob = femg.Problem(cfg)
+    a = prob.arrays()
+    from oracle import oracle as O
+    t, nt = prob.terms()
+    S = min(a["E"], args.ref_sample)
+    b = sub_arrays(a, S)
+    for _ in range(args.warmup):
+        O.assemble(b, t, nt)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.assemble(b, t, nt)
+        times.append(time.perf_counter() - t0)
+    ms = 1000.0 * float(np.mean(times))
+    rate = S / (ms / 1000.0)
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "element matrices/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "complex128", "data": "synthetic (seeded, reference configuration shapes)",
+            "config": {"workload": wname, "elements": int(a["E"]), "nnz": prob.nnz, "sample_elements": S},
+            "nnz_per_s": rate * prob.nnz / a["E"],
+            "cpu_baseline": {"value": rate, "unit": "element matrices/s", "cores": O.num_threads(), "kind": "port",
+                             "sample": "first %d of %d elements per step, oracle restatement of Formulation::assemble" % (S, a["E"])},
+            "e2e": {"value": rate, "unit": "element matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c3")
+    ap.add_argument("--m", type=int, default=0)
+    ap.add_argument("--ref-sample", type=int, default=60000)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    femg = load_femg()
+    cfg, wname = workload_config(femg, args.workload, args.m)
+    t0 = time.perf_counter()
+    prob = femg.Problem(cfg)
+    pre_s = prob.pre_seconds()
+    t1 = time.perf_counter()
+    plan = prob.plan()
+    plan_s = time.perf_counter() - t1
+    plan.bind_terms()
+    a_info = plan.info()
+    E, nnz, nrows = a_info["E"], a_info["nnz"], int(prob.sys.n_rows)
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+    dv = torch.empty(2 * nnz, dtype=torch.float64, device="cuda")
+    db = torch.empty(2 * nrows, dtype=torch.float64, device="cuda")
+    dv64 = torch.empty_like(dv)
+
+    precisions = ["mixed", "fp64"]
+    try:
+        plan.assemble("mixed", values=dv.data_ptr(), rhs=db.data_ptr(), bound=True, stream=sptr)
+    except femg.FgError as e:
+        if e.status != femg.FG_ERR_UNSUPPORTED:
+            raise
+        precisions = ["fp64"]
+
+    def step(prec, out):
+        plan.assemble(prec, values=out.data_ptr(), rhs=db.data_ptr(), bound=True, stream=sptr)
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+
+    def timed(prec, out, steps, profile=False):
+        for _ in range(args.warmup):
+            step(prec, out)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        if profile:
+            femg.profile_read()
+            femg.profile_enable(True)
+        l0 = femg.lib().fg_launch_count()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step(prec, out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        launches = femg.lib().fg_launch_count() - l0
+        prof = None
+        if profile:
+            femg.profile_enable(False)
+            prof = femg.profile_read()
+        barrier()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        if ws > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, launches, prof
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    head = precisions[0]
+    ms_head, launches, prof = timed(head, dv, args.steps, profile=True)
+    clk = clocks.stop()
+    fp64_steps = max(3, min(args.steps, 5)) if head == "mixed" else args.steps
+    ms_fp64 = ms_head if head == "fp64" else timed("fp64", dv64, fp64_steps)[0]
+    if head == "mixed":
+        step("fp64", dv64)
+        torch.cuda.synchronize()
+        vm = dv.view(torch.complex128) if hasattr(dv, "view") else dv
+        diff = torch.linalg.vector_norm(dv - dv64).item() / max(torch.linalg.vector_norm(dv64).item(), 1e-300)
+    else:
+        diff = 0.0
+
+    # end to end through the C ABI: host coefficient arrays and host (pinned) outputs
+    hv = torch.empty(2 * nnz, dtype=torch.float64, pin_memory=True)
+    hb = torch.empty(2 * nrows, dtype=torch.float64, pin_memory=True)
+    tt, nt = prob.terms()
+    h2d = 0
+    for k in range(nt):
+        for ex in (tt[k].coef, tt[k].coef2):
+            h2d += ex.n_arrays * E * 16
+    h2d += int(prob.sys.n_fixed) * 16
+    d2h = (nnz + nrows) * 16
+    L = femg.lib()
+    dptr = C.cast(prob.dir_ptr, C.c_void_p) if prob.sys.n_fixed else None
+    fn = L.fg_assemble_mixed if head == "mixed" else L.fg_assemble_fp64
+    extra = (None,) if head == "mixed" else ()
+
+    def e2e_step():
+        femg.check(fn(plan.ptr, tt, nt, 0.0, dptr, hv.data_ptr(), hb.data_ptr(), sptr, *extra))
+
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    w0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = 1000.0 * (time.perf_counter() - w0) / e2e_steps
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # roofline of the dominant kernel (algorithmic bytes of the fused minimum
+    # per launch / measured average launch time)
+    pk, pk_kind = peaks()
+    dom, (dcount, dms) = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 0.0))
+    n_el = plan.info()["n"]
+    nv_nodes = 4
+    coef_bytes = 16  # per-element complex coefficient
+    alg_bytes = E * (nv_nodes * 3 * 8 + nv_nodes * 4 + coef_bytes + n_el * n_el * 4) + nnz * 16 + nrows * 16
+    avg_ms = dms / max(dcount, 1)
+    achieved = alg_bytes / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
+    roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"], "traffic": None, "kernel": dom,
+            "kernel_avg_ms": avg_ms, "algorithmic_bytes": alg_bytes, "peak_source": pk_kind,
+            "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in (prof or {}).items()}}
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            a = prob.arrays()
+            rate, S, dt, cores = cpu_rate(prob, a, args.cpu_seconds)
+            cpu = {"value": rate, "unit": "element matrices/s", "cores": cores, "kind": "port",
+                   "sample": "first %d of %d elements, %.1f s, oracle restatement of Formulation::assemble" % (S, E, dt)}
+        value = ws * E / (ms_head / 1000.0)
+        line = {"metric": METRIC, "value": value, "unit": "element matrices/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_head, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "fp32-tf32x3/fp64" if head == "mixed" else "fp64",
+                "data": "synthetic (seeded, reference configuration shapes)",
+                "config": {"workload": wname, "elements": E, "nnz": nnz, "unknowns": nrows, "dofs_per_element": n_el,
+                           "quadrature_points": plan.info()["nq"], "precision": head, "l2": "CSR output larger than L2, no flush",
+                           "parallelism": "replicas" if ws > 1 else "single"},
+                "nnz_per_s": ws * nnz / (ms_head / 1000.0),
+                "fp64": {"value": ws * E / (ms_fp64 / 1000.0), "ms_per_step": ms_fp64, "nnz_per_s": ws * nnz / (ms_fp64 / 1000.0)},
+                "mixed_vs_fp64_rel_fro": diff,
+                "speedup_mixed_vs_fp64": ms_fp64 / ms_head,
+                "pre_seconds": pre_s, "plan_seconds": plan_s,
+                "e2e": {"value": ws * E / (e2e_ms / 1000.0), "unit": "element matrices/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -173,6 +173,7 @@ int launchElementFp64(fg_plan *plan, const DevTerms &terms, double *ke, double *
     if (cplx) k_element_fp64<M, true><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, terms, ke, be2); \
     else k_element_fp64<M, false><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, terms, ke, be2);  \
   } while (0)
+  ProfScope prof("k_element_fp64", s);
   if (perLane <= 1) FG_LAUNCH_ELEM(1);
   else if (perLane <= 8) FG_LAUNCH_ELEM(8);
   else if (perLane <= 20) FG_LAUNCH_ELEM(20);
@@ -271,6 +272,7 @@ int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, 
     FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                  \
     kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be2, uD, v2, r2, wpb);                      \
   } while (0)
+  ProfScope prof("k_gather", s);
   if (p.slotBytes == 1) {
     if (keIsFloat) {
       if (keComplex) FG_GATHER(uint8_t, true, float); else FG_GATHER(uint8_t, false, float);

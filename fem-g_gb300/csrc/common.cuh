@@ -14,6 +14,19 @@ namespace femg {
 void setLastError(const std::string &msg);
 void countLaunch(int n = 1);
 
+// Brackets one kernel launch with CUDA events on its stream while the kernel
+// timer (fg_profile_enable) is on; a no-op otherwise.
+class ProfScope {
+ public:
+  ProfScope(const char *name, cudaStream_t s);
+  ~ProfScope();
+
+ private:
+  const char *name_;
+  cudaStream_t s_;
+  cudaEvent_t a_ = nullptr, b_ = nullptr;
+};
+
 #define FG_CUDA(call)                                                                          \
   do {                                                                                         \
     cudaError_t _e = (call);                                                                   \

@@ -27,6 +27,33 @@ static std::atomic<int64_t> g_launches{0};
 void setLastError(const std::string &msg) { g_lastError = msg; }
 void countLaunch(int n) { g_launches += n; }
 
+namespace {
+struct ProfRecord {
+  std::string name;
+  cudaEvent_t a, b;
+};
+std::mutex g_profMutex;
+std::vector<ProfRecord> g_prof;
+std::atomic<bool> g_profOn{false};
+}  // namespace
+
+ProfScope::ProfScope(const char *name, cudaStream_t s) : name_(name), s_(s) {
+  if (!g_profOn.load()) return;
+  if (cudaEventCreate(&a_) != cudaSuccess || cudaEventCreate(&b_) != cudaSuccess) {
+    a_ = b_ = nullptr;
+    cudaGetLastError();
+    return;
+  }
+  cudaEventRecord(a_, s_);
+}
+
+ProfScope::~ProfScope() {
+  if (!a_) return;
+  cudaEventRecord(b_, s_);
+  std::lock_guard<std::mutex> lk(g_profMutex);
+  g_prof.push_back({name_, a_, b_});
+}
+
 int ensureDevice(void **ptr, size_t *cap, size_t bytes) {
   if (bytes <= *cap && *ptr) return FG_OK;
   if (*ptr) cudaFree(*ptr);
@@ -503,6 +530,50 @@ int fg_plan_bind_terms(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms
   int st = uploadTerms(plan, terms, n_terms, frequency, &plan->bound, plan->boundArrays);
   if (st == FG_OK) plan->hasBound = true;
   return st;
+}
+
+int fg_profile_enable(int on) {
+  g_profOn = on != 0;
+  return FG_OK;
+}
+
+int fg_profile_read(char *names, int32_t name_bytes, int64_t *launches, double *total_ms, int32_t cap) {
+  std::vector<ProfRecord> recs;
+  {
+    std::lock_guard<std::mutex> lk(g_profMutex);
+    recs.swap(g_prof);
+  }
+  std::vector<std::string> order;
+  std::vector<int64_t> cnt;
+  std::vector<double> ms;
+  for (auto &r : recs) {
+    float t = 0.0f;
+    cudaEventSynchronize(r.b);
+    cudaEventElapsedTime(&t, r.a, r.b);
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+    size_t k = 0;
+    while (k < order.size() && order[k] != r.name) ++k;
+    if (k == order.size()) {
+      order.push_back(r.name);
+      cnt.push_back(0);
+      ms.push_back(0.0);
+    }
+    cnt[k]++;
+    ms[k] += t;
+  }
+  cudaGetLastError();
+  std::string joined;
+  for (size_t k = 0; k < order.size() && (int32_t)k < cap; ++k) {
+    if (launches) launches[k] = cnt[k];
+    if (total_ms) total_ms[k] = ms[k];
+    joined += order[k] + "\n";
+  }
+  if (names && name_bytes > 0) {
+    std::strncpy(names, joined.c_str(), (size_t)name_bytes - 1);
+    names[name_bytes - 1] = 0;
+  }
+  return (int)order.size();
 }
 
 const char *fg_last_error(void) { return g_lastError.c_str(); }

@@ -97,6 +97,8 @@ def lib():
         "fg_batch_create": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.POINTER(P)]),
         "fg_batch_run": (C.c_int, [P, P, P, P]),
         "fg_batch_destroy": (None, [P]),
+        "fg_profile_enable": (C.c_int, [C.c_int]),
+        "fg_profile_read": (C.c_int, [C.c_char_p, C.c_int32, P, P, C.c_int32]),
         "fg_last_error": (C.c_char_p, []),
         "fg_launch_count": (C.c_int64, []),
         "fg_host_alloc": (C.c_int, [C.POINTER(P), C.c_size_t]),
@@ -125,10 +127,25 @@ def exported_symbols():
     """Names bound above (the C ABI of both headers)."""
     return [
         "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_assemble_fp64", "fg_assemble_mixed",
-        "fg_assemble_multi_freq", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_last_error", "fg_launch_count",
+        "fg_assemble_multi_freq", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_profile_enable",
+        "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
         "fg_problem_raw_dofs", "fg_problem_created_dofs", "fg_problem_reserve_log", "fg_problem_bbox", "fg_problem_pre_seconds", "fg_problem_assemble",
     ]
+
+
+def profile_enable(on=True):
+    lib().fg_profile_enable(1 if on else 0)
+
+
+def profile_read():
+    """{kernel name: (launches, total device ms)} since the last read."""
+    buf = C.create_string_buffer(4096)
+    cnt = np.zeros(64, np.int64)
+    ms = np.zeros(64, np.float64)
+    k = lib().fg_profile_read(buf, 4096, cnt.ctypes.data, ms.ctypes.data, 64)
+    names = buf.value.decode().split("\n")[:k]
+    return {n: (int(cnt[i]), float(ms[i])) for i, n in enumerate(names)}
 
 
 def check(status):

@@ -221,6 +221,14 @@ const char *fg_last_error(void);
 /* number of kernel launches issued by this library since load (for the
  * launch count a benchmark reports) */
 int64_t fg_launch_count(void);
+/* Kernel timer: while enabled, every kernel this library launches is
+ * bracketed by CUDA events on its launch stream. fg_profile_read synchronizes
+ * the recorded events and returns, per kernel name, the launch count and the
+ * summed device milliseconds (names separated by '\n' in names[name_bytes]);
+ * it returns the number of kernels and clears the record. */
+int fg_profile_enable(int on);
+int fg_profile_read(char *names, int32_t name_bytes, int64_t *launches, double *total_ms, int32_t cap);
+
 /* page-locked host buffers for end-to-end transfers */
 int fg_host_alloc(void **ptr, size_t bytes);
 void fg_host_free(void *ptr);
