@@ -292,12 +292,6 @@ int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, 
   return FG_OK;
 }
 
-// outputs: device pointers used in place, host pointers staged through the plan
-struct Outputs {
-  double *values = nullptr, *rhs = nullptr;
-  bool hostValues = false, hostRhs = false;
-};
-
 int prepareOutputs(fg_plan *plan, double *csr_values, double *rhs, Outputs *o) {
   if (!csr_values) {
     setLastError("csr_values must not be NULL");

@@ -1,13 +1,658 @@
-// Mixed-precision assembly (placeholder until the tcgen05 contraction lands).
+// Mixed-precision assembly: FP64 geometry, 3xTF32 tensor-core contraction
+// (tcgen05, accumulators in TMEM), FP32 element matrices, FP64 CSR.
+//
+// The element contraction of BilinearTerm::evaluate (src/term/BilinearTerm.cpp:304-343)
+//     Ke[i][j] = sum_q w_q det_q c (J_q^-T grad phi_j) . (J_q^-T grad phi_i) + c_m phi_j phi_i
+// is refactored for affine elements with per-element coefficients into a
+// product of a per-element factor row and a constant per-orientation tensor:
+//     Ke[i][j] = sum_k D_e[k] T^o[k][i*n + j],
+//     D_e = c det (K_00, K_11, K_22, K_01, K_02, K_12, c_m/c, 0),  K = J^-1 J^-T,
+//     T^o[ab][ij] = sum_q w_q (d_a phi_j d_b phi_i + [a != b] d_b phi_j d_a phi_i),
+//     T^o[6][ij]  = sum_q w_q phi_i phi_j       (orientation o's reference basis).
+// Over all elements that is one GEMM C[M = elements, N = n^2] = A[M, K] B[K, N]
+// with B shared by every element of an orientation: the tensor-core shape.
+// 3xTF32: A = A_hi + A_lo, B = B_hi + B_lo (each part exactly representable
+// in TF32), C = A_hi B_hi + A_lo B_hi + A_hi B_lo, realised as one MMA chain
+// over K' = 3K with A' = [A_hi | A_lo | A_hi] and B' = [B_hi ; B_hi ; B_lo].
+// Geometry (J, det, J^-1) and the factors are computed in FP64; the element
+// matrices leave TMEM as FP32 and are reduced into the FP64 CSR by the same
+// deterministic gather as the FP64 path.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
 #include "common.cuh"
 
-extern "C" void mixedDestroy(fg_plan *plan) { (void)plan; }
+namespace femg {
 
-extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency,
-                                 const double *dirichlet, double *csr_values, double *rhs, void *stream, fg_err_report *report) {
-  (void)plan; (void)terms; (void)n_terms; (void)frequency; (void)dirichlet; (void)csr_values; (void)rhs; (void)stream; (void)report;
-  femg::setLastError("fg_assemble_mixed: not built yet");
-  return FG_ERR_UNSUPPORTED;
+constexpr int kBM = 128;       // rows (element components) per tile = TMEM lanes
+constexpr int kKp = 8;         // factor columns (7 used)
+constexpr int kK3 = 3 * kKp;   // K' of the 3xTF32 chain
+constexpr int kTmemCols = 512;
+constexpr int kThreadsGemm = 128;
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s bound on any device-side wait
+
+struct MixedState {
+  int built = 0;
+  int complexKe = -1;
+  int n = 0, nn2 = 0, Npad = 0;
+  int nOrient = 0;
+  int64_t rows = 0;          // GEMM rows = E * ncomp
+  float *A = nullptr;        // [rows][kK3] row-major split factors
+  size_t Abytes = 0;
+  float *B = nullptr;        // [nOrient] smem images of B' (core-matrix layout)
+  int32_t *perm = nullptr;   // sorted rank -> element
+  int32_t *tiles = nullptr;  // [nTiles][3]: orientation, first row, row count
+  int nTiles = 0;
+  float *ke = nullptr;       // [E][ncomp][n][n] fp32
+  size_t keBytes = 0;
+  int *err = nullptr;        // device error word (wait timeouts)
+};
+
+// ------------------------------------------------------------ TF32 split
+
+// round-to-nearest (ties away from zero) of an fp32 value to TF32 (10 mantissa bits)
+__host__ __device__ inline float tf32Round(float x) {
+  uint32_t b;
+  memcpy(&b, &x, 4);
+  if ((b & 0x7F800000u) == 0x7F800000u) return x;  // inf / nan
+  b = (b + 0x1000u) & 0xFFFFE000u;
+  float r;
+  memcpy(&r, &b, 4);
+  return r;
+}
+
+__host__ __device__ inline void splitTf32(double x, float &hi, float &lo) {
+  hi = tf32Round((float)x);
+  lo = tf32Round((float)(x - (double)hi));
+}
+
+// ------------------------------------------------------- PTX primitives
+
+__device__ inline uint32_t smemAddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: K-major, no swizzle, 8x16B core matrices
+__device__ inline uint64_t smemDesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+  return d;               // base offset 0, relative LBO, SWIZZLE_NONE
+}
+
+// instruction descriptor: kind::tf32, D fp32, A/B tf32 K-major, M x N
+__device__ inline uint32_t idescTf32(int M, int N) {
+  uint32_t d = 0;
+  d |= 1u << 4;                       // D format F32
+  d |= 2u << 7;                       // A format TF32
+  d |= 2u << 10;                      // B format TF32
+  d |= (uint32_t)(N >> 3) << 17;
+  d |= (uint32_t)(M >> 4) << 24;
+  return d;
+}
+
+__device__ inline void tmemAlloc(uint32_t *dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(dst)), "r"(ncols) : "memory");
+}
+__device__ inline void tmemRelinquish() { asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory"); }
+__device__ inline void tmemDealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ inline void mmaTf32(uint32_t dTmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dTmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ inline void mmaCommit(uint64_t *mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smemAddr(mbar)) : "memory");
+}
+__device__ inline void tcFenceBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ inline void tcFenceAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ inline void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ inline void mbarInit(uint64_t *mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(mbar)), "r"(count) : "memory");
+}
+__device__ inline void fenceMbarInit() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ inline bool mbarTryWait(uint64_t *mbar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smemAddr(mbar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; false on timeout
+__device__ inline bool mbarWait(uint64_t *mbar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbarTryWait(mbar, parity))
+    if (clock64() - t0 > kWaitCycles) return false;
+  return true;
+}
+__device__ inline void tmemLoad16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+        "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// ------------------------------------------------- geometry: factor rows
+
+// One thread per element: J, det, J^-1 in FP64 from the vertex nodes (affine
+// elements: the geometric Jacobian is constant), per-element coefficients,
+// factors D_e split into TF32 hi/lo, written as row [hi | lo | hi] at the
+// element's rank in the orientation-sorted order.
+__global__ void k_factors(const PlanDev p, const DevTerms terms, const int32_t *__restrict__ rankOf, float *__restrict__ A,
+                          int ncomp) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.E) return;
+  double X[kMaxNodes * 3];
+  for (int k = 0; k < p.nn; ++k)
+    for (int c = 0; c < 3; ++c) X[3 * k + c] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + k] + c];
+  double J[9], Ji[9];
+  const double det = jacobian(p.dim, p.nn, X, p.geoGrad, J);  // q = 0: affine
+  jacobianInverse(J, det, Ji);
+  double K[6];
+  const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  for (int k = 0; k < 6; ++k) {
+    const int a = ab[k][0], b = ab[k][1];
+    K[k] = Ji[3 * a] * Ji[3 * b] + Ji[3 * a + 1] * Ji[3 * b + 1] + Ji[3 * a + 2] * Ji[3 * b + 2];
+  }
+  double xc[3] = {0.0, 0.0, 0.0};  // coefficients are per element here: any point of it
+  double2 cgg = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0);
+  for (int t = 0; t < terms.n; ++t) {
+    const DevTerm &T = terms.t[t];
+    if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, evalExpr(T.coef, e, xc)));
+    else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xc)));
+  }
+  const int64_t r0 = (int64_t)rankOf[e] * ncomp;
+  for (int comp = 0; comp < ncomp; ++comp) {
+    const double g = (comp == 0 ? cgg.x : cgg.y) * det;
+    const double m = (comp == 0 ? cm.x : cm.y) * det;
+    double d[kKp];
+    for (int k = 0; k < 6; ++k) d[k] = g * K[k];
+    d[6] = m;
+    d[7] = 0.0;
+    float *row = A + (r0 + comp) * kK3;
+    for (int k = 0; k < kKp; ++k) {
+      float hi, lo;
+      splitTf32(d[k], hi, lo);
+      row[k] = hi;
+      row[kKp + k] = lo;
+      row[2 * kKp + k] = hi;
+    }
+  }
+}
+
+// --------------------------------------------------- tcgen05 contraction
+
+struct GemmArgs {
+  const float *A;       // [rows][kK3]
+  const float *B;       // [nOrient][Npad * kK3] core-matrix images
+  const int32_t *tiles; // [nTiles][3]
+  const int32_t *perm;  // rank -> element
+  float *ke;            // [E][ncomp][nn2]
+  int *err;
+  int nTiles, Npad, nn2, ncomp;
+};
+
+// Persistent: one CTA per SM, 4 warps; warp 0 owns the TMEM allocation,
+// thread 0 issues the MMAs, all 128 threads drain TMEM (thread = tile row).
+__global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmArgs g) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  float *Bs = reinterpret_cast<float *>(smem);                       // Npad * kK3
+  float *As = Bs + (size_t)g.Npad * kK3;                             // kBM * kK3
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(As + kBM * kK3);
+  uint32_t *tmemBase = reinterpret_cast<uint32_t *>(mbar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 0) {
+    tmemAlloc(tmemBase, kTmemCols);
+    tmemRelinquish();
+  }
+  if (tid == 0) {
+    mbarInit(mbar, 1);
+    fenceMbarInit();
+  }
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  const uint32_t tmem = *tmemBase;
+  const uint32_t aBase = smemAddr(As), bBase = smemAddr(Bs);
+  const uint32_t bLbo = (uint32_t)g.Npad * 16u;  // K-adjacent core matrices of B
+  int loadedOrient = -1;
+  uint32_t phase = 0;
+  bool failed = false;
+
+  for (int t = blockIdx.x; t < g.nTiles && !failed; t += gridDim.x) {
+    const int o = g.tiles[3 * t], row0 = g.tiles[3 * t + 1], nrows = g.tiles[3 * t + 2];
+    if (o != loadedOrient) {
+      // B' image of orientation o (already in core-matrix order)
+      const float4 *src = reinterpret_cast<const float4 *>(g.B + (size_t)o * g.Npad * kK3);
+      float4 *dst = reinterpret_cast<float4 *>(Bs);
+      for (int k = tid; k < g.Npad * kK3 / 4; k += kThreadsGemm) dst[k] = src[k];
+      loadedOrient = o;
+    }
+    // A tile: row r, 16-byte chunk kc -> core matrix (r/8, kc), K-direction stride 2048 B
+    for (int c = tid; c < kBM * (kK3 / 4); c += kThreadsGemm) {
+      const int r = c / (kK3 / 4), kc = c % (kK3 / 4);
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r < nrows) v = reinterpret_cast<const float4 *>(g.A + (size_t)(row0 + r) * kK3)[kc];
+      *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(As) + kc * 2048 + (r >> 3) * 128 + (r & 7) * 16) = v;
+    }
+    fenceProxyAsync();
+    __syncthreads();
+    if (tid == 0) {
+      tcFenceAfter();
+      for (int n0 = 0, chunk = 0; n0 < g.Npad; n0 += 256, ++chunk) {
+        const int nc = min(256, g.Npad - n0);
+        const uint32_t idesc = idescTf32(kBM, nc);
+        for (int ks = 0; ks < kK3 / 8; ++ks) {
+          const uint64_t ad = smemDesc(aBase + ks * 2 * 2048, 2048, 128);
+          const uint64_t bd = smemDesc(bBase + ks * 2 * bLbo + (n0 >> 3) * 128, bLbo, 128);
+          mmaTf32(tmem + (uint32_t)n0, ad, bd, idesc, ks > 0 ? 1u : 0u);
+        }
+      }
+      mmaCommit(mbar);
+    }
+    __syncwarp();
+    const bool ok = mbarWait(mbar, phase);
+    failed = __syncthreads_or(ok ? 0 : 1) != 0;  // block-uniform
+    if (failed) {
+      if (tid == 0) atomicExch(g.err, 1);
+    } else {
+      phase ^= 1u;
+    }
+    tcFenceAfter();
+    if (!failed) {
+      // epilogue: TMEM lane = tile row; warp w reads lanes [32w, 32w+32)
+      const int r = warp * 32 + lane;
+      const bool live = r < nrows;
+      const int grow = row0 + r;
+      const int64_t e = live ? g.perm[grow / g.ncomp] : 0;
+      float *out = g.ke + ((size_t)e * g.ncomp + (grow % g.ncomp)) * g.nn2;
+      for (int c0 = 0; c0 < g.Npad; c0 += 16) {
+        float v[16];
+        tmemLoad16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        if (live) {
+          if (c0 + 16 <= g.nn2 && ((g.nn2 & 3) == 0)) {
+#pragma unroll
+            for (int k = 0; k < 16; k += 4) *reinterpret_cast<float4 *>(out + c0 + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+          } else {
+            for (int k = 0; k < 16; ++k)
+              if (c0 + k < g.nn2) out[c0 + k] = v[k];
+          }
+        }
+      }
+    }
+    tcFenceBefore();
+    __syncthreads();
+  }
+  if (failed) {
+    // give the in-flight MMA chain a second bounded chance to retire (same
+    // completion parity) before the TMEM is freed
+    mbarWait(mbar, phase);
+  }
+  __syncthreads();
+  tcFenceAfter();
+  if (warp == 0) tmemDealloc(tmem, kTmemCols);
+}
+
+// ---------------------------------------------------- FP64 RHS (mixed)
+
+// b_e[i] = sum_q w det conj(phi_i) f(x_q)  (LinearTerm::evaluate), warp per element
+__global__ void k_rhs_fp64(const PlanDev p, const DevTerms terms, double2 *__restrict__ be) {
+  const int lane = threadIdx.x & 31;
+  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (e >= p.E) return;
+  const int o = p.orient ? p.orient[e] : 0;
+  double X[kMaxNodes * 3];
+  for (int k = 0; k < p.nn; ++k)
+    for (int c = 0; c < 3; ++c) X[3 * k + c] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + k] + c];
+  double2 acc[2] = {make_double2(0, 0), make_double2(0, 0)};
+  for (int q = 0; q < p.nq; ++q) {
+    double2 s = make_double2(0.0, 0.0);
+    if (lane == 0) {
+      double J[9];
+      const double det = jacobian(p.dim, p.nn, X, p.geoGrad + (size_t)q * p.nn * 3, J);
+      double xq[3] = {0, 0, 0};
+      for (int k = 0; k < p.nn; ++k)
+        for (int c = 0; c < 3; ++c) xq[c] += p.geoVal[q * p.nn + k] * X[3 * k + c];
+      double2 f = make_double2(0.0, 0.0);
+      for (int t = 0; t < terms.n; ++t)
+        if (terms.t[t].kind == FG_TERM_SOURCE) f = cadd(f, evalExpr(terms.t[t].coef, e, xq));
+      s = make_double2(p.w[q] * det * f.x, p.w[q] * det * f.y);
+    }
+    s.x = __shfl_sync(0xffffffffu, s.x, 0);
+    s.y = __shfl_sync(0xffffffffu, s.y, 0);
+    const size_t base = ((size_t)o * p.nq + q) * p.nb;
+    for (int i = lane; i < p.nb; i += 32) {
+      const double ph = p.bval[base + i];
+      acc[i >> 5].x += s.x * ph;
+      acc[i >> 5].y += s.y * ph;
+    }
+  }
+  for (int i = lane; i < p.nb; i += 32) be[(size_t)e * p.nb + i] = acc[i >> 5];
+}
+
+// -------------------------------------------- error report (device side)
+
+// per element ||Ke32 - Ke64||_F^2 and ||Ke64||_F^2
+__global__ void k_elem_err(const float *__restrict__ k32, const double *__restrict__ k64, int64_t E, int len, double *__restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (e >= E) return;
+  double d2 = 0.0, r2 = 0.0;
+  for (int k = lane; k < len; k += 32) {
+    const double a = k64[(size_t)e * len + k];
+    const double d = (double)k32[(size_t)e * len + k] - a;
+    d2 += d * d;
+    r2 += a * a;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    d2 += __shfl_down_sync(0xffffffffu, d2, off);
+    r2 += __shfl_down_sync(0xffffffffu, r2, off);
+  }
+  if (lane == 0) {
+    out[2 * e] = d2;
+    out[2 * e + 1] = r2;
+  }
+}
+
+__global__ void k_diff_norms(const double *__restrict__ a, const double *__restrict__ b, int64_t n, double *__restrict__ out) {
+  double d2 = 0.0, r2 = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = a[i] - b[i];
+    d2 += d * d;
+    r2 += b[i] * b[i];
+  }
+  __shared__ double s[2][32];
+  for (int off = 16; off > 0; off >>= 1) {
+    d2 += __shfl_down_sync(0xffffffffu, d2, off);
+    r2 += __shfl_down_sync(0xffffffffu, r2, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s[0][threadIdx.x >> 5] = d2;
+    s[1][threadIdx.x >> 5] = r2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0, y = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      x += s[0][w];
+      y += s[1][w];
+    }
+    out[2 * blockIdx.x] = x;
+    out[2 * blockIdx.x + 1] = y;
+  }
+}
+
+// --------------------------------------------------------------- host
+
+static MixedState *state(fg_plan *plan) {
+  if (!plan->mixed) plan->mixed = new MixedState();
+  return (MixedState *)plan->mixed;
+}
+
+// reference tensors T^o (FP64 on the host from the plan's basis tables), split
+// and laid out as the B' shared-memory image: row n (= i*n + j) of B' holds
+// its K' values; core matrix (n/8, kc) at kc * (Npad*16) + (n/8)*128, row n%8
+// at +16*(n%8)
+static void buildB(const PlanDev &p, const std::vector<double> &w, const std::vector<double> &bval, const std::vector<double> &bgrad,
+                   int o, int Npad, std::vector<float> &img) {
+  const int n = p.nb, nq = p.nq;
+  img.assign((size_t)Npad * kK3, 0.0f);
+  const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double T[kKp] = {0, 0, 0, 0, 0, 0, 0, 0};
+      for (int q = 0; q < nq; ++q) {
+        const double *gi = &bgrad[(((size_t)o * nq + q) * n + i) * 3];
+        const double *gj = &bgrad[(((size_t)o * nq + q) * n + j) * 3];
+        for (int k = 0; k < 6; ++k) {
+          const int a = ab[k][0], b = ab[k][1];
+          T[k] += w[q] * (gj[a] * gi[b] + (a != b ? gj[b] * gi[a] : 0.0));
+        }
+        T[6] += w[q] * bval[((size_t)o * nq + q) * n + i] * bval[((size_t)o * nq + q) * n + j];
+      }
+      const int row = i * n + j;
+      for (int k = 0; k < kKp; ++k) {
+        float hi, lo;
+        splitTf32(T[k], hi, lo);
+        const float vals[3] = {hi, hi, lo};  // K' blocks: [B_hi ; B_hi ; B_lo]
+        for (int blk = 0; blk < 3; ++blk) {
+          const int kk = blk * kKp + k;
+          const int kc = kk >> 2, within = kk & 3;
+          const size_t off = (size_t)kc * (Npad * 4) + (size_t)(row >> 3) * 32 + (row & 7) * 4 + within;  // in floats
+          img[off] = vals[blk];
+        }
+      }
+    }
+}
+
+static int prepareMixed(fg_plan *plan, int complexKe) {
+  MixedState *m = state(plan);
+  const PlanDev &p = plan->d;
+  const int ncomp = complexKe ? 2 : 1;
+  if (m->built && m->complexKe == complexKe) return FG_OK;
+  if (!m->built) {
+    if (p.mult != 1) {
+      setLastError("mixed path: compound fields are not supported yet");
+      return FG_ERR_UNSUPPORTED;
+    }
+    if (p.nn != p.dim + 1) {
+      setLastError("mixed path: needs affine (first-order geometry) elements");
+      return FG_ERR_UNSUPPORTED;
+    }
+    m->n = p.n;
+    m->nn2 = p.n * p.n;
+    m->Npad = (m->nn2 + 15) / 16 * 16;
+    m->nOrient = p.nOrient;
+    if (m->Npad > kTmemCols) {
+      setLastError("mixed path: element matrix wider than the 512 TMEM columns");
+      return FG_ERR_UNSUPPORTED;
+    }
+    if ((size_t)m->Npad * kK3 * 4 + kBM * kK3 * 4 + 64 > 220 * 1024) {
+      setLastError("mixed path: element matrix too large for the shared-memory B tile");
+      return FG_ERR_UNSUPPORTED;
+    }
+    // tables back to the host
+    std::vector<double> w(p.nq), bval((size_t)p.nOrient * p.nq * p.nb), bgrad(bval.size() * 3);
+    FG_CUDA(cudaMemcpy(w.data(), p.w, w.size() * 8, cudaMemcpyDeviceToHost));
+    FG_CUDA(cudaMemcpy(bval.data(), p.bval, bval.size() * 8, cudaMemcpyDeviceToHost));
+    FG_CUDA(cudaMemcpy(bgrad.data(), p.bgrad, bgrad.size() * 8, cudaMemcpyDeviceToHost));
+    std::vector<float> all((size_t)p.nOrient * m->Npad * kK3), img;
+    for (int o = 0; o < p.nOrient; ++o) {
+      buildB(p, w, bval, bgrad, o, m->Npad, img);
+      std::copy(img.begin(), img.end(), all.begin() + (size_t)o * m->Npad * kK3);
+    }
+    FG_CUDA(cudaMalloc(&m->B, all.size() * 4));
+    FG_CUDA(cudaMemcpy(m->B, all.data(), all.size() * 4, cudaMemcpyHostToDevice));
+    // elements sorted by orientation (stable)
+    std::vector<int32_t> orient((size_t)p.E, 0);
+    if (p.orient) FG_CUDA(cudaMemcpy(orient.data(), p.orient, (size_t)p.E * 4, cudaMemcpyDeviceToHost));
+    std::vector<int32_t> perm((size_t)p.E);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(), [&](int32_t a, int32_t b) { return orient[a] < orient[b]; });
+    std::vector<int32_t> rank((size_t)p.E);
+    for (int64_t r = 0; r < p.E; ++r) rank[perm[r]] = (int32_t)r;
+    FG_CUDA(cudaMalloc(&m->perm, (size_t)p.E * 4 * 2));
+    FG_CUDA(cudaMemcpy(m->perm, perm.data(), (size_t)p.E * 4, cudaMemcpyHostToDevice));
+    FG_CUDA(cudaMemcpy(m->perm + p.E, rank.data(), (size_t)p.E * 4, cudaMemcpyHostToDevice));
+    FG_CUDA(cudaMalloc(&m->err, sizeof(int)));
+    FG_CUDA(cudaMemset(m->err, 0, sizeof(int)));
+    m->built = 1;
+  }
+  // tiles (depend on the rows per element)
+  std::vector<int32_t> orient((size_t)p.E, 0);
+  if (p.orient) FG_CUDA(cudaMemcpy(orient.data(), p.orient, (size_t)p.E * 4, cudaMemcpyDeviceToHost));
+  std::vector<int64_t> count(p.nOrient, 0);
+  for (int64_t e = 0; e < p.E; ++e) count[orient[e]]++;
+  std::vector<int32_t> tiles;
+  int64_t start = 0;
+  for (int o = 0; o < p.nOrient; ++o) {
+    const int64_t r0 = start * ncomp, r1 = (start + count[o]) * ncomp;
+    for (int64_t r = r0; r < r1; r += kBM) {
+      tiles.push_back(o);
+      tiles.push_back((int32_t)r);
+      tiles.push_back((int32_t)std::min<int64_t>(kBM, r1 - r));
+    }
+    start += count[o];
+  }
+  if (m->tiles) cudaFree(m->tiles);
+  FG_CUDA(cudaMalloc(&m->tiles, std::max<size_t>(tiles.size(), 3) * 4));
+  FG_CUDA(cudaMemcpy(m->tiles, tiles.data(), tiles.size() * 4, cudaMemcpyHostToDevice));
+  m->nTiles = (int)(tiles.size() / 3);
+  m->rows = p.E * ncomp;
+  int st = ensureDevice((void **)&m->A, &m->Abytes, (size_t)m->rows * kK3 * 4);
+  if (st) return st;
+  st = ensureDevice((void **)&m->ke, &m->keBytes, (size_t)m->rows * m->nn2 * 4);
+  if (st) return st;
+  m->complexKe = complexKe;
+  return FG_OK;
+}
+
+static int launchMixedElement(fg_plan *plan, const DevTerms &dt, cudaStream_t s) {
+  MixedState *m = state(plan);
+  const PlanDev &p = plan->d;
+  const int ncomp = dt.complexKe ? 2 : 1;
+  {
+    ProfScope prof("k_factors", s);
+    k_factors<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dt, m->perm + p.E, m->A, ncomp);
+    countLaunch();
+    FG_CUDA(cudaGetLastError());
+  }
+  GemmArgs g;
+  g.A = m->A;
+  g.B = m->B;
+  g.tiles = m->tiles;
+  g.perm = m->perm;
+  g.ke = m->ke;
+  g.err = m->err;
+  g.nTiles = m->nTiles;
+  g.Npad = m->Npad;
+  g.nn2 = m->nn2;
+  g.ncomp = ncomp;
+  // at least half the SM's shared memory: one CTA per SM, so no CTA ever
+  // waits in tcgen05.alloc for another one's 512 TMEM columns
+  const size_t smem = std::max<size_t>((size_t)m->Npad * kK3 * 4 + kBM * kK3 * 4 + 64, 116 * 1024);
+  FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = std::max(1, std::min(sms, m->nTiles));
+  {
+    ProfScope prof("k_contract_tf32x3", s);
+    k_contract_tf32x3<<<grid, kThreadsGemm, smem, s>>>(g);
+    countLaunch();
+    FG_CUDA(cudaGetLastError());
+  }
+  return FG_OK;
+}
+
+}  // namespace femg
+
+using namespace femg;
+
+extern "C" void mixedDestroy(fg_plan *plan) {
+  MixedState *m = (MixedState *)plan->mixed;
+  if (!m) return;
+  cudaFree(m->A);
+  cudaFree(m->B);
+  cudaFree(m->perm);
+  cudaFree(m->tiles);
+  cudaFree(m->ke);
+  cudaFree(m->err);
+  delete m;
+  plan->mixed = nullptr;
+}
+
+extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency, const double *dirichlet,
+                                 double *csr_values, double *rhs, void *stream, fg_err_report *report) {
+  if (!plan) return FG_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  DevTerms dt;
+  int st = resolveTerms(plan, terms, n_terms, frequency, &dt);
+  if (st) return st;
+  for (int t = 0; t < dt.n; ++t)
+    if (dt.t[t].kind != FG_TERM_SOURCE && dt.t[t].coef.cls == kExprPoint) {
+      setLastError("mixed path: bilinear coefficients must be constant per element");
+      return FG_ERR_UNSUPPORTED;
+    }
+  if ((st = prepareMixed(plan, dt.complexKe))) return st;
+  const double *uD = nullptr;
+  if ((st = uploadDirichlet(plan, dirichlet, &uD, s))) return st;
+  Outputs o;
+  if ((st = prepareOutputs(plan, csr_values, rhs, &o))) return st;
+  const PlanDev &p = plan->d;
+  MixedState *m = state(plan);
+  double *be = nullptr;
+  if (dt.hasSource && rhs) {
+    if ((st = ensureDevice((void **)&plan->be, &plan->beBytes, (size_t)p.E * p.n * 16))) return st;
+    be = plan->be;
+    ProfScope prof("k_rhs_fp64", s);
+    const int64_t threads = p.E * 32;
+    k_rhs_fp64<<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(p, dt, (double2 *)be);
+    countLaunch();
+    FG_CUDA(cudaGetLastError());
+  }
+  if (p.E > 0)
+    if ((st = launchMixedElement(plan, dt, s))) return st;
+  if ((st = launchGather(plan, (const double *)m->ke, dt.complexKe, 1, be, uD, o.values, o.rhs, s))) return st;
+  if (report) {
+    // FP64 element matrices and CSR of the same terms, compared on the device
+    const int ncomp = dt.complexKe ? 2 : 1;
+    const size_t len = (size_t)ncomp * p.n * p.n;
+    if ((st = ensureDevice((void **)&plan->ke, &plan->keBytes, (size_t)p.E * len * 8))) return st;
+    if ((st = launchElementFp64(plan, dt, plan->ke, nullptr, s))) return st;
+    double *tmp = nullptr, *csr64 = nullptr;
+    FG_CUDA(cudaMalloc(&tmp, (size_t)std::max<int64_t>(p.E, 1024) * 16));
+    FG_CUDA(cudaMalloc(&csr64, p.nnz * 16));
+    k_elem_err<<<(unsigned)((p.E + 7) / 8), 256, 0, s>>>(m->ke, plan->ke, p.E, (int)len, tmp);
+    std::vector<double> h((size_t)p.E * 2);
+    FG_CUDA(cudaMemcpyAsync(h.data(), tmp, h.size() * 8, cudaMemcpyDeviceToHost, s));
+    if ((st = launchGather(plan, plan->ke, dt.complexKe, 0, nullptr, uD, csr64, nullptr, s))) return st;
+    k_diff_norms<<<1024, 256, 0, s>>>(o.values, csr64, (int64_t)p.nnz * 2, tmp);
+    std::vector<double> g(2048);
+    FG_CUDA(cudaMemcpyAsync(g.data(), tmp, g.size() * 8, cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaStreamSynchronize(s));
+    countLaunch(2);
+    double mx = 0.0, sum = 0.0;
+    for (int64_t e = 0; e < p.E; ++e) {
+      const double r = h[2 * e + 1] > 0 ? std::sqrt(h[2 * e] / h[2 * e + 1]) : 0.0;
+      mx = std::max(mx, r);
+      sum += r;
+    }
+    double d2 = 0, r2 = 0;
+    for (int b = 0; b < 1024; ++b) {
+      d2 += g[2 * b];
+      r2 += g[2 * b + 1];
+    }
+    report->max_elem_rel_fro = mx;
+    report->mean_elem_rel_fro = p.E ? sum / p.E : 0.0;
+    report->global_rel_fro = r2 > 0 ? std::sqrt(d2 / r2) : 0.0;
+    cudaFree(tmp);
+    cudaFree(csr64);
+  }
+  int herr = 0;
+  FG_CUDA(cudaMemcpyAsync(&herr, m->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if ((st = finishOutputs(plan, o, csr_values, rhs, s))) return st;
+  FG_CUDA(cudaStreamSynchronize(s));
+  if (herr) {
+    setLastError("mixed path: a bounded device wait timed out");
+    return FG_ERR_TIMEOUT;
+  }
+  return FG_OK;
 }
 
 extern "C" int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, const double *omegas, int32_t n_freq,

@@ -133,6 +133,13 @@ bool isDevicePointer(const void *p);
 // FP64 gather of element matrices/vectors into CSR values and RHS
 int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, const double *be,
                  const double *dirichletDev, double *values, double *rhs, cudaStream_t s);
+// outputs: device pointers used in place, host pointers staged through the plan
+struct Outputs {
+  double *values = nullptr, *rhs = nullptr;
+  bool hostValues = false, hostRhs = false;
+};
+int prepareOutputs(fg_plan *plan, double *csr_values, double *rhs, Outputs *o);
+int finishOutputs(fg_plan *plan, const Outputs &o, double *csr_values, double *rhs, cudaStream_t s);
 // FP64 element kernel (also used as the reference for the mixed error report)
 int launchElementFp64(fg_plan *plan, const DevTerms &terms, double *ke, double *be, cudaStream_t s);
 

@@ -130,3 +130,33 @@ def test_full_size_c2_properties(femg, cuda):
     order = np.argsort(key)
     pos = np.searchsorted(key[order], keyT)
     assert np.allclose(v.real, v.real[order[pos]], rtol=0, atol=1e-12 * np.abs(v.real).max())
+
+
+MIXED_CASES = ["c2_m3", "c2_m4_p1", "c2_m3_p2", "c3_m4", "c1_p1mesh_dirichlet1"]
+
+
+@pytest.mark.parametrize("case", MIXED_CASES)
+def test_mixed_matches_oracle(femg, oracle, cuda, case):
+    """3xTF32 tensor-core contraction: global relative Frobenius error <= 1e-6
+    against the FP64 oracle, per-element report against the device FP64 path."""
+    prob = femg.Problem(cases(femg)[case])
+    a = prob.arrays()
+    t, nt = prob.terms()
+    ref_v, ref_b = oracle.assemble(a, t, nt)
+    plan = prob.plan()
+    v, b, rep = plan.assemble("mixed", report=True)
+    assert rel(v, ref_v) <= MIXED_TOL
+    assert rep["global_"] <= MIXED_TOL
+    assert rep["max_elem"] <= 10 * MIXED_TOL
+    if np.linalg.norm(ref_b) > 0:
+        assert rel(b, ref_b) <= FP64_TOL  # the right-hand side stays FP64
+
+
+def test_mixed_deterministic_and_complex(femg, cuda):
+    prob = femg.Problem(femg.config_c3(m=3))
+    plan = prob.plan()
+    v1, _ = plan.assemble("mixed")
+    v2, _ = plan.assemble("mixed")
+    assert np.array_equal(v1.view(np.uint64), v2.view(np.uint64))
+    v64, _ = plan.assemble("fp64")
+    assert rel(v1, v64) <= MIXED_TOL
