@@ -189,10 +189,14 @@ int launchElementFp64(fg_plan *plan, const DevTerms &terms, double *ke, double *
 
 // ------------------------------------------------------------------ gather
 
-template <typename SlotT, bool KCPLX, typename KT>
+// Loads of U element rows are issued back to back (they are independent),
+// then the rows are added into the shared row accumulator one after the
+// other, so the summation order stays the fixed element order.
+template <typename SlotT, bool KCPLX, typename KT, int NJ>
 __global__ void __launch_bounds__(256)
     k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
              double2 *__restrict__ values, double2 *__restrict__ rhs, int warpsPerBlock) {
+  constexpr int U = 4;
   extern __shared__ double2 acc[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -211,27 +215,59 @@ __global__ void __launch_bounds__(256)
     double2 bsum = make_double2(0.0, 0.0);
     double2 dc = make_double2(0.0, 0.0);
     const uint64_t r0 = p.rowPtr[row], r1 = p.rowPtr[row + 1];
-    for (uint64_t r = r0; r < r1; ++r) {
-      const uint32_t packed = p.rowElem[r];
-      const int64_t e = packed >> 6;
-      const int i = packed & 63;
-      const KT *K = ke + (size_t)e * (KCPLX ? 2 : 1) * nn2;
-      const SlotT *sl = slot + ((size_t)e * n + i) * n;
-      for (int j = lane; j < n; j += 32) {
-        const SlotT sv = sl[j];
-        if (sv == kIgnore) continue;
-        if (sv != kFixed) {
-          double2 v = make_double2((double)K[i * n + j], KCPLX ? (double)K[nn2 + i * n + j] : 0.0);
-          A[sv].x += v.x;
-          A[sv].y += v.y;
-        } else {
-          // VectorFactory::addValuesDC: values[j*n + i] * valuesDC[J]
-          const double2 v = make_double2((double)K[j * n + i], KCPLX ? (double)K[nn2 + j * n + i] : 0.0);
-          dc = cadd(dc, cmul(v, uD[p.edof[e * n + j]]));
+    for (uint64_t base = r0; base < r1; base += 32) {
+      const int m = (int)((r1 - base) < 32 ? (r1 - base) : 32);
+      const uint32_t mine = lane < m ? p.rowElem[base + lane] : 0u;
+      double2 bmine = make_double2(0.0, 0.0);
+      if (be && lane < m) bmine = be[(size_t)(mine >> 6) * n + (mine & 63)];
+      for (int k0 = 0; k0 < m; k0 += U) {
+        SlotT sv[U][NJ];
+        KT kr[U][NJ], kim[U][NJ];
+        int ei[U];
+        int64_t ee[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const uint32_t packed = __shfl_sync(0xffffffffu, mine, (k0 + u) & 31);
+          ee[u] = packed >> 6;
+          ei[u] = packed & 63;
+#pragma unroll
+          for (int jj = 0; jj < NJ; ++jj) {
+            const int j = lane + 32 * jj;
+            const bool ok = (k0 + u < m) && j < n;
+            const size_t rowOff = ((size_t)ee[u] * n + ei[u]) * n + j;
+            sv[u][jj] = ok ? slot[rowOff] : kIgnore;
+            const KT *K = ke + (size_t)ee[u] * (KCPLX ? 2 : 1) * nn2;
+            kr[u][jj] = ok ? K[ei[u] * n + j] : (KT)0;
+            kim[u][jj] = (ok && KCPLX) ? K[nn2 + ei[u] * n + j] : (KT)0;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+          for (int jj = 0; jj < NJ; ++jj) {
+            const SlotT s = sv[u][jj];
+            if (s == kIgnore) continue;
+            if (s != kFixed) {
+              A[s].x += (double)kr[u][jj];
+              A[s].y += (double)kim[u][jj];
+            } else {
+              // VectorFactory::addValuesDC: values[j*n + i] * valuesDC[J] (transposed entry)
+              const int j = lane + 32 * jj;
+              const int i = ei[u];
+              const KT *K = ke + (size_t)ee[u] * (KCPLX ? 2 : 1) * nn2;
+              const double2 v = make_double2((double)K[j * n + i], KCPLX ? (double)K[nn2 + j * n + i] : 0.0);
+              dc = cadd(dc, cmul(v, uD[p.edof[ee[u] * n + j]]));
+            }
+          }
+          __syncwarp();
         }
       }
-      if (be) bsum = cadd(bsum, be[e * n + i]);
-      __syncwarp();
+      if (be)
+        for (int k = 0; k < m; ++k) {
+          const double bx = __shfl_sync(0xffffffffu, bmine.x, k), by = __shfl_sync(0xffffffffu, bmine.y, k);
+          bsum.x += bx;
+          bsum.y += by;
+        }
     }
     for (int s = lane; s < len; s += 32) values[start + s] = A[s];
     if (rhs) {
@@ -268,7 +304,7 @@ int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, 
   double2 *r2 = (double2 *)rhs;
 #define FG_GATHER(SLOT, CPLX, KT)                                                                                 \
   do {                                                                                                            \
-    auto kern = k_gather<SLOT, CPLX, KT>;                                                                         \
+    auto kern = p.n > 32 ? k_gather<SLOT, CPLX, KT, 2> : k_gather<SLOT, CPLX, KT, 1>;                             \
     FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                  \
     kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be2, uD, v2, r2, wpb);                      \
   } while (0)

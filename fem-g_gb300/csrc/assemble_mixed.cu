@@ -214,6 +214,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
   float *As = Bs + (size_t)g.Npad * kK3;                             // kBM * kK3
   uint64_t *mbar = reinterpret_cast<uint64_t *>(As + kBM * kK3);
   uint32_t *tmemBase = reinterpret_cast<uint32_t *>(mbar + 1);
+  float *Stage = reinterpret_cast<float *>(mbar + 2);                 // 4 warps x 32 x 17
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (warp == 0) {
@@ -275,24 +276,26 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
     }
     tcFenceAfter();
     if (!failed) {
-      // epilogue: TMEM lane = tile row; warp w reads lanes [32w, 32w+32)
+      // epilogue: TMEM lane = tile row; warp w reads lanes [32w, 32w+32).
+      // Each 32 x 16 chunk goes through a padded shared stage so that a
+      // half-warp stores 16 consecutive floats of one output row.
+      float *stage = Stage + warp * (32 * 17);
       const int r = warp * 32 + lane;
-      const bool live = r < nrows;
       const int grow = row0 + r;
-      const int64_t e = live ? g.perm[grow / g.ncomp] : 0;
-      float *out = g.ke + ((size_t)e * g.ncomp + (grow % g.ncomp)) * g.nn2;
+      const int64_t myRow = r < nrows ? ((int64_t)g.perm[grow / g.ncomp] * g.ncomp + (grow % g.ncomp)) : -1;
       for (int c0 = 0; c0 < g.Npad; c0 += 16) {
         float v[16];
         tmemLoad16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-        if (live) {
-          if (c0 + 16 <= g.nn2 && ((g.nn2 & 3) == 0)) {
 #pragma unroll
-            for (int k = 0; k < 16; k += 4) *reinterpret_cast<float4 *>(out + c0 + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
-          } else {
-            for (int k = 0; k < 16; ++k)
-              if (c0 + k < g.nn2) out[c0 + k] = v[k];
-          }
+        for (int k = 0; k < 16; ++k) stage[lane * 17 + k] = v[k];
+        __syncwarp();
+        const int half = lane >> 4, col = c0 + (lane & 15);
+        for (int rr = 0; rr < 32; rr += 2) {
+          const int src = rr + half;
+          const int64_t orow = __shfl_sync(0xffffffffu, myRow, src);
+          if (orow >= 0 && col < g.nn2) g.ke[(size_t)orow * g.nn2 + col] = stage[src * 17 + (lane & 15)];
         }
+        __syncwarp();
       }
     }
     tcFenceBefore();
@@ -462,7 +465,7 @@ static int prepareMixed(fg_plan *plan, int complexKe) {
       setLastError("mixed path: element matrix wider than the 512 TMEM columns");
       return FG_ERR_UNSUPPORTED;
     }
-    if ((size_t)m->Npad * kK3 * 4 + kBM * kK3 * 4 + 64 > 220 * 1024) {
+    if ((size_t)m->Npad * kK3 * 4 + kBM * kK3 * 4 + 16 + 4 * 32 * 17 * 4 > 220 * 1024) {
       setLastError("mixed path: element matrix too large for the shared-memory B tile");
       return FG_ERR_UNSUPPORTED;
     }
@@ -545,7 +548,7 @@ static int launchMixedElement(fg_plan *plan, const DevTerms &dt, cudaStream_t s)
   g.ncomp = ncomp;
   // at least half the SM's shared memory: one CTA per SM, so no CTA ever
   // waits in tcgen05.alloc for another one's 512 TMEM columns
-  const size_t smem = std::max<size_t>((size_t)m->Npad * kK3 * 4 + kBM * kK3 * 4 + 64, 116 * 1024);
+  const size_t smem = std::max<size_t>((size_t)m->Npad * kK3 * 4 + kBM * kK3 * 4 + 16 + 4 * 32 * 17 * 4, 116 * 1024);
   FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);

@@ -149,7 +149,9 @@ def test_mixed_matches_oracle(femg, oracle, cuda, case):
     assert rep["global_"] <= MIXED_TOL
     assert rep["max_elem"] <= 10 * MIXED_TOL
     if np.linalg.norm(ref_b) > 0:
-        assert rel(b, ref_b) <= FP64_TOL  # the right-hand side stays FP64
+        # source terms stay FP64; the Dirichlet lifting reads the FP32 element matrices
+        lifted = a["n_fixed"] > 0 and np.any(a["dirichlet"] != 0)
+        assert rel(b, ref_b) <= (MIXED_TOL if lifted else FP64_TOL)
 
 
 def test_mixed_deterministic_and_complex(femg, cuda):
