@@ -12,15 +12,8 @@
 // (LinearTerm::evaluate, src/term/LinearTerm.cpp:182-191). Ke is symmetric
 // for these terms, so each lane owns upper-triangle entries.
 //
-// K4 (gather kernel, one warp per CSR row): walks the row's (element, local
-// test index) list in element order and adds each element row into a shared
-// accumulator at the precomputed column slots, then writes the row once.
-// This replaces MatrixFactory::addValues' binary search and atomics
-// (src/system/MatrixFactory.cpp:233-448) with a fixed-order sum, and applies
-// the Dirichlet lifting of VectorFactory::addValuesDC
-// (src/system/VectorFactory.cpp:178-210, which reads values[j*n + i], the
-// transposed element entry) and the element right-hand sides
-// (VectorFactory::addValues, :122-145).
+// The element matrices and vectors then go through the deterministic CSR
+// reduction of gather.cu.
 #include "common.cuh"
 
 namespace femg {
@@ -182,147 +175,6 @@ int launchElementFp64(fg_plan *plan, const DevTerms &terms, double *ke, double *
     return FG_ERR_UNSUPPORTED;
   }
 #undef FG_LAUNCH_ELEM
-  countLaunch();
-  FG_CUDA(cudaGetLastError());
-  return FG_OK;
-}
-
-// ------------------------------------------------------------------ gather
-
-// Loads of U element rows are issued back to back (they are independent),
-// then the rows are added into the shared row accumulator one after the
-// other, so the summation order stays the fixed element order.
-template <typename SlotT, bool KCPLX, typename KT, int NJ>
-__global__ void __launch_bounds__(256)
-    k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
-             double2 *__restrict__ values, double2 *__restrict__ rhs, int warpsPerBlock) {
-  constexpr int U = 4;
-  extern __shared__ double2 acc[];
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  double2 *A = acc + (size_t)warp * p.maxRowLen;
-  const SlotT *slot = (const SlotT *)p.slot;
-  const SlotT kFixed = (SlotT)(sizeof(SlotT) == 1 ? 0xFF : kSlotFixed);
-  const SlotT kIgnore = (SlotT)(sizeof(SlotT) == 1 ? 0xFE : kSlotIgnore);
-  const int n = p.n;
-  const size_t nn2 = (size_t)n * n;
-  const int64_t stride = (int64_t)gridDim.x * warpsPerBlock;
-  for (int64_t row = (int64_t)blockIdx.x * warpsPerBlock + warp; row < (int64_t)p.nRows; row += stride) {
-    const uint64_t start = p.ai[row];
-    const int len = (int)(p.ai[row + 1] - start);
-    for (int s = lane; s < len; s += 32) A[s] = make_double2(0.0, 0.0);
-    __syncwarp();
-    double2 bsum = make_double2(0.0, 0.0);
-    double2 dc = make_double2(0.0, 0.0);
-    const uint64_t r0 = p.rowPtr[row], r1 = p.rowPtr[row + 1];
-    for (uint64_t base = r0; base < r1; base += 32) {
-      const int m = (int)((r1 - base) < 32 ? (r1 - base) : 32);
-      const uint32_t mine = lane < m ? p.rowElem[base + lane] : 0u;
-      double2 bmine = make_double2(0.0, 0.0);
-      if (be && lane < m) bmine = be[(size_t)(mine >> 6) * n + (mine & 63)];
-      for (int k0 = 0; k0 < m; k0 += U) {
-        SlotT sv[U][NJ];
-        KT kr[U][NJ], kim[U][NJ];
-        int ei[U];
-        int64_t ee[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const uint32_t packed = __shfl_sync(0xffffffffu, mine, (k0 + u) & 31);
-          ee[u] = packed >> 6;
-          ei[u] = packed & 63;
-#pragma unroll
-          for (int jj = 0; jj < NJ; ++jj) {
-            const int j = lane + 32 * jj;
-            const bool ok = (k0 + u < m) && j < n;
-            const size_t rowOff = ((size_t)ee[u] * n + ei[u]) * n + j;
-            sv[u][jj] = ok ? slot[rowOff] : kIgnore;
-            const KT *K = ke + (size_t)ee[u] * (KCPLX ? 2 : 1) * nn2;
-            kr[u][jj] = ok ? K[ei[u] * n + j] : (KT)0;
-            kim[u][jj] = (ok && KCPLX) ? K[nn2 + ei[u] * n + j] : (KT)0;
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-#pragma unroll
-          for (int jj = 0; jj < NJ; ++jj) {
-            const SlotT s = sv[u][jj];
-            if (s == kIgnore) continue;
-            if (s != kFixed) {
-              A[s].x += (double)kr[u][jj];
-              A[s].y += (double)kim[u][jj];
-            } else {
-              // VectorFactory::addValuesDC: values[j*n + i] * valuesDC[J] (transposed entry)
-              const int j = lane + 32 * jj;
-              const int i = ei[u];
-              const KT *K = ke + (size_t)ee[u] * (KCPLX ? 2 : 1) * nn2;
-              const double2 v = make_double2((double)K[j * n + i], KCPLX ? (double)K[nn2 + j * n + i] : 0.0);
-              dc = cadd(dc, cmul(v, uD[p.edof[ee[u] * n + j]]));
-            }
-          }
-          __syncwarp();
-        }
-      }
-      if (be)
-        for (int k = 0; k < m; ++k) {
-          const double bx = __shfl_sync(0xffffffffu, bmine.x, k), by = __shfl_sync(0xffffffffu, bmine.y, k);
-          bsum.x += bx;
-          bsum.y += by;
-        }
-    }
-    for (int s = lane; s < len; s += 32) values[start + s] = A[s];
-    if (rhs) {
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        dc.x += __shfl_down_sync(0xffffffffu, dc.x, off);
-        dc.y += __shfl_down_sync(0xffffffffu, dc.y, off);
-      }
-      if (lane == 0) rhs[row] = cadd(bsum, dc);
-    }
-    __syncwarp();
-  }
-}
-
-int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, const double *be, const double *dirichletDev,
-                 double *values, double *rhs, cudaStream_t s) {
-  const PlanDev &p = plan->d;
-  if (p.nRows == 0) return FG_OK;
-  const size_t rowBytes = (size_t)std::max(p.maxRowLen, 1) * sizeof(double2);
-  int wpb = (int)std::min<size_t>(8, (200 * 1024) / rowBytes);
-  if (wpb < 1) {
-    setLastError("gather: CSR row too long for shared memory");
-    return FG_ERR_UNSUPPORTED;
-  }
-  const size_t smem = rowBytes * wpb;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int64_t blocks = ((int64_t)p.nRows + wpb - 1) / wpb;
-  blocks = std::min<int64_t>(blocks, (int64_t)sms * 32);
-  const double2 *be2 = (const double2 *)be;
-  const double2 *uD = (const double2 *)dirichletDev;
-  double2 *v2 = (double2 *)values;
-  double2 *r2 = (double2 *)rhs;
-#define FG_GATHER(SLOT, CPLX, KT)                                                                                 \
-  do {                                                                                                            \
-    auto kern = p.n > 32 ? k_gather<SLOT, CPLX, KT, 2> : k_gather<SLOT, CPLX, KT, 1>;                             \
-    FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                  \
-    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be2, uD, v2, r2, wpb);                      \
-  } while (0)
-  ProfScope prof("k_gather", s);
-  if (p.slotBytes == 1) {
-    if (keIsFloat) {
-      if (keComplex) FG_GATHER(uint8_t, true, float); else FG_GATHER(uint8_t, false, float);
-    } else {
-      if (keComplex) FG_GATHER(uint8_t, true, double); else FG_GATHER(uint8_t, false, double);
-    }
-  } else {
-    if (keIsFloat) {
-      if (keComplex) FG_GATHER(uint16_t, true, float); else FG_GATHER(uint16_t, false, float);
-    } else {
-      if (keComplex) FG_GATHER(uint16_t, true, double); else FG_GATHER(uint16_t, false, double);
-    }
-  }
-#undef FG_GATHER
   countLaunch();
   FG_CUDA(cudaGetLastError());
   return FG_OK;

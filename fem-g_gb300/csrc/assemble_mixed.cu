@@ -146,6 +146,22 @@ __device__ inline void tmemLoad16(uint32_t taddr, float *v) {
   for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+__device__ inline void tmemLoad32(uint32_t taddr, float *v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+        "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+
 // ------------------------------------------------- geometry: factor rows
 
 // One thread per element: J, det, J^-1 in FP64 from the vertex nodes (affine
@@ -214,7 +230,6 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
   float *As = Bs + (size_t)g.Npad * kK3;                             // kBM * kK3
   uint64_t *mbar = reinterpret_cast<uint64_t *>(As + kBM * kK3);
   uint32_t *tmemBase = reinterpret_cast<uint32_t *>(mbar + 1);
-  float *Stage = reinterpret_cast<float *>(mbar + 2);                 // 4 warps x 32 x 17
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (warp == 0) {
@@ -276,26 +291,40 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
     }
     tcFenceAfter();
     if (!failed) {
-      // epilogue: TMEM lane = tile row; warp w reads lanes [32w, 32w+32).
-      // Each 32 x 16 chunk goes through a padded shared stage so that a
-      // half-warp stores 16 consecutive floats of one output row.
-      float *stage = Stage + warp * (32 * 17);
+      // epilogue: TMEM lane = tile row; warp w reads lanes [32w, 32w+32);
+      // each thread stores its own element row (contiguous in global memory)
       const int r = warp * 32 + lane;
+      const bool live = r < nrows;
       const int grow = row0 + r;
-      const int64_t myRow = r < nrows ? ((int64_t)g.perm[grow / g.ncomp] * g.ncomp + (grow % g.ncomp)) : -1;
-      for (int c0 = 0; c0 < g.Npad; c0 += 16) {
+      const int64_t e = live ? g.perm[grow / g.ncomp] : 0;
+      float *out = g.ke + ((size_t)e * g.ncomp + (grow % g.ncomp)) * g.nn2;
+      const bool vec = (g.nn2 & 3) == 0;
+      int c0 = 0;
+      for (; c0 + 32 <= g.Npad; c0 += 32) {
+        float v[32];
+        tmemLoad32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        if (live) {
+          if (vec && c0 + 32 <= g.nn2) {
+#pragma unroll
+            for (int k = 0; k < 32; k += 4) *reinterpret_cast<float4 *>(out + c0 + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+          } else {
+            for (int k = 0; k < 32; ++k)
+              if (c0 + k < g.nn2) out[c0 + k] = v[k];
+          }
+        }
+      }
+      if (c0 < g.Npad) {  // a last 16-column chunk
         float v[16];
         tmemLoad16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        if (live) {
+          if (vec && c0 + 16 <= g.nn2) {
 #pragma unroll
-        for (int k = 0; k < 16; ++k) stage[lane * 17 + k] = v[k];
-        __syncwarp();
-        const int half = lane >> 4, col = c0 + (lane & 15);
-        for (int rr = 0; rr < 32; rr += 2) {
-          const int src = rr + half;
-          const int64_t orow = __shfl_sync(0xffffffffu, myRow, src);
-          if (orow >= 0 && col < g.nn2) g.ke[(size_t)orow * g.nn2 + col] = stage[src * 17 + (lane & 15)];
+            for (int k = 0; k < 16; k += 4) *reinterpret_cast<float4 *>(out + c0 + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+          } else {
+            for (int k = 0; k < 16; ++k)
+              if (c0 + k < g.nn2) out[c0 + k] = v[k];
+          }
         }
-        __syncwarp();
       }
     }
     tcFenceBefore();

@@ -1,0 +1,163 @@
+// K4 + K5: deterministic row-owner reduction of element matrices and vectors
+// into the CSR values and the right-hand side.
+//
+// Replaces MatrixFactory::addValues (src/system/MatrixFactory.cpp:233-448:
+// lower_bound per entry + OpenMP atomics) and VectorFactory::addValues /
+// addValuesDC (src/system/VectorFactory.cpp:122-210). Each CSR row is owned
+// by a sub-warp of L lanes (L * 3 >= element DOFs, so 32/L rows share a warp);
+// the sub-warp walks the row's (element, local test index) list in element
+// order, and every lane adds its columns of that element row into a shared
+// accumulator at the slots precomputed by fg_plan_create. Entries are
+// separated by __syncwarp, so each CSR value is summed in the same order on
+// every run. Rows are visited sorted by their number of contributing
+// elements, so the sub-warps of a warp run loops of equal length.
+// Dirichlet lifting reads the transposed element entry, as addValuesDC does
+// (values[j*n + i] * valuesDC[J], src/system/VectorFactory.cpp:184).
+#include "common.cuh"
+
+namespace femg {
+
+template <typename SlotT, bool KCPLX, typename KT, typename AT, int L>
+__global__ void __launch_bounds__(256)
+    k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
+             double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock) {
+  constexpr int R = 32 / L;  // rows per warp
+  constexpr int J = 3;       // columns per lane
+  constexpr int SS = KCPLX ? 2 : 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / L, lt = lane % L;
+  AT *A = reinterpret_cast<AT *>(smraw) + (size_t)(warp * R + sub) * p.maxRowLen * SS;
+  const SlotT *slot = (const SlotT *)p.slot;
+  const SlotT kFixed = (SlotT)(sizeof(SlotT) == 1 ? 0xFF : kSlotFixed);
+  const SlotT kIgnore = (SlotT)(sizeof(SlotT) == 1 ? 0xFE : kSlotIgnore);
+  const int n = p.n;
+  const size_t nn2 = (size_t)n * n;
+  const int64_t nRows = (int64_t)p.nRows;
+  const int64_t stride = (int64_t)gridDim.x * rowsPerBlock;
+  for (int64_t base = (int64_t)blockIdx.x * rowsPerBlock + warp * R; base < nRows; base += stride) {
+    const int64_t idx = base + sub;
+    const bool live = idx < nRows;
+    const int64_t row = live ? (int64_t)p.rowOrder[idx] : 0;
+    const uint64_t start = live ? p.ai[row] : 0;
+    const int len = live ? (int)(p.ai[row + 1] - start) : 0;
+    for (int s = lt; s < len * SS; s += L) A[s] = (AT)0;
+    const uint64_t r0 = live ? p.rowPtr[row] : 0;
+    const int cnt = live ? (int)(p.rowPtr[row + 1] - r0) : 0;
+    int maxCnt = cnt;
+#pragma unroll
+    for (int off = L; off < 32; off <<= 1) maxCnt = max(maxCnt, __shfl_xor_sync(0xffffffffu, maxCnt, off));
+    __syncwarp();
+    double2 dc = make_double2(0.0, 0.0), bsum = make_double2(0.0, 0.0);
+    for (int k = 0; k < maxCnt; ++k) {
+      const bool act = k < cnt;
+      const uint32_t packed = act ? p.rowElem[r0 + k] : 0u;
+      const int64_t e = packed >> 6;
+      const int i = packed & 63;
+      const size_t rowOff = ((size_t)e * n + i) * n;
+      const KT *K = ke + (size_t)e * SS * nn2;
+      SlotT sv[J];
+      KT vr[J], vi[J];
+#pragma unroll
+      for (int jj = 0; jj < J; ++jj) {
+        const int j = lt + L * jj;
+        const bool ok = act && j < n;
+        sv[jj] = ok ? slot[rowOff + j] : kIgnore;
+        vr[jj] = ok ? K[i * n + j] : (KT)0;
+        vi[jj] = (ok && KCPLX) ? K[nn2 + i * n + j] : (KT)0;
+      }
+      if (be && act && lt == 0) bsum = cadd(bsum, be[(size_t)e * n + i]);
+#pragma unroll
+      for (int jj = 0; jj < J; ++jj) {
+        const SlotT s = sv[jj];
+        if (s == kIgnore) continue;
+        if (s != kFixed) {
+          A[(int)s * SS] += (AT)vr[jj];
+          if (KCPLX) A[(int)s * SS + 1] += (AT)vi[jj];
+        } else {
+          const int j = lt + L * jj;
+          const double2 v = make_double2((double)K[j * n + i], KCPLX ? (double)K[nn2 + j * n + i] : 0.0);
+          dc = cadd(dc, cmul(v, uD[p.edof[e * n + j]]));
+        }
+      }
+      __syncwarp();
+    }
+    for (int s = lt; s < len; s += L)
+      values[start + s] = make_double2((double)A[s * SS], KCPLX ? (double)A[s * SS + 1] : 0.0);
+    if (rhs) {
+#pragma unroll
+      for (int off = L / 2; off > 0; off >>= 1) {
+        dc.x += __shfl_down_sync(0xffffffffu, dc.x, off, L);
+        dc.y += __shfl_down_sync(0xffffffffu, dc.y, off, L);
+      }
+      if (live && lt == 0) rhs[row] = cadd(bsum, dc);
+    }
+    __syncwarp();
+  }
+}
+
+template <typename SlotT, bool KCPLX, typename KT>
+static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, const double2 *uD, double2 *values, double2 *rhs,
+                       cudaStream_t s) {
+  using AT = KT;  // FP32 element matrices accumulate in FP32, FP64 ones in FP64
+  const int n = p.n;
+  int L = 32;
+  if (n <= 6) L = 2;
+  else if (n <= 12) L = 4;
+  else if (n <= 24) L = 8;
+  else if (n <= 48) L = 16;
+  const int R = 32 / L;
+  const size_t rowBytes = (size_t)std::max(p.maxRowLen, 1) * (KCPLX ? 2 : 1) * sizeof(AT);
+  int wpb = 8;
+  while (wpb > 1 && rowBytes * R * wpb > 200 * 1024) wpb >>= 1;
+  if (rowBytes * R * wpb > 200 * 1024) {
+    setLastError("gather: CSR row too long for shared memory");
+    return FG_ERR_UNSUPPORTED;
+  }
+  const size_t smem = rowBytes * R * wpb;
+  const int rowsPerBlock = wpb * R;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t blocks = ((int64_t)p.nRows + rowsPerBlock - 1) / rowsPerBlock;
+  blocks = std::min<int64_t>(blocks, (int64_t)sms * 16);
+#define FG_GATHER_L(LL)                                                                                           \
+  case LL: {                                                                                                      \
+    auto kern = k_gather<SlotT, KCPLX, KT, AT, LL>;                                                               \
+    FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                  \
+    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock);         \
+    break;                                                                                                        \
+  }
+  switch (L) {
+    FG_GATHER_L(2)
+    FG_GATHER_L(4)
+    FG_GATHER_L(8)
+    FG_GATHER_L(16)
+    FG_GATHER_L(32)
+  }
+#undef FG_GATHER_L
+  FG_CUDA(cudaGetLastError());
+  return FG_OK;
+}
+
+int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, const double *be, const double *dirichletDev,
+                 double *values, double *rhs, cudaStream_t s) {
+  const PlanDev &p = plan->d;
+  if (p.nRows == 0) return FG_OK;
+  const double2 *be2 = (const double2 *)be;
+  const double2 *uD = (const double2 *)dirichletDev;
+  double2 *v2 = (double2 *)values;
+  double2 *r2 = (double2 *)rhs;
+  ProfScope prof("k_gather", s);
+  countLaunch();
+  if (p.slotBytes == 1) {
+    if (keIsFloat)
+      return keComplex ? launchTyped<uint8_t, true, float>(p, ke, be2, uD, v2, r2, s) : launchTyped<uint8_t, false, float>(p, ke, be2, uD, v2, r2, s);
+    return keComplex ? launchTyped<uint8_t, true, double>(p, ke, be2, uD, v2, r2, s) : launchTyped<uint8_t, false, double>(p, ke, be2, uD, v2, r2, s);
+  }
+  if (keIsFloat)
+    return keComplex ? launchTyped<uint16_t, true, float>(p, ke, be2, uD, v2, r2, s) : launchTyped<uint16_t, false, float>(p, ke, be2, uD, v2, r2, s);
+  return keComplex ? launchTyped<uint16_t, true, double>(p, ke, be2, uD, v2, r2, s) : launchTyped<uint16_t, false, double>(p, ke, be2, uD, v2, r2, s);
+}
+
+}  // namespace femg

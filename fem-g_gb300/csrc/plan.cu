@@ -202,6 +202,21 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
       }
   }
 
+  // gather visiting order: rows grouped by contribution count (stable)
+  std::vector<uint32_t> rowOrder(sys->n_rows);
+  {
+    uint64_t maxCnt = 0;
+    for (uint64_t r = 0; r < sys->n_rows; ++r) maxCnt = std::max(maxCnt, rowPtr[r + 1] - rowPtr[r]);
+    std::vector<uint64_t> bucket(maxCnt + 2, 0);
+    for (uint64_t r = 0; r < sys->n_rows; ++r) bucket[rowPtr[r + 1] - rowPtr[r] + 1]++;
+    for (uint64_t c = 0; c <= maxCnt; ++c) bucket[c + 1] += bucket[c];
+    for (uint64_t r = 0; r < sys->n_rows; ++r) rowOrder[bucket[rowPtr[r + 1] - rowPtr[r]]++] = (uint32_t)r;
+  }
+  if (sys->n_rows >= (uint64_t(1) << 32)) {
+    setLastError("fg_plan_create: more than 2^32 rows");
+    return FG_ERR_UNSUPPORTED;
+  }
+
   // slots: position of each column inside its row
   uint64_t maxLen = 0;
   for (uint64_t r = 0; r < sys->n_rows; ++r) maxLen = std::max(maxLen, sys->ai[r + 1] - sys->ai[r]);
@@ -267,6 +282,7 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   if ((st = upload(plan, sys->ai, (size_t)sys->n_rows + 1, &d.ai))) return st;
   if ((st = upload(plan, rowPtr.data(), rowPtr.size(), &d.rowPtr))) return st;
   if ((st = upload(plan, rowElem.data(), rowElem.size(), &d.rowElem))) return st;
+  if ((st = upload(plan, rowOrder.data(), rowOrder.size(), &d.rowOrder))) return st;
   if (narrow) {
     const uint8_t *p;
     if ((st = upload(plan, slot8.data(), slot8.size(), &p))) return st;
