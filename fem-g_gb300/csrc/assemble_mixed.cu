@@ -30,7 +30,7 @@ constexpr int kBM = 128;       // rows (element components) per tile = TMEM lane
 constexpr int kKp = 8;         // factor columns (7 used)
 constexpr int kK3 = 3 * kKp;   // K' of the 3xTF32 chain
 constexpr int kTmemCols = 512;
-constexpr int kThreadsGemm = 128;
+constexpr int kThreadsGemm = 256;
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s bound on any device-side wait
 
 struct MixedState {
@@ -48,7 +48,30 @@ struct MixedState {
   float *ke = nullptr;       // [E][ncomp][n][n] fp32
   size_t keBytes = 0;
   int *err = nullptr;        // device error word (wait timeouts)
+  int *errHost = nullptr;    // pinned copy of err
+  cudaEvent_t errEvent = nullptr;
+  bool errPending = false;
 };
+
+// Reports (once) a device wait timeout recorded by an earlier launch: when
+// wait is false only an already completed copy of the error word is read.
+static int checkTimeout(MixedState *m, bool wait) {
+  if (!m->errPending) return FG_OK;
+  if (wait) {
+    if (cudaEventSynchronize(m->errEvent) != cudaSuccess) return FG_ERR_CUDA;
+  } else if (cudaEventQuery(m->errEvent) != cudaSuccess) {
+    cudaGetLastError();  // not ready yet: check on a later call
+    return FG_OK;
+  }
+  m->errPending = false;
+  if (*m->errHost) {
+    *m->errHost = 0;
+    cudaMemset(m->err, 0, sizeof(int));
+    setLastError("mixed path: a bounded device wait timed out");
+    return FG_ERR_TIMEOUT;
+  }
+  return FG_OK;
+}
 
 // ------------------------------------------------------------ TF32 split
 
@@ -222,15 +245,75 @@ struct GemmArgs {
   int nTiles, Npad, nn2, ncomp;
 };
 
-// Persistent: one CTA per SM, 4 warps; warp 0 owns the TMEM allocation,
-// thread 0 issues the MMAs, all 128 threads drain TMEM (thread = tile row).
+__device__ inline void cpAsync16(uint32_t dst, const void *src, uint32_t srcBytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(srcBytes) : "memory");
+}
+__device__ inline void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ inline void cpAsyncWaitAll() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// A tile of rows [row0, row0 + nrows) into the core-matrix image at As:
+// row r, 16-byte chunk kc -> core matrix (r/8, kc), K-direction stride 2048 B;
+// rows past nrows are zero-filled
+__device__ inline void loadATile(const GemmArgs &g, uint32_t As, int row0, int nrows, int tid) {
+  for (int c = tid; c < kBM * (kK3 / 4); c += kThreadsGemm) {
+    const int r = c / (kK3 / 4), kc = c % (kK3 / 4);
+    const bool live = r < nrows;
+    const float *src = g.A + (size_t)(row0 + (live ? r : 0)) * kK3 + kc * 4;
+    cpAsync16(As + kc * 2048 + (r >> 3) * 128 + (r & 7) * 16, src, live ? 16u : 0u);
+  }
+  cpAsyncCommit();
+}
+
+__device__ inline void loadB(const GemmArgs &g, float *Bs, int o, int tid) {
+  const float4 *src = reinterpret_cast<const float4 *>(g.B + (size_t)o * g.Npad * kK3);
+  float4 *dst = reinterpret_cast<float4 *>(Bs);
+  for (int k = tid; k < g.Npad * kK3 / 4; k += kThreadsGemm) dst[k] = src[k];
+}
+
+// drain columns [c0, c1) of this warp's 32 TMEM lanes into the element rows
+__device__ inline void drainColumns(const GemmArgs &g, uint32_t tmemRow, float *out, bool live, int c0, int c1) {
+  const bool vec = (g.nn2 & 3) == 0;
+  int c = c0;
+  for (; c + 32 <= c1; c += 32) {
+    float v[32];
+    tmemLoad32(tmemRow + (uint32_t)c, v);
+    if (live) {
+      if (vec && c + 32 <= g.nn2) {
+#pragma unroll
+        for (int k = 0; k < 32; k += 4) *reinterpret_cast<float4 *>(out + c + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+      } else {
+        for (int k = 0; k < 32; ++k)
+          if (c + k < g.nn2) out[c + k] = v[k];
+      }
+    }
+  }
+  if (c < c1) {
+    float v[16];
+    tmemLoad16(tmemRow + (uint32_t)c, v);
+    if (live) {
+      if (vec && c + 16 <= g.nn2) {
+#pragma unroll
+        for (int k = 0; k < 16; k += 4) *reinterpret_cast<float4 *>(out + c + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+      } else {
+        for (int k = 0; k < 16; ++k)
+          if (c + k < g.nn2) out[c + k] = v[k];
+      }
+    }
+  }
+}
+
+// Persistent: one CTA per SM, 8 warps. Warp 0 owns the TMEM allocation,
+// thread 0 issues the MMAs, all warps drain TMEM (warp w: lanes of quadrant
+// w % 4, half w / 4 of the columns). The next tile's A is fetched with
+// cp.async while the current tile computes and drains.
 __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmArgs g) {
   extern __shared__ __align__(1024) unsigned char smem[];
   float *Bs = reinterpret_cast<float *>(smem);                       // Npad * kK3
-  float *As = Bs + (size_t)g.Npad * kK3;                             // kBM * kK3
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(As + kBM * kK3);
+  float *As0 = Bs + (size_t)g.Npad * kK3;                            // 2 x kBM * kK3
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(As0 + 2 * kBM * kK3);
   uint32_t *tmemBase = reinterpret_cast<uint32_t *>(mbar + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quad = warp & 3, half = warp >> 2;
 
   if (warp == 0) {
     tmemAlloc(tmemBase, kTmemCols);
@@ -244,43 +327,40 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
   __syncthreads();
   tcFenceAfter();
   const uint32_t tmem = *tmemBase;
-  const uint32_t aBase = smemAddr(As), bBase = smemAddr(Bs);
+  const uint32_t aBase[2] = {smemAddr(As0), smemAddr(As0 + kBM * kK3)};
+  const uint32_t bBase = smemAddr(Bs);
   const uint32_t bLbo = (uint32_t)g.Npad * 16u;  // K-adjacent core matrices of B
-  int loadedOrient = -1;
+  const int colSplit = ((g.Npad / 2 + 15) / 16) * 16;
   uint32_t phase = 0;
   bool failed = false;
-
-  for (int t = blockIdx.x; t < g.nTiles && !failed; t += gridDim.x) {
+  int t = blockIdx.x;
+  if (t < g.nTiles) {
+    loadB(g, Bs, g.tiles[3 * t], tid);
+    loadATile(g, aBase[0], g.tiles[3 * t + 1], g.tiles[3 * t + 2], tid);
+  }
+  for (int it = 0; t < g.nTiles && !failed; ++it, t += gridDim.x) {
+    const int buf = it & 1;
     const int o = g.tiles[3 * t], row0 = g.tiles[3 * t + 1], nrows = g.tiles[3 * t + 2];
-    if (o != loadedOrient) {
-      // B' image of orientation o (already in core-matrix order)
-      const float4 *src = reinterpret_cast<const float4 *>(g.B + (size_t)o * g.Npad * kK3);
-      float4 *dst = reinterpret_cast<float4 *>(Bs);
-      for (int k = tid; k < g.Npad * kK3 / 4; k += kThreadsGemm) dst[k] = src[k];
-      loadedOrient = o;
-    }
-    // A tile: row r, 16-byte chunk kc -> core matrix (r/8, kc), K-direction stride 2048 B
-    for (int c = tid; c < kBM * (kK3 / 4); c += kThreadsGemm) {
-      const int r = c / (kK3 / 4), kc = c % (kK3 / 4);
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (r < nrows) v = reinterpret_cast<const float4 *>(g.A + (size_t)(row0 + r) * kK3)[kc];
-      *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(As) + kc * 2048 + (r >> 3) * 128 + (r & 7) * 16) = v;
-    }
+    cpAsyncWaitAll();
     fenceProxyAsync();
     __syncthreads();
     if (tid == 0) {
       tcFenceAfter();
-      for (int n0 = 0, chunk = 0; n0 < g.Npad; n0 += 256, ++chunk) {
+      for (int n0 = 0; n0 < g.Npad; n0 += 256) {
         const int nc = min(256, g.Npad - n0);
         const uint32_t idesc = idescTf32(kBM, nc);
         for (int ks = 0; ks < kK3 / 8; ++ks) {
-          const uint64_t ad = smemDesc(aBase + ks * 2 * 2048, 2048, 128);
+          const uint64_t ad = smemDesc(aBase[buf] + ks * 2 * 2048, 2048, 128);
           const uint64_t bd = smemDesc(bBase + ks * 2 * bLbo + (n0 >> 3) * 128, bLbo, 128);
           mmaTf32(tmem + (uint32_t)n0, ad, bd, idesc, ks > 0 ? 1u : 0u);
         }
       }
       mmaCommit(mbar);
     }
+    // prefetch the next tile's A (its B must be the one in shared memory)
+    const int tn = t + gridDim.x;
+    const bool nextSameB = tn < g.nTiles && g.tiles[3 * tn] == o;
+    if (nextSameB) loadATile(g, aBase[buf ^ 1], g.tiles[3 * tn + 1], g.tiles[3 * tn + 2], tid);
     __syncwarp();
     const bool ok = mbarWait(mbar, phase);
     failed = __syncthreads_or(ok ? 0 : 1) != 0;  // block-uniform
@@ -291,45 +371,24 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
     }
     tcFenceAfter();
     if (!failed) {
-      // epilogue: TMEM lane = tile row; warp w reads lanes [32w, 32w+32);
-      // each thread stores its own element row (contiguous in global memory)
-      const int r = warp * 32 + lane;
+      const int r = quad * 32 + lane;
       const bool live = r < nrows;
       const int grow = row0 + r;
       const int64_t e = live ? g.perm[grow / g.ncomp] : 0;
       float *out = g.ke + ((size_t)e * g.ncomp + (grow % g.ncomp)) * g.nn2;
-      const bool vec = (g.nn2 & 3) == 0;
-      int c0 = 0;
-      for (; c0 + 32 <= g.Npad; c0 += 32) {
-        float v[32];
-        tmemLoad32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-        if (live) {
-          if (vec && c0 + 32 <= g.nn2) {
-#pragma unroll
-            for (int k = 0; k < 32; k += 4) *reinterpret_cast<float4 *>(out + c0 + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
-          } else {
-            for (int k = 0; k < 32; ++k)
-              if (c0 + k < g.nn2) out[c0 + k] = v[k];
-          }
-        }
-      }
-      if (c0 < g.Npad) {  // a last 16-column chunk
-        float v[16];
-        tmemLoad16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-        if (live) {
-          if (vec && c0 + 16 <= g.nn2) {
-#pragma unroll
-            for (int k = 0; k < 16; k += 4) *reinterpret_cast<float4 *>(out + c0 + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
-          } else {
-            for (int k = 0; k < 16; ++k)
-              if (c0 + k < g.nn2) out[c0 + k] = v[k];
-          }
-        }
-      }
+      const uint32_t tmemRow = tmem + ((uint32_t)(quad * 32) << 16);
+      if (half == 0) drainColumns(g, tmemRow, out, live, 0, min(colSplit, g.Npad));
+      else drainColumns(g, tmemRow, out, live, min(colSplit, g.Npad), g.Npad);
     }
     tcFenceBefore();
     __syncthreads();
+    if (!failed && tn < g.nTiles && !nextSameB) {
+      // orientation change: the MMAs are done with Bs, reload it and the next A
+      loadB(g, Bs, g.tiles[3 * tn], tid);
+      loadATile(g, aBase[buf ^ 1], g.tiles[3 * tn + 1], g.tiles[3 * tn + 2], tid);
+    }
   }
+  cpAsyncWaitAll();
   if (failed) {
     // give the in-flight MMA chain a second bounded chance to retire (same
     // completion parity) before the TMEM is freed
@@ -339,6 +398,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
   tcFenceAfter();
   if (warp == 0) tmemDealloc(tmem, kTmemCols);
 }
+
 
 // ---------------------------------------------------- FP64 RHS (mixed)
 
@@ -494,7 +554,7 @@ static int prepareMixed(fg_plan *plan, int complexKe) {
       setLastError("mixed path: element matrix wider than the 512 TMEM columns");
       return FG_ERR_UNSUPPORTED;
     }
-    if ((size_t)m->Npad * kK3 * 4 + kBM * kK3 * 4 + 16 + 4 * 32 * 17 * 4 > 220 * 1024) {
+    if ((size_t)m->Npad * kK3 * 4 + 2 * kBM * kK3 * 4 + 16 > 220 * 1024) {
       setLastError("mixed path: element matrix too large for the shared-memory B tile");
       return FG_ERR_UNSUPPORTED;
     }
@@ -522,6 +582,9 @@ static int prepareMixed(fg_plan *plan, int complexKe) {
     FG_CUDA(cudaMemcpy(m->perm, perm.data(), (size_t)p.E * 4, cudaMemcpyHostToDevice));
     FG_CUDA(cudaMemcpy(m->perm + p.E, rank.data(), (size_t)p.E * 4, cudaMemcpyHostToDevice));
     FG_CUDA(cudaMalloc(&m->err, sizeof(int)));
+    FG_CUDA(cudaMallocHost(&m->errHost, sizeof(int)));
+    *m->errHost = 0;
+    FG_CUDA(cudaEventCreateWithFlags(&m->errEvent, cudaEventDisableTiming));
     FG_CUDA(cudaMemset(m->err, 0, sizeof(int)));
     m->built = 1;
   }
@@ -577,7 +640,7 @@ static int launchMixedElement(fg_plan *plan, const DevTerms &dt, cudaStream_t s)
   g.ncomp = ncomp;
   // at least half the SM's shared memory: one CTA per SM, so no CTA ever
   // waits in tcgen05.alloc for another one's 512 TMEM columns
-  const size_t smem = std::max<size_t>((size_t)m->Npad * kK3 * 4 + kBM * kK3 * 4 + 16 + 4 * 32 * 17 * 4, 116 * 1024);
+  const size_t smem = std::max<size_t>((size_t)m->Npad * kK3 * 4 + 2 * kBM * kK3 * 4 + 16, 116 * 1024);
   FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -605,6 +668,8 @@ extern "C" void mixedDestroy(fg_plan *plan) {
   cudaFree(m->tiles);
   cudaFree(m->ke);
   cudaFree(m->err);
+  if (m->errHost) cudaFreeHost(m->errHost);
+  if (m->errEvent) cudaEventDestroy(m->errEvent);
   delete m;
   plan->mixed = nullptr;
 }
@@ -622,6 +687,7 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
       return FG_ERR_UNSUPPORTED;
     }
   if ((st = prepareMixed(plan, dt.complexKe))) return st;
+  if ((st = checkTimeout(state(plan), false))) return st;  // a timeout of an earlier call
   const double *uD = nullptr;
   if ((st = uploadDirichlet(plan, dirichlet, &uD, s))) return st;
   Outputs o;
@@ -676,14 +742,13 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
     cudaFree(tmp);
     cudaFree(csr64);
   }
-  int herr = 0;
-  FG_CUDA(cudaMemcpyAsync(&herr, m->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  // the device error word comes back asynchronously: host outputs synchronize
+  // below and report it now; with device outputs the next call reports it
+  FG_CUDA(cudaMemcpyAsync(m->errHost, m->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaEventRecord(m->errEvent, s));
+  m->errPending = true;
   if ((st = finishOutputs(plan, o, csr_values, rhs, s))) return st;
-  FG_CUDA(cudaStreamSynchronize(s));
-  if (herr) {
-    setLastError("mixed path: a bounded device wait timed out");
-    return FG_ERR_TIMEOUT;
-  }
+  if (o.hostValues || (rhs && o.hostRhs)) return checkTimeout(m, true);
   return FG_OK;
 }
 

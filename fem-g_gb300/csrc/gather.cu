@@ -52,31 +52,36 @@ __global__ void __launch_bounds__(256)
     for (int k = 0; k < maxCnt; ++k) {
       const bool act = k < cnt;
       const uint32_t packed = act ? p.rowElem[r0 + k] : 0u;
-      const int64_t e = packed >> 6;
+      const uint32_t e32 = packed >> 6;
+      const int64_t e = e32;
       const int i = packed & 63;
-      const size_t rowOff = ((size_t)e * n + i) * n;
-      const KT *K = ke + (size_t)e * SS * nn2;
+      const uint32_t flat = e32 * (uint32_t)n + (uint32_t)i;  // element row index (< 2^32 by plan checks)
+      const SlotT *S = slot + (size_t)flat * n;
+      const KT *K = ke + (KCPLX ? ((size_t)e * 2 * nn2 + (size_t)i * n) : (size_t)flat * n);
       SlotT sv[J];
       KT vr[J], vi[J];
 #pragma unroll
       for (int jj = 0; jj < J; ++jj) {
         const int j = lt + L * jj;
         const bool ok = act && j < n;
-        sv[jj] = ok ? slot[rowOff + j] : kIgnore;
-        vr[jj] = ok ? K[i * n + j] : (KT)0;
-        vi[jj] = (ok && KCPLX) ? K[nn2 + i * n + j] : (KT)0;
+        sv[jj] = ok ? S[j] : kIgnore;
+        vr[jj] = ok ? K[j] : (KT)0;
+        vi[jj] = (ok && KCPLX) ? K[nn2 + j] : (KT)0;
       }
-      if (be && act && lt == 0) bsum = cadd(bsum, be[(size_t)e * n + i]);
+      if (be && act && lt == 0) bsum = cadd(bsum, be[flat]);
 #pragma unroll
       for (int jj = 0; jj < J; ++jj) {
         const SlotT s = sv[jj];
         if (s == kIgnore) continue;
         if (s != kFixed) {
-          A[(int)s * SS] += (AT)vr[jj];
-          if (KCPLX) A[(int)s * SS + 1] += (AT)vi[jj];
+          // the lanes of one element row hit distinct slots; entries are
+          // ordered by the __syncwarp below, so these adds are ordered too
+          atomicAdd(&A[(int)s * SS], (AT)vr[jj]);
+          if (KCPLX) atomicAdd(&A[(int)s * SS + 1], (AT)vi[jj]);
         } else {
+          const KT *Kt = ke + (size_t)e * SS * nn2;
           const int j = lt + L * jj;
-          const double2 v = make_double2((double)K[j * n + i], KCPLX ? (double)K[nn2 + j * n + i] : 0.0);
+          const double2 v = make_double2((double)Kt[j * n + i], KCPLX ? (double)Kt[nn2 + j * n + i] : 0.0);
           dc = cadd(dc, cmul(v, uD[p.edof[e * n + j]]));
         }
       }

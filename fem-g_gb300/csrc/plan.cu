@@ -34,14 +34,33 @@ struct ProfRecord {
 };
 std::mutex g_profMutex;
 std::vector<ProfRecord> g_prof;
+std::vector<cudaEvent_t> g_eventPool;  // events reused across launches
 std::atomic<bool> g_profOn{false};
+
+cudaEvent_t takeEvent() {
+  {
+    std::lock_guard<std::mutex> lk(g_profMutex);
+    if (!g_eventPool.empty()) {
+      cudaEvent_t e = g_eventPool.back();
+      g_eventPool.pop_back();
+      return e;
+    }
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return e;
+}
 }  // namespace
 
 ProfScope::ProfScope(const char *name, cudaStream_t s) : name_(name), s_(s) {
   if (!g_profOn.load()) return;
-  if (cudaEventCreate(&a_) != cudaSuccess || cudaEventCreate(&b_) != cudaSuccess) {
+  a_ = takeEvent();
+  b_ = takeEvent();
+  if (!a_ || !b_) {
     a_ = b_ = nullptr;
-    cudaGetLastError();
     return;
   }
   cudaEventRecord(a_, s_);
@@ -566,8 +585,11 @@ int fg_profile_read(char *names, int32_t name_bytes, int64_t *launches, double *
     float t = 0.0f;
     cudaEventSynchronize(r.b);
     cudaEventElapsedTime(&t, r.a, r.b);
-    cudaEventDestroy(r.a);
-    cudaEventDestroy(r.b);
+    {
+      std::lock_guard<std::mutex> lk(g_profMutex);
+      g_eventPool.push_back(r.a);
+      g_eventPool.push_back(r.b);
+    }
     size_t k = 0;
     while (k < order.size() && order[k] != r.name) ++k;
     if (k == order.size()) {
