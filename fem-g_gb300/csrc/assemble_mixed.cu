@@ -270,21 +270,34 @@ __device__ inline void loadB(const GemmArgs &g, float *Bs, int o, int tid) {
   for (int k = tid; k < g.Npad * kK3 / 4; k += kThreadsGemm) dst[k] = src[k];
 }
 
-// drain columns [c0, c1) of this warp's 32 TMEM lanes into the element rows
-__device__ inline void drainColumns(const GemmArgs &g, uint32_t tmemRow, float *out, bool live, int c0, int c1) {
+// drain columns [c0, c1) of this warp's 32 TMEM lanes into the element rows.
+// Full 32-column chunks go through a padded per-warp stage (32 rows x 36
+// floats) so that each float4 store instruction writes 4 rows x 128
+// contiguous bytes instead of 32 scattered 16-byte pieces.
+__device__ inline void drainColumns(const GemmArgs &g, uint32_t tmemRow, float *out, bool live, int c0, int c1, float *stage) {
+  const int lane = threadIdx.x & 31;
   const bool vec = (g.nn2 & 3) == 0;
   int c = c0;
   for (; c + 32 <= c1; c += 32) {
     float v[32];
     tmemLoad32(tmemRow + (uint32_t)c, v);
-    if (live) {
-      if (vec && c + 32 <= g.nn2) {
+    if (vec && c + 32 <= g.nn2) {
 #pragma unroll
-        for (int k = 0; k < 32; k += 4) *reinterpret_cast<float4 *>(out + c + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
-      } else {
-        for (int k = 0; k < 32; ++k)
-          if (c + k < g.nn2) out[c + k] = v[k];
+      for (int k = 0; k < 32; k += 4) *reinterpret_cast<float4 *>(stage + lane * 36 + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+      __syncwarp();
+      const int sub = lane >> 3, part = lane & 7;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int src = 4 * q + sub;
+        float *dst = reinterpret_cast<float *>(__shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(out), src));
+        const bool dlive = __shfl_sync(0xffffffffu, live ? 1 : 0, src) != 0;
+        const float4 val = *reinterpret_cast<const float4 *>(stage + src * 36 + 4 * part);
+        if (dlive) *reinterpret_cast<float4 *>(dst + c + 4 * part) = val;
       }
+      __syncwarp();
+    } else if (live) {
+      for (int k = 0; k < 32; ++k)
+        if (c + k < g.nn2) out[c + k] = v[k];
     }
   }
   if (c < c1) {
@@ -312,6 +325,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
   float *As0 = Bs + (size_t)g.Npad * kK3;                            // 2 x kBM * kK3
   uint64_t *mbar = reinterpret_cast<uint64_t *>(As0 + 2 * kBM * kK3);
   uint32_t *tmemBase = reinterpret_cast<uint32_t *>(mbar + 1);
+  float *Stage = reinterpret_cast<float *>(mbar + 2);                // 8 warps x 32 x 36 floats
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quad = warp & 3, half = warp >> 2;
 
@@ -377,8 +391,9 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
       const int64_t e = live ? g.perm[grow / g.ncomp] : 0;
       float *out = g.ke + ((size_t)e * g.ncomp + (grow % g.ncomp)) * g.nn2;
       const uint32_t tmemRow = tmem + ((uint32_t)(quad * 32) << 16);
-      if (half == 0) drainColumns(g, tmemRow, out, live, 0, min(colSplit, g.Npad));
-      else drainColumns(g, tmemRow, out, live, min(colSplit, g.Npad), g.Npad);
+      float *stage = Stage + warp * (32 * 36);
+      if (half == 0) drainColumns(g, tmemRow, out, live, 0, min(colSplit, g.Npad), stage);
+      else drainColumns(g, tmemRow, out, live, min(colSplit, g.Npad), g.Npad, stage);
     }
     tcFenceBefore();
     __syncthreads();
@@ -554,7 +569,7 @@ static int prepareMixed(fg_plan *plan, int complexKe) {
       setLastError("mixed path: element matrix wider than the 512 TMEM columns");
       return FG_ERR_UNSUPPORTED;
     }
-    if ((size_t)m->Npad * kK3 * 4 + 2 * kBM * kK3 * 4 + 16 > 220 * 1024) {
+    if ((size_t)m->Npad * kK3 * 4 + 2 * kBM * kK3 * 4 + 16 + 8 * 32 * 36 * 4 > 220 * 1024) {
       setLastError("mixed path: element matrix too large for the shared-memory B tile");
       return FG_ERR_UNSUPPORTED;
     }
@@ -640,7 +655,7 @@ static int launchMixedElement(fg_plan *plan, const DevTerms &dt, cudaStream_t s)
   g.ncomp = ncomp;
   // at least half the SM's shared memory: one CTA per SM, so no CTA ever
   // waits in tcgen05.alloc for another one's 512 TMEM columns
-  const size_t smem = std::max<size_t>((size_t)m->Npad * kK3 * 4 + 2 * kBM * kK3 * 4 + 16, 116 * 1024);
+  const size_t smem = std::max<size_t>((size_t)m->Npad * kK3 * 4 + 2 * kBM * kK3 * 4 + 16 + 8 * 32 * 36 * 4, 116 * 1024);
   FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);

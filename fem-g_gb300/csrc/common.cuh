@@ -156,6 +156,31 @@ __device__ inline double2 cdiv(double2 a, double2 b) {
   return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
 }
 
+// Exact FP32 -> FP64 widening with integer operations. The F2F instruction
+// runs on the FP64 pipe, which is narrow on GB300; the bit manipulation runs
+// on the integer pipes. Handles zeros, subnormals, infinities and NaNs.
+__device__ inline double widen(float x) {
+  const uint32_t b = __float_as_uint(x);
+  const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+  const uint32_t ex = (b >> 23) & 0xFFu;
+  uint32_t man = b & 0x7FFFFFu;
+  uint64_t bits;
+  if (ex == 0xFFu) {
+    bits = sign | (0x7FFull << 52) | ((uint64_t)man << 29);
+  } else if (ex != 0) {
+    bits = sign | ((uint64_t)(ex + 896u) << 52) | ((uint64_t)man << 29);  // 1023 - 127 = 896
+  } else if (man == 0) {
+    bits = sign;
+  } else {
+    // subnormal: value = man * 2^-149; normalise the leading one to bit 23
+    const int lz = __clz(man) - 8;  // shift that brings the leading one to bit 23
+    man = (man << lz) & 0x7FFFFFu;
+    bits = sign | ((uint64_t)(897 - lz) << 52) | ((uint64_t)man << 29);
+  }
+  return __longlong_as_double((long long)bits);
+}
+__device__ inline double widen(double x) { return x; }
+
 // Evaluate a coefficient expression at element e and physical point x
 __device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x) {
   if (ex.cls == kExprConst) return ex.cval;

@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(256)
       __syncwarp();
     }
     for (int s = lt; s < len; s += L)
-      values[start + s] = make_double2((double)A[s * SS], KCPLX ? (double)A[s * SS + 1] : 0.0);
+      values[start + s] = make_double2(widen(A[s * SS]), KCPLX ? widen(A[s * SS + 1]) : 0.0);
     if (rhs) {
 #pragma unroll
       for (int off = L / 2; off > 0; off >>= 1) {
