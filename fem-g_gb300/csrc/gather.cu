@@ -90,12 +90,16 @@ __global__ void __launch_bounds__(256)
     for (int s = lt; s < len; s += L)
       values[start + s] = make_double2(widen(A[s * SS]), KCPLX ? widen(A[s * SS + 1]) : 0.0);
     if (rhs) {
+      if (uD) {  // Dirichlet lifting present: reduce the lanes' lifted terms
 #pragma unroll
-      for (int off = L / 2; off > 0; off >>= 1) {
-        dc.x += __shfl_down_sync(0xffffffffu, dc.x, off, L);
-        dc.y += __shfl_down_sync(0xffffffffu, dc.y, off, L);
+        for (int off = L / 2; off > 0; off >>= 1) {
+          dc.x += __shfl_down_sync(0xffffffffu, dc.x, off, L);
+          dc.y += __shfl_down_sync(0xffffffffu, dc.y, off, L);
+        }
+        if (live && lt == 0) rhs[row] = cadd(bsum, dc);
+      } else if (live && lt == 0) {
+        rhs[row] = bsum;
       }
-      if (live && lt == 0) rhs[row] = cadd(bsum, dc);
     }
     __syncwarp();
   }
