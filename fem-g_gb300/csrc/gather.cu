@@ -49,25 +49,39 @@ __global__ void __launch_bounds__(256)
     for (int off = L; off < 32; off <<= 1) maxCnt = max(maxCnt, __shfl_xor_sync(0xffffffffu, maxCnt, off));
     __syncwarp();
     double2 dc = make_double2(0.0, 0.0), bsum = make_double2(0.0, 0.0);
-    for (int k = 0; k < maxCnt; ++k) {
+    // the row's (element, local index) list, L entries at a time in the lanes
+    uint32_t myPacked = (lt < cnt) ? p.rowElem[r0 + lt] : 0u;
+    // software pipeline: entry k+1's slots and values are in flight while
+    // entry k is added
+    SlotT sv[J], svN[J];
+    KT vr[J], vi[J], vrN[J], viN[J];
+    uint32_t flat = 0, flatN = 0;
+    auto fetch = [&](int k, uint32_t packed, SlotT *s_, KT *r_, KT *i_, uint32_t &f_) {
       const bool act = k < cnt;
-      const uint32_t packed = act ? p.rowElem[r0 + k] : 0u;
       const uint32_t e32 = packed >> 6;
-      const int64_t e = e32;
       const int i = packed & 63;
-      const uint32_t flat = e32 * (uint32_t)n + (uint32_t)i;  // element row index (< 2^32 by plan checks)
-      const SlotT *S = slot + (size_t)flat * n;
-      const KT *K = ke + (KCPLX ? ((size_t)e * 2 * nn2 + (size_t)i * n) : (size_t)flat * n);
-      SlotT sv[J];
-      KT vr[J], vi[J];
+      f_ = e32 * (uint32_t)n + (uint32_t)i;  // element row index (< 2^32 by plan checks)
+      const SlotT *S = slot + (size_t)f_ * n;
+      const KT *K = ke + (KCPLX ? ((size_t)e32 * 2 * nn2 + (size_t)i * n) : (size_t)f_ * n);
 #pragma unroll
       for (int jj = 0; jj < J; ++jj) {
         const int j = lt + L * jj;
         const bool ok = act && j < n;
-        sv[jj] = ok ? S[j] : kIgnore;
-        vr[jj] = ok ? K[j] : (KT)0;
-        vi[jj] = (ok && KCPLX) ? K[nn2 + j] : (KT)0;
+        s_[jj] = ok ? S[j] : kIgnore;
+        r_[jj] = ok ? K[j] : (KT)0;
+        i_[jj] = (ok && KCPLX) ? K[nn2 + j] : (KT)0;
       }
+    };
+    if (maxCnt > 0) fetch(0, __shfl_sync(0xffffffffu, myPacked, sub * L, 32), sv, vr, vi, flat);
+    for (int k = 0; k < maxCnt; ++k) {
+      const uint32_t packedK = __shfl_sync(0xffffffffu, myPacked, sub * L + (k % L), 32);
+      if (k + 1 < maxCnt) {
+        if ((k + 1) % L == 0) myPacked = (k + 1 + lt < cnt) ? p.rowElem[r0 + k + 1 + lt] : 0u;
+        fetch(k + 1, __shfl_sync(0xffffffffu, myPacked, sub * L + ((k + 1) % L), 32), svN, vrN, viN, flatN);
+      }
+      const bool act = k < cnt;
+      const int64_t e = packedK >> 6;
+      const int i = packedK & 63;
       if (be && act && lt == 0) bsum = cadd(bsum, be[flat]);
 #pragma unroll
       for (int jj = 0; jj < J; ++jj) {
@@ -86,6 +100,13 @@ __global__ void __launch_bounds__(256)
         }
       }
       __syncwarp();
+#pragma unroll
+      for (int jj = 0; jj < J; ++jj) {
+        sv[jj] = svN[jj];
+        vr[jj] = vrN[jj];
+        vi[jj] = viN[jj];
+      }
+      flat = flatN;
     }
     for (int s = lt; s < len; s += L)
       values[start + s] = make_double2(widen(A[s * SS]), KCPLX ? widen(A[s * SS + 1]) : 0.0);
