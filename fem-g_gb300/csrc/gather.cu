@@ -35,22 +35,26 @@ __global__ void __launch_bounds__(256)
   const size_t nn2 = (size_t)n * n;
   const int64_t nRows = (int64_t)p.nRows;
   const int64_t stride = (int64_t)gridDim.x * rowsPerBlock;
+  const int64_t first = (int64_t)blockIdx.x * rowsPerBlock + warp * R + sub;
+  uint4 vNext = first < nRows ? p.visit[first] : make_uint4(0, 0, 0, 0);
   for (int64_t base = (int64_t)blockIdx.x * rowsPerBlock + warp * R; base < nRows; base += stride) {
     const int64_t idx = base + sub;
     const bool live = idx < nRows;
-    const int64_t row = live ? (int64_t)p.rowOrder[idx] : 0;
-    const uint64_t start = live ? p.ai[row] : 0;
-    const int len = live ? (int)(p.ai[row + 1] - start) : 0;
+    const uint4 v = vNext;  // this row's record, fetched one iteration ahead
+    vNext = (idx + stride < nRows) ? p.visit[idx + stride] : make_uint4(0, 0, 0, 0);
+    const int64_t row = v.x;
+    const uint64_t start = v.y;
+    const int len = live ? (int)(v.w & 0xFFFFu) : 0;
+    const uint64_t r0 = v.z;
+    const int cnt = live ? (int)(v.w >> 16) : 0;
+    // the row's (element, local index) list, L entries at a time in the lanes
+    uint32_t myPacked = (lt < cnt) ? p.visitElem[r0 + lt] : 0u;
     for (int s = lt; s < len * SS; s += L) A[s] = (AT)0;
-    const uint64_t r0 = live ? p.rowPtr[row] : 0;
-    const int cnt = live ? (int)(p.rowPtr[row + 1] - r0) : 0;
     int maxCnt = cnt;
 #pragma unroll
     for (int off = L; off < 32; off <<= 1) maxCnt = max(maxCnt, __shfl_xor_sync(0xffffffffu, maxCnt, off));
     __syncwarp();
     double2 dc = make_double2(0.0, 0.0), bsum = make_double2(0.0, 0.0);
-    // the row's (element, local index) list, L entries at a time in the lanes
-    uint32_t myPacked = (lt < cnt) ? p.rowElem[r0 + lt] : 0u;
     // software pipeline: entry k+1's slots and values are in flight while
     // entry k is added
     SlotT sv[J], svN[J];
@@ -76,7 +80,7 @@ __global__ void __launch_bounds__(256)
     for (int k = 0; k < maxCnt; ++k) {
       const uint32_t packedK = __shfl_sync(0xffffffffu, myPacked, sub * L + (k % L), 32);
       if (k + 1 < maxCnt) {
-        if ((k + 1) % L == 0) myPacked = (k + 1 + lt < cnt) ? p.rowElem[r0 + k + 1 + lt] : 0u;
+        if ((k + 1) % L == 0) myPacked = (k + 1 + lt < cnt) ? p.visitElem[r0 + k + 1 + lt] : 0u;
         fetch(k + 1, __shfl_sync(0xffffffffu, myPacked, sub * L + ((k + 1) % L), 32), svN, vrN, viN, flatN);
       }
       const bool act = k < cnt;

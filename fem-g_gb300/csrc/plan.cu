@@ -231,9 +231,29 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
     for (uint64_t c = 0; c <= maxCnt; ++c) bucket[c + 1] += bucket[c];
     for (uint64_t r = 0; r < sys->n_rows; ++r) rowOrder[bucket[rowPtr[r + 1] - rowPtr[r]]++] = (uint32_t)r;
   }
-  if (sys->n_rows >= (uint64_t(1) << 32)) {
-    setLastError("fg_plan_create: more than 2^32 rows");
+  if (sys->n_rows >= (uint64_t(1) << 32) || d.nnz >= (uint64_t(1) << 32) || rowElem.size() >= (uint64_t(1) << 32)) {
+    setLastError("fg_plan_create: more than 2^32 rows, nonzeros or element rows in one plan");
     return FG_ERR_UNSUPPORTED;
+  }
+  // visit table: one 16-byte record per row in visiting order (row, CSR
+  // start, start of its element list, length | count << 16), the element
+  // lists stored contiguously in that order
+  std::vector<uint4> visit(sys->n_rows);
+  std::vector<uint32_t> visitElem(rowElem.size());
+  {
+    uint64_t pos = 0;
+    for (uint64_t v = 0; v < sys->n_rows; ++v) {
+      const uint32_t r = rowOrder[v];
+      const uint64_t cnt = rowPtr[r + 1] - rowPtr[r];
+      const uint64_t len = sys->ai[r + 1] - sys->ai[r];
+      if (cnt > 0xFFFF || len > 0xFFFF) {
+        setLastError("fg_plan_create: row with more than 65535 entries or contributions");
+        return FG_ERR_UNSUPPORTED;
+      }
+      std::copy(rowElem.begin() + (int64_t)rowPtr[r], rowElem.begin() + (int64_t)rowPtr[r + 1], visitElem.begin() + (int64_t)pos);
+      visit[v] = make_uint4(r, (uint32_t)sys->ai[r], (uint32_t)pos, (uint32_t)(len | (cnt << 16)));
+      pos += cnt;
+    }
   }
 
   // slots: position of each column inside its row
@@ -302,6 +322,8 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   if ((st = upload(plan, rowPtr.data(), rowPtr.size(), &d.rowPtr))) return st;
   if ((st = upload(plan, rowElem.data(), rowElem.size(), &d.rowElem))) return st;
   if ((st = upload(plan, rowOrder.data(), rowOrder.size(), &d.rowOrder))) return st;
+  if ((st = upload(plan, visit.data(), visit.size(), &d.visit))) return st;
+  if ((st = upload(plan, visitElem.data(), visitElem.size(), &d.visitElem))) return st;
   if (narrow) {
     const uint8_t *p;
     if ((st = upload(plan, slot8.data(), slot8.size(), &p))) return st;
