@@ -33,7 +33,7 @@ struct ElemWarpSmem {
 
 template <int MAXENT, bool CPLX>
 __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
-    k_element_fp64(const PlanDev p, const DevTerms terms, double *__restrict__ ke, double2 *__restrict__ be) {
+    k_element_fp64(const PlanDev p, const DevTerms *__restrict__ terms, double *__restrict__ ke, double2 *__restrict__ be) {
   __shared__ ElemWarpSmem smem[kWarpsPerBlockElem];
   __shared__ uint8_t pairI[kMaxDofs * (kMaxDofs + 1) / 2], pairJ[kMaxDofs * (kMaxDofs + 1) / 2];
   const int lane = threadIdx.x & 31;
@@ -78,8 +78,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
           xq[2] += g * S.X[3 * k + 2];
         }
         double2 cgg = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0), f = make_double2(0.0, 0.0);
-        for (int t = 0; t < terms.n; ++t) {
-          const DevTerm &T = terms.t[t];
+        for (int t = 0; t < terms->n; ++t) {
+          const DevTerm &T = terms->t[t];
           const double2 v = evalExpr(T.coef, e, xq);
           if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, v));
           else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, v));
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
   }
 }
 
-int launchElementFp64(fg_plan *plan, const DevTerms &terms, double *ke, double *be, cudaStream_t s) {
+int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s) {
   const PlanDev &p = plan->d;
   if (p.mult != 1 || terms.hasElastic) {
     setLastError("FP64 element kernel: compound fields go through the elastic kernel");
@@ -153,9 +153,7 @@ int launchElementFp64(fg_plan *plan, const DevTerms &terms, double *ke, double *
   }
   const int nEnt = p.nb * (p.nb + 1) / 2;
   const int perLane = (nEnt + 31) / 32;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = smCount();
   int64_t blocks = (p.E + kWarpsPerBlockElem - 1) / kWarpsPerBlockElem;
   blocks = std::min<int64_t>(blocks, (int64_t)sms * 64);
   if (blocks < 1) blocks = 1;
@@ -163,8 +161,8 @@ int launchElementFp64(fg_plan *plan, const DevTerms &terms, double *ke, double *
   double2 *be2 = (double2 *)be;
 #define FG_LAUNCH_ELEM(M)                                                                                   \
   do {                                                                                                      \
-    if (cplx) k_element_fp64<M, true><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, terms, ke, be2); \
-    else k_element_fp64<M, false><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, terms, ke, be2);  \
+    if (cplx) k_element_fp64<M, true><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, dterms, ke, be2); \
+    else k_element_fp64<M, false><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, dterms, ke, be2);  \
   } while (0)
   ProfScope prof("k_element_fp64", s);
   if (perLane <= 1) FG_LAUNCH_ELEM(1);
@@ -220,7 +218,8 @@ extern "C" int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_
   if (!plan) return FG_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   DevTerms dt;
-  int st = resolveTerms(plan, terms, n_terms, frequency, &dt);
+  const DevTerms *dterms = nullptr;
+  int st = resolveTerms(plan, terms, n_terms, frequency, &dt, &dterms, s);
   if (st) return st;
   const double *uD = nullptr;
   if ((st = uploadDirichlet(plan, dirichlet, &uD, s))) return st;
@@ -235,7 +234,7 @@ extern "C" int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_
     be = plan->be;
   }
   if (p.E > 0) {
-    if ((st = launchElementFp64(plan, dt, plan->ke, be, s))) return st;
+    if ((st = launchElementFp64(plan, dt, dterms, plan->ke, be, s))) return st;
   }
   if ((st = launchGather(plan, plan->ke, dt.complexKe, 0, be, uD, o.values, o.rhs, s))) return st;
   return finishOutputs(plan, o, csr_values, rhs, s);

@@ -191,7 +191,7 @@ __device__ inline void tmemLoad32(uint32_t taddr, float *v) {
 // elements: the geometric Jacobian is constant), per-element coefficients,
 // factors D_e split into TF32 hi/lo, written as row [hi | lo | hi] at the
 // element's rank in the orientation-sorted order.
-__global__ void k_factors(const PlanDev p, const DevTerms terms, const int32_t *__restrict__ rankOf, float *__restrict__ A,
+__global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf, float *__restrict__ A,
                           int ncomp) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= p.E) return;
@@ -209,8 +209,8 @@ __global__ void k_factors(const PlanDev p, const DevTerms terms, const int32_t *
   }
   double xc[3] = {0.0, 0.0, 0.0};  // coefficients are per element here: any point of it
   double2 cgg = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0);
-  for (int t = 0; t < terms.n; ++t) {
-    const DevTerm &T = terms.t[t];
+  for (int t = 0; t < terms->n; ++t) {
+    const DevTerm &T = terms->t[t];
     if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, evalExpr(T.coef, e, xc)));
     else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xc)));
   }
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
 // ---------------------------------------------------- FP64 RHS (mixed)
 
 // b_e[i] = sum_q w det conj(phi_i) f(x_q)  (LinearTerm::evaluate), warp per element
-__global__ void k_rhs_fp64(const PlanDev p, const DevTerms terms, double2 *__restrict__ be) {
+__global__ void k_rhs_fp64(const PlanDev p, const DevTerms *__restrict__ terms, double2 *__restrict__ be) {
   const int lane = threadIdx.x & 31;
   const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (e >= p.E) return;
@@ -436,8 +436,8 @@ __global__ void k_rhs_fp64(const PlanDev p, const DevTerms terms, double2 *__res
       for (int k = 0; k < p.nn; ++k)
         for (int c = 0; c < 3; ++c) xq[c] += p.geoVal[q * p.nn + k] * X[3 * k + c];
       double2 f = make_double2(0.0, 0.0);
-      for (int t = 0; t < terms.n; ++t)
-        if (terms.t[t].kind == FG_TERM_SOURCE) f = cadd(f, evalExpr(terms.t[t].coef, e, xq));
+      for (int t = 0; t < terms->n; ++t)
+        if (terms->t[t].kind == FG_TERM_SOURCE) f = cadd(f, evalExpr(terms->t[t].coef, e, xq));
       s = make_double2(p.w[q] * det * f.x, p.w[q] * det * f.y);
     }
     s.x = __shfl_sync(0xffffffffu, s.x, 0);
@@ -632,13 +632,13 @@ static int prepareMixed(fg_plan *plan, int complexKe) {
   return FG_OK;
 }
 
-static int launchMixedElement(fg_plan *plan, const DevTerms &dt, cudaStream_t s) {
+static int launchMixedElement(fg_plan *plan, const DevTerms &dt, const DevTerms *dterms, cudaStream_t s) {
   MixedState *m = state(plan);
   const PlanDev &p = plan->d;
   const int ncomp = dt.complexKe ? 2 : 1;
   {
     ProfScope prof("k_factors", s);
-    k_factors<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dt, m->perm + p.E, m->A, ncomp);
+    k_factors<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms, m->perm + p.E, m->A, ncomp);
     countLaunch();
     FG_CUDA(cudaGetLastError());
   }
@@ -656,10 +656,12 @@ static int launchMixedElement(fg_plan *plan, const DevTerms &dt, cudaStream_t s)
   // at least half the SM's shared memory: one CTA per SM, so no CTA ever
   // waits in tcgen05.alloc for another one's 512 TMEM columns
   const size_t smem = std::max<size_t>((size_t)m->Npad * kK3 * 4 + 2 * kBM * kK3 * 4 + 16 + 8 * 32 * 36 * 4, 116 * 1024);
-  FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  static size_t smemSet = 0;
+  if (smem > smemSet) {
+    FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    smemSet = smem;
+  }
+  const int sms = smCount();
   const int grid = std::max(1, std::min(sms, m->nTiles));
   {
     ProfScope prof("k_contract_tf32x3", s);
@@ -694,7 +696,8 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
   if (!plan) return FG_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   DevTerms dt;
-  int st = resolveTerms(plan, terms, n_terms, frequency, &dt);
+  const DevTerms *dterms = nullptr;
+  int st = resolveTerms(plan, terms, n_terms, frequency, &dt, &dterms, s);
   if (st) return st;
   for (int t = 0; t < dt.n; ++t)
     if (dt.t[t].kind != FG_TERM_SOURCE && dt.t[t].coef.cls == kExprPoint) {
@@ -715,19 +718,19 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
     be = plan->be;
     ProfScope prof("k_rhs_fp64", s);
     const int64_t threads = p.E * 32;
-    k_rhs_fp64<<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(p, dt, (double2 *)be);
+    k_rhs_fp64<<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(p, dterms, (double2 *)be);
     countLaunch();
     FG_CUDA(cudaGetLastError());
   }
   if (p.E > 0)
-    if ((st = launchMixedElement(plan, dt, s))) return st;
+    if ((st = launchMixedElement(plan, dt, dterms, s))) return st;
   if ((st = launchGather(plan, (const double *)m->ke, dt.complexKe, 1, be, uD, o.values, o.rhs, s))) return st;
   if (report) {
     // FP64 element matrices and CSR of the same terms, compared on the device
     const int ncomp = dt.complexKe ? 2 : 1;
     const size_t len = (size_t)ncomp * p.n * p.n;
     if ((st = ensureDevice((void **)&plan->ke, &plan->keBytes, (size_t)p.E * len * 8))) return st;
-    if ((st = launchElementFp64(plan, dt, plan->ke, nullptr, s))) return st;
+    if ((st = launchElementFp64(plan, dt, dterms, plan->ke, nullptr, s))) return st;
     double *tmp = nullptr, *csr64 = nullptr;
     FG_CUDA(cudaMalloc(&tmp, (size_t)std::max<int64_t>(p.E, 1024) * 16));
     FG_CUDA(cudaMalloc(&csr64, p.nnz * 16));

@@ -116,6 +116,8 @@ struct fg_plan {
   std::vector<void *> termArrays;   // device copies of per-element coefficient arrays (per call)
   std::vector<void *> boundArrays;  // ... of the terms bound by fg_plan_bind_terms
   femg::DevTerms bound;
+  femg::DevTerms *boundDev = nullptr;  // device copy of the bound terms
+  femg::DevTerms *termsDev = nullptr;  // device copy of the last per-call terms
   bool hasBound = false;
   // mixed-precision state (reference tensors per orientation), see assemble_mixed.cu
   void *mixed = nullptr;
@@ -129,7 +131,10 @@ int ensureDevice(void **ptr, size_t *cap, size_t bytes);
 int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double frequency, DevTerms *out,
                 std::vector<void *> &arrays);
 // terms of a call: uploaded now, or the bound ones when terms == NULL
-int resolveTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double frequency, DevTerms *out);
+int resolveTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double frequency, DevTerms *out,
+                 const DevTerms **dev, cudaStream_t s);
+// multiprocessor count of the current device (cached)
+int smCount();
 // copy the Dirichlet values; return device pointer (or null)
 int uploadDirichlet(fg_plan *plan, const double *dirichlet, const double **out, cudaStream_t s);
 bool isDevicePointer(const void *p);
@@ -144,7 +149,7 @@ struct Outputs {
 int prepareOutputs(fg_plan *plan, double *csr_values, double *rhs, Outputs *o);
 int finishOutputs(fg_plan *plan, const Outputs &o, double *csr_values, double *rhs, cudaStream_t s);
 // FP64 element kernel (also used as the reference for the mixed error report)
-int launchElementFp64(fg_plan *plan, const DevTerms &terms, double *ke, double *be, cudaStream_t s);
+int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s);
 
 // ------------------------------------------------------------- device helpers
 

@@ -150,15 +150,17 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
   }
   const size_t smem = rowBytes * R * wpb;
   const int rowsPerBlock = wpb * R;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = smCount();
   int64_t blocks = ((int64_t)p.nRows + rowsPerBlock - 1) / rowsPerBlock;
   blocks = std::min<int64_t>(blocks, (int64_t)sms * 16);
 #define FG_GATHER_L(LL)                                                                                           \
   case LL: {                                                                                                      \
     auto kern = k_gather<SlotT, KCPLX, KT, AT, LL>;                                                               \
-    FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                  \
+    static size_t smemSet = 0;                                                                                    \
+    if (smem > smemSet) {                                                                                         \
+      FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                \
+      smemSet = smem;                                                                                             \
+    }                                                                                                             \
     kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock);         \
     break;                                                                                                        \
   }

@@ -504,16 +504,32 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
   return FG_OK;
 }
 
-int resolveTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double frequency, DevTerms *out) {
+int resolveTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double frequency, DevTerms *out,
+                 const DevTerms **dev, cudaStream_t s) {
   if (!terms) {
     if (!plan->hasBound) {
       setLastError("no terms given and none bound to the plan");
       return FG_ERR_ARG;
     }
     *out = plan->bound;
+    *dev = plan->boundDev;
     return FG_OK;
   }
-  return uploadTerms(plan, terms, nTerms, frequency, out, plan->termArrays);
+  int st = uploadTerms(plan, terms, nTerms, frequency, out, plan->termArrays);
+  if (st) return st;
+  if (!plan->termsDev) FG_CUDA(cudaMalloc(&plan->termsDev, sizeof(DevTerms)));
+  FG_CUDA(cudaMemcpyAsync(plan->termsDev, out, sizeof(DevTerms), cudaMemcpyHostToDevice, s));
+  *dev = plan->termsDev;
+  return FG_OK;
+}
+
+int smCount() {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!cached[dev]) cudaDeviceGetAttribute(&cached[dev], cudaDevAttrMultiProcessorCount, dev);
+  return cached[dev] > 0 ? cached[dev] : 1;
 }
 
 }  // namespace femg
@@ -562,6 +578,8 @@ void fg_plan_destroy(fg_plan *plan) {
   for (void *p : plan->allocs) cudaFree(p);
   for (void *p : plan->termArrays) cudaFree(p);
   for (void *p : plan->boundArrays) cudaFree(p);
+  if (plan->boundDev) cudaFree(plan->boundDev);
+  if (plan->termsDev) cudaFree(plan->termsDev);
   if (plan->ke) cudaFree(plan->ke);
   if (plan->be) cudaFree(plan->be);
   if (plan->dirichlet) cudaFree(plan->dirichlet);
@@ -585,8 +603,11 @@ int fg_plan_bind_terms(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms
   if (!plan) return FG_ERR_ARG;
   plan->hasBound = false;
   int st = uploadTerms(plan, terms, n_terms, frequency, &plan->bound, plan->boundArrays);
-  if (st == FG_OK) plan->hasBound = true;
-  return st;
+  if (st != FG_OK) return st;
+  if (!plan->boundDev) FG_CUDA(cudaMalloc(&plan->boundDev, sizeof(DevTerms)));
+  FG_CUDA(cudaMemcpy(plan->boundDev, &plan->bound, sizeof(DevTerms), cudaMemcpyHostToDevice));
+  plan->hasBound = true;
+  return FG_OK;
 }
 
 int fg_profile_enable(int on) {
