@@ -229,7 +229,7 @@ class Problem:
 
     @property
     def nnz(self):
-        return int(self.ai[-1])
+        return int(self.sys.ai[self.sys.n_rows])  # one element, no copy
 
     def arrays(self):
         m, r, s, y = self.mesh, self.rule, self.space, self.sys
