@@ -145,11 +145,173 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
   }
 }
 
+// Compound (3-component) field with the isotropic Tensor4 term
+// integral(C * grad(dof(u)), grad(tf(u))) and the mass term: the Tensor4
+// evaluator of the reference (src/term/evaluator/EquationEvaluator.h:1267-1276,
+// CompoundFieldEvaluator<Form1,3> src/term/evaluator/FieldEvaluator.h:171-182)
+// with C_ijkl = lambda d_ij d_kl + mu (d_ik d_jl + d_il d_jk) gives, for the
+// test DOF (i, a) and the unknown DOF (j, b) (local index = basis * 3 + component),
+//   Ke = w det [ lambda dj_b di_a + mu d_ab (gi . gj) + mu dj_a di_b ] + w det c_m d_ab phi_i phi_j
+// with g = J^-T grad phi. Lanes own scalar basis pairs (i <= j) and their 3x3
+// blocks; the element matrix is symmetric.
+struct ElasticWarpSmem {
+  double X[kMaxNodes * 3];
+  double J[9], Jinv[9];
+  double det;
+  double2 lam, mu, cm, s;  // scaled by w det
+  double G[3][kMaxDofs / 3 + 1];
+  double phi[kMaxDofs / 3 + 1];
+};
+
+template <int MAXP, bool CPLX>
+__global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
+    k_element_elastic_fp64(const PlanDev p, const DevTerms *__restrict__ terms, double *__restrict__ ke, double2 *__restrict__ be) {
+  __shared__ ElasticWarpSmem smem[kWarpsPerBlockElem];
+  __shared__ uint8_t pairI[256], pairJ[256];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int ns = p.nb, n = 3 * ns;
+  const int nPairs = ns * (ns + 1) / 2;
+  for (int k = threadIdx.x; k < nPairs; k += blockDim.x) {
+    int i = 0, rem = k;
+    while (rem >= ns - i) {
+      rem -= ns - i;
+      ++i;
+    }
+    pairI[k] = (uint8_t)i;
+    pairJ[k] = (uint8_t)(i + rem);
+  }
+  __syncthreads();
+  ElasticWarpSmem &S = smem[warp];
+  const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlockElem;
+  for (int64_t e = (int64_t)blockIdx.x * kWarpsPerBlockElem + warp; e < p.E; e += stride) {
+    const int o = p.orient ? p.orient[e] : 0;
+    for (int t = lane; t < p.nn * 3; t += 32) S.X[t] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + t / 3] + t % 3];
+    __syncwarp();
+    double accR[MAXP][9], accI[MAXP][9];
+#pragma unroll
+    for (int m = 0; m < MAXP; ++m)
+#pragma unroll
+      for (int b = 0; b < 9; ++b) {
+        accR[m][b] = 0.0;
+        accI[m][b] = 0.0;
+      }
+    for (int q = 0; q < p.nq; ++q) {
+      if (lane == 0) {
+        if (q == 0 || !p.affine) {
+          S.det = jacobian(p.dim, p.nn, S.X, p.geoGrad + (size_t)q * p.nn * 3, S.J);
+          jacobianInverse(S.J, S.det, S.Jinv);
+        }
+        double xq[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < p.nn; ++k) {
+          const double g = p.geoVal[q * p.nn + k];
+          xq[0] += g * S.X[3 * k];
+          xq[1] += g * S.X[3 * k + 1];
+          xq[2] += g * S.X[3 * k + 2];
+        }
+        double2 lam = make_double2(0.0, 0.0), mu = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0);
+        for (int t = 0; t < terms->n; ++t) {
+          const DevTerm &T = terms->t[t];
+          if (T.kind == FG_TERM_ELASTIC) {
+            lam = cadd(lam, cmul(T.factor, evalExpr(T.coef, e, xq)));
+            mu = cadd(mu, cmul(T.factor, evalExpr(T.coef2, e, xq)));
+          } else if (T.kind == FG_TERM_MASS) {
+            cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xq)));
+          }
+        }
+        const double wd = p.w[q] * S.det;
+        S.lam = make_double2(wd * lam.x, wd * lam.y);
+        S.mu = make_double2(wd * mu.x, wd * mu.y);
+        S.cm = make_double2(wd * cm.x, wd * cm.y);
+      }
+      __syncwarp();
+      const size_t base = ((size_t)o * p.nq + q) * p.nb;
+      for (int i = lane; i < ns; i += 32) {
+        const double g0 = p.bgrad[3 * (base + i)], g1 = p.bgrad[3 * (base + i) + 1], g2 = p.bgrad[3 * (base + i) + 2];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) S.G[r][i] = S.Jinv[r] * g0 + S.Jinv[3 + r] * g1 + S.Jinv[6 + r] * g2;
+        S.phi[i] = p.bval[base + i];
+      }
+      __syncwarp();
+#pragma unroll
+      for (int m = 0; m < MAXP; ++m) {
+        const int k = lane + 32 * m;
+        if (k < nPairs) {
+          const int i = pairI[k], j = pairJ[k];
+          const double gi[3] = {S.G[0][i], S.G[1][i], S.G[2][i]};
+          const double gj[3] = {S.G[0][j], S.G[1][j], S.G[2][j]};
+          const double dot = gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2];
+          const double pp = S.phi[i] * S.phi[j];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+              const double tl = gj[b] * gi[a];
+              const double tm = gj[a] * gi[b] + (a == b ? dot : 0.0);
+              const double tc = a == b ? pp : 0.0;
+              accR[m][3 * a + b] += S.lam.x * tl + S.mu.x * tm + S.cm.x * tc;
+              if (CPLX) accI[m][3 * a + b] += S.lam.y * tl + S.mu.y * tm + S.cm.y * tc;
+            }
+        }
+      }
+      __syncwarp();
+    }
+    const int ncomp = CPLX ? 2 : 1;
+    double *K = ke + (size_t)e * ncomp * n * n;
+#pragma unroll
+    for (int m = 0; m < MAXP; ++m) {
+      const int k = lane + 32 * m;
+      if (k < nPairs) {
+        const int i = pairI[k], j = pairJ[k];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            const int ii = 3 * i + a, jj = 3 * j + b;  // test (i, a), unknown (j, b)
+            K[ii * n + jj] = accR[m][3 * a + b];
+            K[jj * n + ii] = accR[m][3 * a + b];
+            if (CPLX) {
+              K[n * n + ii * n + jj] = accI[m][3 * a + b];
+              K[n * n + jj * n + ii] = accI[m][3 * a + b];
+            }
+          }
+      }
+    }
+    if (be)
+      for (int i = lane; i < n; i += 32) be[(size_t)e * n + i] = make_double2(0.0, 0.0);
+    __syncwarp();
+  }
+}
+
 int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s) {
   const PlanDev &p = plan->d;
   if (p.mult != 1 || terms.hasElastic) {
-    setLastError("FP64 element kernel: compound fields go through the elastic kernel");
-    return FG_ERR_UNSUPPORTED;
+    if (p.mult != 3 || terms.hasSource) {
+      setLastError("FP64 element kernel: compound fields take the elastic and mass terms only");
+      return FG_ERR_UNSUPPORTED;
+    }
+    const int nPairs = p.nb * (p.nb + 1) / 2;
+    const int perLane = (nPairs + 31) / 32;
+    int64_t blocks = std::min<int64_t>((p.E + kWarpsPerBlockElem - 1) / kWarpsPerBlockElem, (int64_t)smCount() * 64);
+    if (blocks < 1) blocks = 1;
+    const bool cplx = terms.complexKe != 0;
+    ProfScope prof("k_element_elastic_fp64", s);
+#define FG_LAUNCH_EL(M)                                                                                                    \
+  do {                                                                                                                     \
+    if (cplx) k_element_elastic_fp64<M, true><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, dterms, ke, (double2 *)be); \
+    else k_element_elastic_fp64<M, false><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, dterms, ke, (double2 *)be); \
+  } while (0)
+    if (perLane <= 2) FG_LAUNCH_EL(2);
+    else if (perLane <= 4) FG_LAUNCH_EL(4);
+    else if (perLane <= 8) FG_LAUNCH_EL(8);
+    else {
+      setLastError("FP64 elastic kernel: more than 21 scalar basis functions per element");
+      return FG_ERR_UNSUPPORTED;
+    }
+#undef FG_LAUNCH_EL
+    countLaunch();
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
   }
   const int nEnt = p.nb * (p.nb + 1) / 2;
   const int perLane = (nEnt + 31) / 32;
@@ -236,6 +398,6 @@ extern "C" int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_
   if (p.E > 0) {
     if ((st = launchElementFp64(plan, dt, dterms, plan->ke, be, s))) return st;
   }
-  if ((st = launchGather(plan, plan->ke, dt.complexKe, 0, be, uD, o.values, o.rhs, s))) return st;
+  if ((st = launchGather(plan, plan->ke, dt.complexKe, 0, 1, be, uD, o.values, o.rhs, s))) return st;
   return finishOutputs(plan, o, csr_values, rhs, s);
 }

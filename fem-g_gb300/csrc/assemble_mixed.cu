@@ -38,7 +38,11 @@ struct MixedState {
   int complexKe = -1;
   int n = 0, nn2 = 0, Npad = 0;
   int nOrient = 0;
-  int64_t rows = 0;          // GEMM rows = E * ncomp
+  int blocks = 1;            // 9 component blocks per element for a compound field
+  int kp = 0, k3 = 0;        // factor columns and K' of the 3xTF32 chain
+  int rowsPerElem = 1;       // GEMM rows per element = ncomp * blocks
+  std::vector<int64_t> orientCount;
+  int64_t rows = 0;          // GEMM rows = E * rowsPerElem
   float *A = nullptr;        // [rows][kK3] row-major split factors
   size_t Abytes = 0;
   float *B = nullptr;        // [nOrient] smem images of B' (core-matrix layout)
@@ -187,8 +191,8 @@ __device__ inline void tmemLoad32(uint32_t taddr, float *v) {
 
 // ------------------------------------------------- geometry: factor rows
 
-// One thread per element: J, det, J^-1 in FP64 from the vertex nodes (affine
-// elements: the geometric Jacobian is constant), per-element coefficients,
+// One thread per element: J, det, J^-1 in FP64 from the element nodes at the
+// first quadrature point (affine elements: the geometric Jacobian is constant), per-element coefficients,
 // factors D_e split into TF32 hi/lo, written as row [hi | lo | hi] at the
 // element's rank in the orientation-sorted order.
 __global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf, float *__restrict__ A,
@@ -233,16 +237,75 @@ __global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, c
   }
 }
 
+// Compound field with the isotropic Tensor4 term: for every component pair
+// (a, b) (test component a, unknown component b) the block of the element
+// matrix is  Ke_ab[i][j] = sum_{p,p'} D_ab[p p'] S_{p p'}[i][j] + D_ab[9] M[i][j]
+// with S_{pp'}[i][j] = sum_q w d_p phi_j d_p' phi_i (reference gradients),
+// M = sum_q w phi_i phi_j and, with J^-1 = Ji (affine element),
+//   D_ab[p p'] = det (lambda Ji[p][b] Ji[p'][a] + mu Ji[p][a] Ji[p'][b] + mu d_ab K[p][p']),
+//   D_ab[9]   = det c_m d_ab,   K = Ji Ji^T.
+// 16 factor columns (10 used); rows (element, component of the coefficient,
+// block a*3+b) in the orientation-sorted element order.
+constexpr int kKpE = 16;
+constexpr int kK3E = 3 * kKpE;
+__global__ void k_factors_elastic(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
+                                  float *__restrict__ A, int ncomp) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.E) return;
+  double X[kMaxNodes * 3];
+  for (int k = 0; k < p.nn; ++k)
+    for (int c = 0; c < 3; ++c) X[3 * k + c] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + k] + c];
+  double J[9], Ji[9];
+  const double det = jacobian(p.dim, p.nn, X, p.geoGrad, J);
+  jacobianInverse(J, det, Ji);  // Ji[3p + a] = (J^-1)(p, a)
+  double K[9];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) K[3 * a + b] = Ji[3 * a] * Ji[3 * b] + Ji[3 * a + 1] * Ji[3 * b + 1] + Ji[3 * a + 2] * Ji[3 * b + 2];
+  double xc[3] = {0.0, 0.0, 0.0};
+  double2 lam = make_double2(0.0, 0.0), mu = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0);
+  for (int t = 0; t < terms->n; ++t) {
+    const DevTerm &T = terms->t[t];
+    if (T.kind == FG_TERM_ELASTIC) {
+      lam = cadd(lam, cmul(T.factor, evalExpr(T.coef, e, xc)));
+      mu = cadd(mu, cmul(T.factor, evalExpr(T.coef2, e, xc)));
+    } else if (T.kind == FG_TERM_MASS) {
+      cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xc)));
+    }
+  }
+  const int64_t r0 = (int64_t)rankOf[e] * ncomp * 9;
+  for (int comp = 0; comp < ncomp; ++comp) {
+    const double l = (comp == 0 ? lam.x : lam.y) * det, m = (comp == 0 ? mu.x : mu.y) * det;
+    const double c = (comp == 0 ? cm.x : cm.y) * det;
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) {
+        double d[kKpE];
+        for (int pp = 0; pp < 3; ++pp)
+          for (int q = 0; q < 3; ++q)
+            d[3 * pp + q] = l * Ji[3 * pp + b] * Ji[3 * q + a] + m * Ji[3 * pp + a] * Ji[3 * q + b] + (a == b ? m * K[3 * pp + q] : 0.0);
+        d[9] = a == b ? c : 0.0;
+        for (int k = 10; k < kKpE; ++k) d[k] = 0.0;
+        float *row = A + (r0 + comp * 9 + 3 * a + b) * kK3E;
+        for (int k = 0; k < kKpE; ++k) {
+          float hi, lo;
+          splitTf32(d[k], hi, lo);
+          row[k] = hi;
+          row[kKpE + k] = lo;
+          row[2 * kKpE + k] = hi;
+        }
+      }
+  }
+}
+
 // --------------------------------------------------- tcgen05 contraction
 
 struct GemmArgs {
-  const float *A;       // [rows][kK3]
-  const float *B;       // [nOrient][Npad * kK3] core-matrix images
+  const float *A;       // [rows][K3]
+  const float *B;       // [nOrient][Npad * K3] core-matrix images
   const int32_t *tiles; // [nTiles][3]
   const int32_t *perm;  // rank -> element
-  float *ke;            // [E][ncomp][nn2]
+  float *ke;            // [E][rowsPerElem][nn2]
   int *err;
-  int nTiles, Npad, nn2, ncomp;
+  int nTiles, Npad, nn2, rowsPerElem, K3;
 };
 
 __device__ inline void cpAsync16(uint32_t dst, const void *src, uint32_t srcBytes) {
@@ -255,19 +318,20 @@ __device__ inline void cpAsyncWaitAll() { asm volatile("cp.async.wait_all;" ::: 
 // row r, 16-byte chunk kc -> core matrix (r/8, kc), K-direction stride 2048 B;
 // rows past nrows are zero-filled
 __device__ inline void loadATile(const GemmArgs &g, uint32_t As, int row0, int nrows, int tid) {
-  for (int c = tid; c < kBM * (kK3 / 4); c += kThreadsGemm) {
-    const int r = c / (kK3 / 4), kc = c % (kK3 / 4);
+  const int chunks = g.K3 / 4;
+  for (int c = tid; c < kBM * chunks; c += kThreadsGemm) {
+    const int r = c / chunks, kc = c % chunks;
     const bool live = r < nrows;
-    const float *src = g.A + (size_t)(row0 + (live ? r : 0)) * kK3 + kc * 4;
+    const float *src = g.A + (size_t)(row0 + (live ? r : 0)) * g.K3 + kc * 4;
     cpAsync16(As + kc * 2048 + (r >> 3) * 128 + (r & 7) * 16, src, live ? 16u : 0u);
   }
   cpAsyncCommit();
 }
 
 __device__ inline void loadB(const GemmArgs &g, float *Bs, int o, int tid) {
-  const float4 *src = reinterpret_cast<const float4 *>(g.B + (size_t)o * g.Npad * kK3);
+  const float4 *src = reinterpret_cast<const float4 *>(g.B + (size_t)o * g.Npad * g.K3);
   float4 *dst = reinterpret_cast<float4 *>(Bs);
-  for (int k = tid; k < g.Npad * kK3 / 4; k += kThreadsGemm) dst[k] = src[k];
+  for (int k = tid; k < g.Npad * g.K3 / 4; k += kThreadsGemm) dst[k] = src[k];
 }
 
 // drain columns [c0, c1) of this warp's 32 TMEM lanes into the element rows.
@@ -321,9 +385,9 @@ __device__ inline void drainColumns(const GemmArgs &g, uint32_t tmemRow, float *
 // cp.async while the current tile computes and drains.
 __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmArgs g) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  float *Bs = reinterpret_cast<float *>(smem);                       // Npad * kK3
-  float *As0 = Bs + (size_t)g.Npad * kK3;                            // 2 x kBM * kK3
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(As0 + 2 * kBM * kK3);
+  float *Bs = reinterpret_cast<float *>(smem);                       // Npad * K3
+  float *As0 = Bs + (size_t)g.Npad * g.K3;                           // 2 x kBM * K3
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(As0 + 2 * kBM * g.K3);
   uint32_t *tmemBase = reinterpret_cast<uint32_t *>(mbar + 1);
   float *Stage = reinterpret_cast<float *>(mbar + 2);                // 8 warps x 32 x 36 floats
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -341,7 +405,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
   __syncthreads();
   tcFenceAfter();
   const uint32_t tmem = *tmemBase;
-  const uint32_t aBase[2] = {smemAddr(As0), smemAddr(As0 + kBM * kK3)};
+  const uint32_t aBase[2] = {smemAddr(As0), smemAddr(As0 + kBM * g.K3)};
   const uint32_t bBase = smemAddr(Bs);
   const uint32_t bLbo = (uint32_t)g.Npad * 16u;  // K-adjacent core matrices of B
   const int colSplit = ((g.Npad / 2 + 15) / 16) * 16;
@@ -363,7 +427,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
       for (int n0 = 0; n0 < g.Npad; n0 += 256) {
         const int nc = min(256, g.Npad - n0);
         const uint32_t idesc = idescTf32(kBM, nc);
-        for (int ks = 0; ks < kK3 / 8; ++ks) {
+        for (int ks = 0; ks < g.K3 / 8; ++ks) {
           const uint64_t ad = smemDesc(aBase[buf] + ks * 2 * 2048, 2048, 128);
           const uint64_t bd = smemDesc(bBase + ks * 2 * bLbo + (n0 >> 3) * 128, bLbo, 128);
           mmaTf32(tmem + (uint32_t)n0, ad, bd, idesc, ks > 0 ? 1u : 0u);
@@ -388,8 +452,8 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
       const int r = quad * 32 + lane;
       const bool live = r < nrows;
       const int grow = row0 + r;
-      const int64_t e = live ? g.perm[grow / g.ncomp] : 0;
-      float *out = g.ke + ((size_t)e * g.ncomp + (grow % g.ncomp)) * g.nn2;
+      const int64_t e = live ? g.perm[grow / g.rowsPerElem] : 0;
+      float *out = g.ke + ((size_t)e * g.rowsPerElem + (grow % g.rowsPerElem)) * g.nn2;
       const uint32_t tmemRow = tmem + ((uint32_t)(quad * 32) << 16);
       float *stage = Stage + warp * (32 * 36);
       if (half == 0) drainColumns(g, tmemRow, out, live, 0, min(colSplit, g.Npad), stage);
@@ -454,15 +518,25 @@ __global__ void k_rhs_fp64(const PlanDev p, const DevTerms *__restrict__ terms, 
 
 // -------------------------------------------- error report (device side)
 
-// per element ||Ke32 - Ke64||_F^2 and ||Ke64||_F^2
-__global__ void k_elem_err(const float *__restrict__ k32, const double *__restrict__ k64, int64_t E, int len, double *__restrict__ out) {
+// per element ||Ke32 - Ke64||_F^2 and ||Ke64||_F^2; the FP64 matrices are
+// row-major [ncomp][n][n], the FP32 ones row-major or (compound fields) in
+// 3x3 component blocks [ncomp][a*3+b][nb][nb]
+__global__ void k_elem_err(const float *__restrict__ k32, const double *__restrict__ k64, int64_t E, int len, int n, int blk3,
+                           double *__restrict__ out) {
   const int64_t e = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (e >= E) return;
+  const int nn = n * n, nb = n / 3;
   double d2 = 0.0, r2 = 0.0;
   for (int k = lane; k < len; k += 32) {
+    int o32 = k;
+    if (blk3) {
+      const int comp = k / nn, r = k - comp * nn, ii = r / n, jj = r - ii * n;
+      const int i = ii / 3, a = ii - 3 * i, j = jj / 3, b = jj - 3 * j;
+      o32 = comp * nn + ((a * 3 + b) * nb + i) * nb + j;
+    }
     const double a = k64[(size_t)e * len + k];
-    const double d = (double)k32[(size_t)e * len + k] - a;
+    const double d = (double)k32[(size_t)e * len + o32] - a;
     d2 += d * d;
     r2 += a * a;
   }
@@ -512,33 +586,44 @@ static MixedState *state(fg_plan *plan) {
 }
 
 // reference tensors T^o (FP64 on the host from the plan's basis tables), split
-// and laid out as the B' shared-memory image: row n (= i*n + j) of B' holds
-// its K' values; core matrix (n/8, kc) at kc * (Npad*16) + (n/8)*128, row n%8
-// at +16*(n%8)
+// and laid out as the B' shared-memory image: row r (= i*nb + j) of B' holds
+// its K' = 3*kp values; core matrix (r/8, kc) at kc * (Npad*16) + (r/8)*128,
+// row r%8 at +16*(r%8).
+//  scalar field (kp = 8):  T[ab] = sum_q w (d_a phi_j d_b phi_i + [a != b] d_b phi_j d_a phi_i)
+//                          for ab = 00,11,22,01,02,12, T[6] = sum_q w phi_i phi_j
+//  compound field (kp = 16): T[3p+p'] = sum_q w d_p phi_j d_p' phi_i, T[9] = sum_q w phi_i phi_j
 static void buildB(const PlanDev &p, const std::vector<double> &w, const std::vector<double> &bval, const std::vector<double> &bgrad,
-                   int o, int Npad, std::vector<float> &img) {
-  const int n = p.nb, nq = p.nq;
-  img.assign((size_t)Npad * kK3, 0.0f);
+                   int o, int Npad, int kp, std::vector<float> &img) {
+  const int nb = p.nb, nq = p.nq, k3 = 3 * kp;
+  img.assign((size_t)Npad * k3, 0.0f);
   const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) {
-      double T[kKp] = {0, 0, 0, 0, 0, 0, 0, 0};
+  std::vector<double> T(kp);
+  for (int i = 0; i < nb; ++i)
+    for (int j = 0; j < nb; ++j) {
+      std::fill(T.begin(), T.end(), 0.0);
       for (int q = 0; q < nq; ++q) {
-        const double *gi = &bgrad[(((size_t)o * nq + q) * n + i) * 3];
-        const double *gj = &bgrad[(((size_t)o * nq + q) * n + j) * 3];
-        for (int k = 0; k < 6; ++k) {
-          const int a = ab[k][0], b = ab[k][1];
-          T[k] += w[q] * (gj[a] * gi[b] + (a != b ? gj[b] * gi[a] : 0.0));
+        const double *gi = &bgrad[(((size_t)o * nq + q) * nb + i) * 3];
+        const double *gj = &bgrad[(((size_t)o * nq + q) * nb + j) * 3];
+        const double mass = w[q] * bval[((size_t)o * nq + q) * nb + i] * bval[((size_t)o * nq + q) * nb + j];
+        if (kp == kKp) {
+          for (int k = 0; k < 6; ++k) {
+            const int a = ab[k][0], b = ab[k][1];
+            T[k] += w[q] * (gj[a] * gi[b] + (a != b ? gj[b] * gi[a] : 0.0));
+          }
+          T[6] += mass;
+        } else {
+          for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) T[3 * a + b] += w[q] * gj[a] * gi[b];
+          T[9] += mass;
         }
-        T[6] += w[q] * bval[((size_t)o * nq + q) * n + i] * bval[((size_t)o * nq + q) * n + j];
       }
-      const int row = i * n + j;
-      for (int k = 0; k < kKp; ++k) {
+      const int row = i * nb + j;
+      for (int k = 0; k < kp; ++k) {
         float hi, lo;
         splitTf32(T[k], hi, lo);
         const float vals[3] = {hi, hi, lo};  // K' blocks: [B_hi ; B_hi ; B_lo]
         for (int blk = 0; blk < 3; ++blk) {
-          const int kk = blk * kKp + k;
+          const int kk = blk * kp + k;
           const int kc = kk >> 2, within = kk & 3;
           const size_t off = (size_t)kc * (Npad * 4) + (size_t)(row >> 3) * 32 + (row & 7) * 4 + within;  // in floats
           img[off] = vals[blk];
@@ -547,29 +632,38 @@ static void buildB(const PlanDev &p, const std::vector<double> &w, const std::ve
     }
 }
 
+static size_t gemmSmem(int Npad, int k3) {
+  // at least half the SM's shared memory: one CTA per SM, so no CTA ever
+  // waits in tcgen05.alloc for another one's 512 TMEM columns
+  return std::max<size_t>((size_t)Npad * k3 * 4 + 2 * kBM * k3 * 4 + 16 + 8 * 32 * 36 * 4, 116 * 1024);
+}
+
 static int prepareMixed(fg_plan *plan, int complexKe) {
   MixedState *m = state(plan);
   const PlanDev &p = plan->d;
   const int ncomp = complexKe ? 2 : 1;
   if (m->built && m->complexKe == complexKe) return FG_OK;
   if (!m->built) {
-    if (p.mult != 1) {
-      setLastError("mixed path: compound fields are not supported yet");
+    if (p.mult != 1 && p.mult != 3) {
+      setLastError("mixed path: fields of 1 or 3 components only");
       return FG_ERR_UNSUPPORTED;
     }
-    if (p.nn != p.dim + 1) {
-      setLastError("mixed path: needs affine (first-order geometry) elements");
+    if (!p.affine) {
+      setLastError("mixed path: needs geometrically affine (straight-sided) elements");
       return FG_ERR_UNSUPPORTED;
     }
+    m->blocks = p.mult == 3 ? 9 : 1;
+    m->kp = p.mult == 3 ? kKpE : kKp;
+    m->k3 = 3 * m->kp;
     m->n = p.n;
-    m->nn2 = p.n * p.n;
+    m->nn2 = p.nb * p.nb;  // one (block of the) element matrix per GEMM row
     m->Npad = (m->nn2 + 15) / 16 * 16;
     m->nOrient = p.nOrient;
     if (m->Npad > kTmemCols) {
       setLastError("mixed path: element matrix wider than the 512 TMEM columns");
       return FG_ERR_UNSUPPORTED;
     }
-    if ((size_t)m->Npad * kK3 * 4 + 2 * kBM * kK3 * 4 + 16 + 8 * 32 * 36 * 4 > 220 * 1024) {
+    if ((size_t)m->Npad * m->k3 * 4 + 2 * kBM * m->k3 * 4 + 16 + 8 * 32 * 36 * 4 > 220 * 1024) {
       setLastError("mixed path: element matrix too large for the shared-memory B tile");
       return FG_ERR_UNSUPPORTED;
     }
@@ -578,10 +672,10 @@ static int prepareMixed(fg_plan *plan, int complexKe) {
     FG_CUDA(cudaMemcpy(w.data(), p.w, w.size() * 8, cudaMemcpyDeviceToHost));
     FG_CUDA(cudaMemcpy(bval.data(), p.bval, bval.size() * 8, cudaMemcpyDeviceToHost));
     FG_CUDA(cudaMemcpy(bgrad.data(), p.bgrad, bgrad.size() * 8, cudaMemcpyDeviceToHost));
-    std::vector<float> all((size_t)p.nOrient * m->Npad * kK3), img;
+    std::vector<float> all((size_t)p.nOrient * m->Npad * m->k3), img;
     for (int o = 0; o < p.nOrient; ++o) {
-      buildB(p, w, bval, bgrad, o, m->Npad, img);
-      std::copy(img.begin(), img.end(), all.begin() + (size_t)o * m->Npad * kK3);
+      buildB(p, w, bval, bgrad, o, m->Npad, m->kp, img);
+      std::copy(img.begin(), img.end(), all.begin() + (size_t)o * m->Npad * m->k3);
     }
     FG_CUDA(cudaMalloc(&m->B, all.size() * 4));
     FG_CUDA(cudaMemcpy(m->B, all.data(), all.size() * 4, cudaMemcpyHostToDevice));
@@ -593,6 +687,8 @@ static int prepareMixed(fg_plan *plan, int complexKe) {
     std::stable_sort(perm.begin(), perm.end(), [&](int32_t a, int32_t b) { return orient[a] < orient[b]; });
     std::vector<int32_t> rank((size_t)p.E);
     for (int64_t r = 0; r < p.E; ++r) rank[perm[r]] = (int32_t)r;
+    m->orientCount.assign(p.nOrient, 0);
+    for (int64_t e = 0; e < p.E; ++e) m->orientCount[orient[e]]++;
     FG_CUDA(cudaMalloc(&m->perm, (size_t)p.E * 4 * 2));
     FG_CUDA(cudaMemcpy(m->perm, perm.data(), (size_t)p.E * 4, cudaMemcpyHostToDevice));
     FG_CUDA(cudaMemcpy(m->perm + p.E, rank.data(), (size_t)p.E * 4, cudaMemcpyHostToDevice));
@@ -603,28 +699,31 @@ static int prepareMixed(fg_plan *plan, int complexKe) {
     FG_CUDA(cudaMemset(m->err, 0, sizeof(int)));
     m->built = 1;
   }
-  // tiles (depend on the rows per element)
-  std::vector<int32_t> orient((size_t)p.E, 0);
-  if (p.orient) FG_CUDA(cudaMemcpy(orient.data(), p.orient, (size_t)p.E * 4, cudaMemcpyDeviceToHost));
-  std::vector<int64_t> count(p.nOrient, 0);
-  for (int64_t e = 0; e < p.E; ++e) count[orient[e]]++;
+  // tiles: rows of one orientation never share a tile
+  const int rowsPerElem = ncomp * m->blocks;
   std::vector<int32_t> tiles;
   int64_t start = 0;
   for (int o = 0; o < p.nOrient; ++o) {
-    const int64_t r0 = start * ncomp, r1 = (start + count[o]) * ncomp;
+    const int64_t r0 = start * rowsPerElem, r1 = (start + m->orientCount[o]) * rowsPerElem;
     for (int64_t r = r0; r < r1; r += kBM) {
       tiles.push_back(o);
       tiles.push_back((int32_t)r);
       tiles.push_back((int32_t)std::min<int64_t>(kBM, r1 - r));
     }
-    start += count[o];
+    start += m->orientCount[o];
+  }
+  if ((int64_t)p.E * rowsPerElem >= (int64_t(1) << 31)) {
+    setLastError("mixed path: more than 2^31 GEMM rows in one plan");
+    return FG_ERR_UNSUPPORTED;
   }
   if (m->tiles) cudaFree(m->tiles);
+  m->tiles = nullptr;
   FG_CUDA(cudaMalloc(&m->tiles, std::max<size_t>(tiles.size(), 3) * 4));
   FG_CUDA(cudaMemcpy(m->tiles, tiles.data(), tiles.size() * 4, cudaMemcpyHostToDevice));
   m->nTiles = (int)(tiles.size() / 3);
-  m->rows = p.E * ncomp;
-  int st = ensureDevice((void **)&m->A, &m->Abytes, (size_t)m->rows * kK3 * 4);
+  m->rowsPerElem = rowsPerElem;
+  m->rows = p.E * rowsPerElem;
+  int st = ensureDevice((void **)&m->A, &m->Abytes, (size_t)m->rows * m->k3 * 4);
   if (st) return st;
   st = ensureDevice((void **)&m->ke, &m->keBytes, (size_t)m->rows * m->nn2 * 4);
   if (st) return st;
@@ -638,7 +737,8 @@ static int launchMixedElement(fg_plan *plan, const DevTerms &dt, const DevTerms 
   const int ncomp = dt.complexKe ? 2 : 1;
   {
     ProfScope prof("k_factors", s);
-    k_factors<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms, m->perm + p.E, m->A, ncomp);
+    if (m->blocks == 9) k_factors_elastic<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms, m->perm + p.E, m->A, ncomp);
+    else k_factors<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms, m->perm + p.E, m->A, ncomp);
     countLaunch();
     FG_CUDA(cudaGetLastError());
   }
@@ -652,17 +752,15 @@ static int launchMixedElement(fg_plan *plan, const DevTerms &dt, const DevTerms 
   g.nTiles = m->nTiles;
   g.Npad = m->Npad;
   g.nn2 = m->nn2;
-  g.ncomp = ncomp;
-  // at least half the SM's shared memory: one CTA per SM, so no CTA ever
-  // waits in tcgen05.alloc for another one's 512 TMEM columns
-  const size_t smem = std::max<size_t>((size_t)m->Npad * kK3 * 4 + 2 * kBM * kK3 * 4 + 16 + 8 * 32 * 36 * 4, 116 * 1024);
+  g.rowsPerElem = m->rowsPerElem;
+  g.K3 = m->k3;
+  const size_t smem = gemmSmem(m->Npad, m->k3);
   static size_t smemSet = 0;
   if (smem > smemSet) {
     FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     smemSet = smem;
   }
-  const int sms = smCount();
-  const int grid = std::max(1, std::min(sms, m->nTiles));
+  const int grid = std::max(1, std::min(smCount(), m->nTiles));
   {
     ProfScope prof("k_contract_tf32x3", s);
     k_contract_tf32x3<<<grid, kThreadsGemm, smem, s>>>(g);
@@ -724,7 +822,7 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
   }
   if (p.E > 0)
     if ((st = launchMixedElement(plan, dt, dterms, s))) return st;
-  if ((st = launchGather(plan, (const double *)m->ke, dt.complexKe, 1, be, uD, o.values, o.rhs, s))) return st;
+  if ((st = launchGather(plan, (const double *)m->ke, dt.complexKe, 1, m->blocks, be, uD, o.values, o.rhs, s))) return st;
   if (report) {
     // FP64 element matrices and CSR of the same terms, compared on the device
     const int ncomp = dt.complexKe ? 2 : 1;
@@ -734,10 +832,10 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
     double *tmp = nullptr, *csr64 = nullptr;
     FG_CUDA(cudaMalloc(&tmp, (size_t)std::max<int64_t>(p.E, 1024) * 16));
     FG_CUDA(cudaMalloc(&csr64, p.nnz * 16));
-    k_elem_err<<<(unsigned)((p.E + 7) / 8), 256, 0, s>>>(m->ke, plan->ke, p.E, (int)len, tmp);
+    k_elem_err<<<(unsigned)((p.E + 7) / 8), 256, 0, s>>>(m->ke, plan->ke, p.E, (int)len, p.n, m->blocks == 9 ? 1 : 0, tmp);
     std::vector<double> h((size_t)p.E * 2);
     FG_CUDA(cudaMemcpyAsync(h.data(), tmp, h.size() * 8, cudaMemcpyDeviceToHost, s));
-    if ((st = launchGather(plan, plan->ke, dt.complexKe, 0, nullptr, uD, csr64, nullptr, s))) return st;
+    if ((st = launchGather(plan, plan->ke, dt.complexKe, 0, 1, nullptr, uD, csr64, nullptr, s))) return st;
     k_diff_norms<<<1024, 256, 0, s>>>(o.values, csr64, (int64_t)p.nnz * 2, tmp);
     std::vector<double> g(2048);
     FG_CUDA(cudaMemcpyAsync(g.data(), tmp, g.size() * 8, cudaMemcpyDeviceToHost, s));

@@ -139,7 +139,8 @@ int smCount();
 int uploadDirichlet(fg_plan *plan, const double *dirichlet, const double **out, cudaStream_t s);
 bool isDevicePointer(const void *p);
 // FP64 gather of element matrices/vectors into CSR values and RHS
-int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, const double *be,
+// keBlocks: 1 = element matrices row-major [n][n]; 9 = 3x3 component blocks
+int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
                  const double *dirichletDev, double *values, double *rhs, cudaStream_t s);
 // outputs: device pointers used in place, host pointers staged through the plan
 struct Outputs {

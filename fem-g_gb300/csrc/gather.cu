@@ -20,10 +20,19 @@ namespace femg {
 template <typename SlotT, bool KCPLX, typename KT, typename AT, int L>
 __global__ void __launch_bounds__(256)
     k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
-             double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock) {
+             double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock, int blk3) {
   constexpr int R = 32 / L;  // rows per warp
   constexpr int J = 3;       // columns per lane
   constexpr int SS = KCPLX ? 2 : 1;
+  // offset of entry (test ii, unknown jj) inside one component of an element
+  // matrix: row-major [n][n], or (compound fields from the tensor-core path)
+  // 3x3 blocks [a*3+b][nb][nb] with ii = i*3 + a, jj = j*3 + b
+  const int nbk = p.nb;
+  auto keOff = [&](int ii, int jj) -> int {
+    if (!blk3) return ii * p.n + jj;
+    const int i = ii / 3, a = ii - 3 * i, j = jj / 3, b = jj - 3 * j;
+    return ((a * 3 + b) * nbk + i) * nbk + j;
+  };
   extern __shared__ __align__(16) unsigned char smraw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / L, lt = lane % L;
@@ -66,14 +75,15 @@ __global__ void __launch_bounds__(256)
       const int i = packed & 63;
       f_ = e32 * (uint32_t)n + (uint32_t)i;  // element row index (< 2^32 by plan checks)
       const SlotT *S = slot + (size_t)f_ * n;
-      const KT *K = ke + (KCPLX ? ((size_t)e32 * 2 * nn2 + (size_t)i * n) : (size_t)f_ * n);
+      const KT *K = ke + (size_t)e32 * SS * nn2;
 #pragma unroll
       for (int jj = 0; jj < J; ++jj) {
         const int j = lt + L * jj;
         const bool ok = act && j < n;
+        const int o = keOff(i, j);
         s_[jj] = ok ? S[j] : kIgnore;
-        r_[jj] = ok ? K[j] : (KT)0;
-        i_[jj] = (ok && KCPLX) ? K[nn2 + j] : (KT)0;
+        r_[jj] = ok ? K[o] : (KT)0;
+        i_[jj] = (ok && KCPLX) ? K[nn2 + o] : (KT)0;
       }
     };
     if (maxCnt > 0) fetch(0, __shfl_sync(0xffffffffu, myPacked, sub * L, 32), sv, vr, vi, flat);
@@ -99,7 +109,8 @@ __global__ void __launch_bounds__(256)
         } else {
           const KT *Kt = ke + (size_t)e * SS * nn2;
           const int j = lt + L * jj;
-          const double2 v = make_double2((double)Kt[j * n + i], KCPLX ? (double)Kt[nn2 + j * n + i] : 0.0);
+          const int o = keOff(j, i);
+          const double2 v = make_double2((double)Kt[o], KCPLX ? (double)Kt[nn2 + o] : 0.0);
           dc = cadd(dc, cmul(v, uD[p.edof[e * n + j]]));
         }
       }
@@ -132,7 +143,7 @@ __global__ void __launch_bounds__(256)
 
 template <typename SlotT, bool KCPLX, typename KT>
 static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, const double2 *uD, double2 *values, double2 *rhs,
-                       cudaStream_t s) {
+                       int blk3, cudaStream_t s) {
   using AT = KT;  // FP32 element matrices accumulate in FP32, FP64 ones in FP64
   const int n = p.n;
   int L = 32;
@@ -161,7 +172,7 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
       FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                \
       smemSet = smem;                                                                                             \
     }                                                                                                             \
-    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock);         \
+    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock, blk3);   \
     break;                                                                                                        \
   }
   switch (L) {
@@ -176,8 +187,9 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
   return FG_OK;
 }
 
-int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, const double *be, const double *dirichletDev,
-                 double *values, double *rhs, cudaStream_t s) {
+int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+                 const double *dirichletDev, double *values, double *rhs, cudaStream_t s) {
+  const int blk3 = keBlocks == 9 ? 1 : 0;
   const PlanDev &p = plan->d;
   if (p.nRows == 0) return FG_OK;
   const double2 *be2 = (const double2 *)be;
@@ -188,12 +200,12 @@ int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, 
   countLaunch();
   if (p.slotBytes == 1) {
     if (keIsFloat)
-      return keComplex ? launchTyped<uint8_t, true, float>(p, ke, be2, uD, v2, r2, s) : launchTyped<uint8_t, false, float>(p, ke, be2, uD, v2, r2, s);
-    return keComplex ? launchTyped<uint8_t, true, double>(p, ke, be2, uD, v2, r2, s) : launchTyped<uint8_t, false, double>(p, ke, be2, uD, v2, r2, s);
+      return keComplex ? launchTyped<uint8_t, true, float>(p, ke, be2, uD, v2, r2, blk3, s) : launchTyped<uint8_t, false, float>(p, ke, be2, uD, v2, r2, blk3, s);
+    return keComplex ? launchTyped<uint8_t, true, double>(p, ke, be2, uD, v2, r2, blk3, s) : launchTyped<uint8_t, false, double>(p, ke, be2, uD, v2, r2, blk3, s);
   }
   if (keIsFloat)
-    return keComplex ? launchTyped<uint16_t, true, float>(p, ke, be2, uD, v2, r2, s) : launchTyped<uint16_t, false, float>(p, ke, be2, uD, v2, r2, s);
-  return keComplex ? launchTyped<uint16_t, true, double>(p, ke, be2, uD, v2, r2, s) : launchTyped<uint16_t, false, double>(p, ke, be2, uD, v2, r2, s);
+    return keComplex ? launchTyped<uint16_t, true, float>(p, ke, be2, uD, v2, r2, blk3, s) : launchTyped<uint16_t, false, float>(p, ke, be2, uD, v2, r2, blk3, s);
+  return keComplex ? launchTyped<uint16_t, true, double>(p, ke, be2, uD, v2, r2, blk3, s) : launchTyped<uint16_t, false, double>(p, ke, be2, uD, v2, r2, blk3, s);
 }
 
 }  // namespace femg

@@ -176,6 +176,35 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
     setLastError("fg_plan_create: element node index out of range");
     return FG_ERR_INDEX;
   }
+  // Geometrically affine elements (straight-sided second-order elements too):
+  // the Jacobian at every quadrature point equals the one at the first point.
+  if (!d.affine) {
+    int curved = 0;
+#pragma omp parallel for reduction(+ : curved)
+    for (int64_t e = 0; e < E; ++e) {
+      double J0[9] = {0}, scale = 0.0;
+      for (int q = 0; q < rule->nq && !curved; ++q) {
+        double J[9] = {0};
+        for (int k = 0; k < nn; ++k) {
+          const double *X = mesh->node_xyz + 3 * en[(size_t)(e * nn + k)];
+          for (int c = 0; c < mesh->dim; ++c) {
+            const double g = rule->geo_grad[((size_t)q * nn + k) * 3 + c];
+            for (int r = 0; r < 3; ++r) J[3 * c + r] += X[r] * g;
+          }
+        }
+        if (q == 0) {
+          for (int k = 0; k < 9; ++k) {
+            J0[k] = J[k];
+            scale = std::max(scale, std::fabs(J[k]));
+          }
+        } else {
+          for (int k = 0; k < 9; ++k)
+            if (std::fabs(J[k] - J0[k]) > 1e-13 * scale) curved = 1;
+        }
+      }
+    }
+    d.affine = curved ? 0 : 1;
+  }
   if (space->n_orientations > 1) {
     if (!space->elem_orientation) {
       setLastError("fg_plan_create: elem_orientation required with several orientations");

@@ -27,10 +27,14 @@ def cases(femg):
         "c2_m2_p4": femg.config_c2(m=2, order=4),
         "c3_m4": femg.config_c3(m=4),
         "tet_lagrange_p2": femg.config(dim=3, m=3, mesh_order=2, space=femg.FG_SPACE_LAGRANGE, gauss=4),
+        "c5_m2": femg.config_c5(m=2),
+        "c5_m3_p1": femg.config(kind=femg.FG_PROBLEM_NAVIER, dim=3, m=3, mesh_order=1, space=femg.FG_SPACE_HIERARCHICAL_H1,
+                                order=1, gauss=2, jitter=0.15, seed=9, omega=2.0, lame_sigma=0.5),
     }
 
 
-CASES = ["c1_m8", "c1_full", "c1_p1mesh_dirichlet1", "c2_m3", "c2_m4_p1", "c2_m3_p2", "c2_m2_p4", "c3_m4", "tet_lagrange_p2"]
+CASES = ["c1_m8", "c1_full", "c1_p1mesh_dirichlet1", "c2_m3", "c2_m4_p1", "c2_m3_p2", "c2_m2_p4", "c3_m4", "tet_lagrange_p2",
+         "c5_m2", "c5_m3_p1"]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -132,7 +136,7 @@ def test_full_size_c2_properties(femg, cuda):
     assert np.allclose(v.real, v.real[order[pos]], rtol=0, atol=1e-12 * np.abs(v.real).max())
 
 
-MIXED_CASES = ["c2_m3", "c2_m4_p1", "c2_m3_p2", "c3_m4", "c1_p1mesh_dirichlet1"]
+MIXED_CASES = ["c2_m3", "c2_m4_p1", "c2_m3_p2", "c3_m4", "c1_m8", "c1_full", "c1_p1mesh_dirichlet1", "c5_m2", "c5_m3_p1"]
 
 
 @pytest.mark.parametrize("case", MIXED_CASES)
