@@ -93,6 +93,7 @@ def lib():
         "fg_plan_bind_terms": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_double]),
         "fg_assemble_fp64": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_double, P, P, P, P]),
         "fg_assemble_mixed": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_double, P, P, P, P, C.POINTER(ErrReport)]),
+        "fg_assemble_fp64_static": (C.c_int, [P, P, P, P, P]),
         "fg_assemble_multi_freq": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, P, C.c_int32, C.c_int32, P, P]),
         "fg_batch_create": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.POINTER(P)]),
         "fg_batch_run": (C.c_int, [P, P, P, P]),
@@ -127,7 +128,7 @@ def exported_symbols():
     """Names bound above (the C ABI of both headers)."""
     return [
         "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_assemble_fp64", "fg_assemble_mixed",
-        "fg_assemble_multi_freq", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_profile_enable",
+        "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_profile_enable",
         "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
         "fg_problem_raw_dofs", "fg_problem_created_dofs", "fg_problem_reserve_log", "fg_problem_bbox", "fg_problem_pre_seconds", "fg_problem_assemble",

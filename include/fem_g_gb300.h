@@ -192,6 +192,23 @@ int fg_plan_bind_terms(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms
  * outputs it returns after the results are copied back. */
 int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency,
                      const double *dirichlet, double *csr_values, double *rhs, void *stream);
+/* No counterpart in the reference. fg_assemble_fp64 with bound terms, but it
+ * allocates nothing: its element-matrix and element-vector scratch is a
+ * file-scope device array of FG_STATIC_SCRATCH_BYTES per device (64 MiB), and
+ * csr_values, rhs (may be NULL) and dirichlet (NULL when n_fixed == 0) must be
+ * device memory. For callers that may not call cudaMalloc/cudaFree once set
+ * up: cudaFree synchronizes the whole device, which stalls a caller that
+ * overlaps the assembly of one step with the solve of the previous one on
+ * other streams, and a solver that owns the device memory pool allows no
+ * allocation from outside it. Requires fg_plan_bind_terms first. Returns
+ * FG_ERR_UNSUPPORTED when the scratch, E * (1 or 2 for complex) * n^2 * 8
+ * bytes plus E * n * 16 bytes with a source term and rhs, exceeds the array;
+ * FG_ERR_ARG for host outputs or no bound terms. The first call on a device
+ * resolves the array's address (cudaGetSymbolAddress, that device current):
+ * make it before any stream capture. The array is shared by all plans on a
+ * device: calls in flight at the same time on one device race on it. */
+#define FG_STATIC_SCRATCH_BYTES ((size_t)64 << 20)
+int fg_assemble_fp64_static(fg_plan *plan, const double *dirichlet, double *csr_values, double *rhs, void *stream);
 /* Mixed precision: FP64 geometry, 3xTF32 tcgen05 contraction with FP32
  * accumulation, FP64 CSR reduction. report may be NULL (no error report). */
 int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency,
