@@ -35,12 +35,12 @@ constexpr long long kWaitCycles = 4000000000LL;  // ~2 s bound on any device-sid
 
 struct MixedState {
   int built = 0;
-  int complexKe = -1;
+  int ncomp = 0, groups = 0;  // layout of the current tiles and buffers
   int n = 0, nn2 = 0, Npad = 0;
   int nOrient = 0;
   int blocks = 1;            // 9 component blocks per element for a compound field
   int kp = 0, k3 = 0;        // factor columns and K' of the 3xTF32 chain
-  int rowsPerElem = 1;       // GEMM rows per element = ncomp * blocks
+  int rowsPerElem = 1;       // GEMM rows per element = groups * ncomp * blocks
   std::vector<int64_t> orientCount;
   int64_t rows = 0;          // GEMM rows = E * rowsPerElem
   float *A = nullptr;        // [rows][kK3] row-major split factors
@@ -49,7 +49,7 @@ struct MixedState {
   int32_t *perm = nullptr;   // sorted rank -> element
   int32_t *tiles = nullptr;  // [nTiles][3]: orientation, first row, row count
   int nTiles = 0;
-  float *ke = nullptr;       // [E][ncomp][n][n] fp32
+  float *ke = nullptr;       // [E][groups][ncomp][n][n] fp32
   size_t keBytes = 0;
   int *err = nullptr;        // device error word (wait timeouts)
   int *errHost = nullptr;    // pinned copy of err
@@ -196,7 +196,7 @@ __device__ inline void tmemLoad32(uint32_t taddr, float *v) {
 // factors D_e split into TF32 hi/lo, written as row [hi | lo | hi] at the
 // element's rank in the orientation-sorted order.
 __global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf, float *__restrict__ A,
-                          int ncomp) {
+                          int ncomp, int rowsPerElem, int rowOff) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= p.E) return;
   double X[kMaxNodes * 3];
@@ -218,7 +218,7 @@ __global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, c
     if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, evalExpr(T.coef, e, xc)));
     else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xc)));
   }
-  const int64_t r0 = (int64_t)rankOf[e] * ncomp;
+  const int64_t r0 = (int64_t)rankOf[e] * rowsPerElem + rowOff;
   for (int comp = 0; comp < ncomp; ++comp) {
     const double g = (comp == 0 ? cgg.x : cgg.y) * det;
     const double m = (comp == 0 ? cm.x : cm.y) * det;
@@ -249,7 +249,7 @@ __global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, c
 constexpr int kKpE = 16;
 constexpr int kK3E = 3 * kKpE;
 __global__ void k_factors_elastic(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
-                                  float *__restrict__ A, int ncomp) {
+                                  float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= p.E) return;
   double X[kMaxNodes * 3];
@@ -272,7 +272,7 @@ __global__ void k_factors_elastic(const PlanDev p, const DevTerms *__restrict__ 
       cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xc)));
     }
   }
-  const int64_t r0 = (int64_t)rankOf[e] * ncomp * 9;
+  const int64_t r0 = (int64_t)rankOf[e] * rowsPerElem + rowOff;
   for (int comp = 0; comp < ncomp; ++comp) {
     const double l = (comp == 0 ? lam.x : lam.y) * det, m = (comp == 0 ? mu.x : mu.y) * det;
     const double c = (comp == 0 ? cm.x : cm.y) * det;
@@ -638,11 +638,13 @@ static size_t gemmSmem(int Npad, int k3) {
   return std::max<size_t>((size_t)Npad * k3 * 4 + 2 * kBM * k3 * 4 + 16 + 8 * 32 * 36 * 4, 116 * 1024);
 }
 
-static int prepareMixed(fg_plan *plan, int complexKe) {
+// Tables, tiles and buffers for element matrices of `groups` term groups
+// (one per frequency factor of the multi-frequency path; 1 otherwise), each
+// with ncomp (1 real, 2 complex) parts.
+int prepareMixed(fg_plan *plan, int ncomp, int groups) {
   MixedState *m = state(plan);
   const PlanDev &p = plan->d;
-  const int ncomp = complexKe ? 2 : 1;
-  if (m->built && m->complexKe == complexKe) return FG_OK;
+  if (m->built && m->ncomp == ncomp && m->groups == groups) return FG_OK;
   if (!m->built) {
     if (p.mult != 1 && p.mult != 3) {
       setLastError("mixed path: fields of 1 or 3 components only");
@@ -700,7 +702,7 @@ static int prepareMixed(fg_plan *plan, int complexKe) {
     m->built = 1;
   }
   // tiles: rows of one orientation never share a tile
-  const int rowsPerElem = ncomp * m->blocks;
+  const int rowsPerElem = groups * ncomp * m->blocks;
   std::vector<int32_t> tiles;
   int64_t start = 0;
   for (int o = 0; o < p.nOrient; ++o) {
@@ -727,18 +729,24 @@ static int prepareMixed(fg_plan *plan, int complexKe) {
   if (st) return st;
   st = ensureDevice((void **)&m->ke, &m->keBytes, (size_t)m->rows * m->nn2 * 4);
   if (st) return st;
-  m->complexKe = complexKe;
+  m->ncomp = ncomp;
+  m->groups = groups;
   return FG_OK;
 }
 
-static int launchMixedElement(fg_plan *plan, const DevTerms &dt, const DevTerms *dterms, cudaStream_t s) {
+// Factor rows of every term group (group g: rows g * ncomp * blocks onwards
+// within an element), then one tensor-core contraction over all of them into
+// m->ke ([E][groups][ncomp][n][n]).
+int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups, cudaStream_t s) {
   MixedState *m = state(plan);
   const PlanDev &p = plan->d;
-  const int ncomp = dt.complexKe ? 2 : 1;
-  {
+  const int ncomp = m->ncomp;
+  for (int gi = 0; gi < groups; ++gi) {
     ProfScope prof("k_factors", s);
-    if (m->blocks == 9) k_factors_elastic<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms, m->perm + p.E, m->A, ncomp);
-    else k_factors<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms, m->perm + p.E, m->A, ncomp);
+    const int off = gi * ncomp * m->blocks;
+    if (m->blocks == 9)
+      k_factors_elastic<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms[gi], m->perm + p.E, m->A, ncomp, m->rowsPerElem, off);
+    else k_factors<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms[gi], m->perm + p.E, m->A, ncomp, m->rowsPerElem, off);
     countLaunch();
     FG_CUDA(cudaGetLastError());
   }
@@ -767,6 +775,38 @@ static int launchMixedElement(fg_plan *plan, const DevTerms &dt, const DevTerms 
     countLaunch();
     FG_CUDA(cudaGetLastError());
   }
+  return FG_OK;
+}
+
+// FP64 element right-hand sides of the source terms into be ([E][n] complex)
+int launchRhsFp64(fg_plan *plan, const DevTerms *dterms, double *be, cudaStream_t s) {
+  const PlanDev &p = plan->d;
+  if (p.E == 0) return FG_OK;
+  ProfScope prof("k_rhs_fp64", s);
+  const int64_t threads = p.E * 32;
+  k_rhs_fp64<<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(p, dterms, (double2 *)be);
+  countLaunch();
+  FG_CUDA(cudaGetLastError());
+  return FG_OK;
+}
+
+// Accessors for the multi-frequency path
+float *mixedKe(fg_plan *plan, int *blocks) {
+  MixedState *m = state(plan);
+  *blocks = m->blocks;
+  return m->ke;
+}
+
+// Reports a wait timeout of an earlier call (wait == false) or of this one
+// (wait == true, after the outputs were copied back).
+int mixedCheckTimeout(fg_plan *plan, bool wait) { return checkTimeout(state(plan), wait); }
+
+// Queues the copy of the device error word behind this call's launches.
+int mixedRecordError(fg_plan *plan, cudaStream_t s) {
+  MixedState *m = state(plan);
+  FG_CUDA(cudaMemcpyAsync(m->errHost, m->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaEventRecord(m->errEvent, s));
+  m->errPending = true;
   return FG_OK;
 }
 
@@ -802,7 +842,7 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
       setLastError("mixed path: bilinear coefficients must be constant per element");
       return FG_ERR_UNSUPPORTED;
     }
-  if ((st = prepareMixed(plan, dt.complexKe))) return st;
+  if ((st = prepareMixed(plan, dt.complexKe ? 2 : 1, 1))) return st;
   if ((st = checkTimeout(state(plan), false))) return st;  // a timeout of an earlier call
   const double *uD = nullptr;
   if ((st = uploadDirichlet(plan, dirichlet, &uD, s))) return st;
@@ -821,7 +861,7 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
     FG_CUDA(cudaGetLastError());
   }
   if (p.E > 0)
-    if ((st = launchMixedElement(plan, dt, dterms, s))) return st;
+    if ((st = launchMixedElement(plan, &dterms, 1, s))) return st;
   if ((st = launchGather(plan, (const double *)m->ke, dt.complexKe, 1, m->blocks, be, uD, o.values, o.rhs, s))) return st;
   if (report) {
     // FP64 element matrices and CSR of the same terms, compared on the device
@@ -866,13 +906,6 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
   if ((st = finishOutputs(plan, o, csr_values, rhs, s))) return st;
   if (o.hostValues || (rhs && o.hostRhs)) return checkTimeout(m, true);
   return FG_OK;
-}
-
-extern "C" int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, const double *omegas, int32_t n_freq,
-                                      int32_t mixed, double *csr_values, void *stream) {
-  (void)plan; (void)terms; (void)n_terms; (void)omegas; (void)n_freq; (void)mixed; (void)csr_values; (void)stream;
-  femg::setLastError("fg_assemble_multi_freq: not built yet");
-  return FG_ERR_UNSUPPORTED;
 }
 
 extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const *terms, const int32_t *n_terms, int32_t n_problems,

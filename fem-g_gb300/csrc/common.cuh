@@ -121,6 +121,8 @@ struct fg_plan {
   bool hasBound = false;
   // mixed-precision state (reference tensors per orientation), see assemble_mixed.cu
   void *mixed = nullptr;
+  // multi-frequency state (term groups, element matrices), see multi_freq.cu
+  void *multi = nullptr;
 };
 
 namespace femg {
@@ -151,6 +153,13 @@ int prepareOutputs(fg_plan *plan, double *csr_values, double *rhs, Outputs *o);
 int finishOutputs(fg_plan *plan, const Outputs &o, double *csr_values, double *rhs, cudaStream_t s);
 // FP64 element kernel (also used as the reference for the mixed error report)
 int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s);
+// mixed path pieces shared with the multi-frequency path (assemble_mixed.cu)
+int prepareMixed(fg_plan *plan, int ncomp, int groups);
+int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups, cudaStream_t s);
+int launchRhsFp64(fg_plan *plan, const DevTerms *dterms, double *be, cudaStream_t s);
+float *mixedKe(fg_plan *plan, int *blocks);
+int mixedCheckTimeout(fg_plan *plan, bool wait);
+int mixedRecordError(fg_plan *plan, cudaStream_t s);
 
 // ------------------------------------------------------------- device helpers
 

@@ -1,0 +1,388 @@
+// Multi-frequency assembly: the system of the AFrequency module at n_freq
+// angular frequencies from one integration of the element matrices.
+//
+// The reference assembles one frequency per assemble() call: every term with a
+// time derivative is scaled by the module factor of the formulation's current
+// frequency, -omega^2 for dt2 and -i omega for dt1, before the element matrix
+// is summed (src/term/Assembler.cpp:263-305; AFrequencyModule,
+// src/system/MatrixModule.cpp:100-171). The terms split into at most three
+// groups by time derivative, K (none), C (dt) and M (dt2), whose element
+// matrices do not depend on the frequency. They are integrated once (FP64
+// element kernels, or the mixed-precision factor rows and one tensor-core
+// contraction over all groups), and one row-owner reduction accumulates the
+// group sums of each CSR row in shared memory and writes every frequency's
+//   values_f = K + (-i omega_f) C + (-omega_f^2) M
+// and right-hand side (sources, plus the Dirichlet lifting of each group
+// scaled the same way). The reduction visits the element rows in the order
+// of the single-frequency gather, so each group sum is deterministic.
+#include <cstring>
+
+#include "common.cuh"
+
+namespace femg {
+
+constexpr int kMaxGroups = 3;
+constexpr int kMaxFreq = 64;
+
+struct MultiIn {
+  const void *ke[kMaxGroups];    // element matrices of group g (KT)
+  int64_t stride[kMaxGroups];    // KT entries from one element to the next
+  int cplx[kMaxGroups];          // group g has an imaginary part (at +n*n)
+  int G, F, blk3;
+  const double2 *coef;           // [F][G] module factors
+  const double2 *be;             // [E][n] element right-hand sides or null
+  const double2 *uD;             // Dirichlet values or null
+  double2 *values;               // [F][nnz]
+  double2 *rhs;                  // [F][nRows] or null
+};
+
+template <typename SlotT, typename KT, int L>
+__global__ void __launch_bounds__(256)
+    k_gather_multi(const PlanDev p, const MultiIn in, int rowsPerBlock) {
+  using AT = KT;
+  constexpr int R = 32 / L;
+  constexpr int J = 3;
+  const int G = in.G, F = in.F;
+  const int nbk = p.nb;
+  const int blk3 = in.blk3;
+  auto keOff = [&](int ii, int jj) -> int {
+    if (!blk3) return ii * p.n + jj;
+    const int i = ii / 3, a = ii - 3 * i, j = jj / 3, b = jj - 3 * j;
+    return ((a * 3 + b) * nbk + i) * nbk + j;
+  };
+  extern __shared__ __align__(16) unsigned char smraw[];
+  AT *cf = reinterpret_cast<AT *>(smraw);  // [F][G][2] factors in the accumulation type
+  for (int k = threadIdx.x; k < F * G; k += blockDim.x) {
+    cf[2 * k] = (AT)in.coef[k].x;
+    cf[2 * k + 1] = (AT)in.coef[k].y;
+  }
+  __syncthreads();
+  const size_t cfBytes = ((size_t)F * G * 2 * sizeof(AT) + 15) / 16 * 16;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / L, lt = lane % L;
+  const int perSlot = 2 * G;
+  AT *A = reinterpret_cast<AT *>(smraw + cfBytes) + (size_t)(warp * R + sub) * p.maxRowLen * perSlot;
+  const SlotT *slot = (const SlotT *)p.slot;
+  const SlotT kFixed = (SlotT)(sizeof(SlotT) == 1 ? 0xFF : kSlotFixed);
+  const SlotT kIgnore = (SlotT)(sizeof(SlotT) == 1 ? 0xFE : kSlotIgnore);
+  const int n = p.n;
+  const int nn2 = n * n;
+  const int64_t nRows = (int64_t)p.nRows;
+  const int64_t stride = (int64_t)gridDim.x * rowsPerBlock;
+  for (int64_t base = (int64_t)blockIdx.x * rowsPerBlock + warp * R; base < nRows; base += stride) {
+    const int64_t idx = base + sub;
+    const bool live = idx < nRows;
+    const uint4 v = live ? p.visit[idx] : make_uint4(0, 0, 0, 0);
+    const int64_t row = v.x;
+    const uint64_t start = v.y;
+    const int len = live ? (int)(v.w & 0xFFFFu) : 0;
+    const uint64_t r0 = v.z;
+    const int cnt = live ? (int)(v.w >> 16) : 0;
+    for (int s = lt; s < len * perSlot; s += L) A[s] = (AT)0;
+    int maxCnt = cnt;
+#pragma unroll
+    for (int off = L; off < 32; off <<= 1) maxCnt = max(maxCnt, __shfl_xor_sync(0xffffffffu, maxCnt, off));
+    __syncwarp();
+    double2 dc[kMaxGroups];
+#pragma unroll
+    for (int g = 0; g < kMaxGroups; ++g) dc[g] = make_double2(0.0, 0.0);
+    double2 bsum = make_double2(0.0, 0.0);
+    for (int k = 0; k < maxCnt; ++k) {
+      if (k < cnt) {
+        const uint32_t packed = p.visitElem[r0 + k];
+        const int64_t e = packed >> 6;
+        const int i = packed & 63;
+        const SlotT *S = slot + ((size_t)e * n + i) * n;
+        if (in.be && lt == 0) bsum = cadd(bsum, in.be[e * n + i]);
+#pragma unroll
+        for (int jj = 0; jj < J; ++jj) {
+          const int j = lt + L * jj;
+          if (j >= n) continue;
+          const SlotT s = S[j];
+          if (s == kIgnore) continue;
+          if (s != kFixed) {
+            const int o = keOff(i, j);
+#pragma unroll
+            for (int g = 0; g < kMaxGroups; ++g) {
+              if (g >= G) break;
+              const KT *K = (const KT *)in.ke[g] + e * in.stride[g];
+              // distinct slots per lane within an element row; rows are
+              // separated by the __syncwarp below, so the adds are ordered
+              atomicAdd(&A[(int)s * perSlot + 2 * g], (AT)K[o]);
+              if (in.cplx[g]) atomicAdd(&A[(int)s * perSlot + 2 * g + 1], (AT)K[nn2 + o]);
+            }
+          } else {
+            // lifting with the transposed entry (VectorFactory::addValuesDC)
+            const int o = keOff(j, i);
+            const double2 u = in.uD[p.edof[e * n + j]];
+#pragma unroll
+            for (int g = 0; g < kMaxGroups; ++g) {
+              if (g >= G) break;
+              const KT *K = (const KT *)in.ke[g] + e * in.stride[g];
+              const double2 kv = make_double2((double)K[o], in.cplx[g] ? (double)K[nn2 + o] : 0.0);
+              dc[g] = cadd(dc[g], cmul(kv, u));
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+    for (int s = lt; s < len; s += L) {
+      AT ar[kMaxGroups], ai[kMaxGroups];
+#pragma unroll
+      for (int g = 0; g < kMaxGroups; ++g) {
+        ar[g] = g < G ? A[s * perSlot + 2 * g] : (AT)0;
+        ai[g] = g < G ? A[s * perSlot + 2 * g + 1] : (AT)0;
+      }
+      for (int f = 0; f < F; ++f) {
+        AT re = (AT)0, im = (AT)0;
+#pragma unroll
+        for (int g = 0; g < kMaxGroups; ++g) {
+          if (g >= G) break;
+          const AT cr = cf[2 * (f * G + g)], ci = cf[2 * (f * G + g) + 1];
+          re += cr * ar[g] - ci * ai[g];
+          im += cr * ai[g] + ci * ar[g];
+        }
+        in.values[(size_t)f * p.nnz + start + s] = make_double2(widen(re), widen(im));
+      }
+    }
+    if (in.rhs) {
+      if (in.uD) {
+#pragma unroll
+        for (int g = 0; g < kMaxGroups; ++g)
+#pragma unroll
+          for (int off = L / 2; off > 0; off >>= 1) {
+            dc[g].x += __shfl_down_sync(0xffffffffu, dc[g].x, off, L);
+            dc[g].y += __shfl_down_sync(0xffffffffu, dc[g].y, off, L);
+          }
+      }
+      if (live && lt == 0)
+        for (int f = 0; f < F; ++f) {
+          double2 r = bsum;
+#pragma unroll
+          for (int g = 0; g < kMaxGroups; ++g)
+            if (g < G) r = cadd(r, cmul(in.coef[f * G + g], dc[g]));
+          in.rhs[(size_t)f * p.nRows + row] = r;
+        }
+    }
+    __syncwarp();
+  }
+}
+
+template <typename SlotT, typename KT>
+static int launchMultiTyped(const PlanDev &p, const MultiIn &in, cudaStream_t s) {
+  const int n = p.n;
+  int L = 32;
+  if (n <= 6) L = 2;
+  else if (n <= 12) L = 4;
+  else if (n <= 24) L = 8;
+  else if (n <= 48) L = 16;
+  const int R = 32 / L;
+  const size_t cfBytes = ((size_t)in.F * in.G * 2 * sizeof(KT) + 15) / 16 * 16;
+  const size_t rowBytes = (size_t)std::max(p.maxRowLen, 1) * 2 * in.G * sizeof(KT);
+  int wpb = 8;
+  while (wpb > 1 && cfBytes + rowBytes * R * wpb > 200 * 1024) wpb >>= 1;
+  const size_t smem = cfBytes + rowBytes * R * wpb;
+  if (smem > 200 * 1024) {
+    setLastError("multi-frequency gather: CSR row too long for shared memory");
+    return FG_ERR_UNSUPPORTED;
+  }
+  const int rowsPerBlock = wpb * R;
+  int64_t blocks = ((int64_t)p.nRows + rowsPerBlock - 1) / rowsPerBlock;
+  blocks = std::min<int64_t>(blocks, (int64_t)smCount() * 16);
+#define FG_MULTI_L(LL)                                                                             \
+  case LL: {                                                                                       \
+    auto kern = k_gather_multi<SlotT, KT, LL>;                                                     \
+    static size_t smemSet = 0;                                                                     \
+    if (smem > smemSet) {                                                                          \
+      FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+      smemSet = smem;                                                                              \
+    }                                                                                              \
+    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, in, rowsPerBlock);                            \
+    break;                                                                                         \
+  }
+  switch (L) {
+    FG_MULTI_L(2)
+    FG_MULTI_L(4)
+    FG_MULTI_L(8)
+    FG_MULTI_L(16)
+    FG_MULTI_L(32)
+  }
+#undef FG_MULTI_L
+  FG_CUDA(cudaGetLastError());
+  return FG_OK;
+}
+
+static int launchGatherMulti(fg_plan *plan, const MultiIn &in, bool isFloat, cudaStream_t s) {
+  const PlanDev &p = plan->d;
+  if (p.nRows == 0) return FG_OK;
+  ProfScope prof("k_gather_multi", s);
+  countLaunch();
+  if (p.slotBytes == 1)
+    return isFloat ? launchMultiTyped<uint8_t, float>(p, in, s) : launchMultiTyped<uint8_t, double>(p, in, s);
+  return isFloat ? launchMultiTyped<uint16_t, float>(p, in, s) : launchMultiTyped<uint16_t, double>(p, in, s);
+}
+
+struct MultiState {
+  DevTerms terms[kMaxGroups];
+  DevTerms *dev[kMaxGroups] = {nullptr, nullptr, nullptr};
+  std::vector<void *> arrays[kMaxGroups];
+  double *ke[kMaxGroups] = {nullptr, nullptr, nullptr};
+  size_t keBytes[kMaxGroups] = {0, 0, 0};
+  double2 *coef = nullptr;
+  double *values = nullptr, *rhs = nullptr;  // staging for host outputs
+  size_t valuesBytes = 0, rhsBytes = 0;
+};
+
+static MultiState *multiState(fg_plan *plan) {
+  if (!plan->multi) plan->multi = new MultiState();
+  return (MultiState *)plan->multi;
+}
+
+}  // namespace femg
+
+using namespace femg;
+
+extern "C" void multiDestroy(fg_plan *plan) {
+  MultiState *m = (MultiState *)plan->multi;
+  if (!m) return;
+  for (int g = 0; g < kMaxGroups; ++g) {
+    for (void *p : m->arrays[g]) cudaFree(p);
+    cudaFree(m->dev[g]);
+    cudaFree(m->ke[g]);
+  }
+  cudaFree(m->coef);
+  cudaFree(m->values);
+  cudaFree(m->rhs);
+  delete m;
+  plan->multi = nullptr;
+}
+
+extern "C" int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, const double *omegas, int32_t n_freq,
+                                      int32_t mixed, const double *dirichlet, double *csr_values, double *rhs, void *stream) {
+  if (!plan) return FG_ERR_ARG;
+  if (!terms || n_terms <= 0 || n_terms > kMaxTerms || !omegas || n_freq <= 0 || n_freq > kMaxFreq || !csr_values) {
+    setLastError("fg_assemble_multi_freq: terms, 1..64 frequencies and csr_values are required");
+    return FG_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  MultiState *m = multiState(plan);
+  const PlanDev &p = plan->d;
+  // groups by time derivative; the module factor is applied in the reduction
+  int dts[kMaxGroups], G = 0;
+  fg_term_desc grp[kMaxTerms];
+  for (int d = FG_DT_NONE; d <= FG_DT_2; ++d) {
+    int cnt = 0;
+    for (int t = 0; t < n_terms; ++t) {
+      if (terms[t].dt < FG_DT_NONE || terms[t].dt > FG_DT_2) {
+        setLastError("fg_assemble_multi_freq: unknown time derivative");
+        return FG_ERR_ARG;
+      }
+      if (terms[t].kind == FG_TERM_SOURCE && terms[t].dt != FG_DT_NONE) {
+        setLastError("a linear term cannot carry a time derivative");
+        return FG_ERR_ARG;
+      }
+      if (terms[t].dt == d) {
+        grp[cnt] = terms[t];
+        grp[cnt].dt = FG_DT_NONE;
+        ++cnt;
+      }
+    }
+    if (!cnt) continue;
+    int st = uploadTerms(plan, grp, cnt, 0.0, &m->terms[G], m->arrays[G]);
+    if (st) return st;
+    if (!m->dev[G]) FG_CUDA(cudaMalloc(&m->dev[G], sizeof(DevTerms)));
+    FG_CUDA(cudaMemcpyAsync(m->dev[G], &m->terms[G], sizeof(DevTerms), cudaMemcpyHostToDevice, s));
+    dts[G++] = d;
+  }
+  std::vector<double2> coef((size_t)n_freq * G);
+  for (int f = 0; f < n_freq; ++f)
+    for (int g = 0; g < G; ++g) {
+      const double w = omegas[f];
+      coef[(size_t)f * G + g] = dts[g] == FG_DT_2 ? make_double2(-w * w, 0.0) : dts[g] == FG_DT_1 ? make_double2(0.0, -w) : make_double2(1.0, 0.0);
+    }
+  if (!m->coef) FG_CUDA(cudaMalloc(&m->coef, (size_t)kMaxFreq * kMaxGroups * sizeof(double2)));
+  FG_CUDA(cudaMemcpyAsync(m->coef, coef.data(), coef.size() * sizeof(double2), cudaMemcpyHostToDevice, s));
+  const double *uD = nullptr;
+  int st = uploadDirichlet(plan, dirichlet, &uD, s);
+  if (st) return st;
+  // outputs: device pointers in place, host pointers through staging buffers
+  const bool hostValues = !isDevicePointer(csr_values);
+  const bool hostRhs = rhs && !isDevicePointer(rhs);
+  double *dValues = csr_values, *dRhs = rhs;
+  if (hostValues) {
+    if ((st = ensureDevice((void **)&m->values, &m->valuesBytes, (size_t)n_freq * p.nnz * 16))) return st;
+    dValues = m->values;
+  }
+  if (hostRhs) {
+    if ((st = ensureDevice((void **)&m->rhs, &m->rhsBytes, (size_t)n_freq * p.nRows * 16))) return st;
+    dRhs = m->rhs;
+  }
+  // source terms are linear terms without time derivative: group of dt 0
+  const int g0 = dts[0] == FG_DT_NONE ? 0 : -1;
+  double *be = nullptr;
+  const bool source = g0 == 0 && m->terms[0].hasSource && rhs;
+  if (source) {
+    if ((st = ensureDevice((void **)&plan->be, &plan->beBytes, (size_t)p.E * p.n * 16))) return st;
+    be = plan->be;
+  }
+  MultiIn in;
+  std::memset(&in, 0, sizeof(in));
+  in.G = G;
+  in.F = n_freq;
+  in.coef = m->coef;
+  in.be = (const double2 *)be;
+  in.uD = (const double2 *)uD;
+  in.values = (double2 *)dValues;
+  in.rhs = (double2 *)dRhs;
+  const size_t nn = (size_t)p.n * p.n;
+  bool isFloat = false;
+  if (!mixed) {
+    for (int g = 0; g < G; ++g) {
+      const int ncomp = m->terms[g].complexKe ? 2 : 1;
+      if ((st = ensureDevice((void **)&m->ke[g], &m->keBytes[g], (size_t)p.E * ncomp * nn * sizeof(double)))) return st;
+      if (p.E > 0)
+        if ((st = launchElementFp64(plan, m->terms[g], m->dev[g], m->ke[g], g == g0 && source ? be : nullptr, s))) return st;
+      in.ke[g] = m->ke[g];
+      in.stride[g] = (int64_t)(ncomp * nn);
+      in.cplx[g] = ncomp == 2;
+    }
+  } else {
+    int ncomp = 1;
+    for (int g = 0; g < G; ++g) {
+      if (m->terms[g].complexKe) ncomp = 2;
+      for (int t = 0; t < m->terms[g].n; ++t)
+        if (m->terms[g].t[t].kind != FG_TERM_SOURCE && m->terms[g].t[t].coef.cls == kExprPoint) {
+          setLastError("mixed path: bilinear coefficients must be constant per element");
+          return FG_ERR_UNSUPPORTED;
+        }
+    }
+    if ((st = prepareMixed(plan, ncomp, G))) return st;
+    if ((st = mixedCheckTimeout(plan, false))) return st;
+    if (source)
+      if ((st = launchRhsFp64(plan, m->dev[0], be, s))) return st;
+    if (p.E > 0) {
+      const DevTerms *devs[kMaxGroups] = {m->dev[0], m->dev[1], m->dev[2]};
+      if ((st = launchMixedElement(plan, devs, G, s))) return st;
+    }
+    int blocks = 1;
+    const float *ke = mixedKe(plan, &blocks);
+    for (int g = 0; g < G; ++g) {
+      in.ke[g] = ke + (size_t)g * ncomp * nn;
+      in.stride[g] = (int64_t)((size_t)G * ncomp * nn);
+      in.cplx[g] = ncomp == 2 && m->terms[g].complexKe;
+    }
+    in.blk3 = blocks == 9 ? 1 : 0;
+    isFloat = true;
+  }
+  if ((st = launchGatherMulti(plan, in, isFloat, s))) return st;
+  if (mixed)
+    if ((st = mixedRecordError(plan, s))) return st;
+  if (hostValues) FG_CUDA(cudaMemcpyAsync(csr_values, dValues, (size_t)n_freq * p.nnz * 16, cudaMemcpyDeviceToHost, s));
+  if (hostRhs) FG_CUDA(cudaMemcpyAsync(rhs, dRhs, (size_t)n_freq * p.nRows * 16, cudaMemcpyDeviceToHost, s));
+  if (hostValues || hostRhs) {
+    FG_CUDA(cudaStreamSynchronize(s));
+    if (mixed) return mixedCheckTimeout(plan, true);
+  }
+  return FG_OK;
+}

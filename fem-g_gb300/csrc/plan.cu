@@ -601,6 +601,7 @@ int fg_plan_create(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_
 }
 
 void mixedDestroy(fg_plan *plan);
+void multiDestroy(fg_plan *plan);
 
 void fg_plan_destroy(fg_plan *plan) {
   if (!plan) return;
@@ -615,6 +616,7 @@ void fg_plan_destroy(fg_plan *plan) {
   if (plan->values) cudaFree(plan->values);
   if (plan->rhs) cudaFree(plan->rhs);
   mixedDestroy(plan);
+  multiDestroy(plan);
   delete plan;
 }
 

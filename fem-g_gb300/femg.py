@@ -94,7 +94,7 @@ def lib():
         "fg_assemble_fp64": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_double, P, P, P, P]),
         "fg_assemble_mixed": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_double, P, P, P, P, C.POINTER(ErrReport)]),
         "fg_assemble_fp64_static": (C.c_int, [P, P, P, P, P]),
-        "fg_assemble_multi_freq": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, P, C.c_int32, C.c_int32, P, P]),
+        "fg_assemble_multi_freq": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, P, C.c_int32, C.c_int32, P, P, P, P]),
         "fg_batch_create": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.POINTER(P)]),
         "fg_batch_run": (C.c_int, [P, P, P, P]),
         "fg_batch_destroy": (None, [P]),
@@ -331,7 +331,26 @@ class Plan:
         t, nt = self.prob.terms()
         check(lib().fg_plan_bind_terms(self.ptr, t, nt, frequency))
 
-    def assemble(self, precision="fp64", values=None, rhs=None, bound=False, frequency=0.0, stream=None, report=False):
+    def assemble_multi_freq(self, omegas, precision="fp64", terms=None, values=None, rhs=None, stream=None):
+        """fg_assemble_multi_freq: (values [F][nnz], rhs [F][n_rows]) for the
+        angular frequencies omegas (numpy outputs unless device pointers)."""
+        p = self.prob
+        om = np.ascontiguousarray(omegas, dtype=np.float64)
+        F = len(om)
+        if values is None:
+            values = np.zeros((F, p.nnz), np.complex128)
+        if rhs is None:
+            rhs = np.zeros((F, int(p.sys.n_rows)), np.complex128)
+        vptr = values if isinstance(values, int) else values.ctypes.data
+        rptr = rhs if isinstance(rhs, int) else (rhs.ctypes.data if rhs is not False else None)
+        t, nt = terms if terms is not None else p.terms()
+        dptr = C.cast(p.dir_ptr, C.c_void_p) if p.sys.n_fixed else None
+        check(lib().fg_assemble_multi_freq(self.ptr, t, nt, om.ctypes.data, F, 1 if precision == "mixed" else 0, dptr,
+                                           vptr, rptr, stream))
+        return values, rhs
+
+    def assemble(self, precision="fp64", values=None, rhs=None, bound=False, frequency=0.0, stream=None, report=False,
+                 terms=None):
         """Assemble into numpy arrays (host outputs) or raw device pointers
         (ints); returns (values, rhs[, report])."""
         L = lib()
@@ -344,7 +363,7 @@ class Plan:
             rhs = np.zeros(nrows, np.complex128)
         vptr = values if isinstance(values, int) else values.ctypes.data
         rptr = rhs if isinstance(rhs, int) else (rhs.ctypes.data if rhs is not False else None)
-        t, nt = (None, 0) if bound else p.terms()
+        t, nt = (None, 0) if bound else (terms if terms is not None else p.terms())
         dptr = C.cast(p.dir_ptr, C.c_void_p) if p.sys.n_fixed else None
         if precision == "fp64":
             check(L.fg_assemble_fp64(self.ptr, t, nt, frequency, dptr, vptr, rptr, stream))

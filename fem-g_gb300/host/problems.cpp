@@ -71,7 +71,8 @@ static void buildProblem(fg_problem *p) {
     }
     Tensor4Isotropic C{Function::perElement(lam), Function::perElement(mu)};
     f.integral(C * grad(dof(u)), grad(tf(u)), omega, gauss);
-    f.integral(Function(-c.omega * c.omega) * dof(u), tf(u), omega, gauss);  // rho = 1
+    if (c.omega > 0.0) f.integral(Function(-c.omega * c.omega) * dof(u), tf(u), omega, gauss);  // rho = 1
+    else f.integral(dt2_dof(u), tf(u), omega, gauss);  // frequency of the assemble call (AFrequency)
   } else {
     throw std::invalid_argument("unknown problem kind");
   }

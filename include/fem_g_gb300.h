@@ -215,10 +215,19 @@ int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms,
                       const double *dirichlet, double *csr_values, double *rhs, void *stream,
                       fg_err_report *report);
 
-/* Several frequencies sharing K_e and M_e: values[f] = K - omega_f^2 * M
- * assembled for n_freq frequencies in one pass (csr_values: [n_freq][nnz][2]). */
+/* The system at n_freq angular frequencies in one pass: what n_freq calls of
+ * fg_assemble_fp64 (mixed == 0) or fg_assemble_mixed (mixed != 0) with
+ * frequency = omegas[f] produce, i.e. what the reference's assemble() gives
+ * after each change of the formulation's frequency (AFrequency module,
+ * src/term/Assembler.cpp:263-305; src/system/MatrixModule.cpp:100-171). The
+ * terms are split by time derivative into at most three groups whose element
+ * matrices are integrated once; the row-owner reduction then writes
+ *   values[f] = K + (-i omega_f) C + (-omega_f^2) M
+ * for every frequency. csr_values: [n_freq][nnz][2]; rhs: [n_freq][n_rows][2]
+ * or NULL; host or device memory (detected); dirichlet as in fg_assemble_fp64. */
 int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, const double *omegas,
-                           int32_t n_freq, int32_t mixed, double *csr_values, void *stream);
+                           int32_t n_freq, int32_t mixed, const double *dirichlet, double *csr_values, double *rhs,
+                           void *stream);
 
 /* -------------------------------------------------------------- batching */
 

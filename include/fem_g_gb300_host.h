@@ -44,7 +44,8 @@ typedef struct {
   int32_t dirichlet; /* 1: u = dirichlet_value on the boundary curves (2D) */
   double dirichlet_value;
   int32_t source;    /* 1: f = heaviside(0.01 - (x-.5)^2 - (y-.5)^2) as integral(-f, tf(u)) */
-  double omega;      /* Navier: frequency of the mass term -omega^2 rho dof(u) */
+  double omega;      /* Navier: frequency of the mass term -omega^2 rho dof(u); <= 0: the mass
+                        term is integral(dt2_dof(u), tf(u)) and the frequency is the assemble call's */
   double lame_sigma; /* Navier: lambda, mu lognormal(median 1, sigma) per element */
 } fg_problem_config;
 
