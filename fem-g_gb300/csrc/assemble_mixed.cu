@@ -47,8 +47,12 @@ struct MixedState {
   size_t Abytes = 0;
   float *B = nullptr;        // [nOrient] smem images of B' (core-matrix layout)
   int32_t *perm = nullptr;   // sorted rank -> element
-  int32_t *tiles = nullptr;  // [nTiles][3]: orientation, first row, row count
+  int4 *tiles = nullptr;     // [nTiles]: problem 0, orientation, first row, row count
   int nTiles = 0;
+  int32_t *ctaStart = nullptr;  // contiguous tile ranges of the persistent CTAs
+  int nCta = 0;
+  int mmaN = 256;               // N of one MMA instruction
+  void *probDev = nullptr;      // this plan's GemmProblem on the device
   float *ke = nullptr;       // [E][groups][ncomp][n][n] fp32
   size_t keBytes = 0;
   int *err = nullptr;        // device error word (wait timeouts)
@@ -298,14 +302,24 @@ __global__ void k_factors_elastic(const PlanDev p, const DevTerms *__restrict__ 
 
 // --------------------------------------------------- tcgen05 contraction
 
-struct GemmArgs {
+// One problem (element bucket) of a contraction launch
+struct GemmProblem {
   const float *A;       // [rows][K3]
   const float *B;       // [nOrient][Npad * K3] core-matrix images
-  const int32_t *tiles; // [nTiles][3]
   const int32_t *perm;  // rank -> element
   float *ke;            // [E][rowsPerElem][nn2]
+  int Npad, nn2, rowsPerElem, K3;
+  int mmaN;             // N of one MMA instruction (16..256, multiple of 16)
+  int pad_;
+};
+
+// Tiles of one launch: tile t = (problem, orientation, first row, rows);
+// CTA b takes the contiguous tiles [ctaStart[b], ctaStart[b + 1]).
+struct GemmSched {
+  const GemmProblem *probs;
+  const int4 *tiles;
+  const int32_t *ctaStart;
   int *err;
-  int nTiles, Npad, nn2, rowsPerElem, K3;
 };
 
 __device__ inline void cpAsync16(uint32_t dst, const void *src, uint32_t srcBytes) {
@@ -317,7 +331,7 @@ __device__ inline void cpAsyncWaitAll() { asm volatile("cp.async.wait_all;" ::: 
 // A tile of rows [row0, row0 + nrows) into the core-matrix image at As:
 // row r, 16-byte chunk kc -> core matrix (r/8, kc), K-direction stride 2048 B;
 // rows past nrows are zero-filled
-__device__ inline void loadATile(const GemmArgs &g, uint32_t As, int row0, int nrows, int tid) {
+__device__ inline void loadATile(const GemmProblem &g, uint32_t As, int row0, int nrows, int tid) {
   const int chunks = g.K3 / 4;
   for (int c = tid; c < kBM * chunks; c += kThreadsGemm) {
     const int r = c / chunks, kc = c % chunks;
@@ -328,24 +342,28 @@ __device__ inline void loadATile(const GemmArgs &g, uint32_t As, int row0, int n
   cpAsyncCommit();
 }
 
-__device__ inline void loadB(const GemmArgs &g, float *Bs, int o, int tid) {
+__device__ inline void loadB(const GemmProblem &g, float *Bs, int o, int tid) {
   const float4 *src = reinterpret_cast<const float4 *>(g.B + (size_t)o * g.Npad * g.K3);
   float4 *dst = reinterpret_cast<float4 *>(Bs);
   for (int k = tid; k < g.Npad * g.K3 / 4; k += kThreadsGemm) dst[k] = src[k];
 }
 
-// drain columns [c0, c1) of this warp's 32 TMEM lanes into the element rows.
-// Full 32-column chunks go through a padded per-warp stage (32 rows x 36
-// floats) so that each float4 store instruction writes 4 rows x 128
-// contiguous bytes instead of 32 scattered 16-byte pieces.
-__device__ inline void drainColumns(const GemmArgs &g, uint32_t tmemRow, float *out, bool live, int c0, int c1, float *stage) {
+// drain TMEM columns [c0, c1) of this warp's 32 lanes into the element rows
+// (element-matrix column = colOff + TMEM column). Full 32-column chunks go
+// through a padded per-warp stage (32 rows x 36 floats) so that each float4
+// store instruction writes 4 rows x 128 contiguous bytes instead of 32
+// scattered 16-byte pieces.
+__device__ inline void drainColumns(const GemmProblem &g, uint32_t tmemRow, float *out, bool live, int c0, int c1, float *stage,
+                                    int colOff) {
   const int lane = threadIdx.x & 31;
   const bool vec = (g.nn2 & 3) == 0;
+  out += colOff;
+  const int nn2 = g.nn2 - colOff;  // columns left in the element row
   int c = c0;
   for (; c + 32 <= c1; c += 32) {
     float v[32];
     tmemLoad32(tmemRow + (uint32_t)c, v);
-    if (vec && c + 32 <= g.nn2) {
+    if (vec && c + 32 <= nn2) {
 #pragma unroll
       for (int k = 0; k < 32; k += 4) *reinterpret_cast<float4 *>(stage + lane * 36 + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
       __syncwarp();
@@ -361,35 +379,39 @@ __device__ inline void drainColumns(const GemmArgs &g, uint32_t tmemRow, float *
       __syncwarp();
     } else if (live) {
       for (int k = 0; k < 32; ++k)
-        if (c + k < g.nn2) out[c + k] = v[k];
+        if (c + k < nn2) out[c + k] = v[k];
     }
   }
   if (c < c1) {
     float v[16];
     tmemLoad16(tmemRow + (uint32_t)c, v);
     if (live) {
-      if (vec && c + 16 <= g.nn2) {
+      if (vec && c + 16 <= nn2) {
 #pragma unroll
         for (int k = 0; k < 16; k += 4) *reinterpret_cast<float4 *>(out + c + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
       } else {
         for (int k = 0; k < 16; ++k)
-          if (c + k < g.nn2) out[c + k] = v[k];
+          if (c + k < nn2) out[c + k] = v[k];
       }
     }
   }
 }
 
-// Persistent: one CTA per SM, 8 warps. Warp 0 owns the TMEM allocation,
-// thread 0 issues the MMAs, all warps drain TMEM (warp w: lanes of quadrant
-// w % 4, half w / 4 of the columns). The next tile's A is fetched with
-// cp.async while the current tile computes and drains.
-__global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmArgs g) {
+// Persistent: one CTA per SM, 8 warps, over a contiguous range of tiles of
+// one or many problems. Warp 0 owns the TMEM allocation, thread 0 issues the
+// MMAs, all warps drain TMEM (warp w: lanes of quadrant w % 4, half w / 4 of
+// the columns). Element matrices wider than the 512 TMEM columns are done in
+// column chunks of 512. The next tile's A is fetched with cp.async while the
+// current tile computes and drains when both share the B image in shared
+// memory; B is reloaded when the (problem, orientation) changes.
+__global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmSched sc, int maxK3) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  float *Bs = reinterpret_cast<float *>(smem);                       // Npad * K3
-  float *As0 = Bs + (size_t)g.Npad * g.K3;                           // 2 x kBM * K3
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(As0 + 2 * kBM * g.K3);
-  uint32_t *tmemBase = reinterpret_cast<uint32_t *>(mbar + 1);
-  float *Stage = reinterpret_cast<float *>(mbar + 2);                // 8 warps x 32 x 36 floats
+  __shared__ GemmProblem gs;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem);
+  uint32_t *tmemBase = reinterpret_cast<uint32_t *>(smem + 8);
+  float *Stage = reinterpret_cast<float *>(smem + 16);                 // 8 warps x 32 x 36 floats
+  float *As0 = Stage + 8 * 32 * 36;                                    // 2 x kBM * maxK3
+  float *Bs = As0 + 2 * kBM * maxK3;                                   // Npad * K3
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quad = warp & 3, half = warp >> 2;
 
@@ -405,66 +427,77 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
   __syncthreads();
   tcFenceAfter();
   const uint32_t tmem = *tmemBase;
-  const uint32_t aBase[2] = {smemAddr(As0), smemAddr(As0 + kBM * g.K3)};
   const uint32_t bBase = smemAddr(Bs);
-  const uint32_t bLbo = (uint32_t)g.Npad * 16u;  // K-adjacent core matrices of B
-  const int colSplit = ((g.Npad / 2 + 15) / 16) * 16;
   uint32_t phase = 0;
   bool failed = false;
-  int t = blockIdx.x;
-  if (t < g.nTiles) {
-    loadB(g, Bs, g.tiles[3 * t], tid);
-    loadATile(g, aBase[0], g.tiles[3 * t + 1], g.tiles[3 * t + 2], tid);
+  const int t0 = sc.ctaStart[blockIdx.x], t1 = sc.ctaStart[blockIdx.x + 1];
+  if (t0 < t1) {
+    const int4 T = sc.tiles[t0];
+    if (tid == 0) gs = sc.probs[T.x];
+    __syncthreads();
+    loadB(gs, Bs, T.y, tid);
+    loadATile(gs, smemAddr(As0), T.z, T.w, tid);
   }
-  for (int it = 0; t < g.nTiles && !failed; ++it, t += gridDim.x) {
+  for (int t = t0, it = 0; t < t1 && !failed; ++t, ++it) {
     const int buf = it & 1;
-    const int o = g.tiles[3 * t], row0 = g.tiles[3 * t + 1], nrows = g.tiles[3 * t + 2];
+    const int4 T = sc.tiles[t];
+    const int o = T.y, row0 = T.z, nrows = T.w;
+    const uint32_t aAddr = smemAddr(As0 + buf * kBM * gs.K3);
+    const uint32_t bLbo = (uint32_t)gs.Npad * 16u;  // K-adjacent core matrices of B
     cpAsyncWaitAll();
     fenceProxyAsync();
     __syncthreads();
-    if (tid == 0) {
-      tcFenceAfter();
-      for (int n0 = 0; n0 < g.Npad; n0 += 256) {
-        const int nc = min(256, g.Npad - n0);
-        const uint32_t idesc = idescTf32(kBM, nc);
-        for (int ks = 0; ks < g.K3 / 8; ++ks) {
-          const uint64_t ad = smemDesc(aBase[buf] + ks * 2 * 2048, 2048, 128);
-          const uint64_t bd = smemDesc(bBase + ks * 2 * bLbo + (n0 >> 3) * 128, bLbo, 128);
-          mmaTf32(tmem + (uint32_t)n0, ad, bd, idesc, ks > 0 ? 1u : 0u);
+    // prefetch the next tile's A when it shares this B image
+    const int tn = t + 1;
+    int4 Tn = make_int4(-1, -1, 0, 0);
+    if (tn < t1) Tn = sc.tiles[tn];
+    const bool nextSameB = tn < t1 && Tn.x == T.x && Tn.y == o;
+    const int r = quad * 32 + lane;
+    const bool live = r < nrows;
+    const int grow = row0 + r;
+    const int64_t e = live ? gs.perm[grow / gs.rowsPerElem] : 0;
+    float *out = gs.ke + ((size_t)e * gs.rowsPerElem + (grow % gs.rowsPerElem)) * gs.nn2;
+    const uint32_t tmemRow = tmem + ((uint32_t)(quad * 32) << 16);
+    float *stage = Stage + warp * (32 * 36);
+    for (int n0 = 0; n0 < gs.Npad && !failed; n0 += kTmemCols) {
+      const int ncols = min(kTmemCols, gs.Npad - n0);
+      if (tid == 0) {
+        tcFenceAfter();
+        for (int c0 = 0; c0 < ncols; c0 += gs.mmaN) {
+          const int nc = min(gs.mmaN, ncols - c0);
+          const uint32_t idesc = idescTf32(kBM, nc);
+          for (int ks = 0; ks < gs.K3 / 8; ++ks) {
+            const uint64_t ad = smemDesc(aAddr + ks * 2 * 2048, 2048, 128);
+            const uint64_t bd = smemDesc(bBase + ks * 2 * bLbo + ((n0 + c0) >> 3) * 128, bLbo, 128);
+            mmaTf32(tmem + (uint32_t)c0, ad, bd, idesc, ks > 0 ? 1u : 0u);
+          }
         }
+        mmaCommit(mbar);
       }
-      mmaCommit(mbar);
+      if (n0 == 0 && nextSameB) loadATile(gs, smemAddr(As0 + (buf ^ 1) * kBM * gs.K3), Tn.z, Tn.w, tid);
+      __syncwarp();
+      const bool ok = mbarWait(mbar, phase);
+      failed = __syncthreads_or(ok ? 0 : 1) != 0;  // block-uniform
+      if (failed) {
+        if (tid == 0) atomicExch(sc.err, 1);
+      } else {
+        phase ^= 1u;
+      }
+      tcFenceAfter();
+      if (!failed) {
+        const int colSplit = ((ncols / 2 + 15) / 16) * 16;
+        if (half == 0) drainColumns(gs, tmemRow, out, live, 0, min(colSplit, ncols), stage, n0);
+        else drainColumns(gs, tmemRow, out, live, min(colSplit, ncols), ncols, stage, n0);
+      }
+      tcFenceBefore();
+      __syncthreads();
     }
-    // prefetch the next tile's A (its B must be the one in shared memory)
-    const int tn = t + gridDim.x;
-    const bool nextSameB = tn < g.nTiles && g.tiles[3 * tn] == o;
-    if (nextSameB) loadATile(g, aBase[buf ^ 1], g.tiles[3 * tn + 1], g.tiles[3 * tn + 2], tid);
-    __syncwarp();
-    const bool ok = mbarWait(mbar, phase);
-    failed = __syncthreads_or(ok ? 0 : 1) != 0;  // block-uniform
-    if (failed) {
-      if (tid == 0) atomicExch(g.err, 1);
-    } else {
-      phase ^= 1u;
-    }
-    tcFenceAfter();
-    if (!failed) {
-      const int r = quad * 32 + lane;
-      const bool live = r < nrows;
-      const int grow = row0 + r;
-      const int64_t e = live ? g.perm[grow / g.rowsPerElem] : 0;
-      float *out = g.ke + ((size_t)e * g.rowsPerElem + (grow % g.rowsPerElem)) * g.nn2;
-      const uint32_t tmemRow = tmem + ((uint32_t)(quad * 32) << 16);
-      float *stage = Stage + warp * (32 * 36);
-      if (half == 0) drainColumns(g, tmemRow, out, live, 0, min(colSplit, g.Npad), stage);
-      else drainColumns(g, tmemRow, out, live, min(colSplit, g.Npad), g.Npad, stage);
-    }
-    tcFenceBefore();
-    __syncthreads();
-    if (!failed && tn < g.nTiles && !nextSameB) {
-      // orientation change: the MMAs are done with Bs, reload it and the next A
-      loadB(g, Bs, g.tiles[3 * tn], tid);
-      loadATile(g, aBase[buf ^ 1], g.tiles[3 * tn + 1], g.tiles[3 * tn + 2], tid);
+    if (!failed && tn < t1 && !nextSameB) {
+      // problem or orientation change: the MMAs are done with Bs, reload it and the next A
+      if (tid == 0 && Tn.x != T.x) gs = sc.probs[Tn.x];
+      __syncthreads();
+      loadB(gs, Bs, Tn.y, tid);
+      loadATile(gs, smemAddr(As0 + (buf ^ 1) * kBM * gs.K3), Tn.z, Tn.w, tid);
     }
   }
   cpAsyncWaitAll();
@@ -477,7 +510,6 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmA
   tcFenceAfter();
   if (warp == 0) tmemDealloc(tmem, kTmemCols);
 }
-
 
 // ---------------------------------------------------- FP64 RHS (mixed)
 
@@ -632,10 +664,76 @@ static void buildB(const PlanDev &p, const std::vector<double> &w, const std::ve
     }
 }
 
-static size_t gemmSmem(int Npad, int k3) {
+size_t gemmSmem(int Npad, int k3) {
   // at least half the SM's shared memory: one CTA per SM, so no CTA ever
   // waits in tcgen05.alloc for another one's 512 TMEM columns
-  return std::max<size_t>((size_t)Npad * k3 * 4 + 2 * kBM * k3 * 4 + 16 + 8 * 32 * 36 * 4, 116 * 1024);
+  return std::max<size_t>(16 + 8 * 32 * 36 * 4 + 2 * (size_t)kBM * k3 * 4 + (size_t)Npad * k3 * 4, 116 * 1024);
+}
+
+// Contiguous tile ranges for nCta persistent CTAs with about equal summed cost
+std::vector<int32_t> partitionTiles(const std::vector<double> &cost, int nCta) {
+  std::vector<int32_t> start((size_t)nCta + 1, (int32_t)cost.size());
+  double total = 0.0;
+  for (double c : cost) total += c;
+  double acc = 0.0;
+  int b = 0;
+  start[0] = 0;
+  for (size_t t = 0; t < cost.size() && b + 1 < nCta; ++t) {
+    acc += cost[t];
+    while (b + 1 < nCta && acc >= total * (b + 1) / nCta) start[++b] = (int32_t)(t + 1);
+  }
+  for (int k = b + 1; k <= nCta; ++k) start[k] = (int32_t)cost.size();
+  return start;
+}
+
+// One contraction launch over the tiles of one or many problems
+int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ctaStartDev, int nCta, int *err, int maxK3,
+                   size_t smem, cudaStream_t s) {
+  static size_t smemSet = 0;
+  if (smem > smemSet) {
+    FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    smemSet = smem;
+  }
+  GemmSched sc;
+  sc.probs = (const GemmProblem *)probsDev;
+  sc.tiles = tilesDev;
+  sc.ctaStart = ctaStartDev;
+  sc.err = err;
+  ProfScope prof("k_contract_tf32x3", s);
+  k_contract_tf32x3<<<std::max(1, nCta), kThreadsGemm, smem, s>>>(sc, maxK3);
+  countLaunch();
+  FG_CUDA(cudaGetLastError());
+  return FG_OK;
+}
+
+// GEMM tiles of a plan (problem index `prob` of a launch): 128 rows of one
+// orientation each, rows = element rank * rowsPerElem + row within element
+std::vector<int4> mixedTiles(fg_plan *plan, int prob, int rowsPerElem) {
+  MixedState *m = state(plan);
+  std::vector<int4> tiles;
+  int64_t start = 0;
+  for (int o = 0; o < plan->d.nOrient; ++o) {
+    const int64_t r0 = start * rowsPerElem, r1 = (start + m->orientCount[o]) * rowsPerElem;
+    for (int64_t r = r0; r < r1; r += kBM) tiles.push_back(make_int4(prob, o, (int)r, (int)std::min<int64_t>(kBM, r1 - r)));
+    start += m->orientCount[o];
+  }
+  return tiles;
+}
+
+GemmProblem mixedGemmProblem(fg_plan *plan) {
+  MixedState *m = state(plan);
+  GemmProblem g;
+  std::memset(&g, 0, sizeof(g));
+  g.A = m->A;
+  g.B = m->B;
+  g.perm = m->perm;
+  g.ke = m->ke;
+  g.Npad = m->Npad;
+  g.nn2 = m->nn2;
+  g.rowsPerElem = m->rowsPerElem;
+  g.K3 = m->k3;
+  g.mmaN = std::min(m->mmaN, std::min(m->Npad, 256));
+  return g;
 }
 
 // Tables, tiles and buffers for element matrices of `groups` term groups
@@ -661,11 +759,7 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
     m->nn2 = p.nb * p.nb;  // one (block of the) element matrix per GEMM row
     m->Npad = (m->nn2 + 15) / 16 * 16;
     m->nOrient = p.nOrient;
-    if (m->Npad > kTmemCols) {
-      setLastError("mixed path: element matrix wider than the 512 TMEM columns");
-      return FG_ERR_UNSUPPORTED;
-    }
-    if ((size_t)m->Npad * m->k3 * 4 + 2 * kBM * m->k3 * 4 + 16 + 8 * 32 * 36 * 4 > 220 * 1024) {
+    if (gemmSmem(m->Npad, m->k3) > 220 * 1024) {
       setLastError("mixed path: element matrix too large for the shared-memory B tile");
       return FG_ERR_UNSUPPORTED;
     }
@@ -703,26 +797,22 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
   }
   // tiles: rows of one orientation never share a tile
   const int rowsPerElem = groups * ncomp * m->blocks;
-  std::vector<int32_t> tiles;
-  int64_t start = 0;
-  for (int o = 0; o < p.nOrient; ++o) {
-    const int64_t r0 = start * rowsPerElem, r1 = (start + m->orientCount[o]) * rowsPerElem;
-    for (int64_t r = r0; r < r1; r += kBM) {
-      tiles.push_back(o);
-      tiles.push_back((int32_t)r);
-      tiles.push_back((int32_t)std::min<int64_t>(kBM, r1 - r));
-    }
-    start += m->orientCount[o];
-  }
   if ((int64_t)p.E * rowsPerElem >= (int64_t(1) << 31)) {
     setLastError("mixed path: more than 2^31 GEMM rows in one plan");
     return FG_ERR_UNSUPPORTED;
   }
+  std::vector<int4> tiles = mixedTiles(plan, 0, rowsPerElem);
+  m->nTiles = (int)tiles.size();
+  m->nCta = std::max(1, std::min(smCount(), m->nTiles));
+  std::vector<int32_t> start = partitionTiles(std::vector<double>(tiles.size(), 1.0), m->nCta);
   if (m->tiles) cudaFree(m->tiles);
+  if (m->ctaStart) cudaFree(m->ctaStart);
   m->tiles = nullptr;
-  FG_CUDA(cudaMalloc(&m->tiles, std::max<size_t>(tiles.size(), 3) * 4));
-  FG_CUDA(cudaMemcpy(m->tiles, tiles.data(), tiles.size() * 4, cudaMemcpyHostToDevice));
-  m->nTiles = (int)(tiles.size() / 3);
+  m->ctaStart = nullptr;
+  FG_CUDA(cudaMalloc(&m->tiles, std::max<size_t>(tiles.size(), 1) * sizeof(int4)));
+  if (!tiles.empty()) FG_CUDA(cudaMemcpy(m->tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  FG_CUDA(cudaMalloc(&m->ctaStart, start.size() * 4));
+  FG_CUDA(cudaMemcpy(m->ctaStart, start.data(), start.size() * 4, cudaMemcpyHostToDevice));
   m->rowsPerElem = rowsPerElem;
   m->rows = p.E * rowsPerElem;
   int st = ensureDevice((void **)&m->A, &m->Abytes, (size_t)m->rows * m->k3 * 4);
@@ -731,6 +821,9 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
   if (st) return st;
   m->ncomp = ncomp;
   m->groups = groups;
+  GemmProblem gp = mixedGemmProblem(plan);
+  if (!m->probDev) FG_CUDA(cudaMalloc(&m->probDev, sizeof(GemmProblem)));
+  FG_CUDA(cudaMemcpy(m->probDev, &gp, sizeof(GemmProblem), cudaMemcpyHostToDevice));
   return FG_OK;
 }
 
@@ -750,32 +843,8 @@ int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups,
     countLaunch();
     FG_CUDA(cudaGetLastError());
   }
-  GemmArgs g;
-  g.A = m->A;
-  g.B = m->B;
-  g.tiles = m->tiles;
-  g.perm = m->perm;
-  g.ke = m->ke;
-  g.err = m->err;
-  g.nTiles = m->nTiles;
-  g.Npad = m->Npad;
-  g.nn2 = m->nn2;
-  g.rowsPerElem = m->rowsPerElem;
-  g.K3 = m->k3;
-  const size_t smem = gemmSmem(m->Npad, m->k3);
-  static size_t smemSet = 0;
-  if (smem > smemSet) {
-    FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    smemSet = smem;
-  }
-  const int grid = std::max(1, std::min(smCount(), m->nTiles));
-  {
-    ProfScope prof("k_contract_tf32x3", s);
-    k_contract_tf32x3<<<grid, kThreadsGemm, smem, s>>>(g);
-    countLaunch();
-    FG_CUDA(cudaGetLastError());
-  }
-  return FG_OK;
+  if (m->nTiles == 0) return FG_OK;
+  return launchContract(m->probDev, m->tiles, m->ctaStart, m->nCta, m->err, m->k3, gemmSmem(m->Npad, m->k3), s);
 }
 
 // FP64 element right-hand sides of the source terms into be ([E][n] complex)
@@ -821,6 +890,8 @@ extern "C" void mixedDestroy(fg_plan *plan) {
   cudaFree(m->B);
   cudaFree(m->perm);
   cudaFree(m->tiles);
+  cudaFree(m->ctaStart);
+  cudaFree(m->probDev);
   cudaFree(m->ke);
   cudaFree(m->err);
   if (m->errHost) cudaFreeHost(m->errHost);

@@ -136,7 +136,7 @@ def test_full_size_c2_properties(femg, cuda):
     assert np.allclose(v.real, v.real[order[pos]], rtol=0, atol=1e-12 * np.abs(v.real).max())
 
 
-MIXED_CASES = ["c2_m3", "c2_m4_p1", "c2_m3_p2", "c3_m4", "c1_m8", "c1_full", "c1_p1mesh_dirichlet1", "c5_m2", "c5_m3_p1"]
+MIXED_CASES = ["c2_m3", "c2_m4_p1", "c2_m3_p2", "c2_m2_p4", "c3_m4", "c1_m8", "c1_full", "c1_p1mesh_dirichlet1", "c5_m2", "c5_m3_p1"]
 
 
 @pytest.mark.parametrize("case", MIXED_CASES)
