@@ -199,10 +199,8 @@ __device__ inline void tmemLoad32(uint32_t taddr, float *v) {
 // first quadrature point (affine elements: the geometric Jacobian is constant), per-element coefficients,
 // factors D_e split into TF32 hi/lo, written as row [hi | lo | hi] at the
 // element's rank in the orientation-sorted order.
-__global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf, float *__restrict__ A,
-                          int ncomp, int rowsPerElem, int rowOff) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= p.E) return;
+__device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
+                                              float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff, int64_t e) {
   double X[kMaxNodes * 3];
   for (int k = 0; k < p.nn; ++k)
     for (int c = 0; c < 3; ++c) X[3 * k + c] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + k] + c];
@@ -241,6 +239,12 @@ __global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, c
   }
 }
 
+__global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf, float *__restrict__ A,
+                          int ncomp, int rowsPerElem, int rowOff) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < p.E) factorsScalar(p, terms, rankOf, A, ncomp, rowsPerElem, rowOff, e);
+}
+
 // Compound field with the isotropic Tensor4 term: for every component pair
 // (a, b) (test component a, unknown component b) the block of the element
 // matrix is  Ke_ab[i][j] = sum_{p,p'} D_ab[p p'] S_{p p'}[i][j] + D_ab[9] M[i][j]
@@ -252,10 +256,8 @@ __global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, c
 // block a*3+b) in the orientation-sorted element order.
 constexpr int kKpE = 16;
 constexpr int kK3E = 3 * kKpE;
-__global__ void k_factors_elastic(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
-                                  float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= p.E) return;
+__device__ __forceinline__ void factorsElastic(const PlanDev &p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
+                                               float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff, int64_t e) {
   double X[kMaxNodes * 3];
   for (int k = 0; k < p.nn; ++k)
     for (int c = 0; c < 3; ++c) X[3 * k + c] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + k] + c];
@@ -300,18 +302,30 @@ __global__ void k_factors_elastic(const PlanDev p, const DevTerms *__restrict__ 
   }
 }
 
-// --------------------------------------------------- tcgen05 contraction
+__global__ void k_factors_elastic(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
+                                  float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < p.E) factorsElastic(p, terms, rankOf, A, ncomp, rowsPerElem, rowOff, e);
+}
 
-// One problem (element bucket) of a contraction launch
-struct GemmProblem {
-  const float *A;       // [rows][K3]
-  const float *B;       // [nOrient][Npad * K3] core-matrix images
-  const int32_t *perm;  // rank -> element
-  float *ke;            // [E][rowsPerElem][nn2]
-  int Npad, nn2, rowsPerElem, K3;
-  int mmaN;             // N of one MMA instruction (16..256, multiple of 16)
-  int pad_;
-};
+// Factor rows of many plans in one launch: thread -> (job, element) through
+// the jobs' element offsets
+__global__ void k_factors_batch(const FactorJob *__restrict__ jobs, int nJobs, int64_t total) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total) return;
+  int lo = 0, hi = nJobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].elemStart <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  const FactorJob &J = jobs[lo];
+  const int64_t e = g - J.elemStart;
+  if (J.elastic) factorsElastic(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
+  else factorsScalar(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
+}
+
+// --------------------------------------------------- tcgen05 contraction
 
 // Tiles of one launch: tile t = (problem, orientation, first row, rows);
 // CTA b takes the contiguous tiles [ctaStart[b], ctaStart[b + 1]).
@@ -847,6 +861,32 @@ int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups,
   return launchContract(m->probDev, m->tiles, m->ctaStart, m->nCta, m->err, m->k3, gemmSmem(m->Npad, m->k3), s);
 }
 
+int launchFactorsBatch(const FactorJob *jobsDev, int nJobs, int64_t total, cudaStream_t s) {
+  if (total <= 0) return FG_OK;
+  ProfScope prof("k_factors_batch", s);
+  k_factors_batch<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(jobsDev, nJobs, total);
+  countLaunch();
+  FG_CUDA(cudaGetLastError());
+  return FG_OK;
+}
+
+// This plan's factor job (terms on the device, group 0)
+FactorJob mixedFactorJob(fg_plan *plan, const DevTerms *dterms, int64_t elemStart) {
+  MixedState *m = state(plan);
+  FactorJob j;
+  std::memset(&j, 0, sizeof(j));
+  j.p = plan->d;
+  j.terms = dterms;
+  j.rankOf = m->perm + plan->d.E;
+  j.A = m->A;
+  j.ncomp = m->ncomp;
+  j.rowsPerElem = m->rowsPerElem;
+  j.rowOff = 0;
+  j.elastic = m->blocks == 9;
+  j.elemStart = elemStart;
+  return j;
+}
+
 // FP64 element right-hand sides of the source terms into be ([E][n] complex)
 int launchRhsFp64(fg_plan *plan, const DevTerms *dterms, double *be, cudaStream_t s) {
   const PlanDev &p = plan->d;
@@ -979,17 +1019,4 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
   return FG_OK;
 }
 
-extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const *terms, const int32_t *n_terms, int32_t n_problems,
-                               int32_t mixed, fg_batch **out) {
-  (void)plans; (void)terms; (void)n_terms; (void)n_problems; (void)mixed;
-  if (out) *out = nullptr;
-  femg::setLastError("fg_batch_create: not built yet");
-  return FG_ERR_UNSUPPORTED;
-}
 
-extern "C" int fg_batch_run(fg_batch *batch, double *const *csr_values, double *const *rhs, void *stream) {
-  (void)batch; (void)csr_values; (void)rhs; (void)stream;
-  return FG_ERR_UNSUPPORTED;
-}
-
-extern "C" void fg_batch_destroy(fg_batch *batch) { (void)batch; }

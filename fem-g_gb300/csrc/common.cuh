@@ -16,6 +16,9 @@ void countLaunch(int n = 1);
 
 // Brackets one kernel launch with CUDA events on its stream while the kernel
 // timer (fg_profile_enable) is on; a no-op otherwise.
+// while suspended (stream capture), this thread's ProfScopes record nothing
+void profSuspend(bool on);
+
 class ProfScope {
  public:
   ProfScope(const char *name, cudaStream_t s);
@@ -153,6 +156,46 @@ int prepareOutputs(fg_plan *plan, double *csr_values, double *rhs, Outputs *o);
 int finishOutputs(fg_plan *plan, const Outputs &o, double *csr_values, double *rhs, cudaStream_t s);
 // FP64 element kernel (also used as the reference for the mixed error report)
 int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s);
+// One plan of a batched gather launch
+struct GatherJob {
+  PlanDev p;
+  const void *ke;  // element matrices (float or double, one layout per launch)
+  const double2 *be, *uD;
+  double2 *values, *rhs;
+  int32_t blk3, pad_;
+  int64_t blockStart, nBlocks;
+};
+struct GatherShape {
+  int L = 0, wpb = 0, rowsPerBlock = 0;
+  size_t smem = 0;
+  bool ok = false;
+};
+// L, wpb <= 0: the defaults of the single-plan gather
+GatherShape gatherShape(int n, int maxRowLen, int kcplx, int keIsFloat, int L, int wpb);
+int launchGatherBatch(const GatherJob *jobsDev, int nJobs, int64_t blocks, int slotBytes, int kcplx, int keIsFloat,
+                      const GatherShape &g, cudaStream_t s);
+
+// One problem (element bucket) of a tensor-core contraction launch
+struct GemmProblem {
+  const float *A;       // [rows][K3] split factor rows
+  const float *B;       // [nOrient][Npad * K3] core-matrix images
+  const int32_t *perm;  // rank -> element
+  float *ke;            // [E][rowsPerElem][nn2]
+  int Npad, nn2, rowsPerElem, K3;
+  int mmaN;             // N of one MMA instruction (16..256, multiple of 16)
+  int pad_;
+};
+
+// One plan of a batched factor-row launch (mixed path)
+struct FactorJob {
+  PlanDev p;
+  const DevTerms *terms;
+  const int32_t *rankOf;
+  float *A;
+  int32_t ncomp, rowsPerElem, rowOff, elastic;
+  int64_t elemStart;
+};
+
 // mixed path pieces shared with the multi-frequency path (assemble_mixed.cu)
 int prepareMixed(fg_plan *plan, int ncomp, int groups);
 int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups, cudaStream_t s);
@@ -160,6 +203,15 @@ int launchRhsFp64(fg_plan *plan, const DevTerms *dterms, double *be, cudaStream_
 float *mixedKe(fg_plan *plan, int *blocks);
 int mixedCheckTimeout(fg_plan *plan, bool wait);
 int mixedRecordError(fg_plan *plan, cudaStream_t s);
+// ... and with the batch (batch.cu)
+int launchFactorsBatch(const FactorJob *jobsDev, int nJobs, int64_t total, cudaStream_t s);
+FactorJob mixedFactorJob(fg_plan *plan, const DevTerms *dterms, int64_t elemStart);
+std::vector<int4> mixedTiles(fg_plan *plan, int prob, int rowsPerElem);
+size_t gemmSmem(int Npad, int k3);
+std::vector<int32_t> partitionTiles(const std::vector<double> &cost, int nCta);
+int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ctaStartDev, int nCta, int *err, int maxK3,
+                   size_t smem, cudaStream_t s);
+GemmProblem mixedGemmProblem(fg_plan *plan);
 
 // ------------------------------------------------------------- device helpers
 

@@ -17,10 +17,12 @@
 
 namespace femg {
 
+// The rows of one plan handled by block `blk` of `nblk` (grid-stride over row
+// groups of rowsPerBlock rows).
 template <typename SlotT, bool KCPLX, typename KT, typename AT, int L>
-__global__ void __launch_bounds__(256)
-    k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
-             double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock, int blk3) {
+__device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restrict__ ke, const double2 *__restrict__ be,
+                                           const double2 *__restrict__ uD, double2 *__restrict__ values,
+                                           double2 *__restrict__ rhs, int rowsPerBlock, int blk3, int64_t blk, int64_t nblk) {
   constexpr int R = 32 / L;  // rows per warp
   constexpr int J = 3;       // columns per lane
   constexpr int SS = KCPLX ? 2 : 1;
@@ -43,10 +45,10 @@ __global__ void __launch_bounds__(256)
   const int n = p.n;
   const size_t nn2 = (size_t)n * n;
   const int64_t nRows = (int64_t)p.nRows;
-  const int64_t stride = (int64_t)gridDim.x * rowsPerBlock;
-  const int64_t first = (int64_t)blockIdx.x * rowsPerBlock + warp * R + sub;
+  const int64_t stride = nblk * rowsPerBlock;
+  const int64_t first = blk * rowsPerBlock + warp * R + sub;
   uint4 vNext = first < nRows ? p.visit[first] : make_uint4(0, 0, 0, 0);
-  for (int64_t base = (int64_t)blockIdx.x * rowsPerBlock + warp * R; base < nRows; base += stride) {
+  for (int64_t base = blk * rowsPerBlock + warp * R; base < nRows; base += stride) {
     const int64_t idx = base + sub;
     const bool live = idx < nRows;
     const uint4 v = vNext;  // this row's record, fetched one iteration ahead
@@ -141,6 +143,27 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+template <typename SlotT, bool KCPLX, typename KT, typename AT, int L>
+__global__ void __launch_bounds__(256)
+    k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
+             double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock, int blk3) {
+  gatherRows<SlotT, KCPLX, KT, AT, L>(p, ke, be, uD, values, rhs, rowsPerBlock, blk3, blockIdx.x, gridDim.x);
+}
+
+// Many plans in one launch: job q owns blocks [blockStart, blockStart + nBlocks)
+template <typename SlotT, bool KCPLX, typename KT, typename AT, int L>
+__global__ void __launch_bounds__(256) k_gather_batch(const GatherJob *__restrict__ jobs, int nJobs, int rowsPerBlock) {
+  int lo = 0, hi = nJobs - 1;
+  while (lo < hi) {  // last job whose blockStart <= blockIdx.x
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blockStart <= (int64_t)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const GatherJob &J = jobs[lo];
+  gatherRows<SlotT, KCPLX, KT, AT, L>(J.p, (const KT *)J.ke, J.be, J.uD, J.values, J.rhs, rowsPerBlock, J.blk3,
+                                      (int64_t)blockIdx.x - J.blockStart, J.nBlocks);
+}
+
 template <typename SlotT, bool KCPLX, typename KT>
 static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, const double2 *uD, double2 *values, double2 *rhs,
                        int blk3, cudaStream_t s) {
@@ -206,6 +229,73 @@ int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, 
   if (keIsFloat)
     return keComplex ? launchTyped<uint16_t, true, float>(p, ke, be2, uD, v2, r2, blk3, s) : launchTyped<uint16_t, false, float>(p, ke, be2, uD, v2, r2, blk3, s);
   return keComplex ? launchTyped<uint16_t, true, double>(p, ke, be2, uD, v2, r2, blk3, s) : launchTyped<uint16_t, false, double>(p, ke, be2, uD, v2, r2, blk3, s);
+}
+
+// Shared memory and rows per block of one gather configuration
+GatherShape gatherShape(int n, int maxRowLen, int kcplx, int keIsFloat, int L, int wpb) {
+  GatherShape g;
+  if (L <= 0) {
+    L = 32;
+    if (n <= 6) L = 2;
+    else if (n <= 12) L = 4;
+    else if (n <= 24) L = 8;
+    else if (n <= 48) L = 16;
+  }
+  const int R = 32 / L;
+  const size_t rowBytes = (size_t)std::max(maxRowLen, 1) * (kcplx ? 2 : 1) * (keIsFloat ? 4 : 8);
+  if (wpb <= 0) {
+    wpb = 8;
+    while (wpb > 1 && rowBytes * R * wpb > 200 * 1024) wpb >>= 1;
+  }
+  g.L = L;
+  g.wpb = wpb;
+  g.rowsPerBlock = wpb * R;
+  g.smem = rowBytes * R * wpb;
+  g.ok = g.smem <= 200 * 1024 && 3 * L >= n;
+  return g;
+}
+
+template <typename SlotT, bool KCPLX, typename KT>
+static int launchBatchTyped(const GatherJob *jobs, int nJobs, int64_t blocks, const GatherShape &g, cudaStream_t s) {
+  using AT = KT;
+#define FG_GATHER_B(LL)                                                                                   \
+  case LL: {                                                                                              \
+    auto kern = k_gather_batch<SlotT, KCPLX, KT, AT, LL>;                                                 \
+    static size_t smemSet = 0;                                                                            \
+    if (g.smem > smemSet) {                                                                               \
+      FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem));      \
+      smemSet = g.smem;                                                                                   \
+    }                                                                                                     \
+    kern<<<(unsigned)blocks, 32 * g.wpb, g.smem, s>>>(jobs, nJobs, g.rowsPerBlock);                       \
+    break;                                                                                                \
+  }
+  switch (g.L) {
+    FG_GATHER_B(2)
+    FG_GATHER_B(4)
+    FG_GATHER_B(8)
+    FG_GATHER_B(16)
+    FG_GATHER_B(32)
+    default:
+      setLastError("batched gather: lanes per row must be 2, 4, 8, 16 or 32");
+      return FG_ERR_ARG;
+  }
+#undef FG_GATHER_B
+  FG_CUDA(cudaGetLastError());
+  return FG_OK;
+}
+
+int launchGatherBatch(const GatherJob *jobsDev, int nJobs, int64_t blocks, int slotBytes, int kcplx, int keIsFloat,
+                      const GatherShape &g, cudaStream_t s) {
+  if (blocks <= 0) return FG_OK;
+  countLaunch();
+  if (slotBytes == 1) {
+    if (keIsFloat)
+      return kcplx ? launchBatchTyped<uint8_t, true, float>(jobsDev, nJobs, blocks, g, s) : launchBatchTyped<uint8_t, false, float>(jobsDev, nJobs, blocks, g, s);
+    return kcplx ? launchBatchTyped<uint8_t, true, double>(jobsDev, nJobs, blocks, g, s) : launchBatchTyped<uint8_t, false, double>(jobsDev, nJobs, blocks, g, s);
+  }
+  if (keIsFloat)
+    return kcplx ? launchBatchTyped<uint16_t, true, float>(jobsDev, nJobs, blocks, g, s) : launchBatchTyped<uint16_t, false, float>(jobsDev, nJobs, blocks, g, s);
+  return kcplx ? launchBatchTyped<uint16_t, true, double>(jobsDev, nJobs, blocks, g, s) : launchBatchTyped<uint16_t, false, double>(jobsDev, nJobs, blocks, g, s);
 }
 
 }  // namespace femg

@@ -55,8 +55,11 @@ cudaEvent_t takeEvent() {
 }
 }  // namespace
 
+static thread_local bool t_profSuspended = false;
+void profSuspend(bool on) { t_profSuspended = on; }
+
 ProfScope::ProfScope(const char *name, cudaStream_t s) : name_(name), s_(s) {
-  if (!g_profOn.load()) return;
+  if (!g_profOn.load() || t_profSuspended) return;
   a_ = takeEvent();
   b_ = takeEvent();
   if (!a_ || !b_) {

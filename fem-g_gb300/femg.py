@@ -98,6 +98,7 @@ def lib():
         "fg_batch_create": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.POINTER(P)]),
         "fg_batch_run": (C.c_int, [P, P, P, P]),
         "fg_batch_destroy": (None, [P]),
+        "fg_batch_tuning": (C.c_char_p, [P]),
         "fg_profile_enable": (C.c_int, [C.c_int]),
         "fg_profile_read": (C.c_int, [C.c_char_p, C.c_int32, P, P, C.c_int32]),
         "fg_last_error": (C.c_char_p, []),
@@ -128,7 +129,7 @@ def exported_symbols():
     """Names bound above (the C ABI of both headers)."""
     return [
         "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_assemble_fp64", "fg_assemble_mixed",
-        "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_profile_enable",
+        "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_profile_enable",
         "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
         "fg_problem_raw_dofs", "fg_problem_created_dofs", "fg_problem_reserve_log", "fg_problem_bbox", "fg_problem_pre_seconds", "fg_problem_assemble",
@@ -191,6 +192,21 @@ def config_c5(m=60, seed=5, omega=5.0):
     """3D Navier, 3-component hierarchical H1 order 2, Gauss4, lognormal Lame."""
     return config(kind=FG_PROBLEM_NAVIER, dim=3, m=m, mesh_order=1, space=FG_SPACE_HIERARCHICAL_H1, order=2, gauss=4,
                   jitter=0.15, seed=seed, omega=omega, lame_sigma=0.5)
+
+
+def config_c4(n=64, seed=4, m_lo=8, m_hi=48, orders=(1, 2, 3, 4), k_lo=5.0, k_hi=40.0):
+    """Batch of 3D Helmholtz problems: cube resolutions m ~ U{m_lo..m_hi}
+    (x 6 tets), hierarchical H1 orders ~ U(orders), k ~ U[k_lo, k_hi],
+    jitter 0.15 h, rule Gauss(2p); all drawn from one seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for q in range(n):
+        m = int(rng.integers(m_lo, m_hi + 1))
+        p = int(rng.choice(orders))
+        k = float(rng.uniform(k_lo, k_hi))
+        out.append(config(dim=3, m=m, mesh_order=1, space=FG_SPACE_HIERARCHICAL_H1, order=p, gauss=2 * p, jitter=0.15,
+                          seed=seed * 1000 + q, k=k))
+    return out
 
 
 class Problem:
@@ -373,3 +389,48 @@ class Plan:
         if report:
             return values, rhs, dict(max_elem=rep.max_elem_rel_fro, mean_elem=rep.mean_elem_rel_fro, global_=rep.global_rel_fro)
         return values, rhs
+
+
+class Batch:
+    """fg_batch over plans (their problems' terms unless bound=True)."""
+
+    def __init__(self, plans, mixed=False, bound=False):
+        L = lib()
+        self.plans = list(plans)
+        n = len(self.plans)
+        self.ptr = C.c_void_p()
+        ptrs = (C.c_void_p * n)(*[p.ptr.value for p in self.plans])
+        if bound:
+            tl = None
+            nl = None
+        else:
+            tl = (C.c_void_p * n)(*[C.cast(p.prob.terms()[0], C.c_void_p).value for p in self.plans])
+            nl = (C.c_int32 * n)(*[p.prob.terms()[1] for p in self.plans])
+        check(L.fg_batch_create(ptrs, tl, nl, n, 1 if mixed else 0, C.byref(self.ptr)))
+
+    def run(self, values=None, rhs=None, stream=None):
+        """values / rhs: lists of numpy arrays or device pointers (ints);
+        None allocates numpy outputs (rhs None: no right-hand sides)."""
+        n = len(self.plans)
+        if values is None:
+            values = [np.zeros(p.prob.nnz, np.complex128) for p in self.plans]
+        vp = (C.c_void_p * n)(*[v if isinstance(v, int) else v.ctypes.data for v in values])
+        rp = None
+        if rhs is not None:
+            rp = (C.c_void_p * n)(*[r if isinstance(r, int) else r.ctypes.data for r in rhs])
+        check(lib().fg_batch_run(self.ptr, vp, rp, stream))
+        return values, rhs
+
+    def tuning(self):
+        return lib().fg_batch_tuning(self.ptr).decode()
+
+    def close(self):
+        if self.ptr:
+            lib().fg_batch_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

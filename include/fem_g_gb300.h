@@ -240,6 +240,10 @@ int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const *terms, con
 /* values[p] / rhs[p]: device or host output arrays per problem (NULL rhs allowed) */
 int fg_batch_run(fg_batch *batch, double *const *csr_values, double *const *rhs, void *stream);
 void fg_batch_destroy(fg_batch *batch);
+/* JSON description of the shapes the autotuner chose in the first run
+ * (reduction lanes and warps per class, MMA width per contraction class);
+ * empty before it. Valid until the next call on the batch. */
+const char *fg_batch_tuning(const fg_batch *batch);
 
 /* ----------------------------------------------------------------- misc */
 
