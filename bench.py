@@ -140,6 +140,132 @@ def cpu_rate(prob, a, target_s):
         S = int(min(a["E"], max(S * 2, S * target_s / max(dt, 1e-3) * 1.1)))
 
 
+def timed_events(torch, stream, fn, warmup, steps):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def bench_batch(args, femg, torch):
+    """Batched workload: 64 3D Helmholtz problems, m ~ U{m_lo..m_hi}, orders
+    U{1..4}, k ~ U[5, 40], Gauss(2p), one seed; one step = one fg_batch_run
+    (graph replay) over all problems, outputs resident in HBM."""
+    cfgs = femg.config_c4(n=args.c4_n, m_lo=args.c4_m_lo, m_hi=args.c4_m_hi)
+    probs = [femg.Problem(c) for c in cfgs]
+    pre_s = sum(p.pre_seconds() for p in probs)
+    plans = [p.plan() for p in probs]
+    E = sum(p.info()["E"] for p in plans)
+    nnz = sum(p.nnz for p in probs)
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+    outs = [torch.empty(2 * p.nnz, dtype=torch.float64, device="cuda") for p in probs]
+    ptrs = [o.data_ptr() for o in outs]
+    res = {}
+    for prec in ("mixed", "fp64"):
+        b = femg.Batch(plans, mixed=prec == "mixed")
+        t0 = time.perf_counter()
+        b.run(values=ptrs, stream=sptr)
+        torch.cuda.synchronize()
+        first_s = time.perf_counter() - t0
+        l0 = femg.lib().fg_launch_count()
+        steps = args.steps if prec == "mixed" else max(3, min(args.steps, 5))
+        ms = timed_events(torch, stream, lambda: b.run(values=ptrs, stream=sptr), args.warmup, steps)
+        launches = (femg.lib().fg_launch_count() - l0) // (args.warmup + steps)
+        res[prec] = {"ms": ms, "first_run_s": first_s, "tuning": json.loads(b.tuning()), "launches_per_step": int(launches)}
+        if prec == "mixed":
+            # relative Frobenius error of every problem's CSR against the FP64 path
+            tmp = torch.empty(2 * max(p.nnz for p in probs), dtype=torch.float64, device="cuda")
+            d2 = r2 = 0.0
+            worst = 0.0
+            for p, o in zip(plans, outs):
+                n2 = 2 * p.prob.nnz
+                p.assemble("fp64", values=tmp.data_ptr(), rhs=False, stream=sptr)
+                torch.cuda.synchronize()
+                dd = torch.linalg.vector_norm(o - tmp[:n2]).item() ** 2
+                rr = torch.linalg.vector_norm(tmp[:n2]).item() ** 2
+                d2 += dd
+                r2 += rr
+                worst = max(worst, (dd / rr) ** 0.5 if rr > 0 else 0.0)
+            res["rel_fro"] = (d2 / r2) ** 0.5
+            res["worst_problem_rel_fro"] = worst
+            del tmp
+        b.close()
+    orders = {}
+    for c in cfgs:
+        orders[str(c.order)] = orders.get(str(c.order), 0) + 1
+    line = {"metric": METRIC, "value": E / (res["mixed"]["ms"] / 1000.0), "unit": "element matrices/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["mixed"]["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32-tf32x3/fp64", "data": "synthetic (seeded, reference configuration shapes)",
+            "config": {"workload": "helmholtz3d_batch%d_m%d-%d_p1-4_k5-40_gauss2p" % (args.c4_n, args.c4_m_lo, args.c4_m_hi),
+                       "problems": len(probs), "elements": E, "nnz": nnz, "orders": orders,
+                       "l2": "CSR outputs larger than L2, no flush", "parallelism": "single"},
+            "nnz_per_s": nnz / (res["mixed"]["ms"] / 1000.0),
+            "fp64": {"value": E / (res["fp64"]["ms"] / 1000.0), "ms_per_step": res["fp64"]["ms"]},
+            "speedup_mixed_vs_fp64": res["fp64"]["ms"] / res["mixed"]["ms"],
+            "mixed_vs_fp64_rel_fro": res["rel_fro"], "worst_problem_rel_fro": res["worst_problem_rel_fro"],
+            "first_run_s": {"mixed": res["mixed"]["first_run_s"], "fp64": res["fp64"]["first_run_s"]},
+            "tuning": {"mixed": res["mixed"]["tuning"], "fp64": res["fp64"]["tuning"]},
+            "gpu_launches": res["mixed"]["launches_per_step"] * args.steps, "pre_seconds": pre_s}
+    print(json.dumps(line), flush=True)
+
+
+def bench_multi_freq(args, femg, torch):
+    """Navier 3-component P2 on m^3 x 6 tets, Lame lognormal per tet, 16
+    frequencies omega ~ U[1, 10] in one pass; one step = one
+    fg_assemble_multi_freq writing all 16 CSR value arrays in HBM."""
+    m = args.m or 60
+    prob = femg.Problem(femg.config_c5(m=m, omega=0.0))
+    plan = prob.plan()
+    E, nnz = plan.info()["E"], prob.nnz
+    F = args.n_freq
+    omegas = np.random.default_rng(5).uniform(1.0, 10.0, F)
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+    out = torch.empty(F * 2 * nnz, dtype=torch.float64, device="cuda")
+    res = {}
+    femg.profile_read()
+    for prec in ("mixed", "fp64"):
+        steps = args.steps if prec == "mixed" else 2
+        if prec == "mixed":
+            femg.profile_enable(True)
+        ms = timed_events(torch, stream, lambda: plan.assemble_multi_freq(omegas, precision=prec, values=out.data_ptr(),
+                                                                          rhs=False, stream=sptr), args.warmup if prec == "mixed" else 1, steps)
+        if prec == "mixed":
+            femg.profile_enable(False)
+            res["prof"] = femg.profile_read()
+            first = out[: 2 * nnz].clone()
+        else:
+            ref = out[: 2 * nnz]
+            res["rel_fro"] = torch.linalg.vector_norm(first - ref).item() / torch.linalg.vector_norm(ref).item()
+        res[prec] = ms
+    pk, pk_kind = peaks()
+    prof = res["prof"]
+    dom, (dcount, dms) = max(prof.items(), key=lambda kv: kv[1][1])
+    avg = dms / max(dcount, 1)
+    alg = F * nnz * 16 + 2 * E * plan.info()["n"] ** 2 * 4 + E * plan.info()["n"] ** 2 * 2
+    line = {"metric": METRIC, "value": F * E / (res["mixed"] / 1000.0), "unit": "element matrices/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["mixed"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32-tf32x3/fp64", "data": "synthetic (seeded, reference configuration shapes)",
+            "config": {"workload": "navier3d_tet_h1p2x3_%d3x6_gauss4_lame_%dfreq" % (m, F), "elements": E, "nnz_per_freq": nnz,
+                       "frequencies": F, "l2": "CSR outputs larger than L2, no flush", "parallelism": "single"},
+            "nnz_per_s": F * nnz / (res["mixed"] / 1000.0),
+            "fp64": {"value": F * E / (res["fp64"] / 1000.0), "ms_per_step": res["fp64"]},
+            "speedup_mixed_vs_fp64": res["fp64"] / res["mixed"], "mixed_vs_fp64_rel_fro_freq0": res["rel_fro"],
+            "roofline": {"bound": "hbm", "kernel": dom, "kernel_avg_ms": avg, "algorithmic_bytes": alg,
+                         "achieved": alg / (avg / 1000.0) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": alg / (avg / 1000.0) / 1e9 / pk["hbm_gbs"], "peak_source": pk_kind,
+                         "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()}}}
+    print(json.dumps(line), flush=True)
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -189,6 +315,10 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=60000)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--c4-n", type=int, default=64)
+    ap.add_argument("--c4-m-lo", type=int, default=8)
+    ap.add_argument("--c4-m-hi", type=int, default=48)
+    ap.add_argument("--n-freq", type=int, default=16)
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -201,6 +331,11 @@ def main():
     if ws > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     femg = load_femg()
+    if args.workload in ("c4", "c5mf"):
+        if ws > 1:
+            raise SystemExit("the batched and multi-frequency workloads run on one GPU")
+        (bench_batch if args.workload == "c4" else bench_multi_freq)(args, femg, torch)
+        return
     cfg, wname = workload_config(femg, args.workload, args.m)
     t0 = time.perf_counter()
     prob = femg.Problem(cfg)

@@ -391,22 +391,41 @@ __device__ inline void drainColumns(const GemmProblem &g, uint32_t tmemRow, floa
         if (dlive) *reinterpret_cast<float4 *>(dst + c + 4 * part) = val;
       }
       __syncwarp();
-    } else if (live) {
-      for (int k = 0; k < 32; ++k)
-        if (c + k < nn2) out[c + k] = v[k];
+    } else {
+      // rows not 16-byte aligned (n^2 not a multiple of 4): transpose through
+      // the stage and write one row per instruction, 32 consecutive floats
+#pragma unroll
+      for (int k = 0; k < 32; ++k) stage[lane * 33 + k] = v[k];
+      __syncwarp();
+      for (int rr = 0; rr < 32; ++rr) {
+        float *dst = reinterpret_cast<float *>(__shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(out), rr));
+        const bool dlive = __shfl_sync(0xffffffffu, live ? 1 : 0, rr) != 0;
+        if (dlive && c + lane < nn2) dst[c + lane] = stage[rr * 33 + lane];
+      }
+      __syncwarp();
     }
   }
   if (c < c1) {
     float v[16];
     tmemLoad16(tmemRow + (uint32_t)c, v);
-    if (live) {
-      if (vec && c + 16 <= nn2) {
+    if (vec && c + 16 <= nn2) {
+      if (live) {
 #pragma unroll
         for (int k = 0; k < 16; k += 4) *reinterpret_cast<float4 *>(out + c + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
-      } else {
-        for (int k = 0; k < 16; ++k)
-          if (c + k < nn2) out[c + k] = v[k];
       }
+    } else {
+      // two rows per instruction, 16 consecutive floats each
+#pragma unroll
+      for (int k = 0; k < 16; ++k) stage[lane * 33 + k] = v[k];
+      __syncwarp();
+      const int col = lane & 15;
+      for (int rr = 0; rr < 32; rr += 2) {
+        const int row = rr + (lane >> 4);
+        float *dst = reinterpret_cast<float *>(__shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(out), row));
+        const bool dlive = __shfl_sync(0xffffffffu, live ? 1 : 0, row) != 0;
+        if (dlive && c + col < nn2) dst[c + col] = stage[row * 33 + col];
+      }
+      __syncwarp();
     }
   }
 }
