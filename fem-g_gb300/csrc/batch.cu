@@ -416,12 +416,12 @@ extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const 
       if ((st = ensureDevice((void **)&pl->ke, &pl->keBytes, (size_t)pl->d.E * ncomp * pl->d.n * pl->d.n * sizeof(double)))) return fail(st);
     }
   }
-  // reduction classes: (element type, order, rule, slot width, complex)
-  std::map<std::tuple<int, int, int, int, int, int>, int> classOf;
+  // reduction classes: (element type, order, rule, slot width, complex, field components)
+  std::map<std::tuple<int, int, int, int, int, int, int>, int> classOf;
   for (int q = 0; q < n_problems; ++q) {
     const PlanDev &p = plans[q]->d;
     const int kc = b->terms[q].complexKe ? 1 : 0;
-    auto key = std::make_tuple(p.dim, p.nn, p.n, p.nq, p.slotBytes, kc);
+    auto key = std::make_tuple(p.dim, p.nn, p.n, p.nq, p.slotBytes, kc, p.mult);
     auto it = classOf.find(key);
     if (it == classOf.end()) {
       GatherClass c;

@@ -91,8 +91,9 @@ struct PlanDev {
   const uint32_t *rowOrder;// rows sorted by their number of contributing element rows
   const uint4 *visit;      // per visited row: row, CSR start, element-list start, len | count << 16
   const uint32_t *visitElem;// element lists in visiting order
-  const void *slot;       // [E][n][n] uint8 or uint16 position in the row
+  const void *slot;       // [E][n][slotLd] uint8 or uint16 position in the row
   int32_t slotBytes;
+  int32_t slotLd;         // slot row stride (entries)
   int32_t maxRowLen;
 };
 
@@ -166,7 +167,7 @@ struct GatherJob {
   int64_t blockStart, nBlocks;
 };
 struct GatherShape {
-  int L = 0, wpb = 0, rowsPerBlock = 0;
+  int L = 0, J = 3, wpb = 0, rowsPerBlock = 0;  // lanes per row, columns per lane
   size_t smem = 0;
   bool ok = false;
 };

@@ -76,7 +76,7 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
       const uint32_t e32 = packed >> 6;
       const int i = packed & 63;
       f_ = e32 * (uint32_t)n + (uint32_t)i;  // element row index (< 2^32 by plan checks)
-      const SlotT *S = slot + (size_t)f_ * n;
+      const SlotT *S = slot + (size_t)f_ * p.slotLd;
       const KT *K = ke + (size_t)e32 * SS * nn2;
 #pragma unroll
       for (int jj = 0; jj < J; ++jj) {
@@ -234,6 +234,7 @@ int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, 
 // Shared memory and rows per block of one gather configuration
 GatherShape gatherShape(int n, int maxRowLen, int kcplx, int keIsFloat, int L, int wpb) {
   GatherShape g;
+  g.J = 3;
   if (L <= 0) {
     L = 32;
     if (n <= 6) L = 2;

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256)
         const uint32_t packed = p.visitElem[r0 + k];
         const int64_t e = packed >> 6;
         const int i = packed & 63;
-        const SlotT *S = slot + ((size_t)e * n + i) * n;
+        const SlotT *S = slot + ((size_t)e * n + i) * p.slotLd;
         if (in.be && lt == 0) bsum = cadd(bsum, in.be[e * n + i]);
 #pragma unroll
         for (int jj = 0; jj < J; ++jj) {

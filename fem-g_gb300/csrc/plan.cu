@@ -298,7 +298,9 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   d.maxRowLen = (int32_t)maxLen;
   const bool narrow = maxLen < 0xFE;
   d.slotBytes = narrow ? 1 : 2;
-  const size_t nSlots = (size_t)E * n * n;
+  const int nS = n;
+  d.slotLd = nS;
+  const size_t nSlots = (size_t)E * n * nS;
   std::vector<uint8_t> slot8;
   std::vector<uint16_t> slot16;
   if (narrow) slot8.assign(nSlots, 0xFF); else slot16.assign(nSlots, kSlotIgnore);
@@ -326,7 +328,7 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
             s = (uint16_t)(p - b);
           }
         }
-        const size_t ks = ki * n + j;
+        const size_t ks = ki * nS + j;
         if (narrow) slot8[ks] = s == kSlotFixed ? 0xFF : (s == kSlotIgnore ? 0xFE : (uint8_t)s);
         else slot16[ks] = s;
       }
