@@ -99,6 +99,26 @@ __host__ __device__ inline void splitTf32(double x, float &hi, float &lo) {
   lo = tf32Round((float)(x - (double)hi));
 }
 
+// The same split on the device with one FP64 operation (GB300's FP64 pipe is
+// narrow): x rounded to 11 significant bits on its bit pattern (ties away
+// from zero, the carry runs into the exponent), the exact remainder rounded
+// the same way, each narrowed to float by moving the exponent.
+__device__ inline double roundTf32Bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return __longlong_as_double((long long)((b + (1ull << 41)) & ~((1ull << 42) - 1ull)));
+}
+__device__ inline float narrowTf32(double h) {  // h has at most 11 significant bits
+  const unsigned long long b = (unsigned long long)__double_as_longlong(h);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+  if (e <= 0 || e >= 255) return (float)h;  // zero, float subnormal, overflow, inf/nan
+  return __uint_as_float(((uint32_t)(b >> 32) & 0x80000000u) | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7FFFFFu));
+}
+__device__ inline void splitTf32Dev(double x, float &hi, float &lo) {
+  const double h = roundTf32Bits(x);
+  hi = narrowTf32(h);
+  lo = narrowTf32(roundTf32Bits(x - h));  // x - h is exact
+}
+
 // ------------------------------------------------------- PTX primitives
 
 __device__ inline uint32_t smemAddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -202,10 +222,11 @@ __device__ inline void tmemLoad32(uint32_t taddr, float *v) {
 __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
                                               float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff, int64_t e) {
   double X[kMaxNodes * 3];
-  for (int k = 0; k < p.nn; ++k)
+  const int nx = p.p1geom ? p.dim + 1 : p.nn;
+  for (int k = 0; k < nx; ++k)
     for (int c = 0; c < 3; ++c) X[3 * k + c] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + k] + c];
   double J[9], Ji[9];
-  const double det = jacobian(p.dim, p.nn, X, p.geoGrad, J);  // q = 0: affine
+  const double det = p.p1geom ? jacobianP1(p.dim, X, J) : jacobian(p.dim, p.nn, X, p.geoGrad, J);  // q = 0: affine
   jacobianInverse(J, det, Ji);
   double K[6];
   const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
@@ -231,7 +252,7 @@ __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *
     float *row = A + (r0 + comp) * kK3;
     for (int k = 0; k < kKp; ++k) {
       float hi, lo;
-      splitTf32(d[k], hi, lo);
+      splitTf32Dev(d[k], hi, lo);
       row[k] = hi;
       row[kKp + k] = lo;
       row[2 * kKp + k] = hi;
@@ -259,10 +280,11 @@ constexpr int kK3E = 3 * kKpE;
 __device__ __forceinline__ void factorsElastic(const PlanDev &p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
                                                float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff, int64_t e) {
   double X[kMaxNodes * 3];
-  for (int k = 0; k < p.nn; ++k)
+  const int nx = p.p1geom ? p.dim + 1 : p.nn;
+  for (int k = 0; k < nx; ++k)
     for (int c = 0; c < 3; ++c) X[3 * k + c] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + k] + c];
   double J[9], Ji[9];
-  const double det = jacobian(p.dim, p.nn, X, p.geoGrad, J);
+  const double det = p.p1geom ? jacobianP1(p.dim, X, J) : jacobian(p.dim, p.nn, X, p.geoGrad, J);
   jacobianInverse(J, det, Ji);  // Ji[3p + a] = (J^-1)(p, a)
   double K[9];
   for (int a = 0; a < 3; ++a)
@@ -293,7 +315,7 @@ __device__ __forceinline__ void factorsElastic(const PlanDev &p, const DevTerms 
         float *row = A + (r0 + comp * 9 + 3 * a + b) * kK3E;
         for (int k = 0; k < kKpE; ++k) {
           float hi, lo;
-          splitTf32(d[k], hi, lo);
+          splitTf32Dev(d[k], hi, lo);
           row[k] = hi;
           row[kKpE + k] = lo;
           row[2 * kKpE + k] = hi;

@@ -73,6 +73,7 @@ struct DevTerms {
 // Device-resident data of one element bucket
 struct PlanDev {
   int32_t dim, nn, nq, nb, mult, n, nOrient, affine;
+  int32_t p1geom;         // first-order simplex geometry with the standard node order
   int64_t E, nNodes;
   uint64_t nRows, nnz, nFixed;
   const double *xyz;      // [nNodes][3]
@@ -309,6 +310,23 @@ __device__ inline double jacobian(int dim, int nn, const double *X /*[nn][3]*/, 
     J[8] = nz / len;
   }
   // det of the column-major matrix
+  return J[0] * (J[4] * J[8] - J[7] * J[5]) - J[3] * (J[1] * J[8] - J[7] * J[2]) + J[6] * (J[1] * J[5] - J[4] * J[2]);
+}
+
+// The same for first-order simplex geometry (N_0 = 1 - sum u, N_k = u_k):
+// the Jacobian's columns are edge vectors from node 0; X holds dim + 1 nodes.
+__device__ inline double jacobianP1(int dim, const double *X, double *J) {
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) J[3 * c + r] = c < dim ? X[3 * (c + 1) + r] - X[r] : 0.0;
+  if (dim == 2) {
+    const double nx = J[1] * J[5] - J[2] * J[4];
+    const double ny = J[2] * J[3] - J[0] * J[5];
+    const double nz = J[0] * J[4] - J[1] * J[3];
+    const double len = sqrt(nx * nx + ny * ny + nz * nz);
+    J[6] = nx / len;
+    J[7] = ny / len;
+    J[8] = nz / len;
+  }
   return J[0] * (J[4] * J[8] - J[7] * J[5]) - J[3] * (J[1] * J[8] - J[7] * J[2]) + J[6] * (J[1] * J[5] - J[4] * J[2]);
 }
 

@@ -158,6 +158,13 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   d.n = n;
   d.nOrient = space->n_orientations;
   d.affine = (nn == mesh->dim + 1) ? 1 : 0;
+  // first-order simplex with the standard basis: dN_0 = -1, dN_k = e_(k-1)
+  d.p1geom = d.affine;
+  for (int k = 0; k < nn && d.p1geom; ++k)
+    for (int c = 0; c < mesh->dim; ++c) {
+      const double want = k == 0 ? -1.0 : (c == k - 1 ? 1.0 : 0.0);
+      if (rule->geo_grad[(size_t)k * 3 + c] != want) d.p1geom = 0;
+    }
   d.E = E;
   d.nNodes = mesh->n_nodes;
   d.nRows = sys->n_rows;
@@ -577,8 +584,8 @@ int fg_plan_create(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_
   if (!out) return FG_ERR_ARG;
   *out = nullptr;
   if (!mesh || !rule || !space || !sys || !mesh->node_xyz || !mesh->elem_nodes || !rule->weights || !rule->geo_val ||
-      !rule->geo_grad || !space->basis_val || !space->basis_grad || !sys->ai || !sys->aj || !sys->elem_dof_idx ||
-      !sys->elem_dof_type) {
+      !rule->geo_grad || !space->basis_val || !space->basis_grad || !sys->ai || !sys->elem_dof_idx || !sys->elem_dof_type ||
+      (!sys->aj && sys->ai[sys->n_rows] != 0)) {
     setLastError("fg_plan_create: null descriptor field");
     return FG_ERR_ARG;
   }
