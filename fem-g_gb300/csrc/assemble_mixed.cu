@@ -245,18 +245,19 @@ __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *
   for (int comp = 0; comp < ncomp; ++comp) {
     const double g = (comp == 0 ? cgg.x : cgg.y) * det;
     const double m = (comp == 0 ? cm.x : cm.y) * det;
-    double d[kKp];
-    for (int k = 0; k < 6; ++k) d[k] = g * K[k];
-    d[6] = m;
-    d[7] = 0.0;
-    float *row = A + (r0 + comp) * kK3;
-    for (int k = 0; k < kKp; ++k) {
-      float hi, lo;
-      splitTf32Dev(d[k], hi, lo);
-      row[k] = hi;
-      row[kKp + k] = lo;
-      row[2 * kKp + k] = hi;
-    }
+    float hi[kKp], lo[kKp];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) splitTf32Dev(g * K[k], hi[k], lo[k]);
+    splitTf32Dev(m, hi[6], lo[6]);
+    hi[7] = lo[7] = 0.0f;
+    // [hi | lo | hi] as 16-byte stores (rows are 96 bytes)
+    float4 *row = reinterpret_cast<float4 *>(A + (r0 + comp) * kK3);
+    row[0] = make_float4(hi[0], hi[1], hi[2], hi[3]);
+    row[1] = make_float4(hi[4], hi[5], hi[6], hi[7]);
+    row[2] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+    row[3] = make_float4(lo[4], lo[5], lo[6], lo[7]);
+    row[4] = row[0];
+    row[5] = row[1];
   }
 }
 
@@ -304,22 +305,45 @@ __device__ __forceinline__ void factorsElastic(const PlanDev &p, const DevTerms 
   for (int comp = 0; comp < ncomp; ++comp) {
     const double l = (comp == 0 ? lam.x : lam.y) * det, m = (comp == 0 ? mu.x : mu.y) * det;
     const double c = (comp == 0 ? cm.x : cm.y) * det;
+    double lJ[9], mJ[9];  // l Ji, m Ji
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      lJ[k] = l * Ji[k];
+      mJ[k] = m * Ji[k];
+    }
+    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
     for (int a = 0; a < 3; ++a)
+#pragma unroll
       for (int b = 0; b < 3; ++b) {
-        double d[kKpE];
+        float hi[12], lo[12];
+#pragma unroll
         for (int pp = 0; pp < 3; ++pp)
-          for (int q = 0; q < 3; ++q)
-            d[3 * pp + q] = l * Ji[3 * pp + b] * Ji[3 * q + a] + m * Ji[3 * pp + a] * Ji[3 * q + b] + (a == b ? m * K[3 * pp + q] : 0.0);
-        d[9] = a == b ? c : 0.0;
-        for (int k = 10; k < kKpE; ++k) d[k] = 0.0;
-        float *row = A + (r0 + comp * 9 + 3 * a + b) * kK3E;
-        for (int k = 0; k < kKpE; ++k) {
-          float hi, lo;
-          splitTf32Dev(d[k], hi, lo);
-          row[k] = hi;
-          row[kKpE + k] = lo;
-          row[2 * kKpE + k] = hi;
-        }
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            double d = fma(lJ[3 * pp + b], Ji[3 * q + a], mJ[3 * pp + a] * Ji[3 * q + b]);
+            if (a == b) d = fma(m, K[3 * pp + q], d);
+            splitTf32Dev(d, hi[3 * pp + q], lo[3 * pp + q]);
+          }
+        if (a == b) splitTf32Dev(c, hi[9], lo[9]);
+        else hi[9] = lo[9] = 0.0f;
+        hi[10] = hi[11] = lo[10] = lo[11] = 0.0f;
+        // [hi | lo | hi] of 16 columns (10 used) as 16-byte stores (rows are 192 bytes)
+        float4 *row = reinterpret_cast<float4 *>(A + (r0 + comp * 9 + 3 * a + b) * kK3E);
+        const float4 h0 = make_float4(hi[0], hi[1], hi[2], hi[3]), h1 = make_float4(hi[4], hi[5], hi[6], hi[7]),
+                     h2 = make_float4(hi[8], hi[9], 0.0f, 0.0f);
+        row[0] = h0;
+        row[1] = h1;
+        row[2] = h2;
+        row[3] = zero;
+        row[4] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        row[5] = make_float4(lo[4], lo[5], lo[6], lo[7]);
+        row[6] = make_float4(lo[8], lo[9], 0.0f, 0.0f);
+        row[7] = zero;
+        row[8] = h0;
+        row[9] = h1;
+        row[10] = h2;
+        row[11] = zero;
       }
   }
 }
