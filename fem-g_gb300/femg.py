@@ -99,6 +99,7 @@ def lib():
         "fg_batch_run": (C.c_int, [P, P, P, P]),
         "fg_batch_destroy": (None, [P]),
         "fg_batch_tuning": (C.c_char_p, [P]),
+        "fg_pattern_build": (C.c_int, [P, P, C.c_int64, C.c_int32, C.c_uint64, P, C.POINTER(P)]),
         "fg_profile_enable": (C.c_int, [C.c_int]),
         "fg_profile_read": (C.c_int, [C.c_char_p, C.c_int32, P, P, C.c_int32]),
         "fg_last_error": (C.c_char_p, []),
@@ -129,7 +130,7 @@ def exported_symbols():
     """Names bound above (the C ABI of both headers)."""
     return [
         "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_assemble_fp64", "fg_assemble_mixed",
-        "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_profile_enable",
+        "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_pattern_build", "fg_profile_enable",
         "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
         "fg_problem_raw_dofs", "fg_problem_created_dofs", "fg_problem_reserve_log", "fg_problem_bbox", "fg_problem_pre_seconds", "fg_problem_assemble",
@@ -434,3 +435,19 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def pattern_build(edof, etype, n_rows):
+    """fg_pattern_build on an element DOF map ([E][n] indices and types):
+    (ai, aj) as numpy uint64 arrays."""
+    L = lib()
+    edof = np.ascontiguousarray(edof, np.uint64)
+    etype = np.ascontiguousarray(etype, np.int32)
+    E, n = edof.shape
+    ai = np.zeros(int(n_rows) + 1, np.uint64)
+    ajp = C.c_void_p()
+    check(L.fg_pattern_build(edof.ctypes.data, etype.ctypes.data, E, n, int(n_rows), ai.ctypes.data, C.byref(ajp)))
+    nnz = int(ai[-1])
+    aj = np.ctypeslib.as_array(C.cast(ajp, C.POINTER(C.c_uint64)), shape=(max(nnz, 1),))[:nnz].copy()
+    L.fg_host_free(ajp)
+    return ai, aj

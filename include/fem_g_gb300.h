@@ -245,6 +245,20 @@ void fg_batch_destroy(fg_batch *batch);
  * empty before it. Valid until the next call on the batch. */
 const char *fg_batch_tuning(const fg_batch *batch);
 
+/* --------------------------------------------------------- symbolic phase */
+
+/* GPU symbolic assembly of one element bucket's CSR pattern, the part of the
+ * reference's pre() done by MatrixFactory::addPattern
+ * (src/system/MatrixFactory.cpp:459-539) and finalizePattern (:188-213) when
+ * the test and unknown DOFs are one field: row I (an Unknown, Unknown bubble
+ * or Unknown global DOF) holds the sorted unique Unknown DOFs of the elements
+ * that have I, Fixed DOFs take no column, and the bubble rows of an element
+ * after its first alias that row. elem_dof_idx / elem_dof_type as in
+ * fg_system_desc ([n_elements][n_dofs]). ai: [n_rows + 1], the caller's;
+ * *aj: [ai[n_rows]] allocated by the call (free it with fg_host_free). */
+int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *elem_dof_type, int64_t n_elements, int32_t n_dofs,
+                     uint64_t n_rows, uint64_t *ai, uint64_t **aj);
+
 /* ----------------------------------------------------------------- misc */
 
 const char *fg_last_error(void);
