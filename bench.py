@@ -73,7 +73,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -416,13 +416,15 @@ def main():
             ms = max_over_ranks(ms, dist, "cuda")
         return ms, launches, prof
 
+    # clocks are sampled over both timed regions (the mixed one alone lasts
+    # only milliseconds)
     clocks = ClockSampler(local)
     clocks.start()
     head = precisions[0]
     ms_head, launches, prof = timed(head, dv, args.steps, profile=True)
-    clk = clocks.stop()
     fp64_steps = max(3, min(args.steps, 5)) if head == "mixed" else args.steps
     ms_fp64 = ms_head if head == "fp64" else timed("fp64", dv64, fp64_steps)[0]
+    clk = clocks.stop()
     if head == "mixed":
         step("fp64", dv64)
         torch.cuda.synchronize()
