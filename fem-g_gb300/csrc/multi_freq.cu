@@ -16,6 +16,7 @@
 // scaled the same way). The reduction visits the element rows in the order
 // of the single-frequency gather, so each group sum is deterministic.
 #include <cstring>
+#include <functional>
 
 #include "common.cuh"
 
@@ -28,12 +29,13 @@ struct MultiIn {
   const void *ke[kMaxGroups];    // element matrices of group g (KT)
   int64_t stride[kMaxGroups];    // KT entries from one element to the next
   int cplx[kMaxGroups];          // group g has an imaginary part (at +n*n)
-  int G, F, blk3;
-  const double2 *coef;           // [F][G] module factors
+  int G, F, R, blk3;
+  const double2 *coef;           // [F][G] factors of the value arrays
+  const double2 *rcoef;          // [R][G] factors of the liftings in the right-hand sides
   const double2 *be;             // [E][n] element right-hand sides or null
   const double2 *uD;             // Dirichlet values or null
-  double2 *values;               // [F][nnz]
-  double2 *rhs;                  // [F][nRows] or null
+  double2 *const *values;        // F value arrays [nnz] (device table)
+  double2 *const *rhs;           // R right-hand sides [nRows] (device table), or null
 };
 
 template <typename SlotT, typename KT, int L>
@@ -143,7 +145,7 @@ __global__ void __launch_bounds__(256)
           re += cr * ar[g] - ci * ai[g];
           im += cr * ai[g] + ci * ar[g];
         }
-        in.values[(size_t)f * p.nnz + start + s] = make_double2(widen(re), widen(im));
+        in.values[f][start + s] = make_double2(widen(re), widen(im));
       }
     }
     if (in.rhs) {
@@ -157,12 +159,12 @@ __global__ void __launch_bounds__(256)
           }
       }
       if (live && lt == 0)
-        for (int f = 0; f < F; ++f) {
-          double2 r = bsum;
+        for (int r = 0; r < in.R; ++r) {
+          double2 v = bsum;
 #pragma unroll
           for (int g = 0; g < kMaxGroups; ++g)
-            if (g < G) r = cadd(r, cmul(in.coef[f * G + g], dc[g]));
-          in.rhs[(size_t)f * p.nRows + row] = r;
+            if (g < G) v = cadd(v, cmul(in.rcoef[r * G + g], dc[g]));
+          in.rhs[r][row] = v;
         }
     }
     __syncwarp();
@@ -229,7 +231,8 @@ struct MultiState {
   std::vector<void *> arrays[kMaxGroups];
   double *ke[kMaxGroups] = {nullptr, nullptr, nullptr};
   size_t keBytes[kMaxGroups] = {0, 0, 0};
-  double2 *coef = nullptr;
+  double2 *coef = nullptr;                   // [kMaxFreq][kMaxGroups] value factors, then as many lifting factors
+  double2 **ptrs = nullptr;                  // device tables: value arrays, then right-hand sides
   double *values = nullptr, *rhs = nullptr;  // staging for host outputs
   size_t valuesBytes = 0, rhsBytes = 0;
 };
@@ -252,30 +255,32 @@ extern "C" void multiDestroy(fg_plan *plan) {
     cudaFree(m->ke[g]);
   }
   cudaFree(m->coef);
+  cudaFree(m->ptrs);
   cudaFree(m->values);
   cudaFree(m->rhs);
   delete m;
   plan->multi = nullptr;
 }
 
-extern "C" int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, const double *omegas, int32_t n_freq,
-                                      int32_t mixed, const double *dirichlet, double *csr_values, double *rhs, void *stream) {
-  if (!plan) return FG_ERR_ARG;
-  if (!terms || n_terms <= 0 || n_terms > kMaxTerms || !omegas || n_freq <= 0 || n_freq > kMaxFreq || !csr_values) {
-    setLastError("fg_assemble_multi_freq: terms, 1..64 frequencies and csr_values are required");
-    return FG_ERR_ARG;
-  }
-  cudaStream_t s = (cudaStream_t)stream;
+namespace {
+
+// Splits the terms by time derivative, integrates each group once (unit
+// factor) and runs the fused reduction. coefOf(dts, G, coef, rcoef) fills
+// the [F][G] value factors and [R][G] lifting factors. values[f] /
+// rhs[r]: host or device arrays ([nnz] / [nRows]); rhs may be null.
+int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t mixed, const double *dirichlet, int F,
+              double *const *values, int R, double *const *rhs, cudaStream_t s,
+              const std::function<int(const int *, int, double2 *, double2 *)> &coefOf) {
   MultiState *m = multiState(plan);
   const PlanDev &p = plan->d;
-  // groups by time derivative; the module factor is applied in the reduction
+  // groups by time derivative; the factors are applied in the reduction
   int dts[kMaxGroups], G = 0;
   fg_term_desc grp[kMaxTerms];
   for (int d = FG_DT_NONE; d <= FG_DT_2; ++d) {
     int cnt = 0;
     for (int t = 0; t < n_terms; ++t) {
       if (terms[t].dt < FG_DT_NONE || terms[t].dt > FG_DT_2) {
-        setLastError("fg_assemble_multi_freq: unknown time derivative");
+        setLastError("unknown time derivative");
         return FG_ERR_ARG;
       }
       if (terms[t].kind == FG_TERM_SOURCE && terms[t].dt != FG_DT_NONE) {
@@ -295,33 +300,39 @@ extern "C" int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, 
     FG_CUDA(cudaMemcpyAsync(m->dev[G], &m->terms[G], sizeof(DevTerms), cudaMemcpyHostToDevice, s));
     dts[G++] = d;
   }
-  std::vector<double2> coef((size_t)n_freq * G);
-  for (int f = 0; f < n_freq; ++f)
-    for (int g = 0; g < G; ++g) {
-      const double w = omegas[f];
-      coef[(size_t)f * G + g] = dts[g] == FG_DT_2 ? make_double2(-w * w, 0.0) : dts[g] == FG_DT_1 ? make_double2(0.0, -w) : make_double2(1.0, 0.0);
-    }
-  if (!m->coef) FG_CUDA(cudaMalloc(&m->coef, (size_t)kMaxFreq * kMaxGroups * sizeof(double2)));
+  std::vector<double2> coef((size_t)2 * kMaxFreq * kMaxGroups, make_double2(0.0, 0.0));
+  int st = coefOf(dts, G, coef.data(), coef.data() + (size_t)kMaxFreq * kMaxGroups);
+  if (st) return st;
+  if (!m->coef) FG_CUDA(cudaMalloc(&m->coef, coef.size() * sizeof(double2)));
   FG_CUDA(cudaMemcpyAsync(m->coef, coef.data(), coef.size() * sizeof(double2), cudaMemcpyHostToDevice, s));
   const double *uD = nullptr;
-  int st = uploadDirichlet(plan, dirichlet, &uD, s);
-  if (st) return st;
-  // outputs: device pointers in place, host pointers through staging buffers
-  const bool hostValues = !isDevicePointer(csr_values);
-  const bool hostRhs = rhs && !isDevicePointer(rhs);
-  double *dValues = csr_values, *dRhs = rhs;
-  if (hostValues) {
-    if ((st = ensureDevice((void **)&m->values, &m->valuesBytes, (size_t)n_freq * p.nnz * 16))) return st;
-    dValues = m->values;
+  if ((st = uploadDirichlet(plan, dirichlet, &uD, s))) return st;
+  // outputs: device arrays in place, host arrays through staging buffers
+  std::vector<double2 *> dv(F), dr(R, nullptr);
+  std::vector<char> hv(F, 0), hr(R, 0);
+  size_t stageV = 0, stageR = 0;
+  for (int f = 0; f < F; ++f) {
+    hv[f] = !isDevicePointer(values[f]);
+    stageV += hv[f];
   }
-  if (hostRhs) {
-    if ((st = ensureDevice((void **)&m->rhs, &m->rhsBytes, (size_t)n_freq * p.nRows * 16))) return st;
-    dRhs = m->rhs;
+  for (int r = 0; r < R; ++r) {
+    hr[r] = rhs[r] && !isDevicePointer(rhs[r]);
+    stageR += hr[r];
   }
+  if (stageV && (st = ensureDevice((void **)&m->values, &m->valuesBytes, stageV * p.nnz * 16))) return st;
+  if (stageR && (st = ensureDevice((void **)&m->rhs, &m->rhsBytes, stageR * p.nRows * 16))) return st;
+  for (int f = 0, k = 0; f < F; ++f) dv[f] = hv[f] ? (double2 *)(m->values + 2 * p.nnz * k++) : (double2 *)values[f];
+  for (int r = 0, k = 0; r < R; ++r) dr[r] = hr[r] ? (double2 *)(m->rhs + 2 * p.nRows * k++) : (double2 *)rhs[r];
+  const bool anyRhs = R > 0 && rhs[0];
+  if (!m->ptrs) FG_CUDA(cudaMalloc(&m->ptrs, 2 * kMaxFreq * sizeof(double2 *)));
+  std::vector<double2 *> table(2 * kMaxFreq, nullptr);
+  std::copy(dv.begin(), dv.end(), table.begin());
+  std::copy(dr.begin(), dr.end(), table.begin() + kMaxFreq);
+  FG_CUDA(cudaMemcpyAsync(m->ptrs, table.data(), table.size() * sizeof(double2 *), cudaMemcpyHostToDevice, s));
   // source terms are linear terms without time derivative: group of dt 0
   const int g0 = dts[0] == FG_DT_NONE ? 0 : -1;
   double *be = nullptr;
-  const bool source = g0 == 0 && m->terms[0].hasSource && rhs;
+  const bool source = g0 == 0 && m->terms[0].hasSource && anyRhs;
   if (source) {
     if ((st = ensureDevice((void **)&plan->be, &plan->beBytes, (size_t)p.E * p.n * 16))) return st;
     be = plan->be;
@@ -329,12 +340,14 @@ extern "C" int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, 
   MultiIn in;
   std::memset(&in, 0, sizeof(in));
   in.G = G;
-  in.F = n_freq;
+  in.F = F;
+  in.R = anyRhs ? R : 0;
   in.coef = m->coef;
+  in.rcoef = m->coef + (size_t)kMaxFreq * kMaxGroups;
   in.be = (const double2 *)be;
   in.uD = (const double2 *)uD;
-  in.values = (double2 *)dValues;
-  in.rhs = (double2 *)dRhs;
+  in.values = m->ptrs;
+  in.rhs = anyRhs ? m->ptrs + kMaxFreq : nullptr;
   const size_t nn = (size_t)p.n * p.n;
   bool isFloat = false;
   if (!mixed) {
@@ -378,11 +391,89 @@ extern "C" int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, 
   if ((st = launchGatherMulti(plan, in, isFloat, s))) return st;
   if (mixed)
     if ((st = mixedRecordError(plan, s))) return st;
-  if (hostValues) FG_CUDA(cudaMemcpyAsync(csr_values, dValues, (size_t)n_freq * p.nnz * 16, cudaMemcpyDeviceToHost, s));
-  if (hostRhs) FG_CUDA(cudaMemcpyAsync(rhs, dRhs, (size_t)n_freq * p.nRows * 16, cudaMemcpyDeviceToHost, s));
-  if (hostValues || hostRhs) {
+  bool anyHost = false;
+  for (int f = 0; f < F; ++f)
+    if (hv[f]) {
+      FG_CUDA(cudaMemcpyAsync(values[f], dv[f], p.nnz * 16, cudaMemcpyDeviceToHost, s));
+      anyHost = true;
+    }
+  for (int r = 0; r < R; ++r)
+    if (hr[r]) {
+      FG_CUDA(cudaMemcpyAsync(rhs[r], dr[r], p.nRows * 16, cudaMemcpyDeviceToHost, s));
+      anyHost = true;
+    }
+  if (anyHost) {
     FG_CUDA(cudaStreamSynchronize(s));
     if (mixed) return mixedCheckTimeout(plan, true);
   }
   return FG_OK;
+}
+
+}  // namespace
+
+extern "C" int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, const double *omegas, int32_t n_freq,
+                                      int32_t mixed, const double *dirichlet, double *csr_values, double *rhs, void *stream) {
+  if (!plan) return FG_ERR_ARG;
+  if (!terms || n_terms <= 0 || n_terms > kMaxTerms || !omegas || n_freq <= 0 || n_freq > kMaxFreq || !csr_values) {
+    setLastError("fg_assemble_multi_freq: terms, 1..64 frequencies and csr_values are required");
+    return FG_ERR_ARG;
+  }
+  const PlanDev &p = plan->d;
+  std::vector<double *> v(n_freq), r(n_freq);
+  for (int f = 0; f < n_freq; ++f) {
+    v[f] = csr_values + 2 * p.nnz * (size_t)f;
+    r[f] = rhs ? rhs + 2 * p.nRows * (size_t)f : nullptr;
+  }
+  // AFrequency factors (src/term/Assembler.cpp:283-295), on values and liftings alike
+  auto coefOf = [&](const int *dts, int G, double2 *coef, double2 *rcoef) {
+    for (int f = 0; f < n_freq; ++f)
+      for (int g = 0; g < G; ++g) {
+        const double w = omegas[f];
+        const double2 c = dts[g] == FG_DT_2 ? make_double2(-w * w, 0.0) : dts[g] == FG_DT_1 ? make_double2(0.0, -w) : make_double2(1.0, 0.0);
+        coef[(size_t)f * G + g] = c;
+        rcoef[(size_t)f * G + g] = c;
+      }
+    return FG_OK;
+  };
+  return runGroups(plan, terms, n_terms, mixed, dirichlet, n_freq, v.data(), rhs ? n_freq : 0, r.data(), (cudaStream_t)stream, coefOf);
+}
+
+extern "C" int fg_assemble_separate(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t mixed, const double *dirichlet,
+                                    double *k_values, double *c_values, double *m_values, double *rhs, void *stream) {
+  if (!plan) return FG_ERR_ARG;
+  if (!terms || n_terms <= 0 || n_terms > kMaxTerms) {
+    setLastError("fg_assemble_separate: terms are required");
+    return FG_ERR_ARG;
+  }
+  bool have[3] = {false, false, false};
+  for (int t = 0; t < n_terms; ++t)
+    if (terms[t].kind != FG_TERM_SOURCE && terms[t].dt >= FG_DT_NONE && terms[t].dt <= FG_DT_2) have[terms[t].dt] = true;
+  double *out[3] = {k_values, c_values, m_values};
+  for (int d = 0; d < 3; ++d) {
+    if (have[d] && !out[d]) {
+      setLastError("fg_assemble_separate: the formulation has a matrix whose output array is NULL");
+      return FG_ERR_ARG;
+    }
+  }
+  // value array f <- group f (the groups present, in the order K, C, M); the
+  // right-hand side lifts with K alone (src/term/Assembler.cpp:306-347)
+  auto coefOf = [&](const int *dts, int G, double2 *coef, double2 *rcoef) {
+    for (int f = 0; f < G; ++f)
+      for (int g = 0; g < G; ++g) coef[(size_t)f * G + g] = make_double2(f == g ? 1.0 : 0.0, 0.0);
+    for (int g = 0; g < G; ++g) rcoef[g] = make_double2(dts[g] == FG_DT_NONE ? 1.0 : 0.0, 0.0);
+    return FG_OK;
+  };
+  // a source without K terms still makes a group of dt 0
+  bool sourceOnlyK = false;
+  for (int t = 0; t < n_terms; ++t)
+    if (terms[t].kind == FG_TERM_SOURCE) sourceOnlyK = !have[0];
+  if (sourceOnlyK && !k_values) {
+    setLastError("fg_assemble_separate: source terms need k_values (the stiffness group carries the right-hand side)");
+    return FG_ERR_ARG;
+  }
+  std::vector<double *> vv;
+  for (int d = 0; d < 3; ++d)
+    if (have[d] || (d == FG_DT_NONE && sourceOnlyK)) vv.push_back(out[d]);
+  double *r[1] = {rhs};
+  return runGroups(plan, terms, n_terms, mixed, dirichlet, (int)vv.size(), vv.data(), rhs ? 1 : 0, r, (cudaStream_t)stream, coefOf);
 }

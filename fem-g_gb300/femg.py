@@ -95,6 +95,7 @@ def lib():
         "fg_assemble_mixed": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_double, P, P, P, P, C.POINTER(ErrReport)]),
         "fg_assemble_fp64_static": (C.c_int, [P, P, P, P, P]),
         "fg_assemble_multi_freq": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, P, C.c_int32, C.c_int32, P, P, P, P]),
+        "fg_assemble_separate": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_int32, P, P, P, P, P, P]),
         "fg_batch_create": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.POINTER(P)]),
         "fg_batch_run": (C.c_int, [P, P, P, P]),
         "fg_batch_destroy": (None, [P]),
@@ -130,7 +131,7 @@ def exported_symbols():
     """Names bound above (the C ABI of both headers)."""
     return [
         "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_assemble_fp64", "fg_assemble_mixed",
-        "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_pattern_build", "fg_profile_enable",
+        "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_assemble_separate", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_pattern_build", "fg_profile_enable",
         "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
         "fg_problem_raw_dofs", "fg_problem_created_dofs", "fg_problem_reserve_log", "fg_problem_bbox", "fg_problem_pre_seconds", "fg_problem_assemble",
@@ -347,6 +348,21 @@ class Plan:
     def bind_terms(self, frequency=0.0):
         t, nt = self.prob.terms()
         check(lib().fg_plan_bind_terms(self.ptr, t, nt, frequency))
+
+    def assemble_separate(self, precision="fp64", terms=None, with_rhs=True, stream=None):
+        """fg_assemble_separate: (K, C, M, rhs) numpy arrays (None for a
+        matrix the formulation does not have)."""
+        p = self.prob
+        t, nt = terms if terms is not None else p.terms()
+        have = set(int(t[i].dt) for i in range(nt) if t[i].kind != FG_TERM_SOURCE)
+        has_source = any(t[i].kind == FG_TERM_SOURCE for i in range(nt))
+        out = [np.zeros(p.nnz, np.complex128) if (d in have or (d == 0 and has_source)) else None for d in range(3)]
+        rhs = np.zeros(int(p.sys.n_rows), np.complex128) if with_rhs else None
+        ptr = lambda a: a.ctypes.data if a is not None else None
+        dptr = C.cast(p.dir_ptr, C.c_void_p) if p.sys.n_fixed else None
+        check(lib().fg_assemble_separate(self.ptr, t, nt, 1 if precision == "mixed" else 0, dptr, ptr(out[0]), ptr(out[1]),
+                                         ptr(out[2]), ptr(rhs), stream))
+        return out[0], out[1], out[2], rhs
 
     def assemble_multi_freq(self, omegas, precision="fp64", terms=None, values=None, rhs=None, stream=None):
         """fg_assemble_multi_freq: (values [F][nnz], rhs [F][n_rows]) for the

@@ -229,6 +229,17 @@ int fg_assemble_multi_freq(fg_plan *plan, const fg_term_desc *terms, int32_t n_t
                            int32_t n_freq, int32_t mixed, const double *dirichlet, double *csr_values, double *rhs,
                            void *stream);
 
+/* The system as separate matrices sharing the pattern, the reference's
+ * assemble(separate = true) with the MK, CK or MCK module
+ * (src/problem/Formulation.cpp:1096-1149, src/term/Assembler.cpp:306-347,
+ * src/system/MatrixModule.cpp:180-395): K from the terms without time
+ * derivative, C from the dt terms, M from the dt2 terms, each without the
+ * frequency factor; the right-hand side holds the sources and the Dirichlet
+ * lifting with K alone. An output may be NULL when the formulation has no
+ * term of that kind; host or device memory (detected). */
+int fg_assemble_separate(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t mixed, const double *dirichlet,
+                         double *k_values, double *c_values, double *m_values, double *rhs, void *stream);
+
 /* -------------------------------------------------------------- batching */
 
 typedef struct fg_batch fg_batch;
