@@ -29,6 +29,8 @@ struct MultiIn {
   const void *ke[kMaxGroups];    // element matrices of group g (KT)
   int64_t stride[kMaxGroups];    // KT entries from one element to the next
   int cplx[kMaxGroups];          // group g has an imaginary part (at +n*n)
+  int realFactor[kMaxGroups];    // the factors of group g are real for every output
+  int imagFactor[kMaxGroups];    // ... purely imaginary for every output
   int G, F, R, blk3;
   const double2 *coef;           // [F][G] factors of the value arrays
   const double2 *rcoef;          // [R][G] factors of the liftings in the right-hand sides
@@ -142,8 +144,18 @@ __global__ void __launch_bounds__(256)
         for (int g = 0; g < kMaxGroups; ++g) {
           if (g >= G) break;
           const AT cr = cf[2 * (f * G + g)], ci = cf[2 * (f * G + g) + 1];
-          re += cr * ar[g] - ci * ai[g];
-          im += cr * ai[g] + ci * ar[g];
+          // real sums and real or imaginary factors (the usual case) skip the
+          // zero products: they cost FP64 issue slots on the FP64 path
+          if (in.realFactor[g]) re += cr * ar[g];
+          else if (in.imagFactor[g]) im += ci * ar[g];
+          else {
+            re += cr * ar[g];
+            im += ci * ar[g];
+          }
+          if (in.cplx[g]) {
+            re -= ci * ai[g];
+            im += cr * ai[g];
+          }
         }
         in.values[f][start + s] = make_double2(widen(re), widen(im));
       }
@@ -341,6 +353,15 @@ int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t
   std::memset(&in, 0, sizeof(in));
   in.G = G;
   in.F = F;
+  for (int g = 0; g < G; ++g) {
+    bool re = true, im = true;
+    for (int f = 0; f < F; ++f) {
+      re = re && coef[(size_t)f * G + g].y == 0.0;
+      im = im && coef[(size_t)f * G + g].x == 0.0;
+    }
+    in.realFactor[g] = re;
+    in.imagFactor[g] = im && !re;
+  }
   in.R = anyRhs ? R : 0;
   in.coef = m->coef;
   in.rcoef = m->coef + (size_t)kMaxFreq * kMaxGroups;
