@@ -101,6 +101,8 @@ def lib():
         "fg_batch_destroy": (None, [P]),
         "fg_batch_tuning": (C.c_char_p, [P]),
         "fg_pattern_build": (C.c_int, [P, P, C.c_int64, C.c_int32, C.c_uint64, P, C.POINTER(P)]),
+        "fg_hilbert_order": (C.c_int, [C.c_int32, C.c_uint64, P, P, P, P]),
+        "fg_hilbert_numbering": (C.c_int, [C.c_int32, P, C.c_uint64, P, P, P]),
         "fg_profile_enable": (C.c_int, [C.c_int]),
         "fg_profile_read": (C.c_int, [C.c_char_p, C.c_int32, P, P, C.c_int32]),
         "fg_last_error": (C.c_char_p, []),
@@ -131,7 +133,7 @@ def exported_symbols():
     """Names bound above (the C ABI of both headers)."""
     return [
         "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_assemble_fp64", "fg_assemble_mixed",
-        "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_assemble_separate", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_pattern_build", "fg_profile_enable",
+        "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_assemble_separate", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_pattern_build", "fg_hilbert_order", "fg_hilbert_numbering", "fg_profile_enable",
         "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
         "fg_problem_raw_dofs", "fg_problem_created_dofs", "fg_problem_reserve_log", "fg_problem_bbox", "fg_problem_pre_seconds", "fg_problem_assemble",
@@ -467,3 +469,23 @@ def pattern_build(edof, etype, n_rows):
     aj = np.ctypeslib.as_array(C.cast(ajp, C.POINTER(C.c_uint64)), shape=(max(nnz, 1),))[:nnz].copy()
     L.fg_host_free(ajp)
     return ai, aj
+
+
+def hilbert_order(dim, pts, mn, mx):
+    """fg_hilbert_order: the stable Hilbert order of float points [n][dim]."""
+    pts = np.ascontiguousarray(pts, np.float32)
+    mn = np.ascontiguousarray(mn, np.float32)
+    mx = np.ascontiguousarray(mx, np.float32)
+    perm = np.zeros(len(pts), np.uint32)
+    check(lib().fg_hilbert_order(dim, len(pts), pts.ctypes.data, mn.ctypes.data, mx.ctypes.data, perm.ctypes.data))
+    return perm
+
+
+def hilbert_numbering(dim, bbox, xyz, assemble_type, num_dof):
+    """fg_hilbert_numbering on DOFs in dictionary order; returns the new num_dof."""
+    bbox = np.ascontiguousarray(bbox, np.float64)
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    at = np.ascontiguousarray(assemble_type, np.int32)
+    out = np.ascontiguousarray(num_dof, np.uint64).copy()
+    check(lib().fg_hilbert_numbering(dim, bbox.ctypes.data, len(at), xyz.ctypes.data, at.ctypes.data, out.ctypes.data))
+    return out

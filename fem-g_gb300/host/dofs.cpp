@@ -262,6 +262,12 @@ const HilbertTables &tables(int dim) {
 
 }  // namespace
 
+void hilbertTableData(int dim, uint8_t *code, uint8_t *next) {
+  const HilbertTables &t = tables(dim);
+  std::memcpy(code, t.code, sizeof(t.code));
+  std::memcpy(next, t.nextED, sizeof(t.nextED));
+}
+
 uint64_t hilbertKey(int dim, const uint32_t *u) {
   const HilbertTables &t = tables(dim);
   const int begBit = (64 / dim) - 1;

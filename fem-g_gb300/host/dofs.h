@@ -93,6 +93,8 @@ struct DofDictionary {
 };
 
 // Hilbert key of integer coordinates (dim 2: 32 levels, dim 3: 21 levels)
+// the Hilbert state tables (code[state][corner], nextED[state][corner], 24 x 8)
+void hilbertTableData(int dim, uint8_t *code, uint8_t *next);
 uint64_t hilbertKey(int dim, const uint32_t *u);
 // Hilbert order of float points (stable by key): returns the permutation
 std::vector<uint32_t> hilbertOrder(int dim, const std::vector<float> &pts, const float *mn, const float *mx);

@@ -270,6 +270,18 @@ const char *fg_batch_tuning(const fg_batch *batch);
 int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *elem_dof_type, int64_t n_elements, int32_t n_dofs,
                      uint64_t n_rows, uint64_t *ai, uint64_t **aj);
 
+/* GPU Hilbert order of n points (float [n][dim], dim 2 or 3) in the box
+ * [mn, mx]: the stable order of the keys of src/reorder/Hilbert.cpp:174-288
+ * (perm[k] = index of the k-th point). */
+int fg_hilbert_order(int32_t dim, uint64_t n, const float *pts, const float *mn, const float *mx, uint32_t *perm);
+/* GPU DOF numbering, DofsManager::reorderWithHilbert(true)
+ * (src/dofs/DofsManager.cpp:118-331): the DOFs in dictionary iteration order
+ * (xyz [n_dofs][3] float, FG_AT_* types); Unknown DOFs get 1..nu-nb in
+ * Hilbert order, Unknown bubble DOFs nu-nb+1..nu; the other entries of
+ * num_dof are left as they are. bbox: xmin, ymin, zmin, xmax, ymax, zmax. */
+int fg_hilbert_numbering(int32_t dim, const double *bbox, uint64_t n_dofs, const float *xyz, const int32_t *assemble_type,
+                         uint64_t *num_dof);
+
 /* ----------------------------------------------------------------- misc */
 
 const char *fg_last_error(void);
