@@ -283,8 +283,131 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
   }
 }
 
+// Lowest-order-and-up HCurl field (FG_FORM_1): with the Form1 values
+// P = J^-T v and the Form2 curls C = J c / det (FieldEvaluator<Form1/Form2>,
+// src/term/evaluator/FieldEvaluator.h:59-105),
+//   Ke[i][j] = sum_q w det (c_curl C_j . C_i + c_m P_j . P_i).
+// Warp per element, lanes over the pairs i <= j; the matrix is symmetric.
+struct HcurlWarpSmem {
+  double X[kMaxNodes * 3];
+  double J[9], Jinv[9];
+  double det;
+  double2 a, b;  // w det c_curl, w det c_m
+  double C[3][kMaxDofs], P[3][kMaxDofs];
+};
+
+template <int MAXENT, bool CPLX>
+__global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
+    k_element_hcurl_fp64(const PlanDev p, const DevTerms *__restrict__ terms, double *__restrict__ ke) {
+  __shared__ HcurlWarpSmem smem[kWarpsPerBlockElem];
+  __shared__ uint8_t pairI[kMaxDofs * (kMaxDofs + 1) / 2], pairJ[kMaxDofs * (kMaxDofs + 1) / 2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n = p.nb;
+  const int nEnt = n * (n + 1) / 2;
+  for (int k = threadIdx.x; k < nEnt; k += blockDim.x) {
+    int i = 0, rem = k;
+    while (rem >= n - i) {
+      rem -= n - i;
+      ++i;
+    }
+    pairI[k] = (uint8_t)i;
+    pairJ[k] = (uint8_t)(i + rem);
+  }
+  __syncthreads();
+  HcurlWarpSmem &S = smem[warp];
+  const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlockElem;
+  for (int64_t e = (int64_t)blockIdx.x * kWarpsPerBlockElem + warp; e < p.E; e += stride) {
+    const int o = p.orient ? p.orient[e] : 0;
+    for (int t = lane; t < p.nn * 3; t += 32) S.X[t] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + t / 3] + t % 3];
+    __syncwarp();
+    double accR[MAXENT], accI[MAXENT];
+#pragma unroll
+    for (int m = 0; m < MAXENT; ++m) accR[m] = accI[m] = 0.0;
+    for (int q = 0; q < p.nq; ++q) {
+      if (lane == 0) {
+        if (q == 0 || !p.affine) {
+          S.det = jacobian(p.dim, p.nn, S.X, p.geoGrad + (size_t)q * p.nn * 3, S.J);
+          jacobianInverse(S.J, S.det, S.Jinv);
+        }
+        double xq[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < p.nn; ++k)
+          for (int c = 0; c < 3; ++c) xq[c] += p.geoVal[q * p.nn + k] * S.X[3 * k + c];
+        double2 cc = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0);
+        for (int t = 0; t < terms->n; ++t) {
+          const DevTerm &T = terms->t[t];
+          const double2 v = evalExpr(T.coef, e, xq);
+          if (T.kind == FG_TERM_GRAD_GRAD) cc = cadd(cc, cmul(T.factor, v));
+          else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, v));
+        }
+        const double wd = p.w[q] * S.det;
+        S.a = make_double2(wd * cc.x, wd * cc.y);
+        S.b = make_double2(wd * cm.x, wd * cm.y);
+      }
+      __syncwarp();
+      const size_t base = ((size_t)o * p.nq + q) * p.nb;
+      for (int i = lane; i < n; i += 32) {
+        const double *cr = p.bgrad + 3 * (base + i), *vr = p.bval + 3 * (base + i);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          S.C[r][i] = (S.J[r] * cr[0] + S.J[3 + r] * cr[1] + S.J[6 + r] * cr[2]) / S.det;
+          S.P[r][i] = S.Jinv[r] * vr[0] + S.Jinv[3 + r] * vr[1] + S.Jinv[6 + r] * vr[2];
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int m = 0; m < MAXENT; ++m) {
+        const int k = lane + 32 * m;
+        if (k < nEnt) {
+          const int i = pairI[k], j = pairJ[k];
+          const double cc = S.C[0][i] * S.C[0][j] + S.C[1][i] * S.C[1][j] + S.C[2][i] * S.C[2][j];
+          const double pp = S.P[0][i] * S.P[0][j] + S.P[1][i] * S.P[1][j] + S.P[2][i] * S.P[2][j];
+          accR[m] += S.a.x * cc + S.b.x * pp;
+          if (CPLX) accI[m] += S.a.y * cc + S.b.y * pp;
+        }
+      }
+      __syncwarp();
+    }
+    const int ncomp = CPLX ? 2 : 1;
+    double *K = ke + (size_t)e * ncomp * n * n;
+#pragma unroll
+    for (int m = 0; m < MAXENT; ++m) {
+      const int k = lane + 32 * m;
+      if (k < nEnt) {
+        const int i = pairI[k], j = pairJ[k];
+        K[i * n + j] = K[j * n + i] = accR[m];
+        if (CPLX) K[n * n + i * n + j] = K[n * n + j * n + i] = accI[m];
+      }
+    }
+    __syncwarp();
+  }
+}
+
 int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s) {
   const PlanDev &p = plan->d;
+  if (p.form == FG_FORM_1) {
+    const int nEnt = p.nb * (p.nb + 1) / 2;
+    const int perLane = (nEnt + 31) / 32;
+    int64_t blocks = std::min<int64_t>((p.E + kWarpsPerBlockElem - 1) / kWarpsPerBlockElem, (int64_t)smCount() * 64);
+    if (blocks < 1) blocks = 1;
+    const bool cplx = terms.complexKe != 0;
+    ProfScope prof("k_element_hcurl_fp64", s);
+#define FG_LAUNCH_HC(M)                                                                                              \
+  do {                                                                                                               \
+    if (cplx) k_element_hcurl_fp64<M, true><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, dterms, ke);     \
+    else k_element_hcurl_fp64<M, false><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, dterms, ke);        \
+  } while (0)
+    if (perLane <= 1) FG_LAUNCH_HC(1);
+    else if (perLane <= 8) FG_LAUNCH_HC(8);
+    else {
+      setLastError("FP64 HCurl kernel: more than 22 basis functions per element");
+      return FG_ERR_UNSUPPORTED;
+    }
+#undef FG_LAUNCH_HC
+    (void)be;
+    countLaunch();
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+  }
   if (p.mult != 1 || terms.hasElastic) {
     if (p.mult != 3 || terms.hasSource) {
       setLastError("FP64 element kernel: compound fields take the elastic and mass terms only");

@@ -354,6 +354,60 @@ __global__ void k_factors_elastic(const PlanDev p, const DevTerms *__restrict__ 
   if (e < p.E) factorsElastic(p, terms, rankOf, A, ncomp, rowsPerElem, rowOff, e);
 }
 
+// HCurl field (lowest order and up), affine elements, per-element coefficients:
+//   curl-curl: sum_q w det c (J c_j / det) . (J c_i / det) = (c / det) sum_ab (J^T J)_ab T_ab[i][j]
+//   mass:      sum_q w det c (J^-T v_j) . (J^-T v_i)       = c det sum_ab (J^-1 J^-T)_ab T_6+ab[i][j]
+// 12 factors in 16 columns, rows [hi | lo | hi] as for the scalar field.
+__device__ __forceinline__ void factorsHcurl(const PlanDev &p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
+                                             float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff, int64_t e) {
+  double X[kMaxNodes * 3];
+  const int nx = p.p1geom ? p.dim + 1 : p.nn;
+  for (int k = 0; k < nx; ++k)
+    for (int c = 0; c < 3; ++c) X[3 * k + c] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + k] + c];
+  double J[9], Ji[9];
+  const double det = p.p1geom ? jacobianP1(p.dim, X, J) : jacobian(p.dim, p.nn, X, p.geoGrad, J);
+  jacobianInverse(J, det, Ji);
+  const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  double K[6], M[6];
+  for (int k = 0; k < 6; ++k) {
+    const int a = ab[k][0], b = ab[k][1];
+    K[k] = Ji[3 * a] * Ji[3 * b] + Ji[3 * a + 1] * Ji[3 * b + 1] + Ji[3 * a + 2] * Ji[3 * b + 2];
+    M[k] = J[3 * a] * J[3 * b] + J[3 * a + 1] * J[3 * b + 1] + J[3 * a + 2] * J[3 * b + 2];  // columns of J
+  }
+  double xc[3] = {0.0, 0.0, 0.0};
+  double2 cc = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0);
+  for (int t = 0; t < terms->n; ++t) {
+    const DevTerm &T = terms->t[t];
+    if (T.kind == FG_TERM_GRAD_GRAD) cc = cadd(cc, cmul(T.factor, evalExpr(T.coef, e, xc)));
+    else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xc)));
+  }
+  const int64_t r0 = (int64_t)rankOf[e] * rowsPerElem + rowOff;
+  for (int comp = 0; comp < ncomp; ++comp) {
+    const double gc = (comp == 0 ? cc.x : cc.y) / det, gm = (comp == 0 ? cm.x : cm.y) * det;
+    float hi[kKpE], lo[kKpE];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      splitTf32Dev(gc * M[k], hi[k], lo[k]);
+      splitTf32Dev(gm * K[k], hi[6 + k], lo[6 + k]);
+    }
+#pragma unroll
+    for (int k = 12; k < kKpE; ++k) hi[k] = lo[k] = 0.0f;
+    float4 *row = reinterpret_cast<float4 *>(A + (r0 + comp) * kK3E);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      row[q] = make_float4(hi[4 * q], hi[4 * q + 1], hi[4 * q + 2], hi[4 * q + 3]);
+      row[4 + q] = make_float4(lo[4 * q], lo[4 * q + 1], lo[4 * q + 2], lo[4 * q + 3]);
+      row[8 + q] = row[q];
+    }
+  }
+}
+
+__global__ void k_factors_hcurl(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
+                                float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < p.E) factorsHcurl(p, terms, rankOf, A, ncomp, rowsPerElem, rowOff, e);
+}
+
 // Factor rows of many plans in one launch: thread -> (job, element) through
 // the jobs' element offsets
 __global__ void k_factors_batch(const FactorJob *__restrict__ jobs, int nJobs, int64_t total) {
@@ -367,7 +421,8 @@ __global__ void k_factors_batch(const FactorJob *__restrict__ jobs, int nJobs, i
   }
   const FactorJob &J = jobs[lo];
   const int64_t e = g - J.elemStart;
-  if (J.elastic) factorsElastic(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
+  if (J.kind == 1) factorsElastic(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
+  else if (J.kind == 2) factorsHcurl(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
   else factorsScalar(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
 }
 
@@ -703,6 +758,8 @@ static MixedState *state(fg_plan *plan) {
 //  scalar field (kp = 8):  T[ab] = sum_q w (d_a phi_j d_b phi_i + [a != b] d_b phi_j d_a phi_i)
 //                          for ab = 00,11,22,01,02,12, T[6] = sum_q w phi_i phi_j
 //  compound field (kp = 16): T[3p+p'] = sum_q w d_p phi_j d_p' phi_i, T[9] = sum_q w phi_i phi_j
+//  HCurl field (kp = 16):    T[ab] as the scalar field's with the reference curls c,
+//                            T[6 + ab] the same with the reference vector values v
 static void buildB(const PlanDev &p, const std::vector<double> &w, const std::vector<double> &bval, const std::vector<double> &bgrad,
                    int o, int Npad, int kp, std::vector<float> &img) {
   const int nb = p.nb, nq = p.nq, k3 = 3 * kp;
@@ -715,6 +772,16 @@ static void buildB(const PlanDev &p, const std::vector<double> &w, const std::ve
       for (int q = 0; q < nq; ++q) {
         const double *gi = &bgrad[(((size_t)o * nq + q) * nb + i) * 3];
         const double *gj = &bgrad[(((size_t)o * nq + q) * nb + j) * 3];
+        if (p.form == FG_FORM_1) {
+          const double *vi = &bval[(((size_t)o * nq + q) * nb + i) * 3];
+          const double *vj = &bval[(((size_t)o * nq + q) * nb + j) * 3];
+          for (int k = 0; k < 6; ++k) {
+            const int a = ab[k][0], b = ab[k][1];
+            T[k] += w[q] * (gj[a] * gi[b] + (a != b ? gj[b] * gi[a] : 0.0));
+            T[6 + k] += w[q] * (vj[a] * vi[b] + (a != b ? vj[b] * vi[a] : 0.0));
+          }
+          continue;
+        }
         const double mass = w[q] * bval[((size_t)o * nq + q) * nb + i] * bval[((size_t)o * nq + q) * nb + j];
         if (kp == kKp) {
           for (int k = 0; k < 6; ++k) {
@@ -832,7 +899,7 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
       return FG_ERR_UNSUPPORTED;
     }
     m->blocks = p.mult == 3 ? 9 : 1;
-    m->kp = p.mult == 3 ? kKpE : kKp;
+    m->kp = (p.mult == 3 || p.form == FG_FORM_1) ? kKpE : kKp;
     m->k3 = 3 * m->kp;
     m->n = p.n;
     m->nn2 = p.nb * p.nb;  // one (block of the) element matrix per GEMM row
@@ -843,7 +910,8 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
       return FG_ERR_UNSUPPORTED;
     }
     // tables back to the host
-    std::vector<double> w(p.nq), bval((size_t)p.nOrient * p.nq * p.nb), bgrad(bval.size() * 3);
+    std::vector<double> w(p.nq), bval((size_t)p.nOrient * p.nq * p.nb * (p.form == FG_FORM_1 ? 3 : 1)),
+        bgrad((size_t)p.nOrient * p.nq * p.nb * 3);
     FG_CUDA(cudaMemcpy(w.data(), p.w, w.size() * 8, cudaMemcpyDeviceToHost));
     FG_CUDA(cudaMemcpy(bval.data(), p.bval, bval.size() * 8, cudaMemcpyDeviceToHost));
     FG_CUDA(cudaMemcpy(bgrad.data(), p.bgrad, bgrad.size() * 8, cudaMemcpyDeviceToHost));
@@ -916,7 +984,9 @@ int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups,
   for (int gi = 0; gi < groups; ++gi) {
     ProfScope prof("k_factors", s);
     const int off = gi * ncomp * m->blocks;
-    if (m->blocks == 9)
+    if (p.form == FG_FORM_1)
+      k_factors_hcurl<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms[gi], m->perm + p.E, m->A, ncomp, m->rowsPerElem, off);
+    else if (m->blocks == 9)
       k_factors_elastic<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms[gi], m->perm + p.E, m->A, ncomp, m->rowsPerElem, off);
     else k_factors<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms[gi], m->perm + p.E, m->A, ncomp, m->rowsPerElem, off);
     countLaunch();
@@ -947,7 +1017,7 @@ FactorJob mixedFactorJob(fg_plan *plan, const DevTerms *dterms, int64_t elemStar
   j.ncomp = m->ncomp;
   j.rowsPerElem = m->rowsPerElem;
   j.rowOff = 0;
-  j.elastic = m->blocks == 9;
+  j.kind = plan->d.form == FG_FORM_1 ? 2 : (m->blocks == 9 ? 1 : 0);
   j.elemStart = elemStart;
   return j;
 }

@@ -74,6 +74,7 @@ struct DevTerms {
 struct PlanDev {
   int32_t dim, nn, nq, nb, mult, n, nOrient, affine;
   int32_t p1geom;         // first-order simplex geometry with the standard node order
+  int32_t form;           // FG_FORM_0 (H1) or FG_FORM_1 (HCurl: vector values, curls)
   int64_t E, nNodes;
   uint64_t nRows, nnz, nFixed;
   const double *xyz;      // [nNodes][3]
@@ -81,8 +82,8 @@ struct PlanDev {
   const double *w;        // [nq]
   const double *geoVal;   // [nq][nn]
   const double *geoGrad;  // [nq][nn][3]
-  const double *bval;     // [nOrient][nq][nb]
-  const double *bgrad;    // [nOrient][nq][nb][3]
+  const double *bval;     // [nOrient][nq][nb] (FG_FORM_1: [nOrient][nq][nb][3] vector values)
+  const double *bgrad;    // [nOrient][nq][nb][3] gradients (FG_FORM_1: curls)
   const int32_t *orient;  // [E] or null
   const uint32_t *edof;   // [E][n]: row/column index, or fixed index for fixed DOFs
   const uint8_t *etype;   // [E][n]: FG_AT_*
@@ -194,7 +195,7 @@ struct FactorJob {
   const DevTerms *terms;
   const int32_t *rankOf;
   float *A;
-  int32_t ncomp, rowsPerElem, rowOff, elastic;
+  int32_t ncomp, rowsPerElem, rowOff, kind;  // kind: 0 scalar H1, 1 Tensor4 compound, 2 HCurl
   int64_t elemStart;
 };
 

@@ -155,6 +155,15 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   d.nq = rule->nq;
   d.nb = space->n_basis;
   d.mult = space->multiplicity;
+  d.form = space->form;
+  if (d.form != FG_FORM_0 && d.form != FG_FORM_1) {
+    setLastError("fg_plan_create: unknown space form");
+    return FG_ERR_ARG;
+  }
+  if (d.form == FG_FORM_1 && d.mult != 1) {
+    setLastError("fg_plan_create: HCurl fields have one component");
+    return FG_ERR_UNSUPPORTED;
+  }
   d.n = n;
   d.nOrient = space->n_orientations;
   d.affine = (nn == mesh->dim + 1) ? 1 : 0;
@@ -352,7 +361,9 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   if ((st = upload(plan, rule->weights, (size_t)rule->nq, &d.w))) return st;
   if ((st = upload(plan, rule->geo_val, (size_t)rule->nq * nn, &d.geoVal))) return st;
   if ((st = upload(plan, rule->geo_grad, (size_t)rule->nq * nn * 3, &d.geoGrad))) return st;
-  if ((st = upload(plan, space->basis_val, (size_t)space->n_orientations * rule->nq * space->n_basis, &d.bval))) return st;
+  if ((st = upload(plan, space->basis_val, (size_t)space->n_orientations * rule->nq * space->n_basis * (d.form == FG_FORM_1 ? 3 : 1),
+                    &d.bval)))
+    return st;
   if ((st = upload(plan, space->basis_grad, (size_t)space->n_orientations * rule->nq * space->n_basis * 3, &d.bgrad))) return st;
   d.orient = nullptr;
   if (space->n_orientations > 1)
@@ -514,6 +525,10 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
     }
     if (src.kind == FG_TERM_ELASTIC && plan->d.mult != 3) {
       setLastError("the elastic (Tensor4) term needs a 3-component compound field");
+      return FG_ERR_UNSUPPORTED;
+    }
+    if (plan->d.form == FG_FORM_1 && (src.kind == FG_TERM_ELASTIC || src.kind == FG_TERM_SOURCE)) {
+      setLastError("HCurl fields take the curl-curl and mass terms");
       return FG_ERR_UNSUPPORTED;
     }
     if (src.kind != FG_TERM_ELASTIC && plan->d.mult != 1 && src.kind != FG_TERM_MASS) {

@@ -16,8 +16,9 @@ LIB_PATH = os.path.join(HERE, "_build", "libfemg.so")
 
 FG_OK, FG_ERR_ARG, FG_ERR_OOM, FG_ERR_CUDA, FG_ERR_INDEX, FG_ERR_TIMEOUT, FG_ERR_UNSUPPORTED, FG_ERR_NO_DEVICE = range(8)
 FG_TERM_GRAD_GRAD, FG_TERM_MASS, FG_TERM_ELASTIC, FG_TERM_SOURCE = range(4)
-FG_PROBLEM_HELMHOLTZ, FG_PROBLEM_NAVIER = range(2)
-FG_SPACE_LAGRANGE, FG_SPACE_HIERARCHICAL_H1 = range(2)
+FG_PROBLEM_HELMHOLTZ, FG_PROBLEM_NAVIER, FG_PROBLEM_MAXWELL = range(3)
+FG_SPACE_LAGRANGE, FG_SPACE_HIERARCHICAL_H1, FG_SPACE_HCURL = range(3)
+FG_FORM_0, FG_FORM_1 = range(2)
 FG_EXPR_MAX_CODE = 32
 FG_EXPR_MAX_ARRAYS = 4
 
@@ -41,7 +42,7 @@ class RuleDesc(C.Structure):
 class SpaceDesc(C.Structure):
     _fields_ = [("n_basis", C.c_int32), ("multiplicity", C.c_int32), ("n_orientations", C.c_int32),
                 ("basis_val", C.POINTER(C.c_double)), ("basis_grad", C.POINTER(C.c_double)),
-                ("elem_orientation", C.POINTER(C.c_int32))]
+                ("elem_orientation", C.POINTER(C.c_int32)), ("form", C.c_int32)]
 
 
 class SystemDesc(C.Structure):
@@ -262,7 +263,9 @@ class Problem:
             w=_arr(r.weights, nq, np.float64),
             geo_val=_arr(r.geo_val, nq * nn, np.float64).reshape(nq, nn),
             geo_grad=_arr(r.geo_grad, nq * nn * 3, np.float64).reshape(nq, nn, 3),
-            bval=_arr(s.basis_val, no * nq * nb, np.float64).reshape(no, nq, nb),
+            form=s.form,
+            bval=(_arr(s.basis_val, no * nq * nb * 3, np.float64).reshape(no, nq, nb, 3) if s.form == FG_FORM_1
+                  else _arr(s.basis_val, no * nq * nb, np.float64).reshape(no, nq, nb)),
             bgrad=_arr(s.basis_grad, no * nq * nb * 3, np.float64).reshape(no, nq, nb, 3),
             orient=(_arr(s.elem_orientation, m.n_elements, np.int32) if no > 1 else np.zeros(m.n_elements, np.int32)),
             n_rows=y.n_rows, ai=self.ai, aj=_arr(y.aj, int(self.ai[-1]), np.uint64),

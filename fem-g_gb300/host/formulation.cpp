@@ -31,6 +31,7 @@ bool Domain::have(int dim, int tag) const {
 
 int FunctionSpace::keysPerElement(int elementType) const {
   if (type == SpaceType::Lagrange) return elementNodes(elementType);
+  if (type == SpaceType::HCurl) return whitneyCount(elementDim(elementType));
   const int dim = elementDim(elementType);
   if (dim == 1) return 2 + (order - 1);
   return hierarchicalCount(dim, order);
@@ -63,6 +64,20 @@ void FunctionSpace::getKeys(const Mesh &mesh, const ElementBlock &blk, bool with
         pushCoord(&mesh.xyz[3 * node]);
         if (infoDim) infoDim->push_back(k < nv ? 0 : 1);
       }
+    return;
+  }
+  if (type == SpaceType::HCurl) {  // one key per edge: (1, edge tag) at the edge midpoint
+    for (int64_t e = 0; e < E; ++e) {
+      const int64_t *v = &blk.nodes[(size_t)(e * nn)];
+      for (auto &ed : simplexEdges(dim)) {
+        double mid[3];
+        for (int c = 0; c < 3; ++c) mid[c] = 0.5 * (mesh.xyz[3 * v[ed[0]] + c] + mesh.xyz[3 * v[ed[1]] + c]);
+        typeKeys.push_back(1);
+        entityKeys.push_back((uint64_t)mesh.edgeTagOf(v[ed[0]], v[ed[1]]));
+        pushCoord(mid);
+        if (infoDim) infoDim->push_back(1);
+      }
+    }
     return;
   }
   const int p = order;
@@ -122,7 +137,7 @@ void FunctionSpace::getKeys(const Mesh &mesh, const ElementBlock &blk, bool with
 int FunctionSpace::basisFunctions(bool derivative, const Mesh &mesh, const ElementBlock &blk, const QuadRule &rule,
                                   std::vector<double> &table, std::vector<int32_t> &denseOrient, int &nOrient) const {
   const int64_t E = blk.size();
-  const int ncomp = derivative ? 3 : 1;
+  const int ncomp = (derivative || type == SpaceType::HCurl) ? 3 : 1;
   denseOrient.assign((size_t)E, 0);
   table.clear();
   if (type == SpaceType::Lagrange) {
@@ -137,7 +152,8 @@ int FunctionSpace::basisFunctions(bool derivative, const Mesh &mesh, const Eleme
     return n;
   }
   const int dim = elementDim(blk.type);
-  const int n = hierarchicalCount(dim, order);
+  const bool hcurl = type == SpaceType::HCurl;
+  const int n = hcurl ? whitneyCount(dim) : hierarchicalCount(dim, order);
   const int nn = blk.nodesPerElement;
   const int nv = elementVertices(blk.type);
   // raw orientation per element, then the dense numbering of first
@@ -147,7 +163,7 @@ int FunctionSpace::basisFunctions(bool derivative, const Mesh &mesh, const Eleme
   for (int64_t e = 0; e < E; ++e) {
     int64_t tags[4];
     for (int a = 0; a < nv; ++a) tags[a] = blk.nodes[(size_t)(e * nn + a)] + 1;
-    const int code = orientationFree() ? 0 : hierarchicalOrientation(dim, tags);
+    const int code = orientationFree() ? 0 : (hcurl ? whitneyOrientation(dim, tags) : hierarchicalOrientation(dim, tags));
     auto it = denseOf.find(code);
     if (it == denseOf.end()) {
       it = denseOf.emplace(code, (int)unique.size()).first;
@@ -156,9 +172,15 @@ int FunctionSpace::basisFunctions(bool derivative, const Mesh &mesh, const Eleme
     denseOrient[(size_t)e] = it->second;
   }
   nOrient = (int)unique.size();
-  std::vector<double> val(n), grad(3 * n);
+  std::vector<double> val(3 * n), grad(3 * n);
   for (int o = 0; o < nOrient; ++o)
     for (int q = 0; q < rule.nq; ++q) {
+      if (hcurl) {  // values [n][3], curls [n][3]
+        whitneyBasis(dim, unique[o], &rule.points[3 * q], val.data(), grad.data());
+        for (int i = 0; i < n; ++i)
+          for (int c = 0; c < 3; ++c) table.push_back(derivative ? grad[3 * i + c] : val[3 * i + c]);
+        continue;
+      }
       hierarchicalBasis(dim, order, unique[o], &rule.points[3 * q], val.data(), grad.data());
       for (int i = 0; i < n; ++i)
         for (int c = 0; c < ncomp; ++c) table.push_back(derivative ? grad[3 * i + c] : val[i]);
@@ -310,7 +332,13 @@ Operand dt2_dof(Field &f) {
   return o;
 }
 Operand grad(Operand o) {
+  if (o.field && o.field->fs.type == SpaceType::HCurl) throw std::invalid_argument("grad of an HCurl field: use curl");
   o.grad = true;
+  return o;
+}
+Operand curl(Operand o) {
+  if (!o.field || o.field->fs.type != SpaceType::HCurl) throw std::invalid_argument("curl needs an HCurl field");
+  o.grad = true;  // the derivative term of a Form1 field is its curl (Form2)
   return o;
 }
 Operand operator*(const Function &c, Operand o) {
@@ -521,6 +549,7 @@ void Formulation::descs(fg_mesh_desc *md, fg_rule_desc *rd, fg_space_desc *sd, f
   sd->basis_val = basisVal.data();
   sd->basis_grad = basisGrad.data();
   sd->elem_orientation = nOrient > 1 ? orient.data() : nullptr;
+  sd->form = field->fs.form();
   sys->n_rows = nUnknown;
   sys->ai = ai.data();
   sys->aj = aj.data();

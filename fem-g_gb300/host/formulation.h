@@ -36,7 +36,7 @@ struct Domain {
   bool have(int dim, int tag) const;
 };
 
-enum class SpaceType { Lagrange = 0, HierarchicalH1 = 1 };
+enum class SpaceType { Lagrange = 0, HierarchicalH1 = 1, HCurl = 2 /* lowest-order edge functions */ };
 
 class FunctionSpace {
  public:
@@ -45,7 +45,8 @@ class FunctionSpace {
 
   // "None" for Lagrange and hierarchical order 1, "HierarchicalSolin" otherwise
   // (src/field/FunctionSpaceHierarchicalH1.cpp:44-50)
-  bool orientationFree() const { return type == SpaceType::Lagrange || order == 1; }
+  bool orientationFree() const { return type == SpaceType::Lagrange || (type == SpaceType::HierarchicalH1 && order == 1); }
+  int form() const { return type == SpaceType::HCurl ? 1 : 0; }  // FG_FORM_*
   bool isConstantByElements() const { return type == SpaceType::Lagrange; }
   int keysPerElement(int elementType) const;
   // keys of all elements of a block in element order (gmsh getKeys semantics
@@ -125,6 +126,7 @@ Operand tf(Field &f);
 Operand dt_dof(Field &f);
 Operand dt2_dof(Field &f);
 Operand grad(Operand o);
+Operand curl(Operand o);  // the derivative of an HCurl field
 Operand operator*(const Function &c, Operand o);
 Operand operator*(const Tensor4Isotropic &C, Operand o);
 

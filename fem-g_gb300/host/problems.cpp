@@ -34,11 +34,15 @@ static void buildProblem(fg_problem *p) {
   else
     throw std::invalid_argument("dim must be 2 or 3");
   Domain omega(p->mesh, "omega");
-  const SpaceType st = c.space == FG_SPACE_LAGRANGE ? SpaceType::Lagrange : SpaceType::HierarchicalH1;
+  const SpaceType st = c.space == FG_SPACE_LAGRANGE ? SpaceType::Lagrange
+                       : c.space == FG_SPACE_HCURL  ? SpaceType::HCurl
+                                                    : SpaceType::HierarchicalH1;
+  if ((c.kind == FG_PROBLEM_MAXWELL) != (st == SpaceType::HCurl))
+    throw std::invalid_argument("the Maxwell problem takes the HCurl space, and only it does");
   const int mult = c.kind == FG_PROBLEM_NAVIER ? 3 : 1;
   p->u.reset(new Field("u", omega, st, c.order, mult, 0));
   Field &u = *p->u;
-  p->form.reset(new Formulation(c.kind == FG_PROBLEM_NAVIER ? "navier" : "helmholtz"));
+  p->form.reset(new Formulation(c.kind == FG_PROBLEM_NAVIER ? "navier" : c.kind == FG_PROBLEM_MAXWELL ? "maxwell" : "helmholtz"));
   Formulation &f = *p->form;
   const std::string gauss = "Gauss" + std::to_string(c.gauss);
   const int64_t E = p->mesh.find(c.dim, 1)->blocks[0].size();
@@ -61,6 +65,17 @@ static void buildProblem(fg_problem *p) {
       Function x = Function::x(), y = Function::y();
       Function fsrc = heaviside(Function(0.01) - (x - Function(0.5)) * (x - Function(0.5)) - (y - Function(0.5)) * (y - Function(0.5)));
       f.integral(-fsrc, tf(u), omega, gauss);
+    }
+  } else if (c.kind == FG_PROBLEM_MAXWELL) {
+    // curl curl E - k^2 c E: constant or per-element relative permittivity
+    f.integral(curl(dof(u)), curl(tf(u)), omega, gauss);
+    if (c.coef_mode == FG_COEF_MODE_CONSTANT) {
+      f.integral(Function(-c.k * c.k) * dof(u), tf(u), omega, gauss);
+    } else {
+      Rng rng(c.seed + 1);
+      std::vector<cplx> ce((size_t)E);
+      for (int64_t e = 0; e < E; ++e) ce[(size_t)e] = cplx(-c.k * c.k * (1.0 + 0.3 * rng.normal()), 0.0);
+      f.integral(Function::perElement(ce) * dof(u), tf(u), omega, gauss);
     }
   } else if (c.kind == FG_PROBLEM_NAVIER) {
     Rng rng(c.seed + 2);

@@ -211,6 +211,31 @@ int hierarchicalOrientation(int dim, const int64_t *tags) {
   return code;
 }
 
+int whitneyCount(int dim) { return (int)simplexEdges(dim).size(); }
+
+int whitneyOrientation(int dim, const int64_t *tags) {
+  const auto &edges = simplexEdges(dim);
+  int code = 0;
+  for (size_t e = 0; e < edges.size(); ++e)
+    if (tags[edges[e][0]] > tags[edges[e][1]]) code |= 1 << e;
+  return code;
+}
+
+void whitneyBasis(int dim, int code, const double *uvw, double *val, double *curl) {
+  VG lam[4];
+  barycentric(dim, uvw, lam);
+  const auto &edges = simplexEdges(dim);
+  for (size_t e = 0; e < edges.size(); ++e) {
+    int a = edges[e][0], b = edges[e][1];
+    if ((code >> e) & 1) std::swap(a, b);  // from the lower global tag to the higher
+    const double *ga = lam[a].g, *gb = lam[b].g;
+    for (int c = 0; c < 3; ++c) val[3 * e + c] = lam[a].v * gb[c] - lam[b].v * ga[c];
+    curl[3 * e + 0] = 2.0 * (ga[1] * gb[2] - ga[2] * gb[1]);
+    curl[3 * e + 1] = 2.0 * (ga[2] * gb[0] - ga[0] * gb[2]);
+    curl[3 * e + 2] = 2.0 * (ga[0] * gb[1] - ga[1] * gb[0]);
+  }
+}
+
 void hierarchicalBasis(int dim, int p, int code, const double *uvw, double *val, double *grad) {
   VG lam[4];
   barycentric(dim, uvw, lam);

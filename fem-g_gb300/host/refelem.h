@@ -1,5 +1,5 @@
-// Reference-element data: quadrature rules, geometric (Lagrange) basis and the
-// hierarchical H1 basis with orientations.
+// Reference-element data: quadrature rules, geometric (Lagrange) basis, the
+// hierarchical H1 basis with orientations and the lowest-order HCurl basis.
 //
 // In the reference these come from gmsh:
 //  - quadrature: gmsh::model::mesh::getIntegrationPoints(type, "GaussN") via
@@ -44,6 +44,17 @@ int hierarchicalCount(int dim, int p);
 int hierarchicalOrientation(int dim, const int64_t *vertexTags);
 // Basis values [n] and reference gradients [n][3] for an orientation code.
 void hierarchicalBasis(int dim, int p, int orientationCode, const double *uvw, double *val, double *grad);
+
+// Lowest-order HCurl (Whitney / Nedelec first kind edge functions) on a
+// simplex: one function per edge (a, b) of simplexEdges, directed from the
+// lower global vertex tag to the higher one,
+//   w_ab = lambda_a grad(lambda_b) - lambda_b grad(lambda_a),  curl w_ab = 2 grad(lambda_a) x grad(lambda_b),
+// in reference coordinates (the Form1 / Form2 maps apply J^-T and J / det).
+// The orientation code is the edge reversal bits of hierarchicalOrientation.
+int whitneyCount(int dim);
+int whitneyOrientation(int dim, const int64_t *vertexTags);
+// values [n][3] and curls [n][3] for an orientation code
+void whitneyBasis(int dim, int orientationCode, const double *uvw, double *val, double *curl);
 
 // Legendre polynomial P_k and derivative
 void legendre(int k, double x, double &p, double &dp);

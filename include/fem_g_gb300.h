@@ -86,13 +86,19 @@ typedef struct {
 /* Function space on the bucket: reference basis per orientation, in the
  * reference's layout bf[(o*nq + q)*ncomp*n + dof*ncomp + comp]
  * (src/term/BilinearTerm.cpp:316) */
+enum {
+  FG_FORM_0 = 0, /* H1 (Form0): scalar values, gradients mapped by J^-T (FieldEvaluator<Form0/Form1>) */
+  FG_FORM_1 = 1  /* HCurl (Form1): vector values mapped by J^-T, curls mapped by J / det
+                    (FieldEvaluator<Form1> / <Form2>, src/term/evaluator/FieldEvaluator.h:59-105) */
+};
 typedef struct {
-  int32_t n_basis;      /* scalar basis functions per element */
+  int32_t n_basis;      /* basis functions per element (per component of a compound field) */
   int32_t multiplicity; /* 1 (Field) or 3 (CompoundField, DOF = basis*3 + component) */
   int32_t n_orientations;
-  const double *basis_val;         /* [n_orientations][nq][n_basis] */
-  const double *basis_grad;        /* [n_orientations][nq][n_basis][3] */
+  const double *basis_val;         /* FG_FORM_0: [n_orientations][nq][n_basis]; FG_FORM_1: [...][n_basis][3] */
+  const double *basis_grad;        /* FG_FORM_0: gradients, FG_FORM_1: curls, [n_orientations][nq][n_basis][3] */
   const int32_t *elem_orientation; /* [n_elements] dense orientation, NULL if n_orientations == 1 */
+  int32_t form;                    /* FG_FORM_*; for FG_FORM_1 the derivative terms are curl-curl */
 } fg_space_desc;
 
 /* Pattern and element DOF map produced by the reference's pre():

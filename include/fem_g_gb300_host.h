@@ -21,9 +21,10 @@ extern "C" {
 
 enum {
   FG_PROBLEM_HELMHOLTZ = 0, /* -div grad u - k^2 c u = f, scalar */
-  FG_PROBLEM_NAVIER = 1     /* time-harmonic elastodynamics, 3-component field */
+  FG_PROBLEM_NAVIER = 1,    /* time-harmonic elastodynamics, 3-component field */
+  FG_PROBLEM_MAXWELL = 2    /* curl curl E - k^2 c E, lowest-order HCurl (edge) field */
 };
-enum { FG_SPACE_LAGRANGE = 0, FG_SPACE_HIERARCHICAL_H1 = 1 };
+enum { FG_SPACE_LAGRANGE = 0, FG_SPACE_HIERARCHICAL_H1 = 1, FG_SPACE_HCURL = 2 /* lowest order (edge functions) */ };
 enum {
   FG_COEF_MODE_CONSTANT = 0,   /* mass coefficient -k^2 */
   FG_COEF_MODE_PER_ELEMENT = 1 /* mass coefficient -k^2 (1 + 0.3 xi_e), xi_e ~ N(0,1) per element */

@@ -61,6 +61,7 @@ typedef struct {
   const double *bval;     /* [no][nq][nb] */
   const double *bgrad;    /* [no][nq][nb][3] */
   const int32_t *orient;  /* [E] (NULL: one table, Lagrange's isConstantByElements) */
+  int32_t form;           /* 0: H1 (bval scalar, bgrad gradients); 1: HCurl (bval [..][nb][3] values, bgrad curls) */
 } or_bucket;
 
 /* -------------------------------------------------------- expressions */
@@ -184,7 +185,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
     cplx *target = (frequencyModule && T->dt) ? tmp : Ae;
     if (T->kind != TERM_SOURCE && !bilinear) continue;
     if (T->kind == TERM_SOURCE) {
-      if (!be) continue;
+      if (!be || b->form == 1) continue; /* scalar sources only (H1 test functions) */
       for (int q = 0; q < nq; ++q) {
         double J[9], xq[3];
         double det = or_jacobian(b, e, q, J, xq);
@@ -202,7 +203,28 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
       double det = or_jacobian(b, e, q, J, xq);
       const double wd = b->w[q] * det;
       cplx c = eval_expr(&T->coef, e, xq);
-      if (T->kind == TERM_MASS) {
+      if (T->kind == TERM_MASS && b->form == 1) {
+        /* FieldEvaluator<Form1>: J^-T applied to the vector values */
+        or_form1(J, b->bval + ((size_t)o * nq + q) * nb * 3, nb, G);
+        for (int ii = 0; ii < n; ++ii)
+          for (int jj = 0; jj < n; ++jj) {
+            cplx s = 0.0;
+            for (int r = 0; r < 3; ++r) s += (c * G[r * nb + jj]) * conj(G[r * nb + ii]);
+            target[jj + ii * n] += wd * s;
+          }
+      } else if (T->kind == TERM_GRAD_GRAD && b->form == 1) {
+        /* the curl of a Form1 field is a Form2 field: FieldEvaluator<Form2>,
+         * J / det applied to the reference curls (FieldEvaluator.h:93-96) */
+        const double *cf = b->bgrad + ((size_t)o * nq + q) * nb * 3;
+        for (int i = 0; i < nb; ++i)
+          for (int r = 0; r < 3; ++r) G[r * nb + i] = (J[r] * cf[3 * i] + J[3 + r] * cf[3 * i + 1] + J[6 + r] * cf[3 * i + 2]) / det;
+        for (int ii = 0; ii < n; ++ii)
+          for (int jj = 0; jj < n; ++jj) {
+            cplx s = 0.0;
+            for (int r = 0; r < 3; ++r) s += (c * G[r * nb + jj]) * conj(G[r * nb + ii]);
+            target[jj + ii * n] += wd * s;
+          }
+      } else if (T->kind == TERM_MASS) {
         const double *bf = b->bval + ((size_t)o * nq + q) * nb;
         for (int k = 0; k < nb; ++k) phi[k] = bf[k];
         /* compound Form0: 3 x 3nb field, component c of dof i at row c */

@@ -19,7 +19,8 @@ _ref = None
 class Bucket(C.Structure):
     _fields_ = [("dim", C.c_int), ("nn", C.c_int), ("nq", C.c_int), ("nb", C.c_int), ("mult", C.c_int), ("E", C.c_int64),
                 ("xyz", C.c_void_p), ("enodes", C.c_void_p), ("w", C.c_void_p), ("geo_val", C.c_void_p),
-                ("geo_grad", C.c_void_p), ("bval", C.c_void_p), ("bgrad", C.c_void_p), ("orient", C.c_void_p)]
+                ("geo_grad", C.c_void_p), ("bval", C.c_void_p), ("bgrad", C.c_void_p), ("orient", C.c_void_p),
+                ("form", C.c_int32)]
 
 
 def lib():
@@ -84,7 +85,7 @@ def bucket(a):
     k.orient = np.ascontiguousarray(a["orient"], np.int32)
     b = Bucket(a["dim"], a["nn"], a["nq"], a["nb"], a["mult"], a["E"], k.xyz.ctypes.data, k.enodes.ctypes.data, k.w.ctypes.data,
                k.gv.ctypes.data, k.gg.ctypes.data, k.bv.ctypes.data, k.bg.ctypes.data,
-               k.orient.ctypes.data if a["n_orient"] > 1 else None)
+               k.orient.ctypes.data if a["n_orient"] > 1 else None, int(a.get("form", 0)))
     b._keep = k
     return b
 

@@ -1,0 +1,56 @@
+"""Lowest-order HCurl (Maxwell curl-curl + mass) on the GPU: FP64 and the
+tensor-core path against the oracle, the discrete de Rham identity on the
+GPU's own matrix, and HCurl problems inside a batch with H1 problems."""
+import numpy as np
+import pytest
+
+from test_hcurl import EDGES, csr_apply, edge_values, maxwell, only
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+CASES = {"tri_m8": (2, 8, 0), "tet_m4": (3, 4, 0), "tet_m4_percell": (3, 4, 1), "tet_m12": (3, 12, 0)}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_maxwell_matches_oracle(femg, oracle, cuda, case, precision):
+    dim, m, mode = CASES[case]
+    prob = maxwell(femg, dim, m, coef_mode=mode)
+    a = prob.arrays()
+    t, nt = prob.terms()
+    ref_v, _ = oracle.assemble(a, t, nt)
+    plan = prob.plan()
+    if precision == "mixed":
+        v, _, rep = plan.assemble("mixed", report=True)
+        assert rep["global_"] <= 1e-6
+    else:
+        v, _ = plan.assemble("fp64")
+    assert rel(v, ref_v) <= (1e-12 if precision == "fp64" else 1e-6)
+
+
+def test_gpu_curl_kernel(femg, cuda):
+    prob = maxwell(femg, 3, 6)
+    a = prob.arrays()
+    t, nt = only(femg, prob, femg.FG_TERM_GRAD_GRAD)
+    v, _ = prob.plan().assemble("fp64", terms=(t, nt))
+    u = edge_values(a, np.random.default_rng(9).standard_normal(len(a["xyz"])))
+    Ku = csr_apply(a, v, u)
+    assert np.linalg.norm(Ku) <= 1e-12 * np.abs(v).max() * np.linalg.norm(u) * np.sqrt(len(u))
+
+
+def test_batch_with_hcurl_and_h1(femg, oracle, cuda):
+    probs = [maxwell(femg, 3, 4), femg.Problem(femg.config_c2(m=2, order=2)), maxwell(femg, 2, 6, coef_mode=1)]
+    plans = [p.plan() for p in probs]
+    for mixed, tol in ((False, 1e-12), (True, 1e-6)):
+        batch = femg.Batch(plans, mixed=mixed)
+        vals, _ = batch.run()
+        for p, v in zip(probs, vals):
+            t, nt = p.terms()
+            ref, _ = oracle.assemble(p.arrays(), t, nt)
+            assert rel(v, ref) <= tol
+        batch.close()
