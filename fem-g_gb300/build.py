@@ -16,7 +16,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libfemg.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CUDA_SOURCES = ["csrc/plan.cu", "csrc/assemble_fp64.cu", "csrc/assemble_mixed.cu", "csrc/gather.cu", "csrc/assemble_static.cu", "csrc/multi_freq.cu", "csrc/batch.cu", "csrc/pattern.cu", "csrc/numbering.cu"]
+CUDA_SOURCES = ["csrc/plan.cu", "csrc/assemble_fp64.cu", "csrc/assemble_fp64f.cu", "csrc/assemble_mixed.cu", "csrc/gather.cu", "csrc/assemble_static.cu", "csrc/multi_freq.cu", "csrc/batch.cu", "csrc/pattern.cu", "csrc/numbering.cu"]
 HOST_SOURCES = ["host/mesh.cpp", "host/refelem.cpp", "host/dofs.cpp", "host/formulation.cpp", "host/problems.cpp"]
 HEADERS = ["csrc/common.cuh", "host/mesh.h", "host/refelem.h", "host/dofs.h", "host/formulation.h"]
 

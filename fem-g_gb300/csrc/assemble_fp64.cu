@@ -384,6 +384,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
 
 int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s) {
   const PlanDev &p = plan->d;
+  if (p.E > 0 && factoredFp64Applies(plan, terms)) {
+    int st = launchFactoredFp64(plan, terms, dterms, ke, s);
+    if (st) return st;
+    if (be) {
+      if (p.form == FG_FORM_1) {
+        setLastError("HCurl fields take no source terms");
+        return FG_ERR_UNSUPPORTED;
+      }
+      return launchRhsFp64(plan, dterms, be, s);
+    }
+    return FG_OK;
+  }
   if (p.form == FG_FORM_1) {
     const int nEnt = p.nb * (p.nb + 1) / 2;
     const int perLane = (nEnt + 31) / 32;

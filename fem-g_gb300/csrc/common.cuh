@@ -129,6 +129,9 @@ struct fg_plan {
   void *mixed = nullptr;
   // multi-frequency state (term groups, element matrices), see multi_freq.cu
   void *multi = nullptr;
+  // FP64 factorization state (reference tensors, tiles), see assemble_fp64f.cu
+  void *fp64f = nullptr;
+  int fp64Method = 0;  // FG_FP64_* (FG_FP64_QUADRATURE)
 };
 
 namespace femg {
@@ -198,6 +201,11 @@ struct FactorJob {
   int32_t ncomp, rowsPerElem, rowOff, kind;  // kind: 0 scalar H1, 1 Tensor4 compound, 2 HCurl
   int64_t elemStart;
 };
+
+// FP64 element matrices by factorization (assemble_fp64f.cu): affine elements,
+// element-constant bilinear coefficients, one-component fields
+bool factoredFp64Applies(const fg_plan *plan, const DevTerms &terms);
+int launchFactoredFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, cudaStream_t s);
 
 // mixed path pieces shared with the multi-frequency path (assemble_mixed.cu)
 int prepareMixed(fg_plan *plan, int ncomp, int groups);

@@ -629,6 +629,7 @@ int fg_plan_create(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_
 
 void mixedDestroy(fg_plan *plan);
 void multiDestroy(fg_plan *plan);
+void fp64fDestroy(fg_plan *plan);
 
 void fg_plan_destroy(fg_plan *plan) {
   if (!plan) return;
@@ -644,6 +645,7 @@ void fg_plan_destroy(fg_plan *plan) {
   if (plan->rhs) cudaFree(plan->rhs);
   mixedDestroy(plan);
   multiDestroy(plan);
+  fp64fDestroy(plan);
   delete plan;
 }
 

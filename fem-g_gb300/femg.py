@@ -19,6 +19,9 @@ FG_TERM_GRAD_GRAD, FG_TERM_MASS, FG_TERM_ELASTIC, FG_TERM_SOURCE = range(4)
 FG_PROBLEM_HELMHOLTZ, FG_PROBLEM_NAVIER, FG_PROBLEM_MAXWELL = range(3)
 FG_SPACE_LAGRANGE, FG_SPACE_HIERARCHICAL_H1, FG_SPACE_HCURL = range(3)
 FG_FORM_0, FG_FORM_1 = range(2)
+FG_FP64_QUADRATURE, FG_FP64_FACTORED = range(2)
+(FG_OP_CONST, FG_OP_X, FG_OP_Y, FG_OP_Z, FG_OP_ELEM, FG_OP_ADD, FG_OP_SUB, FG_OP_MUL, FG_OP_DIV, FG_OP_NEG,
+ FG_OP_HEAVISIDE) = range(11)
 FG_EXPR_MAX_CODE = 32
 FG_EXPR_MAX_ARRAYS = 4
 
@@ -102,6 +105,7 @@ def lib():
         "fg_batch_destroy": (None, [P]),
         "fg_batch_tuning": (C.c_char_p, [P]),
         "fg_pattern_build": (C.c_int, [P, P, C.c_int64, C.c_int32, C.c_uint64, P, C.POINTER(P)]),
+        "fg_plan_set_fp64_method": (C.c_int, [P, C.c_int32]),
         "fg_hilbert_order": (C.c_int, [C.c_int32, C.c_uint64, P, P, P, P]),
         "fg_hilbert_numbering": (C.c_int, [C.c_int32, P, C.c_uint64, P, P, P]),
         "fg_profile_enable": (C.c_int, [C.c_int]),
@@ -133,7 +137,7 @@ def lib():
 def exported_symbols():
     """Names bound above (the C ABI of both headers)."""
     return [
-        "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_assemble_fp64", "fg_assemble_mixed",
+        "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_plan_set_fp64_method", "fg_assemble_fp64", "fg_assemble_mixed",
         "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_assemble_separate", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_pattern_build", "fg_hilbert_order", "fg_hilbert_numbering", "fg_profile_enable",
         "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
@@ -349,6 +353,9 @@ class Plan:
         n, nq, no = C.c_int32(), C.c_int32(), C.c_int32()
         check(lib().fg_plan_info(self.ptr, C.byref(nnz), C.byref(E), C.byref(n), C.byref(nq), C.byref(no)))
         return dict(nnz=nnz.value, E=E.value, n=n.value, nq=nq.value, n_orient=no.value)
+
+    def set_fp64_method(self, method):
+        check(lib().fg_plan_set_fp64_method(self.ptr, method))
 
     def bind_terms(self, frequency=0.0):
         t, nt = self.prob.terms()

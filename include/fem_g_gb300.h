@@ -215,6 +215,13 @@ int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, 
  * device: calls in flight at the same time on one device race on it. */
 #define FG_STATIC_SCRATCH_BYTES ((size_t)64 << 20)
 int fg_assemble_fp64_static(fg_plan *plan, const double *dirichlet, double *csr_values, double *rhs, void *stream);
+/* FP64 element-matrix method of a plan. FG_FP64_QUADRATURE (default, the
+ * plain method): the quadrature loop of BilinearTerm::evaluate. FG_FP64_FACTORED:
+ * where it is exact (affine elements, element-constant coefficients,
+ * one-component fields) the factorization Ke = sum_k D_e[k] T_o[k] of the
+ * mixed path, kept in FP64 on the CUDA cores; the quadrature loop elsewhere. */
+enum { FG_FP64_QUADRATURE = 0, FG_FP64_FACTORED = 1 };
+int fg_plan_set_fp64_method(fg_plan *plan, int32_t method);
 /* Mixed precision: FP64 geometry, 3xTF32 tcgen05 contraction with FP32
  * accumulation, FP64 CSR reduction. report may be NULL (no error report). */
 int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency,

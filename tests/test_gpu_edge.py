@@ -91,3 +91,38 @@ def test_long_rows_use_16bit_slots(femg, oracle, cuda):
     for precision, tol in (("fp64", FP64_TOL), ("mixed", MIXED_TOL)):
         v, _ = plan.assemble(precision)
         assert rel(v, ref_v) <= tol
+
+
+def _point_coefficient_terms(femg, prob):
+    """The problem's terms with the mass coefficient multiplied by (1 + x):
+    a coefficient that varies inside the elements."""
+    t, nt = prob.terms()
+    arr = (femg.TermDesc * nt)()
+    for k in range(nt):
+        C.memmove(C.byref(arr[k]), C.byref(t[k]), C.sizeof(femg.TermDesc))
+    mass = [k for k in range(nt) if arr[k].kind == femg.FG_TERM_MASS][0]
+    ex = arr[mass].coef
+    n = ex.n_code
+    extra = [(femg.FG_OP_X, 0, 0.0, 0.0), (femg.FG_OP_CONST, 0, 1.0, 0.0), (femg.FG_OP_ADD, 0, 0.0, 0.0), (femg.FG_OP_MUL, 0, 0.0, 0.0)]
+    for i, (op, arg, re, im) in enumerate(extra):
+        ex.code[n + i].op, ex.code[n + i].arg, ex.code[n + i].re, ex.code[n + i].im = op, arg, re, im
+    ex.n_code = n + len(extra)
+    return arr, nt
+
+
+@pytest.mark.parametrize("cfg", ["tet_p3", "tri_p2_curvedfree"])
+def test_point_dependent_coefficient_uses_quadrature(femg, oracle, cuda, cfg):
+    c = {"tet_p3": femg.config_c2(m=3), "tri_p2_curvedfree": femg.config_c1(m=6)}[cfg]
+    prob = femg.Problem(c)
+    a = prob.arrays()
+    t, nt = _point_coefficient_terms(femg, prob)
+    ref_v, ref_b = oracle.assemble(a, t, nt)
+    plan = prob.plan()
+    plan.set_fp64_method(femg.FG_FP64_FACTORED)  # not exact here: falls back to the quadrature loop
+    v, b = plan.assemble("fp64", terms=(t, nt))
+    assert rel(v, ref_v) <= FP64_TOL
+    if np.linalg.norm(ref_b) > 0:
+        assert rel(b, ref_b) <= FP64_TOL
+    with pytest.raises(femg.FgError) as err:
+        plan.assemble("mixed", terms=(t, nt))
+    assert err.value.status == femg.FG_ERR_UNSUPPORTED

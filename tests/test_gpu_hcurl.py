@@ -17,7 +17,7 @@ CASES = {"tri_m8": (2, 8, 0), "tet_m4": (3, 4, 0), "tet_m4_percell": (3, 4, 1), 
 
 
 @pytest.mark.parametrize("case", list(CASES))
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "fp64_factored", "mixed"])
 def test_maxwell_matches_oracle(femg, oracle, cuda, case, precision):
     dim, m, mode = CASES[case]
     prob = maxwell(femg, dim, m, coef_mode=mode)
@@ -29,8 +29,10 @@ def test_maxwell_matches_oracle(femg, oracle, cuda, case, precision):
         v, _, rep = plan.assemble("mixed", report=True)
         assert rep["global_"] <= 1e-6
     else:
+        if precision == "fp64_factored":
+            plan.set_fp64_method(femg.FG_FP64_FACTORED)
         v, _ = plan.assemble("fp64")
-    assert rel(v, ref_v) <= (1e-12 if precision == "fp64" else 1e-6)
+    assert rel(v, ref_v) <= (1e-6 if precision == "mixed" else 1e-12)
 
 
 def test_gpu_curl_kernel(femg, cuda):

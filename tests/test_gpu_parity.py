@@ -166,3 +166,21 @@ def test_mixed_deterministic_and_complex(femg, cuda):
     assert np.array_equal(v1.view(np.uint64), v2.view(np.uint64))
     v64, _ = plan.assemble("fp64")
     assert rel(v1, v64) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("case", ["c3_m4", "c1_m8", "c2_m2_p4", "tet_lagrange_p2"])
+def test_fp64_methods_agree(femg, oracle, cuda, case):
+    """FG_FP64_QUADRATURE (the plain quadrature loop) and FG_FP64_FACTORED
+    (exact factorization on affine elements, FP64) both give the oracle's
+    CSR; an unknown method is an argument error."""
+    prob = femg.Problem(cases(femg)[case])
+    a = prob.arrays()
+    t, nt = prob.terms()
+    ref_v, _ = oracle.assemble(a, t, nt)
+    plan = prob.plan()
+    v_quad, _ = plan.assemble("fp64")
+    plan.set_fp64_method(femg.FG_FP64_FACTORED)
+    v_auto, _ = plan.assemble("fp64")
+    assert rel(v_auto, ref_v) <= FP64_TOL and rel(v_quad, ref_v) <= FP64_TOL
+    assert rel(v_auto, v_quad) <= FP64_TOL
+    assert femg.lib().fg_plan_set_fp64_method(plan.ptr, 7) == femg.FG_ERR_ARG
