@@ -29,7 +29,6 @@ namespace femg {
 constexpr int kBM = 128;       // rows (element components) per tile = TMEM lanes
 constexpr int kKp = 8;         // factor columns (7 used)
 constexpr int kK3 = 3 * kKp;   // K' of the 3xTF32 chain
-constexpr int kTmemCols = 512;
 constexpr int kThreadsGemm = 256;
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s bound on any device-side wait
 
@@ -51,6 +50,7 @@ struct MixedState {
   int nTiles = 0;
   int32_t *ctaStart = nullptr;  // contiguous tile ranges of the persistent CTAs
   int nCta = 0;
+  int ctasPerSm = 1;            // contraction CTAs per SM (TMEM columns 512 / ctasPerSm each)
   int mmaN = 256;               // N of one MMA instruction
   void *probDev = nullptr;      // this plan's GemmProblem on the device
   float *ke = nullptr;       // [E][groups][ncomp][n][n] fp32
@@ -538,7 +538,7 @@ __device__ inline void drainColumns(const GemmProblem &g, uint32_t tmemRow, floa
 // column chunks of 512. The next tile's A is fetched with cp.async while the
 // current tile computes and drains when both share the B image in shared
 // memory; B is reloaded when the (problem, orientation) changes.
-__global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmSched sc, int maxK3) {
+__global__ void __launch_bounds__(kThreadsGemm, 2) k_contract_tf32x3(const GemmSched sc, int maxK3, int tmemCols) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ GemmProblem gs;
   uint64_t *mbar = reinterpret_cast<uint64_t *>(smem);
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmS
   const int quad = warp & 3, half = warp >> 2;
 
   if (warp == 0) {
-    tmemAlloc(tmemBase, kTmemCols);
+    tmemAlloc(tmemBase, (uint32_t)tmemCols);
     tmemRelinquish();
   }
   if (tid == 0) {
@@ -593,8 +593,8 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmS
     float *out = gs.ke + ((size_t)e * gs.rowsPerElem + (grow % gs.rowsPerElem)) * gs.nn2;
     const uint32_t tmemRow = tmem + ((uint32_t)(quad * 32) << 16);
     float *stage = Stage + warp * (32 * 36);
-    for (int n0 = 0; n0 < gs.Npad && !failed; n0 += kTmemCols) {
-      const int ncols = min(kTmemCols, gs.Npad - n0);
+    for (int n0 = 0; n0 < gs.Npad && !failed; n0 += tmemCols) {
+      const int ncols = min(tmemCols, gs.Npad - n0);
       if (tid == 0) {
         tcFenceAfter();
         for (int c0 = 0; c0 < ncols; c0 += gs.mmaN) {
@@ -642,7 +642,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) k_contract_tf32x3(const GemmS
   }
   __syncthreads();
   tcFenceAfter();
-  if (warp == 0) tmemDealloc(tmem, kTmemCols);
+  if (warp == 0) tmemDealloc(tmem, (uint32_t)tmemCols);
 }
 
 // ---------------------------------------------------- FP64 RHS (mixed)
@@ -810,10 +810,13 @@ static void buildB(const PlanDev &p, const std::vector<double> &w, const std::ve
     }
 }
 
-size_t gemmSmem(int Npad, int k3) {
-  // at least half the SM's shared memory: one CTA per SM, so no CTA ever
-  // waits in tcgen05.alloc for another one's 512 TMEM columns
-  return std::max<size_t>(16 + 8 * 32 * 36 * 4 + 2 * (size_t)kBM * k3 * 4 + (size_t)Npad * k3 * 4, 116 * 1024);
+static size_t gemmSmemNeed(int Npad, int k3) { return 16 + 8 * 32 * 36 * 4 + 2 * (size_t)kBM * k3 * 4 + (size_t)Npad * k3 * 4; }
+int gemmCtasPerSm(int Npad, int k3) { return gemmSmemNeed(Npad, k3) <= 110 * 1024 ? 2 : 1; }
+size_t gemmSmem(int Npad, int k3, int ctasPerSm) {
+  // one CTA per SM takes at least half the SM's shared memory and all 512
+  // TMEM columns; two take at least a third each and 256 columns each. No
+  // CTA ever waits in tcgen05.alloc for another one's columns.
+  return std::max<size_t>(gemmSmemNeed(Npad, k3), ctasPerSm == 2 ? 80 * 1024 : 116 * 1024);
 }
 
 // Contiguous tile ranges for nCta persistent CTAs with about equal summed cost
@@ -834,7 +837,7 @@ std::vector<int32_t> partitionTiles(const std::vector<double> &cost, int nCta) {
 
 // One contraction launch over the tiles of one or many problems
 int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ctaStartDev, int nCta, int *err, int maxK3,
-                   size_t smem, cudaStream_t s) {
+                   size_t smem, cudaStream_t s, int tmemCols) {
   static size_t smemSet = 0;
   if (smem > smemSet) {
     FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -846,7 +849,7 @@ int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ct
   sc.ctaStart = ctaStartDev;
   sc.err = err;
   ProfScope prof("k_contract_tf32x3", s);
-  k_contract_tf32x3<<<std::max(1, nCta), kThreadsGemm, smem, s>>>(sc, maxK3);
+  k_contract_tf32x3<<<std::max(1, nCta), kThreadsGemm, smem, s>>>(sc, maxK3, tmemCols);
   countLaunch();
   FG_CUDA(cudaGetLastError());
   return FG_OK;
@@ -950,7 +953,8 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
   }
   std::vector<int4> tiles = mixedTiles(plan, 0, rowsPerElem);
   m->nTiles = (int)tiles.size();
-  m->nCta = std::max(1, std::min(smCount(), m->nTiles));
+  m->ctasPerSm = gemmCtasPerSm(m->Npad, m->k3);
+  m->nCta = std::max(1, std::min(m->ctasPerSm * smCount(), m->nTiles));
   std::vector<int32_t> start = partitionTiles(std::vector<double>(tiles.size(), 1.0), m->nCta);
   if (m->tiles) cudaFree(m->tiles);
   if (m->ctaStart) cudaFree(m->ctaStart);
@@ -993,7 +997,8 @@ int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups,
     FG_CUDA(cudaGetLastError());
   }
   if (m->nTiles == 0) return FG_OK;
-  return launchContract(m->probDev, m->tiles, m->ctaStart, m->nCta, m->err, m->k3, gemmSmem(m->Npad, m->k3), s);
+  return launchContract(m->probDev, m->tiles, m->ctaStart, m->nCta, m->err, m->k3, gemmSmem(m->Npad, m->k3, m->ctasPerSm), s,
+                        512 / m->ctasPerSm);
 }
 
 int launchFactorsBatch(const FactorJob *jobsDev, int nJobs, int64_t total, cudaStream_t s) {

@@ -218,10 +218,12 @@ int mixedRecordError(fg_plan *plan, cudaStream_t s);
 int launchFactorsBatch(const FactorJob *jobsDev, int nJobs, int64_t total, cudaStream_t s);
 FactorJob mixedFactorJob(fg_plan *plan, const DevTerms *dterms, int64_t elemStart);
 std::vector<int4> mixedTiles(fg_plan *plan, int prob, int rowsPerElem);
-size_t gemmSmem(int Npad, int k3);
+// contraction CTAs per SM (1 or 2) and the dynamic shared memory that pins it
+int gemmCtasPerSm(int Npad, int k3);
+size_t gemmSmem(int Npad, int k3, int ctasPerSm = 1);
 std::vector<int32_t> partitionTiles(const std::vector<double> &cost, int nCta);
 int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ctaStartDev, int nCta, int *err, int maxK3,
-                   size_t smem, cudaStream_t s);
+                   size_t smem, cudaStream_t s, int tmemCols = 512);
 GemmProblem mixedGemmProblem(fg_plan *plan);
 
 // ------------------------------------------------------------- device helpers

@@ -168,6 +168,23 @@ def test_mixed_deterministic_and_complex(femg, cuda):
     assert rel(v1, v64) <= MIXED_TOL
 
 
+@pytest.mark.parametrize("case", ["scalar_m32", "elastic_m16"])
+def test_mixed_chunked_contraction(femg, oracle, cuda, case):
+    """Sizes at which the contraction runs in chunks, with the next chunk's
+    factor rows computed on a second stream; the elastic rows (9 per element)
+    put chunk boundaries inside elements."""
+    c = {"scalar_m32": femg.config_c3(m=32), "elastic_m16": femg.config_c5(m=16)}[case]
+    prob = femg.Problem(c)
+    a = prob.arrays()
+    t, nt = prob.terms()
+    ref_v, _ = oracle.assemble(a, t, nt)
+    plan = prob.plan()
+    v1, _ = plan.assemble("mixed")
+    v2, _ = plan.assemble("mixed")
+    assert np.array_equal(v1.view(np.uint64), v2.view(np.uint64))
+    assert rel(v1, ref_v) <= MIXED_TOL
+
+
 @pytest.mark.parametrize("case", ["c3_m4", "c1_m8", "c2_m2_p4", "tet_lagrange_p2"])
 def test_fp64_methods_agree(femg, oracle, cuda, case):
     """FG_FP64_QUADRATURE (the plain quadrature loop) and FG_FP64_FACTORED
