@@ -169,10 +169,10 @@ def test_mixed_deterministic_and_complex(femg, cuda):
 
 
 @pytest.mark.parametrize("case", ["scalar_m32", "elastic_m16"])
-def test_mixed_chunked_contraction(femg, oracle, cuda, case):
-    """Sizes at which the contraction runs in chunks, with the next chunk's
-    factor rows computed on a second stream; the elastic rows (9 per element)
-    put chunk boundaries inside elements."""
+def test_mixed_many_tiles_per_cta(femg, oracle, cuda, case):
+    """Sizes at which every persistent contraction CTA walks several tiles,
+    across orientation changes; the elastic rows (9 per element) put tile
+    boundaries inside elements. Two runs are bit-identical."""
     c = {"scalar_m32": femg.config_c3(m=32), "elastic_m16": femg.config_c5(m=16)}[case]
     prob = femg.Problem(c)
     a = prob.arrays()
