@@ -22,8 +22,8 @@ constexpr int kWarpsPerBlockElem = 4;
 
 struct ElemWarpSmem {
   double X[kMaxNodes * 3];
-  double J[9], Jinv[9];
-  double det;
+  double J0[9], J[9], Jinv[9];
+  double det0, det;
   double2 a, b, s;  // w det c_gradgrad, w det c_mass, w det f
   double G[3][kMaxDofs];
   double phi[kMaxDofs];
@@ -64,22 +64,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
       accI[m] = 0.0;
     }
     double2 bacc[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
-    for (int q = 0; q < p.nq; ++q) {
+    // one pass over the points per group of terms sharing a Jacobian modificator
+    const int nG = terms->nMod > 1 ? terms->nMod : 1;
+    for (int gq = 0; gq < nG * p.nq; ++gq) {
+      const int g = gq / p.nq, q = gq - g * p.nq;
       if (lane == 0) {
-        if (q == 0 || !p.affine) {
-          S.det = jacobian(p.dim, p.nn, S.X, p.geoGrad + (size_t)q * p.nn * 3, S.J);
-          jacobianInverse(S.J, S.det, S.Jinv);
-        }
-        double xq[3] = {0.0, 0.0, 0.0};
-        for (int k = 0; k < p.nn; ++k) {
-          const double g = p.geoVal[q * p.nn + k];
-          xq[0] += g * S.X[3 * k];
-          xq[1] += g * S.X[3 * k + 1];
-          xq[2] += g * S.X[3 * k + 2];
-        }
+        double xq[3];
+        pointGeometry(p, terms, g, q, S.X, S.J0, S.det0, S.J, S.det, S.Jinv, xq);
         double2 cgg = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0), f = make_double2(0.0, 0.0);
         for (int t = 0; t < terms->n; ++t) {
           const DevTerm &T = terms->t[t];
+          if (T.mod != g) continue;
           const double2 v = evalExpr(T.coef, e, xq);
           if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, v));
           else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, v));
@@ -156,8 +151,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
 // blocks; the element matrix is symmetric.
 struct ElasticWarpSmem {
   double X[kMaxNodes * 3];
-  double J[9], Jinv[9];
-  double det;
+  double J0[9], J[9], Jinv[9];
+  double det0, det;
   double2 lam, mu, cm, s;  // scaled by w det
   double G[3][kMaxDofs / 3 + 1];
   double phi[kMaxDofs / 3 + 1];
@@ -196,22 +191,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         accR[m][b] = 0.0;
         accI[m][b] = 0.0;
       }
-    for (int q = 0; q < p.nq; ++q) {
+    const int nG = terms->nMod > 1 ? terms->nMod : 1;
+    for (int gq = 0; gq < nG * p.nq; ++gq) {
+      const int g = gq / p.nq, q = gq - g * p.nq;
       if (lane == 0) {
-        if (q == 0 || !p.affine) {
-          S.det = jacobian(p.dim, p.nn, S.X, p.geoGrad + (size_t)q * p.nn * 3, S.J);
-          jacobianInverse(S.J, S.det, S.Jinv);
-        }
-        double xq[3] = {0.0, 0.0, 0.0};
-        for (int k = 0; k < p.nn; ++k) {
-          const double g = p.geoVal[q * p.nn + k];
-          xq[0] += g * S.X[3 * k];
-          xq[1] += g * S.X[3 * k + 1];
-          xq[2] += g * S.X[3 * k + 2];
-        }
+        double xq[3];
+        pointGeometry(p, terms, g, q, S.X, S.J0, S.det0, S.J, S.det, S.Jinv, xq);
         double2 lam = make_double2(0.0, 0.0), mu = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0);
         for (int t = 0; t < terms->n; ++t) {
           const DevTerm &T = terms->t[t];
+          if (T.mod != g) continue;
           if (T.kind == FG_TERM_ELASTIC) {
             lam = cadd(lam, cmul(T.factor, evalExpr(T.coef, e, xq)));
             mu = cadd(mu, cmul(T.factor, evalExpr(T.coef2, e, xq)));
@@ -290,8 +279,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
 // Warp per element, lanes over the pairs i <= j; the matrix is symmetric.
 struct HcurlWarpSmem {
   double X[kMaxNodes * 3];
-  double J[9], Jinv[9];
-  double det;
+  double J0[9], J[9], Jinv[9];
+  double det0, det;
   double2 a, b;  // w det c_curl, w det c_m
   double C[3][kMaxDofs], P[3][kMaxDofs];
 };
@@ -323,18 +312,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
     double accR[MAXENT], accI[MAXENT];
 #pragma unroll
     for (int m = 0; m < MAXENT; ++m) accR[m] = accI[m] = 0.0;
-    for (int q = 0; q < p.nq; ++q) {
+    const int nG = terms->nMod > 1 ? terms->nMod : 1;
+    for (int gq = 0; gq < nG * p.nq; ++gq) {
+      const int g = gq / p.nq, q = gq - g * p.nq;
       if (lane == 0) {
-        if (q == 0 || !p.affine) {
-          S.det = jacobian(p.dim, p.nn, S.X, p.geoGrad + (size_t)q * p.nn * 3, S.J);
-          jacobianInverse(S.J, S.det, S.Jinv);
-        }
-        double xq[3] = {0.0, 0.0, 0.0};
-        for (int k = 0; k < p.nn; ++k)
-          for (int c = 0; c < 3; ++c) xq[c] += p.geoVal[q * p.nn + k] * S.X[3 * k + c];
+        double xq[3];
+        pointGeometry(p, terms, g, q, S.X, S.J0, S.det0, S.J, S.det, S.Jinv, xq);
         double2 cc = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0);
         for (int t = 0; t < terms->n; ++t) {
           const DevTerm &T = terms->t[t];
+          if (T.mod != g) continue;
           const double2 v = evalExpr(T.coef, e, xq);
           if (T.kind == FG_TERM_GRAD_GRAD) cc = cadd(cc, cmul(T.factor, v));
           else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, v));
@@ -382,7 +369,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
   }
 }
 
-int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s) {
+static int launchElementKernels(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s) {
   const PlanDev &p = plan->d;
   if (p.E > 0 && factoredFp64Applies(plan, terms)) {
     int st = launchFactoredFp64(plan, terms, dterms, ke, s);
@@ -472,6 +459,29 @@ int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dter
 #undef FG_LAUNCH_ELEM
   countLaunch();
   FG_CUDA(cudaGetLastError());
+  return FG_OK;
+}
+
+// With Jacobian modificators the kernels flag integration points outside a
+// shell; the flag is read back here (the reference throws from apply()).
+int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s) {
+  const PlanDev &p = plan->d;
+  if (!terms.hasJacMod || p.E == 0) return launchElementKernels(plan, terms, dterms, ke, be, s);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  FG_CUDA(cudaStreamIsCapturing(s, &cs));
+  if (cs != cudaStreamCaptureStatusNone) {
+    setLastError("Jacobian modificators: the shell-radius check reads a device word back, which a stream capture cannot");
+    return FG_ERR_UNSUPPORTED;
+  }
+  FG_CUDA(cudaMemsetAsync(p.jmErr, 0, sizeof(int), s));
+  int st = launchElementKernels(plan, terms, dterms, ke, be, s);
+  if (st) return st;
+  FG_CUDA(cudaMemcpyAsync(plan->jmErrHost, p.jmErr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  if (*plan->jmErrHost) {
+    setLastError("Jacobian modificator: an integration point lies outside the shell [r_min, r_max]");
+    return FG_ERR_ARG;
+  }
   return FG_OK;
 }
 

@@ -225,29 +225,48 @@ __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *
   const int nx = p.p1geom ? p.dim + 1 : p.nn;
   for (int k = 0; k < nx; ++k)
     for (int c = 0; c < 3; ++c) X[3 * k + c] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + k] + c];
-  double J[9], Ji[9];
-  const double det = p.p1geom ? jacobianP1(p.dim, X, J) : jacobian(p.dim, p.nn, X, p.geoGrad, J);  // q = 0: affine
-  jacobianInverse(J, det, Ji);
-  double K[6];
+  double J[9];
+  if (p.p1geom) jacobianP1(p.dim, X, J);
+  else jacobian(p.dim, p.nn, X, p.geoGrad, J);  // q = 0: affine
+  // FP64 geometry without the explicit inverse (the FP64 pipe is GB300's
+  // narrowest): with the cofactors C, J^-1 = C^T / det, so
+  // det K = det J^-1 J^-T = (C^T C) / det, and det = J column 0 . C column 0.
+  auto Jm = [&](int r, int c) { return J[3 * c + r]; };
+  double C[9];  // C[3a + r] = (adj J)(a, r)
+  C[0] = Jm(1, 1) * Jm(2, 2) - Jm(1, 2) * Jm(2, 1);
+  C[1] = Jm(0, 2) * Jm(2, 1) - Jm(0, 1) * Jm(2, 2);
+  C[2] = Jm(0, 1) * Jm(1, 2) - Jm(0, 2) * Jm(1, 1);
+  C[3] = Jm(1, 2) * Jm(2, 0) - Jm(1, 0) * Jm(2, 2);
+  C[4] = Jm(0, 0) * Jm(2, 2) - Jm(0, 2) * Jm(2, 0);
+  C[5] = Jm(0, 2) * Jm(1, 0) - Jm(0, 0) * Jm(1, 2);
+  C[6] = Jm(1, 0) * Jm(2, 1) - Jm(1, 1) * Jm(2, 0);
+  C[7] = Jm(0, 1) * Jm(2, 0) - Jm(0, 0) * Jm(2, 1);
+  C[8] = Jm(0, 0) * Jm(1, 1) - Jm(0, 1) * Jm(1, 0);
+  const double det = C[0] * Jm(0, 0) + C[1] * Jm(1, 0) + C[2] * Jm(2, 0);
+  double CC[6];  // (C C^T)(a, b) = det^2 K(a, b)
   const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
   for (int k = 0; k < 6; ++k) {
     const int a = ab[k][0], b = ab[k][1];
-    K[k] = Ji[3 * a] * Ji[3 * b] + Ji[3 * a + 1] * Ji[3 * b + 1] + Ji[3 * a + 2] * Ji[3 * b + 2];
+    CC[k] = C[3 * a] * C[3 * b] + C[3 * a + 1] * C[3 * b + 1] + C[3 * a + 2] * C[3 * b + 2];
   }
   double xc[3] = {0.0, 0.0, 0.0};  // coefficients are per element here: any point of it
   double2 cgg = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0);
   for (int t = 0; t < terms->n; ++t) {
     const DevTerm &T = terms->t[t];
-    if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, evalExpr(T.coef, e, xc)));
-    else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xc)));
+    const double2 v = evalExpr(T.coef, e, xc);
+    // real factor times real coefficient: one multiply instead of a complex product
+    const double2 fv = (T.factor.y == 0.0 && v.y == 0.0) ? make_double2(T.factor.x * v.x, 0.0) : cmul(T.factor, v);
+    if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, fv);
+    else if (T.kind == FG_TERM_MASS) cm = cadd(cm, fv);
   }
+  const double idet = 1.0 / det;
   const int64_t r0 = (int64_t)rankOf[e] * rowsPerElem + rowOff;
   for (int comp = 0; comp < ncomp; ++comp) {
-    const double g = (comp == 0 ? cgg.x : cgg.y) * det;
+    const double g = (comp == 0 ? cgg.x : cgg.y) * idet;
     const double m = (comp == 0 ? cm.x : cm.y) * det;
     float hi[kKp], lo[kKp];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) splitTf32Dev(g * K[k], hi[k], lo[k]);
+    for (int k = 0; k < 6; ++k) splitTf32Dev(g * CC[k], hi[k], lo[k]);
     splitTf32Dev(m, hi[6], lo[6]);
     hi[7] = lo[7] = 0.0f;
     // [hi | lo | hi] as 16-byte stores (rows are 96 bytes)
@@ -1093,6 +1112,10 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
       setLastError("mixed path: bilinear coefficients must be constant per element");
       return FG_ERR_UNSUPPORTED;
     }
+  if (dt.hasJacMod) {
+    setLastError("mixed path: Jacobian modificators make the geometry point-dependent; use the FP64 path");
+    return FG_ERR_UNSUPPORTED;
+  }
   if ((st = prepareMixed(plan, dt.complexKe ? 2 : 1, 1))) return st;
   if ((st = checkTimeout(state(plan), false))) return st;  // a timeout of an earlier call
   const double *uD = nullptr;

@@ -382,8 +382,8 @@ extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const 
       setLastError("fg_batch_create: null plan");
       return fail(FG_ERR_ARG);
     }
-    if (pl->d.nFixed > 0) {
-      setLastError("fg_batch_create: problems with fixed (Dirichlet) DOFs are assembled with fg_assemble_*");
+    if (pl->d.nFixed > 0 || pl->d.lscale) {
+      setLastError("fg_batch_create: problems with fixed (Dirichlet) or linked DOFs are assembled with fg_assemble_*");
       return fail(FG_ERR_UNSUPPORTED);
     }
     if (terms && terms[q]) {
@@ -402,6 +402,10 @@ extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const 
       b->termsDev[q] = pl->boundDev;
     }
     const DevTerms &dt = b->terms[q];
+    if (dt.hasJacMod) {
+      setLastError("fg_batch_create: terms with Jacobian modificators are assembled with fg_assemble_fp64");
+      return fail(FG_ERR_UNSUPPORTED);
+    }
     b->source[q] = dt.hasSource ? 1 : 0;
     if (b->source[q] && (st = ensureDevice((void **)&pl->be, &pl->beBytes, (size_t)pl->d.E * pl->d.n * 16))) return fail(st);
     if (b->mixed) {

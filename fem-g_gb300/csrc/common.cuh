@@ -55,11 +55,18 @@ struct DevExpr {
   const double2 *arr[FG_EXPR_MAX_ARRAYS];
 };
 
+struct DevJacMod {
+  int32_t kind, axis, exponent, pad_;
+  double rmin, rmax, center[3];
+};
+
 struct DevTerm {
   int32_t kind;
   int32_t dt;
   double2 factor;  // module factor: 1, -omega^2 (dt2) or -i omega (dt1)
   DevExpr coef, coef2;
+  int32_t mod;     // index of the term's Jacobian modificator in DevTerms::mods
+  int32_t pad_;
 };
 
 struct DevTerms {
@@ -67,7 +74,10 @@ struct DevTerms {
   int32_t complexKe;   // element matrices need an imaginary part
   int32_t hasSource;
   int32_t hasElastic;
+  int32_t nMod;        // distinct Jacobian modificators of the terms (>= 1; FG_JACMOD_NONE counts)
+  int32_t hasJacMod;   // some term has a modificator other than FG_JACMOD_NONE
   DevTerm t[kMaxTerms];
+  DevJacMod mods[kMaxTerms];
 };
 
 // Device-resident data of one element bucket
@@ -97,6 +107,8 @@ struct PlanDev {
   int32_t slotBytes;
   int32_t slotLd;         // slot row stride (entries)
   int32_t maxRowLen;
+  int *jmErr;             // set by the FP64 element kernels: an integration point outside a shell
+  const double2 *lscale;  // [E][n] linked DOF coefficient (1 for other DOFs), or null without linked DOFs
 };
 
 }  // namespace femg
@@ -132,6 +144,7 @@ struct fg_plan {
   // FP64 factorization state (reference tensors, tiles), see assemble_fp64f.cu
   void *fp64f = nullptr;
   int fp64Method = 0;  // FG_FP64_* (FG_FP64_QUADRATURE)
+  int *jmErrHost = nullptr;  // pinned copy of d.jmErr
 };
 
 namespace femg {
@@ -357,5 +370,93 @@ __device__ inline void jacobianInverse(const double *J, double det, double *Jinv
   Jinv[7] = (Jm(0, 1) * Jm(2, 0) - Jm(0, 0) * Jm(2, 1)) * id;
   Jinv[8] = (Jm(0, 0) * Jm(1, 1) - Jm(0, 1) * Jm(1, 0)) * id;
 }
+
+// Jacobian modificators (src/domain/Axisymmetry.cpp:33-56,
+// AxisymmetryShell.cpp:37-95, PolarShell.cpp:37-93, CylindricalShell.cpp:37-101,
+// SphericalShell.cpp:37-95): at the physical point x the Jacobian
+// (J[3c + r] = dx_r/du_c) becomes J * jac with jac[m][l] = dx'_l/dx_m of the
+// shell map x -> x', and det is multiplied by det(jac). The shells stretch
+// the radius r in [rmin, rmax) with f = (rmin (rmax - rmin) / (r (rmax - r)))^k
+// and theta = k (rmax - 2r) / (rmax - r): jac = f (I - theta dr dr^T) in the
+// stretched directions. Returns false for a radius outside [rmin, rmax] (10
+// machine epsilons of slack); a radius at rmax is pulled inside by 10 epsilons.
+__host__ __device__ inline bool applyJacMod(const DevJacMod &m, const double *x, double *J, double &det) {
+  constexpr double eps = 2.220446049250313e-16;  // double machine epsilon
+  if (m.kind == FG_JACMOD_AXISYMMETRY) {
+    const double r = x[0] == 0.0 ? eps : x[0];
+    J[8] = r;
+    det *= r;
+    return true;
+  }
+  double d[3] = {0.0, 0.0, 0.0};
+  int nd = 3;
+  if (m.kind == FG_JACMOD_AXISYMMETRY_SHELL) {
+    d[0] = x[0];
+    d[1] = x[1] - m.center[1];
+    nd = 2;
+  } else if (m.kind == FG_JACMOD_POLAR_SHELL) {
+    d[0] = x[0] - m.center[0];
+    d[1] = x[1] - m.center[1];
+    nd = 2;
+  } else {
+    for (int j = 0; j < 3; ++j) d[j] = (m.kind == FG_JACMOD_CYLINDRICAL_SHELL && j == m.axis) ? 0.0 : x[j] - m.center[j];
+  }
+  double R = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  if (R < m.rmin - 10.0 * eps || R > m.rmax + 10.0 * eps) return false;
+  if (R >= m.rmax) R = m.rmax - 10.0 * eps;
+  double g[3];
+  for (int j = 0; j < 3; ++j) g[j] = d[j] / R;
+  const double base = (m.rmin * (m.rmax - m.rmin)) / (R * (m.rmax - R));
+  double f = 1.0;
+  for (int k = 0; k < m.exponent; ++k) f *= base;
+  const double theta = m.exponent * (m.rmax - 2.0 * R) / (m.rmax - R);
+  double jac[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) jac[a][b] = f * ((a == b ? 1.0 : 0.0) - theta * g[a] * g[b]);
+  double J2[9];
+  if (nd == 3) {
+    if (m.kind == FG_JACMOD_CYLINDRICAL_SHELL) jac[m.axis][m.axis] = 1.0;
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l) J2[3 * k + l] = J[3 * k] * jac[0][l] + J[3 * k + 1] * jac[1][l] + J[3 * k + 2] * jac[2][l];
+    det *= m.kind == FG_JACMOD_CYLINDRICAL_SHELL ? f * f * (1.0 - theta) : f * f * f * (1.0 - theta);
+  } else {
+    for (int k = 0; k < 2; ++k)
+      for (int l = 0; l < 2; ++l) J2[3 * k + l] = J[3 * k] * jac[0][l] + J[3 * k + 1] * jac[1][l];
+    J2[2] = J2[5] = J2[6] = J2[7] = 0.0;
+    if (m.kind == FG_JACMOD_POLAR_SHELL) {
+      J2[8] = 1.0;
+      det *= f * f * (1.0 - theta);
+    } else {
+      const double S = x[0] == 0.0 ? eps : x[0];
+      J2[8] = S * f;
+      det *= S * (f * f * f * (1.0 - theta));
+    }
+  }
+  for (int k = 0; k < 9; ++k) J[k] = J2[k];
+  return true;
+}
+
+// Lane-0 geometry of integration point q for the terms of modificator group
+// g: J0/det0 hold the unmodified Jacobian (formed once for affine elements),
+// J/det/Jinv the one the group's terms use, xq the physical point.
+__device__ inline void pointGeometry(const PlanDev &p, const DevTerms *terms, int g, int q, const double *X, double *J0, double &det0,
+                                     double *J, double &det, double *Jinv, double *xq) {
+  if (q == 0 || !p.affine) det0 = jacobian(p.dim, p.nn, X, p.geoGrad + (size_t)q * p.nn * 3, J0);
+  xq[0] = xq[1] = xq[2] = 0.0;
+  for (int k = 0; k < p.nn; ++k) {
+    const double v = p.geoVal[q * p.nn + k];
+    xq[0] += v * X[3 * k];
+    xq[1] += v * X[3 * k + 1];
+    xq[2] += v * X[3 * k + 2];
+  }
+  const DevJacMod &m = terms->mods[g];
+  if (m.kind != FG_JACMOD_NONE || q == 0 || !p.affine || terms->nMod > 1) {
+    for (int k = 0; k < 9; ++k) J[k] = J0[k];
+    det = det0;
+    if (m.kind != FG_JACMOD_NONE && !applyJacMod(m, xq, J, det)) atomicOr(p.jmErr, 1);
+    jacobianInverse(J, det, Jinv);
+  }
+}
+
 
 }  // namespace femg

@@ -98,21 +98,37 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
       const bool act = k < cnt;
       const int64_t e = packedK >> 6;
       const int i = packedK & 63;
-      if (be && act && lt == 0) bsum = cadd(bsum, be[flat]);
+      // linked DOFs (complex element matrices only): the row scales by the
+      // conjugate of its coefficient, each column by its own
+      const bool linked = KCPLX && p.lscale != nullptr;
+      double2 cI = make_double2(1.0, 0.0);
+      if (linked && act) {
+        cI = p.lscale[e * n + i];
+        cI.y = -cI.y;
+      }
+      if (be && act && lt == 0) bsum = cadd(bsum, linked ? cmul(cI, be[flat]) : be[flat]);
 #pragma unroll
       for (int jj = 0; jj < J; ++jj) {
         const SlotT s = sv[jj];
         if (s == kIgnore) continue;
         if (s != kFixed) {
+          AT ar = (AT)vr[jj], ai = KCPLX ? (AT)vi[jj] : (AT)0;
+          if (linked) {
+            const double2 c = cmul(cI, p.lscale[e * n + lt + L * jj]);
+            const AT tr = ar * (AT)c.x - ai * (AT)c.y;
+            ai = ar * (AT)c.y + ai * (AT)c.x;
+            ar = tr;
+          }
           // the lanes of one element row hit distinct slots; entries are
           // ordered by the __syncwarp below, so these adds are ordered too
-          atomicAdd(&A[(int)s * SS], (AT)vr[jj]);
-          if (KCPLX) atomicAdd(&A[(int)s * SS + 1], (AT)vi[jj]);
+          atomicAdd(&A[(int)s * SS], ar);
+          if (KCPLX) atomicAdd(&A[(int)s * SS + 1], ai);
         } else {
           const KT *Kt = ke + (size_t)e * SS * nn2;
           const int j = lt + L * jj;
           const int o = keOff(j, i);
-          const double2 v = make_double2((double)Kt[o], KCPLX ? (double)Kt[nn2 + o] : 0.0);
+          double2 v = make_double2((double)Kt[o], KCPLX ? (double)Kt[nn2 + o] : 0.0);
+          if (linked) v = cmul(cI, v);
           dc = cadd(dc, cmul(v, uD[p.edof[e * n + j]]));
         }
       }
@@ -215,6 +231,10 @@ int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, 
   const int blk3 = keBlocks == 9 ? 1 : 0;
   const PlanDev &p = plan->d;
   if (p.nRows == 0) return FG_OK;
+  if (p.lscale && !keComplex) {
+    setLastError("gather: linked DOFs need complex element matrices");
+    return FG_ERR_UNSUPPORTED;
+  }
   const double2 *be2 = (const double2 *)be;
   const double2 *uD = (const double2 *)dirichletDev;
   double2 *v2 = (double2 *)values;

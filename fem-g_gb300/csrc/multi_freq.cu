@@ -285,6 +285,10 @@ int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t
               const std::function<int(const int *, int, double2 *, double2 *)> &coefOf) {
   MultiState *m = multiState(plan);
   const PlanDev &p = plan->d;
+  if (p.lscale) {
+    setLastError("several frequencies / separate matrices: plans with linked DOFs are assembled one frequency at a time");
+    return FG_ERR_UNSUPPORTED;
+  }
   // groups by time derivative; the factors are applied in the reduction
   int dts[kMaxGroups], G = 0;
   fg_term_desc grp[kMaxTerms];
@@ -386,8 +390,8 @@ int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t
     for (int g = 0; g < G; ++g) {
       if (m->terms[g].complexKe) ncomp = 2;
       for (int t = 0; t < m->terms[g].n; ++t)
-        if (m->terms[g].t[t].kind != FG_TERM_SOURCE && m->terms[g].t[t].coef.cls == kExprPoint) {
-          setLastError("mixed path: bilinear coefficients must be constant per element");
+        if ((m->terms[g].t[t].kind != FG_TERM_SOURCE && m->terms[g].t[t].coef.cls == kExprPoint) || m->terms[g].hasJacMod) {
+          setLastError("mixed path: bilinear coefficients must be constant per element, without Jacobian modificators");
           return FG_ERR_UNSUPPORTED;
         }
     }

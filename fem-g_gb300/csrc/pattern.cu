@@ -69,7 +69,7 @@ __global__ void k_pat_fill(const uint32_t *__restrict__ edof, const uint8_t *__r
 template <bool WRITE>
 __global__ void k_pat_rows(const uint32_t *__restrict__ edof, const uint8_t *__restrict__ etype, int n,
                            const uint64_t *__restrict__ rowStart, const uint32_t *__restrict__ rowElem,
-                           const uint32_t *__restrict__ alias, uint64_t nRows, int cap, uint32_t *__restrict__ rowLen,
+                           const uint32_t *__restrict__ alias, uint64_t nRows, int cap, int upper, uint32_t *__restrict__ rowLen,
                            const uint64_t *__restrict__ ai, uint64_t *__restrict__ aj) {
   extern __shared__ uint32_t patBuf[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -88,7 +88,8 @@ __global__ void k_pat_rows(const uint32_t *__restrict__ edof, const uint8_t *__r
         const uint32_t pk = rowElem[s0 + k / n];
         const int64_t e = pk >> 6;
         const int j = k % n;
-        if (patRow(etype[e * n + j])) v = edof[e * n + j];
+        // upper storage keeps the columns at or right of the (first bubble's) row
+        if (patRow(etype[e * n + j]) && (!upper || edof[e * n + j] >= row)) v = edof[e * n + j];
       }
       buf[k] = v;
     }
@@ -160,7 +161,8 @@ int devAlloc(DevBuf &b, size_t bytes) {
 }  // namespace
 
 extern "C" int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *elem_dof_type, int64_t n_elements, int32_t n_dofs,
-                                uint64_t n_rows, uint64_t *ai, uint64_t **aj) {
+                                uint64_t n_rows, uint64_t *ai, uint64_t **aj, int32_t upper, const uint64_t *linked_row,
+                                uint64_t n_linked) {
   if (!ai || !aj || n_elements < 0 || n_dofs <= 0 || n_dofs > 64 || (n_elements > 0 && (!elem_dof_idx || !elem_dof_type))) {
     setLastError("fg_pattern_build: invalid arguments");
     return FG_ERR_ARG;
@@ -183,18 +185,28 @@ extern "C" int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *ele
   std::vector<uint8_t> et(en);
   int bad = 0;
   for (size_t k = 0; k < en; ++k) {
-    const int t = elem_dof_type[k];
-    if (t == FG_AT_LINKED || t == FG_AT_LINKED_BUBBLE) {
-      setLastError("fg_pattern_build: linked DOFs are not supported");
+    int t = elem_dof_type[k];
+    uint64_t v = elem_dof_idx[k];
+    if (t == FG_AT_LINKED_BUBBLE) {
+      setLastError("fg_pattern_build: linked bubble DOFs are not supported");
       return FG_ERR_UNSUPPORTED;
+    }
+    if (t == FG_AT_LINKED) {
+      // a linked DOF is a row and a column of its master (MatrixFactory.cpp:468-470, :481-483)
+      if (!linked_row || v >= n_linked) {
+        ++bad;
+        continue;
+      }
+      v = linked_row[v];
+      t = FG_AT_UNKNOWN;
     }
     et[k] = (uint8_t)t;
     const bool row = t == FG_AT_UNKNOWN || t == FG_AT_UNKNOWN_BUBBLE || t == FG_AT_UNKNOWN_GLOBAL;
-    if (row && elem_dof_idx[k] >= n_rows) ++bad;
-    ed[k] = row ? (uint32_t)elem_dof_idx[k] : 0u;
+    if (row && v >= n_rows) ++bad;
+    ed[k] = row ? (uint32_t)v : 0u;
   }
   if (bad) {
-    setLastError("fg_pattern_build: a DOF index is not below n_rows");
+    setLastError("fg_pattern_build: a DOF index is not below n_rows (or a linked index not below n_linked)");
     return FG_ERR_INDEX;
   }
   DevBuf dEd, dEt, dCnt, dAlias, dStart, dFill, dElem, dLen, dAi, dAj;
@@ -245,7 +257,7 @@ extern "C" int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *ele
   const unsigned rb = (unsigned)std::min<uint64_t>(std::max<uint64_t>(1, (n_rows + wpb - 1) / wpb), (uint64_t)smCount() * 64);
   if (n_rows > 0) {
     k_pat_rows<false><<<rb, 32 * wpb, smem>>>((const uint32_t *)dEd.p, (const uint8_t *)dEt.p, n, rowStart,
-                                               (const uint32_t *)dElem.p, alias, n_rows, cap, len, nullptr, nullptr);
+                                               (const uint32_t *)dElem.p, alias, n_rows, cap, upper ? 1 : 0, len, nullptr, nullptr);
     k_pat_alias_len<<<(unsigned)((n_rows + 255) / 256), 256>>>(alias, n_rows, len);
     countLaunch(2);
     FG_CUDA(cudaGetLastError());
@@ -258,7 +270,7 @@ extern "C" int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *ele
   if ((st = devAlloc(dAj, nnz * 8))) return st;
   if (n_rows > 0) {
     k_pat_rows<true><<<rb, 32 * wpb, smem>>>((const uint32_t *)dEd.p, (const uint8_t *)dEt.p, n, rowStart,
-                                              (const uint32_t *)dElem.p, alias, n_rows, cap, len, dai, (uint64_t *)dAj.p);
+                                              (const uint32_t *)dElem.p, alias, n_rows, cap, upper ? 1 : 0, len, dai, (uint64_t *)dAj.p);
     k_pat_alias_copy<<<(unsigned)((n_rows + 7) / 8), 256>>>(alias, n_rows, dai, (uint64_t *)dAj.p);
     countLaunch(2);
     FG_CUDA(cudaGetLastError());

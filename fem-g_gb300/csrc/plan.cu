@@ -127,6 +127,7 @@ static bool isRow(int t) { return t == FG_AT_UNKNOWN || t == FG_AT_UNKNOWN_BUBBL
 static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_space_desc *space, const fg_system_desc *sys,
                       fg_plan *plan) {
   PlanDev &d = plan->d;
+  std::memset(&d, 0, sizeof(d));  // every table absent until uploaded
   if (mesh->dim != 2 && mesh->dim != 3) {
     setLastError("fg_plan_create: element dimension must be 2 or 3");
     return FG_ERR_ARG;
@@ -236,21 +237,38 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
       }
   }
 
-  // element DOF map: row/column index (or fixed index) and type
+  // element DOF map: row/column index (or fixed index) and type. A linked
+  // DOF takes its master's row and column (MatrixFactory.cpp:241-246,
+  // :254-259), so it is stored as an Unknown DOF of that row; its coefficient
+  // goes to the scale table the reduction applies.
   std::vector<uint32_t> edof((size_t)E * n);
   std::vector<uint8_t> etype((size_t)E * n);
-#pragma omp parallel for reduction(+ : bad)
+  int linkedBubble = 0, linked = 0;
+#pragma omp parallel for reduction(+ : bad, linkedBubble, linked)
   for (int64_t i = 0; i < E * n; ++i) {
     const int t = sys->elem_dof_type[i];
-    const uint64_t v = sys->elem_dof_idx[i];
+    uint64_t v = sys->elem_dof_idx[i];
     etype[(size_t)i] = (uint8_t)t;
-    edof[(size_t)i] = (uint32_t)v;
-    if (t == FG_AT_LINKED || t == FG_AT_LINKED_BUBBLE || t < 0 || t > FG_AT_LINKED_BUBBLE) ++bad;
-    else if (isRow(t) && v >= sys->n_rows) ++bad;
+    if (t == FG_AT_LINKED_BUBBLE) ++linkedBubble;
+    else if (t < 0 || t > FG_AT_LINKED_BUBBLE) ++bad;
+    else if (t == FG_AT_LINKED) {
+      if (!sys->linked_row || !sys->linked_value || v >= sys->n_linked || sys->linked_row[v] >= sys->n_rows) {
+        ++bad;
+      } else {
+        v = sys->linked_row[v];
+        etype[(size_t)i] = FG_AT_UNKNOWN;
+        ++linked;
+      }
+    } else if (isRow(t) && v >= sys->n_rows) ++bad;
     else if (t == FG_AT_FIXED && v >= sys->n_fixed) ++bad;
+    edof[(size_t)i] = (uint32_t)v;
+  }
+  if (linkedBubble) {
+    setLastError("fg_plan_create: linked bubble DOFs are not supported");
+    return FG_ERR_UNSUPPORTED;
   }
   if (bad) {
-    setLastError("fg_plan_create: element DOF index/type out of range (linked DOFs are not supported)");
+    setLastError("fg_plan_create: element DOF index/type out of range");
     return FG_ERR_INDEX;
   }
 
@@ -334,14 +352,19 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
         uint16_t s;
         if (t == FG_AT_FIXED) s = kSlotFixed;
         else if (!isRow(t)) s = kSlotIgnore;
+        else if (sys->upper && edof[kj] < I) s = kSlotIgnore;  // below the diagonal: not stored
         else {
           const uint64_t J = edof[kj];
           const uint64_t *p = std::lower_bound(b, en2, J);
-          if (p == en2 || *p != J) {
+          if (p != en2 && (*p == J || sys->upper)) {
+            // Upper storage: an aliased bubble row whose first bubble has a
+            // larger index lacks the columns between the two; the reference
+            // adds those entries at the lower_bound position without checking
+            // it (MatrixFactory.cpp:267-268), and so does this map.
+            s = (uint16_t)(p - b);
+          } else {
             ++bad;
             s = kSlotIgnore;
-          } else {
-            s = (uint16_t)(p - b);
           }
         }
         const size_t ks = ki * nS + j;
@@ -385,6 +408,21 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
     if ((st = upload(plan, slot16.data(), slot16.size(), &p))) return st;
     d.slot = p;
   }
+  if (linked) {
+    std::vector<double2> ls((size_t)E * n, make_double2(1.0, 0.0));
+    for (int64_t i = 0; i < E * n; ++i)
+      if (sys->elem_dof_type[i] == FG_AT_LINKED) {
+        const uint64_t v = sys->elem_dof_idx[i];
+        ls[(size_t)i] = make_double2(sys->linked_value[2 * v], sys->linked_value[2 * v + 1]);
+      }
+    if ((st = upload(plan, ls.data(), ls.size(), &d.lscale))) return st;
+  }
+  // error word of the Jacobian modificators, and its pinned host copy
+  const int zero = 0;
+  const int *err = nullptr;
+  if ((st = upload(plan, &zero, 1, &err))) return st;
+  d.jmErr = const_cast<int *>(err);
+  FG_CUDA(cudaMallocHost(&plan->jmErrHost, sizeof(int)));
   return FG_OK;
 }
 
@@ -514,6 +552,7 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
   for (int t = 0; t < nTerms; ++t) anyDt = anyDt || terms[t].dt != FG_DT_NONE;
   bool cplx = false;
   out->n = nTerms;
+  out->nMod = 0;
   for (int t = 0; t < nTerms; ++t) {
     const fg_term_desc &src = terms[t];
     DevTerm &dt = out->t[t];
@@ -554,8 +593,37 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
       out->hasElastic = 1;
     }
     if (src.kind == FG_TERM_SOURCE) out->hasSource = 1;
+    // the term's Jacobian modificator: terms with equal ones share a group
+    const fg_jacmod &jm = src.jacmod;
+    if (jm.kind < FG_JACMOD_NONE || jm.kind > FG_JACMOD_SPHERICAL_SHELL) {
+      setLastError("unknown Jacobian modificator");
+      return FG_ERR_ARG;
+    }
+    DevJacMod m;
+    std::memset(&m, 0, sizeof(m));
+    m.kind = jm.kind;
+    if (jm.kind >= FG_JACMOD_AXISYMMETRY_SHELL) {
+      if (!(jm.r_min > 0.0) || !(jm.r_max > jm.r_min) || jm.exponent < 0 ||
+          (jm.kind == FG_JACMOD_CYLINDRICAL_SHELL && (jm.axis < 0 || jm.axis > 2))) {
+        setLastError("Jacobian modificator: needs 0 < r_min < r_max, exponent >= 0 and a cylinder axis in 0..2");
+        return FG_ERR_ARG;
+      }
+      m.axis = jm.kind == FG_JACMOD_CYLINDRICAL_SHELL ? jm.axis : 0;
+      m.exponent = jm.exponent;
+      m.rmin = jm.r_min;
+      m.rmax = jm.r_max;
+      for (int c = 0; c < 3; ++c) m.center[c] = jm.center[c];
+    }
+    int g = 0;
+    while (g < out->nMod && std::memcmp(&out->mods[g], &m, sizeof(m)) != 0) ++g;
+    if (g == out->nMod) out->mods[out->nMod++] = m;
+    dt.mod = g;
+    if (m.kind != FG_JACMOD_NONE) out->hasJacMod = 1;
   }
   (void)anyDt;
+  // linked DOFs scale element entries by complex coefficients: the reduction
+  // then runs on complex element matrices
+  if (plan->d.lscale) cplx = true;
   out->complexKe = cplx ? 1 : 0;
   return FG_OK;
 }
@@ -646,6 +714,7 @@ void fg_plan_destroy(fg_plan *plan) {
   mixedDestroy(plan);
   multiDestroy(plan);
   fp64fDestroy(plan);
+  if (plan->jmErrHost) cudaFreeHost(plan->jmErrHost);
   delete plan;
 }
 

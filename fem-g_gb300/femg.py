@@ -19,6 +19,8 @@ FG_TERM_GRAD_GRAD, FG_TERM_MASS, FG_TERM_ELASTIC, FG_TERM_SOURCE = range(4)
 FG_PROBLEM_HELMHOLTZ, FG_PROBLEM_NAVIER, FG_PROBLEM_MAXWELL = range(3)
 FG_SPACE_LAGRANGE, FG_SPACE_HIERARCHICAL_H1, FG_SPACE_HCURL = range(3)
 FG_FORM_0, FG_FORM_1 = range(2)
+FG_JACMOD_NONE, FG_JACMOD_AXISYMMETRY, FG_JACMOD_AXISYMMETRY_SHELL, FG_JACMOD_POLAR_SHELL, FG_JACMOD_CYLINDRICAL_SHELL, \
+    FG_JACMOD_SPHERICAL_SHELL = range(6)
 FG_FP64_QUADRATURE, FG_FP64_FACTORED = range(2)
 (FG_OP_CONST, FG_OP_X, FG_OP_Y, FG_OP_Z, FG_OP_ELEM, FG_OP_ADD, FG_OP_SUB, FG_OP_MUL, FG_OP_DIV, FG_OP_NEG,
  FG_OP_HEAVISIDE) = range(11)
@@ -50,7 +52,9 @@ class SpaceDesc(C.Structure):
 
 class SystemDesc(C.Structure):
     _fields_ = [("n_rows", C.c_uint64), ("ai", C.POINTER(C.c_uint64)), ("aj", C.POINTER(C.c_uint64)),
-                ("elem_dof_idx", C.POINTER(C.c_uint64)), ("elem_dof_type", C.POINTER(C.c_int32)), ("n_fixed", C.c_uint64)]
+                ("elem_dof_idx", C.POINTER(C.c_uint64)), ("elem_dof_type", C.POINTER(C.c_int32)), ("n_fixed", C.c_uint64),
+                ("upper", C.c_int32), ("n_linked", C.c_uint64), ("linked_row", C.POINTER(C.c_uint64)),
+                ("linked_value", C.POINTER(C.c_double))]
 
 
 class Instr(C.Structure):
@@ -62,8 +66,13 @@ class Expr(C.Structure):
                 ("elem_values", C.POINTER(C.c_double) * FG_EXPR_MAX_ARRAYS)]
 
 
+class JacMod(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("axis", C.c_int32), ("exponent", C.c_int32), ("pad_", C.c_int32),
+                ("r_min", C.c_double), ("r_max", C.c_double), ("center", C.c_double * 3)]
+
+
 class TermDesc(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("dt", C.c_int32), ("coef", Expr), ("coef2", Expr)]
+    _fields_ = [("kind", C.c_int32), ("dt", C.c_int32), ("coef", Expr), ("coef2", Expr), ("jacmod", JacMod)]
 
 
 class ErrReport(C.Structure):
@@ -75,7 +84,7 @@ class ProblemConfig(C.Structure):
                 ("space", C.c_int32), ("order", C.c_int32), ("gauss", C.c_int32), ("jitter", C.c_double),
                 ("seed", C.c_uint64), ("k", C.c_double), ("coef_mode", C.c_int32), ("dirichlet", C.c_int32),
                 ("dirichlet_value", C.c_double), ("source", C.c_int32), ("omega", C.c_double),
-                ("lame_sigma", C.c_double)]
+                ("lame_sigma", C.c_double), ("upper", C.c_int32)]
 
 
 _lib = None
@@ -104,7 +113,7 @@ def lib():
         "fg_batch_run": (C.c_int, [P, P, P, P]),
         "fg_batch_destroy": (None, [P]),
         "fg_batch_tuning": (C.c_char_p, [P]),
-        "fg_pattern_build": (C.c_int, [P, P, C.c_int64, C.c_int32, C.c_uint64, P, C.POINTER(P)]),
+        "fg_pattern_build": (C.c_int, [P, P, C.c_int64, C.c_int32, C.c_uint64, P, C.POINTER(P), C.c_int32, P, C.c_uint64]),
         "fg_plan_set_fp64_method": (C.c_int, [P, C.c_int32]),
         "fg_hilbert_order": (C.c_int, [C.c_int32, C.c_uint64, P, P, P, P]),
         "fg_hilbert_numbering": (C.c_int, [C.c_int32, P, C.c_uint64, P, P, P]),
@@ -171,9 +180,9 @@ def _arr(ptr, count, dtype):
 
 
 def config(kind=FG_PROBLEM_HELMHOLTZ, dim=2, m=4, mesh_order=2, space=FG_SPACE_LAGRANGE, order=1, gauss=4, jitter=0.2,
-           seed=1, k=10.0, coef_mode=0, dirichlet=0, dirichlet_value=0.0, source=0, omega=1.0, lame_sigma=0.5):
+           seed=1, k=10.0, coef_mode=0, dirichlet=0, dirichlet_value=0.0, source=0, omega=1.0, lame_sigma=0.5, upper=0):
     return ProblemConfig(kind, dim, m, mesh_order, space, order, gauss, jitter, seed, k, coef_mode, dirichlet,
-                         dirichlet_value, source, omega, lame_sigma)
+                         dirichlet_value, source, omega, lame_sigma, upper)
 
 
 # The benchmark workloads (seeded synthetic inputs with the shapes of the
@@ -268,6 +277,7 @@ class Problem:
             geo_val=_arr(r.geo_val, nq * nn, np.float64).reshape(nq, nn),
             geo_grad=_arr(r.geo_grad, nq * nn * 3, np.float64).reshape(nq, nn, 3),
             form=s.form,
+            upper=y.upper,
             bval=(_arr(s.basis_val, no * nq * nb * 3, np.float64).reshape(no, nq, nb, 3) if s.form == FG_FORM_1
                   else _arr(s.basis_val, no * nq * nb, np.float64).reshape(no, nq, nb)),
             bgrad=_arr(s.basis_grad, no * nq * nb * 3, np.float64).reshape(no, nq, nb, 3),
@@ -465,7 +475,7 @@ class Batch:
             pass
 
 
-def pattern_build(edof, etype, n_rows):
+def pattern_build(edof, etype, n_rows, upper=False, linked_row=None):
     """fg_pattern_build on an element DOF map ([E][n] indices and types):
     (ai, aj) as numpy uint64 arrays."""
     L = lib()
@@ -474,7 +484,10 @@ def pattern_build(edof, etype, n_rows):
     E, n = edof.shape
     ai = np.zeros(int(n_rows) + 1, np.uint64)
     ajp = C.c_void_p()
-    check(L.fg_pattern_build(edof.ctypes.data, etype.ctypes.data, E, n, int(n_rows), ai.ctypes.data, C.byref(ajp)))
+    lrow = None if linked_row is None else np.ascontiguousarray(linked_row, np.uint64)
+    check(L.fg_pattern_build(edof.ctypes.data, etype.ctypes.data, E, n, int(n_rows), ai.ctypes.data, C.byref(ajp),
+                             1 if upper else 0, lrow.ctypes.data if lrow is not None and lrow.size else None,
+                             0 if lrow is None else len(lrow)))
     nnz = int(ai[-1])
     aj = np.ctypeslib.as_array(C.cast(ajp, C.POINTER(C.c_uint64)), shape=(max(nnz, 1),))[:nnz].copy()
     L.fg_host_free(ajp)

@@ -463,6 +463,7 @@ void Formulation::pre(const Mesh &m) {
   // ---- pattern over the entities carrying bilinear terms
   PatternBuilder pb;
   pb.init(nUnknown);
+  pb.symmetric = symmetric_;
   bucket = nullptr;
   for (auto &ent : m.entities) {
     bool have = false;
@@ -556,6 +557,10 @@ void Formulation::descs(fg_mesh_desc *md, fg_rule_desc *rd, fg_space_desc *sd, f
   sys->elem_dof_idx = elemDofIdx.data();
   sys->elem_dof_type = elemDofType.data();
   sys->n_fixed = nFixed;
+  sys->upper = symmetric_ ? 1 : 0;
+  sys->n_linked = 0;
+  sys->linked_row = nullptr;
+  sys->linked_value = nullptr;
 }
 
 }  // namespace femg

@@ -136,6 +136,11 @@ class Formulation {
   void integral(const Operand &unknown, const Operand &test, const Domain &d, const std::string &gauss);
   void integral(const Function &f, const Operand &test, const Domain &d, const std::string &gauss);
 
+  // the formulation's symmetric() / hermitian() option: upper-triangle
+  // storage of the system matrix (MatrixFactory::addPattern/addValues)
+  void setSymmetric(bool on) { symmetric_ = on; }
+  bool symmetric() const { return symmetric_; }
+
   // DOFs, Hilbert numbering, CSR pattern, element bucket data
   void pre(const Mesh &mesh);
 
@@ -165,6 +170,7 @@ class Formulation {
   std::vector<Dof> created;
 
  private:
+  bool symmetric_ = false;
   struct BTerm {
     Operand unknown, test;
     Domain domain;

@@ -43,6 +43,7 @@ static void buildProblem(fg_problem *p) {
   p->u.reset(new Field("u", omega, st, c.order, mult, 0));
   Field &u = *p->u;
   p->form.reset(new Formulation(c.kind == FG_PROBLEM_NAVIER ? "navier" : c.kind == FG_PROBLEM_MAXWELL ? "maxwell" : "helmholtz"));
+  p->form->setSymmetric(c.upper != 0);
   Formulation &f = *p->form;
   const std::string gauss = "Gauss" + std::to_string(c.gauss);
   const int64_t E = p->mesh.find(c.dim, 1)->blocks[0].size();

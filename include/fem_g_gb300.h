@@ -111,6 +111,17 @@ typedef struct {
   const uint64_t *elem_dof_idx; /* [n_elements][n_basis*multiplicity]: numDof - 1 */
   const int32_t *elem_dof_type; /* same shape: FG_AT_* */
   uint64_t n_fixed;             /* fixed DOFs (size of the Dirichlet value array) */
+  int32_t upper;                /* 1: symmetric or hermitian storage (the formulation's symmetric()
+                                   or hermitian() option): the pattern holds the upper triangle and
+                                   entries below the diagonal are not added
+                                   (MatrixFactory::addPattern/addValues, "jIndex < iIndex") */
+  uint64_t n_linked;            /* linked DOFs (FG_AT_LINKED; elem_dof_idx holds their index below),
+                                   e.g. periodic or Bloch conditions */
+  const uint64_t *linked_row;   /* [n_linked] the row of each linked DOF's master (MatrixFactory _indicesLC) */
+  const double *linked_value;   /* [n_linked][2] its coefficient c (_valuesLC): a linked row adds into its
+                                   master's row times conj(c), a linked column into its master's column
+                                   times c (MatrixFactory.cpp:233-448, VectorFactory.cpp:122-210).
+                                   FG_AT_LINKED_BUBBLE is not supported. */
 } fg_system_desc;
 
 /* Coefficient expression: a complex-valued program over the physical point
@@ -154,11 +165,38 @@ enum {
 };
 enum { FG_DT_NONE = 0, FG_DT_1 = 1, FG_DT_2 = 2 }; /* dof, dt_dof, dt2_dof */
 
+/* Jacobian modificator of the term's domain on this bucket's entity
+ * (domain::JacobiansModificator, src/domain/JacobiansModificator.h:16-30,
+ * applied per term in Assembler::_assembleBilinear/_assembleLinear,
+ * src/term/Assembler.cpp:178-228 and :386-436). At every integration point x
+ * the Jacobian becomes J * jac(x) and the determinant det * det(jac(x)):
+ * transformation shells that stretch [r_min, r_max) to [r_min, infinity),
+ * and the axisymmetric measure r dr dz. An integration point whose shell
+ * radius lies outside [r_min, r_max] (10 machine epsilons of slack) is an
+ * argument error, reported after the element kernel (the reference throws). */
+enum {
+  FG_JACMOD_NONE = 0,
+  FG_JACMOD_AXISYMMETRY = 1,       /* Axisymmetry.cpp:33-56: J(2,2) = x, det *= x */
+  FG_JACMOD_AXISYMMETRY_SHELL = 2, /* AxisymmetryShell.cpp:37-95: r about (0, center[1]), times x */
+  FG_JACMOD_POLAR_SHELL = 3,       /* PolarShell.cpp:37-93: 2D, r about (center[0], center[1]) */
+  FG_JACMOD_CYLINDRICAL_SHELL = 4, /* CylindricalShell.cpp:37-101: r about the axis through center */
+  FG_JACMOD_SPHERICAL_SHELL = 5    /* SphericalShell.cpp:37-95: r about center */
+};
+typedef struct {
+  int32_t kind;     /* FG_JACMOD_* */
+  int32_t axis;     /* cylindrical shell: the axis (0, 1 or 2) */
+  int32_t exponent; /* shells: the exponent of the stretching (1 by default in the reference) */
+  int32_t pad_;
+  double r_min, r_max;
+  double center[3];
+} fg_jacmod;
+
 typedef struct {
   int32_t kind; /* FG_TERM_* */
   int32_t dt;   /* FG_DT_*: with any dt term the AFrequency module applies */
   fg_expr coef; /* c, f, or lambda for FG_TERM_ELASTIC */
   fg_expr coef2; /* mu for FG_TERM_ELASTIC */
+  fg_jacmod jacmod; /* all zero: none */
 } fg_term_desc;
 
 /* ------------------------------------------------------------- plan / run */
@@ -279,9 +317,14 @@ const char *fg_batch_tuning(const fg_batch *batch);
  * that have I, Fixed DOFs take no column, and the bubble rows of an element
  * after its first alias that row. elem_dof_idx / elem_dof_type as in
  * fg_system_desc ([n_elements][n_dofs]). ai: [n_rows + 1], the caller's;
- * *aj: [ai[n_rows]] allocated by the call (free it with fg_host_free). */
+ * *aj: [ai[n_rows]] allocated by the call (free it with fg_host_free).
+ * upper = 1: symmetric storage, only the columns J >= I of a row (for an
+ * aliased bubble row, those of the first bubble's row). linked_row
+ * ([n_linked], as in fg_system_desc): an FG_AT_LINKED DOF is a row and a
+ * column of its master; NULL when there are none. */
 int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *elem_dof_type, int64_t n_elements, int32_t n_dofs,
-                     uint64_t n_rows, uint64_t *ai, uint64_t **aj);
+                     uint64_t n_rows, uint64_t *ai, uint64_t **aj, int32_t upper, const uint64_t *linked_row,
+                     uint64_t n_linked);
 
 /* GPU Hilbert order of n points (float [n][dim], dim 2 or 3) in the box
  * [mn, mx]: the stable order of the keys of src/reorder/Hilbert.cpp:174-288

@@ -48,6 +48,7 @@ typedef struct {
   double omega;      /* Navier: frequency of the mass term -omega^2 rho dof(u); <= 0: the mass
                         term is integral(dt2_dof(u), tf(u)) and the frequency is the assemble call's */
   double lame_sigma; /* Navier: lambda, mu lognormal(median 1, sigma) per element */
+  int32_t upper;     /* 1: symmetric (upper-triangle) storage of the system matrix */
 } fg_problem_config;
 
 typedef struct fg_problem fg_problem;

@@ -46,8 +46,13 @@ typedef struct {
   const double *elem_values[4];
 } or_expr;
 typedef struct {
+  int32_t kind, axis, exponent, pad_;
+  double r_min, r_max, center[3];
+} or_jacmod;
+typedef struct {
   int32_t kind, dt;
   or_expr coef, coef2;
+  or_jacmod jacmod;
 } or_term;
 
 typedef struct {
@@ -62,7 +67,30 @@ typedef struct {
   const double *bgrad;    /* [no][nq][nb][3] */
   const int32_t *orient;  /* [E] (NULL: one table, Lagrange's isConstantByElements) */
   int32_t form;           /* 0: H1 (bval scalar, bgrad gradients); 1: HCurl (bval [..][nb][3] values, bgrad curls) */
+  int32_t upper;          /* symmetric()/hermitian() storage: columns J >= I only */
+  const uint64_t *linked_row; /* [n_linked] master row of a linked DOF (MatrixFactory _indicesLC), or NULL */
+  const double *linked_value; /* [n_linked][2] its coefficient (_valuesLC) */
 } or_bucket;
+
+enum { AT_LINKED = 5, AT_LINKED_BUBBLE = 6 };
+
+/* Row (or column) of an element DOF and its scale: Unknown-like DOFs are
+ * their own row with scale 1; a linked DOF is its master's row with its
+ * coefficient (MatrixFactory.cpp:241-246, :254-259). Returns 0 for the DOFs
+ * that take no row (fixed, undefined). */
+static int or_dof_row(const or_bucket *b, int t, uint64_t idx, uint64_t *row, cplx *scale) {
+  if (t == AT_UNKNOWN || t == AT_UNKNOWN_BUBBLE || t == AT_UNKNOWN_GLOBAL) {
+    *row = idx;
+    *scale = 1.0;
+    return 1;
+  }
+  if (t == AT_LINKED && b->linked_row) {
+    *row = b->linked_row[idx];
+    *scale = b->linked_value[2 * idx] + I * b->linked_value[2 * idx + 1];
+    return 1;
+  }
+  return 0;
+}
 
 /* -------------------------------------------------------- expressions */
 
@@ -132,6 +160,76 @@ static double or_jacobian(const or_bucket *b, int64_t e, int q, double *J, doubl
 #undef M
 }
 
+/* Jacobian modificators, restated from the reference's five implementations:
+ *   Axisymmetry      src/domain/Axisymmetry.cpp:33-56
+ *   AxisymmetryShell src/domain/AxisymmetryShell.cpp:37-95
+ *   PolarShell       src/domain/PolarShell.cpp:37-93
+ *   CylindricalShell src/domain/CylindricalShell.cpp:37-101
+ *   SphericalShell   src/domain/SphericalShell.cpp:37-95
+ * applied by Assembler::_assembleBilinear / _assembleLinear to the term's
+ * Jacobians and determinants (src/term/Assembler.cpp:208-228, :416-436).
+ * Row-major storage as gmsh returns it: jac[9i + 3k + l] = dx_l/du_k, which is
+ * the J[3c + r] layout used here. Returns 0, or 1 when the radius lies
+ * outside the shell (the reference throws). */
+enum { JM_NONE = 0, JM_AXI, JM_AXI_SHELL, JM_POLAR, JM_CYL, JM_SPH };
+static int or_jacmod_apply(const or_jacmod *m, const double *x, double *J, double *det) {
+  const double eps = 2.220446049250313e-16;
+  if (m->kind == JM_NONE) return 0;
+  if (m->kind == JM_AXI) {
+    double R = x[0];
+    if (R == 0.) R = eps;
+    J[8] = R;
+    *det *= R;
+    return 0;
+  }
+  double R, dRdx[3] = {0., 0., 0.}, S = x[0];
+  int two = m->kind == JM_AXI_SHELL || m->kind == JM_POLAR;
+  if (m->kind == JM_AXI_SHELL) {
+    R = sqrt(x[0] * x[0] + (x[1] - m->center[1]) * (x[1] - m->center[1]));
+  } else {
+    double R2 = 0.;
+    for (int j = 0; j < (two ? 2 : 3); ++j) {
+      if (m->kind == JM_CYL && j == m->axis) continue;
+      R2 += (x[j] - m->center[j]) * (x[j] - m->center[j]);
+    }
+    R = sqrt(R2);
+  }
+  if (R < m->r_min - 10. * eps || R > m->r_max + 10. * eps) return 1;
+  if (R >= m->r_max) R = m->r_max - 10 * eps;
+  if (m->kind == JM_AXI_SHELL) {
+    if (S == 0.) S = eps;
+    dRdx[0] = x[0] / R;
+    dRdx[1] = (x[1] - m->center[1]) / R;
+  } else {
+    for (int j = 0; j < (two ? 2 : 3); ++j) dRdx[j] = (m->kind == JM_CYL && j == m->axis) ? 0. : (x[j] - m->center[j]) / R;
+  }
+  const double f = pow((m->r_min * (m->r_max - m->r_min)) / (R * (m->r_max - R)), m->exponent);
+  const double theta = m->exponent * (m->r_max - 2. * R) / (m->r_max - R);
+  double jac[3][3], nj[9];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) jac[a][b] = f * ((a == b ? 1.0 : 0.0) - theta * dRdx[a] * dRdx[b]);
+  if (!two) {
+    if (m->kind == JM_CYL) jac[m->axis][m->axis] = 1.;
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l) nj[k * 3 + l] = J[k * 3 + 0] * jac[0][l] + J[k * 3 + 1] * jac[1][l] + J[k * 3 + 2] * jac[2][l];
+    *det *= m->kind == JM_CYL ? f * f * (1.0 - theta) : f * f * f * (1.0 - theta);
+  } else {
+    for (int k = 0; k < 2; ++k)
+      for (int l = 0; l < 2; ++l) nj[k * 3 + l] = J[k * 3 + 0] * jac[0][l] + J[k * 3 + 1] * jac[1][l];
+    nj[2] = nj[5] = nj[6] = nj[7] = 0.;
+    if (m->kind == JM_POLAR) {
+      nj[8] = 1.;
+      *det *= f * f * (1.0 - theta);
+    } else {
+      nj[8] = S * f;
+      *det *= S * (f * f * f * (1.0 - theta));
+    }
+  }
+  memcpy(J, nj, sizeof(nj));
+  return 0;
+}
+static int or_jacmod_err = 0;
+
 /* FieldEvaluator<Form1>: J^T.inverse() * bf (src/term/evaluator/FieldEvaluator.h:67-70);
  * out G[3][nb] */
 static void or_form1(const double *J, const double *bf, int nb, double *G) {
@@ -189,6 +287,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
       for (int q = 0; q < nq; ++q) {
         double J[9], xq[3];
         double det = or_jacobian(b, e, q, J, xq);
+        if (or_jacmod_apply(&T->jacmod, xq, J, &det)) or_jacmod_err = 1;
         cplx f = eval_expr(&T->coef, e, xq);
         const double *bf = b->bval + ((size_t)o * nq + q) * nb;
         for (int i = 0; i < nb; ++i)
@@ -201,6 +300,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
     for (int q = 0; q < nq; ++q) {
       double J[9], xq[3];
       double det = or_jacobian(b, e, q, J, xq);
+      if (or_jacmod_apply(&T->jacmod, xq, J, &det)) or_jacmod_err = 1;
       const double wd = b->w[q] * det;
       cplx c = eval_expr(&T->coef, e, xq);
       if (T->kind == TERM_MASS && b->form == 1) {
@@ -337,6 +437,7 @@ int or_assemble(const or_bucket *b, const or_term *terms, int nterms, double fre
   for (int t = 0; t < nterms; ++t)
     if (terms[t].kind == TERM_SOURCE) hasSource = 1;
   int err = 0;
+  or_jacmod_err = 0;
 #pragma omp parallel
   {
     cplx *Ae = malloc(sizeof(cplx) * n * n), *tmp = malloc(sizeof(cplx) * n * n), *bl = malloc(sizeof(cplx) * n);
@@ -354,31 +455,46 @@ int or_assemble(const or_bucket *b, const or_term *terms, int nterms, double fre
           haveDC = 1;
           continue;
         }
-        if (ti != AT_UNKNOWN && ti != AT_UNKNOWN_BUBBLE && ti != AT_UNKNOWN_GLOBAL) continue;
-        const uint64_t row = idx[i];
+        uint64_t row, col;
+        cplx si, sj;
+        if (!or_dof_row(b, ti, idx[i], &row, &si)) {
+          if (ti == AT_LINKED_BUBBLE) {
+#pragma omp atomic write
+            err = 3;
+          }
+          continue;
+        }
         for (int j = 0; j < n; ++j) {
           const int tj = typ[j];
           if (tj == AT_FIXED) {
             haveDC = 1;
             continue;
           }
-          if (tj != AT_UNKNOWN && tj != AT_UNKNOWN_BUBBLE && tj != AT_UNKNOWN_GLOBAL) continue;
-          const uint64_t pos = lower_bound_u64(aj, ai[row], ai[row + 1], idx[j]);
-          if (pos == ai[row + 1] || aj[pos] != idx[j]) {
+          if (!or_dof_row(b, tj, idx[j], &col, &sj)) continue;
+          if (b->upper && col < row) continue; /* upper triangular matrix (MatrixFactory.cpp:265) */
+          const uint64_t pos = lower_bound_u64(aj, ai[row], ai[row + 1], col);
+          /* the reference adds at the lower_bound position unchecked (MatrixFactory.cpp:267-268);
+           * with upper storage an aliased bubble row can miss columns, which then land on
+           * the next column of the row */
+          if (pos == ai[row + 1] || (aj[pos] != col && !b->upper)) {
 #pragma omp atomic write
             err = 1;
             continue;
           }
-          atomic_add_c(values + 2 * pos, Ae[i * n + j]);
+          /* linked rows scale by conj(coefficient), linked columns by the coefficient */
+          atomic_add_c(values + 2 * pos, conj(si) * sj * Ae[i * n + j]);
         }
       }
       if (haveDC && rhs) {
+        /* addValuesDC, transposed read (VectorFactory.cpp:178-210) */
         for (int i = 0; i < n; ++i) {
-          if (typ[i] != AT_UNKNOWN && typ[i] != AT_UNKNOWN_BUBBLE && typ[i] != AT_UNKNOWN_GLOBAL) continue;
+          uint64_t row;
+          cplx si;
+          if (!or_dof_row(b, typ[i], idx[i], &row, &si)) continue;
           for (int j = 0; j < n; ++j)
             if (typ[j] == AT_FIXED) {
               cplx uD = dirichlet[2 * idx[j]] + I * dirichlet[2 * idx[j] + 1];
-              atomic_add_c(rhs + 2 * idx[i], Ae[j * n + i] * uD);
+              atomic_add_c(rhs + 2 * row, conj(si) * Ae[j * n + i] * uD);
             }
         }
       }
@@ -391,8 +507,12 @@ int or_assemble(const or_bucket *b, const or_term *terms, int nterms, double fre
         or_element(b, terms, nterms, freq, e, Ae, bl, tmp, G, phi, 0);
         const uint64_t *idx = edof + (size_t)e * n;
         const int32_t *typ = etype + (size_t)e * n;
-        for (int i = 0; i < n; ++i)
-          if (typ[i] == AT_UNKNOWN || typ[i] == AT_UNKNOWN_BUBBLE || typ[i] == AT_UNKNOWN_GLOBAL) atomic_add_c(rhs + 2 * idx[i], bl[i]);
+        for (int i = 0; i < n; ++i) {
+          uint64_t row;
+          cplx si;
+          /* VectorFactory::addValues (VectorFactory.cpp:122-145) */
+          if (or_dof_row(b, typ[i], idx[i], &row, &si)) atomic_add_c(rhs + 2 * row, conj(si) * bl[i]);
+        }
       }
     }
     free(Ae);
@@ -401,7 +521,7 @@ int or_assemble(const or_bucket *b, const or_term *terms, int nterms, double fre
     free(G);
     free(phi);
   }
-  return err;
+  return or_jacmod_err ? 2 : err;
 }
 
 /* --------------------------------------------------------------- pattern */
@@ -429,7 +549,10 @@ static void vec_insert_sorted(u64vec *r, uint64_t x) {
   r->n++;
 }
 
-int or_pattern(int64_t E, int n, const uint64_t *edof, const int32_t *etype, uint64_t n_rows, uint64_t *ai, uint64_t **aj_out) {
+int or_pattern(int64_t E, int n, const uint64_t *edof, const int32_t *etype, uint64_t n_rows, uint64_t *ai, uint64_t **aj_out,
+               int upper, const uint64_t *linked_row) {
+  for (int64_t k = 0; k < E * n; ++k)
+    if (etype[k] == AT_LINKED_BUBBLE || (etype[k] == AT_LINKED && !linked_row)) return 3; /* not restated */
   u64vec *rows = calloc(n_rows, sizeof(u64vec));
   int64_t *alias = malloc(n_rows * sizeof(int64_t));
   for (uint64_t r = 0; r < n_rows; ++r) alias[r] = -1;
@@ -439,8 +562,11 @@ int or_pattern(int64_t E, int n, const uint64_t *edof, const int32_t *etype, uin
     int64_t bubble = -1;
     for (int i = 0; i < n; ++i) {
       const int ti = typ[i];
-      if (ti != AT_UNKNOWN && ti != AT_UNKNOWN_GLOBAL && ti != AT_UNKNOWN_BUBBLE) continue;
-      const uint64_t Ir = idx[i];
+      uint64_t Ir, Jc;
+      /* a linked row is its master's row (MatrixFactory.cpp:468-470) */
+      if (ti == AT_LINKED) Ir = linked_row[idx[i]];
+      else if (ti == AT_UNKNOWN || ti == AT_UNKNOWN_GLOBAL || ti == AT_UNKNOWN_BUBBLE) Ir = idx[i];
+      else continue;
       if (ti == AT_UNKNOWN_BUBBLE) {
         if (bubble >= 0) {
           alias[Ir] = bubble;
@@ -450,8 +576,11 @@ int or_pattern(int64_t E, int n, const uint64_t *edof, const int32_t *etype, uin
       }
       for (int j = 0; j < n; ++j) {
         const int tj = typ[j];
-        if (tj != AT_UNKNOWN && tj != AT_UNKNOWN_GLOBAL && tj != AT_UNKNOWN_BUBBLE) continue;
-        vec_insert_sorted(&rows[Ir], idx[j]);
+        if (tj == AT_LINKED) Jc = linked_row[idx[j]];
+        else if (tj == AT_UNKNOWN || tj == AT_UNKNOWN_GLOBAL || tj == AT_UNKNOWN_BUBBLE) Jc = idx[j];
+        else continue;
+        if (upper && Jc < Ir) continue; /* upper triangular matrix (MatrixFactory.cpp:491) */
+        vec_insert_sorted(&rows[Ir], Jc);
       }
     }
   }

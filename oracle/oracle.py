@@ -20,7 +20,7 @@ class Bucket(C.Structure):
     _fields_ = [("dim", C.c_int), ("nn", C.c_int), ("nq", C.c_int), ("nb", C.c_int), ("mult", C.c_int), ("E", C.c_int64),
                 ("xyz", C.c_void_p), ("enodes", C.c_void_p), ("w", C.c_void_p), ("geo_val", C.c_void_p),
                 ("geo_grad", C.c_void_p), ("bval", C.c_void_p), ("bgrad", C.c_void_p), ("orient", C.c_void_p),
-                ("form", C.c_int32)]
+                ("form", C.c_int32), ("upper", C.c_int32), ("linked_row", C.c_void_p), ("linked_value", C.c_void_p)]
 
 
 def lib():
@@ -31,7 +31,7 @@ def lib():
         P = C.c_void_p
         L.or_element_matrices.argtypes = [C.POINTER(Bucket), P, C.c_int, C.c_double, P, P]
         L.or_assemble.argtypes = [C.POINTER(Bucket), P, C.c_int, C.c_double, P, P, P, P, P, P, P]
-        L.or_pattern.argtypes = [C.c_int64, C.c_int, P, P, C.c_uint64, P, C.POINTER(P)]
+        L.or_pattern.argtypes = [C.c_int64, C.c_int, P, P, C.c_uint64, P, C.POINTER(P), C.c_int, P]
         L.or_free.argtypes = [P]
         L.or_hilbert_keys.argtypes = [C.c_int, C.c_int64, P, P, P, P]
         L.or_hilbert_sort.argtypes = [C.c_int64, P, P]
@@ -83,9 +83,12 @@ def bucket(a):
     k.bv = np.ascontiguousarray(a["bval"], np.float64)
     k.bg = np.ascontiguousarray(a["bgrad"], np.float64)
     k.orient = np.ascontiguousarray(a["orient"], np.int32)
+    k.lrow = np.ascontiguousarray(a.get("linked_row", np.zeros(0)), np.uint64)
+    k.lval = np.ascontiguousarray(a.get("linked_value", np.zeros(0)), np.complex128)
     b = Bucket(a["dim"], a["nn"], a["nq"], a["nb"], a["mult"], a["E"], k.xyz.ctypes.data, k.enodes.ctypes.data, k.w.ctypes.data,
                k.gv.ctypes.data, k.gg.ctypes.data, k.bv.ctypes.data, k.bg.ctypes.data,
-               k.orient.ctypes.data if a["n_orient"] > 1 else None, int(a.get("form", 0)))
+               k.orient.ctypes.data if a["n_orient"] > 1 else None, int(a.get("form", 0)), int(a.get("upper", 0)),
+               k.lrow.ctypes.data if k.lrow.size else None, k.lval.ctypes.data if k.lval.size else None)
     b._keep = k
     return b
 
@@ -113,18 +116,26 @@ def assemble(a, terms_ptr, n_terms, freq=0.0, with_rhs=True):
     err = lib().or_assemble(C.byref(b), C.cast(terms_ptr, C.c_void_p), n_terms, freq, ai.ctypes.data, aj.ctypes.data,
                             edof.ctypes.data, etype.ctypes.data, dirichlet.ctypes.data if dirichlet.size else None,
                             values.ctypes.data, rhs.ctypes.data if with_rhs else None)
+    if err == 2:
+        raise ValueError("oracle: an integration point lies outside a Jacobian modificator's shell")
+    if err == 3:
+        raise ValueError("oracle: linked bubble DOFs are not restated")
     if err:
         raise RuntimeError("oracle: an element DOF pair is missing from the pattern")
     return values, rhs
 
 
-def pattern(edof, etype, n_rows):
+def pattern(edof, etype, n_rows, upper=False, linked_row=None):
     edof = np.ascontiguousarray(edof, np.uint64)
     etype = np.ascontiguousarray(etype, np.int32)
     E, n = edof.shape
     ai = np.zeros(int(n_rows) + 1, np.uint64)
     ajp = C.c_void_p()
-    lib().or_pattern(E, n, edof.ctypes.data, etype.ctypes.data, int(n_rows), ai.ctypes.data, C.byref(ajp))
+    lrow = None if linked_row is None else np.ascontiguousarray(linked_row, np.uint64)
+    st = lib().or_pattern(E, n, edof.ctypes.data, etype.ctypes.data, int(n_rows), ai.ctypes.data, C.byref(ajp), 1 if upper else 0,
+                          lrow.ctypes.data if lrow is not None and lrow.size else None)
+    if st:
+        raise ValueError("oracle: linked bubble DOFs are not restated")
     nnz = int(ai[-1])
     aj = np.ctypeslib.as_array(C.cast(ajp, C.POINTER(C.c_uint64)), shape=(max(nnz, 1),))[:nnz].copy()
     lib().or_free(ajp)
