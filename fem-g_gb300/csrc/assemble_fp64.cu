@@ -510,7 +510,8 @@ int prepareOutputs(fg_plan *plan, double *csr_values, double *rhs, Outputs *o) {
 }
 
 int finishOutputs(fg_plan *plan, const Outputs &o, double *csr_values, double *rhs, cudaStream_t s) {
-  if (o.hostValues) FG_CUDA(cudaMemcpyAsync(csr_values, o.values, plan->d.nnz * 16, cudaMemcpyDeviceToHost, s));
+  if (o.hostValues && !o.valuesCopied) FG_CUDA(cudaMemcpyAsync(csr_values, o.values, plan->d.nnz * 16, cudaMemcpyDeviceToHost, s));
+  if (o.valuesCopied) FG_CUDA(cudaStreamSynchronize(plan->copyStream));
   if (rhs && o.hostRhs) FG_CUDA(cudaMemcpyAsync(rhs, o.rhs, plan->d.nRows * 16, cudaMemcpyDeviceToHost, s));
   if (o.hostValues || (rhs && o.hostRhs)) FG_CUDA(cudaStreamSynchronize(s));
   return FG_OK;
@@ -543,6 +544,6 @@ extern "C" int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_
   if (p.E > 0) {
     if ((st = launchElementFp64(plan, dt, dterms, plan->ke, be, s))) return st;
   }
-  if ((st = launchGather(plan, plan->ke, dt.complexKe, 0, 1, be, uD, o.values, o.rhs, s))) return st;
+  if ((st = gatherToOutputs(plan, plan->ke, dt.complexKe, 0, 1, be, uD, o, csr_values, s))) return st;
   return finishOutputs(plan, o, csr_values, rhs, s);
 }

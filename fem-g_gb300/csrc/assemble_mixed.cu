@@ -1136,7 +1136,7 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
   }
   if (p.E > 0)
     if ((st = launchMixedElement(plan, &dterms, 1, s))) return st;
-  if ((st = launchGather(plan, (const double *)m->ke, dt.complexKe, 1, m->blocks, be, uD, o.values, o.rhs, s))) return st;
+  if ((st = gatherToOutputs(plan, (const double *)m->ke, dt.complexKe, 1, m->blocks, be, uD, o, csr_values, s))) return st;
   if (report) {
     // FP64 element matrices and CSR of the same terms, compared on the device
     const int ncomp = dt.complexKe ? 2 : 1;

@@ -42,6 +42,7 @@ class ProfScope {
 constexpr int kMaxDofs = 64;         // element DOFs (basis x multiplicity) handled on device
 constexpr int kMaxNodes = 10;        // geometric nodes per element
 constexpr int kMaxTerms = 6;
+constexpr int kOutChunks = 8;        // row ranges of the gather for overlapped host copies
 constexpr uint16_t kSlotFixed = 0xFFFF;   // column is a fixed DOF (Dirichlet lifting)
 constexpr uint16_t kSlotIgnore = 0xFFFE;  // column does not assemble (undefined type)
 
@@ -118,6 +119,11 @@ struct fg_plan {
   // host copies needed by later calls
   std::vector<uint64_t> hAi;
   int64_t E = 0;
+  // row ranges of the gather's visiting order ([k] .. [k + 1]), copied out
+  // one by one when the CSR values go to the host
+  std::vector<uint64_t> outChunkRow;
+  cudaStream_t copyStream = nullptr;
+  std::vector<cudaEvent_t> copyEvents;
   // owned device allocations
   std::vector<void *> allocs;
   // scratch (grown on demand)
@@ -170,9 +176,14 @@ int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, 
 struct Outputs {
   double *values = nullptr, *rhs = nullptr;
   bool hostValues = false, hostRhs = false;
+  bool valuesCopied = false;  // the host copy of the values is already queued (range by range)
 };
 int prepareOutputs(fg_plan *plan, double *csr_values, double *rhs, Outputs *o);
 int finishOutputs(fg_plan *plan, const Outputs &o, double *csr_values, double *rhs, cudaStream_t s);
+// The CSR reduction into the outputs: with host values, range by range, each
+// range's slice copied to the host on a second stream while the next reduces
+int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+                    const double *dirichletDev, Outputs &o, double *csr_values, cudaStream_t s);
 // FP64 element kernel (also used as the reference for the mixed error report)
 int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s);
 // One plan of a batched gather launch

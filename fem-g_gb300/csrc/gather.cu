@@ -22,7 +22,8 @@ namespace femg {
 template <typename SlotT, bool KCPLX, typename KT, typename AT, int L>
 __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restrict__ ke, const double2 *__restrict__ be,
                                            const double2 *__restrict__ uD, double2 *__restrict__ values,
-                                           double2 *__restrict__ rhs, int rowsPerBlock, int blk3, int64_t blk, int64_t nblk) {
+                                           double2 *__restrict__ rhs, int rowsPerBlock, int blk3, int64_t blk, int64_t nblk,
+                                           int64_t v0, int64_t v1) {
   constexpr int R = 32 / L;  // rows per warp
   constexpr int J = 3;       // columns per lane
   constexpr int SS = KCPLX ? 2 : 1;
@@ -44,11 +45,12 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
   const SlotT kIgnore = (SlotT)(sizeof(SlotT) == 1 ? 0xFE : kSlotIgnore);
   const int n = p.n;
   const size_t nn2 = (size_t)n * n;
-  const int64_t nRows = (int64_t)p.nRows;
+  // visit records [v0, v1) of this launch
+  const int64_t nRows = v1;
   const int64_t stride = nblk * rowsPerBlock;
-  const int64_t first = blk * rowsPerBlock + warp * R + sub;
+  const int64_t first = v0 + blk * rowsPerBlock + warp * R + sub;
   uint4 vNext = first < nRows ? p.visit[first] : make_uint4(0, 0, 0, 0);
-  for (int64_t base = blk * rowsPerBlock + warp * R; base < nRows; base += stride) {
+  for (int64_t base = v0 + blk * rowsPerBlock + warp * R; base < nRows; base += stride) {
     const int64_t idx = base + sub;
     const bool live = idx < nRows;
     const uint4 v = vNext;  // this row's record, fetched one iteration ahead
@@ -162,8 +164,8 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
 template <typename SlotT, bool KCPLX, typename KT, typename AT, int L>
 __global__ void __launch_bounds__(256)
     k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
-             double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock, int blk3) {
-  gatherRows<SlotT, KCPLX, KT, AT, L>(p, ke, be, uD, values, rhs, rowsPerBlock, blk3, blockIdx.x, gridDim.x);
+             double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock, int blk3, int64_t v0, int64_t v1) {
+  gatherRows<SlotT, KCPLX, KT, AT, L>(p, ke, be, uD, values, rhs, rowsPerBlock, blk3, blockIdx.x, gridDim.x, v0, v1);
 }
 
 // Many plans in one launch: job q owns blocks [blockStart, blockStart + nBlocks)
@@ -177,12 +179,12 @@ __global__ void __launch_bounds__(256) k_gather_batch(const GatherJob *__restric
   }
   const GatherJob &J = jobs[lo];
   gatherRows<SlotT, KCPLX, KT, AT, L>(J.p, (const KT *)J.ke, J.be, J.uD, J.values, J.rhs, rowsPerBlock, J.blk3,
-                                      (int64_t)blockIdx.x - J.blockStart, J.nBlocks);
+                                      (int64_t)blockIdx.x - J.blockStart, J.nBlocks, 0, (int64_t)J.p.nRows);
 }
 
 template <typename SlotT, bool KCPLX, typename KT>
 static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, const double2 *uD, double2 *values, double2 *rhs,
-                       int blk3, cudaStream_t s) {
+                       int blk3, int64_t v0, int64_t v1, cudaStream_t s) {
   using AT = KT;  // FP32 element matrices accumulate in FP32, FP64 ones in FP64
   const int n = p.n;
   int L = 32;
@@ -201,8 +203,8 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
   const size_t smem = rowBytes * R * wpb;
   const int rowsPerBlock = wpb * R;
   const int sms = smCount();
-  int64_t blocks = ((int64_t)p.nRows + rowsPerBlock - 1) / rowsPerBlock;
-  blocks = std::min<int64_t>(blocks, (int64_t)sms * 16);
+  int64_t blocks = (v1 - v0 + rowsPerBlock - 1) / rowsPerBlock;
+  blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)sms * 16));
 #define FG_GATHER_L(LL)                                                                                           \
   case LL: {                                                                                                      \
     auto kern = k_gather<SlotT, KCPLX, KT, AT, LL>;                                                               \
@@ -211,7 +213,7 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
       FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                \
       smemSet = smem;                                                                                             \
     }                                                                                                             \
-    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock, blk3);   \
+    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock, blk3, v0, v1); \
     break;                                                                                                        \
   }
   switch (L) {
@@ -226,11 +228,12 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
   return FG_OK;
 }
 
-int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
-                 const double *dirichletDev, double *values, double *rhs, cudaStream_t s) {
+// The rows of visit records [v0, v1) (all rows: 0, nRows).
+static int launchGatherRange(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+                             const double *dirichletDev, double *values, double *rhs, int64_t v0, int64_t v1, cudaStream_t s) {
   const int blk3 = keBlocks == 9 ? 1 : 0;
   const PlanDev &p = plan->d;
-  if (p.nRows == 0) return FG_OK;
+  if (v1 <= v0) return FG_OK;
   if (p.lscale && !keComplex) {
     setLastError("gather: linked DOFs need complex element matrices");
     return FG_ERR_UNSUPPORTED;
@@ -243,12 +246,44 @@ int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, 
   countLaunch();
   if (p.slotBytes == 1) {
     if (keIsFloat)
-      return keComplex ? launchTyped<uint8_t, true, float>(p, ke, be2, uD, v2, r2, blk3, s) : launchTyped<uint8_t, false, float>(p, ke, be2, uD, v2, r2, blk3, s);
-    return keComplex ? launchTyped<uint8_t, true, double>(p, ke, be2, uD, v2, r2, blk3, s) : launchTyped<uint8_t, false, double>(p, ke, be2, uD, v2, r2, blk3, s);
+      return keComplex ? launchTyped<uint8_t, true, float>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s) : launchTyped<uint8_t, false, float>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s);
+    return keComplex ? launchTyped<uint8_t, true, double>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s) : launchTyped<uint8_t, false, double>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s);
   }
   if (keIsFloat)
-    return keComplex ? launchTyped<uint16_t, true, float>(p, ke, be2, uD, v2, r2, blk3, s) : launchTyped<uint16_t, false, float>(p, ke, be2, uD, v2, r2, blk3, s);
-  return keComplex ? launchTyped<uint16_t, true, double>(p, ke, be2, uD, v2, r2, blk3, s) : launchTyped<uint16_t, false, double>(p, ke, be2, uD, v2, r2, blk3, s);
+    return keComplex ? launchTyped<uint16_t, true, float>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s) : launchTyped<uint16_t, false, float>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s);
+  return keComplex ? launchTyped<uint16_t, true, double>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s) : launchTyped<uint16_t, false, double>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s);
+}
+
+int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+                 const double *dirichletDev, double *values, double *rhs, cudaStream_t s) {
+  return launchGatherRange(plan, ke, keComplex, keIsFloat, keBlocks, be, dirichletDev, values, rhs, 0, (int64_t)plan->d.nRows, s);
+}
+
+// Host values: the reduction runs range by range; after each range an event
+// lets the copy stream bring that range's CSR slice to the host while the
+// next range reduces (the copy, not the reduction, bounds a host-output call).
+int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+                    const double *dirichletDev, Outputs &o, double *csr_values, cudaStream_t s) {
+  const size_t nc = plan->outChunkRow.size() > 1 ? plan->outChunkRow.size() - 1 : 0;
+  if (!o.hostValues || nc < 2)
+    return launchGather(plan, ke, keComplex, keIsFloat, keBlocks, be, dirichletDev, o.values, o.rhs, s);
+  if (!plan->copyStream) {
+    FG_CUDA(cudaStreamCreateWithFlags(&plan->copyStream, cudaStreamNonBlocking));
+    plan->copyEvents.assign(nc, nullptr);
+    for (auto &ev : plan->copyEvents) FG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  for (size_t c = 0; c < nc; ++c) {
+    const uint64_t r0 = plan->outChunkRow[c], r1 = plan->outChunkRow[c + 1];
+    int st = launchGatherRange(plan, ke, keComplex, keIsFloat, keBlocks, be, dirichletDev, o.values, o.rhs, (int64_t)r0, (int64_t)r1, s);
+    if (st) return st;
+    FG_CUDA(cudaEventRecord(plan->copyEvents[c], s));
+    FG_CUDA(cudaStreamWaitEvent(plan->copyStream, plan->copyEvents[c], 0));
+    const uint64_t a0 = plan->hAi[r0], a1 = plan->hAi[r1];
+    if (a1 > a0)
+      FG_CUDA(cudaMemcpyAsync(csr_values + 2 * a0, o.values + 2 * a0, (a1 - a0) * 16, cudaMemcpyDeviceToHost, plan->copyStream));
+  }
+  o.valuesCopied = true;
+  return FG_OK;
 }
 
 // Shared memory and rows per block of one gather configuration

@@ -287,15 +287,27 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
       }
   }
 
-  // gather visiting order: rows grouped by contribution count (stable)
+  // gather visiting order: the rows in kOutChunks consecutive ranges (the
+  // visit indices of a range are its rows' indices, so the CSR slice of a
+  // range is complete once its part of the visit order has run, and can be
+  // copied out while the next range reduces); within a range, rows grouped
+  // by contribution count (stable)
   std::vector<uint32_t> rowOrder(sys->n_rows);
   {
+    const int nChunks = sys->n_rows >= (uint64_t)kOutChunks * 4096 ? kOutChunks : 1;
+    plan->outChunkRow.assign((size_t)nChunks + 1, 0);
+    for (int c = 0; c <= nChunks; ++c) plan->outChunkRow[(size_t)c] = sys->n_rows * (uint64_t)c / (uint64_t)nChunks;
     uint64_t maxCnt = 0;
     for (uint64_t r = 0; r < sys->n_rows; ++r) maxCnt = std::max(maxCnt, rowPtr[r + 1] - rowPtr[r]);
-    std::vector<uint64_t> bucket(maxCnt + 2, 0);
-    for (uint64_t r = 0; r < sys->n_rows; ++r) bucket[rowPtr[r + 1] - rowPtr[r] + 1]++;
-    for (uint64_t c = 0; c <= maxCnt; ++c) bucket[c + 1] += bucket[c];
-    for (uint64_t r = 0; r < sys->n_rows; ++r) rowOrder[bucket[rowPtr[r + 1] - rowPtr[r]]++] = (uint32_t)r;
+    std::vector<uint64_t> bucket(maxCnt + 2);
+    for (int c = 0; c < nChunks; ++c) {
+      const uint64_t ra = plan->outChunkRow[(size_t)c], rb = plan->outChunkRow[(size_t)c + 1];
+      std::fill(bucket.begin(), bucket.end(), 0);
+      bucket[0] = ra;
+      for (uint64_t r = ra; r < rb; ++r) bucket[rowPtr[r + 1] - rowPtr[r] + 1]++;
+      for (uint64_t k = 0; k <= maxCnt; ++k) bucket[k + 1] += bucket[k];
+      for (uint64_t r = ra; r < rb; ++r) rowOrder[bucket[rowPtr[r + 1] - rowPtr[r]]++] = (uint32_t)r;
+    }
   }
   if (sys->n_rows >= (uint64_t(1) << 32) || d.nnz >= (uint64_t(1) << 32) || rowElem.size() >= (uint64_t(1) << 32)) {
     setLastError("fg_plan_create: more than 2^32 rows, nonzeros or element rows in one plan");
@@ -715,6 +727,9 @@ void fg_plan_destroy(fg_plan *plan) {
   multiDestroy(plan);
   fp64fDestroy(plan);
   if (plan->jmErrHost) cudaFreeHost(plan->jmErrHost);
+  for (cudaEvent_t ev : plan->copyEvents)
+    if (ev) cudaEventDestroy(ev);
+  if (plan->copyStream) cudaStreamDestroy(plan->copyStream);
   delete plan;
 }
 
