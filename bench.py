@@ -462,7 +462,7 @@ def main():
     def e2e_step():
         femg.check(fn(plan.ptr, tt, nt, 0.0, dptr, hv.data_ptr(), hb.data_ptr(), sptr, *extra))
 
-    e2e_steps = max(3, min(args.steps, 10))
+    e2e_steps = max(3, min(args.steps, 20))
     for _ in range(args.warmup):
         e2e_step()
     torch.cuda.synchronize()

@@ -122,6 +122,8 @@ struct fg_plan {
   // row ranges of the gather's visiting order ([k] .. [k + 1]), copied out
   // one by one when the CSR values go to the host
   std::vector<uint64_t> outChunkRow;
+  const uint4 *visitRanged = nullptr;         // the visit tables in range-major order
+  const uint32_t *visitElemRanged = nullptr;
   cudaStream_t copyStream = nullptr;
   std::vector<cudaEvent_t> copyEvents;
   // owned device allocations

@@ -229,10 +229,9 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
 }
 
 // The rows of visit records [v0, v1) (all rows: 0, nRows).
-static int launchGatherRange(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+static int launchGatherRange(const PlanDev &p, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
                              const double *dirichletDev, double *values, double *rhs, int64_t v0, int64_t v1, cudaStream_t s) {
   const int blk3 = keBlocks == 9 ? 1 : 0;
-  const PlanDev &p = plan->d;
   if (v1 <= v0) return FG_OK;
   if (p.lscale && !keComplex) {
     setLastError("gather: linked DOFs need complex element matrices");
@@ -256,7 +255,7 @@ static int launchGatherRange(fg_plan *plan, const double *ke, int keComplex, int
 
 int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
                  const double *dirichletDev, double *values, double *rhs, cudaStream_t s) {
-  return launchGatherRange(plan, ke, keComplex, keIsFloat, keBlocks, be, dirichletDev, values, rhs, 0, (int64_t)plan->d.nRows, s);
+  return launchGatherRange(plan->d, ke, keComplex, keIsFloat, keBlocks, be, dirichletDev, values, rhs, 0, (int64_t)plan->d.nRows, s);
 }
 
 // Host values: the reduction runs range by range; after each range an event
@@ -272,9 +271,12 @@ int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloa
     plan->copyEvents.assign(nc, nullptr);
     for (auto &ev : plan->copyEvents) FG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   }
+  PlanDev pr = plan->d;  // the range-major visiting order
+  pr.visit = plan->visitRanged;
+  pr.visitElem = plan->visitElemRanged;
   for (size_t c = 0; c < nc; ++c) {
     const uint64_t r0 = plan->outChunkRow[c], r1 = plan->outChunkRow[c + 1];
-    int st = launchGatherRange(plan, ke, keComplex, keIsFloat, keBlocks, be, dirichletDev, o.values, o.rhs, (int64_t)r0, (int64_t)r1, s);
+    int st = launchGatherRange(pr, ke, keComplex, keIsFloat, keBlocks, be, dirichletDev, o.values, o.rhs, (int64_t)r0, (int64_t)r1, s);
     if (st) return st;
     FG_CUDA(cudaEventRecord(plan->copyEvents[c], s));
     FG_CUDA(cudaStreamWaitEvent(plan->copyStream, plan->copyEvents[c], 0));

@@ -287,26 +287,31 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
       }
   }
 
-  // gather visiting order: the rows in kOutChunks consecutive ranges (the
-  // visit indices of a range are its rows' indices, so the CSR slice of a
-  // range is complete once its part of the visit order has run, and can be
-  // copied out while the next range reduces); within a range, rows grouped
-  // by contribution count (stable)
-  std::vector<uint32_t> rowOrder(sys->n_rows);
+  // gather visiting orders, rows grouped by contribution count (stable):
+  // over all rows (rowOrder, for device outputs), and within kOutChunks
+  // consecutive row ranges (rowOrderRanged, for host outputs: the visit
+  // indices of a range are its rows' indices, so the CSR slice of a range is
+  // complete once its part of the order has run, and can be copied out while
+  // the next range reduces)
+  std::vector<uint32_t> rowOrder(sys->n_rows), rowOrderRanged;
+  const int nChunks = sys->n_rows >= (uint64_t)kOutChunks * 4096 ? kOutChunks : 1;
   {
-    const int nChunks = sys->n_rows >= (uint64_t)kOutChunks * 4096 ? kOutChunks : 1;
     plan->outChunkRow.assign((size_t)nChunks + 1, 0);
     for (int c = 0; c <= nChunks; ++c) plan->outChunkRow[(size_t)c] = sys->n_rows * (uint64_t)c / (uint64_t)nChunks;
     uint64_t maxCnt = 0;
     for (uint64_t r = 0; r < sys->n_rows; ++r) maxCnt = std::max(maxCnt, rowPtr[r + 1] - rowPtr[r]);
     std::vector<uint64_t> bucket(maxCnt + 2);
-    for (int c = 0; c < nChunks; ++c) {
-      const uint64_t ra = plan->outChunkRow[(size_t)c], rb = plan->outChunkRow[(size_t)c + 1];
+    auto countSort = [&](uint64_t ra, uint64_t rb, std::vector<uint32_t> &order) {
       std::fill(bucket.begin(), bucket.end(), 0);
       bucket[0] = ra;
       for (uint64_t r = ra; r < rb; ++r) bucket[rowPtr[r + 1] - rowPtr[r] + 1]++;
       for (uint64_t k = 0; k <= maxCnt; ++k) bucket[k + 1] += bucket[k];
-      for (uint64_t r = ra; r < rb; ++r) rowOrder[bucket[rowPtr[r + 1] - rowPtr[r]]++] = (uint32_t)r;
+      for (uint64_t r = ra; r < rb; ++r) order[bucket[rowPtr[r + 1] - rowPtr[r]]++] = (uint32_t)r;
+    };
+    countSort(0, sys->n_rows, rowOrder);
+    if (nChunks > 1) {
+      rowOrderRanged.resize(sys->n_rows);
+      for (int c = 0; c < nChunks; ++c) countSort(plan->outChunkRow[(size_t)c], plan->outChunkRow[(size_t)c + 1], rowOrderRanged);
     }
   }
   if (sys->n_rows >= (uint64_t(1) << 32) || d.nnz >= (uint64_t(1) << 32) || rowElem.size() >= (uint64_t(1) << 32)) {
@@ -316,22 +321,29 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   // visit table: one 16-byte record per row in visiting order (row, CSR
   // start, start of its element list, length | count << 16), the element
   // lists stored contiguously in that order
-  std::vector<uint4> visit(sys->n_rows);
-  std::vector<uint32_t> visitElem(rowElem.size());
-  {
+  std::vector<uint4> visit(sys->n_rows), visitRanged;
+  std::vector<uint32_t> visitElem(rowElem.size()), visitElemRanged;
+  auto buildVisit = [&](const std::vector<uint32_t> &order, std::vector<uint4> &vis, std::vector<uint32_t> &visElem) -> int {
     uint64_t pos = 0;
     for (uint64_t v = 0; v < sys->n_rows; ++v) {
-      const uint32_t r = rowOrder[v];
+      const uint32_t r = order[v];
       const uint64_t cnt = rowPtr[r + 1] - rowPtr[r];
       const uint64_t len = sys->ai[r + 1] - sys->ai[r];
       if (cnt > 0xFFFF || len > 0xFFFF) {
         setLastError("fg_plan_create: row with more than 65535 entries or contributions");
         return FG_ERR_UNSUPPORTED;
       }
-      std::copy(rowElem.begin() + (int64_t)rowPtr[r], rowElem.begin() + (int64_t)rowPtr[r + 1], visitElem.begin() + (int64_t)pos);
-      visit[v] = make_uint4(r, (uint32_t)sys->ai[r], (uint32_t)pos, (uint32_t)(len | (cnt << 16)));
+      std::copy(rowElem.begin() + (int64_t)rowPtr[r], rowElem.begin() + (int64_t)rowPtr[r + 1], visElem.begin() + (int64_t)pos);
+      vis[v] = make_uint4(r, (uint32_t)sys->ai[r], (uint32_t)pos, (uint32_t)(len | (cnt << 16)));
       pos += cnt;
     }
+    return FG_OK;
+  };
+  if (int st0 = buildVisit(rowOrder, visit, visitElem)) return st0;
+  if (nChunks > 1) {
+    visitRanged.resize(sys->n_rows);
+    visitElemRanged.resize(rowElem.size());
+    if (int st0 = buildVisit(rowOrderRanged, visitRanged, visitElemRanged)) return st0;
   }
 
   // slots: position of each column inside its row
@@ -411,6 +423,12 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   if ((st = upload(plan, rowOrder.data(), rowOrder.size(), &d.rowOrder))) return st;
   if ((st = upload(plan, visit.data(), visit.size(), &d.visit))) return st;
   if ((st = upload(plan, visitElem.data(), visitElem.size(), &d.visitElem))) return st;
+  plan->visitRanged = d.visit;
+  plan->visitElemRanged = d.visitElem;
+  if (nChunks > 1) {
+    if ((st = upload(plan, visitRanged.data(), visitRanged.size(), &plan->visitRanged))) return st;
+    if ((st = upload(plan, visitElemRanged.data(), visitElemRanged.size(), &plan->visitElemRanged))) return st;
+  }
   if (narrow) {
     const uint8_t *p;
     if ((st = upload(plan, slot8.data(), slot8.size(), &p))) return st;
