@@ -294,7 +294,8 @@ int tune(fg_batch *b, cudaStream_t s) {
     if ((st = uploadJobs(c, s))) return st;
     js += std::string(ci ? ", " : "") + "{\"dim\": " + std::to_string(c.dim) + ", \"n\": " + std::to_string(c.n) +
           ", \"nq\": " + std::to_string(c.nq) + ", \"problems\": " + std::to_string(c.probs.size()) +
-          ", \"lanes\": " + std::to_string(c.shape.L) + ", \"warps\": " + std::to_string(c.shape.wpb) +
+          ", \"lanes\": " + std::to_string(c.shape.L) + ", \"columns\": " + std::to_string(c.shape.J) +
+          ", \"warps\": " + std::to_string(c.shape.wpb) +
           ", \"ms\": " + std::to_string(best) + "}";
   }
   b->tuning = js + "]}";

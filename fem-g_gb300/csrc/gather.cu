@@ -19,13 +19,12 @@ namespace femg {
 
 // The rows of one plan handled by block `blk` of `nblk` (grid-stride over row
 // groups of rowsPerBlock rows).
-template <typename SlotT, bool KCPLX, typename KT, typename AT, int L>
+template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J>
 __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restrict__ ke, const double2 *__restrict__ be,
                                            const double2 *__restrict__ uD, double2 *__restrict__ values,
                                            double2 *__restrict__ rhs, int rowsPerBlock, int blk3, int64_t blk, int64_t nblk,
                                            int64_t v0, int64_t v1) {
-  constexpr int R = 32 / L;  // rows per warp
-  constexpr int J = 3;       // columns per lane
+  constexpr int R = 32 / L;  // rows per warp; J: columns per lane (L * J >= n)
   constexpr int SS = KCPLX ? 2 : 1;
   // offset of entry (test ii, unknown jj) inside one component of an element
   // matrix: row-major [n][n], or (compound fields from the tensor-core path)
@@ -161,15 +160,15 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
   }
 }
 
-template <typename SlotT, bool KCPLX, typename KT, typename AT, int L>
+template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J>
 __global__ void __launch_bounds__(256)
     k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
              double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock, int blk3, int64_t v0, int64_t v1) {
-  gatherRows<SlotT, KCPLX, KT, AT, L>(p, ke, be, uD, values, rhs, rowsPerBlock, blk3, blockIdx.x, gridDim.x, v0, v1);
+  gatherRows<SlotT, KCPLX, KT, AT, L, J>(p, ke, be, uD, values, rhs, rowsPerBlock, blk3, blockIdx.x, gridDim.x, v0, v1);
 }
 
 // Many plans in one launch: job q owns blocks [blockStart, blockStart + nBlocks)
-template <typename SlotT, bool KCPLX, typename KT, typename AT, int L>
+template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J>
 __global__ void __launch_bounds__(256) k_gather_batch(const GatherJob *__restrict__ jobs, int nJobs, int rowsPerBlock) {
   int lo = 0, hi = nJobs - 1;
   while (lo < hi) {  // last job whose blockStart <= blockIdx.x
@@ -177,21 +176,17 @@ __global__ void __launch_bounds__(256) k_gather_batch(const GatherJob *__restric
     if (jobs[mid].blockStart <= (int64_t)blockIdx.x) lo = mid;
     else hi = mid - 1;
   }
-  const GatherJob &J = jobs[lo];
-  gatherRows<SlotT, KCPLX, KT, AT, L>(J.p, (const KT *)J.ke, J.be, J.uD, J.values, J.rhs, rowsPerBlock, J.blk3,
-                                      (int64_t)blockIdx.x - J.blockStart, J.nBlocks, 0, (int64_t)J.p.nRows);
+  const GatherJob &Jb = jobs[lo];
+  gatherRows<SlotT, KCPLX, KT, AT, L, J>(Jb.p, (const KT *)Jb.ke, Jb.be, Jb.uD, Jb.values, Jb.rhs, rowsPerBlock, Jb.blk3,
+                                         (int64_t)blockIdx.x - Jb.blockStart, Jb.nBlocks, 0, (int64_t)Jb.p.nRows);
 }
 
 template <typename SlotT, bool KCPLX, typename KT>
 static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, const double2 *uD, double2 *values, double2 *rhs,
                        int blk3, int64_t v0, int64_t v1, cudaStream_t s) {
   using AT = KT;  // FP32 element matrices accumulate in FP32, FP64 ones in FP64
-  const int n = p.n;
-  int L = 32;
-  if (n <= 6) L = 2;
-  else if (n <= 12) L = 4;
-  else if (n <= 24) L = 8;
-  else if (n <= 48) L = 16;
+  const GatherShape shape = gatherShape(p.n, p.maxRowLen, KCPLX ? 1 : 0, sizeof(KT) == 4 ? 1 : 0, 0, 0);
+  const int L = shape.L, J = shape.J;
   const int R = 32 / L;
   const size_t rowBytes = (size_t)std::max(p.maxRowLen, 1) * (KCPLX ? 2 : 1) * sizeof(AT);
   int wpb = 8;
@@ -205,24 +200,22 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
   const int sms = smCount();
   int64_t blocks = (v1 - v0 + rowsPerBlock - 1) / rowsPerBlock;
   blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)sms * 16));
-#define FG_GATHER_L(LL)                                                                                           \
-  case LL: {                                                                                                      \
-    auto kern = k_gather<SlotT, KCPLX, KT, AT, LL>;                                                               \
+#define FG_GATHER_L(LL, JJ)                                                                                       \
+  if (L == LL && J == JJ) {                                                                                       \
+    auto kern = k_gather<SlotT, KCPLX, KT, AT, LL, JJ>;                                                           \
     static size_t smemSet = 0;                                                                                    \
     if (smem > smemSet) {                                                                                         \
       FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                \
       smemSet = smem;                                                                                             \
     }                                                                                                             \
     kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock, blk3, v0, v1); \
-    break;                                                                                                        \
   }
-  switch (L) {
-    FG_GATHER_L(2)
-    FG_GATHER_L(4)
-    FG_GATHER_L(8)
-    FG_GATHER_L(16)
-    FG_GATHER_L(32)
-  }
+  FG_GATHER_L(2, 3)
+  FG_GATHER_L(4, 3)
+  FG_GATHER_L(8, 3)
+  FG_GATHER_L(8, 5)
+  FG_GATHER_L(16, 3)
+  FG_GATHER_L(32, 3)
 #undef FG_GATHER_L
   FG_CUDA(cudaGetLastError());
   return FG_OK;
@@ -289,16 +282,20 @@ int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloa
 }
 
 // Shared memory and rows per block of one gather configuration
+// Lanes per row and columns per lane: (2, 3), (4, 3), (8, 3), (8, 5),
+// (16, 3) or (32, 3). By default the narrowest that covers n (8 x 5 for
+// 25..40 columns measured 7% faster than 16 x 3 on order-4 tets); for a given
+// L, J = 3 when 3L covers n, else 5 (L = 8 only).
 GatherShape gatherShape(int n, int maxRowLen, int kcplx, int keIsFloat, int L, int wpb) {
   GatherShape g;
-  g.J = 3;
   if (L <= 0) {
     L = 32;
     if (n <= 6) L = 2;
     else if (n <= 12) L = 4;
-    else if (n <= 24) L = 8;
+    else if (n <= 40) L = 8;
     else if (n <= 48) L = 16;
   }
+  g.J = 3 * L >= n ? 3 : 5;
   const int R = 32 / L;
   const size_t rowBytes = (size_t)std::max(maxRowLen, 1) * (kcplx ? 2 : 1) * (keIsFloat ? 4 : 8);
   if (wpb <= 0) {
@@ -309,35 +306,34 @@ GatherShape gatherShape(int n, int maxRowLen, int kcplx, int keIsFloat, int L, i
   g.wpb = wpb;
   g.rowsPerBlock = wpb * R;
   g.smem = rowBytes * R * wpb;
-  g.ok = g.smem <= 200 * 1024 && 3 * L >= n;
+  g.ok = g.smem <= 200 * 1024 && g.J * L >= n && (g.J == 3 || L == 8);
   return g;
 }
 
 template <typename SlotT, bool KCPLX, typename KT>
 static int launchBatchTyped(const GatherJob *jobs, int nJobs, int64_t blocks, const GatherShape &g, cudaStream_t s) {
   using AT = KT;
-#define FG_GATHER_B(LL)                                                                                   \
-  case LL: {                                                                                              \
-    auto kern = k_gather_batch<SlotT, KCPLX, KT, AT, LL>;                                                 \
+#define FG_GATHER_B(LL, JJ)                                                                               \
+  if (g.L == LL && g.J == JJ) {                                                                           \
+    auto kern = k_gather_batch<SlotT, KCPLX, KT, AT, LL, JJ>;                                             \
     static size_t smemSet = 0;                                                                            \
     if (g.smem > smemSet) {                                                                               \
       FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem));      \
       smemSet = g.smem;                                                                                   \
     }                                                                                                     \
     kern<<<(unsigned)blocks, 32 * g.wpb, g.smem, s>>>(jobs, nJobs, g.rowsPerBlock);                       \
-    break;                                                                                                \
+    FG_CUDA(cudaGetLastError());                                                                          \
+    return FG_OK;                                                                                         \
   }
-  switch (g.L) {
-    FG_GATHER_B(2)
-    FG_GATHER_B(4)
-    FG_GATHER_B(8)
-    FG_GATHER_B(16)
-    FG_GATHER_B(32)
-    default:
-      setLastError("batched gather: lanes per row must be 2, 4, 8, 16 or 32");
-      return FG_ERR_ARG;
-  }
+  FG_GATHER_B(2, 3)
+  FG_GATHER_B(4, 3)
+  FG_GATHER_B(8, 3)
+  FG_GATHER_B(8, 5)
+  FG_GATHER_B(16, 3)
+  FG_GATHER_B(32, 3)
 #undef FG_GATHER_B
+  setLastError("batched gather: unsupported (lanes, columns) shape");
+  return FG_ERR_ARG;
   FG_CUDA(cudaGetLastError());
   return FG_OK;
 }

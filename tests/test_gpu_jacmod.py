@@ -128,3 +128,21 @@ def test_batches_decline_modificators(femg, cuda):
     nts = (C.c_int32 * 1)(nt)
     out = C.c_void_p()
     assert L.fg_batch_create(plans, tl, nts, 1, 0, C.byref(out)) == femg.FG_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("bad", ["kind", "radii", "axis", "exponent"])
+def test_invalid_modificator_arguments(femg, cuda, bad):
+    prob = jm_problem(femg, 3, 2, gauss=4)
+    t, nt = copy_terms(femg, prob)
+    args = dict(center=(-2.0, 0.5, 0.5))
+    if bad == "kind":
+        set_jm(femg, t[0], 9, **args)
+    elif bad == "radii":
+        set_jm(femg, t[0], femg.FG_JACMOD_SPHERICAL_SHELL, r_min=3.0, r_max=2.0, **args)
+    elif bad == "axis":
+        set_jm(femg, t[0], femg.FG_JACMOD_CYLINDRICAL_SHELL, axis=3, **args)
+    else:
+        set_jm(femg, t[0], femg.FG_JACMOD_POLAR_SHELL, exponent=-1, **args)
+    with pytest.raises(femg.FgError) as err:
+        prob.plan().assemble("fp64", terms=(t, nt))
+    assert err.value.status == femg.FG_ERR_ARG

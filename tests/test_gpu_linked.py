@@ -19,7 +19,7 @@ def rel(a, b):
 
 
 class LinkedPlan:
-    def __init__(self, femg, prob, b):
+    def __init__(self, femg, prob, b, upper=0):
         self.keep = []
 
         def arr(x, dt):
@@ -32,7 +32,7 @@ class LinkedPlan:
         lr, lv = arr(b["linked_row"], np.uint64), arr(b["linked_value"], np.complex128)
         U64, I32, F64 = C.POINTER(C.c_uint64), C.POINTER(C.c_int32), C.POINTER(C.c_double)
         self.sys = femg.SystemDesc(int(b["n_rows"]), ai.ctypes.data_as(U64), aj.ctypes.data_as(U64), ed.ctypes.data_as(U64),
-                                   et.ctypes.data_as(I32), prob.sys.n_fixed, 0, len(lr), lr.ctypes.data_as(U64),
+                                   et.ctypes.data_as(I32), prob.sys.n_fixed, upper, len(lr), lr.ctypes.data_as(U64),
                                    lv.ctypes.data_as(F64))
         self.ptr = C.c_void_p()
         self.L = femg.lib()
@@ -93,4 +93,19 @@ def test_linked_plans_are_declined_where_unsupported(femg, oracle, cuda):
     plans = (C.c_void_p * 1)(plan.ptr)
     out = C.c_void_p()
     assert L.fg_batch_create(plans, None, None, 1, 0, C.byref(out)) == femg.FG_ERR_UNSUPPORTED
+    plan.close()
+
+
+def test_linked_with_upper_storage(femg, oracle, cuda):
+    prob, b, _ = linked_pattern(femg, oracle, "tri_p2_dirichlet", 0.7)
+    bu = dict(b, upper=1)
+    ai, aj = oracle.pattern(bu["edof"], bu["etype"], bu["n_rows"], upper=True, linked_row=bu["linked_row"])
+    bu.update(ai=ai, aj=aj)
+    t, nt = prob.terms()
+    ref_v, ref_b = oracle.assemble(bu, t, nt)
+    plan = LinkedPlan(femg, prob, bu, upper=1)
+    v, r = plan.assemble("fp64", (t, nt))
+    assert rel(v, ref_v) <= 1e-12 and rel(r, ref_b) <= 1e-12
+    gai, gaj = femg.pattern_build(bu["edof"], bu["etype"], bu["n_rows"], upper=True, linked_row=bu["linked_row"])
+    assert np.array_equal(gai, ai) and np.array_equal(gaj, aj)
     plan.close()

@@ -107,3 +107,20 @@ def test_linked_values_are_the_reduced_system(femg, oracle, name, phi):
     scale = np.abs(vf).max()
     assert abs(Al - Ar).max() <= 1e-13 * scale
     assert np.abs(bl - P.conj().T @ bf).max() <= 1e-13 * max(np.abs(bf).max(), 1.0)
+
+
+def test_linked_with_upper_storage(femg, oracle):
+    """Symmetric storage on a linked system: rows and columns map to the
+    masters first, then the entries left of the diagonal drop (MatrixFactory.cpp:
+    265, 491); the result is the upper triangle of the linked system's values."""
+    prob, b, P = linked_pattern(femg, oracle, "tri_p1", 0.0)
+    t, nt = prob.terms()
+    vl, _ = oracle.assemble(b, t, nt)
+    bu = dict(b, upper=1)
+    ai, aj = oracle.pattern(bu["edof"], bu["etype"], bu["n_rows"], upper=True, linked_row=bu["linked_row"])
+    bu.update(ai=ai, aj=aj)
+    vu, _ = oracle.assemble(bu, t, nt)
+    rows = np.repeat(np.arange(len(b["ai"]) - 1), np.diff(b["ai"].astype(np.int64)))
+    keep = b["aj"].astype(np.int64) >= rows
+    assert np.array_equal(aj, b["aj"][keep])
+    assert np.allclose(vu, vl[keep], rtol=0, atol=1e-13 * np.abs(vl).max())
