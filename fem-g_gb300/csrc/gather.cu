@@ -200,8 +200,10 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
   const int sms = smCount();
   int64_t blocks = (v1 - v0 + rowsPerBlock - 1) / rowsPerBlock;
   blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)sms * 16));
+  bool launched = false;
 #define FG_GATHER_L(LL, JJ)                                                                                       \
   if (L == LL && J == JJ) {                                                                                       \
+    launched = true;                                                                                              \
     auto kern = k_gather<SlotT, KCPLX, KT, AT, LL, JJ>;                                                           \
     static size_t smemSet = 0;                                                                                    \
     if (smem > smemSet) {                                                                                         \
@@ -217,6 +219,10 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
   FG_GATHER_L(16, 3)
   FG_GATHER_L(32, 3)
 #undef FG_GATHER_L
+  if (!launched) {
+    setLastError("gather: no kernel for this (lanes, columns) shape");
+    return FG_ERR_UNSUPPORTED;
+  }
   FG_CUDA(cudaGetLastError());
   return FG_OK;
 }

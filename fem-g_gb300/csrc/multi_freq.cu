@@ -207,8 +207,10 @@ static int launchMultiTyped(const PlanDev &p, const MultiIn &in, cudaStream_t s)
   const int rowsPerBlock = wpb * R;
   int64_t blocks = ((int64_t)p.nRows + rowsPerBlock - 1) / rowsPerBlock;
   blocks = std::min<int64_t>(blocks, (int64_t)smCount() * 16);
+  bool launched = false;
 #define FG_MULTI_L(LL, JJ)                                                                         \
   if (L == LL && J == JJ) {                                                                        \
+    launched = true;                                                                               \
     auto kern = k_gather_multi<SlotT, KT, LL, JJ>;                                                 \
     static size_t smemSet = 0;                                                                     \
     if (smem > smemSet) {                                                                          \
@@ -224,6 +226,10 @@ static int launchMultiTyped(const PlanDev &p, const MultiIn &in, cudaStream_t s)
   FG_MULTI_L(16, 3)
   FG_MULTI_L(32, 3)
 #undef FG_MULTI_L
+  if (!launched) {
+    setLastError("multi-frequency gather: no kernel for this (lanes, columns) shape");
+    return FG_ERR_UNSUPPORTED;
+  }
   FG_CUDA(cudaGetLastError());
   return FG_OK;
 }
