@@ -22,6 +22,9 @@
 #include <cstring>
 #include <numeric>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "common.cuh"
 
 namespace femg {
@@ -51,6 +54,7 @@ struct MixedState {
   int32_t *ctaStart = nullptr;  // contiguous tile ranges of the persistent CTAs
   int nCta = 0;
   int ctasPerSm = 1;            // contraction CTAs per SM (TMEM columns 512 / ctasPerSm each)
+  alignas(64) CUtensorMap aMap;  // TMA view of A: [rows][k3] floats, box 4 x 128
   int mmaN = 256;               // N of one MMA instruction
   void *probDev = nullptr;      // this plan's GemmProblem on the device
   float *ke = nullptr;       // [E][groups][ncomp][n][n] fp32
@@ -184,6 +188,18 @@ __device__ inline bool mbarWait(uint64_t *mbar, uint32_t parity) {
     if (clock64() - t0 > kWaitCycles) return false;
   return true;
 }
+// TMA: the arrival that announces `bytes` of transaction on the barrier,
+// and a 2D tiled load of box {4 floats, 128 rows} at (x, y) completing on it
+__device__ inline void mbarExpectTx(uint64_t *mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(mbar)), "r"(bytes) : "memory");
+}
+__device__ inline void tmaLoad2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint64_t *mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smemAddr(mbar))
+      : "memory");
+}
+
 __device__ inline void tmemLoad16(uint32_t taddr, float *v) {
   uint32_t r[16];
   asm volatile(
@@ -450,10 +466,12 @@ __global__ void k_factors_batch(const FactorJob *__restrict__ jobs, int nJobs, i
 // Tiles of one launch: tile t = (problem, orientation, first row, rows);
 // CTA b takes the contiguous tiles [ctaStart[b], ctaStart[b + 1]).
 struct GemmSched {
+  CUtensorMap aMap;  // one problem: its factor rows [rows][K3] as a TMA tensor (box 4 x 128)
   const GemmProblem *probs;
   const int4 *tiles;
   const int32_t *ctaStart;
   int *err;
+  int tma;           // A tiles by TMA through aMap (one problem), else by cp.async
 };
 
 __device__ inline void cpAsync16(uint32_t dst, const void *src, uint32_t srcBytes) {
@@ -474,6 +492,20 @@ __device__ inline void loadATile(const GemmProblem &g, uint32_t As, int row0, in
     cpAsync16(As + kc * 2048 + (r >> 3) * 128 + (r & 7) * 16, src, live ? 16u : 0u);
   }
   cpAsyncCommit();
+}
+
+// The A tile of rows [row0, row0 + nrows) into As: by TMA (one thread; the
+// whole 128-row box, rows past the array read as zero) completing on `bar`,
+// or by cp.async from every thread.
+__device__ inline void issueATile(const GemmSched &sc, const GemmProblem &g, float *As, int row0, int nrows, int tid, uint64_t *bar) {
+  if (sc.tma) {
+    if (tid == 0) {
+      mbarExpectTx(bar, (uint32_t)(kBM * g.K3 * 4));
+      for (int kc = 0; kc < g.K3 / 4; ++kc) tmaLoad2d(smemAddr(As) + kc * 2048, &sc.aMap, 4 * kc, row0, bar);
+    }
+  } else {
+    loadATile(g, smemAddr(As), row0, nrows, tid);
+  }
 }
 
 __device__ inline void loadB(const GemmProblem &g, float *Bs, int o, int tid) {
@@ -557,14 +589,16 @@ __device__ inline void drainColumns(const GemmProblem &g, uint32_t tmemRow, floa
 // column chunks of 512. The next tile's A is fetched with cp.async while the
 // current tile computes and drains when both share the B image in shared
 // memory; B is reloaded when the (problem, orientation) changes.
-__global__ void __launch_bounds__(kThreadsGemm, 2) k_contract_tf32x3(const GemmSched sc, int maxK3, int tmemCols) {
+__global__ void __launch_bounds__(kThreadsGemm, 2)
+    k_contract_tf32x3(const __grid_constant__ GemmSched sc, int maxK3, int tmemCols) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ GemmProblem gs;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem);
-  uint32_t *tmemBase = reinterpret_cast<uint32_t *>(smem + 8);
-  float *Stage = reinterpret_cast<float *>(smem + 16);                 // 8 warps x 32 x 36 floats
-  float *As0 = Stage + 8 * 32 * 36;                                    // 2 x kBM * maxK3
-  float *Bs = As0 + 2 * kBM * maxK3;                                   // Npad * K3
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem);      // MMA completion
+  uint64_t *aBar = reinterpret_cast<uint64_t *>(smem + 8);  // [2] TMA loads of the A buffers
+  uint32_t *tmemBase = reinterpret_cast<uint32_t *>(smem + 24);
+  float *Stage = reinterpret_cast<float *>(smem + 128);     // 8 warps x 32 x 36 floats
+  float *As0 = Stage + 8 * 32 * 36;                         // 2 x kBM * maxK3, 128-byte aligned (TMA)
+  float *Bs = As0 + 2 * kBM * maxK3;                        // Npad * K3
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quad = warp & 3, half = warp >> 2;
 
@@ -574,6 +608,8 @@ __global__ void __launch_bounds__(kThreadsGemm, 2) k_contract_tf32x3(const GemmS
   }
   if (tid == 0) {
     mbarInit(mbar, 1);
+    mbarInit(&aBar[0], 1);
+    mbarInit(&aBar[1], 1);
     fenceMbarInit();
   }
   tcFenceBefore();
@@ -582,6 +618,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 2) k_contract_tf32x3(const GemmS
   const uint32_t tmem = *tmemBase;
   const uint32_t bBase = smemAddr(Bs);
   uint32_t phase = 0;
+  uint32_t aParity = 0, aPending = 0;  // per A buffer: completion parity, load in flight
   bool failed = false;
   const int t0 = sc.ctaStart[blockIdx.x], t1 = sc.ctaStart[blockIdx.x + 1];
   if (t0 < t1) {
@@ -589,7 +626,8 @@ __global__ void __launch_bounds__(kThreadsGemm, 2) k_contract_tf32x3(const GemmS
     if (tid == 0) gs = sc.probs[T.x];
     __syncthreads();
     loadB(gs, Bs, T.y, tid);
-    loadATile(gs, smemAddr(As0), T.z, T.w, tid);
+    issueATile(sc, gs, As0, T.z, T.w, tid, &aBar[0]);
+    aPending |= 1u;
   }
   for (int t = t0, it = 0; t < t1 && !failed; ++t, ++it) {
     const int buf = it & 1;
@@ -597,8 +635,19 @@ __global__ void __launch_bounds__(kThreadsGemm, 2) k_contract_tf32x3(const GemmS
     const int o = T.y, row0 = T.z, nrows = T.w;
     const uint32_t aAddr = smemAddr(As0 + buf * kBM * gs.K3);
     const uint32_t bLbo = (uint32_t)gs.Npad * 16u;  // K-adjacent core matrices of B
-    cpAsyncWaitAll();
-    fenceProxyAsync();
+    if (sc.tma) {
+      const bool okA = mbarWait(&aBar[buf], (aParity >> buf) & 1u);
+      if (__syncthreads_or(okA ? 0 : 1)) {
+        if (tid == 0) atomicExch(sc.err, 1);
+        failed = true;
+        break;
+      }
+      aParity ^= 1u << buf;
+      aPending &= ~(1u << buf);
+    } else {
+      cpAsyncWaitAll();
+    }
+    fenceProxyAsync();  // the B image (generic stores) before the MMAs read it
     __syncthreads();
     // prefetch the next tile's A when it shares this B image
     const int tn = t + 1;
@@ -627,7 +676,10 @@ __global__ void __launch_bounds__(kThreadsGemm, 2) k_contract_tf32x3(const GemmS
         }
         mmaCommit(mbar);
       }
-      if (n0 == 0 && nextSameB) loadATile(gs, smemAddr(As0 + (buf ^ 1) * kBM * gs.K3), Tn.z, Tn.w, tid);
+      if (n0 == 0 && nextSameB) {
+        issueATile(sc, gs, As0 + (buf ^ 1) * kBM * gs.K3, Tn.z, Tn.w, tid, &aBar[buf ^ 1]);
+        aPending |= 1u << (buf ^ 1);
+      }
       __syncwarp();
       const bool ok = mbarWait(mbar, phase);
       failed = __syncthreads_or(ok ? 0 : 1) != 0;  // block-uniform
@@ -650,14 +702,18 @@ __global__ void __launch_bounds__(kThreadsGemm, 2) k_contract_tf32x3(const GemmS
       if (tid == 0 && Tn.x != T.x) gs = sc.probs[Tn.x];
       __syncthreads();
       loadB(gs, Bs, Tn.y, tid);
-      loadATile(gs, smemAddr(As0 + (buf ^ 1) * kBM * gs.K3), Tn.z, Tn.w, tid);
+      issueATile(sc, gs, As0 + (buf ^ 1) * kBM * gs.K3, Tn.z, Tn.w, tid, &aBar[buf ^ 1]);
+      aPending |= 1u << (buf ^ 1);
     }
   }
   cpAsyncWaitAll();
   if (failed) {
     // give the in-flight MMA chain a second bounded chance to retire (same
-    // completion parity) before the TMEM is freed
+    // completion parity) before the TMEM is freed, and the TMA loads in
+    // flight one before the shared memory is released
     mbarWait(mbar, phase);
+    for (int b = 0; b < 2; ++b)
+      if (aPending & (1u << b)) mbarWait(&aBar[b], (aParity >> b) & 1u);
   }
   __syncthreads();
   tcFenceAfter();
@@ -829,7 +885,38 @@ static void buildB(const PlanDev &p, const std::vector<double> &w, const std::ve
     }
 }
 
-static size_t gemmSmemNeed(int Npad, int k3) { return 16 + 8 * 32 * 36 * 4 + 2 * (size_t)kBM * k3 * 4 + (size_t)Npad * k3 * 4; }
+static size_t gemmSmemNeed(int Npad, int k3) { return 128 + 8 * 32 * 36 * 4 + 2 * (size_t)kBM * k3 * 4 + (size_t)Npad * k3 * 4; }
+// TMA tensor map of the factor rows A [rows][k3] (floats, 16-byte rows
+// pieces): box {4 floats, 128 rows}, no swizzle, zero fill past the rows,
+// so one box lands at As + kc * 2048 with row r at 16 r, the K-major
+// core-matrix layout of the MMA descriptors.
+static int encodeRowsMap(CUtensorMap *map, const float *A, int k3, int64_t rows) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      cudaGetLastError();
+      setLastError("mixed path: cuTensorMapEncodeTiled not available");
+      return FG_ERR_CUDA;
+    }
+    encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)k3, (cuuint64_t)std::max<int64_t>(rows, 1)};
+  const cuuint64_t strides[1] = {(cuuint64_t)k3 * 4};
+  const cuuint32_t box[2] = {4, (cuuint32_t)kBM};
+  const cuuint32_t elemStrides[2] = {1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(A), dims, strides, box, elemStrides,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    setLastError("mixed path: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return FG_ERR_CUDA;
+  }
+  return FG_OK;
+}
+
 int gemmCtasPerSm(int Npad, int k3) { return gemmSmemNeed(Npad, k3) <= 110 * 1024 ? 2 : 1; }
 size_t gemmSmem(int Npad, int k3, int ctasPerSm) {
   // one CTA per SM takes at least half the SM's shared memory and all 512
@@ -856,13 +943,18 @@ std::vector<int32_t> partitionTiles(const std::vector<double> &cost, int nCta) {
 
 // One contraction launch over the tiles of one or many problems
 int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ctaStartDev, int nCta, int *err, int maxK3,
-                   size_t smem, cudaStream_t s, int tmemCols) {
+                   size_t smem, cudaStream_t s, int tmemCols, const void *aMap) {
   static size_t smemSet = 0;
   if (smem > smemSet) {
     FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     smemSet = smem;
   }
   GemmSched sc;
+  std::memset(&sc, 0, sizeof(sc));
+  if (aMap) {
+    std::memcpy(&sc.aMap, aMap, sizeof(CUtensorMap));
+    sc.tma = 1;
+  }
   sc.probs = (const GemmProblem *)probsDev;
   sc.tiles = tilesDev;
   sc.ctaStart = ctaStartDev;
@@ -987,6 +1079,7 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
   m->rows = p.E * rowsPerElem;
   int st = ensureDevice((void **)&m->A, &m->Abytes, (size_t)m->rows * m->k3 * 4);
   if (st) return st;
+  if ((st = encodeRowsMap(&m->aMap, m->A, m->k3, m->rows))) return st;
   st = ensureDevice((void **)&m->ke, &m->keBytes, (size_t)m->rows * m->nn2 * 4);
   if (st) return st;
   m->ncomp = ncomp;
@@ -1017,7 +1110,7 @@ int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups,
   }
   if (m->nTiles == 0) return FG_OK;
   return launchContract(m->probDev, m->tiles, m->ctaStart, m->nCta, m->err, m->k3, gemmSmem(m->Npad, m->k3, m->ctasPerSm), s,
-                        512 / m->ctasPerSm);
+                        512 / m->ctasPerSm, &m->aMap);
 }
 
 int launchFactorsBatch(const FactorJob *jobsDev, int nJobs, int64_t total, cudaStream_t s) {

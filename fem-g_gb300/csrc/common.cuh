@@ -249,7 +249,7 @@ int gemmCtasPerSm(int Npad, int k3);
 size_t gemmSmem(int Npad, int k3, int ctasPerSm = 1);
 std::vector<int32_t> partitionTiles(const std::vector<double> &cost, int nCta);
 int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ctaStartDev, int nCta, int *err, int maxK3,
-                   size_t smem, cudaStream_t s, int tmemCols = 512);
+                   size_t smem, cudaStream_t s, int tmemCols = 512, const void *aMap = nullptr);
 GemmProblem mixedGemmProblem(fg_plan *plan);
 
 // ------------------------------------------------------------- device helpers
