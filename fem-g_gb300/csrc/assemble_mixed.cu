@@ -200,6 +200,14 @@ __device__ inline void tmaLoad2d(uint32_t dst, const CUtensorMap *map, int x, in
       : "memory");
 }
 
+// TMA bulk copy (no tensor map) of `bytes` (a multiple of 16, both
+// addresses 16-byte aligned) completing on the barrier
+__device__ inline void bulkLoad(uint32_t dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smemAddr(mbar))
+               : "memory");
+}
+
 __device__ inline void tmemLoad16(uint32_t taddr, float *v) {
   uint32_t r[16];
   asm volatile(
@@ -508,10 +516,14 @@ __device__ inline void issueATile(const GemmSched &sc, const GemmProblem &g, flo
   }
 }
 
-__device__ inline void loadB(const GemmProblem &g, float *Bs, int o, int tid) {
-  const float4 *src = reinterpret_cast<const float4 *>(g.B + (size_t)o * g.Npad * g.K3);
-  float4 *dst = reinterpret_cast<float4 *>(Bs);
-  for (int k = tid; k < g.Npad * g.K3 / 4; k += kThreadsGemm) dst[k] = src[k];
+// The B image of orientation o (Npad x K3 floats, core-matrix layout) by
+// one TMA bulk copy completing on `bar`.
+__device__ inline void loadB(const GemmProblem &g, float *Bs, int o, int tid, uint64_t *bar) {
+  if (tid == 0) {
+    const uint32_t bytes = (uint32_t)g.Npad * (uint32_t)g.K3 * 4u;
+    mbarExpectTx(bar, bytes);
+    bulkLoad(smemAddr(Bs), g.B + (size_t)o * g.Npad * g.K3, bytes, bar);
+  }
 }
 
 // drain TMEM columns [c0, c1) of this warp's 32 lanes into the element rows
@@ -595,7 +607,8 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
   __shared__ GemmProblem gs;
   uint64_t *mbar = reinterpret_cast<uint64_t *>(smem);      // MMA completion
   uint64_t *aBar = reinterpret_cast<uint64_t *>(smem + 8);  // [2] TMA loads of the A buffers
-  uint32_t *tmemBase = reinterpret_cast<uint32_t *>(smem + 24);
+  uint64_t *bBar = reinterpret_cast<uint64_t *>(smem + 24); // TMA load of the B image
+  uint32_t *tmemBase = reinterpret_cast<uint32_t *>(smem + 32);
   float *Stage = reinterpret_cast<float *>(smem + 128);     // 8 warps x 32 x 36 floats
   float *As0 = Stage + 8 * 32 * 36;                         // 2 x kBM * maxK3, 128-byte aligned (TMA)
   float *Bs = As0 + 2 * kBM * maxK3;                        // Npad * K3
@@ -610,6 +623,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
     mbarInit(mbar, 1);
     mbarInit(&aBar[0], 1);
     mbarInit(&aBar[1], 1);
+    mbarInit(bBar, 1);
     fenceMbarInit();
   }
   tcFenceBefore();
@@ -619,13 +633,15 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
   const uint32_t bBase = smemAddr(Bs);
   uint32_t phase = 0;
   uint32_t aParity = 0, aPending = 0;  // per A buffer: completion parity, load in flight
+  uint32_t bParity = 0, bPending = 0;  // the B image: completion parity, load in flight
   bool failed = false;
   const int t0 = sc.ctaStart[blockIdx.x], t1 = sc.ctaStart[blockIdx.x + 1];
   if (t0 < t1) {
     const int4 T = sc.tiles[t0];
     if (tid == 0) gs = sc.probs[T.x];
     __syncthreads();
-    loadB(gs, Bs, T.y, tid);
+    loadB(gs, Bs, T.y, tid, bBar);
+    bPending = 1;
     issueATile(sc, gs, As0, T.z, T.w, tid, &aBar[0]);
     aPending |= 1u;
   }
@@ -647,7 +663,17 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
     } else {
       cpAsyncWaitAll();
     }
-    fenceProxyAsync();  // the B image (generic stores) before the MMAs read it
+    if (bPending) {
+      const bool okB = mbarWait(bBar, bParity);
+      if (__syncthreads_or(okB ? 0 : 1)) {
+        if (tid == 0) atomicExch(sc.err, 1);
+        failed = true;
+        break;
+      }
+      bParity ^= 1u;
+      bPending = 0;
+    }
+    fenceProxyAsync();  // cp.async A tiles (generic proxy) before the MMAs read them
     __syncthreads();
     // prefetch the next tile's A when it shares this B image
     const int tn = t + 1;
@@ -701,7 +727,8 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
       // problem or orientation change: the MMAs are done with Bs, reload it and the next A
       if (tid == 0 && Tn.x != T.x) gs = sc.probs[Tn.x];
       __syncthreads();
-      loadB(gs, Bs, Tn.y, tid);
+      loadB(gs, Bs, Tn.y, tid, bBar);
+      bPending = 1;
       issueATile(sc, gs, As0 + (buf ^ 1) * kBM * gs.K3, Tn.z, Tn.w, tid, &aBar[buf ^ 1]);
       aPending |= 1u << (buf ^ 1);
     }
@@ -714,6 +741,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
     mbarWait(mbar, phase);
     for (int b = 0; b < 2; ++b)
       if (aPending & (1u << b)) mbarWait(&aBar[b], (aParity >> b) & 1u);
+    if (bPending) mbarWait(bBar, bParity);
   }
   __syncthreads();
   tcFenceAfter();
