@@ -525,7 +525,10 @@ static int validateExpr(const fg_expr &ex) {
   return depth == 1 ? 0 : 1;
 }
 
-static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complexOut, std::vector<void *> &arrays) {
+// arrays: the device copies of per-element coefficient arrays ([E] complex
+// each); the first `used` are this upload's, later ones are reused from the
+// previous upload (same size) instead of freed and allocated again.
+static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complexOut, std::vector<void *> &arrays, size_t &used) {
   if (validateExpr(ex)) {
     setLastError("invalid coefficient expression");
     return FG_ERR_ARG;
@@ -555,11 +558,16 @@ static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complex
         break;
       }
     void *p = nullptr;
-    if (cudaMalloc(&p, bytes) != cudaSuccess) {
-      setLastError("coefficient upload: out of device memory");
-      return FG_ERR_OOM;
+    if (used < arrays.size()) {
+      p = arrays[used];
+    } else {
+      if (cudaMalloc(&p, bytes) != cudaSuccess) {
+        setLastError("coefficient upload: out of device memory");
+        return FG_ERR_OOM;
+      }
+      arrays.push_back(p);
     }
-    arrays.push_back(p);
+    ++used;
     if (cudaMemcpy(p, ex.elem_values[a], bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
       setLastError("coefficient upload failed");
       return FG_ERR_CUDA;
@@ -571,8 +579,21 @@ static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complex
 
 int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double frequency, DevTerms *out,
                 std::vector<void *> &arrays) {
-  for (void *p : arrays) cudaFree(p);
-  arrays.clear();
+  // kernels of an earlier call may still read the arrays about to be
+  // overwritten (the device-wide wait that freeing them used to imply)
+  if (!arrays.empty() && cudaDeviceSynchronize() != cudaSuccess) {
+    setLastError(std::string("coefficient upload: ") + cudaGetErrorString(cudaGetLastError()));
+    return FG_ERR_CUDA;
+  }
+  size_t used = 0;
+  struct Trim {  // on every return: free the arrays this upload did not use
+    std::vector<void *> &a;
+    size_t &u;
+    ~Trim() {
+      for (size_t k = u; k < a.size(); ++k) cudaFree(a[k]);
+      a.resize(std::min(u, a.size()));
+    }
+  } trim{arrays, used};
   std::memset(out, 0, sizeof(*out));
   if (nTerms <= 0 || nTerms > kMaxTerms || !terms) {
     setLastError("term count must be in [1, 6]");
@@ -615,10 +636,10 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
       return FG_ERR_ARG;
     }
     bool sourceComplex = false;  // the right-hand side is always complex
-    int st = devExpr(plan, src.coef, &dt.coef, src.kind == FG_TERM_SOURCE ? &sourceComplex : &cplx, arrays);
+    int st = devExpr(plan, src.coef, &dt.coef, src.kind == FG_TERM_SOURCE ? &sourceComplex : &cplx, arrays, used);
     if (st) return st;
     if (src.kind == FG_TERM_ELASTIC) {
-      st = devExpr(plan, src.coef2, &dt.coef2, &cplx, arrays);
+      st = devExpr(plan, src.coef2, &dt.coef2, &cplx, arrays, used);
       if (st) return st;
       out->hasElastic = 1;
     }
