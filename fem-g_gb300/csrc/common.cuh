@@ -101,7 +101,6 @@ struct PlanDev {
   const uint64_t *ai;     // [nRows+1]
   const uint64_t *rowPtr; // [nRows+1] into rowElem
   const uint32_t *rowElem;// (e << 6) | i : element and local test index
-  const uint32_t *rowOrder;// rows sorted by their number of contributing element rows
   const uint4 *visit;      // per visited row: row, CSR start, element-list start, len | count << 16
   const uint32_t *visitElem;// element lists in visiting order
   const void *slot;       // [E][n][slotLd] uint8 or uint16 position in the row

@@ -420,7 +420,6 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   if ((st = upload(plan, sys->ai, (size_t)sys->n_rows + 1, &d.ai))) return st;
   if ((st = upload(plan, rowPtr.data(), rowPtr.size(), &d.rowPtr))) return st;
   if ((st = upload(plan, rowElem.data(), rowElem.size(), &d.rowElem))) return st;
-  if ((st = upload(plan, rowOrder.data(), rowOrder.size(), &d.rowOrder))) return st;
   if ((st = upload(plan, visit.data(), visit.size(), &d.visit))) return st;
   if ((st = upload(plan, visitElem.data(), visitElem.size(), &d.visitElem))) return st;
   plan->visitRanged = d.visit;
