@@ -9,8 +9,12 @@
 // and accumulates Ke += w det (c L)^T conj(R) (BilinearTerm::evaluate,
 // src/term/BilinearTerm.cpp:314-326) with the AFrequency factors
 // (src/term/Assembler.cpp:283-295), and b_e += w det conj(phi) f
-// (LinearTerm::evaluate, src/term/LinearTerm.cpp:182-191). Ke is symmetric
-// for these terms, so each lane owns upper-triangle entries.
+// (LinearTerm::evaluate, src/term/LinearTerm.cpp:182-191). The tensor
+// grad-grad term (a TensorFunction times grad(dof), the left-order evaluator
+// src/term/evaluator/EquationEvaluator.h:134-173 with a degree-2 function)
+// maps the unknown's gradients by w det c D before the product; D is
+// symmetric here. Ke is symmetric for these terms, so each lane owns
+// upper-triangle entries.
 //
 // The element matrices and vectors then go through the deterministic CSR
 // reduction of gather.cu.
@@ -25,6 +29,7 @@ struct ElemWarpSmem {
   double J0[9], J[9], Jinv[9];
   double det0, det;
   double2 a, b, s;  // w det c_gradgrad, w det c_mass, w det f
+  double2 Aw[6];    // w det times the diffusion tensor (tensor grad-grad term)
   double G[3][kMaxDofs];
   double phi[kMaxDofs];
   double Gs[2][3][kMaxDofs];
@@ -84,18 +89,38 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         S.a = make_double2(wd * cgg.x, wd * cgg.y);
         S.b = make_double2(wd * cm.x, wd * cm.y);
         S.s = make_double2(wd * f.x, wd * f.y);
+        if (terms->tensorTerm >= 0) {
+          double2 A[6];
+          diffusionTensor(terms, g, e, xq, cgg, A);
+          for (int k = 0; k < 6; ++k) S.Aw[k] = make_double2(wd * A[k].x, wd * A[k].y);
+        }
       }
       __syncwarp();
       const size_t base = ((size_t)o * p.nq + q) * p.nb;
+      const bool tensor = terms->tensorTerm >= 0;
       for (int i = lane; i < n; i += 32) {
         const double g0 = p.bgrad[3 * (base + i)], g1 = p.bgrad[3 * (base + i) + 1], g2 = p.bgrad[3 * (base + i) + 2];
         const double ph = p.bval[base + i];
+        double G[3];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-          const double G = S.Jinv[r] * g0 + S.Jinv[3 + r] * g1 + S.Jinv[6 + r] * g2;
-          S.G[r][i] = G;
-          S.Gs[0][r][i] = S.a.x * G;
-          if (CPLX) S.Gs[1][r][i] = S.a.y * G;
+          G[r] = S.Jinv[r] * g0 + S.Jinv[3 + r] * g1 + S.Jinv[6 + r] * g2;
+          S.G[r][i] = G[r];
+        }
+        if (tensor) {
+          // (w det A) G with A symmetric: rows (00 01 02), (01 11 12), (02 12 22)
+          const int row[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            S.Gs[0][r][i] = S.Aw[row[r][0]].x * G[0] + S.Aw[row[r][1]].x * G[1] + S.Aw[row[r][2]].x * G[2];
+            if (CPLX) S.Gs[1][r][i] = S.Aw[row[r][0]].y * G[0] + S.Aw[row[r][1]].y * G[1] + S.Aw[row[r][2]].y * G[2];
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            S.Gs[0][r][i] = S.a.x * G[r];
+            if (CPLX) S.Gs[1][r][i] = S.a.y * G[r];
+          }
         }
         S.phi[i] = ph;
         S.phis[0][i] = S.b.x * ph;

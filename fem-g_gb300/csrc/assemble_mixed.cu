@@ -285,12 +285,32 @@ __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *
   }
   const double idet = 1.0 / det;
   const int64_t r0 = (int64_t)rankOf[e] * rowsPerElem + rowOff;
+  // tensor grad-grad term: det J^-1 A J^-T = C^T A C / det in place of c det K
+  const bool tensor = terms->tensorTerm >= 0;
+  double2 A6[6];
+  if (tensor) diffusionTensor(terms, 0, e, xc, cgg, A6);
   for (int comp = 0; comp < ncomp; ++comp) {
     const double g = (comp == 0 ? cgg.x : cgg.y) * idet;
     const double m = (comp == 0 ? cm.x : cm.y) * det;
     float hi[kKp], lo[kKp];
+    if (tensor) {
+      const int sym[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+      double CA[9];  // CA[3a + s] = sum_r C[3a + r] A(r, s)
+      for (int a = 0; a < 3; ++a)
+        for (int s2 = 0; s2 < 3; ++s2) {
+          double v = 0.0;
+          for (int r = 0; r < 3; ++r) v += C[3 * a + r] * (comp == 0 ? A6[sym[r][s2]].x : A6[sym[r][s2]].y);
+          CA[3 * a + s2] = v;
+        }
+      for (int k = 0; k < 6; ++k) {
+        const int a = ab[k][0], b = ab[k][1];
+        const double f = (CA[3 * a] * C[3 * b] + CA[3 * a + 1] * C[3 * b + 1] + CA[3 * a + 2] * C[3 * b + 2]) * idet;
+        splitTf32Dev(f, hi[k], lo[k]);
+      }
+    } else {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) splitTf32Dev(g * CC[k], hi[k], lo[k]);
+      for (int k = 0; k < 6; ++k) splitTf32Dev(g * CC[k], hi[k], lo[k]);
+    }
     splitTf32Dev(m, hi[6], lo[6]);
     hi[7] = lo[7] = 0.0f;
     // [hi | lo | hi] as 16-byte stores (rows are 96 bytes)
@@ -1229,7 +1249,7 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
   int st = resolveTerms(plan, terms, n_terms, frequency, &dt, &dterms, s);
   if (st) return st;
   for (int t = 0; t < dt.n; ++t)
-    if (dt.t[t].kind != FG_TERM_SOURCE && dt.t[t].coef.cls == kExprPoint) {
+    if ((dt.t[t].kind != FG_TERM_SOURCE && dt.t[t].coef.cls == kExprPoint) || dt.tensorPoint) {
       setLastError("mixed path: bilinear coefficients must be constant per element");
       return FG_ERR_UNSUPPORTED;
     }

@@ -411,7 +411,7 @@ extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const 
     if (b->source[q] && (st = ensureDevice((void **)&pl->be, &pl->beBytes, (size_t)pl->d.E * pl->d.n * 16))) return fail(st);
     if (b->mixed) {
       for (int t = 0; t < dt.n; ++t)
-        if (dt.t[t].kind != FG_TERM_SOURCE && dt.t[t].coef.cls == kExprPoint) {
+        if ((dt.t[t].kind != FG_TERM_SOURCE && dt.t[t].coef.cls == kExprPoint) || dt.tensorPoint) {
           setLastError("mixed path: bilinear coefficients must be constant per element");
           return fail(FG_ERR_UNSUPPORTED);
         }

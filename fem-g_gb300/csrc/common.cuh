@@ -77,8 +77,11 @@ struct DevTerms {
   int32_t hasElastic;
   int32_t nMod;        // distinct Jacobian modificators of the terms (>= 1; FG_JACMOD_NONE counts)
   int32_t hasJacMod;   // some term has a modificator other than FG_JACMOD_NONE
+  int32_t tensorTerm;  // index of the FG_TERM_GRAD_GRAD_TENSOR term (at most one), -1 when none
+  int32_t tensorPoint; // some entry of that tensor depends on the point
   DevTerm t[kMaxTerms];
   DevJacMod mods[kMaxTerms];
+  DevExpr tensor[6];   // entries (00, 11, 22, 01, 02, 12) of the symmetric tensor
 };
 
 // Device-resident data of one element bucket
@@ -320,6 +323,17 @@ __device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x
     }
   }
   return st[0];
+}
+
+// Diffusion tensor of the grad-grad terms of modificator group g at element e
+// and point x: A = cgg I + factor c D, with cgg the summed scalar grad-grad
+// coefficients and D the tensor term's entries (00, 11, 22, 01, 02, 12).
+__device__ inline void diffusionTensor(const DevTerms *terms, int g, int64_t e, const double *x, double2 cgg, double2 *A) {
+  for (int k = 0; k < 6; ++k) A[k] = k < 3 ? cgg : make_double2(0.0, 0.0);
+  const DevTerm &T = terms->t[terms->tensorTerm];
+  if (T.mod != g) return;
+  const double2 fc = cmul(T.factor, evalExpr(T.coef, e, x));
+  for (int k = 0; k < 6; ++k) A[k] = cadd(A[k], cmul(fc, evalExpr(terms->tensor[k], e, x)));
 }
 
 // Jacobian at a quadrature point from the geometric nodes, stored column-major

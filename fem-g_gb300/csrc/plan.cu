@@ -603,12 +603,13 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
   bool cplx = false;
   out->n = nTerms;
   out->nMod = 0;
+  out->tensorTerm = -1;
   for (int t = 0; t < nTerms; ++t) {
     const fg_term_desc &src = terms[t];
     DevTerm &dt = out->t[t];
     dt.kind = src.kind;
     dt.dt = src.dt;
-    if (src.kind < FG_TERM_GRAD_GRAD || src.kind > FG_TERM_SOURCE) {
+    if (src.kind < FG_TERM_GRAD_GRAD || src.kind > FG_TERM_GRAD_GRAD_TENSOR) {
       setLastError("unknown term kind");
       return FG_ERR_ARG;
     }
@@ -618,6 +619,10 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
     }
     if (plan->d.form == FG_FORM_1 && (src.kind == FG_TERM_ELASTIC || src.kind == FG_TERM_SOURCE)) {
       setLastError("HCurl fields take the curl-curl and mass terms");
+      return FG_ERR_UNSUPPORTED;
+    }
+    if (src.kind == FG_TERM_GRAD_GRAD_TENSOR && (plan->d.form != FG_FORM_0 || plan->d.mult != 1)) {
+      setLastError("the tensor grad-grad term needs a scalar H1 field");
       return FG_ERR_UNSUPPORTED;
     }
     if (src.kind != FG_TERM_ELASTIC && plan->d.mult != 1 && src.kind != FG_TERM_MASS) {
@@ -643,6 +648,18 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
       out->hasElastic = 1;
     }
     if (src.kind == FG_TERM_SOURCE) out->hasSource = 1;
+    if (src.kind == FG_TERM_GRAD_GRAD_TENSOR) {
+      if (out->tensorTerm >= 0 || !src.tensor) {
+        setLastError(src.tensor ? "at most one tensor grad-grad term per assembly" : "tensor grad-grad term without tensor");
+        return FG_ERR_ARG;
+      }
+      out->tensorTerm = t;
+      for (int k = 0; k < 6; ++k) {
+        st = devExpr(plan, src.tensor[k], &out->tensor[k], &cplx, arrays, used);
+        if (st) return st;
+        if (out->tensor[k].cls == kExprPoint) out->tensorPoint = 1;
+      }
+    }
     // the term's Jacobian modificator: terms with equal ones share a group
     const fg_jacmod &jm = src.jacmod;
     if (jm.kind < FG_JACMOD_NONE || jm.kind > FG_JACMOD_SPHERICAL_SHELL) {

@@ -15,10 +15,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libfemg.so")
 
 FG_OK, FG_ERR_ARG, FG_ERR_OOM, FG_ERR_CUDA, FG_ERR_INDEX, FG_ERR_TIMEOUT, FG_ERR_UNSUPPORTED, FG_ERR_NO_DEVICE = range(8)
-FG_TERM_GRAD_GRAD, FG_TERM_MASS, FG_TERM_ELASTIC, FG_TERM_SOURCE = range(4)
+FG_TERM_GRAD_GRAD, FG_TERM_MASS, FG_TERM_ELASTIC, FG_TERM_SOURCE, FG_TERM_GRAD_GRAD_TENSOR = range(5)
 FG_PROBLEM_HELMHOLTZ, FG_PROBLEM_NAVIER, FG_PROBLEM_MAXWELL = range(3)
 FG_SPACE_LAGRANGE, FG_SPACE_HIERARCHICAL_H1, FG_SPACE_HCURL = range(3)
 FG_FORM_0, FG_FORM_1 = range(2)
+FG_DT_NONE, FG_DT_1, FG_DT_2 = range(3)
 FG_JACMOD_NONE, FG_JACMOD_AXISYMMETRY, FG_JACMOD_AXISYMMETRY_SHELL, FG_JACMOD_POLAR_SHELL, FG_JACMOD_CYLINDRICAL_SHELL, \
     FG_JACMOD_SPHERICAL_SHELL = range(6)
 FG_FP64_QUADRATURE, FG_FP64_FACTORED = range(2)
@@ -72,7 +73,8 @@ class JacMod(C.Structure):
 
 
 class TermDesc(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("dt", C.c_int32), ("coef", Expr), ("coef2", Expr), ("jacmod", JacMod)]
+    _fields_ = [("kind", C.c_int32), ("dt", C.c_int32), ("coef", Expr), ("coef2", Expr), ("jacmod", JacMod),
+                ("tensor", C.POINTER(Expr))]
 
 
 class ErrReport(C.Structure):

@@ -351,6 +351,12 @@ Operand operator*(const Tensor4Isotropic &C, Operand o) {
   return o;
 }
 
+Operand operator*(const TensorFunction &D, Operand o) {
+  o.tensor2 = true;
+  o.D = D;
+  return o;
+}
+
 // ----------------------------------------------------------- Formulation
 
 void Formulation::integral(const Operand &unknown, const Operand &test, const Domain &d, const std::string &gauss) {
@@ -504,6 +510,7 @@ void Formulation::pre(const Mesh &m) {
 
   // ---- terms for the C ABI
   termDescs.clear();
+  tensorExprs.clear();
   for (auto &t : bterms_) {
     fg_term_desc d;
     std::memset(&d, 0, sizeof(d));
@@ -516,6 +523,13 @@ void Formulation::pre(const Mesh &m) {
       d.kind = FG_TERM_ELASTIC;
       d.coef = (t.unknown.coef * t.unknown.C.lambda).toExpr();
       d.coef2 = (t.unknown.coef * t.unknown.C.mu).toExpr();
+    } else if (t.unknown.tensor2) {
+      if (!t.unknown.grad) throw std::invalid_argument("a tensor function multiplies gradients");
+      const TensorFunction &D = t.unknown.D;
+      d.kind = FG_TERM_GRAD_GRAD_TENSOR;
+      d.coef = t.unknown.coef.toExpr();
+      tensorExprs.push_back({D.xx.toExpr(), D.yy.toExpr(), D.zz.toExpr(), D.xy.toExpr(), D.xz.toExpr(), D.yz.toExpr()});
+      d.tensor = tensorExprs.back().data();
     } else {
       d.kind = t.unknown.grad ? FG_TERM_GRAD_GRAD : FG_TERM_MASS;
       d.coef = t.unknown.coef.toExpr();

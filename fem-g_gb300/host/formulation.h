@@ -14,7 +14,9 @@
 // assemble() is the GPU drop-in: it runs through the C ABI of
 // include/fem_g_gb300.h (fg_plan_create + fg_assemble_fp64/mixed).
 #pragma once
+#include <array>
 #include <complex>
+#include <deque>
 #include <memory>
 #include <string>
 #include <vector>
@@ -94,6 +96,13 @@ struct Tensor4Isotropic {  // C_ijkl = lambda d_ij d_kl + mu (d_ik d_jl + d_il d
   Function lambda, mu;
 };
 
+// Symmetric 3x3 tensor of coefficient functions (the reference's
+// TensorFunction, src/function/TensorFunction.h, restricted to symmetric D)
+struct TensorFunction {
+  Function xx = Function(1.0), yy = Function(1.0), zz = Function(1.0);
+  Function xy = Function(0.0), xz = Function(0.0), yz = Function(0.0);
+};
+
 class Field {
  public:
   Field(const std::string &name, const Domain &domain, SpaceType type, int order, int multiplicity, unsigned tag);
@@ -120,6 +129,8 @@ struct Operand {
   Function coef = Function(1.0);
   bool tensor4 = false;
   Tensor4Isotropic C;
+  bool tensor2 = false;  // D * grad(...) with a TensorFunction D
+  TensorFunction D;
 };
 Operand dof(Field &f);
 Operand tf(Field &f);
@@ -129,6 +140,7 @@ Operand grad(Operand o);
 Operand curl(Operand o);  // the derivative of an HCurl field
 Operand operator*(const Function &c, Operand o);
 Operand operator*(const Tensor4Isotropic &C, Operand o);
+Operand operator*(const TensorFunction &D, Operand o);
 
 class Formulation {
  public:
@@ -159,6 +171,7 @@ class Formulation {
   std::vector<int32_t> elemDofType;
   std::vector<double> dirichlet;          // [nFixed][2]
   std::vector<fg_term_desc> termDescs;    // C ABI terms
+  std::deque<std::array<fg_expr, 6>> tensorExprs;  // entries of the tensor terms' D (stable addresses)
   // reserve calls on the DOF dictionary: (DOFs created before the call, argument)
   std::vector<std::pair<uint64_t, uint64_t>> reserveLog;
   double preSeconds = 0.0;

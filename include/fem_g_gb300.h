@@ -161,7 +161,10 @@ enum {
   FG_TERM_GRAD_GRAD = 0, /* integral(c * grad(dof(u)), grad(tf(u))) */
   FG_TERM_MASS = 1,      /* integral(c * dof(u), tf(u)) */
   FG_TERM_ELASTIC = 2,   /* integral(C * grad(dof(u)), grad(tf(u))), C isotropic Tensor4 (lambda, mu) */
-  FG_TERM_SOURCE = 3     /* integral(f, tf(u)) : right-hand side */
+  FG_TERM_SOURCE = 3,    /* integral(f, tf(u)) : right-hand side */
+  FG_TERM_GRAD_GRAD_TENSOR = 4 /* integral(c * D * grad(dof(u)), grad(tf(u))), D a symmetric 3x3 tensor of
+                                  coefficient programs (TensorFunction * grad, EquationEvaluator tensor-left);
+                                  scalar H1 fields */
 };
 enum { FG_DT_NONE = 0, FG_DT_1 = 1, FG_DT_2 = 2 }; /* dof, dt_dof, dt2_dof */
 
@@ -197,6 +200,7 @@ typedef struct {
   fg_expr coef; /* c, f, or lambda for FG_TERM_ELASTIC */
   fg_expr coef2; /* mu for FG_TERM_ELASTIC */
   fg_jacmod jacmod; /* all zero: none */
+  const fg_expr *tensor; /* FG_TERM_GRAD_GRAD_TENSOR: [6] programs of D_xx, D_yy, D_zz, D_xy, D_xz, D_yz */
 } fg_term_desc;
 
 /* ------------------------------------------------------------- plan / run */

@@ -5,7 +5,8 @@
 // coverage tests of assembled systems (unitTests/coverage/posts.cpp:393-548:
 // a Hermitian left-hand side for real wavenumbers, consistent nonzero counts)
 // and its exact integrals of 1 over simple domains (:77-118), here as the
-// exact energies u^T A u of u = 1 and u = x.
+// exact energies u^T A u of u = 1 and u = x. A second formulation with a
+// TensorFunction coefficient checks the energies x_a^T A x_b = D_ab.
 //
 // Usage: formulation_test [--cpu]   (--cpu: pre() checks only, no GPU)
 // Exit status 0 when every check passes.
@@ -133,6 +134,49 @@ int main(int argc, char **argv) {
         rep.max_elem_rel_fro);
 
   fg_plan_destroy(plan);
+
+  // anisotropic medium: integral(D * grad(dof(v)), grad(tf(v))) with a
+  // constant symmetric TensorFunction D; for linear a, b in the span of the
+  // vertex functions, a^T A b = grad a . D grad b |cube|
+  Field v("v", omega, SpaceType::HierarchicalH1, 2, 1, 0);
+  Formulation aniso("anisotropic");
+  TensorFunction D;
+  D.xx = Function(2.0);
+  D.yy = Function(3.0);
+  D.zz = Function(4.0);
+  D.xy = Function(0.5);
+  D.xz = Function(0.25);
+  D.yz = Function(-0.5);
+  aniso.integral(D * grad(dof(v)), grad(tf(v)), omega, "Gauss4");
+  aniso.pre(mesh);
+  aniso.descs(&md, &rd, &sd, &sys);
+  st = fg_plan_create(&md, &rd, &sd, &sys, &plan);
+  CHECK(st == FG_OK, "fg_plan_create (anisotropic): %s", fg_last_error());
+  if (st == FG_OK) {
+    const uint64_t nnzA = aniso.ai.back();
+    std::vector<std::complex<double>> B64(nnzA), B32(nnzA);
+    const auto &at = aniso.termDescs;
+    st = fg_assemble_fp64(plan, at.data(), (int)at.size(), 0.0, nullptr, reinterpret_cast<double *>(B64.data()), nullptr, nullptr);
+    CHECK(st == FG_OK, "fg_assemble_fp64 (anisotropic): %s", fg_last_error());
+    st = fg_assemble_mixed(plan, at.data(), (int)at.size(), 0.0, nullptr, reinterpret_cast<double *>(B32.data()), nullptr, nullptr,
+                           nullptr);
+    CHECK(st == FG_OK, "fg_assemble_mixed (anisotropic): %s", fg_last_error());
+    std::vector<double> X[3];
+    for (int c = 0; c < 3; ++c) X[c].assign(aniso.nUnknown, 0.0);
+    for (const Dof &d : aniso.field->dofs.pool) {
+      if ((d.assembleType != 2 && d.assembleType != 3) || d.numType != 0) continue;
+      for (int c = 0; c < 3; ++c) X[c][d.numDof - 1] = mesh.xyz[3 * (d.entity - 1) + c];
+    }
+    const double Dm[3][3] = {{2.0, 0.5, 0.25}, {0.5, 3.0, -0.5}, {0.25, -0.5, 4.0}};
+    for (const auto *B : {&B64, &B32})
+      for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) {
+          const double e = quad(aniso, *B, X[a], X[c]), tol = B == &B64 ? 1e-11 : 1e-6;
+          CHECK(std::abs(e - Dm[a][c]) <= tol * 4.0, "x%d^T A x%d = %.15g, expected %g (%s)", a, c, e, Dm[a][c],
+                B == &B64 ? "FP64" : "mixed");
+        }
+    fg_plan_destroy(plan);
+  }
   std::printf("%s\n", failures ? "FAILED" : "OK");
   return failures ? 1 : 0;
 }
