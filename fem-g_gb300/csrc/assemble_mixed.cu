@@ -243,6 +243,7 @@ __device__ inline void tmemLoad32(uint32_t taddr, float *v) {
 // first quadrature point (affine elements: the geometric Jacobian is constant), per-element coefficients,
 // factors D_e split into TF32 hi/lo, written as row [hi | lo | hi] at the
 // element's rank in the orientation-sorted order.
+template <bool TENSOR>
 __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
                                               float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff, int64_t e) {
   double X[kMaxNodes * 3];
@@ -285,15 +286,16 @@ __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *
   }
   const double idet = 1.0 / det;
   const int64_t r0 = (int64_t)rankOf[e] * rowsPerElem + rowOff;
-  // tensor grad-grad term: det J^-1 A J^-T = C^T A C / det in place of c det K
-  const bool tensor = terms->tensorTerm >= 0;
+  // tensor grad-grad term (TENSOR: the terms have one; a separate
+  // instantiation keeps the scalar kernel's registers):
+  // det J^-1 A J^-T = C^T A C / det in place of c det K
   double2 A6[6];
-  if (tensor) diffusionTensor(terms, 0, e, xc, cgg, A6);
+  if (TENSOR) diffusionTensor(terms, 0, e, xc, cgg, A6);
   for (int comp = 0; comp < ncomp; ++comp) {
     const double g = (comp == 0 ? cgg.x : cgg.y) * idet;
     const double m = (comp == 0 ? cm.x : cm.y) * det;
     float hi[kKp], lo[kKp];
-    if (tensor) {
+    if (TENSOR) {
       const int sym[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
       double CA[9];  // CA[3a + s] = sum_r C[3a + r] A(r, s)
       for (int a = 0; a < 3; ++a)
@@ -324,10 +326,11 @@ __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *
   }
 }
 
+template <bool TENSOR>
 __global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf, float *__restrict__ A,
                           int ncomp, int rowsPerElem, int rowOff) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < p.E) factorsScalar(p, terms, rankOf, A, ncomp, rowsPerElem, rowOff, e);
+  if (e < p.E) factorsScalar<TENSOR>(p, terms, rankOf, A, ncomp, rowsPerElem, rowOff, e);
 }
 
 // Compound field with the isotropic Tensor4 term: for every component pair
@@ -486,7 +489,8 @@ __global__ void k_factors_batch(const FactorJob *__restrict__ jobs, int nJobs, i
   const int64_t e = g - J.elemStart;
   if (J.kind == 1) factorsElastic(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
   else if (J.kind == 2) factorsHcurl(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
-  else factorsScalar(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
+  else if (J.kind == 3) factorsScalar<true>(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
+  else factorsScalar<false>(J.p, J.terms, J.rankOf, J.A, J.ncomp, J.rowsPerElem, J.rowOff, e);
 }
 
 // --------------------------------------------------- tcgen05 contraction
@@ -1141,7 +1145,7 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
 // Factor rows of every term group (group g: rows g * ncomp * blocks onwards
 // within an element), then one tensor-core contraction over all of them into
 // m->ke ([E][groups][ncomp][n][n]).
-int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups, cudaStream_t s) {
+int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups, uint32_t tensorMask, cudaStream_t s) {
   MixedState *m = state(plan);
   const PlanDev &p = plan->d;
   const int ncomp = m->ncomp;
@@ -1152,7 +1156,9 @@ int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups,
       k_factors_hcurl<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms[gi], m->perm + p.E, m->A, ncomp, m->rowsPerElem, off);
     else if (m->blocks == 9)
       k_factors_elastic<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms[gi], m->perm + p.E, m->A, ncomp, m->rowsPerElem, off);
-    else k_factors<<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms[gi], m->perm + p.E, m->A, ncomp, m->rowsPerElem, off);
+    else if (tensorMask >> gi & 1)
+      k_factors<true><<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms[gi], m->perm + p.E, m->A, ncomp, m->rowsPerElem, off);
+    else k_factors<false><<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms[gi], m->perm + p.E, m->A, ncomp, m->rowsPerElem, off);
     countLaunch();
     FG_CUDA(cudaGetLastError());
   }
@@ -1171,7 +1177,7 @@ int launchFactorsBatch(const FactorJob *jobsDev, int nJobs, int64_t total, cudaS
 }
 
 // This plan's factor job (terms on the device, group 0)
-FactorJob mixedFactorJob(fg_plan *plan, const DevTerms *dterms, int64_t elemStart) {
+FactorJob mixedFactorJob(fg_plan *plan, const DevTerms *dterms, bool tensor, int64_t elemStart) {
   MixedState *m = state(plan);
   FactorJob j;
   std::memset(&j, 0, sizeof(j));
@@ -1182,7 +1188,7 @@ FactorJob mixedFactorJob(fg_plan *plan, const DevTerms *dterms, int64_t elemStar
   j.ncomp = m->ncomp;
   j.rowsPerElem = m->rowsPerElem;
   j.rowOff = 0;
-  j.kind = plan->d.form == FG_FORM_1 ? 2 : (m->blocks == 9 ? 1 : 0);
+  j.kind = plan->d.form == FG_FORM_1 ? 2 : (m->blocks == 9 ? 1 : (tensor ? 3 : 0));
   j.elemStart = elemStart;
   return j;
 }
@@ -1276,7 +1282,7 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
     FG_CUDA(cudaGetLastError());
   }
   if (p.E > 0)
-    if ((st = launchMixedElement(plan, &dterms, 1, s))) return st;
+    if ((st = launchMixedElement(plan, &dterms, 1, dt.tensorTerm >= 0 ? 1u : 0u, s))) return st;
   if ((st = gatherToOutputs(plan, (const double *)m->ke, dt.complexKe, 1, m->blocks, be, uD, o, csr_values, s))) return st;
   if (report) {
     // FP64 element matrices and CSR of the same terms, compared on the device

@@ -470,7 +470,7 @@ extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const 
     b->gemmHost.resize(n_problems);
     std::map<std::pair<int, int>, int> gcOf;
     for (int q = 0; q < n_problems; ++q) {
-      fj.push_back(mixedFactorJob(plans[q], b->termsDev[q], b->totalElems));
+      fj.push_back(mixedFactorJob(plans[q], b->termsDev[q], b->terms[q].tensorTerm >= 0, b->totalElems));
       b->totalElems += plans[q]->d.E;
       b->gemmHost[q] = mixedGemmProblem(plans[q]);
       const GemmProblem &g = b->gemmHost[q];

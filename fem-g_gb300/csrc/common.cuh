@@ -226,7 +226,7 @@ struct FactorJob {
   const DevTerms *terms;
   const int32_t *rankOf;
   float *A;
-  int32_t ncomp, rowsPerElem, rowOff, kind;  // kind: 0 scalar H1, 1 Tensor4 compound, 2 HCurl
+  int32_t ncomp, rowsPerElem, rowOff, kind;  // kind: 0 scalar H1, 1 Tensor4 compound, 2 HCurl, 3 scalar H1 with a tensor term
   int64_t elemStart;
 };
 
@@ -237,14 +237,14 @@ int launchFactoredFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dte
 
 // mixed path pieces shared with the multi-frequency path (assemble_mixed.cu)
 int prepareMixed(fg_plan *plan, int ncomp, int groups);
-int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups, cudaStream_t s);
+int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups, uint32_t tensorMask, cudaStream_t s);
 int launchRhsFp64(fg_plan *plan, const DevTerms *dterms, double *be, cudaStream_t s);
 float *mixedKe(fg_plan *plan, int *blocks);
 int mixedCheckTimeout(fg_plan *plan, bool wait);
 int mixedRecordError(fg_plan *plan, cudaStream_t s);
 // ... and with the batch (batch.cu)
 int launchFactorsBatch(const FactorJob *jobsDev, int nJobs, int64_t total, cudaStream_t s);
-FactorJob mixedFactorJob(fg_plan *plan, const DevTerms *dterms, int64_t elemStart);
+FactorJob mixedFactorJob(fg_plan *plan, const DevTerms *dterms, bool tensor, int64_t elemStart);
 std::vector<int4> mixedTiles(fg_plan *plan, int prob, int rowsPerElem);
 // contraction CTAs per SM (1 or 2) and the dynamic shared memory that pins it
 int gemmCtasPerSm(int Npad, int k3);

@@ -409,7 +409,10 @@ int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t
       if ((st = launchRhsFp64(plan, m->dev[0], be, s))) return st;
     if (p.E > 0) {
       const DevTerms *devs[kMaxGroups] = {m->dev[0], m->dev[1], m->dev[2]};
-      if ((st = launchMixedElement(plan, devs, G, s))) return st;
+      uint32_t tensorMask = 0;
+      for (int g = 0; g < G; ++g)
+        if (m->terms[g].tensorTerm >= 0) tensorMask |= 1u << g;
+      if ((st = launchMixedElement(plan, devs, G, tensorMask, s))) return st;
     }
     int blocks = 1;
     const float *ke = mixedKe(plan, &blocks);
