@@ -569,6 +569,6 @@ extern "C" int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_
   if (p.E > 0) {
     if ((st = launchElementFp64(plan, dt, dterms, plan->ke, be, s))) return st;
   }
-  if ((st = gatherToOutputs(plan, plan->ke, dt.complexKe, 0, 1, be, uD, o, csr_values, s))) return st;
+  if ((st = gatherToOutputs(plan, plan->ke, dt.complexKe, 0, keFull(plan->d.n), be, uD, o, csr_values, s))) return st;
   return finishOutputs(plan, o, csr_values, rhs, s);
 }

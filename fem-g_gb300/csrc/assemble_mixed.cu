@@ -57,13 +57,18 @@ struct MixedState {
   alignas(64) CUtensorMap aMap;  // TMA view of A: [rows][k3] floats, box 4 x 128
   int mmaN = 256;               // N of one MMA instruction
   void *probDev = nullptr;      // this plan's GemmProblem on the device
-  float *ke = nullptr;       // [E][groups][ncomp][n][n] fp32
+  float *ke = nullptr;       // [E][groups][ncomp][n][n] fp32 (layout: mixedLayout)
   size_t keBytes = 0;
   int *err = nullptr;        // device error word (wait timeouts)
   int *errHost = nullptr;    // pinned copy of err
   cudaEvent_t errEvent = nullptr;
   bool errPending = false;
 };
+
+// The layout of m->ke for the reduction
+static KeLayout mixedLayout(const MixedState *m) {
+  return KeLayout{m->blocks == 9 ? kKeBlocks3 : kKeFull, m->n * m->n};
+}
 
 // Reports (once) a device wait timeout recorded by an earlier launch: when
 // wait is false only an already completed copy of the error word is read.
@@ -812,24 +817,19 @@ __global__ void k_rhs_fp64(const PlanDev p, const DevTerms *__restrict__ terms, 
 // -------------------------------------------- error report (device side)
 
 // per element ||Ke32 - Ke64||_F^2 and ||Ke64||_F^2; the FP64 matrices are
-// row-major [ncomp][n][n], the FP32 ones row-major or (compound fields) in
-// 3x3 component blocks [ncomp][a*3+b][nb][nb]
-__global__ void k_elem_err(const float *__restrict__ k32, const double *__restrict__ k64, int64_t E, int len, int n, int blk3,
+// row-major [ncomp][n][n], the FP32 ones [ncomp][lay.ld] in the layout lay
+__global__ void k_elem_err(const float *__restrict__ k32, const double *__restrict__ k64, int64_t E, int ncomp, int n, KeLayout lay,
                            double *__restrict__ out) {
   const int64_t e = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (e >= E) return;
-  const int nn = n * n, nb = n / 3;
+  const int nn = n * n, len = ncomp * nn;
   double d2 = 0.0, r2 = 0.0;
   for (int k = lane; k < len; k += 32) {
-    int o32 = k;
-    if (blk3) {
-      const int comp = k / nn, r = k - comp * nn, ii = r / n, jj = r - ii * n;
-      const int i = ii / 3, a = ii - 3 * i, j = jj / 3, b = jj - 3 * j;
-      o32 = comp * nn + ((a * 3 + b) * nb + i) * nb + j;
-    }
+    const int comp = k / nn, r = k - comp * nn, ii = r / n, jj = r - ii * n;
+    const int o32 = comp * lay.ld + keOffset(lay, n, ii, jj);
     const double a = k64[(size_t)e * len + k];
-    const double d = (double)k32[(size_t)e * len + o32] - a;
+    const double d = (double)k32[(size_t)e * ncomp * lay.ld + o32] - a;
     d2 += d * d;
     r2 += a * a;
   }
@@ -1206,9 +1206,9 @@ int launchRhsFp64(fg_plan *plan, const DevTerms *dterms, double *be, cudaStream_
 }
 
 // Accessors for the multi-frequency path
-float *mixedKe(fg_plan *plan, int *blocks) {
+float *mixedKe(fg_plan *plan, KeLayout *lay) {
   MixedState *m = state(plan);
-  *blocks = m->blocks;
+  *lay = mixedLayout(m);
   return m->ke;
 }
 
@@ -1283,7 +1283,7 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
   }
   if (p.E > 0)
     if ((st = launchMixedElement(plan, &dterms, 1, dt.tensorTerm >= 0 ? 1u : 0u, s))) return st;
-  if ((st = gatherToOutputs(plan, (const double *)m->ke, dt.complexKe, 1, m->blocks, be, uD, o, csr_values, s))) return st;
+  if ((st = gatherToOutputs(plan, (const double *)m->ke, dt.complexKe, 1, mixedLayout(m), be, uD, o, csr_values, s))) return st;
   if (report) {
     // FP64 element matrices and CSR of the same terms, compared on the device
     const int ncomp = dt.complexKe ? 2 : 1;
@@ -1293,10 +1293,10 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
     double *tmp = nullptr, *csr64 = nullptr;
     FG_CUDA(cudaMalloc(&tmp, (size_t)std::max<int64_t>(p.E, 1024) * 16));
     FG_CUDA(cudaMalloc(&csr64, p.nnz * 16));
-    k_elem_err<<<(unsigned)((p.E + 7) / 8), 256, 0, s>>>(m->ke, plan->ke, p.E, (int)len, p.n, m->blocks == 9 ? 1 : 0, tmp);
+    k_elem_err<<<(unsigned)((p.E + 7) / 8), 256, 0, s>>>(m->ke, plan->ke, p.E, ncomp, p.n, mixedLayout(m), tmp);
     std::vector<double> h((size_t)p.E * 2);
     FG_CUDA(cudaMemcpyAsync(h.data(), tmp, h.size() * 8, cudaMemcpyDeviceToHost, s));
-    if ((st = launchGather(plan, plan->ke, dt.complexKe, 0, 1, nullptr, uD, csr64, nullptr, s))) return st;
+    if ((st = launchGather(plan, plan->ke, dt.complexKe, 0, keFull(p.n), nullptr, uD, csr64, nullptr, s))) return st;
     k_diff_norms<<<1024, 256, 0, s>>>(o.values, csr64, (int64_t)p.nnz * 2, tmp);
     std::vector<double> g(2048);
     FG_CUDA(cudaMemcpyAsync(g.data(), tmp, g.size() * 8, cudaMemcpyDeviceToHost, s));

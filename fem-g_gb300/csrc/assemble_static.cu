@@ -93,5 +93,5 @@ extern "C" int fg_assemble_fp64_static(fg_plan *plan, const double *dirichlet, d
   if (p.E > 0) {
     if ((st = launchElementFp64(plan, dt, plan->boundDev, ke, be, s))) return st;
   }
-  return launchGather(plan, ke, dt.complexKe, 0, 1, be, uD, csr_values, rhs, s);
+  return launchGather(plan, ke, dt.complexKe, 0, keFull(p.n), be, uD, csr_values, rhs, s);
 }

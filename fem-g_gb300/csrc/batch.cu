@@ -457,9 +457,8 @@ extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const 
       fg_plan *pl = plans[q];
       GatherJob &J = c.jobsHost[k];
       J.p = pl->d;
-      int blocks = 1;
-      J.ke = b->mixed ? (const void *)mixedKe(pl, &blocks) : (const void *)pl->ke;
-      J.blk3 = blocks == 9 ? 1 : 0;
+      J.lay = keFull(pl->d.n);
+      J.ke = b->mixed ? (const void *)mixedKe(pl, &J.lay) : (const void *)pl->ke;
       J.be = b->source[q] ? (const double2 *)pl->be : nullptr;
       J.uD = nullptr;
     }

@@ -172,9 +172,25 @@ int smCount();
 // copy the Dirichlet values; return device pointer (or null)
 int uploadDirichlet(fg_plan *plan, const double *dirichlet, const double **out, cudaStream_t s);
 bool isDevicePointer(const void *p);
-// FP64 gather of element matrices/vectors into CSR values and RHS
-// keBlocks: 1 = element matrices row-major [n][n]; 9 = 3x3 component blocks
-int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+// Layout of the element matrices the reduction reads: row-major [n][n]
+// (FP64 kernels, scalar and HCurl fields) or 3x3 component blocks
+// [a*3+b][nb][nb] (compound fields on the tensor-core path). ld = entries per
+// component (imaginary part at +ld, next element at +ncomp*ld). A packed
+// upper triangle for the symmetric scalar case halved the contraction's
+// output but made the reduction's reads of the lower half scattered: the
+// 384,000-tet order-3 step went from 0.854 to 0.877 ms, so it is not used.
+enum { kKeFull = 0, kKeBlocks3 = 1 };
+struct KeLayout {
+  int32_t kind, ld;
+};
+inline KeLayout keFull(int n) { return KeLayout{kKeFull, n * n}; }
+__device__ __forceinline__ int keOffset(const KeLayout &lay, int n, int ii, int jj) {
+  if (lay.kind == kKeFull) return ii * n + jj;
+  const int nb = n / 3, i = ii / 3, a = ii - 3 * i, j = jj / 3, b = jj - 3 * j;
+  return ((a * 3 + b) * nb + i) * nb + j;
+}
+// gather of element matrices/vectors into CSR values and RHS
+int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, KeLayout lay, const double *be,
                  const double *dirichletDev, double *values, double *rhs, cudaStream_t s);
 // outputs: device pointers used in place, host pointers staged through the plan
 struct Outputs {
@@ -186,7 +202,7 @@ int prepareOutputs(fg_plan *plan, double *csr_values, double *rhs, Outputs *o);
 int finishOutputs(fg_plan *plan, const Outputs &o, double *csr_values, double *rhs, cudaStream_t s);
 // The CSR reduction into the outputs: with host values, range by range, each
 // range's slice copied to the host on a second stream while the next reduces
-int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, KeLayout lay, const double *be,
                     const double *dirichletDev, Outputs &o, double *csr_values, cudaStream_t s);
 // FP64 element kernel (also used as the reference for the mixed error report)
 int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s);
@@ -196,7 +212,7 @@ struct GatherJob {
   const void *ke;  // element matrices (float or double, one layout per launch)
   const double2 *be, *uD;
   double2 *values, *rhs;
-  int32_t blk3, pad_;
+  KeLayout lay;
   int64_t blockStart, nBlocks;
 };
 struct GatherShape {
@@ -239,7 +255,7 @@ int launchFactoredFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dte
 int prepareMixed(fg_plan *plan, int ncomp, int groups);
 int launchMixedElement(fg_plan *plan, const DevTerms *const *dterms, int groups, uint32_t tensorMask, cudaStream_t s);
 int launchRhsFp64(fg_plan *plan, const DevTerms *dterms, double *be, cudaStream_t s);
-float *mixedKe(fg_plan *plan, int *blocks);
+float *mixedKe(fg_plan *plan, KeLayout *lay);
 int mixedCheckTimeout(fg_plan *plan, bool wait);
 int mixedRecordError(fg_plan *plan, cudaStream_t s);
 // ... and with the batch (batch.cu)

@@ -22,19 +22,13 @@ namespace femg {
 template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J>
 __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restrict__ ke, const double2 *__restrict__ be,
                                            const double2 *__restrict__ uD, double2 *__restrict__ values,
-                                           double2 *__restrict__ rhs, int rowsPerBlock, int blk3, int64_t blk, int64_t nblk,
+                                           double2 *__restrict__ rhs, int rowsPerBlock, KeLayout lay, int64_t blk, int64_t nblk,
                                            int64_t v0, int64_t v1) {
   constexpr int R = 32 / L;  // rows per warp; J: columns per lane (L * J >= n)
   constexpr int SS = KCPLX ? 2 : 1;
   // offset of entry (test ii, unknown jj) inside one component of an element
-  // matrix: row-major [n][n], or (compound fields from the tensor-core path)
-  // 3x3 blocks [a*3+b][nb][nb] with ii = i*3 + a, jj = j*3 + b
-  const int nbk = p.nb;
-  auto keOff = [&](int ii, int jj) -> int {
-    if (!blk3) return ii * p.n + jj;
-    const int i = ii / 3, a = ii - 3 * i, j = jj / 3, b = jj - 3 * j;
-    return ((a * 3 + b) * nbk + i) * nbk + j;
-  };
+  // matrix in the layout lay (compound blocks: ii = i*3 + a, jj = j*3 + b)
+  auto keOff = [&](int ii, int jj) -> int { return keOffset(lay, p.n, ii, jj); };
   extern __shared__ __align__(16) unsigned char smraw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / L, lt = lane % L;
@@ -43,7 +37,7 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
   const SlotT kFixed = (SlotT)(sizeof(SlotT) == 1 ? 0xFF : kSlotFixed);
   const SlotT kIgnore = (SlotT)(sizeof(SlotT) == 1 ? 0xFE : kSlotIgnore);
   const int n = p.n;
-  const size_t nn2 = (size_t)n * n;
+  const size_t nn2 = (size_t)lay.ld;  // entries per component
   // visit records [v0, v1) of this launch
   const int64_t nRows = v1;
   const int64_t stride = nblk * rowsPerBlock;
@@ -163,8 +157,8 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
 template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J>
 __global__ void __launch_bounds__(256)
     k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
-             double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock, int blk3, int64_t v0, int64_t v1) {
-  gatherRows<SlotT, KCPLX, KT, AT, L, J>(p, ke, be, uD, values, rhs, rowsPerBlock, blk3, blockIdx.x, gridDim.x, v0, v1);
+             double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock, KeLayout lay, int64_t v0, int64_t v1) {
+  gatherRows<SlotT, KCPLX, KT, AT, L, J>(p, ke, be, uD, values, rhs, rowsPerBlock, lay, blockIdx.x, gridDim.x, v0, v1);
 }
 
 // Many plans in one launch: job q owns blocks [blockStart, blockStart + nBlocks)
@@ -177,13 +171,13 @@ __global__ void __launch_bounds__(256) k_gather_batch(const GatherJob *__restric
     else hi = mid - 1;
   }
   const GatherJob &Jb = jobs[lo];
-  gatherRows<SlotT, KCPLX, KT, AT, L, J>(Jb.p, (const KT *)Jb.ke, Jb.be, Jb.uD, Jb.values, Jb.rhs, rowsPerBlock, Jb.blk3,
+  gatherRows<SlotT, KCPLX, KT, AT, L, J>(Jb.p, (const KT *)Jb.ke, Jb.be, Jb.uD, Jb.values, Jb.rhs, rowsPerBlock, Jb.lay,
                                          (int64_t)blockIdx.x - Jb.blockStart, Jb.nBlocks, 0, (int64_t)Jb.p.nRows);
 }
 
 template <typename SlotT, bool KCPLX, typename KT>
 static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, const double2 *uD, double2 *values, double2 *rhs,
-                       int blk3, int64_t v0, int64_t v1, cudaStream_t s) {
+                       KeLayout lay, int64_t v0, int64_t v1, cudaStream_t s) {
   using AT = KT;  // FP32 element matrices accumulate in FP32, FP64 ones in FP64
   const GatherShape shape = gatherShape(p.n, p.maxRowLen, KCPLX ? 1 : 0, sizeof(KT) == 4 ? 1 : 0, 0, 0);
   const int L = shape.L, J = shape.J;
@@ -210,7 +204,7 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
       FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                \
       smemSet = smem;                                                                                             \
     }                                                                                                             \
-    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock, blk3, v0, v1); \
+    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock, lay, v0, v1); \
   }
   FG_GATHER_L(2, 3)
   FG_GATHER_L(4, 3)
@@ -228,9 +222,8 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
 }
 
 // The rows of visit records [v0, v1) (all rows: 0, nRows).
-static int launchGatherRange(const PlanDev &p, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+static int launchGatherRange(const PlanDev &p, const double *ke, int keComplex, int keIsFloat, KeLayout lay, const double *be,
                              const double *dirichletDev, double *values, double *rhs, int64_t v0, int64_t v1, cudaStream_t s) {
-  const int blk3 = keBlocks == 9 ? 1 : 0;
   if (v1 <= v0) return FG_OK;
   if (p.lscale && !keComplex) {
     setLastError("gather: linked DOFs need complex element matrices");
@@ -244,27 +237,27 @@ static int launchGatherRange(const PlanDev &p, const double *ke, int keComplex, 
   countLaunch();
   if (p.slotBytes == 1) {
     if (keIsFloat)
-      return keComplex ? launchTyped<uint8_t, true, float>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s) : launchTyped<uint8_t, false, float>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s);
-    return keComplex ? launchTyped<uint8_t, true, double>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s) : launchTyped<uint8_t, false, double>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s);
+      return keComplex ? launchTyped<uint8_t, true, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, s) : launchTyped<uint8_t, false, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, s);
+    return keComplex ? launchTyped<uint8_t, true, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, s) : launchTyped<uint8_t, false, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, s);
   }
   if (keIsFloat)
-    return keComplex ? launchTyped<uint16_t, true, float>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s) : launchTyped<uint16_t, false, float>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s);
-  return keComplex ? launchTyped<uint16_t, true, double>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s) : launchTyped<uint16_t, false, double>(p, ke, be2, uD, v2, r2, blk3, v0, v1, s);
+    return keComplex ? launchTyped<uint16_t, true, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, s) : launchTyped<uint16_t, false, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, s);
+  return keComplex ? launchTyped<uint16_t, true, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, s) : launchTyped<uint16_t, false, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, s);
 }
 
-int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, KeLayout lay, const double *be,
                  const double *dirichletDev, double *values, double *rhs, cudaStream_t s) {
-  return launchGatherRange(plan->d, ke, keComplex, keIsFloat, keBlocks, be, dirichletDev, values, rhs, 0, (int64_t)plan->d.nRows, s);
+  return launchGatherRange(plan->d, ke, keComplex, keIsFloat, lay, be, dirichletDev, values, rhs, 0, (int64_t)plan->d.nRows, s);
 }
 
 // Host values: the reduction runs range by range; after each range an event
 // lets the copy stream bring that range's CSR slice to the host while the
 // next range reduces (the copy, not the reduction, bounds a host-output call).
-int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, int keBlocks, const double *be,
+int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, KeLayout lay, const double *be,
                     const double *dirichletDev, Outputs &o, double *csr_values, cudaStream_t s) {
   const size_t nc = plan->outChunkRow.size() > 1 ? plan->outChunkRow.size() - 1 : 0;
   if (!o.hostValues || nc < 2)
-    return launchGather(plan, ke, keComplex, keIsFloat, keBlocks, be, dirichletDev, o.values, o.rhs, s);
+    return launchGather(plan, ke, keComplex, keIsFloat, lay, be, dirichletDev, o.values, o.rhs, s);
   if (!plan->copyStream) {
     FG_CUDA(cudaStreamCreateWithFlags(&plan->copyStream, cudaStreamNonBlocking));
     plan->copyEvents.assign(nc, nullptr);
@@ -275,7 +268,7 @@ int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloa
   pr.visitElem = plan->visitElemRanged;
   for (size_t c = 0; c < nc; ++c) {
     const uint64_t r0 = plan->outChunkRow[c], r1 = plan->outChunkRow[c + 1];
-    int st = launchGatherRange(pr, ke, keComplex, keIsFloat, keBlocks, be, dirichletDev, o.values, o.rhs, (int64_t)r0, (int64_t)r1, s);
+    int st = launchGatherRange(pr, ke, keComplex, keIsFloat, lay, be, dirichletDev, o.values, o.rhs, (int64_t)r0, (int64_t)r1, s);
     if (st) return st;
     FG_CUDA(cudaEventRecord(plan->copyEvents[c], s));
     FG_CUDA(cudaStreamWaitEvent(plan->copyStream, plan->copyEvents[c], 0));

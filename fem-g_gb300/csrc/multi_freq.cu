@@ -31,7 +31,8 @@ struct MultiIn {
   int cplx[kMaxGroups];          // group g has an imaginary part (at +n*n)
   int realFactor[kMaxGroups];    // the factors of group g are real for every output
   int imagFactor[kMaxGroups];    // ... purely imaginary for every output
-  int G, F, R, blk3;
+  int G, F, R;
+  KeLayout lay;                  // element-matrix layout (ld entries per component)
   const double2 *coef;           // [F][G] factors of the value arrays
   const double2 *rcoef;          // [R][G] factors of the liftings in the right-hand sides
   const double2 *be;             // [E][n] element right-hand sides or null
@@ -46,13 +47,7 @@ __global__ void __launch_bounds__(256)
   using AT = KT;
   constexpr int R = 32 / L;  // rows per warp; J columns per lane (L * J >= n)
   const int G = in.G, F = in.F;
-  const int nbk = p.nb;
-  const int blk3 = in.blk3;
-  auto keOff = [&](int ii, int jj) -> int {
-    if (!blk3) return ii * p.n + jj;
-    const int i = ii / 3, a = ii - 3 * i, j = jj / 3, b = jj - 3 * j;
-    return ((a * 3 + b) * nbk + i) * nbk + j;
-  };
+  auto keOff = [&](int ii, int jj) -> int { return keOffset(in.lay, p.n, ii, jj); };
   extern __shared__ __align__(16) unsigned char smraw[];
   AT *cf = reinterpret_cast<AT *>(smraw);  // [F][G][2] factors in the accumulation type
   for (int k = threadIdx.x; k < F * G; k += blockDim.x) {
@@ -69,7 +64,7 @@ __global__ void __launch_bounds__(256)
   const SlotT kFixed = (SlotT)(sizeof(SlotT) == 1 ? 0xFF : kSlotFixed);
   const SlotT kIgnore = (SlotT)(sizeof(SlotT) == 1 ? 0xFE : kSlotIgnore);
   const int n = p.n;
-  const int nn2 = n * n;
+  const int nn2 = in.lay.ld;  // entries per component
   const int64_t nRows = (int64_t)p.nRows;
   const int64_t stride = (int64_t)gridDim.x * rowsPerBlock;
   for (int64_t base = (int64_t)blockIdx.x * rowsPerBlock + warp * R; base < nRows; base += stride) {
@@ -383,6 +378,7 @@ int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t
   const size_t nn = (size_t)p.n * p.n;
   bool isFloat = false;
   if (!mixed) {
+    in.lay = keFull(p.n);
     for (int g = 0; g < G; ++g) {
       const int ncomp = m->terms[g].complexKe ? 2 : 1;
       if ((st = ensureDevice((void **)&m->ke[g], &m->keBytes[g], (size_t)p.E * ncomp * nn * sizeof(double)))) return st;
@@ -414,14 +410,13 @@ int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t
         if (m->terms[g].tensorTerm >= 0) tensorMask |= 1u << g;
       if ((st = launchMixedElement(plan, devs, G, tensorMask, s))) return st;
     }
-    int blocks = 1;
-    const float *ke = mixedKe(plan, &blocks);
+    const float *ke = mixedKe(plan, &in.lay);
+    const size_t ld = (size_t)in.lay.ld;
     for (int g = 0; g < G; ++g) {
-      in.ke[g] = ke + (size_t)g * ncomp * nn;
-      in.stride[g] = (int64_t)((size_t)G * ncomp * nn);
+      in.ke[g] = ke + (size_t)g * ncomp * ld;
+      in.stride[g] = (int64_t)((size_t)G * ncomp * ld);
       in.cplx[g] = ncomp == 2 && m->terms[g].complexKe;
     }
-    in.blk3 = blocks == 9 ? 1 : 0;
     isFloat = true;
   }
   if ((st = launchGatherMulti(plan, in, isFloat, s))) return st;
