@@ -77,10 +77,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         double xq[3];
         pointGeometry(p, terms, g, q, S.X, S.J0, S.det0, S.J, S.det, S.Jinv, xq);
         double2 cgg = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0), f = make_double2(0.0, 0.0);
+        const double *phq = p.bval + ((size_t)o * p.nq + q) * p.nb;  // for field-node coefficients
         for (int t = 0; t < terms->n; ++t) {
           const DevTerm &T = terms->t[t];
           if (T.mod != g) continue;
-          const double2 v = evalExpr(T.coef, e, xq);
+          const double2 v = evalExpr(T.coef, e, xq, phq, p.nb);
           if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, v));
           else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, v));
           else if (T.kind == FG_TERM_SOURCE) f = cadd(f, v);
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         S.s = make_double2(wd * f.x, wd * f.y);
         if (terms->tensorTerm >= 0) {
           double2 A[6];
-          diffusionTensor(terms, g, e, xq, cgg, A);
+          diffusionTensor(terms, g, e, xq, cgg, A, phq, p.nb);
           for (int k = 0; k < 6; ++k) S.Aw[k] = make_double2(wd * A[k].x, wd * A[k].y);
         }
       }
@@ -223,14 +224,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         double xq[3];
         pointGeometry(p, terms, g, q, S.X, S.J0, S.det0, S.J, S.det, S.Jinv, xq);
         double2 lam = make_double2(0.0, 0.0), mu = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0);
+        const double *phq = p.bval + ((size_t)o * p.nq + q) * p.nb;  // scalar basis values (field nodes)
         for (int t = 0; t < terms->n; ++t) {
           const DevTerm &T = terms->t[t];
           if (T.mod != g) continue;
           if (T.kind == FG_TERM_ELASTIC) {
-            lam = cadd(lam, cmul(T.factor, evalExpr(T.coef, e, xq)));
-            mu = cadd(mu, cmul(T.factor, evalExpr(T.coef2, e, xq)));
+            lam = cadd(lam, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb)));
+            mu = cadd(mu, cmul(T.factor, evalExpr(T.coef2, e, xq, phq, p.nb)));
           } else if (T.kind == FG_TERM_MASS) {
-            cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xq)));
+            cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb)));
           }
         }
         const double wd = p.w[q] * S.det;

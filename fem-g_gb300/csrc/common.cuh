@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/fem_g_gb300.h"
@@ -142,6 +143,7 @@ struct fg_plan {
   double *rhs = nullptr;
   size_t rhsBytes = 0;
   std::vector<void *> termArrays;   // device copies of per-element coefficient arrays (per call)
+  std::unordered_map<void *, size_t> arrayBytes;  // allocated size of each coefficient array
   std::vector<void *> boundArrays;  // ... of the terms bound by fg_plan_bind_terms
   femg::DevTerms bound;
   femg::DevTerms *boundDev = nullptr;  // device copy of the bound terms
@@ -307,8 +309,11 @@ __device__ inline double widen(float x) {
 }
 __device__ inline double widen(double x) { return x; }
 
-// Evaluate a coefficient expression at element e and physical point x
-__device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x) {
+// Evaluate a coefficient expression at element e and physical point x; phi:
+// the scalar basis values at the point (nb of them) for field nodes, null
+// where the expression is evaluated once per element (field nodes make an
+// expression point-dependent, which those paths refuse)
+__device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x, const double *phi = nullptr, int nb = 0) {
   if (ex.cls == kExprConst) return ex.cval;
   double2 st[16];
   int sp = 0;
@@ -320,6 +325,17 @@ __device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x
       case FG_OP_Y: st[sp++] = make_double2(x[1], 0.0); break;
       case FG_OP_Z: st[sp++] = make_double2(x[2], 0.0); break;
       case FG_OP_ELEM: st[sp++] = ex.arr[in.arg][e]; break;
+      case FG_OP_FIELD: {
+        const double2 *u = ex.arr[in.arg] + (size_t)e * nb;
+        double2 s = make_double2(0.0, 0.0);
+        for (int j = 0; phi && j < nb; ++j) {
+          const double2 v = u[j];
+          s.x += phi[j] * v.x;
+          s.y += phi[j] * v.y;
+        }
+        st[sp++] = s;
+        break;
+      }
       case FG_OP_NEG: st[sp - 1] = make_double2(-st[sp - 1].x, -st[sp - 1].y); break;
       case FG_OP_HEAVISIDE: {
         const double r = st[sp - 1].x;
@@ -344,12 +360,13 @@ __device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x
 // Diffusion tensor of the grad-grad terms of modificator group g at element e
 // and point x: A = cgg I + factor c D, with cgg the summed scalar grad-grad
 // coefficients and D the tensor term's entries (00, 11, 22, 01, 02, 12).
-__device__ inline void diffusionTensor(const DevTerms *terms, int g, int64_t e, const double *x, double2 cgg, double2 *A) {
+__device__ inline void diffusionTensor(const DevTerms *terms, int g, int64_t e, const double *x, double2 cgg, double2 *A,
+                                       const double *phi = nullptr, int nb = 0) {
   for (int k = 0; k < 6; ++k) A[k] = k < 3 ? cgg : make_double2(0.0, 0.0);
   const DevTerm &T = terms->t[terms->tensorTerm];
   if (T.mod != g) return;
-  const double2 fc = cmul(T.factor, evalExpr(T.coef, e, x));
-  for (int k = 0; k < 6; ++k) A[k] = cadd(A[k], cmul(fc, evalExpr(terms->tensor[k], e, x)));
+  const double2 fc = cmul(T.factor, evalExpr(T.coef, e, x, phi, nb));
+  for (int k = 0; k < 6; ++k) A[k] = cadd(A[k], cmul(fc, evalExpr(terms->tensor[k], e, x, phi, nb)));
 }
 
 // Jacobian at a quadrature point from the geometric nodes, stored column-major

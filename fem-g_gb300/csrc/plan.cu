@@ -476,7 +476,8 @@ int uploadDirichlet(fg_plan *plan, const double *dirichlet, const double **out, 
 static int classify(const fg_expr &ex) {
   int cls = kExprConst;
   for (int k = 0; k < ex.n_code; ++k) {
-    if (ex.code[k].op == FG_OP_X || ex.code[k].op == FG_OP_Y || ex.code[k].op == FG_OP_Z) return kExprPoint;
+    if (ex.code[k].op == FG_OP_X || ex.code[k].op == FG_OP_Y || ex.code[k].op == FG_OP_Z || ex.code[k].op == FG_OP_FIELD)
+      return kExprPoint;
     if (ex.code[k].op == FG_OP_ELEM) cls = kExprElem;
   }
   return cls;
@@ -509,8 +510,10 @@ static int validateExpr(const fg_expr &ex) {
   int depth = 0;
   for (int k = 0; k < ex.n_code; ++k) {
     const int op = ex.code[k].op;
-    if (op <= FG_OP_ELEM) {
-      if (op == FG_OP_ELEM && (ex.code[k].arg < 0 || ex.code[k].arg >= ex.n_arrays || !ex.elem_values[ex.code[k].arg])) return 1;
+    if (op <= FG_OP_ELEM || op == FG_OP_FIELD) {
+      if ((op == FG_OP_ELEM || op == FG_OP_FIELD) &&
+          (ex.code[k].arg < 0 || ex.code[k].arg >= ex.n_arrays || !ex.elem_values[ex.code[k].arg]))
+        return 1;
       if (++depth > 16) return 1;
     } else if (op == FG_OP_NEG || op == FG_OP_HEAVISIDE) {
       if (depth < 1) return 1;
@@ -525,8 +528,9 @@ static int validateExpr(const fg_expr &ex) {
 }
 
 // arrays: the device copies of per-element coefficient arrays ([E] complex
-// each); the first `used` are this upload's, later ones are reused from the
-// previous upload (same size) instead of freed and allocated again.
+// each, or [E][nb] for the field values of FG_OP_FIELD); the first `used` are
+// this upload's, later ones are reused from the previous upload instead of
+// freed and allocated again (a buffer too small for its new array is replaced).
 static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complexOut, std::vector<void *> &arrays, size_t &used) {
   if (validateExpr(ex)) {
     setLastError("invalid coefficient expression");
@@ -545,26 +549,45 @@ static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complex
     if (v.imag() != 0.0) *complexOut = true;
   }
   for (int a = 0; a < ex.n_arrays; ++a) {
-    const size_t bytes = (size_t)plan->E * 16;
+    bool elem = false, field = false;
+    for (int k = 0; k < ex.n_code; ++k) {
+      elem = elem || (ex.code[k].op == FG_OP_ELEM && ex.code[k].arg == a);
+      field = field || (ex.code[k].op == FG_OP_FIELD && ex.code[k].arg == a);
+    }
+    if (elem && field) {
+      setLastError("a coefficient array is used both per element and as field values");
+      return FG_ERR_ARG;
+    }
+    if (field && plan->d.form != FG_FORM_0) {
+      setLastError("field values (FG_OP_FIELD) need an H1 bucket");
+      return FG_ERR_UNSUPPORTED;
+    }
+    const size_t bytes = (size_t)plan->E * 16 * (field ? (size_t)plan->d.nb : 1);
     if (isDevicePointer(ex.elem_values[a])) {
       out->arr[a] = (const double2 *)ex.elem_values[a];
       *complexOut = true;  // cannot scan device data cheaply: assume complex
       continue;
     }
-    for (int64_t e = 0; e < plan->E; ++e)
-      if (ex.elem_values[a][2 * e + 1] != 0.0) {
+    for (size_t k = 0; k < bytes / 16; ++k)
+      if (ex.elem_values[a][2 * k + 1] != 0.0) {
         *complexOut = true;
         break;
       }
     void *p = nullptr;
-    if (used < arrays.size()) {
+    if (used < arrays.size() && plan->arrayBytes[arrays[used]] >= bytes) {
       p = arrays[used];
     } else {
       if (cudaMalloc(&p, bytes) != cudaSuccess) {
         setLastError("coefficient upload: out of device memory");
         return FG_ERR_OOM;
       }
-      arrays.push_back(p);
+      plan->arrayBytes[p] = bytes;
+      if (used < arrays.size()) {
+        cudaFree(arrays[used]);
+        arrays[used] = p;
+      } else {
+        arrays.push_back(p);
+      }
     }
     ++used;
     if (cudaMemcpy(p, ex.elem_values[a], bytes, cudaMemcpyHostToDevice) != cudaSuccess) {

@@ -24,7 +24,7 @@ FG_JACMOD_NONE, FG_JACMOD_AXISYMMETRY, FG_JACMOD_AXISYMMETRY_SHELL, FG_JACMOD_PO
     FG_JACMOD_SPHERICAL_SHELL = range(6)
 FG_FP64_QUADRATURE, FG_FP64_FACTORED = range(2)
 (FG_OP_CONST, FG_OP_X, FG_OP_Y, FG_OP_Z, FG_OP_ELEM, FG_OP_ADD, FG_OP_SUB, FG_OP_MUL, FG_OP_DIV, FG_OP_NEG,
- FG_OP_HEAVISIDE) = range(11)
+ FG_OP_HEAVISIDE, FG_OP_FIELD) = range(12)
 FG_EXPR_MAX_CODE = 32
 FG_EXPR_MAX_ARRAYS = 4
 

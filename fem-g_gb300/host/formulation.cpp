@@ -221,9 +221,15 @@ Function Function::perElement(const std::vector<cplx> &values) {
   return f;
 }
 
+Function Function::fieldValues(const std::vector<cplx> &elemDofValues) {
+  Function f = perElement(elemDofValues);
+  f.code[0].op = FG_OP_FIELD;
+  return f;
+}
+
 bool Function::usesPoints() const {
   for (auto &i : code)
-    if (i.op == FG_OP_X || i.op == FG_OP_Y || i.op == FG_OP_Z) return true;
+    if (i.op == FG_OP_X || i.op == FG_OP_Y || i.op == FG_OP_Z || i.op == FG_OP_FIELD) return true;
   return false;
 }
 
@@ -279,7 +285,7 @@ Function Function::binary(const Function &a, const Function &b, int op) {
   r.arrays = a.arrays;
   const int32_t shift = (int32_t)a.arrays.size();
   for (auto in : b.code) {
-    if (in.op == FG_OP_ELEM) in.arg += shift;
+    if (in.op == FG_OP_ELEM || in.op == FG_OP_FIELD) in.arg += shift;
     r.code.push_back(in);
   }
   r.arrays.insert(r.arrays.end(), b.arrays.begin(), b.arrays.end());

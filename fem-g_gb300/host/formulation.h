@@ -66,7 +66,7 @@ class FunctionSpace {
 class Function {
  public:
   std::vector<fg_instr> code;
-  std::vector<std::shared_ptr<std::vector<double>>> arrays;  // per element (re, im)
+  std::vector<std::shared_ptr<std::vector<double>>> arrays;  // per element (re, im), or per element DOF for field values
 
   Function(double v = 0.0) : Function(cplx(v, 0.0)) {}
   Function(cplx v);
@@ -74,6 +74,10 @@ class Function {
   static Function y();
   static Function z();
   static Function perElement(const std::vector<cplx> &values);
+  // a scalar field of the bucket's own H1 space at the quadrature points (the
+  // reference's field node): its values at every element's local DOFs,
+  // [n_elements][n] in the element DOF order of pre()
+  static Function fieldValues(const std::vector<cplx> &elemDofValues);
 
   bool usesPoints() const;
   bool usesElements() const;

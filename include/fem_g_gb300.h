@@ -139,7 +139,10 @@ enum {
   FG_OP_MUL = 7,
   FG_OP_DIV = 8,
   FG_OP_NEG = 9,
-  FG_OP_HEAVISIDE = 10 /* 1 if Re>0, 0 if Re<0, 0.5 if Re==0 (unaryOperations.h:1008-1021) */
+  FG_OP_HEAVISIDE = 10, /* 1 if Re>0, 0 if Re<0, 0.5 if Re==0 (unaryOperations.h:1008-1021) */
+  FG_OP_FIELD = 11      /* push u(x) = sum_j phi_j(x) u_e[j]: a scalar field of the bucket's own H1 space
+                           at the point (field node, fieldOperations.h:160-170); elem_values[arg] is then
+                           [n_elements][nb][2], the field's values at each element's local DOFs */
 };
 typedef struct {
   int32_t op;

@@ -31,7 +31,7 @@ typedef double complex cplx;
 
 enum { AT_UNDEFINED = 0, AT_FIXED = 1, AT_UNKNOWN = 2, AT_UNKNOWN_BUBBLE = 3, AT_UNKNOWN_GLOBAL = 4 };
 enum { TERM_GRAD_GRAD = 0, TERM_MASS = 1, TERM_ELASTIC = 2, TERM_SOURCE = 3, TERM_GRAD_GRAD_TENSOR = 4 };
-enum { OP_CONST = 0, OP_X, OP_Y, OP_Z, OP_ELEM, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_HEAVISIDE };
+enum { OP_CONST = 0, OP_X, OP_Y, OP_Z, OP_ELEM, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_HEAVISIDE, OP_FIELD };
 
 /* same memory layout as fg_instr / fg_expr / fg_term_desc of the C ABI, so
  * the tests can pass the product's term descriptors unchanged */
@@ -99,7 +99,10 @@ static int or_dof_row(const or_bucket *b, int t, uint64_t idx, uint64_t *row, cp
  * (src/function/ScalarFunction.cpp:203-223; nullary x/y/z/constant
  * src/function/executionTree/nullaryOperations.h:284-345,1399-1484; heaviside
  * src/function/executionTree/unaryOperations.h:1008-1021) */
-static cplx eval_expr(const or_expr *ex, int64_t e, const double *x) {
+/* phi: the bucket's scalar basis values at the point (nb of them), for the
+ * field-node op: u(x) = sum_j phi_j u_e[j] with the element's DOF values u_e
+ * (fieldOperations.h:160-170, Form0 field evaluated on the gauss points) */
+static cplx eval_expr(const or_expr *ex, int64_t e, const double *x, const double *phi, int nb) {
   cplx st[16];
   int sp = 0;
   for (int k = 0; k < ex->n_code; ++k) {
@@ -110,6 +113,13 @@ static cplx eval_expr(const or_expr *ex, int64_t e, const double *x) {
       case OP_Y: st[sp++] = x[1]; break;
       case OP_Z: st[sp++] = x[2]; break;
       case OP_ELEM: st[sp++] = ex->elem_values[in->arg][2 * e] + I * ex->elem_values[in->arg][2 * e + 1]; break;
+      case OP_FIELD: {
+        const double *u = ex->elem_values[in->arg] + 2 * (size_t)e * nb;
+        cplx s = 0.0;
+        for (int j = 0; phi && j < nb; ++j) s += phi[j] * (u[2 * j] + I * u[2 * j + 1]);
+        st[sp++] = s;
+        break;
+      }
       case OP_NEG: st[sp - 1] = -st[sp - 1]; break;
       case OP_HEAVISIDE: {
         double r = creal(st[sp - 1]);
@@ -289,8 +299,8 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
         double J[9], xq[3];
         double det = or_jacobian(b, e, q, J, xq);
         if (or_jacmod_apply(&T->jacmod, xq, J, &det)) or_jacmod_err = 1;
-        cplx f = eval_expr(&T->coef, e, xq);
         const double *bf = b->bval + ((size_t)o * nq + q) * nb;
+        cplx f = eval_expr(&T->coef, e, xq, bf, nb);
         for (int i = 0; i < nb; ++i)
           for (int c = 0; c < mult; ++c) be[i * mult + c] += b->w[q] * det * conj(bf[i]) * f;
       }
@@ -303,7 +313,8 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
       double det = or_jacobian(b, e, q, J, xq);
       if (or_jacmod_apply(&T->jacmod, xq, J, &det)) or_jacmod_err = 1;
       const double wd = b->w[q] * det;
-      cplx c = eval_expr(&T->coef, e, xq);
+      const double *ph = b->form == 0 ? b->bval + ((size_t)o * nq + q) * nb : NULL;
+      cplx c = eval_expr(&T->coef, e, xq, ph, nb);
       if (T->kind == TERM_MASS && b->form == 1) {
         /* FieldEvaluator<Form1>: J^-T applied to the vector values */
         or_form1(J, b->bval + ((size_t)o * nq + q) * nb * 3, nb, G);
@@ -340,7 +351,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
         static const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
         cplx D[3][3];
         for (int k = 0; k < 6; ++k) {
-          const cplx d = c * eval_expr(&T->tensor[k], e, xq);
+          const cplx d = c * eval_expr(&T->tensor[k], e, xq, ph, nb);
           D[ab[k][0]][ab[k][1]] = D[ab[k][1]][ab[k][0]] = d;
         }
         or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
@@ -365,7 +376,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
         /* (C : grad u) : grad v with grad u_{a,k} = d u_a / d x_k: for unknown
          * DOF (j, beta) the field is the 3x3 matrix D with D[beta][k] = G[k][j];
          * C : D = lambda tr(D) I + mu (D + D^T) */
-        cplx lam = c, mu = eval_expr(&T->coef2, e, xq);
+        cplx lam = c, mu = eval_expr(&T->coef2, e, xq, ph, nb);
         or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
         for (int ii = 0; ii < n; ++ii)
           for (int jj = 0; jj < n; ++jj) {
