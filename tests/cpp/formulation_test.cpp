@@ -6,7 +6,8 @@
 // a Hermitian left-hand side for real wavenumbers, consistent nonzero counts)
 // and its exact integrals of 1 over simple domains (:77-118), here as the
 // exact energies u^T A u of u = 1 and u = x. A second formulation with a
-// TensorFunction coefficient checks the energies x_a^T A x_b = D_ab.
+// TensorFunction coefficient checks the energies x_a^T A x_b = D_ab, and a
+// field-node coefficient u = x is checked against the point function x.
 //
 // Usage: formulation_test [--cpu]   (--cpu: pre() checks only, no GPU)
 // Exit status 0 when every check passes.
@@ -176,6 +177,51 @@ int main(int argc, char **argv) {
                 B == &B64 ? "FP64" : "mixed");
         }
     fg_plan_destroy(plan);
+  }
+
+  // field node (Picard-style coefficient): u = x given by its values at the
+  // element DOFs (vertex functions; zero on the higher hierarchical ones)
+  // against the point function x, in the mass term of a second field
+  {
+    Field w1("w1", omega, SpaceType::HierarchicalH1, 2, 1, 0), w2("w2", omega, SpaceType::HierarchicalH1, 2, 1, 0);
+    Formulation byPoint("by-point");
+    byPoint.integral(Function::x() * dof(w1), tf(w1), omega, "Gauss5");
+    byPoint.pre(mesh);
+    byPoint.descs(&md, &rd, &sd, &sys);
+    const int64_t E = md.n_elements;
+    const int nd = sd.n_basis;
+    std::vector<double> xv(byPoint.nUnknown, 0.0);
+    for (const Dof &d : byPoint.field->dofs.pool)
+      if ((d.assembleType == 2 || d.assembleType == 3) && d.numType == 0) xv[d.numDof - 1] = mesh.xyz[3 * (d.entity - 1)];
+    std::vector<std::complex<double>> ue((size_t)E * nd);
+    for (int64_t e = 0; e < E; ++e)
+      for (int j = 0; j < nd; ++j) {
+        const int32_t t = sys.elem_dof_type[e * nd + j];
+        ue[e * nd + j] = (t == FG_AT_UNKNOWN || t == FG_AT_UNKNOWN_BUBBLE) ? xv[sys.elem_dof_idx[e * nd + j]] : 0.0;
+      }
+    Formulation byField("by-field");
+    byField.integral(Function::fieldValues(ue) * dof(w2), tf(w2), omega, "Gauss5");
+    byField.pre(mesh);
+    std::vector<std::complex<double>> P, F;
+    for (Formulation *f : {&byPoint, &byField}) {
+      f->descs(&md, &rd, &sd, &sys);
+      st = fg_plan_create(&md, &rd, &sd, &sys, &plan);
+      CHECK(st == FG_OK, "fg_plan_create (%s): %s", f == &byPoint ? "point" : "field", fg_last_error());
+      if (st != FG_OK) continue;
+      std::vector<std::complex<double>> &A = f == &byPoint ? P : F;
+      A.assign(f->ai.back(), 0.0);
+      st = fg_assemble_fp64(plan, f->termDescs.data(), (int)f->termDescs.size(), 0.0, nullptr, reinterpret_cast<double *>(A.data()),
+                            nullptr, nullptr);
+      CHECK(st == FG_OK, "fg_assemble_fp64 (%s): %s", f == &byPoint ? "point" : "field", fg_last_error());
+      fg_plan_destroy(plan);
+    }
+    double dmax = 0.0, amax = 0.0;
+    CHECK(P.size() == F.size() && byPoint.aj == byField.aj, "same pattern for both fields");
+    for (size_t k = 0; k < std::min(P.size(), F.size()); ++k) {
+      dmax = std::max(dmax, std::abs(P[k] - F[k]));
+      amax = std::max(amax, std::abs(P[k]));
+    }
+    CHECK(dmax <= 1e-12 * amax, "field node u = x against the point function x: %g", dmax / amax);
   }
   std::printf("%s\n", failures ? "FAILED" : "OK");
   return failures ? 1 : 0;

@@ -153,3 +153,30 @@ def test_buffers_reused_across_array_sizes(femg, oracle, cuda):
     for terms, ref in [((own, nown), ref_own), ((tf, ntf), ref_f), ((own, nown), ref_own), ((tf, ntf), ref_f)]:
         v, _ = plan.assemble("fp64", terms=terms, rhs=False)
         assert rel(v, ref) <= FP64_TOL
+
+
+def test_batch_and_multi_frequency(femg, oracle, cuda):
+    """Field coefficients through fg_batch (FP64; the mixed batch refuses
+    them) and fg_assemble_multi_freq (mass with a second time derivative)."""
+    prob = problem(femg, 2)
+    a = prob.arrays()
+    u = random_field(a, seed=6)
+    O = femg
+    code = {O.FG_TERM_MASS: [(O.FG_OP_FIELD, 0, 0.0, 0.0)], O.FG_TERM_GRAD_GRAD: [(O.FG_OP_CONST, 0, 1.0, 0.0)],
+            O.FG_TERM_SOURCE: [(O.FG_OP_FIELD, 0, 0.0, 0.0)]}
+    t, nt = field_terms(femg, prob, lambda k: code[k], [u])
+    plan = prob.plan()
+    femg.check(femg.lib().fg_plan_bind_terms(plan.ptr, t, nt, 0.0))
+    ref_v, _ = oracle.assemble(a, t, nt, with_rhs=False)
+    vals, _ = femg.Batch([plan], mixed=False, bound=True).run()
+    assert rel(vals[0], ref_v) <= FP64_TOL
+    with pytest.raises(femg.FgError) as err:
+        femg.Batch([plan], mixed=True, bound=True)
+    assert err.value.status == femg.FG_ERR_UNSUPPORTED
+    mass = [k for k in range(nt) if t[k].kind == femg.FG_TERM_MASS][0]
+    t[mass].dt = femg.FG_DT_2
+    omegas = [1.0, 2.5]
+    mv, mr = plan.assemble_multi_freq(omegas, terms=(t, nt))
+    for f, om in enumerate(omegas):
+        rv, rb = oracle.assemble(a, t, nt, freq=om)
+        assert rel(mv[f], rv) <= FP64_TOL and rel(mr[f], rb) <= FP64_TOL
