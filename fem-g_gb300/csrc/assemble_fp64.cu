@@ -302,14 +302,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
 // Lowest-order-and-up HCurl field (FG_FORM_1): with the Form1 values
 // P = J^-T v and the Form2 curls C = J c / det (FieldEvaluator<Form1/Form2>,
 // src/term/evaluator/FieldEvaluator.h:59-105),
-//   Ke[i][j] = sum_q w det (c_curl C_j . C_i + c_m P_j . P_i).
+//   Ke[i][j] = sum_q w det (c_curl C_j . C_i + c_m P_j . P_i),
+// or, with tensor terms (TensorFunction * curl, TensorFunction * dof: the
+// Maxwell PML), sum_q w det (C_i . A C_j + P_i . B P_j) with A = c_curl I + c D.
 // Warp per element, lanes over the pairs i <= j; the matrix is symmetric.
 struct HcurlWarpSmem {
   double X[kMaxNodes * 3];
   double J0[9], J[9], Jinv[9];
   double det0, det;
   double2 a, b;  // w det c_curl, w det c_m
+  double2 Aw[6], Bw[6];  // w det times the curl and mass coefficient tensors (tensor terms)
   double C[3][kMaxDofs], P[3][kMaxDofs];
+  double Cs[2][3][kMaxDofs], Ps[2][3][kMaxDofs];  // tensor terms: (w det A) C, (w det B) P (real, imaginary)
 };
 
 template <int MAXENT, bool CPLX>
@@ -331,6 +335,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
   }
   __syncthreads();
   HcurlWarpSmem &S = smem[warp];
+  const bool tensor = terms->tensorTerm >= 0 || terms->tensorMassTerm >= 0;
   const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlockElem;
   for (int64_t e = (int64_t)blockIdx.x * kWarpsPerBlockElem + warp; e < p.E; e += stride) {
     const int o = p.orient ? p.orient[e] : 0;
@@ -356,15 +361,39 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         const double wd = p.w[q] * S.det;
         S.a = make_double2(wd * cc.x, wd * cc.y);
         S.b = make_double2(wd * cm.x, wd * cm.y);
+        if (tensor) {
+          double2 A[6], B[6];
+          coefTensor(terms, terms->tensorTerm, terms->tensor, g, e, xq, cc, A);
+          coefTensor(terms, terms->tensorMassTerm, terms->tensorMass, g, e, xq, cm, B);
+          for (int k = 0; k < 6; ++k) {
+            S.Aw[k] = make_double2(wd * A[k].x, wd * A[k].y);
+            S.Bw[k] = make_double2(wd * B[k].x, wd * B[k].y);
+          }
+        }
       }
       __syncwarp();
       const size_t base = ((size_t)o * p.nq + q) * p.nb;
       for (int i = lane; i < n; i += 32) {
         const double *cr = p.bgrad + 3 * (base + i), *vr = p.bval + 3 * (base + i);
+        double Ci[3], Pi[3];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-          S.C[r][i] = (S.J[r] * cr[0] + S.J[3 + r] * cr[1] + S.J[6 + r] * cr[2]) / S.det;
-          S.P[r][i] = S.Jinv[r] * vr[0] + S.Jinv[3 + r] * vr[1] + S.Jinv[6 + r] * vr[2];
+          Ci[r] = (S.J[r] * cr[0] + S.J[3 + r] * cr[1] + S.J[6 + r] * cr[2]) / S.det;
+          Pi[r] = S.Jinv[r] * vr[0] + S.Jinv[3 + r] * vr[1] + S.Jinv[6 + r] * vr[2];
+          S.C[r][i] = Ci[r];
+          S.P[r][i] = Pi[r];
+        }
+        if (tensor) {
+          const int row[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            S.Cs[0][r][i] = S.Aw[row[r][0]].x * Ci[0] + S.Aw[row[r][1]].x * Ci[1] + S.Aw[row[r][2]].x * Ci[2];
+            S.Ps[0][r][i] = S.Bw[row[r][0]].x * Pi[0] + S.Bw[row[r][1]].x * Pi[1] + S.Bw[row[r][2]].x * Pi[2];
+            if (CPLX) {
+              S.Cs[1][r][i] = S.Aw[row[r][0]].y * Ci[0] + S.Aw[row[r][1]].y * Ci[1] + S.Aw[row[r][2]].y * Ci[2];
+              S.Ps[1][r][i] = S.Bw[row[r][0]].y * Pi[0] + S.Bw[row[r][1]].y * Pi[1] + S.Bw[row[r][2]].y * Pi[2];
+            }
+          }
         }
       }
       __syncwarp();
@@ -373,10 +402,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         const int k = lane + 32 * m;
         if (k < nEnt) {
           const int i = pairI[k], j = pairJ[k];
-          const double cc = S.C[0][i] * S.C[0][j] + S.C[1][i] * S.C[1][j] + S.C[2][i] * S.C[2][j];
-          const double pp = S.P[0][i] * S.P[0][j] + S.P[1][i] * S.P[1][j] + S.P[2][i] * S.P[2][j];
-          accR[m] += S.a.x * cc + S.b.x * pp;
-          if (CPLX) accI[m] += S.a.y * cc + S.b.y * pp;
+          if (tensor) {
+            accR[m] += S.C[0][i] * S.Cs[0][0][j] + S.C[1][i] * S.Cs[0][1][j] + S.C[2][i] * S.Cs[0][2][j] +
+                       S.P[0][i] * S.Ps[0][0][j] + S.P[1][i] * S.Ps[0][1][j] + S.P[2][i] * S.Ps[0][2][j];
+            if (CPLX)
+              accI[m] += S.C[0][i] * S.Cs[1][0][j] + S.C[1][i] * S.Cs[1][1][j] + S.C[2][i] * S.Cs[1][2][j] +
+                         S.P[0][i] * S.Ps[1][0][j] + S.P[1][i] * S.Ps[1][1][j] + S.P[2][i] * S.Ps[1][2][j];
+          } else {
+            const double cc = S.C[0][i] * S.C[0][j] + S.C[1][i] * S.C[1][j] + S.C[2][i] * S.C[2][j];
+            const double pp = S.P[0][i] * S.P[0][j] + S.P[1][i] * S.P[1][j] + S.P[2][i] * S.P[2][j];
+            accR[m] += S.a.x * cc + S.b.x * pp;
+            if (CPLX) accI[m] += S.a.y * cc + S.b.y * pp;
+          }
         }
       }
       __syncwarp();

@@ -453,13 +453,31 @@ __device__ __forceinline__ void factorsHcurl(const PlanDev &p, const DevTerms *_
     else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xc)));
   }
   const int64_t r0 = (int64_t)rankOf[e] * rowsPerElem + rowOff;
+  // tensor terms (Maxwell PML): (J^T A J)(a, b) / det for the curls and
+  // det (J^-1 B J^-T)(a, b) for the values, in place of c M / det and c det K
+  const bool tensor = terms->tensorTerm >= 0 || terms->tensorMassTerm >= 0;
+  double2 A6[6], B6[6];
+  if (tensor) {
+    coefTensor(terms, terms->tensorTerm, terms->tensor, 0, e, xc, cc, A6);
+    coefTensor(terms, terms->tensorMassTerm, terms->tensorMass, 0, e, xc, cm, B6);
+  }
   for (int comp = 0; comp < ncomp; ++comp) {
     const double gc = (comp == 0 ? cc.x : cc.y) / det, gm = (comp == 0 ? cm.x : cm.y) * det;
     float hi[kKpE], lo[kKpE];
+    if (tensor) {
+      double FA[6], FB[6];
+      congruence6(J, A6, comp, FA);
+      congruence6(Ji, B6, comp, FB);
+      for (int k = 0; k < 6; ++k) {
+        splitTf32Dev(FA[k] / det, hi[k], lo[k]);
+        splitTf32Dev(FB[k] * det, hi[6 + k], lo[6 + k]);
+      }
+    } else {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      splitTf32Dev(gc * M[k], hi[k], lo[k]);
-      splitTf32Dev(gm * K[k], hi[6 + k], lo[6 + k]);
+      for (int k = 0; k < 6; ++k) {
+        splitTf32Dev(gc * M[k], hi[k], lo[k]);
+        splitTf32Dev(gm * K[k], hi[6 + k], lo[6 + k]);
+      }
     }
 #pragma unroll
     for (int k = 12; k < kKpE; ++k) hi[k] = lo[k] = 0.0f;

@@ -79,10 +79,13 @@ struct DevTerms {
   int32_t nMod;        // distinct Jacobian modificators of the terms (>= 1; FG_JACMOD_NONE counts)
   int32_t hasJacMod;   // some term has a modificator other than FG_JACMOD_NONE
   int32_t tensorTerm;  // index of the FG_TERM_GRAD_GRAD_TENSOR term (at most one), -1 when none
-  int32_t tensorPoint; // some entry of that tensor depends on the point
+  int32_t tensorMassTerm;  // index of the FG_TERM_MASS_TENSOR term (HCurl; at most one), -1 when none
+  int32_t tensorPoint; // some entry of those tensors depends on the point
+  int32_t pad_;
   DevTerm t[kMaxTerms];
   DevJacMod mods[kMaxTerms];
-  DevExpr tensor[6];   // entries (00, 11, 22, 01, 02, 12) of the symmetric tensor
+  DevExpr tensor[6];   // entries (00, 11, 22, 01, 02, 12) of the grad-grad (curl-curl) term's symmetric tensor
+  DevExpr tensorMass[6];  // the same for the mass term's tensor
 };
 
 // Device-resident data of one element bucket
@@ -357,16 +360,40 @@ __device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x
   return st[0];
 }
 
-// Diffusion tensor of the grad-grad terms of modificator group g at element e
-// and point x: A = cgg I + factor c D, with cgg the summed scalar grad-grad
-// coefficients and D the tensor term's entries (00, 11, 22, 01, 02, 12).
-__device__ inline void diffusionTensor(const DevTerms *terms, int g, int64_t e, const double *x, double2 cgg, double2 *A,
-                                       const double *phi = nullptr, int nb = 0) {
-  for (int k = 0; k < 6; ++k) A[k] = k < 3 ? cgg : make_double2(0.0, 0.0);
-  const DevTerm &T = terms->t[terms->tensorTerm];
+// Coefficient tensor of modificator group g at element e and point x:
+// A = c0 I + factor c D, with c0 the summed scalar coefficients of the same
+// kind and D the entries (00, 11, 22, 01, 02, 12) of tensor term `term`
+// (none when term < 0).
+__device__ inline void coefTensor(const DevTerms *terms, int term, const DevExpr *D, int g, int64_t e, const double *x, double2 c0,
+                                  double2 *A, const double *phi = nullptr, int nb = 0) {
+  for (int k = 0; k < 6; ++k) A[k] = k < 3 ? c0 : make_double2(0.0, 0.0);
+  if (term < 0) return;
+  const DevTerm &T = terms->t[term];
   if (T.mod != g) return;
   const double2 fc = cmul(T.factor, evalExpr(T.coef, e, x, phi, nb));
-  for (int k = 0; k < 6; ++k) A[k] = cadd(A[k], cmul(fc, evalExpr(terms->tensor[k], e, x, phi, nb)));
+  for (int k = 0; k < 6; ++k) A[k] = cadd(A[k], cmul(fc, evalExpr(D[k], e, x, phi, nb)));
+}
+// the grad-grad (diffusion) tensor
+__device__ inline void diffusionTensor(const DevTerms *terms, int g, int64_t e, const double *x, double2 cgg, double2 *A,
+                                       const double *phi = nullptr, int nb = 0) {
+  coefTensor(terms, terms->tensorTerm, terms->tensor, g, e, x, cgg, A, phi, nb);
+}
+// F(a, b) = sum_rs Q[3a + r] A(r, s) Q[3b + s] for the six pairs (a, b), of
+// the real (comp 0) or imaginary (comp 1) part of the symmetric A
+__device__ inline void congruence6(const double *Q, const double2 *A6, int comp, double *F) {
+  const int sym[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+  const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  double QA[9];
+  for (int a = 0; a < 3; ++a)
+    for (int s = 0; s < 3; ++s) {
+      double v = 0.0;
+      for (int r = 0; r < 3; ++r) v += Q[3 * a + r] * (comp == 0 ? A6[sym[r][s]].x : A6[sym[r][s]].y);
+      QA[3 * a + s] = v;
+    }
+  for (int k = 0; k < 6; ++k) {
+    const int a = ab[k][0], b = ab[k][1];
+    F[k] = QA[3 * a] * Q[3 * b] + QA[3 * a + 1] * Q[3 * b + 1] + QA[3 * a + 2] * Q[3 * b + 2];
+  }
 }
 
 // Jacobian at a quadrature point from the geometric nodes, stored column-major

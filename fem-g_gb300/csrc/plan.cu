@@ -627,12 +627,13 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
   out->n = nTerms;
   out->nMod = 0;
   out->tensorTerm = -1;
+  out->tensorMassTerm = -1;
   for (int t = 0; t < nTerms; ++t) {
     const fg_term_desc &src = terms[t];
     DevTerm &dt = out->t[t];
     dt.kind = src.kind;
     dt.dt = src.dt;
-    if (src.kind < FG_TERM_GRAD_GRAD || src.kind > FG_TERM_GRAD_GRAD_TENSOR) {
+    if (src.kind < FG_TERM_GRAD_GRAD || src.kind > FG_TERM_MASS_TENSOR) {
       setLastError("unknown term kind");
       return FG_ERR_ARG;
     }
@@ -644,8 +645,12 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
       setLastError("HCurl fields take the curl-curl and mass terms");
       return FG_ERR_UNSUPPORTED;
     }
-    if (src.kind == FG_TERM_GRAD_GRAD_TENSOR && (plan->d.form != FG_FORM_0 || plan->d.mult != 1)) {
-      setLastError("the tensor grad-grad term needs a scalar H1 field");
+    if (src.kind == FG_TERM_GRAD_GRAD_TENSOR && plan->d.mult != 1) {
+      setLastError("the tensor grad-grad term needs a scalar H1 or an HCurl field");
+      return FG_ERR_UNSUPPORTED;
+    }
+    if (src.kind == FG_TERM_MASS_TENSOR && plan->d.form != FG_FORM_1) {
+      setLastError("the tensor mass term needs an HCurl field");
       return FG_ERR_UNSUPPORTED;
     }
     if (src.kind != FG_TERM_ELASTIC && plan->d.mult != 1 && src.kind != FG_TERM_MASS) {
@@ -671,16 +676,19 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
       out->hasElastic = 1;
     }
     if (src.kind == FG_TERM_SOURCE) out->hasSource = 1;
-    if (src.kind == FG_TERM_GRAD_GRAD_TENSOR) {
-      if (out->tensorTerm >= 0 || !src.tensor) {
-        setLastError(src.tensor ? "at most one tensor grad-grad term per assembly" : "tensor grad-grad term without tensor");
+    if (src.kind == FG_TERM_GRAD_GRAD_TENSOR || src.kind == FG_TERM_MASS_TENSOR) {
+      const bool gg = src.kind == FG_TERM_GRAD_GRAD_TENSOR;
+      int32_t &slot = gg ? out->tensorTerm : out->tensorMassTerm;
+      if (slot >= 0 || !src.tensor) {
+        setLastError(src.tensor ? "at most one tensor term of each kind per assembly" : "tensor term without tensor");
         return FG_ERR_ARG;
       }
-      out->tensorTerm = t;
+      slot = t;
+      DevExpr *D = gg ? out->tensor : out->tensorMass;
       for (int k = 0; k < 6; ++k) {
-        st = devExpr(plan, src.tensor[k], &out->tensor[k], &cplx, arrays, used);
+        st = devExpr(plan, src.tensor[k], &D[k], &cplx, arrays, used);
         if (st) return st;
-        if (out->tensor[k].cls == kExprPoint) out->tensorPoint = 1;
+        if (D[k].cls == kExprPoint) out->tensorPoint = 1;
       }
     }
     // the term's Jacobian modificator: terms with equal ones share a group

@@ -165,9 +165,10 @@ enum {
   FG_TERM_MASS = 1,      /* integral(c * dof(u), tf(u)) */
   FG_TERM_ELASTIC = 2,   /* integral(C * grad(dof(u)), grad(tf(u))), C isotropic Tensor4 (lambda, mu) */
   FG_TERM_SOURCE = 3,    /* integral(f, tf(u)) : right-hand side */
-  FG_TERM_GRAD_GRAD_TENSOR = 4 /* integral(c * D * grad(dof(u)), grad(tf(u))), D a symmetric 3x3 tensor of
-                                  coefficient programs (TensorFunction * grad, EquationEvaluator tensor-left);
-                                  scalar H1 fields */
+  FG_TERM_GRAD_GRAD_TENSOR = 4, /* integral(c * D * grad(dof(u)), grad(tf(u))), D a symmetric 3x3 tensor of
+                                   coefficient programs (TensorFunction * grad, EquationEvaluator tensor-left);
+                                   scalar H1 fields; on HCurl fields the curls: integral(c * D * curl, curl) */
+  FG_TERM_MASS_TENSOR = 5        /* integral(c * D * dof(u), tf(u)) for HCurl fields (D symmetric, as above) */
 };
 enum { FG_DT_NONE = 0, FG_DT_1 = 1, FG_DT_2 = 2 }; /* dof, dt_dof, dt2_dof */
 

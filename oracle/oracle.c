@@ -30,7 +30,7 @@ typedef double complex cplx;
 /* ---------------------------------------------------------------- types */
 
 enum { AT_UNDEFINED = 0, AT_FIXED = 1, AT_UNKNOWN = 2, AT_UNKNOWN_BUBBLE = 3, AT_UNKNOWN_GLOBAL = 4 };
-enum { TERM_GRAD_GRAD = 0, TERM_MASS = 1, TERM_ELASTIC = 2, TERM_SOURCE = 3, TERM_GRAD_GRAD_TENSOR = 4 };
+enum { TERM_GRAD_GRAD = 0, TERM_MASS = 1, TERM_ELASTIC = 2, TERM_SOURCE = 3, TERM_GRAD_GRAD_TENSOR = 4, TERM_MASS_TENSOR = 5 };
 enum { OP_CONST = 0, OP_X, OP_Y, OP_Z, OP_ELEM, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_HEAVISIDE, OP_FIELD };
 
 /* same memory layout as fg_instr / fg_expr / fg_term_desc of the C ABI, so
@@ -53,7 +53,7 @@ typedef struct {
   int32_t kind, dt;
   or_expr coef, coef2;
   or_jacmod jacmod;
-  const or_expr *tensor; /* TERM_GRAD_GRAD_TENSOR: D_xx, D_yy, D_zz, D_xy, D_xz, D_yz */
+  const or_expr *tensor; /* TERM_GRAD_GRAD_TENSOR, TERM_MASS_TENSOR: D_xx, D_yy, D_zz, D_xy, D_xz, D_yz */
 } or_term;
 
 typedef struct {
@@ -345,16 +345,26 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
             if (ii % mult != jj % mult) continue;
             target[jj + ii * n] += wd * (c * phi[jj / mult]) * conj(phi[ii / mult]);
           }
-      } else if (T->kind == TERM_GRAD_GRAD_TENSOR) {
-        /* tensor-left evaluator (EquationEvaluator, TensorFunction * grad): the unknown's
-         * field is c D G_j, tested against G_i */
+      } else if (T->kind == TERM_GRAD_GRAD_TENSOR || T->kind == TERM_MASS_TENSOR) {
+        /* tensor-left evaluator (EquationEvaluator, TensorFunction * field): the unknown's
+         * field is c D G_j, tested against G_i, with G the physical gradients (H1),
+         * curls (HCurl, grad-grad kind: J / det on the reference curls) or
+         * values (HCurl, mass kind: J^-T on the reference values) */
         static const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
         cplx D[3][3];
         for (int k = 0; k < 6; ++k) {
           const cplx d = c * eval_expr(&T->tensor[k], e, xq, ph, nb);
           D[ab[k][0]][ab[k][1]] = D[ab[k][1]][ab[k][0]] = d;
         }
-        or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
+        if (b->form == 1 && T->kind == TERM_GRAD_GRAD_TENSOR) {
+          const double *cf = b->bgrad + ((size_t)o * nq + q) * nb * 3;
+          for (int i = 0; i < nb; ++i)
+            for (int r = 0; r < 3; ++r) G[r * nb + i] = (J[r] * cf[3 * i] + J[3 + r] * cf[3 * i + 1] + J[6 + r] * cf[3 * i + 2]) / det;
+        } else if (b->form == 1) {
+          or_form1(J, b->bval + ((size_t)o * nq + q) * nb * 3, nb, G);
+        } else {
+          or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
+        }
         for (int ii = 0; ii < n; ++ii)
           for (int jj = 0; jj < n; ++jj) {
             cplx s = 0.0;

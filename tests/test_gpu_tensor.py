@@ -136,14 +136,14 @@ def test_argument_checks(femg, cuda):
     with pytest.raises(femg.FgError) as err:
         plan.assemble("fp64", terms=(both, 2), rhs=False)
     assert err.value.status == femg.FG_ERR_ARG
-    # a vector (HCurl) field does not take the tensor term
-    mx = femg.Problem(femg.config(kind=femg.FG_PROBLEM_MAXWELL, dim=3, m=2, mesh_order=1, space=femg.FG_SPACE_HCURL, order=0,
-                                  gauss=2, jitter=0.1, seed=3))
-    mt, mnt = mx.terms()
+    # a compound (3-component) field does not take the tensor term
+    nav = femg.Problem(femg.config(kind=femg.FG_PROBLEM_NAVIER, dim=3, m=2, mesh_order=1, space=femg.FG_SPACE_HIERARCHICAL_H1,
+                                   order=1, gauss=2, jitter=0.15, seed=9, omega=2.0, lame_sigma=0.5))
+    nt_, nnt = nav.terms()
     tt = (femg.TermDesc * 1)()
-    C.memmove(C.byref(tt[0]), C.byref(mt[0]), C.sizeof(femg.TermDesc))
+    C.memmove(C.byref(tt[0]), C.byref(nt_[0]), C.sizeof(femg.TermDesc))
     tt[0].kind = femg.FG_TERM_GRAD_GRAD_TENSOR
     tt[0].tensor = t2[0].tensor
     with pytest.raises(femg.FgError) as err:
-        mx.plan().assemble("fp64", terms=(tt, 1), rhs=False)
+        nav.plan().assemble("fp64", terms=(tt, 1), rhs=False)
     assert err.value.status == femg.FG_ERR_UNSUPPORTED
