@@ -530,9 +530,11 @@ void Formulation::pre(const Mesh &m) {
       d.coef = (t.unknown.coef * t.unknown.C.lambda).toExpr();
       d.coef2 = (t.unknown.coef * t.unknown.C.mu).toExpr();
     } else if (t.unknown.tensor2) {
-      if (!t.unknown.grad) throw std::invalid_argument("a tensor function multiplies gradients");
+      // D * grad (H1), D * curl (HCurl) or D * dof (HCurl values)
+      if (!t.unknown.grad && t.unknown.field->fs.form() != 1)
+        throw std::invalid_argument("a tensor function multiplies gradients, curls or HCurl values");
       const TensorFunction &D = t.unknown.D;
-      d.kind = FG_TERM_GRAD_GRAD_TENSOR;
+      d.kind = t.unknown.grad ? FG_TERM_GRAD_GRAD_TENSOR : FG_TERM_MASS_TENSOR;
       d.coef = t.unknown.coef.toExpr();
       tensorExprs.push_back({D.xx.toExpr(), D.yy.toExpr(), D.zz.toExpr(), D.xy.toExpr(), D.xz.toExpr(), D.yz.toExpr()});
       d.tensor = tensorExprs.back().data();
