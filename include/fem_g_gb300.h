@@ -204,7 +204,7 @@ typedef struct {
   fg_expr coef; /* c, f, or lambda for FG_TERM_ELASTIC */
   fg_expr coef2; /* mu for FG_TERM_ELASTIC */
   fg_jacmod jacmod; /* all zero: none */
-  const fg_expr *tensor; /* FG_TERM_GRAD_GRAD_TENSOR: [6] programs of D_xx, D_yy, D_zz, D_xy, D_xz, D_yz */
+  const fg_expr *tensor; /* FG_TERM_GRAD_GRAD_TENSOR, FG_TERM_MASS_TENSOR: [6] programs of D_xx, D_yy, D_zz, D_xy, D_xz, D_yz */
 } fg_term_desc;
 
 /* ------------------------------------------------------------- plan / run */
