@@ -555,6 +555,10 @@ int prepareOutputs(fg_plan *plan, double *csr_values, double *rhs, Outputs *o) {
     return FG_ERR_ARG;
   }
   o->hostValues = !isDevicePointer(csr_values);
+  if (plan->accumulate && (o->hostValues || (rhs && !isDevicePointer(rhs)))) {
+    setLastError("accumulating assembly adds into device outputs: csr_values and rhs must be device memory");
+    return FG_ERR_ARG;
+  }
   o->values = csr_values;
   if (o->hostValues) {
     int st = ensureDevice((void **)&plan->values, &plan->valuesBytes, plan->d.nnz * 16);

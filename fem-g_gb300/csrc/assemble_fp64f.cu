@@ -214,6 +214,15 @@ extern "C" int fg_plan_set_fp64_method(fg_plan *plan, int32_t method) {
   return FG_OK;
 }
 
+extern "C" int fg_plan_set_accumulate(fg_plan *plan, int32_t accumulate) {
+  if (!plan || (accumulate != 0 && accumulate != 1)) {
+    femg::setLastError("fg_plan_set_accumulate: invalid arguments");
+    return FG_ERR_ARG;
+  }
+  plan->accumulate = accumulate;
+  return FG_OK;
+}
+
 extern "C" void fp64fDestroy(fg_plan *plan) {
   femg::FactoredState *f = (femg::FactoredState *)plan->fp64f;
   if (!f) return;

@@ -1282,6 +1282,10 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
     setLastError("mixed path: Jacobian modificators make the geometry point-dependent; use the FP64 path");
     return FG_ERR_UNSUPPORTED;
   }
+  if (report && plan->accumulate) {
+    setLastError("mixed path: the error report compares overwritten values; the plan accumulates");
+    return FG_ERR_ARG;
+  }
   if ((st = prepareMixed(plan, dt.complexKe ? 2 : 1, 1))) return st;
   if ((st = checkTimeout(state(plan), false))) return st;  // a timeout of an earlier call
   const double *uD = nullptr;

@@ -363,6 +363,11 @@ extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const 
     setLastError("fg_batch_create: 1..4096 plans required");
     return FG_ERR_ARG;
   }
+  for (int32_t q = 0; q < n_problems; ++q)
+    if (plans[q] && plans[q]->accumulate) {
+      setLastError("fg_batch_create: a plan accumulates into shared outputs; batches overwrite theirs");
+      return FG_ERR_UNSUPPORTED;
+    }
   fg_batch *b = new (std::nothrow) fg_batch;
   if (!b) return FG_ERR_OOM;
   auto fail = [&](int st) {

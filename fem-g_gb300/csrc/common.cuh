@@ -159,6 +159,7 @@ struct fg_plan {
   // FP64 factorization state (reference tensors, tiles), see assemble_fp64f.cu
   void *fp64f = nullptr;
   int fp64Method = 0;  // FG_FP64_* (FG_FP64_QUADRATURE)
+  int accumulate = 0;  // add into device outputs instead of overwriting them (fg_plan_set_accumulate)
   int *jmErrHost = nullptr;  // pinned copy of d.jmErr
 };
 

@@ -19,7 +19,7 @@ namespace femg {
 
 // The rows of one plan handled by block `blk` of `nblk` (grid-stride over row
 // groups of rowsPerBlock rows).
-template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J>
+template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J, bool ACC>
 __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restrict__ ke, const double2 *__restrict__ be,
                                            const double2 *__restrict__ uD, double2 *__restrict__ values,
                                            double2 *__restrict__ rhs, int rowsPerBlock, KeLayout lay, int64_t blk, int64_t nblk,
@@ -136,8 +136,12 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
       }
       flat = flatN;
     }
-    for (int s = lt; s < len; s += L)
-      values[start + s] = make_double2(widen(A[s * SS]), KCPLX ? widen(A[s * SS + 1]) : 0.0);
+    // ACC: add into the values (several buckets sharing rows) instead of overwriting them
+    for (int s = lt; s < len; s += L) {
+      double2 v = make_double2(widen(A[s * SS]), KCPLX ? widen(A[s * SS + 1]) : 0.0);
+      if (ACC) v = cadd(values[start + s], v);
+      values[start + s] = v;
+    }
     if (rhs) {
       if (uD) {  // Dirichlet lifting present: reduce the lanes' lifted terms
 #pragma unroll
@@ -145,20 +149,20 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
           dc.x += __shfl_down_sync(0xffffffffu, dc.x, off, L);
           dc.y += __shfl_down_sync(0xffffffffu, dc.y, off, L);
         }
-        if (live && lt == 0) rhs[row] = cadd(bsum, dc);
+        if (live && lt == 0) rhs[row] = ACC ? cadd(rhs[row], cadd(bsum, dc)) : cadd(bsum, dc);
       } else if (live && lt == 0) {
-        rhs[row] = bsum;
+        rhs[row] = ACC ? cadd(rhs[row], bsum) : bsum;
       }
     }
     __syncwarp();
   }
 }
 
-template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J>
+template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J, bool ACC>
 __global__ void __launch_bounds__(256)
     k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
              double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock, KeLayout lay, int64_t v0, int64_t v1) {
-  gatherRows<SlotT, KCPLX, KT, AT, L, J>(p, ke, be, uD, values, rhs, rowsPerBlock, lay, blockIdx.x, gridDim.x, v0, v1);
+  gatherRows<SlotT, KCPLX, KT, AT, L, J, ACC>(p, ke, be, uD, values, rhs, rowsPerBlock, lay, blockIdx.x, gridDim.x, v0, v1);
 }
 
 // Many plans in one launch: job q owns blocks [blockStart, blockStart + nBlocks)
@@ -171,13 +175,13 @@ __global__ void __launch_bounds__(256) k_gather_batch(const GatherJob *__restric
     else hi = mid - 1;
   }
   const GatherJob &Jb = jobs[lo];
-  gatherRows<SlotT, KCPLX, KT, AT, L, J>(Jb.p, (const KT *)Jb.ke, Jb.be, Jb.uD, Jb.values, Jb.rhs, rowsPerBlock, Jb.lay,
+  gatherRows<SlotT, KCPLX, KT, AT, L, J, false>(Jb.p, (const KT *)Jb.ke, Jb.be, Jb.uD, Jb.values, Jb.rhs, rowsPerBlock, Jb.lay,
                                          (int64_t)blockIdx.x - Jb.blockStart, Jb.nBlocks, 0, (int64_t)Jb.p.nRows);
 }
 
 template <typename SlotT, bool KCPLX, typename KT>
 static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, const double2 *uD, double2 *values, double2 *rhs,
-                       KeLayout lay, int64_t v0, int64_t v1, cudaStream_t s) {
+                       KeLayout lay, int64_t v0, int64_t v1, bool acc, cudaStream_t s) {
   using AT = KT;  // FP32 element matrices accumulate in FP32, FP64 ones in FP64
   const GatherShape shape = gatherShape(p.n, p.maxRowLen, KCPLX ? 1 : 0, sizeof(KT) == 4 ? 1 : 0, 0, 0);
   const int L = shape.L, J = shape.J;
@@ -195,16 +199,20 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
   int64_t blocks = (v1 - v0 + rowsPerBlock - 1) / rowsPerBlock;
   blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)sms * 16));
   bool launched = false;
-#define FG_GATHER_L(LL, JJ)                                                                                       \
-  if (L == LL && J == JJ) {                                                                                       \
-    launched = true;                                                                                              \
-    auto kern = k_gather<SlotT, KCPLX, KT, AT, LL, JJ>;                                                           \
+#define FG_GATHER_K(LL, JJ, AA)                                                                                   \
+  {                                                                                                               \
+    auto kern = k_gather<SlotT, KCPLX, KT, AT, LL, JJ, AA>;                                                       \
     static size_t smemSet = 0;                                                                                    \
     if (smem > smemSet) {                                                                                         \
       FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                \
       smemSet = smem;                                                                                             \
     }                                                                                                             \
     kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock, lay, v0, v1); \
+  }
+#define FG_GATHER_L(LL, JJ)                                                                                       \
+  if (L == LL && J == JJ) {                                                                                       \
+    launched = true;                                                                                              \
+    if (acc) FG_GATHER_K(LL, JJ, true) else FG_GATHER_K(LL, JJ, false)                                            \
   }
   FG_GATHER_L(2, 3)
   FG_GATHER_L(4, 3)
@@ -213,6 +221,7 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
   FG_GATHER_L(16, 3)
   FG_GATHER_L(32, 3)
 #undef FG_GATHER_L
+#undef FG_GATHER_K
   if (!launched) {
     setLastError("gather: no kernel for this (lanes, columns) shape");
     return FG_ERR_UNSUPPORTED;
@@ -223,7 +232,8 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
 
 // The rows of visit records [v0, v1) (all rows: 0, nRows).
 static int launchGatherRange(const PlanDev &p, const double *ke, int keComplex, int keIsFloat, KeLayout lay, const double *be,
-                             const double *dirichletDev, double *values, double *rhs, int64_t v0, int64_t v1, cudaStream_t s) {
+                             const double *dirichletDev, double *values, double *rhs, int64_t v0, int64_t v1, bool acc,
+                             cudaStream_t s) {
   if (v1 <= v0) return FG_OK;
   if (p.lscale && !keComplex) {
     setLastError("gather: linked DOFs need complex element matrices");
@@ -237,17 +247,18 @@ static int launchGatherRange(const PlanDev &p, const double *ke, int keComplex, 
   countLaunch();
   if (p.slotBytes == 1) {
     if (keIsFloat)
-      return keComplex ? launchTyped<uint8_t, true, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, s) : launchTyped<uint8_t, false, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, s);
-    return keComplex ? launchTyped<uint8_t, true, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, s) : launchTyped<uint8_t, false, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, s);
+      return keComplex ? launchTyped<uint8_t, true, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, acc, s) : launchTyped<uint8_t, false, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, acc, s);
+    return keComplex ? launchTyped<uint8_t, true, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, acc, s) : launchTyped<uint8_t, false, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, acc, s);
   }
   if (keIsFloat)
-    return keComplex ? launchTyped<uint16_t, true, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, s) : launchTyped<uint16_t, false, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, s);
-  return keComplex ? launchTyped<uint16_t, true, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, s) : launchTyped<uint16_t, false, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, s);
+    return keComplex ? launchTyped<uint16_t, true, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, acc, s) : launchTyped<uint16_t, false, float>(p, ke, be2, uD, v2, r2, lay, v0, v1, acc, s);
+  return keComplex ? launchTyped<uint16_t, true, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, acc, s) : launchTyped<uint16_t, false, double>(p, ke, be2, uD, v2, r2, lay, v0, v1, acc, s);
 }
 
 int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, KeLayout lay, const double *be,
                  const double *dirichletDev, double *values, double *rhs, cudaStream_t s) {
-  return launchGatherRange(plan->d, ke, keComplex, keIsFloat, lay, be, dirichletDev, values, rhs, 0, (int64_t)plan->d.nRows, s);
+  return launchGatherRange(plan->d, ke, keComplex, keIsFloat, lay, be, dirichletDev, values, rhs, 0, (int64_t)plan->d.nRows,
+                           plan->accumulate != 0, s);
 }
 
 // Host values: the reduction runs range by range; after each range an event
@@ -268,7 +279,7 @@ int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloa
   pr.visitElem = plan->visitElemRanged;
   for (size_t c = 0; c < nc; ++c) {
     const uint64_t r0 = plan->outChunkRow[c], r1 = plan->outChunkRow[c + 1];
-    int st = launchGatherRange(pr, ke, keComplex, keIsFloat, lay, be, dirichletDev, o.values, o.rhs, (int64_t)r0, (int64_t)r1, s);
+    int st = launchGatherRange(pr, ke, keComplex, keIsFloat, lay, be, dirichletDev, o.values, o.rhs, (int64_t)r0, (int64_t)r1, false, s);
     if (st) return st;
     FG_CUDA(cudaEventRecord(plan->copyEvents[c], s));
     FG_CUDA(cudaStreamWaitEvent(plan->copyStream, plan->copyEvents[c], 0));

@@ -287,6 +287,10 @@ int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t
               const std::function<int(const int *, int, double2 *, double2 *)> &coefOf) {
   MultiState *m = multiState(plan);
   const PlanDev &p = plan->d;
+  if (plan->accumulate) {
+    setLastError("several frequencies / separate matrices: the plan accumulates; assemble one frequency at a time");
+    return FG_ERR_UNSUPPORTED;
+  }
   if (p.lscale) {
     setLastError("several frequencies / separate matrices: plans with linked DOFs are assembled one frequency at a time");
     return FG_ERR_UNSUPPORTED;

@@ -117,6 +117,7 @@ def lib():
         "fg_batch_tuning": (C.c_char_p, [P]),
         "fg_pattern_build": (C.c_int, [P, P, C.c_int64, C.c_int32, C.c_uint64, P, C.POINTER(P), C.c_int32, P, C.c_uint64]),
         "fg_plan_set_fp64_method": (C.c_int, [P, C.c_int32]),
+        "fg_plan_set_accumulate": (C.c_int, [P, C.c_int32]),
         "fg_hilbert_order": (C.c_int, [C.c_int32, C.c_uint64, P, P, P, P]),
         "fg_hilbert_numbering": (C.c_int, [C.c_int32, P, C.c_uint64, P, P, P]),
         "fg_profile_enable": (C.c_int, [C.c_int]),
@@ -148,7 +149,7 @@ def lib():
 def exported_symbols():
     """Names bound above (the C ABI of both headers)."""
     return [
-        "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_plan_set_fp64_method", "fg_assemble_fp64", "fg_assemble_mixed",
+        "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_plan_set_fp64_method", "fg_plan_set_accumulate", "fg_assemble_fp64", "fg_assemble_mixed",
         "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_assemble_separate", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_pattern_build", "fg_hilbert_order", "fg_hilbert_numbering", "fg_profile_enable",
         "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
@@ -368,6 +369,9 @@ class Plan:
 
     def set_fp64_method(self, method):
         check(lib().fg_plan_set_fp64_method(self.ptr, method))
+
+    def set_accumulate(self, on=True):
+        check(lib().fg_plan_set_accumulate(self.ptr, 1 if on else 0))
 
     def bind_terms(self, frequency=0.0):
         t, nt = self.prob.terms()

@@ -268,6 +268,14 @@ int fg_assemble_fp64_static(fg_plan *plan, const double *dirichlet, double *csr_
  * mixed path, kept in FP64 on the CUDA cores; the quadrature loop elsewhere. */
 enum { FG_FP64_QUADRATURE = 0, FG_FP64_FACTORED = 1 };
 int fg_plan_set_fp64_method(fg_plan *plan, int32_t method);
+/* Buckets (element types, entities, boundary terms) that share rows add into
+ * one system, as _assembleDim adds every bucket into one module
+ * (src/problem/Formulation.cpp:1418-1493). With accumulate = 1 the assemble
+ * calls of this plan add its contributions to csr_values and rhs instead of
+ * overwriting them; both must then be device memory (FG_ERR_ARG otherwise).
+ * Batches, the multi-frequency calls and the mixed error report refuse such
+ * a plan. Default 0. */
+int fg_plan_set_accumulate(fg_plan *plan, int32_t accumulate);
 /* Mixed precision: FP64 geometry, 3xTF32 tcgen05 contraction with FP32
  * accumulation, FP64 CSR reduction. report may be NULL (no error report). */
 int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency,
