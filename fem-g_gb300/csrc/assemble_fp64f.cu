@@ -178,9 +178,18 @@ bool factoredFp64Applies(const fg_plan *plan, const DevTerms &terms) {
   return true;
 }
 
+bool factoredFp64Ready(const fg_plan *plan) {
+  const FactoredState *f = (const FactoredState *)plan->fp64f;
+  return f && f->built;
+}
+
+// The tables are built when the method is chosen (fg_plan_set_fp64_method),
+// so a launch allocates nothing and issues no blocking copy.
 int launchFactoredFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, cudaStream_t s) {
-  int st = prepareFactored(plan);
-  if (st) return st;
+  if (!factoredFp64Ready(plan)) {
+    setLastError("FP64 factored kernel: the plan's reference tensors are not built");
+    return FG_ERR_ARG;
+  }
   FactoredState *f = factoredState(plan);
   const PlanDev &p = plan->d;
   if (f->nTiles == 0) return FG_OK;
@@ -191,11 +200,8 @@ int launchFactoredFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dte
   }
   const bool cplx = terms.complexKe != 0;
   auto kern = cplx ? k_element_factored_fp64<true> : k_element_factored_fp64<false>;
-  static size_t smemSet[2] = {0, 0};
-  if (smem > smemSet[cplx]) {
-    FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    smemSet[cplx] = smem;
-  }
+  static SmemAllowance allowed[2];
+  FG_CUDA(allowSmem(kern, smem, allowed[cplx]));
   ProfScope prof("k_element_factored_fp64", s);
   kern<<<f->nTiles, 256, smem, s>>>(p, dterms, f->T, f->perm, f->tiles, f->kp, ke);
   countLaunch();
@@ -209,6 +215,12 @@ extern "C" int fg_plan_set_fp64_method(fg_plan *plan, int32_t method) {
   if (!plan || (method != FG_FP64_QUADRATURE && method != FG_FP64_FACTORED)) {
     femg::setLastError("fg_plan_set_fp64_method: invalid arguments");
     return FG_ERR_ARG;
+  }
+  // the reference tensors and element tiles are built here, once, so that
+  // assemble calls (fg_assemble_fp64_static included) allocate nothing for them
+  if (method == FG_FP64_FACTORED && plan->d.E > 0) {
+    const int st = femg::prepareFactored(plan);
+    if (st) return st;
   }
   plan->fp64Method = method;
   return FG_OK;

@@ -1015,11 +1015,8 @@ std::vector<int32_t> partitionTiles(const std::vector<double> &cost, int nCta) {
 // One contraction launch over the tiles of one or many problems
 int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ctaStartDev, int nCta, int *err, int maxK3,
                    size_t smem, cudaStream_t s, int tmemCols, const void *aMap) {
-  static size_t smemSet = 0;
-  if (smem > smemSet) {
-    FG_CUDA(cudaFuncSetAttribute(k_contract_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    smemSet = smem;
-  }
+  static SmemAllowance allowed;
+  FG_CUDA(allowSmem(k_contract_tf32x3, smem, allowed));
   GemmSched sc;
   std::memset(&sc, 0, sizeof(sc));
   if (aMap) {

@@ -40,6 +40,24 @@ class ProfScope {
     }                                                                                          \
   } while (0)
 
+// Dynamic shared memory above 48 KB has to be allowed per kernel on every
+// device that runs it; a SmemAllowance remembers, per device ordinal, the
+// largest size already allowed for one kernel (races only repeat the call).
+constexpr int kSmemMaxDevices = 64;
+struct SmemAllowance {
+  size_t bytes[kSmemMaxDevices] = {};
+};
+template <typename K>
+inline cudaError_t allowSmem(K kern, size_t smem, SmemAllowance &a) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < kSmemMaxDevices && smem <= a.bytes[dev]) return cudaSuccess;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && dev >= 0 && dev < kSmemMaxDevices) a.bytes[dev] = smem;
+  return e;
+}
+
 constexpr int kMaxDofs = 64;         // element DOFs (basis x multiplicity) handled on device
 constexpr int kMaxNodes = 10;        // geometric nodes per element
 constexpr int kMaxTerms = 6;

@@ -202,11 +202,8 @@ static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, cons
 #define FG_GATHER_K(LL, JJ, AA)                                                                                   \
   {                                                                                                               \
     auto kern = k_gather<SlotT, KCPLX, KT, AT, LL, JJ, AA>;                                                       \
-    static size_t smemSet = 0;                                                                                    \
-    if (smem > smemSet) {                                                                                         \
-      FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                \
-      smemSet = smem;                                                                                             \
-    }                                                                                                             \
+    static SmemAllowance allowed;                                                                                \
+    FG_CUDA(allowSmem(kern, smem, allowed));                                                                      \
     kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, (const KT *)ke, be, uD, values, rhs, rowsPerBlock, lay, v0, v1); \
   }
 #define FG_GATHER_L(LL, JJ)                                                                                       \
@@ -326,11 +323,8 @@ static int launchBatchTyped(const GatherJob *jobs, int nJobs, int64_t blocks, co
 #define FG_GATHER_B(LL, JJ)                                                                               \
   if (g.L == LL && g.J == JJ) {                                                                           \
     auto kern = k_gather_batch<SlotT, KCPLX, KT, AT, LL, JJ>;                                             \
-    static size_t smemSet = 0;                                                                            \
-    if (g.smem > smemSet) {                                                                               \
-      FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem));      \
-      smemSet = g.smem;                                                                                   \
-    }                                                                                                     \
+    static SmemAllowance allowed;                                                                        \
+    FG_CUDA(allowSmem(kern, g.smem, allowed));                                                           \
     kern<<<(unsigned)blocks, 32 * g.wpb, g.smem, s>>>(jobs, nJobs, g.rowsPerBlock);                       \
     FG_CUDA(cudaGetLastError());                                                                          \
     return FG_OK;                                                                                         \

@@ -207,11 +207,8 @@ static int launchMultiTyped(const PlanDev &p, const MultiIn &in, cudaStream_t s)
   if (L == LL && J == JJ) {                                                                        \
     launched = true;                                                                               \
     auto kern = k_gather_multi<SlotT, KT, LL, JJ>;                                                 \
-    static size_t smemSet = 0;                                                                     \
-    if (smem > smemSet) {                                                                          \
-      FG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-      smemSet = smem;                                                                              \
-    }                                                                                              \
+    static SmemAllowance allowed;                                                                                \
+    FG_CUDA(allowSmem(kern, smem, allowed));                                                                      \
     kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, in, rowsPerBlock);                            \
   }
   FG_MULTI_L(2, 3)

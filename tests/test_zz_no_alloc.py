@@ -1,11 +1,23 @@
-"""fg_assemble_fp64_static (element scratch in a fixed device array, no
-allocation in the call) against fg_assemble_fp64 on the same plan, two calls
-in a row; its argument and size checks. Collected last so that it also runs
-after every other GPU test in the same process."""
+"""fg_assemble_fp64_static: the FP64 assembly for callers that may not
+allocate device memory once set up (a solver that owns the device memory
+pool, or one that overlaps this step's assembly with the previous step's
+solve and cannot afford the device-wide synchronisation of cudaFree). Its
+element scratch is a fixed device array inside the library.
+
+Each case makes a fresh plan that is only bound (no assemble call before),
+calls the static entry twice in a row, and checks
+  * the result against the oracle and against fg_assemble_fp64 on a second
+    plan of the same problem, at the FP64 tolerance;
+  * that the device's free memory is the same before and after the calls;
+with the quadrature method, the factored method and a Jacobian modificator.
+Collected last so that it also runs after every other GPU test in the same
+process."""
 import ctypes as C
 
 import numpy as np
 import pytest
+
+from test_jacmod import SHELLS, SQ, jm_problem
 
 pytestmark = pytest.mark.gpu
 
@@ -18,7 +30,7 @@ def rel(a, b):
     return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
 
 
-def _static_call(femg, torch, plan, prob, with_rhs=True):
+def _outputs(femg, torch, prob, with_rhs=True):
     nnz, nrows = prob.nnz, int(prob.sys.n_rows)
     dv = torch.full((2 * nnz,), float("nan"), dtype=torch.float64, device="cuda")
     db = torch.full((2 * nrows,), float("nan"), dtype=torch.float64, device="cuda") if with_rhs else None
@@ -26,41 +38,99 @@ def _static_call(femg, torch, plan, prob, with_rhs=True):
     if prob.sys.n_fixed:
         a = prob.arrays()
         dd = torch.from_numpy(np.ascontiguousarray(a["dirichlet"]).view(np.float64).copy()).cuda()
-    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    st = femg.lib().fg_assemble_fp64_static(plan.ptr, dd.data_ptr() if dd is not None else None, dv.data_ptr(),
-                                            db.data_ptr() if db is not None else None, stream)
     torch.cuda.synchronize()
-    assert st == femg.FG_OK, femg.lib().fg_last_error()
-    v = dv.cpu().numpy().view(np.complex128)
-    b = db.cpu().numpy().view(np.complex128) if db is not None else None
-    return v, b
+    return dv, db, dd
 
 
-@pytest.mark.parametrize("case", ["c3_m4", "c1_m8", "c5_m2"])
-def test_static_matches_fp64_twice(femg, cuda, case):
+def _static_calls(femg, torch, plan, prob, with_rhs=True, calls=2):
+    """`calls` static calls in a row into preallocated device outputs; returns
+    the results of each call and the free device bytes before and after."""
+    dv, db, dd = _outputs(femg, torch, prob, with_rhs)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = []
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(calls):
+        dv.fill_(float("nan"))
+        if db is not None:
+            db.fill_(float("nan"))
+        st = femg.lib().fg_assemble_fp64_static(plan.ptr, dd.data_ptr() if dd is not None else None, dv.data_ptr(),
+                                                db.data_ptr() if db is not None else None, stream)
+        torch.cuda.synchronize()
+        assert st == femg.FG_OK, femg.lib().fg_last_error()
+        out.append((dv.cpu().numpy().view(np.complex128).copy(),
+                    db.cpu().numpy().view(np.complex128).copy() if db is not None else None))
+    free1 = torch.cuda.mem_get_info()[0]
+    return out, free0, free1
+
+
+def _check(v, b, ref_v, ref_b):
+    assert rel(v, ref_v) <= FP64_TOL
+    if b is None:
+        return
+    if np.linalg.norm(ref_b) > 0:
+        assert rel(b, ref_b) <= FP64_TOL
+    else:
+        assert np.all(b == 0)
+
+
+CASES = {"c3_m4": ("config_c3", dict(m=4)), "c1_m8": ("config_c1", dict(m=8)), "c5_m2": ("config_c5", dict(m=2))}
+
+
+@pytest.mark.parametrize("method", ["quadrature", "factored"])
+@pytest.mark.parametrize("case", list(CASES))
+def test_static_matches_oracle_and_fp64_twice(femg, oracle, cuda, case, method):
     torch = cuda
-    cfg = {"c3_m4": femg.config_c3(m=4), "c1_m8": femg.config_c1(m=8), "c5_m2": femg.config_c5(m=2)}[case]
-    prob = femg.Problem(cfg)
-    plan = prob.plan()
-    v_ref, b_ref = plan.assemble("fp64")
+    fn, kw = CASES[case]
+    prob = femg.Problem(getattr(femg, fn)(**kw))
+    a = prob.arrays()
+    t, nt = prob.terms()
+    ref_v, ref_b = oracle.assemble(a, t, nt)
+    other = prob.plan()  # fg_assemble_fp64 on a second plan
+    v64, b64 = other.assemble("fp64")
+    plan = prob.plan()  # fresh: bound, never assembled
+    if method == "factored":
+        plan.set_fp64_method(femg.FG_FP64_FACTORED)
     plan.bind_terms()
-    for _ in range(2):
-        v, b = _static_call(femg, torch, plan, prob)
-        assert rel(v, v_ref) <= FP64_TOL
-        if np.linalg.norm(b_ref) > 0:
-            assert rel(b, b_ref) <= FP64_TOL
-        else:
-            assert np.all(b == 0)
+    out, free0, free1 = _static_calls(femg, torch, plan, prob)
+    assert free0 == free1, "device memory changed across the static calls: %d -> %d" % (free0, free1)
+    for v, b in out:
+        _check(v, b, ref_v, ref_b)
+        _check(v, b, v64, b64)
+    plan.close()
+    other.close()
 
 
-def test_static_without_rhs(femg, cuda):
+def test_static_jacobian_modificator(femg, oracle, cuda):
+    """A spherical shell on every term: the element kernel's shell-radius
+    check reads a device word back, which allocates nothing either."""
+    torch = cuda
+    from test_gpu_jacmod import copy_terms, set_jm
+    prob = jm_problem(femg, 3, 4, gauss=6)
+    a = prob.arrays()
+    t, nt = copy_terms(femg, prob, source=True)
+    for k in range(nt):
+        set_jm(femg, t[k], femg.FG_JACMOD_SPHERICAL_SHELL, **dict(SHELLS["spherical"][2], **SQ))
+    ref_v, ref_b = oracle.assemble(a, t, nt)
+    plan = prob.plan()
+    assert femg.lib().fg_plan_bind_terms(plan.ptr, t, nt, 0.0) == femg.FG_OK, femg.lib().fg_last_error()
+    out, free0, free1 = _static_calls(femg, torch, plan, prob)
+    assert free0 == free1
+    for v, b in out:
+        _check(v, b, ref_v, ref_b)
+    plan.close()
+
+
+def test_static_without_rhs(femg, oracle, cuda):
     torch = cuda
     prob = femg.Problem(femg.config_c3(m=3))
+    t, nt = prob.terms()
+    ref_v, _ = oracle.assemble(prob.arrays(), t, nt)
     plan = prob.plan()
-    v_ref, _ = plan.assemble("fp64")
     plan.bind_terms()
-    v, _ = _static_call(femg, torch, plan, prob, with_rhs=False)
-    assert rel(v, v_ref) <= FP64_TOL
+    out, free0, free1 = _static_calls(femg, torch, plan, prob, with_rhs=False)
+    assert free0 == free1
+    for v, _ in out:
+        assert rel(v, ref_v) <= FP64_TOL
 
 
 def test_static_rejects(femg, cuda):
