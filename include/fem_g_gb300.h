@@ -256,8 +256,12 @@ int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, 
  * FG_ERR_UNSUPPORTED when the scratch, E * (1 or 2 for complex) * n^2 * 8
  * bytes plus E * n * 16 bytes with a source term and rhs, exceeds the array;
  * FG_ERR_ARG for host outputs or no bound terms. The first call on a device
- * resolves the array's address (cudaGetSymbolAddress, that device current):
- * make it before any stream capture. The array is shared by all plans on a
+ * resolves the array's address (cudaGetSymbolAddress, that device current);
+ * under CUDA's lazy module loading (the default) that is also when the driver
+ * loads the code module holding the array and its 64 MiB of device memory,
+ * kept until exit. Make that first call during set-up, before any stream
+ * capture. FG_FP64_FACTORED plans build their reference tensors in
+ * fg_plan_set_fp64_method, so no later call allocates. The array is shared by all plans on a
  * device: calls in flight at the same time on one device race on it. */
 #define FG_STATIC_SCRATCH_BYTES ((size_t)64 << 20)
 int fg_assemble_fp64_static(fg_plan *plan, const double *dirichlet, double *csr_values, double *rhs, void *stream);

@@ -7,11 +7,14 @@ and assembly path, from the reference's own code where it builds here.
 - robin_<case>: the DOF dictionary iteration order that the reference's
   robin_hood 3.8.0 map (robin_hood.h as vendored in the reference tree, in
   libref.so) gives for the case's DOF creation and reserve() script.
-- csr_<case>: ai, aj, CSR values and right-hand side of the oracle
-  (oracle/oracle.c, a restatement of Formulation::assemble) for small cases.
+- csr_<case>: ai, aj, CSR values and right-hand side that the reference's
+  own Formulation::pre() and assemble() produce (oracle/_ref/ref_assemble:
+  the reference library compiled with the gmsh stand-in), and dof_<case>:
+  the reference's DOF dictionary in iteration order (keys, assemble types,
+  numbering).
 
-Run from the repository root after oracle/build.py has built liboracle.so
-and libref.so:  python tests/golden/make_golden.py
+Run from the repository root after oracle/build.py has built liboracle.so,
+libref.so and ref_assemble:  python tests/golden/make_golden.py
 """
 import os
 import sys
@@ -24,16 +27,29 @@ sys.path.insert(0, os.path.join(ROOT, "fem-g_gb300"))
 
 CASES = {
     "c1_m8": dict(cfg="config_c1", kw=dict(m=8)),
+    "c1_m8_dirichlet1": dict(cfg="config_c1", kw=dict(m=8), set=dict(dirichlet_value=1.0)),
     "c2_m2": dict(cfg="config_c2", kw=dict(m=2)),
     "c2_m1_p4": dict(cfg="config_c2", kw=dict(m=1, order=4)),
     "c3_m2": dict(cfg="config_c3", kw=dict(m=2)),
+    "c3_m4": dict(cfg="config_c3", kw=dict(m=4)),
     "c5_m1": dict(cfg="config_c5", kw=dict(m=1)),
+    "c5_m2": dict(cfg="config_c5", kw=dict(m=2)),
+    "maxwell_3d_m2": dict(cfg="config", kw=dict(kind=2, dim=3, m=2, mesh_order=1, space=2, order=0, gauss=2, jitter=0.15,
+                                                seed=7, k=3.0, coef_mode=1)),
+    "upper_c3_m2": dict(cfg="config_c3", kw=dict(m=2), set=dict(upper=1)),
 }
 
 
-def build_case(femg, name):
+def build_config(femg, name):
     spec = CASES[name]
-    return femg.Problem(getattr(femg, spec["cfg"])(**spec["kw"]))
+    cfg = getattr(femg, spec["cfg"])(**spec["kw"])
+    for k, v in spec.get("set", {}).items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def build_case(femg, name):
+    return femg.Problem(build_config(femg, name))
 
 
 def dictionary_script(oracle, prob):
@@ -45,10 +61,12 @@ def dictionary_script(oracle, prob):
 
 def main():
     import femg
-    from oracle import oracle
+    from oracle import oracle, reference
 
     if oracle.ref() is None:
         raise SystemExit("oracle/_ref/libref.so is not built (the reference tree is needed to make the fixtures)")
+    if not reference.available():
+        raise SystemExit("oracle/_ref/ref_assemble is not built (the reference tree is needed to make the fixtures)")
     out = {}
     for dim in (2, 3):
         rng = np.random.default_rng(100 + dim)
@@ -62,13 +80,13 @@ def main():
         prob = build_case(femg, name)
         cr, kinds, args = dictionary_script(oracle, prob)
         out["robin_%s" % name] = oracle.robin_order(kinds, args, cr["num_type"], cr["entity"], use_ref=True)
-        a = prob.arrays()
-        t, nt = prob.terms()
-        v, b = oracle.assemble(a, t, nt)
-        out["csr_%s_ai" % name] = a["ai"]
-        out["csr_%s_aj" % name] = a["aj"]
-        out["csr_%s_values" % name] = v
-        out["csr_%s_rhs" % name] = b
+        ref = reference.run(build_config(femg, name), threads=4)
+        out["csr_%s_ai" % name] = ref["ai"]
+        out["csr_%s_aj" % name] = ref["aj"]
+        out["csr_%s_values" % name] = ref["values"]
+        out["csr_%s_rhs" % name] = ref["rhs"]
+        for k in ("num_type", "entity", "num_dof", "assemble_type"):
+            out["dof_%s_%s" % (name, k)] = ref["dof_" + k]
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden_small.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes")
