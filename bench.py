@@ -1,6 +1,6 @@
 """Benchmark of the GB300 assembly path (one JSON line on rank 0).
 
-Workload (default): the 3D Helmholtz system on the unit cube, 40^3 cubes x 6
+Headline workload: the 3D Helmholtz system on the unit cube, 40^3 cubes x 6
 Kuhn tetrahedra = 384,000 tets, hierarchical H1 order 3 (20 DOFs per tet),
 Gauss6, k = 20, per-tet coefficient -k^2 (1 + 0.3 xi), xi ~ N(0,1): 84,640,201
 CSR nonzeros, 1,771,561 unknowns. Inputs are seeded synthetic data with the
@@ -13,10 +13,18 @@ value is element matrices/s of the mixed-precision path (FP64 geometry,
 and the relative Frobenius error between the two. The CSR output (1.35 GB)
 is larger than L2, so no flush is needed between steps.
 
---impl reference times the reference algorithm on the host cores: the CPU
-oracle (a restatement of the reference's assemble; the reference itself does
-not build here: gmsh is absent), all threads, on a bounded sample of the
-same workload per step.
+The default line also carries, as "c4" and "c5mf", the batched workload (64
+Helmholtz problems of orders 1-4 in one graph replay) and the multi-frequency
+workload (Navier P2 x 3 on 1,296,000 tets at 16 frequencies in one pass),
+each with its own FP64 comparisons, clocks, roofline, CPU baseline and
+end-to-end figure (--no-c4 / --no-c5 leave them out; --workload c4 or c5mf
+prints one of them alone).
+
+--impl reference times the reference's CPU implementation on the host cores
+in a process that does not load the GPU library: the reference's own
+Formulation::assemble where its library was built (its sources with the gmsh
+stand-in; kind "reference"), else the oracle's C restatement of it, pinned to
+the reference at 1e-13 (kind "port"), on a bounded sample of the elements.
 
 Multi-GPU: every rank assembles its own replica of the workload (the path
 has no exchange step); value = all ranks' element matrices / max rank time.
@@ -134,7 +142,7 @@ def sub_arrays(a, S):
     return b
 
 
-def cpu_rate(prob, a, target_s):
+def cpu_rate(prob, a, target_s, freq=0.0):
     """Oracle assemble on the first S elements (all host threads): element
     matrices/s. S grows until one run takes target_s seconds or covers the mesh."""
     from oracle import oracle as O
@@ -143,7 +151,7 @@ def cpu_rate(prob, a, target_s):
     while True:
         b = sub_arrays(a, S)
         t0 = time.perf_counter()
-        O.assemble(b, t, nt)
+        O.assemble(b, t, nt, freq=freq)
         dt = time.perf_counter() - t0
         if dt >= target_s or S >= a["E"]:
             return S / dt, S, dt, O.num_threads()
@@ -164,22 +172,66 @@ def timed_events(torch, stream, fn, warmup, steps):
     return e0.elapsed_time(e1) / steps
 
 
+def profile_run(femg, torch, fn):
+    """{kernel: (launches, total ms)} of one call of fn with the kernel timer on."""
+    torch.cuda.synchronize()
+    femg.profile_read()
+    femg.profile_enable(True)
+    fn()
+    torch.cuda.synchronize()
+    femg.profile_enable(False)
+    return femg.profile_read()
+
+
+def roofline(prof, alg_bytes, pk, pk_kind, traffic=None, traffic_src=None, steps=1):
+    """Roofline of the dominant kernel: the algorithmic bytes its launches
+    carry per step over their summed device time per step."""
+    dom, (dcount, dms) = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 0.0))
+    per_step_ms = dms / max(steps, 1)
+    achieved = alg_bytes / (per_step_ms / 1000.0) / 1e9 if per_step_ms > 0 else 0.0
+    return {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+            "traffic": traffic, "traffic_source": traffic_src, "kernel": dom,
+            "kernel_launches_per_step": dcount / max(steps, 1), "kernel_ms_per_step": per_step_ms,
+            "kernel_avg_ms": dms / max(dcount, 1), "algorithmic_bytes": alg_bytes, "peak_source": pk_kind,
+            "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()}}
+
+
+def fused_bytes(E, n, nnz, nrows, nv=4, coef=16):
+    """Algorithmic bytes of one assembly, the fused minimum: per element its
+    vertices (3 doubles) and connectivity (4-byte indices), its coefficient
+    and its n^2 element-to-nonzero map entries (4 bytes); per nonzero one
+    complex double written; per row one complex double of right-hand side."""
+    return E * (nv * 3 * 8 + nv * 4 + coef + n * n * 4) + nnz * 16 + nrows * 16
+
+
+def build_problems(femg, cfgs, workers=4):
+    """The host pre() of many problems, a few at a time (each is threaded)."""
+    import concurrent.futures
+    with concurrent.futures.ThreadPoolExecutor(max_workers=workers) as ex:
+        return list(ex.map(femg.Problem, cfgs))
+
+
 def bench_batch(args, femg, torch):
     """Batched workload: 64 3D Helmholtz problems, m ~ U{m_lo..m_hi}, orders
     U{1..4}, k ~ U[5, 40], Gauss(2p), one seed; one step = one fg_batch_run
     (graph replay) over all problems, outputs resident in HBM."""
     cfgs = femg.config_c4(n=args.c4_n, m_lo=args.c4_m_lo, m_hi=args.c4_m_hi)
-    probs = [femg.Problem(c) for c in cfgs]
+    w0 = time.perf_counter()
+    probs = build_problems(femg, cfgs)
+    pre_wall = time.perf_counter() - w0
     pre_s = sum(p.pre_seconds() for p in probs)
     plans = [p.plan() for p in probs]
     E = sum(p.info()["E"] for p in plans)
     nnz = sum(p.nnz for p in probs)
+    rows = sum(int(p.sys.n_rows) for p in probs)
     stream = torch.cuda.current_stream()
     sptr = C.c_void_p(stream.cuda_stream)
     outs = [torch.empty(2 * p.nnz, dtype=torch.float64, device="cuda") for p in probs]
     ptrs = [o.data_ptr() for o in outs]
     res = {}
-    for prec in ("mixed", "fp64", "fp64_factored"):
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    for prec in ("mixed", "fp64_factored", "fp64"):
         for p in plans:
             p.set_fp64_method(femg.FG_FP64_FACTORED if prec == "fp64_factored" else femg.FG_FP64_QUADRATURE)
         b = femg.Batch(plans, mixed=prec == "mixed")
@@ -188,11 +240,13 @@ def bench_batch(args, femg, torch):
         torch.cuda.synchronize()
         first_s = time.perf_counter() - t0
         l0 = femg.lib().fg_launch_count()
-        steps = args.steps if prec == "mixed" else max(3, min(args.steps, 5))
-        ms = timed_events(torch, stream, lambda: b.run(values=ptrs, stream=sptr), args.warmup, steps)
-        launches = (femg.lib().fg_launch_count() - l0) // (args.warmup + steps)
+        steps = args.steps if prec == "mixed" else (3 if prec == "fp64_factored" else 2)
+        warm = args.warmup if prec == "mixed" else 1
+        ms = timed_events(torch, stream, lambda: b.run(values=ptrs, stream=sptr), warm, steps)
+        launches = (femg.lib().fg_launch_count() - l0) // (warm + steps)
         res[prec] = {"ms": ms, "first_run_s": first_s, "tuning": json.loads(b.tuning()), "launches_per_step": int(launches)}
         if prec == "mixed":
+            res["prof"] = profile_run(femg, torch, lambda: b.run(values=ptrs, stream=sptr))
             # relative Frobenius error of every problem's CSR against the FP64 path
             tmp = torch.empty(2 * max(p.nnz for p in probs), dtype=torch.float64, device="cuda")
             d2 = r2 = 0.0
@@ -209,16 +263,54 @@ def bench_batch(args, femg, torch):
             res["rel_fro"] = (d2 / r2) ** 0.5
             res["worst_problem_rel_fro"] = worst
             del tmp
+            # end to end: the batch's CSR values into host memory, as the
+            # reference's module arrays hold them (ordinary pageable memory)
+            hv = [np.empty(p.nnz, np.complex128) for p in probs]
+            hptrs = [h.ctypes.data for h in hv]
+            b.run(values=hptrs, stream=sptr)  # warm-up: first touch of the host pages
+            e2e_steps = 2
+            e0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                b.run(values=hptrs, stream=sptr)
+            torch.cuda.synchronize()
+            res["e2e_ms"] = 1000.0 * (time.perf_counter() - e0) / e2e_steps
+            del hv
         b.close()
+    clk = clocks.stop()
+    for o in outs:
+        del o
+    pk, pk_kind = peaks()
+    alg = sum(fused_bytes(p.info()["E"], p.info()["n"], p.prob.nnz, int(p.prob.sys.n_rows), coef=0) for p in plans)
+    roof = roofline(res["prof"], alg, pk, pk_kind)
+    cpu = None
+    if not args.no_cpu:
+        # the oracle per order on the largest problem of that order, a bounded
+        # sample each; the batch rate is the element-weighted harmonic mean
+        by_order = {}
+        for p in probs:
+            o = int(p.cfg.order)
+            if o not in by_order or p.E > by_order[o].E:
+                by_order[o] = p
+        rates, samples = {}, []
+        for o, p in sorted(by_order.items()):
+            r, S, dt, cores = cpu_rate(p, p.arrays(), args.cpu_seconds / max(len(by_order), 1))
+            rates[o] = r
+            samples.append("order %d: first %d of %d elements, %.1f s" % (o, S, p.E, dt))
+        t_all = sum(p.E / rates[int(p.cfg.order)] for p in probs)
+        cpu = {"value": E / t_all, "unit": "element matrices/s", "cores": cores, "kind": "port",
+               "sample": "; ".join(samples) + "; batch rate = all elements / sum over problems of elements / rate of its order"}
     orders = {}
     for c in cfgs:
         orders[str(c.order)] = orders.get(str(c.order), 0) + 1
-    line = {"metric": METRIC, "value": E / (res["mixed"]["ms"] / 1000.0), "unit": "element matrices/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["mixed"]["ms"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp32-tf32x3/fp64", "data": "synthetic (seeded, reference configuration shapes)",
+    for p in plans:
+        p.close()
+    for p in probs:
+        p.close()
+    return {"metric": METRIC, "value": E / (res["mixed"]["ms"] / 1000.0), "unit": "element matrices/s",
+            "ms_per_step": res["mixed"]["ms"], "steps": args.steps, "warmup": args.warmup,
             "config": {"workload": "helmholtz3d_batch%d_m%d-%d_p1-4_k5-40_gauss2p" % (args.c4_n, args.c4_m_lo, args.c4_m_hi),
-                       "problems": len(probs), "elements": E, "nnz": nnz, "orders": orders,
-                       "l2": "CSR outputs larger than L2, no flush", "parallelism": "single"},
+                       "problems": len(probs), "elements": E, "nnz": nnz, "unknowns": rows, "orders": orders,
+                       "l2": "CSR outputs larger than L2, no flush"},
             "nnz_per_s": nnz / (res["mixed"]["ms"] / 1000.0),
             "fp64": {"value": E / (res["fp64"]["ms"] / 1000.0), "ms_per_step": res["fp64"]["ms"],
                      "method": "plain: quadrature loop of BilinearTerm::evaluate in FP64"},
@@ -229,57 +321,89 @@ def bench_batch(args, femg, torch):
             "mixed_vs_fp64_rel_fro": res["rel_fro"], "worst_problem_rel_fro": res["worst_problem_rel_fro"],
             "first_run_s": {k: res[k]["first_run_s"] for k in ("mixed", "fp64", "fp64_factored")},
             "tuning": {"mixed": res["mixed"]["tuning"], "fp64": res["fp64"]["tuning"]},
-            "gpu_launches": res["mixed"]["launches_per_step"] * args.steps, "pre_seconds": pre_s}
-    print(json.dumps(line), flush=True)
+            "gpu_launches": res["mixed"]["launches_per_step"] * args.steps,
+            "e2e": {"value": E / (res["e2e_ms"] / 1000.0), "unit": "element matrices/s", "ms_per_step": res["e2e_ms"],
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": nnz * 16,
+                    "note": "fg_batch_run into pageable host arrays; the coefficients are constants (no input arrays)"},
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "pre_seconds": pre_s, "pre_wall_seconds": pre_wall}
 
 
 def bench_multi_freq(args, femg, torch):
     """Navier 3-component P2 on m^3 x 6 tets, Lame lognormal per tet, 16
     frequencies omega ~ U[1, 10] in one pass; one step = one
     fg_assemble_multi_freq writing all 16 CSR value arrays in HBM."""
-    m = args.m or 60
+    m = args.c5_m or 60
     prob = femg.Problem(femg.config_c5(m=m, omega=0.0))
+    pre_s = prob.pre_seconds()
     plan = prob.plan()
-    E, nnz = plan.info()["E"], prob.nnz
+    info = plan.info()
+    E, nnz, n = info["E"], prob.nnz, info["n"]
+    rows = int(prob.sys.n_rows)
     F = args.n_freq
     omegas = np.random.default_rng(5).uniform(1.0, 10.0, F)
     stream = torch.cuda.current_stream()
     sptr = C.c_void_p(stream.cuda_stream)
     out = torch.empty(F * 2 * nnz, dtype=torch.float64, device="cuda")
     res = {}
-    femg.profile_read()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
     for prec in ("mixed", "fp64"):
         steps = args.steps if prec == "mixed" else 2
+        fn = lambda: plan.assemble_multi_freq(omegas, precision=prec, values=out.data_ptr(), rhs=False, stream=sptr)
+        l0 = femg.lib().fg_launch_count()
+        ms = timed_events(torch, stream, fn, args.warmup if prec == "mixed" else 1, steps)
+        launches = (femg.lib().fg_launch_count() - l0) // ((args.warmup if prec == "mixed" else 1) + steps)
         if prec == "mixed":
-            femg.profile_enable(True)
-        ms = timed_events(torch, stream, lambda: plan.assemble_multi_freq(omegas, precision=prec, values=out.data_ptr(),
-                                                                          rhs=False, stream=sptr), args.warmup if prec == "mixed" else 1, steps)
-        if prec == "mixed":
-            femg.profile_enable(False)
-            res["prof"] = femg.profile_read()
+            res["prof"] = profile_run(femg, torch, fn)
+            res["launches"] = int(launches)
             first = out[: 2 * nnz].clone()
         else:
             ref = out[: 2 * nnz]
             res["rel_fro"] = torch.linalg.vector_norm(first - ref).item() / torch.linalg.vector_norm(ref).item()
+            del first
         res[prec] = ms
+    clk = clocks.stop()
+    del out
+    torch.cuda.empty_cache()
+    # end to end: the Lame arrays from the host, all frequencies' CSR values
+    # into pageable host memory (the reference's module arrays)
+    tt, nt = prob.terms()
+    h2d = sum(ex.n_arrays * E * 16 for k in range(nt) for ex in (tt[k].coef, tt[k].coef2)) + F * 8
+    hv = np.empty((F, nnz), np.complex128)
+    efn = lambda: plan.assemble_multi_freq(omegas, precision="mixed", values=hv, rhs=False, stream=sptr)
+    efn()  # warm-up: first touch of the host pages
+    e0 = time.perf_counter()
+    for _ in range(2):
+        efn()
+    e2e_ms = 1000.0 * (time.perf_counter() - e0) / 2
+    del hv
     pk, pk_kind = peaks()
-    prof = res["prof"]
-    dom, (dcount, dms) = max(prof.items(), key=lambda kv: kv[1][1])
-    avg = dms / max(dcount, 1)
-    alg = F * nnz * 16 + 2 * E * plan.info()["n"] ** 2 * 4 + E * plan.info()["n"] ** 2 * 2
-    line = {"metric": METRIC, "value": F * E / (res["mixed"] / 1000.0), "unit": "element matrices/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["mixed"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp32-tf32x3/fp64", "data": "synthetic (seeded, reference configuration shapes)",
+    # fused minimum with all frequencies written: elements' geometry, Lame
+    # pair and map once, F complex values per nonzero
+    alg = E * (4 * 3 * 8 + 4 * 4 + 32 + n * n * 4) + F * nnz * 16
+    roof = roofline(res["prof"], alg, pk, pk_kind)
+    cpu = None
+    if not args.no_cpu:
+        a = prob.arrays()
+        r, S, dt, cores = cpu_rate(prob, a, args.cpu_seconds, freq=float(omegas[0]))
+        cpu = {"value": r, "unit": "element matrices/s", "cores": cores, "kind": "port",
+               "sample": "one frequency, first %d of %d elements, %.1f s (every frequency is a full assembly)" % (S, E, dt)}
+    plan.close()
+    prob.close()
+    return {"metric": METRIC, "value": F * E / (res["mixed"] / 1000.0), "unit": "element matrices/s",
+            "ms_per_step": res["mixed"], "steps": args.steps, "warmup": args.warmup,
             "config": {"workload": "navier3d_tet_h1p2x3_%d3x6_gauss4_lame_%dfreq" % (m, F), "elements": E, "nnz_per_freq": nnz,
-                       "frequencies": F, "l2": "CSR outputs larger than L2, no flush", "parallelism": "single"},
+                       "unknowns": rows, "frequencies": F, "units": "element matrices: elements x frequencies",
+                       "l2": "CSR outputs larger than L2, no flush"},
             "nnz_per_s": F * nnz / (res["mixed"] / 1000.0),
             "fp64": {"value": F * E / (res["fp64"] / 1000.0), "ms_per_step": res["fp64"]},
             "speedup_mixed_vs_fp64": res["fp64"] / res["mixed"], "mixed_vs_fp64_rel_fro_freq0": res["rel_fro"],
-            "roofline": {"bound": "hbm", "kernel": dom, "kernel_avg_ms": avg, "algorithmic_bytes": alg,
-                         "achieved": alg / (avg / 1000.0) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                         "frac": alg / (avg / 1000.0) / 1e9 / pk["hbm_gbs"], "peak_source": pk_kind,
-                         "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()}}}
-    print(json.dumps(line), flush=True)
+            "gpu_launches": res["launches"] * args.steps,
+            "e2e": {"value": F * E / (e2e_ms / 1000.0), "unit": "element matrices/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": F * nnz * 16,
+                    "note": "fg_assemble_multi_freq with host coefficient arrays and pageable host outputs"},
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "pre_seconds": pre_s}
 
 
 def max_over_ranks(x, dist, device):
@@ -303,14 +427,58 @@ def dist_setup():
     return ws, rank, local
 
 
+def load_femg_host():
+    """The ctypes binding without the GPU library: problems come from
+    libfemg_host.so (built here if missing, host compiler only)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("femg_build", os.path.join(ROOT, "fem-g_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build_host()
+    from oracle import build as ob
+    ob.build_oracle()
+    spec = importlib.util.spec_from_file_location("femg", os.path.join(ROOT, "fem-g_gb300", "femg.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["femg"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def run_reference(args, ws, rank):
+    """The reference's CPU implementation of the path on this host's cores.
+    Where the reference's own library was built (oracle/_ref/ref_assemble:
+    its sources with the gmsh stand-in), its Formulation::assemble is timed
+    on the whole workload (kind "reference"); elsewhere the oracle's C
+    restatement of it, pinned to the reference at 1e-13 (kind "port"), on a
+    bounded sample of the workload's elements. The process never loads the
+    GPU library: problem set-up comes from the host-only library."""
     if rank != 0:
         return
-    femg = load_femg()
-    cfg, wname = workload_config(femg, args.workload, args.m)
-    prob = femg.Problem(cfg)
-    a = prob.arrays()
+    femg = load_femg_host()
+    cfg, wname = workload_config(femg, args.workload if args.workload not in ("c4", "c5mf") else "c3", args.m)
+    from oracle import reference as R
     from oracle import oracle as O
+    base = {"impl": "reference", "metric": METRIC, "unit": "element matrices/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex128",
+            "data": "synthetic (seeded, reference configuration shapes)"}
+    if R.available() and args.ref_kind in ("auto", "reference"):
+        runs = max(1, min(args.steps, 3))
+        r = R.run(cfg, threads=0, repeats=runs + 1)
+        prob = femg.Problem(cfg, host_only=True)
+        E = prob.E
+        rate = E / r["assemble_seconds"]
+        line = dict(base, value=rate, ms_per_step=1000.0 * r["assemble_seconds"],
+                    config={"workload": wname, "elements": E, "nnz": r["nnz"], "sample_elements": E},
+                    nnz_per_s=r["nnz"] / r["assemble_seconds"],
+                    cpu_baseline={"value": rate, "unit": "element matrices/s", "cores": r["threads"], "kind": "reference",
+                                  "sample": "the whole workload: the reference's Formulation::assemble (its sources, gmsh "
+                                            "stand-in), median of %d runs after one" % r["timed_runs"]},
+                    e2e={"value": rate, "unit": "element matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                    pre_seconds=r["pre_seconds"])
+        print(json.dumps(line), flush=True)
+        return
+    prob = femg.Problem(cfg, host_only=True)
+    a = prob.arrays()
     t, nt = prob.terms()
     S = min(a["E"], args.ref_sample)
     b = sub_arrays(a, S)
@@ -323,14 +491,13 @@ def run_reference(args, ws, rank):
         times.append(time.perf_counter() - t0)
     ms = 1000.0 * float(np.mean(times))
     rate = S / (ms / 1000.0)
-    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "element matrices/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "complex128", "data": "synthetic (seeded, reference configuration shapes)",
-            "config": {"workload": wname, "elements": int(a["E"]), "nnz": prob.nnz, "sample_elements": S},
-            "nnz_per_s": rate * prob.nnz / a["E"],
-            "cpu_baseline": {"value": rate, "unit": "element matrices/s", "cores": O.num_threads(), "kind": "port",
-                             "sample": "first %d of %d elements per step, oracle restatement of Formulation::assemble" % (S, a["E"])},
-            "e2e": {"value": rate, "unit": "element matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line = dict(base, value=rate, ms_per_step=ms,
+                config={"workload": wname, "elements": int(a["E"]), "nnz": prob.nnz, "sample_elements": S},
+                nnz_per_s=rate * prob.nnz / a["E"],
+                cpu_baseline={"value": rate, "unit": "element matrices/s", "cores": O.num_threads(), "kind": "port",
+                              "sample": "first %d of %d elements per step, the oracle's C restatement of "
+                                        "Formulation::assemble (pinned to the reference's own assembly)" % (S, a["E"])},
+                e2e={"value": rate, "unit": "element matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
     print(json.dumps(line), flush=True)
 
 
@@ -349,6 +516,10 @@ def main():
     ap.add_argument("--c4-m-lo", type=int, default=8)
     ap.add_argument("--c4-m-hi", type=int, default=48)
     ap.add_argument("--n-freq", type=int, default=16)
+    ap.add_argument("--c5-m", type=int, default=60)
+    ap.add_argument("--no-c4", action="store_true", help="leave the batched workload out of the default line")
+    ap.add_argument("--no-c5", action="store_true", help="leave the multi-frequency workload out of the default line")
+    ap.add_argument("--ref-kind", default="auto", choices=["auto", "reference", "port"])
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -364,8 +535,32 @@ def main():
     if args.workload in ("c4", "c5mf"):
         if ws > 1:
             raise SystemExit("the batched and multi-frequency workloads run on one GPU")
-        (bench_batch if args.workload == "c4" else bench_multi_freq)(args, femg, torch)
+        sub = (bench_batch if args.workload == "c4" else bench_multi_freq)(args, femg, torch)
+        line = dict(sub, n_gpus=1, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="fp32-tf32x3/fp64",
+                    data="synthetic (seeded, reference configuration shapes)")
+        line["config"] = dict(sub["config"], parallelism="single")
+        print(json.dumps(line), flush=True)
         return
+    line = bench_headline(args, femg, torch, ws, rank, local, dist)
+    # the batched (c4) and multi-frequency (c5) workloads of the target, one
+    # GPU each, after the headline's buffers are released
+    if rank == 0 and ws == 1 and args.workload == "c3":
+        torch.cuda.empty_cache()
+        if not args.no_c4:
+            line["c4"] = bench_batch(args, femg, torch)
+            torch.cuda.empty_cache()
+        if not args.no_c5:
+            line["c5mf"] = bench_multi_freq(args, femg, torch)
+            torch.cuda.empty_cache()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def bench_headline(args, femg, torch, ws, rank, local, dist):
+    """The headline workload (default: 384,000 order-3 tets with per-tet
+    coefficients), timed on every rank; returns rank 0's line (None elsewhere)."""
     cfg, wname = workload_config(femg, args.workload, args.m)
     t0 = time.perf_counter()
     prob = femg.Problem(cfg)
@@ -481,6 +676,22 @@ def main():
     e2e_ms = 1000.0 * (time.perf_counter() - w0) / e2e_steps
     if ws > 1:
         e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
+    # the same into ordinary (pageable) host memory: the reference's module
+    # array is a std::vector, which a drop-in writes unless it registers it
+    pv = np.empty(nnz, np.complex128)
+    pb = np.empty(nrows, np.complex128)
+
+    def e2e_pageable_step():
+        femg.check(fn(plan.ptr, tt, nt, 0.0, dptr, pv.ctypes.data, pb.ctypes.data, sptr, *extra))
+
+    e2e_pageable_step()  # first touch of the pages
+    p_calls = []
+    for _ in range(e2e_steps):
+        c0 = time.perf_counter()
+        e2e_pageable_step()
+        p_calls.append(1000.0 * (time.perf_counter() - c0))
+    e2e_pageable_ms = float(np.mean(p_calls))
+    del pv, pb
 
     # roofline of the dominant kernel (algorithmic bytes of the fused minimum
     # per launch / measured average launch time)
@@ -526,12 +737,15 @@ def main():
                 "speedup_mixed_vs_fp64": ms_fp64 / ms_head,
                 "pre_seconds": pre_s, "plan_seconds": plan_s,
                 "e2e": {"value": replica_value(E, e2e_ms, ws), "unit": "element matrices/s", "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                        "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "host_memory": "page-locked",
                         "ms_per_call": {"median": float(np.median(e2e_calls)), "min": min(e2e_calls), "max": max(e2e_calls)}},
+                "e2e_pageable": {"value": replica_value(E, e2e_pageable_ms, ws), "unit": "element matrices/s",
+                                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_pageable_ms,
+                                 "host_memory": "pageable (as the reference's std::vector module array)",
+                                 "ms_per_call": {"median": float(np.median(p_calls)), "min": min(p_calls), "max": max(p_calls)}},
                 "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
-        print(json.dumps(line), flush=True)
-    if ws > 1:
-        dist.destroy_process_group()
+        return line
+    return None
 
 
 if __name__ == "__main__":

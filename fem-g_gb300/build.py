@@ -1,5 +1,7 @@
 """Build the in-tree shared library libfemg.so (CUDA kernels for sm_103a, the
-C ABI and the host-side mirror of the reference interface).
+C ABI and the host-side mirror of the reference interface), and
+libfemg_host.so: the host mirror alone (problem set-up and pre(), no CUDA),
+which the CPU baseline loads so that its process never maps the GPU library.
 
 Every translation unit is compiled in parallel into ``_build/`` next to this
 file; nothing is installed. ``build()`` is idempotent: a unit is recompiled
@@ -17,8 +19,11 @@ LIB = os.path.join(BUILD, "libfemg.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CUDA_SOURCES = ["csrc/plan.cu", "csrc/assemble_fp64.cu", "csrc/assemble_fp64f.cu", "csrc/assemble_mixed.cu", "csrc/gather.cu", "csrc/assemble_static.cu", "csrc/multi_freq.cu", "csrc/batch.cu", "csrc/pattern.cu", "csrc/numbering.cu"]
-HOST_SOURCES = ["host/mesh.cpp", "host/refelem.cpp", "host/dofs.cpp", "host/formulation.cpp", "host/problems.cpp"]
-HEADERS = ["csrc/common.cuh", "host/mesh.h", "host/refelem.h", "host/dofs.h", "host/formulation.h"]
+HOST_ONLY_SOURCES = ["host/errors.cpp", "host/mesh.cpp", "host/refelem.cpp", "host/dofs.cpp", "host/formulation.cpp",
+                     "host/problems.cpp"]
+HOST_SOURCES = HOST_ONLY_SOURCES + ["host/problem_assemble.cpp"]
+HEADERS = ["csrc/common.cuh", "host/mesh.h", "host/refelem.h", "host/dofs.h", "host/formulation.h", "host/problem_internal.h"]
+HOST_LIB = os.path.join(BUILD, "libfemg_host.so")
 
 
 def _nvcc():
@@ -73,5 +78,22 @@ def build(verbose=False):
     return LIB
 
 
+def build_host(verbose=False):
+    """libfemg_host.so: the host mirror's problem set-up without any GPU code."""
+    os.makedirs(BUILD, exist_ok=True)
+    hdr = _newest_header()
+    objs = [_compile(s, hdr) for s in HOST_ONLY_SOURCES]
+    if os.path.exists(HOST_LIB) and os.path.getmtime(HOST_LIB) >= max(os.path.getmtime(o) for o in objs):
+        return HOST_LIB
+    r = subprocess.run(["g++", "-shared", "-fopenmp", "-o", HOST_LIB] + objs + ["-Wl,--no-undefined"], capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))
+    if verbose:
+        print("built", HOST_LIB)
+    return HOST_LIB
+
+
 if __name__ == "__main__":
     build(verbose=True)
+    build_host(verbose=True)

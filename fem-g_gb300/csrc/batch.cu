@@ -560,6 +560,10 @@ extern "C" int fg_batch_run(fg_batch *b, double *const *csr_values, double *cons
   FG_CUDA(cudaEventRecord(b->jobsCopied, s));
   if (!b->tuned) {
     if ((st = tune(b, s))) return st;
+  } else if (profEnabled()) {
+    // with the kernel timer on, the launches run one by one (the graph's
+    // kernels cannot be timed apart), the same launches the graph holds
+    if ((st = runAll(b, s))) return st;
   } else {
     ProfScope prof("fg_batch_graph", s);
     int nSource = 0;

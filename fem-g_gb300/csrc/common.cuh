@@ -19,6 +19,8 @@ void countLaunch(int n = 1);
 // timer (fg_profile_enable) is on; a no-op otherwise.
 // while suspended (stream capture), this thread's ProfScopes record nothing
 void profSuspend(bool on);
+// whether the kernel timer is on (fg_profile_enable)
+bool profEnabled();
 
 class ProfScope {
  public:

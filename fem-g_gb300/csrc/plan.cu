@@ -21,10 +21,8 @@
 
 namespace femg {
 
-static thread_local std::string g_lastError;
 static std::atomic<int64_t> g_launches{0};
 
-void setLastError(const std::string &msg) { g_lastError = msg; }
 void countLaunch(int n) { g_launches += n; }
 
 namespace {
@@ -57,6 +55,7 @@ cudaEvent_t takeEvent() {
 
 static thread_local bool t_profSuspended = false;
 void profSuspend(bool on) { t_profSuspended = on; }
+bool profEnabled() { return g_profOn.load(); }
 
 ProfScope::ProfScope(const char *name, cudaStream_t s) : name_(name), s_(s) {
   if (!g_profOn.load() || t_profSuspended) return;
@@ -887,7 +886,6 @@ int fg_profile_read(char *names, int32_t name_bytes, int64_t *launches, double *
   return (int)order.size();
 }
 
-const char *fg_last_error(void) { return g_lastError.c_str(); }
 
 int64_t fg_launch_count(void) { return g_launches.load(); }
 

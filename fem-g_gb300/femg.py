@@ -13,6 +13,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libfemg.so")
+HOST_LIB_PATH = os.path.join(HERE, "_build", "libfemg_host.so")
 
 FG_OK, FG_ERR_ARG, FG_ERR_OOM, FG_ERR_CUDA, FG_ERR_INDEX, FG_ERR_TIMEOUT, FG_ERR_UNSUPPORTED, FG_ERR_NO_DEVICE = range(8)
 FG_TERM_GRAD_GRAD, FG_TERM_MASS, FG_TERM_ELASTIC, FG_TERM_SOURCE, FG_TERM_GRAD_GRAD_TENSOR, FG_TERM_MASS_TENSOR = range(6)
@@ -90,6 +91,7 @@ class ProblemConfig(C.Structure):
 
 
 _lib = None
+_host_lib = None
 
 
 def lib():
@@ -99,7 +101,23 @@ def lib():
         return _lib
     if not os.path.exists(LIB_PATH):
         raise RuntimeError("libfemg.so is not built: run __graft_entry__.build()")
-    L = C.CDLL(LIB_PATH)
+    _lib = _bind(C.CDLL(LIB_PATH))
+    return _lib
+
+
+def host_lib():
+    """Load libfemg_host.so: the host mirror alone (problem set-up and pre(),
+    no GPU code), for processes that must not map the GPU library."""
+    global _host_lib
+    if _host_lib is not None:
+        return _host_lib
+    if not os.path.exists(HOST_LIB_PATH):
+        raise RuntimeError("libfemg_host.so is not built: run __graft_entry__.build()")
+    _host_lib = _bind(C.CDLL(HOST_LIB_PATH))
+    return _host_lib
+
+
+def _bind(L):
     P = C.c_void_p
     sig = {
         "fg_plan_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(RuleDesc), C.POINTER(SpaceDesc), C.POINTER(SystemDesc), C.POINTER(P)]),
@@ -139,10 +157,11 @@ def lib():
         "fg_problem_assemble": (C.c_int, [P, C.c_int32, P, P, P]),
     }
     for name, (res, args) in sig.items():
+        if not hasattr(L, name):  # the host-only library has the fg_problem_* calls alone
+            continue
         f = getattr(L, name)
         f.restype = res
         f.argtypes = args
-    _lib = L
     return L
 
 
@@ -171,9 +190,9 @@ def profile_read():
     return {n: (int(cnt[i]), float(ms[i])) for i, n in enumerate(names)}
 
 
-def check(status):
+def check(status, L=None):
     if status != FG_OK:
-        raise FgError(status, lib().fg_last_error().decode())
+        raise FgError(status, (L or lib()).fg_last_error().decode())
 
 
 def _arr(ptr, count, dtype):
@@ -231,23 +250,25 @@ def config_c4(n=64, seed=4, m_lo=8, m_hi=48, orders=(1, 2, 3, 4), k_lo=5.0, k_hi
 
 
 class Problem:
-    """A problem built by the host mirror (mesh, field, terms, pre())."""
+    """A problem built by the host mirror (mesh, field, terms, pre()).
+    host_only: through libfemg_host.so, without loading the GPU library."""
 
-    def __init__(self, cfg):
-        L = lib()
+    def __init__(self, cfg, host_only=False):
+        L = host_lib() if host_only else lib()
+        self._L = L
         self.ptr = C.c_void_p()
-        check(L.fg_problem_create(C.byref(cfg), C.byref(self.ptr)))
+        check(L.fg_problem_create(C.byref(cfg), C.byref(self.ptr)), L)
         self.cfg = cfg
         self.mesh, self.rule, self.space, self.sys = MeshDesc(), RuleDesc(), SpaceDesc(), SystemDesc()
         self.terms_ptr = C.POINTER(TermDesc)()
         self.n_terms = C.c_int32()
         self.dir_ptr = C.POINTER(C.c_double)()
         check(L.fg_problem_descs(self.ptr, C.byref(self.mesh), C.byref(self.rule), C.byref(self.space), C.byref(self.sys),
-                                 C.byref(self.terms_ptr), C.byref(self.n_terms), C.byref(self.dir_ptr)))
+                                 C.byref(self.terms_ptr), C.byref(self.n_terms), C.byref(self.dir_ptr)), L)
 
     def close(self):
         if self.ptr:
-            lib().fg_problem_destroy(self.ptr)
+            self._L.fg_problem_destroy(self.ptr)
             self.ptr = C.c_void_p()
 
     def __del__(self):
@@ -301,7 +322,7 @@ class Problem:
         return self.terms_ptr, self.n_terms.value
 
     def raw_dofs(self):
-        L = lib()
+        L = self._L
         n = L.fg_problem_n_dofs(self.ptr)
         nt = np.zeros(n, np.uint64)
         ent = np.zeros(n, np.uint64)
@@ -312,7 +333,7 @@ class Problem:
         return dict(num_type=nt, entity=ent, num_dof=nd, assemble_type=at, xyz=xyz)
 
     def created_dofs(self):
-        L = lib()
+        L = self._L
         n = L.fg_problem_n_dofs(self.ptr)
         nt = np.zeros(n, np.uint64)
         ent = np.zeros(n, np.uint64)
@@ -322,7 +343,7 @@ class Problem:
         return dict(num_type=nt, entity=ent, assemble_type=at, xyz=xyz)
 
     def reserve_log(self):
-        L = lib()
+        L = self._L
         n = L.fg_problem_reserve_log(self.ptr, None, None, 0)
         at = np.zeros(n, np.uint64)
         arg = np.zeros(n, np.uint64)
@@ -331,11 +352,11 @@ class Problem:
 
     def bbox(self):
         b = np.zeros(6)
-        check(lib().fg_problem_bbox(self.ptr, b.ctypes.data))
+        check(self._L.fg_problem_bbox(self.ptr, b.ctypes.data), self._L)
         return b
 
     def pre_seconds(self):
-        return lib().fg_problem_pre_seconds(self.ptr)
+        return self._L.fg_problem_pre_seconds(self.ptr)
 
     def plan(self):
         return Plan(self)

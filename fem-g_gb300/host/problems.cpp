@@ -1,6 +1,8 @@
 // C ABI of the host mirror (include/fem_g_gb300_host.h): builds the benchmark
 // problems the way a GmshFEM user program does (mesh, field, constraints,
 // Formulation::integral, pre) and hands their descriptors to the GPU plan.
+// Host code only: fg_problem_assemble, which drives the GPU, is in
+// problem_assemble.cpp, so this file also builds the host-only library.
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -15,13 +17,8 @@ namespace femg {
 void setLastError(const std::string &msg);
 }
 
-struct fg_problem {
-  fg_problem_config cfg;
-  femg::Mesh mesh;
-  std::unique_ptr<femg::Field> u;
-  std::unique_ptr<femg::Formulation> form;
-  fg_plan *plan = nullptr;
-};
+#include "problem_internal.h"
+
 
 using namespace femg;
 
@@ -123,7 +120,7 @@ int fg_problem_create(const fg_problem_config *cfg, fg_problem **out) {
 
 void fg_problem_destroy(fg_problem *p) {
   if (!p) return;
-  if (p->plan) fg_plan_destroy(p->plan);
+  if (p->plan && p->destroyPlan) p->destroyPlan(p->plan);
   delete p;
 }
 
@@ -194,22 +191,5 @@ int fg_problem_bbox(const fg_problem *p, double *bbox) {
 }
 
 double fg_problem_pre_seconds(const fg_problem *p) { return p ? p->form->preSeconds : -1.0; }
-
-int fg_problem_assemble(fg_problem *p, int32_t precision, double *csr_values, double *rhs, void *stream) {
-  if (!p) return FG_ERR_ARG;
-  fg_mesh_desc m;
-  fg_rule_desc r;
-  fg_space_desc s;
-  fg_system_desc y;
-  p->form->descs(&m, &r, &s, &y);
-  if (!p->plan) {
-    int st = fg_plan_create(&m, &r, &s, &y, &p->plan);
-    if (st != FG_OK) return st;
-  }
-  const auto &t = p->form->termDescs;
-  const double *dir = p->form->nFixed ? p->form->dirichlet.data() : nullptr;
-  if (precision == 0) return fg_assemble_fp64(p->plan, t.data(), (int32_t)t.size(), 0.0, dir, csr_values, rhs, stream);
-  return fg_assemble_mixed(p->plan, t.data(), (int32_t)t.size(), 0.0, dir, csr_values, rhs, stream, nullptr);
-}
 
 }  // extern "C"

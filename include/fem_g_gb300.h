@@ -319,7 +319,9 @@ typedef struct fg_batch fg_batch;
  * from the built-in autotuner on the first run. */
 int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const *terms, const int32_t *n_terms,
                     int32_t n_problems, int32_t mixed, fg_batch **out);
-/* values[p] / rhs[p]: device or host output arrays per problem (NULL rhs allowed) */
+/* values[p] / rhs[p]: device or host output arrays per problem (NULL rhs allowed).
+ * While the kernel timer is on (fg_profile_enable), a run issues the graph's
+ * launches one by one instead of the graph, so that each kernel is timed. */
 int fg_batch_run(fg_batch *batch, double *const *csr_values, double *const *rhs, void *stream);
 void fg_batch_destroy(fg_batch *batch);
 /* JSON description of the shapes the autotuner chose in the first run
