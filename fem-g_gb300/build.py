@@ -18,11 +18,11 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libfemg.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CUDA_SOURCES = ["csrc/plan.cu", "csrc/assemble_fp64.cu", "csrc/assemble_fp64f.cu", "csrc/assemble_mixed.cu", "csrc/gather.cu", "csrc/assemble_static.cu", "csrc/multi_freq.cu", "csrc/batch.cu", "csrc/pattern.cu", "csrc/numbering.cu"]
+CUDA_SOURCES = ["csrc/plan.cu", "csrc/assemble_fp64.cu", "csrc/assemble_fp64f.cu", "csrc/assemble_mixed.cu", "csrc/gather.cu", "csrc/assemble_static.cu", "csrc/multi_freq.cu", "csrc/batch.cu", "csrc/pattern.cu", "csrc/numbering.cu", "csrc/fused.cu"]
 HOST_ONLY_SOURCES = ["host/errors.cpp", "host/mesh.cpp", "host/refelem.cpp", "host/dofs.cpp", "host/formulation.cpp",
                      "host/problems.cpp"]
 HOST_SOURCES = HOST_ONLY_SOURCES + ["host/problem_assemble.cpp"]
-HEADERS = ["csrc/common.cuh", "host/mesh.h", "host/refelem.h", "host/dofs.h", "host/formulation.h", "host/problem_internal.h"]
+HEADERS = ["csrc/common.cuh", "csrc/tc_ptx.cuh", "host/mesh.h", "host/refelem.h", "host/dofs.h", "host/formulation.h", "host/problem_internal.h"]
 HOST_LIB = os.path.join(BUILD, "libfemg_host.so")
 
 

@@ -33,7 +33,6 @@ constexpr int kBM = 128;       // rows (element components) per tile = TMEM lane
 constexpr int kKp = 8;         // factor columns (7 used)
 constexpr int kK3 = 3 * kKp;   // K' of the 3xTF32 chain
 constexpr int kThreadsGemm = 256;
-constexpr long long kWaitCycles = 4000000000LL;  // ~2 s bound on any device-side wait
 
 struct MixedState {
   int built = 0;
@@ -90,157 +89,7 @@ static int checkTimeout(MixedState *m, bool wait) {
   return FG_OK;
 }
 
-// ------------------------------------------------------------ TF32 split
-
-// round-to-nearest (ties away from zero) of an fp32 value to TF32 (10 mantissa bits)
-__host__ __device__ inline float tf32Round(float x) {
-  uint32_t b;
-  memcpy(&b, &x, 4);
-  if ((b & 0x7F800000u) == 0x7F800000u) return x;  // inf / nan
-  b = (b + 0x1000u) & 0xFFFFE000u;
-  float r;
-  memcpy(&r, &b, 4);
-  return r;
-}
-
-__host__ __device__ inline void splitTf32(double x, float &hi, float &lo) {
-  hi = tf32Round((float)x);
-  lo = tf32Round((float)(x - (double)hi));
-}
-
-// The same split on the device with one FP64 operation (GB300's FP64 pipe is
-// narrow): x rounded to 11 significant bits on its bit pattern (ties away
-// from zero, the carry runs into the exponent), the exact remainder rounded
-// the same way, each narrowed to float by moving the exponent.
-__device__ inline double roundTf32Bits(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  return __longlong_as_double((long long)((b + (1ull << 41)) & ~((1ull << 42) - 1ull)));
-}
-__device__ inline float narrowTf32(double h) {  // h has at most 11 significant bits
-  const unsigned long long b = (unsigned long long)__double_as_longlong(h);
-  const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
-  if (e <= 0 || e >= 255) return (float)h;  // zero, float subnormal, overflow, inf/nan
-  return __uint_as_float(((uint32_t)(b >> 32) & 0x80000000u) | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7FFFFFu));
-}
-__device__ inline void splitTf32Dev(double x, float &hi, float &lo) {
-  const double h = roundTf32Bits(x);
-  hi = narrowTf32(h);
-  lo = narrowTf32(roundTf32Bits(x - h));  // x - h is exact
-}
-
-// ------------------------------------------------------- PTX primitives
-
-__device__ inline uint32_t smemAddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// shared-memory matrix descriptor: K-major, no swizzle, 8x16B core matrices
-__device__ inline uint64_t smemDesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
-  return d;               // base offset 0, relative LBO, SWIZZLE_NONE
-}
-
-// instruction descriptor: kind::tf32, D fp32, A/B tf32 K-major, M x N
-__device__ inline uint32_t idescTf32(int M, int N) {
-  uint32_t d = 0;
-  d |= 1u << 4;                       // D format F32
-  d |= 2u << 7;                       // A format TF32
-  d |= 2u << 10;                      // B format TF32
-  d |= (uint32_t)(N >> 3) << 17;
-  d |= (uint32_t)(M >> 4) << 24;
-  return d;
-}
-
-__device__ inline void tmemAlloc(uint32_t *dst, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(dst)), "r"(ncols) : "memory");
-}
-__device__ inline void tmemRelinquish() { asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory"); }
-__device__ inline void tmemDealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ inline void mmaTf32(uint32_t dTmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dTmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-__device__ inline void mmaCommit(uint64_t *mbar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smemAddr(mbar)) : "memory");
-}
-__device__ inline void tcFenceBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ inline void tcFenceAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ inline void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ inline void mbarInit(uint64_t *mbar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(mbar)), "r"(count) : "memory");
-}
-__device__ inline void fenceMbarInit() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ inline bool mbarTryWait(uint64_t *mbar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(smemAddr(mbar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait; false on timeout
-__device__ inline bool mbarWait(uint64_t *mbar, uint32_t parity) {
-  const long long t0 = clock64();
-  while (!mbarTryWait(mbar, parity))
-    if (clock64() - t0 > kWaitCycles) return false;
-  return true;
-}
-// TMA: the arrival that announces `bytes` of transaction on the barrier,
-// and a 2D tiled load of box {4 floats, 128 rows} at (x, y) completing on it
-__device__ inline void mbarExpectTx(uint64_t *mbar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(mbar)), "r"(bytes) : "memory");
-}
-__device__ inline void tmaLoad2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint64_t *mbar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smemAddr(mbar))
-      : "memory");
-}
-
-// TMA bulk copy (no tensor map) of `bytes` (a multiple of 16, both
-// addresses 16-byte aligned) completing on the barrier
-__device__ inline void bulkLoad(uint32_t dst, const void *src, uint32_t bytes, uint64_t *mbar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smemAddr(mbar))
-               : "memory");
-}
-
-__device__ inline void tmemLoad16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
-        "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr)
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
-}
-
-__device__ inline void tmemLoad32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
-        "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
-        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr)
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
-}
+#include "tc_ptx.cuh"
 
 // ------------------------------------------------- geometry: factor rows
 
@@ -248,7 +97,10 @@ __device__ inline void tmemLoad32(uint32_t taddr, float *v) {
 // first quadrature point (affine elements: the geometric Jacobian is constant), per-element coefficients,
 // factors D_e split into TF32 hi/lo, written as row [hi | lo | hi] at the
 // element's rank in the orientation-sorted order.
-template <bool TENSOR>
+// ROWF: floats per factor row, 24 ([hi | lo | hi], the split contraction) or
+// 16 ([hi | lo], the fused kernel, which reuses hi for the third product);
+// rankOf null: rows in element order.
+template <bool TENSOR, int ROWF = kK3>
 __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *__restrict__ terms, const int32_t *__restrict__ rankOf,
                                               float *__restrict__ A, int ncomp, int rowsPerElem, int rowOff, int64_t e) {
   double X[kMaxNodes * 3];
@@ -290,7 +142,7 @@ __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *
     else if (T.kind == FG_TERM_MASS) cm = cadd(cm, fv);
   }
   const double idet = 1.0 / det;
-  const int64_t r0 = (int64_t)rankOf[e] * rowsPerElem + rowOff;
+  const int64_t r0 = (rankOf ? (int64_t)rankOf[e] : e) * rowsPerElem + rowOff;
   // tensor grad-grad term (TENSOR: the terms have one; a separate
   // instantiation keeps the scalar kernel's registers):
   // det J^-1 A J^-T = C^T A C / det in place of c det K
@@ -320,14 +172,16 @@ __device__ __forceinline__ void factorsScalar(const PlanDev &p, const DevTerms *
     }
     splitTf32Dev(m, hi[6], lo[6]);
     hi[7] = lo[7] = 0.0f;
-    // [hi | lo | hi] as 16-byte stores (rows are 96 bytes)
-    float4 *row = reinterpret_cast<float4 *>(A + (r0 + comp) * kK3);
+    // [hi | lo | hi] (or [hi | lo]) as 16-byte stores (rows are 96 or 64 bytes)
+    float4 *row = reinterpret_cast<float4 *>(A + (r0 + comp) * ROWF);
     row[0] = make_float4(hi[0], hi[1], hi[2], hi[3]);
     row[1] = make_float4(hi[4], hi[5], hi[6], hi[7]);
     row[2] = make_float4(lo[0], lo[1], lo[2], lo[3]);
     row[3] = make_float4(lo[4], lo[5], lo[6], lo[7]);
-    row[4] = row[0];
-    row[5] = row[1];
+    if (ROWF == kK3) {
+      row[4] = row[0];
+      row[5] = row[1];
+    }
   }
 }
 
@@ -336,6 +190,24 @@ __global__ void k_factors(const PlanDev p, const DevTerms *__restrict__ terms, c
                           int ncomp, int rowsPerElem, int rowOff) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e < p.E) factorsScalar<TENSOR>(p, terms, rankOf, A, ncomp, rowsPerElem, rowOff, e);
+}
+
+// Factor rows [hi | lo] in element order for the fused kernel (one
+// component: real element matrices)
+template <bool TENSOR>
+__global__ void k_factors_compact(const PlanDev p, const DevTerms *__restrict__ terms, float *__restrict__ A) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < p.E) factorsScalar<TENSOR, 16>(p, terms, nullptr, A, 1, 1, 0, e);
+}
+
+int launchFactorsCompact(const PlanDev &p, const DevTerms *dterms, bool tensor, float *A16, cudaStream_t s) {
+  if (p.E == 0) return FG_OK;
+  ProfScope prof("k_factors_compact", s);
+  if (tensor) k_factors_compact<true><<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms, A16);
+  else k_factors_compact<false><<<(unsigned)((p.E + 127) / 128), 128, 0, s>>>(p, dterms, A16);
+  countLaunch();
+  FG_CUDA(cudaGetLastError());
+  return FG_OK;
 }
 
 // Compound field with the isotropic Tensor4 term: for every component pair
@@ -529,11 +401,6 @@ struct GemmSched {
   int tma;           // A tiles by TMA through aMap (one problem), else by cp.async
 };
 
-__device__ inline void cpAsync16(uint32_t dst, const void *src, uint32_t srcBytes) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(srcBytes) : "memory");
-}
-__device__ inline void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ inline void cpAsyncWaitAll() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // A tile of rows [row0, row0 + nrows) into the core-matrix image at As:
 // row r, 16-byte chunk kc -> core matrix (r/8, kc), K-direction stride 2048 B;
@@ -906,9 +773,11 @@ static MixedState *state(fg_plan *plan) {
 //  compound field (kp = 16): T[3p+p'] = sum_q w d_p phi_j d_p' phi_i, T[9] = sum_q w phi_i phi_j
 //  HCurl field (kp = 16):    T[ab] as the scalar field's with the reference curls c,
 //                            T[6 + ab] the same with the reference vector values v
-static void buildB(const PlanDev &p, const std::vector<double> &w, const std::vector<double> &bval, const std::vector<double> &bgrad,
-                   int o, int Npad, int kp, std::vector<float> &img) {
-  const int nb = p.nb, nq = p.nq, k3 = 3 * kp;
+// compact: K' = 2 kp, [B_hi ; B_lo] (the fused kernel's image; its third
+// product reads B_hi again)
+void buildB(const PlanDev &p, const std::vector<double> &w, const std::vector<double> &bval, const std::vector<double> &bgrad,
+            int o, int Npad, int kp, std::vector<float> &img, bool compact) {
+  const int nb = p.nb, nq = p.nq, k3 = (compact ? 2 : 3) * kp;
   img.assign((size_t)Npad * k3, 0.0f);
   const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
   std::vector<double> T(kp);
@@ -945,8 +814,8 @@ static void buildB(const PlanDev &p, const std::vector<double> &w, const std::ve
       for (int k = 0; k < kp; ++k) {
         float hi, lo;
         splitTf32(T[k], hi, lo);
-        const float vals[3] = {hi, hi, lo};  // K' blocks: [B_hi ; B_hi ; B_lo]
-        for (int blk = 0; blk < 3; ++blk) {
+        const float vals[3] = {hi, compact ? lo : hi, lo};  // K' blocks: [B_hi ; B_hi ; B_lo] or [B_hi ; B_lo]
+        for (int blk = 0; blk < (compact ? 2 : 3); ++blk) {
           const int kk = blk * kp + k;
           const int kc = kk >> 2, within = kk & 3;
           const size_t off = (size_t)kc * (Npad * 4) + (size_t)(row >> 3) * 32 + (row & 7) * 4 + within;  // in floats
@@ -1099,7 +968,7 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
     FG_CUDA(cudaMemcpy(bgrad.data(), p.bgrad, bgrad.size() * 8, cudaMemcpyDeviceToHost));
     std::vector<float> all((size_t)p.nOrient * m->Npad * m->k3), img;
     for (int o = 0; o < p.nOrient; ++o) {
-      buildB(p, w, bval, bgrad, o, m->Npad, m->kp, img);
+      buildB(p, w, bval, bgrad, o, m->Npad, m->kp, img, false);
       std::copy(img.begin(), img.end(), all.begin() + (size_t)o * m->Npad * m->k3);
     }
     FG_CUDA(cudaMalloc(&m->B, all.size() * 4));
@@ -1282,6 +1151,24 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
   if (report && plan->accumulate) {
     setLastError("mixed path: the error report compares overwritten values; the plan accumulates");
     return FG_ERR_ARG;
+  }
+  if (!report && fusedApplies(plan, dt)) {
+    // contraction and reduction in one kernel: no element matrix in HBM
+    const double *uD0 = nullptr;
+    if ((st = uploadDirichlet(plan, dirichlet, &uD0, s))) return st;
+    Outputs o;
+    if ((st = prepareOutputs(plan, csr_values, rhs, &o))) return st;
+    const PlanDev &p = plan->d;
+    double *be = nullptr;
+    if (dt.hasSource && rhs) {
+      if ((st = ensureDevice((void **)&plan->be, &plan->beBytes, (size_t)p.E * p.n * 16))) return st;
+      be = plan->be;
+      if ((st = launchRhsFp64(plan, dterms, be, s))) return st;
+    }
+    if ((st = launchFused(plan, dt, dterms, (const double2 *)be, (double2 *)o.values, (double2 *)o.rhs, s))) return st;
+    if ((st = finishOutputs(plan, o, csr_values, rhs, s))) return st;
+    if (o.hostValues || (rhs && o.hostRhs)) return fusedTimeout(plan, true);
+    return FG_OK;
   }
   if ((st = prepareMixed(plan, dt.complexKe ? 2 : 1, 1))) return st;
   if ((st = checkTimeout(state(plan), false))) return st;  // a timeout of an earlier call

@@ -180,6 +180,9 @@ struct fg_plan {
   void *fp64f = nullptr;
   int fp64Method = 0;  // FG_FP64_* (FG_FP64_QUADRATURE)
   int accumulate = 0;  // add into device outputs instead of overwriting them (fg_plan_set_accumulate)
+  // fused mixed path (contraction and reduction in one kernel), see fused.cu
+  void *fused = nullptr;
+  int mixedFused = 1;  // fg_plan_set_mixed_fused
   int *jmErrHost = nullptr;  // pinned copy of d.jmErr
 };
 
@@ -230,6 +233,18 @@ int finishOutputs(fg_plan *plan, const Outputs &o, double *csr_values, double *r
 // range's slice copied to the host on a second stream while the next reduces
 int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, KeLayout lay, const double *be,
                     const double *dirichletDev, Outputs &o, double *csr_values, cudaStream_t s);
+// Fused mixed path: whether a call of these terms runs fused (builds the
+// block records on first use), the launch, and its wait-timeout report
+bool fusedApplies(fg_plan *plan, const DevTerms &dt);
+int launchFused(fg_plan *plan, const DevTerms &dt, const DevTerms *dterms, const double2 *be, double2 *values, double2 *rhs,
+                cudaStream_t s);
+int fusedTimeout(fg_plan *plan, bool wait);
+// Factor rows [hi | lo] (16 floats) in element order for the fused kernel
+int launchFactorsCompact(const PlanDev &p, const DevTerms *dterms, bool tensor, float *A16, cudaStream_t s);
+// B' image of orientation o in the shared-memory core-matrix layout (Npad x K'
+// floats; compact: K' = 2 kp [B_hi ; B_lo], else 3 kp [B_hi ; B_hi ; B_lo])
+void buildB(const PlanDev &p, const std::vector<double> &w, const std::vector<double> &bval, const std::vector<double> &bgrad,
+            int o, int Npad, int kp, std::vector<float> &img, bool compact);
 // FP64 element kernel (also used as the reference for the mixed error report)
 int launchElementFp64(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s);
 // One plan of a batched gather launch

@@ -795,6 +795,7 @@ int fg_plan_create(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_
 void mixedDestroy(fg_plan *plan);
 void multiDestroy(fg_plan *plan);
 void fp64fDestroy(fg_plan *plan);
+void fusedDestroy(fg_plan *plan);
 
 void fg_plan_destroy(fg_plan *plan) {
   if (!plan) return;
@@ -811,6 +812,7 @@ void fg_plan_destroy(fg_plan *plan) {
   mixedDestroy(plan);
   multiDestroy(plan);
   fp64fDestroy(plan);
+  fusedDestroy(plan);
   if (plan->jmErrHost) cudaFreeHost(plan->jmErrHost);
   for (cudaEvent_t ev : plan->copyEvents)
     if (ev) cudaEventDestroy(ev);

@@ -281,10 +281,27 @@ int fg_plan_set_fp64_method(fg_plan *plan, int32_t method);
  * a plan. Default 0. */
 int fg_plan_set_accumulate(fg_plan *plan, int32_t accumulate);
 /* Mixed precision: FP64 geometry, 3xTF32 tcgen05 contraction with FP32
- * accumulation, FP64 CSR reduction. report may be NULL (no error report). */
+ * accumulation, FP64 CSR reduction. report may be NULL (no error report).
+ * Where it applies (one-component H1 fields whose element orientations only
+ * flip basis signs, affine elements, real element-constant coefficients, no
+ * fixed or linked DOFs, no error report) the contraction and the reduction
+ * run fused in one kernel over blocks of consecutive CSR rows, and no element
+ * matrix is written to device memory; elsewhere, and with
+ * fg_plan_set_mixed_fused(plan, 0), the contraction writes FP32 element
+ * matrices that a separate reduction reads. */
 int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency,
                       const double *dirichlet, double *csr_values, double *rhs, void *stream,
                       fg_err_report *report);
+
+/* Fused mixed path on (1, the default) or off (0) for this plan. */
+int fg_plan_set_mixed_fused(fg_plan *plan, int32_t on);
+/* Whether the fused mixed path applies to the plan (building its block
+ * records on first use), its number of row blocks, the mean elements per
+ * block and the contractions per element (>= 1: an element whose DOF rows
+ * fall in several blocks is contracted in each). When it does not apply,
+ * fg_last_error() says why. */
+int fg_plan_fused_info(fg_plan *plan, int32_t *applies, int32_t *blocks, double *elems_per_block,
+                       double *contractions_per_element);
 
 /* The system at n_freq angular frequencies in one pass: what n_freq calls of
  * fg_assemble_fp64 (mixed == 0) or fg_assemble_mixed (mixed != 0) with
