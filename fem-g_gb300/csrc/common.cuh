@@ -348,6 +348,115 @@ __device__ inline double widen(float x) {
 }
 __device__ inline double widen(double x) { return x; }
 
+// Complex elementary functions of the coefficient language (the scalar
+// operators of src/function/scalarUnaryOperators.h on std::complex<double>),
+// written from their definitions with CUDA's real math functions, principal
+// branches as in C99 Annex G / std::complex:
+//   exp z = e^x (cos y, sin y); ln z = (ln|z|, arg z); sqrt by the half-angle
+//   form with the sign of y; sin, cos, sinh, cosh by the addition theorems;
+//   tan = sin / cos, tanh = sinh / cosh; the inverse functions through ln and
+//   sqrt: asin z = -i ln(i z + sqrt(1 - z^2)), acos z = pi/2 - asin z,
+//   atan z = (i/2) (ln(1 - i z) - ln(1 + i z)), asinh z = ln(z + sqrt(z^2 + 1)),
+//   acosh z = ln(z + sqrt(z + 1) sqrt(z - 1)), atanh z = (ln(1 + z) - ln(1 - z)) / 2;
+//   z^p for a real power p: x^p when z is real and positive, else
+//   |z|^p (cos p arg z, sin p arg z), as std::pow(complex, real) does.
+__device__ inline double2 cexpD(double2 z) {
+  double s, c;
+  sincos(z.y, &s, &c);
+  const double e = exp(z.x);
+  return make_double2(e * c, e * s);
+}
+__device__ inline double2 clnD(double2 z) { return make_double2(log(hypot(z.x, z.y)), atan2(z.y, z.x)); }
+__device__ inline double2 csqrtD(double2 z) {
+  if (z.x == 0.0 && z.y == 0.0) return make_double2(0.0, z.y);
+  const double t = sqrt(0.5 * (hypot(z.x, z.y) + fabs(z.x)));
+  if (z.x >= 0.0) return make_double2(t, z.y / (2.0 * t));
+  return make_double2(fabs(z.y) / (2.0 * t), copysign(t, z.y));
+}
+__device__ inline double2 csinD(double2 z) {
+  double s, c;
+  sincos(z.x, &s, &c);
+  return make_double2(s * cosh(z.y), c * sinh(z.y));
+}
+__device__ inline double2 ccosD(double2 z) {
+  double s, c;
+  sincos(z.x, &s, &c);
+  return make_double2(c * cosh(z.y), -s * sinh(z.y));
+}
+__device__ inline double2 csinhD(double2 z) {
+  double s, c;
+  sincos(z.y, &s, &c);
+  return make_double2(sinh(z.x) * c, cosh(z.x) * s);
+}
+__device__ inline double2 ccoshD(double2 z) {
+  double s, c;
+  sincos(z.y, &s, &c);
+  return make_double2(cosh(z.x) * c, sinh(z.x) * s);
+}
+__device__ inline double2 cpowRealD(double2 z, double p) {
+  if (z.y == 0.0 && z.x > 0.0) return make_double2(pow(z.x, p), 0.0);
+  const double r = pow(hypot(z.x, z.y), p), th = p * atan2(z.y, z.x);
+  double s, c;
+  sincos(th, &s, &c);
+  return make_double2(r * c, r * s);
+}
+__device__ inline double2 cUnary(int op, int arg, double2 z) {
+  const double2 one = make_double2(1.0, 0.0);
+  const double2 iz = make_double2(-z.y, z.x);  // i z
+  switch (op) {
+    case FG_OP_SQRT: return csqrtD(z);
+    case FG_OP_EXP: return cexpD(z);
+    case FG_OP_LN: return clnD(z);
+    case FG_OP_LOG10: {
+      const double2 l = clnD(z);
+      const double k = 1.0 / log(10.0);
+      return make_double2(l.x * k, l.y * k);
+    }
+    case FG_OP_POW: {
+      if (arg == 1) return z;
+      if (arg == 2) return cmul(z, z);
+      if (arg == 3) return cmul(cmul(z, z), z);
+      if (arg == 4) {
+        const double2 z2 = cmul(z, z);
+        return cmul(z2, z2);
+      }
+      return cpowRealD(z, (double)arg);
+    }
+    case FG_OP_CBRT: return cpowRealD(z, 1.0 / 3.0);
+    case FG_OP_SIN: return csinD(z);
+    case FG_OP_COS: return ccosD(z);
+    case FG_OP_TAN: return cdiv(csinD(z), ccosD(z));
+    case FG_OP_SINH: return csinhD(z);
+    case FG_OP_COSH: return ccoshD(z);
+    case FG_OP_TANH: return cdiv(csinhD(z), ccoshD(z));
+    case FG_OP_ASIN: {
+      const double2 w = clnD(cadd(iz, csqrtD(make_double2(1.0 - (z.x * z.x - z.y * z.y), -2.0 * z.x * z.y))));
+      return make_double2(w.y, -w.x);  // -i w
+    }
+    case FG_OP_ACOS: {
+      const double2 a = cUnary(FG_OP_ASIN, 0, z);
+      return make_double2(1.5707963267948966 - a.x, -a.y);
+    }
+    case FG_OP_ATAN: {
+      const double2 a = clnD(make_double2(1.0 - iz.x, -iz.y)), b = clnD(cadd(one, iz));
+      const double2 d = make_double2(a.x - b.x, a.y - b.y);
+      return make_double2(-0.5 * d.y, 0.5 * d.x);  // (i / 2) d
+    }
+    case FG_OP_ASINH: return clnD(cadd(z, csqrtD(make_double2(z.x * z.x - z.y * z.y + 1.0, 2.0 * z.x * z.y))));
+    case FG_OP_ACOSH:
+      return clnD(cadd(z, cmul(csqrtD(make_double2(z.x + 1.0, z.y)), csqrtD(make_double2(z.x - 1.0, z.y)))));
+    case FG_OP_ATANH: {
+      const double2 a = clnD(make_double2(1.0 + z.x, z.y)), b = clnD(make_double2(1.0 - z.x, -z.y));
+      return make_double2(0.5 * (a.x - b.x), 0.5 * (a.y - b.y));
+    }
+    case FG_OP_ABS: return make_double2(hypot(z.x, z.y), 0.0);
+    case FG_OP_CONJ: return make_double2(z.x, -z.y);
+    case FG_OP_REAL: return make_double2(z.x, 0.0);
+    case FG_OP_IMAG: return make_double2(z.y, 0.0);
+  }
+  return z;
+}
+
 // Evaluate a coefficient expression at element e and physical point x; phi:
 // the scalar basis values at the point (nb of them) for field nodes, null
 // where the expression is evaluated once per element (field nodes make an
@@ -381,16 +490,23 @@ __device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x
         st[sp - 1] = make_double2(r > 0.0 ? 1.0 : (r < 0.0 ? 0.0 : 0.5), 0.0);
         break;
       }
-      default: {
+      case FG_OP_ADD:
+      case FG_OP_SUB:
+      case FG_OP_MUL:
+      case FG_OP_DIV:
+      case FG_OP_ATAN2: {
         const double2 b = st[--sp];
         const double2 a = st[sp - 1];
         double2 r;
         if (in.op == FG_OP_ADD) r = cadd(a, b);
         else if (in.op == FG_OP_SUB) r = make_double2(a.x - b.x, a.y - b.y);
         else if (in.op == FG_OP_MUL) r = cmul(a, b);
-        else r = cdiv(a, b);
+        else if (in.op == FG_OP_DIV) r = cdiv(a, b);
+        else r = make_double2(atan2(a.x, b.x), 0.0);
         st[sp - 1] = r;
+        break;
       }
+      default: st[sp - 1] = cUnary(in.op, in.arg, st[sp - 1]);
     }
   }
   return st[0];

@@ -482,26 +482,67 @@ static int classify(const fg_expr &ex) {
   return cls;
 }
 
+static bool isUnaryOp(int op) { return op == FG_OP_NEG || op == FG_OP_HEAVISIDE || (op >= FG_OP_SQRT && op <= FG_OP_CBRT); }
+static bool isBinaryOp(int op) { return (op >= FG_OP_ADD && op <= FG_OP_DIV) || op == FG_OP_ATAN2; }
+
+// A constant expression, evaluated once on the host with std::complex (the
+// reference's own arithmetic for the same operators).
 static std::complex<double> evalConst(const fg_expr &ex) {
-  std::vector<std::complex<double>> st;
+  using C = std::complex<double>;
+  std::vector<C> st;
   for (int k = 0; k < ex.n_code; ++k) {
     const fg_instr &in = ex.code[k];
-    if (in.op == FG_OP_CONST) st.push_back({in.re, in.im});
-    else if (in.op == FG_OP_NEG) st.back() = -st.back();
-    else if (in.op == FG_OP_HEAVISIDE) {
-      const double r = st.back().real();
-      st.back() = r > 0 ? 1.0 : (r < 0 ? 0.0 : 0.5);
-    } else {
+    if (in.op == FG_OP_CONST) {
+      st.push_back({in.re, in.im});
+      continue;
+    }
+    if (isBinaryOp(in.op)) {
       auto b = st.back();
       st.pop_back();
       auto &a = st.back();
       if (in.op == FG_OP_ADD) a += b;
       else if (in.op == FG_OP_SUB) a -= b;
       else if (in.op == FG_OP_MUL) a *= b;
-      else a /= b;
+      else if (in.op == FG_OP_DIV) a /= b;
+      else a = std::atan2(a.real(), b.real());
+      continue;
+    }
+    C &a = st.back();
+    switch (in.op) {
+      case FG_OP_NEG: a = -a; break;
+      case FG_OP_HEAVISIDE: a = a.real() > 0 ? 1.0 : (a.real() < 0 ? 0.0 : 0.5); break;
+      case FG_OP_SQRT: a = std::sqrt(a); break;
+      case FG_OP_EXP: a = std::exp(a); break;
+      case FG_OP_LN: a = std::log(a); break;
+      case FG_OP_LOG10: a = std::log10(a); break;
+      case FG_OP_POW: a = in.arg == 1 ? a : in.arg == 2 ? a * a : in.arg == 3 ? a * a * a : in.arg == 4 ? (a * a) * (a * a)
+                                                                                         : std::pow(a, (double)in.arg); break;
+      case FG_OP_CBRT: a = std::pow(a, 1.0 / 3.0); break;
+      case FG_OP_SIN: a = std::sin(a); break;
+      case FG_OP_COS: a = std::cos(a); break;
+      case FG_OP_TAN: a = std::tan(a); break;
+      case FG_OP_SINH: a = std::sinh(a); break;
+      case FG_OP_COSH: a = std::cosh(a); break;
+      case FG_OP_TANH: a = std::tanh(a); break;
+      case FG_OP_ASIN: a = std::asin(a); break;
+      case FG_OP_ACOS: a = std::acos(a); break;
+      case FG_OP_ATAN: a = std::atan(a); break;
+      case FG_OP_ASINH: a = std::asinh(a); break;
+      case FG_OP_ACOSH: a = std::acosh(a); break;
+      case FG_OP_ATANH: a = std::atanh(a); break;
+      case FG_OP_ABS: a = std::abs(a); break;
+      case FG_OP_CONJ: a = std::conj(a); break;
+      case FG_OP_REAL: a = a.real(); break;
+      case FG_OP_IMAG: a = a.imag(); break;
     }
   }
   return st.empty() ? 0.0 : st.back();
+}
+
+// operators that can give a complex value from real operands
+static bool mayTurnComplex(int op) {
+  return op == FG_OP_SQRT || op == FG_OP_LN || op == FG_OP_LOG10 || op == FG_OP_CBRT || op == FG_OP_ASIN ||
+         op == FG_OP_ACOS || op == FG_OP_ACOSH || op == FG_OP_ATANH;
 }
 
 static int validateExpr(const fg_expr &ex) {
@@ -514,9 +555,10 @@ static int validateExpr(const fg_expr &ex) {
           (ex.code[k].arg < 0 || ex.code[k].arg >= ex.n_arrays || !ex.elem_values[ex.code[k].arg]))
         return 1;
       if (++depth > 16) return 1;
-    } else if (op == FG_OP_NEG || op == FG_OP_HEAVISIDE) {
+    } else if (isUnaryOp(op)) {
       if (depth < 1) return 1;
-    } else if (op <= FG_OP_DIV) {
+      if (op == FG_OP_POW && ex.code[k].arg < 0) return 1;
+    } else if (isBinaryOp(op)) {
       if (depth < 2) return 1;
       --depth;
     } else {
@@ -542,6 +584,11 @@ static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complex
     if (ex.code[k].op == FG_OP_CONST && ex.code[k].im != 0.0) *complexOut = true;
   }
   out->cls = classify(ex);
+  // a value known only per element or point: an operator that can leave the
+  // reals makes the element matrices complex (a constant is evaluated below)
+  if (out->cls != kExprConst)
+    for (int k = 0; k < ex.n_code; ++k)
+      if (mayTurnComplex(ex.code[k].op)) *complexOut = true;
   if (out->cls == kExprConst) {
     auto v = evalConst(ex);
     out->cval = make_double2(v.real(), v.imag());

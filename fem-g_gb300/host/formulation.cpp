@@ -308,6 +308,35 @@ Function heaviside(const Function &a) {
   return r;
 }
 
+Function Function::unary(const Function &a, int op, int arg) {
+  Function r = a;
+  r.code.push_back({op, arg, 0.0, 0.0});
+  return r;
+}
+Function sqrt(const Function &a) { return Function::unary(a, FG_OP_SQRT); }
+Function exp(const Function &a) { return Function::unary(a, FG_OP_EXP); }
+Function ln(const Function &a) { return Function::unary(a, FG_OP_LN); }
+Function log(const Function &a) { return Function::unary(a, FG_OP_LOG10); }
+Function pow(const Function &a, unsigned n) { return Function::unary(a, FG_OP_POW, (int)n); }
+Function cbrt(const Function &a) { return Function::unary(a, FG_OP_CBRT); }
+Function sin(const Function &a) { return Function::unary(a, FG_OP_SIN); }
+Function cos(const Function &a) { return Function::unary(a, FG_OP_COS); }
+Function tan(const Function &a) { return Function::unary(a, FG_OP_TAN); }
+Function sinh(const Function &a) { return Function::unary(a, FG_OP_SINH); }
+Function cosh(const Function &a) { return Function::unary(a, FG_OP_COSH); }
+Function tanh(const Function &a) { return Function::unary(a, FG_OP_TANH); }
+Function asin(const Function &a) { return Function::unary(a, FG_OP_ASIN); }
+Function acos(const Function &a) { return Function::unary(a, FG_OP_ACOS); }
+Function atan(const Function &a) { return Function::unary(a, FG_OP_ATAN); }
+Function asinh(const Function &a) { return Function::unary(a, FG_OP_ASINH); }
+Function acosh(const Function &a) { return Function::unary(a, FG_OP_ACOSH); }
+Function atanh(const Function &a) { return Function::unary(a, FG_OP_ATANH); }
+Function abs(const Function &a) { return Function::unary(a, FG_OP_ABS); }
+Function conj(const Function &a) { return Function::unary(a, FG_OP_CONJ); }
+Function real(const Function &a) { return Function::unary(a, FG_OP_REAL); }
+Function imag(const Function &a) { return Function::unary(a, FG_OP_IMAG); }
+Function atan2(const Function &a, const Function &b) { return Function::binary(a, b, FG_OP_ATAN2); }
+
 // ------------------------------------------------------------ Field / DSL
 
 Field::Field(const std::string &n, const Domain &d, SpaceType t, int order, int mult, unsigned tg)

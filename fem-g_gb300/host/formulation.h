@@ -91,10 +91,38 @@ class Function {
   friend Function operator/(const Function &a, const Function &b);
   friend Function operator-(const Function &a);
   friend Function heaviside(const Function &a);
+  friend Function atan2(const Function &a, const Function &b);
+  // a unary operator of the coefficient language (FG_OP_SQRT ... FG_OP_CBRT)
+  static Function unary(const Function &a, int op, int arg = 0);
 
  private:
   static Function binary(const Function &a, const Function &b, int op);
 };
+
+// The reference's scalar operators (src/function/scalarUnaryOperators.h:27-120):
+// log() is the decimal logarithm and ln() the natural one, as there.
+Function sqrt(const Function &a);
+Function exp(const Function &a);
+Function ln(const Function &a);
+Function log(const Function &a);
+Function pow(const Function &a, unsigned n);
+Function cbrt(const Function &a);
+Function sin(const Function &a);
+Function cos(const Function &a);
+Function tan(const Function &a);
+Function sinh(const Function &a);
+Function cosh(const Function &a);
+Function tanh(const Function &a);
+Function asin(const Function &a);
+Function acos(const Function &a);
+Function atan(const Function &a);
+Function asinh(const Function &a);
+Function acosh(const Function &a);
+Function atanh(const Function &a);
+Function abs(const Function &a);
+Function conj(const Function &a);
+Function real(const Function &a);
+Function imag(const Function &a);
 
 struct Tensor4Isotropic {  // C_ijkl = lambda d_ij d_kl + mu (d_ik d_jl + d_il d_jk)
   Function lambda, mu;

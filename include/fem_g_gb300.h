@@ -140,9 +140,35 @@ enum {
   FG_OP_DIV = 8,
   FG_OP_NEG = 9,
   FG_OP_HEAVISIDE = 10, /* 1 if Re>0, 0 if Re<0, 0.5 if Re==0 (unaryOperations.h:1008-1021) */
-  FG_OP_FIELD = 11      /* push u(x) = sum_j phi_j(x) u_e[j]: a scalar field of the bucket's own H1 space
+  FG_OP_FIELD = 11,     /* push u(x) = sum_j phi_j(x) u_e[j]: a scalar field of the bucket's own H1 space
                            at the point (field node, fieldOperations.h:160-170); elem_values[arg] is then
                            [n_elements][nb][2], the field's values at each element's local DOFs */
+  /* unary operators on the top of the stack, complex (principal branches), as the reference's
+     scalar operators on std::complex<double> (src/function/scalarUnaryOperators.h:27-120,
+     executionTree/unaryOperations.h) */
+  FG_OP_SQRT = 12,
+  FG_OP_EXP = 13,
+  FG_OP_LN = 14,    /* natural logarithm: the reference's ln() */
+  FG_OP_LOG10 = 15, /* decimal logarithm: the reference's log() */
+  FG_OP_POW = 16,   /* a^arg, arg >= 0 an integer (pow(a, n)) */
+  FG_OP_SIN = 17,
+  FG_OP_COS = 18,
+  FG_OP_TAN = 19,
+  FG_OP_SINH = 20,
+  FG_OP_COSH = 21,
+  FG_OP_TANH = 22,
+  FG_OP_ASIN = 23,
+  FG_OP_ACOS = 24,
+  FG_OP_ATAN = 25,
+  FG_OP_ASINH = 26,
+  FG_OP_ACOSH = 27,
+  FG_OP_ATANH = 28,
+  FG_OP_ABS = 29,   /* |a| */
+  FG_OP_CONJ = 30,
+  FG_OP_REAL = 31,
+  FG_OP_IMAG = 32,
+  FG_OP_CBRT = 33,  /* a^(1/3): real cube root for a > 0, principal complex root otherwise */
+  FG_OP_ATAN2 = 34  /* binary: atan2(Re a, Re b) of the two topmost (scalarBinaryOperators.h:21, real arguments) */
 };
 typedef struct {
   int32_t op;

@@ -31,7 +31,9 @@ typedef double complex cplx;
 
 enum { AT_UNDEFINED = 0, AT_FIXED = 1, AT_UNKNOWN = 2, AT_UNKNOWN_BUBBLE = 3, AT_UNKNOWN_GLOBAL = 4 };
 enum { TERM_GRAD_GRAD = 0, TERM_MASS = 1, TERM_ELASTIC = 2, TERM_SOURCE = 3, TERM_GRAD_GRAD_TENSOR = 4, TERM_MASS_TENSOR = 5 };
-enum { OP_CONST = 0, OP_X, OP_Y, OP_Z, OP_ELEM, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_HEAVISIDE, OP_FIELD };
+enum { OP_CONST = 0, OP_X, OP_Y, OP_Z, OP_ELEM, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_HEAVISIDE, OP_FIELD,
+       OP_SQRT, OP_EXP, OP_LN, OP_LOG10, OP_POW, OP_SIN, OP_COS, OP_TAN, OP_SINH, OP_COSH, OP_TANH, OP_ASIN, OP_ACOS,
+       OP_ATAN, OP_ASINH, OP_ACOSH, OP_ATANH, OP_ABS, OP_CONJ, OP_REAL, OP_IMAG, OP_CBRT, OP_ATAN2 };
 
 /* same memory layout as fg_instr / fg_expr / fg_term_desc of the C ABI, so
  * the tests can pass the product's term descriptors unchanged */
@@ -98,10 +100,67 @@ static int or_dof_row(const or_bucket *b, int t, uint64_t idx, uint64_t *row, cp
 /* Function::evaluate for the operator subset of the ABI
  * (src/function/ScalarFunction.cpp:203-223; nullary x/y/z/constant
  * src/function/executionTree/nullaryOperations.h:284-345,1399-1484; heaviside
- * src/function/executionTree/unaryOperations.h:1008-1021) */
+ * src/function/executionTree/unaryOperations.h:1008-1021; the other unary
+ * operators or_unary above) */
 /* phi: the bucket's scalar basis values at the point (nb of them), for the
  * field-node op: u(x) = sum_j phi_j u_e[j] with the element's DOF values u_e
  * (fieldOperations.h:160-170, Form0 field evaluated on the gauss points) */
+/* z^p for a real power p, as std::pow(complex<double>, double) computes it:
+ * x^p for a real positive z, else |z|^p e^(i p arg z) through the logarithm */
+static cplx or_pow_real(cplx z, double p) {
+  if (cimag(z) == 0.0 && creal(z) > 0.0) return pow(creal(z), p);
+  cplx t = clog(z);
+  double r = exp(p * creal(t)), th = p * cimag(t);
+  return r * cos(th) + I * (r * sin(th));
+}
+
+/* The scalar unary operators of src/function/scalarUnaryOperators.h:27-120
+ * (executionTree/unaryOperations.h) on std::complex<double>, whose functions
+ * are the C99 complex ones: log() is the decimal logarithm (std::log10),
+ * ln() the natural one; pow(a, n) multiplies for n <= 4 (Pow::operator(),
+ * unaryOperations.h:1517-1549) and uses std::pow beyond; cbrt is
+ * std::pow(a, 1/3) for complex scalars. */
+static cplx or_unary(int op, int arg, cplx z) {
+  switch (op) {
+    case OP_NEG: return -z;
+    case OP_HEAVISIDE: {
+      double r = creal(z);
+      return r > 0.0 ? 1.0 : (r < 0.0 ? 0.0 : 0.5);
+    }
+    case OP_SQRT: return csqrt(z);
+    case OP_EXP: return cexp(z);
+    case OP_LN: return clog(z);
+    case OP_LOG10: return clog(z) / log(10.0);
+    case OP_POW:
+      if (arg == 1) return z;
+      if (arg == 2) return z * z;
+      if (arg == 3) return z * z * z;
+      if (arg == 4) {
+        cplx z2 = z * z;
+        return z2 * z2;
+      }
+      return or_pow_real(z, (double)arg);
+    case OP_CBRT: return or_pow_real(z, 1.0 / 3.0);
+    case OP_SIN: return csin(z);
+    case OP_COS: return ccos(z);
+    case OP_TAN: return ctan(z);
+    case OP_SINH: return csinh(z);
+    case OP_COSH: return ccosh(z);
+    case OP_TANH: return ctanh(z);
+    case OP_ASIN: return casin(z);
+    case OP_ACOS: return cacos(z);
+    case OP_ATAN: return catan(z);
+    case OP_ASINH: return casinh(z);
+    case OP_ACOSH: return cacosh(z);
+    case OP_ATANH: return catanh(z);
+    case OP_ABS: return cabs(z);
+    case OP_CONJ: return conj(z);
+    case OP_REAL: return creal(z);
+    case OP_IMAG: return cimag(z);
+  }
+  return z;
+}
+
 static cplx eval_expr(const or_expr *ex, int64_t e, const double *x, const double *phi, int nb) {
   cplx st[16];
   int sp = 0;
@@ -120,21 +179,22 @@ static cplx eval_expr(const or_expr *ex, int64_t e, const double *x, const doubl
         st[sp++] = s;
         break;
       }
-      case OP_NEG: st[sp - 1] = -st[sp - 1]; break;
-      case OP_HEAVISIDE: {
-        double r = creal(st[sp - 1]);
-        st[sp - 1] = r > 0.0 ? 1.0 : (r < 0.0 ? 0.0 : 0.5);
-        break;
-      }
-      default: {
+      case OP_ADD:
+      case OP_SUB:
+      case OP_MUL:
+      case OP_DIV:
+      case OP_ATAN2: {
         cplx b = st[--sp];
         cplx a = st[sp - 1];
         if (in->op == OP_ADD) a = a + b;
         else if (in->op == OP_SUB) a = a - b;
         else if (in->op == OP_MUL) a = a * b;
-        else a = a / b;
+        else if (in->op == OP_DIV) a = a / b;
+        else a = atan2(creal(a), creal(b)); /* scalarBinaryOperators.h:21, real arguments */
         st[sp - 1] = a;
+        break;
       }
+      default: st[sp - 1] = or_unary(in->op, in->arg, st[sp - 1]);
     }
   }
   return st[0];

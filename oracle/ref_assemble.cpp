@@ -18,14 +18,23 @@
 //
 // usage: ref_assemble <out-file> <threads> <repeats> <kind> <dim> <m> <mesh_order> <space> <order> <gauss>
 //                     <jitter> <seed> <k> <coef_mode> <dirichlet> <dirichlet_value> <source> <omega>
-//                     <lame_sigma> <upper>
-// (the fields of fg_problem_config in include/fem_g_gb300_host.h, in order)
+//                     <lame_sigma> <upper> [<coefficient programs>]
+// (the fields of fg_problem_config in include/fem_g_gb300_host.h, in order).
+// The optional last argument names a file of coefficient programs for the
+// scalar (Helmholtz-type) problem, each "<term> <count>" followed by count
+// lines "<op> <arg> <re> <im>" in the bytecode of include/fem_g_gb300.h:
+// term "grad" (integral(g grad(dof u), grad(tf u))), "mass"
+// (integral(m dof(u), tf(u))) or "source" (integral(f, tf(u))). The programs
+// become the reference's own expression trees (x(), y(), z(), constants,
+// + - * /, heaviside and the scalar operators of scalarUnaryOperators.h).
 #include <algorithm>
 #include <chrono>
 #include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -83,6 +92,80 @@ class ElementArray final : public function::NullaryOperation<T, Degree::Degree0>
 function::ScalarFunction<T> elementArray(std::vector<T> values) {
   auto data = std::make_shared<const std::vector<T>>(std::move(values));
   return function::ScalarFunction<T>(new function::NullaryNode<ElementArray>(ElementArray(data)));
+}
+
+struct Instr {
+  int op, arg;
+  double re, im;
+};
+
+// A coefficient program as a reference expression tree (stack machine)
+function::ScalarFunction<T> fromProgram(const std::vector<Instr> &code) {
+  using F = function::ScalarFunction<T>;
+  std::vector<F> st;
+  for (const Instr &in : code) {
+    if (in.op == FG_OP_CONST) {
+      st.push_back(F(T(in.re, in.im)));
+      continue;
+    }
+    if (in.op == FG_OP_X || in.op == FG_OP_Y || in.op == FG_OP_Z) {
+      st.push_back(in.op == FG_OP_X ? function::x<T>() : in.op == FG_OP_Y ? function::y<T>() : function::z<T>());
+      continue;
+    }
+    if (in.op >= FG_OP_ADD && in.op <= FG_OP_DIV) {
+      F b = st.back();
+      st.pop_back();
+      F a = st.back();
+      st.pop_back();
+      st.push_back(in.op == FG_OP_ADD ? F(a + b) : in.op == FG_OP_SUB ? F(a - b) : in.op == FG_OP_MUL ? F(a * b) : F(a / b));
+      continue;
+    }
+    F a = st.back();
+    st.pop_back();
+    switch (in.op) {
+      case FG_OP_NEG: st.push_back(-a); break;
+      case FG_OP_HEAVISIDE: st.push_back(function::heaviside(a)); break;
+      case FG_OP_SQRT: st.push_back(function::sqrt(a)); break;
+      case FG_OP_EXP: st.push_back(function::exp(a)); break;
+      case FG_OP_LN: st.push_back(function::ln(a)); break;
+      case FG_OP_LOG10: st.push_back(function::log(a)); break;
+      case FG_OP_POW: st.push_back(function::pow(a, (unsigned)in.arg)); break;
+      case FG_OP_CBRT: st.push_back(function::cbrt(a)); break;
+      case FG_OP_SIN: st.push_back(function::sin(a)); break;
+      case FG_OP_COS: st.push_back(function::cos(a)); break;
+      case FG_OP_TAN: st.push_back(function::tan(a)); break;
+      case FG_OP_SINH: st.push_back(function::sinh(a)); break;
+      case FG_OP_COSH: st.push_back(function::cosh(a)); break;
+      case FG_OP_TANH: st.push_back(function::tanh(a)); break;
+      case FG_OP_ASIN: st.push_back(function::asin(a)); break;
+      case FG_OP_ACOS: st.push_back(function::acos(a)); break;
+      case FG_OP_ATAN: st.push_back(function::atan(a)); break;
+      case FG_OP_ASINH: st.push_back(function::asinh(a)); break;
+      case FG_OP_ACOSH: st.push_back(function::acosh(a)); break;
+      case FG_OP_ATANH: st.push_back(function::atanh(a)); break;
+      case FG_OP_ABS: st.push_back(function::abs(a)); break;
+      case FG_OP_CONJ: st.push_back(function::conj(a)); break;
+      case FG_OP_REAL: st.push_back(function::real(a)); break;
+      case FG_OP_IMAG: st.push_back(function::imag(a)); break;
+      default: throw std::runtime_error("coefficient program: operator " + std::to_string(in.op) + " not available");
+    }
+  }
+  if (st.size() != 1) throw std::runtime_error("coefficient program: malformed");
+  return st.back();
+}
+
+std::map<std::string, std::vector<Instr>> readPrograms(const char *path) {
+  std::map<std::string, std::vector<Instr>> out;
+  std::ifstream in(path);
+  if (!in) throw std::runtime_error(std::string("cannot read ") + path);
+  std::string term;
+  int count = 0;
+  while (in >> term >> count) {
+    std::vector<Instr> code((size_t)count);
+    for (auto &c : code) in >> c.op >> c.arg >> c.re >> c.im;
+    out[term] = code;
+  }
+  return out;
 }
 
 double median(std::vector<double> v) {
@@ -155,7 +238,7 @@ void run(FORM &formulation, F &u, int repeats, Writer &w) {
 }  // namespace
 
 int main(int argc, char **argv) {
-  if (argc != 21) {
+  if (argc != 21 && argc != 22) {
     std::fprintf(stderr, "usage: ref_assemble <out> <threads> <repeats> <fg_problem_config fields...>\n");
     return 2;
   }
@@ -213,7 +296,23 @@ int main(int argc, char **argv) {
     // option, the reference's -forceSymmetric switch
     common::Options::instance()->forceSymmetric = c.upper != 0;
     const std::string matrixOptions = c.upper ? "Symmetric" : "";
-    if (c.kind == FG_PROBLEM_HELMHOLTZ) {
+    if (c.kind == FG_PROBLEM_HELMHOLTZ && argc == 22) {
+      // the terms from the coefficient programs
+      auto progs = readPrograms(argv[21]);
+      const bool lagrange = c.space == FG_SPACE_LAGRANGE;
+      field::Field<T, field::Form::Form0> u("u", omega,
+                                            lagrange ? field::FunctionSpaceTypeForm0::Lagrange
+                                                     : field::FunctionSpaceTypeForm0::HierarchicalH1,
+                                            lagrange ? c.mesh_order : c.order);
+      problem::Formulation<T> formulation("coefficients", matrixOptions);
+      if (progs.count("grad"))
+        formulation.integral(fromProgram(progs["grad"]) * equation::grad(equation::dof(u)), equation::grad(equation::tf(u)),
+                             omega, gauss);
+      if (progs.count("mass"))
+        formulation.integral(fromProgram(progs["mass"]) * equation::dof(u), equation::tf(u), omega, gauss);
+      if (progs.count("source")) formulation.integral(fromProgram(progs["source"]), equation::tf(u), omega, gauss);
+      run(formulation, u, repeats, w);
+    } else if (c.kind == FG_PROBLEM_HELMHOLTZ) {
       const bool lagrange = c.space == FG_SPACE_LAGRANGE;
       field::Field<T, field::Form::Form0> u("u", omega,
                                             lagrange ? field::FunctionSpaceTypeForm0::Lagrange

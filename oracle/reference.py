@@ -34,18 +34,33 @@ def _args(cfg):
     return out
 
 
-def run(cfg, threads=0, repeats=1, timeout=3600):
+def write_programs(path, programs):
+    """programs: {"grad" | "mass" | "source": [(op, arg, re, im), ...]}"""
+    with open(path, "w") as f:
+        for term, code in programs.items():
+            f.write("%s %d\n" % (term, len(code)))
+            for op, arg, re, im in code:
+                f.write("%d %d %r %r\n" % (op, arg, float(re), float(im)))
+
+
+def run(cfg, threads=0, repeats=1, timeout=3600, programs=None):
     """Reference pre() + assemble() of the problem `cfg` (an
     fg_problem_config, from femg.config*). threads = 0: all host threads.
     repeats > 1: assemble() that many times (setSystemToZero in between) and
-    report the median wall time of the repeats after the first."""
+    report the median wall time of the repeats after the first. programs:
+    coefficient programs that replace the terms of a scalar problem
+    (write_programs)."""
     if not available():
         raise RuntimeError("the reference program is not built (oracle/build.py, needs the reference tree)")
     threads = threads or os.cpu_count() or 1
     with tempfile.TemporaryDirectory() as tmp:
         path = os.path.join(tmp, "out.bin")
+        extra = []
+        if programs:
+            extra = [os.path.join(tmp, "programs.txt")]
+            write_programs(extra[0], programs)
         env = dict(os.environ, OMP_NUM_THREADS=str(threads))
-        r = subprocess.run([EXE, path, str(threads), str(repeats)] + _args(cfg), capture_output=True, text=True,
+        r = subprocess.run([EXE, path, str(threads), str(repeats)] + _args(cfg) + extra, capture_output=True, text=True,
                            timeout=timeout, env=env)
         if r.returncode != 0:
             raise RuntimeError("ref_assemble failed (%d): %s%s" % (r.returncode, r.stdout[-2000:], r.stderr[-2000:]))

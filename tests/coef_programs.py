@@ -1,0 +1,66 @@
+"""Coefficient programs of the operator tests (shared by the CPU tests
+against the reference and the GPU tests against the oracle): every scalar
+operator of the coefficient language applied to a complex, point-dependent
+argument that stays away from the branch cuts,
+    a(x, y) = 0.4 + 0.3 x + 0.2 y + 0.1 i (x - y),
+as the mass coefficient m = op(a) and the source f = op(a) / 2 of
+    integral(grad(dof u), grad(tf u)) + integral(m dof(u), tf(u)) + integral(f, tf(u))."""
+import ctypes as C
+
+
+def argument(F):
+    return [(F.FG_OP_CONST, 0, 0.4, 0.0), (F.FG_OP_X, 0, 0, 0), (F.FG_OP_CONST, 0, 0.3, 0.0), (F.FG_OP_MUL, 0, 0, 0),
+            (F.FG_OP_ADD, 0, 0, 0), (F.FG_OP_Y, 0, 0, 0), (F.FG_OP_CONST, 0, 0.2, 0.0), (F.FG_OP_MUL, 0, 0, 0),
+            (F.FG_OP_ADD, 0, 0, 0), (F.FG_OP_X, 0, 0, 0), (F.FG_OP_Y, 0, 0, 0), (F.FG_OP_SUB, 0, 0, 0),
+            (F.FG_OP_CONST, 0, 0.0, 0.1), (F.FG_OP_MUL, 0, 0, 0), (F.FG_OP_ADD, 0, 0, 0)]
+
+
+OPS = ["SQRT", "EXP", "LN", "LOG10", "POW2", "POW5", "CBRT", "SIN", "COS", "TAN", "SINH", "COSH", "TANH", "ASIN", "ACOS",
+       "ATAN", "ASINH", "ACOSH", "ATANH", "ABS", "CONJ", "REAL", "IMAG", "ATAN2", "HEAVISIDE"]
+
+
+def program(F, name):
+    a = argument(F)
+    if name.startswith("POW"):
+        return a + [(F.FG_OP_POW, int(name[3:]), 0, 0)]
+    if name == "ACOSH":  # argument moved right of the cut (-inf, 1]
+        return a + [(F.FG_OP_CONST, 0, 1.0, 0.0), (F.FG_OP_ADD, 0, 0, 0), (F.FG_OP_ACOSH, 0, 0, 0)]
+    if name == "ATAN2":  # real arguments: atan2(Re a, 0.7 + y)
+        return a + [(F.FG_OP_CONST, 0, 0.7, 0.0), (F.FG_OP_Y, 0, 0, 0), (F.FG_OP_ADD, 0, 0, 0), (F.FG_OP_ATAN2, 0, 0, 0)]
+    if name == "HEAVISIDE":  # of Re(a) - 0.6: both sides of the step inside the domain
+        return a + [(F.FG_OP_CONST, 0, 0.6, 0.0), (F.FG_OP_SUB, 0, 0, 0), (F.FG_OP_HEAVISIDE, 0, 0, 0)]
+    return a + [(getattr(F, "FG_OP_" + name), 0, 0, 0)]
+
+
+def halved(F, code):
+    return code + [(F.FG_OP_CONST, 0, 0.5, 0.0), (F.FG_OP_MUL, 0, 0, 0)]
+
+
+def set_expr(expr, code):
+    expr.n_code = len(code)
+    expr.n_arrays = 0
+    for i, (op, arg, re, im) in enumerate(code):
+        expr.code[i].op, expr.code[i].arg, expr.code[i].re, expr.code[i].im = op, arg, re, im
+
+
+def terms(F, name):
+    """(TermDesc array, count, programs for the reference program)"""
+    m = program(F, name)
+    f = halved(F, m)
+    arr = (F.TermDesc * 3)()
+    for t in arr:
+        C.memset(C.byref(t), 0, C.sizeof(F.TermDesc))
+    arr[0].kind = F.FG_TERM_GRAD_GRAD
+    set_expr(arr[0].coef, [(F.FG_OP_CONST, 0, 1.0, 0.0)])
+    arr[1].kind = F.FG_TERM_MASS
+    set_expr(arr[1].coef, m)
+    arr[2].kind = F.FG_TERM_SOURCE
+    set_expr(arr[2].coef, f)
+    programs = {"grad": [(F.FG_OP_CONST, 0, 1.0, 0.0)], "mass": m, "source": f}
+    return arr, 3, programs
+
+
+def configs(F):
+    return {"tri_p2": F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=3),
+            "tet_h1_p2": F.config(dim=3, m=2, mesh_order=1, space=F.FG_SPACE_HIERARCHICAL_H1, order=2, gauss=4, jitter=0.15,
+                                  seed=3)}
