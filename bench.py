@@ -636,6 +636,20 @@ def bench_headline(args, femg, torch, ws, rank, local, dist):
     plan.set_fp64_method(femg.FG_FP64_FACTORED)
     ms_fp64_fact = timed("fp64", dv64, 5)[0]
     plan.set_fp64_method(femg.FG_FP64_QUADRATURE)
+    # the fused mixed kernel (contraction and reduction in one launch, opt-in)
+    fused = None
+    if head == "mixed":
+        finfo = plan.fused_info()
+        if finfo["applies"]:
+            plan.set_mixed_fused(True)
+            ms_fused, _, fprof = timed("mixed", dv64, 5, profile=True)
+            plan.set_mixed_fused(False)
+            fused = {"ms_per_step": ms_fused, "value": ws * E / (ms_fused / 1000.0), "blocks": finfo["blocks"],
+                     "elements_per_block": finfo["elems_per_block"],
+                     "contractions_per_element": finfo["contractions_per_element"],
+                     "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in (fprof or {}).items()}}
+        else:
+            fused = {"applies": False, "why": finfo["why"]}
     clk = clocks.stop()
     if head == "mixed":
         step("fp64", dv64)
@@ -735,6 +749,7 @@ def bench_headline(args, femg, torch, ws, rank, local, dist):
                 "fp64_factored": {"value": ws * E / (ms_fp64_fact / 1000.0), "ms_per_step": ms_fp64_fact,
                                   "method": "exact factorization of the affine element matrices, FP64 on the CUDA cores"},
                 "speedup_mixed_vs_fp64_factored": ms_fp64_fact / ms_head,
+                "mixed_fused": fused,
                 "mixed_vs_fp64_rel_fro": diff,
                 "speedup_mixed_vs_fp64": ms_fp64 / ms_head,
                 "pre_seconds": pre_s, "plan_seconds": plan_s,

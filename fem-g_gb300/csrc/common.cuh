@@ -182,7 +182,7 @@ struct fg_plan {
   int accumulate = 0;  // add into device outputs instead of overwriting them (fg_plan_set_accumulate)
   // fused mixed path (contraction and reduction in one kernel), see fused.cu
   void *fused = nullptr;
-  int mixedFused = 1;  // fg_plan_set_mixed_fused
+  int mixedFused = 0;  // fg_plan_set_mixed_fused (off by default)
   int *jmErrHost = nullptr;  // pinned copy of d.jmErr
 };
 

@@ -308,18 +308,18 @@ int fg_plan_set_fp64_method(fg_plan *plan, int32_t method);
 int fg_plan_set_accumulate(fg_plan *plan, int32_t accumulate);
 /* Mixed precision: FP64 geometry, 3xTF32 tcgen05 contraction with FP32
  * accumulation, FP64 CSR reduction. report may be NULL (no error report).
- * Where it applies (one-component H1 fields whose element orientations only
- * flip basis signs, affine elements, real element-constant coefficients, no
- * fixed or linked DOFs, no error report) the contraction and the reduction
- * run fused in one kernel over blocks of consecutive CSR rows, and no element
- * matrix is written to device memory; elsewhere, and with
- * fg_plan_set_mixed_fused(plan, 0), the contraction writes FP32 element
- * matrices that a separate reduction reads. */
+ * By default the contraction writes FP32 element matrices that a separate
+ * deterministic reduction reads. With fg_plan_set_mixed_fused(plan, 1), where
+ * it applies (one-component H1 fields whose element orientations only flip
+ * basis signs, affine elements, real element-constant coefficients, no fixed
+ * or linked DOFs, no error report), the contraction and the reduction run
+ * fused in one kernel over blocks of consecutive CSR rows, and no element
+ * matrix is written to device memory. */
 int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency,
                       const double *dirichlet, double *csr_values, double *rhs, void *stream,
                       fg_err_report *report);
 
-/* Fused mixed path on (1, the default) or off (0) for this plan. */
+/* Fused mixed path on (1) or off (0, the default) for this plan. */
 int fg_plan_set_mixed_fused(fg_plan *plan, int32_t on);
 /* Whether the fused mixed path applies to the plan (building its block
  * records on first use), its number of row blocks, the mean elements per

@@ -45,6 +45,7 @@ def test_fused_matches_oracle_split_and_itself(femg, oracle, cuda, name):
     info = plan.fused_info()
     assert info["applies"], info["why"]
     assert info["contractions_per_element"] >= 1.0
+    plan.set_mixed_fused(True)
     v1, b1 = plan.assemble("mixed")
     v2, b2 = plan.assemble("mixed")
     assert np.array_equal(v1, v2) and np.array_equal(b1, b2)  # deterministic
@@ -65,6 +66,7 @@ def test_fused_device_outputs_and_accumulate(femg, oracle, cuda):
     ref_v, _ = oracle.assemble(a, t, nt)
     plan = prob.plan()
     assert plan.fused_info()["applies"]
+    plan.set_mixed_fused(True)
     dv = torch.zeros(2 * prob.nnz, dtype=torch.float64, device="cuda")
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     plan.assemble("mixed", values=dv.data_ptr(), rhs=False, stream=stream)
@@ -89,6 +91,7 @@ def test_fused_declines_and_split_path_runs(femg, oracle, cuda, what):
     info = plan.fused_info()
     assert not info["applies"]
     assert info["why"]
+    plan.set_mixed_fused(True)
     a = prob.arrays()
     t, nt = prob.terms()
     ref_v, _ = oracle.assemble(a, t, nt)
@@ -103,6 +106,7 @@ def test_fused_full_size_c3(femg, oracle, cuda):
     plan = prob.plan()
     info = plan.fused_info()
     assert info["applies"], info["why"]
+    plan.set_mixed_fused(True)
     v, _ = plan.assemble("mixed")
     a = prob.arrays()
     t, nt = prob.terms()

@@ -114,8 +114,8 @@ def _quad(a, v, u, w):
 
 
 def test_full_size_c2_properties(femg, cuda):
-    """384,000 tets, order 3: symmetry and exact energies of 1 and x (the
-    oracle is too slow at this size for an entry-wise comparison)."""
+    """384,000 tets, order 3: symmetry and exact energies of 1 and x, beside
+    the entry-wise comparison with the oracle in test_gpu_full_size.py."""
     k = 20.0
     prob = femg.Problem(femg.config_c2())
     a = prob.arrays()
