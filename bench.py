@@ -261,6 +261,8 @@ def bench_batch(args, femg, torch):
             torch.cuda.synchronize()
             res["e2e_ms"] = 1000.0 * (time.perf_counter() - e0) / e2e_steps
             del hv, hptrs
+        b.close()
+        if prec == "mixed":
             # relative Frobenius error of every problem's CSR against the FP64 path
             tmp = torch.empty(2 * max(p.nnz for p in probs), dtype=torch.float64, device="cuda")
             d2 = r2 = 0.0
@@ -277,10 +279,10 @@ def bench_batch(args, femg, torch):
             res["rel_fro"] = (d2 / r2) ** 0.5
             res["worst_problem_rel_fro"] = worst
             del tmp
-        b.close()
     clk = clocks.stop()
-    for o in outs:
-        del o
+    outs.clear()
+    ptrs = None
+    torch.cuda.empty_cache()
     pk, pk_kind = peaks()
     alg = sum(fused_bytes(p.info()["E"], p.info()["n"], p.prob.nnz, int(p.prob.sys.n_rows), coef=0) for p in plans)
     roof = roofline(res["prof"], alg, pk, pk_kind)

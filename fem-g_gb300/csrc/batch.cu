@@ -275,6 +275,12 @@ int tune(fg_batch *b, cudaStream_t s) {
         GatherShape g = gatherShape(c.n, c.maxRowLen, c.kcplx, b->mixed, L, w);
         if (g.ok) cands.push_back(g);
       }
+    // the vector-load kernel for real FP32 element matrices with n = 4k
+    if (b->mixed && !c.kcplx && c.slotBytes == 1 && c.n % 4 == 0 && c.n <= 32)
+      for (int w : {4, 8}) {
+        GatherShape g = gatherShapeV4(c.n, c.maxRowLen, w);
+        if (g.ok) cands.push_back(g);
+      }
     if (cands.empty()) cands.push_back(base);
     float best = 1e30f;
     GatherShape bestShape = cands[0];
@@ -295,6 +301,7 @@ int tune(fg_batch *b, cudaStream_t s) {
     js += std::string(ci ? ", " : "") + "{\"dim\": " + std::to_string(c.dim) + ", \"n\": " + std::to_string(c.n) +
           ", \"nq\": " + std::to_string(c.nq) + ", \"problems\": " + std::to_string(c.probs.size()) +
           ", \"lanes\": " + std::to_string(c.shape.L) + ", \"columns\": " + std::to_string(c.shape.J) +
+          ", \"vector_loads\": " + std::string(c.shape.v4 ? "true" : "false") +
           ", \"warps\": " + std::to_string(c.shape.wpb) +
           ", \"ms\": " + std::to_string(best) + "}";
   }

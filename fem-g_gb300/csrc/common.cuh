@@ -260,9 +260,12 @@ struct GatherShape {
   int L = 0, J = 3, wpb = 0, rowsPerBlock = 0;  // lanes per row, columns per lane
   size_t smem = 0;
   bool ok = false;
+  bool v4 = false;  // k_gather_batch_v4: L = n / 4 lanes, 4 columns each by vector loads
 };
 // L, wpb <= 0: the defaults of the single-plan gather
 GatherShape gatherShape(int n, int maxRowLen, int kcplx, int keIsFloat, int L, int wpb);
+// the vector-load shape (real FP32 element matrices, n a multiple of 4 up to 32)
+GatherShape gatherShapeV4(int n, int maxRowLen, int wpb);
 int launchGatherBatch(const GatherJob *jobsDev, int nJobs, int64_t blocks, int slotBytes, int kcplx, int keIsFloat,
                       const GatherShape &g, cudaStream_t s);
 

@@ -158,6 +158,121 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
   }
 }
 
+// Real FP32 element matrices in full row-major layout with n a multiple of 4
+// and one-byte slots (the scalar tetrahedral orders 1 and 3): a sub-warp of
+// L = n / 4 lanes per row, lane lt owning columns 4 lt .. 4 lt + 3, so that
+// an element row comes in with one 16-byte load per lane and its slots with
+// one 4-byte load (against 2 n / L scalar loads per lane in k_gather). Same
+// visiting order, same per-entry order (entries separated by __syncwarp),
+// same results.
+// The rows of visit records [v0, v1) handled by block blk of nblk.
+template <bool ACC>
+__device__ __forceinline__ void gatherRowsV4(const PlanDev &p, const float *__restrict__ ke, const double2 *__restrict__ be,
+                                             const double2 *__restrict__ uD, double2 *__restrict__ values,
+                                             double2 *__restrict__ rhs, int L, int64_t blk, int64_t nblk, int64_t v0, int64_t v1) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const int R = 32 / L;  // rows per warp
+  const int sub = lane / L, lt = lane - sub * L;
+  const bool laneLive = sub < R;
+  float *A = reinterpret_cast<float *>(smraw) + (size_t)(warp * R + (laneLive ? sub : 0)) * p.maxRowLen;
+  const int n = p.n, nn2 = n * n;
+  const uint8_t *slot = (const uint8_t *)p.slot;
+  const int64_t stride = nblk * wpb * R;
+  for (int64_t base = v0 + (blk * wpb + warp) * R; base < v1; base += stride) {
+    const int64_t idx = base + sub;
+    const bool live = laneLive && idx < v1;
+    const uint4 v = live ? p.visit[idx] : make_uint4(0, 0, 0, 0);
+    const int len = live ? (int)(v.w & 0xFFFFu) : 0;
+    const int cnt = live ? (int)(v.w >> 16) : 0;
+    for (int s = lt; s < len; s += L) A[s] = 0.0f;
+    int maxCnt = cnt;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) maxCnt = max(maxCnt, __shfl_xor_sync(0xffffffffu, maxCnt, off));
+    __syncwarp();
+    double2 dc = make_double2(0.0, 0.0), bsum = make_double2(0.0, 0.0);
+    float4 kv, kvN;
+    uint32_t sv, svN, flat = 0, flatN = 0;
+    auto fetch = [&](int k, float4 &kv_, uint32_t &sv_, uint32_t &f_) {
+      if (k < cnt) {
+        const uint32_t packed = p.visitElem[v.z + k];
+        const uint32_t e = packed >> 6, i = packed & 63;
+        f_ = e * (uint32_t)n + i;
+        kv_ = *reinterpret_cast<const float4 *>(ke + (size_t)e * nn2 + (size_t)i * n + 4 * lt);
+        sv_ = *reinterpret_cast<const uint32_t *>(slot + (size_t)f_ * n + 4 * lt);
+      } else {
+        kv_ = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        sv_ = 0xFEFEFEFEu;  // ignore
+        f_ = 0;
+      }
+    };
+    if (maxCnt > 0) fetch(0, kv, sv, flat);
+    for (int k = 0; k < maxCnt; ++k) {
+      if (k + 1 < maxCnt) fetch(k + 1, kvN, svN, flatN);
+      const float vals[4] = {kv.x, kv.y, kv.z, kv.w};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const uint32_t s = (sv >> (8 * c)) & 0xFFu;
+        if (s < 0xFEu) {
+          atomicAdd(&A[s], vals[c]);  // distinct slots within an element row; rows ordered by __syncwarp
+        } else if (s == 0xFFu) {
+          // Dirichlet lifting with the transposed entry (addValuesDC, VectorFactory.cpp:184)
+          const uint32_t e = flat / (uint32_t)n, i = flat - e * (uint32_t)n;
+          const int j = 4 * lt + c;
+          const double kt = (double)ke[(size_t)e * nn2 + (size_t)j * n + i];
+          const double2 u = uD[p.edof[(size_t)e * n + j]];
+          dc.x += kt * u.x;
+          dc.y += kt * u.y;
+        }
+      }
+      if (be && lt == 0 && k < cnt) bsum = cadd(bsum, be[flat]);
+      __syncwarp();
+      kv = kvN;
+      sv = svN;
+      flat = flatN;
+    }
+    for (int s = lt; s < len; s += L) {
+      double2 val = make_double2(widen(A[s]), 0.0);
+      if (ACC) val = cadd(values[v.y + s], val);
+      values[v.y + s] = val;
+    }
+    if (rhs) {
+      double2 dtot = dc;
+      if (uD)  // the sub-warp's lifted terms, summed on its first lane
+        for (int t = 1; t < L; ++t) {
+          const int src = sub * L + t < 32 ? sub * L + t : lane;
+          dtot.x += __shfl_sync(0xffffffffu, dc.x, src);
+          dtot.y += __shfl_sync(0xffffffffu, dc.y, src);
+        }
+      if (live && lt == 0) {
+        const double2 tot = cadd(bsum, dtot);
+        rhs[v.x] = ACC ? cadd(rhs[v.x], tot) : tot;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+template <bool ACC>
+__global__ void __launch_bounds__(256)
+    k_gather_v4(const PlanDev p, const float *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
+                double2 *__restrict__ values, double2 *__restrict__ rhs, int L, int64_t v0, int64_t v1) {
+  gatherRowsV4<ACC>(p, ke, be, uD, values, rhs, L, blockIdx.x, gridDim.x, v0, v1);
+}
+
+// Many plans of one class in one launch (k_gather_batch with the vector loads)
+__global__ void __launch_bounds__(256) k_gather_batch_v4(const GatherJob *__restrict__ jobs, int nJobs, int L) {
+  int lo = 0, hi = nJobs - 1;
+  while (lo < hi) {  // last job whose blockStart <= blockIdx.x
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blockStart <= (int64_t)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const GatherJob &Jb = jobs[lo];
+  gatherRowsV4<false>(Jb.p, (const float *)Jb.ke, Jb.be, Jb.uD, Jb.values, Jb.rhs, L, (int64_t)blockIdx.x - Jb.blockStart,
+                      Jb.nBlocks, 0, (int64_t)Jb.p.nRows);
+}
+
 template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J, bool ACC>
 __global__ void __launch_bounds__(256)
     k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
@@ -177,6 +292,38 @@ __global__ void __launch_bounds__(256) k_gather_batch(const GatherJob *__restric
   const GatherJob &Jb = jobs[lo];
   gatherRows<SlotT, KCPLX, KT, AT, L, J, false>(Jb.p, (const KT *)Jb.ke, Jb.be, Jb.uD, Jb.values, Jb.rhs, rowsPerBlock, Jb.lay,
                                          (int64_t)blockIdx.x - Jb.blockStart, Jb.nBlocks, 0, (int64_t)Jb.p.nRows);
+}
+
+// k_gather_v4 where it applies: real FP32 element matrices in full layout,
+// n a multiple of 4 (at most 32 columns), one-byte slots, no linked DOFs
+static bool gatherV4Applies(const PlanDev &p, int keComplex, int keIsFloat, KeLayout lay) {
+  return keIsFloat && !keComplex && lay.kind == kKeFull && p.n % 4 == 0 && p.n <= 32 && p.slotBytes == 1 && !p.lscale;
+}
+
+static int launchV4(const PlanDev &p, const float *ke, const double2 *be, const double2 *uD, double2 *values, double2 *rhs,
+                    int64_t v0, int64_t v1, bool acc, cudaStream_t s) {
+  const int L = p.n / 4, R = 32 / L;
+  int wpb = 8;
+  const size_t rowBytes = (size_t)std::max(p.maxRowLen, 1) * 4;
+  while (wpb > 1 && rowBytes * R * wpb > 200 * 1024) wpb >>= 1;
+  const size_t smem = rowBytes * R * wpb;
+  if (smem > 200 * 1024) {
+    setLastError("gather: CSR row too long for shared memory");
+    return FG_ERR_UNSUPPORTED;
+  }
+  int64_t blocks = (v1 - v0 + (int64_t)wpb * R - 1) / ((int64_t)wpb * R);
+  blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)smCount() * 16));
+  if (acc) {
+    static SmemAllowance allowed;
+    FG_CUDA(allowSmem(k_gather_v4<true>, smem, allowed));
+    k_gather_v4<true><<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, ke, be, uD, values, rhs, L, v0, v1);
+  } else {
+    static SmemAllowance allowed;
+    FG_CUDA(allowSmem(k_gather_v4<false>, smem, allowed));
+    k_gather_v4<false><<<(unsigned)blocks, 32 * wpb, smem, s>>>(p, ke, be, uD, values, rhs, L, v0, v1);
+  }
+  FG_CUDA(cudaGetLastError());
+  return FG_OK;
 }
 
 template <typename SlotT, bool KCPLX, typename KT>
@@ -240,6 +387,11 @@ static int launchGatherRange(const PlanDev &p, const double *ke, int keComplex, 
   const double2 *uD = (const double2 *)dirichletDev;
   double2 *v2 = (double2 *)values;
   double2 *r2 = (double2 *)rhs;
+  if (gatherV4Applies(p, keComplex, keIsFloat, lay)) {
+    ProfScope prof("k_gather_v4", s);
+    countLaunch();
+    return launchV4(p, (const float *)ke, be2, uD, v2, r2, v0, v1, acc, s);
+  }
   ProfScope prof("k_gather", s);
   countLaunch();
   if (p.slotBytes == 1) {
@@ -293,6 +445,24 @@ int gatherToOutputs(fg_plan *plan, const double *ke, int keComplex, int keIsFloa
 // (16, 3) or (32, 3). By default the narrowest that covers n (8 x 5 for
 // 25..40 columns measured 7% faster than 16 x 3 on order-4 tets); for a given
 // L, J = 3 when 3L covers n, else 5 (L = 8 only).
+GatherShape gatherShapeV4(int n, int maxRowLen, int wpb) {
+  GatherShape g;
+  g.v4 = true;
+  g.L = n / 4;
+  g.J = 4;
+  const int R = 32 / g.L;
+  const size_t rowBytes = (size_t)std::max(maxRowLen, 1) * 4;
+  if (wpb <= 0) {
+    wpb = 8;
+    while (wpb > 1 && rowBytes * R * wpb > 200 * 1024) wpb >>= 1;
+  }
+  g.wpb = wpb;
+  g.rowsPerBlock = wpb * R;
+  g.smem = rowBytes * R * wpb;
+  g.ok = n % 4 == 0 && n <= 32 && g.smem <= 200 * 1024;
+  return g;
+}
+
 GatherShape gatherShape(int n, int maxRowLen, int kcplx, int keIsFloat, int L, int wpb) {
   GatherShape g;
   if (L <= 0) {
@@ -346,6 +516,18 @@ int launchGatherBatch(const GatherJob *jobsDev, int nJobs, int64_t blocks, int s
                       const GatherShape &g, cudaStream_t s) {
   if (blocks <= 0) return FG_OK;
   countLaunch();
+  if (g.v4) {
+    if (slotBytes != 1 || kcplx || !keIsFloat) {
+      setLastError("batched gather: vector shape for real FP32 element matrices with one-byte slots only");
+      return FG_ERR_ARG;
+    }
+    static SmemAllowance allowed;
+    FG_CUDA(allowSmem(k_gather_batch_v4, g.smem, allowed));
+    ProfScope prof("k_gather_batch_v4", s);
+    k_gather_batch_v4<<<(unsigned)blocks, 32 * g.wpb, g.smem, s>>>(jobsDev, nJobs, g.L);
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+  }
   if (slotBytes == 1) {
     if (keIsFloat)
       return kcplx ? launchBatchTyped<uint8_t, true, float>(jobsDev, nJobs, blocks, g, s) : launchBatchTyped<uint8_t, false, float>(jobsDev, nJobs, blocks, g, s);
