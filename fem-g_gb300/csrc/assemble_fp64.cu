@@ -166,6 +166,140 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
   }
 }
 
+// Scalar H1 field with terms whose element matrix is not symmetric: a general
+// TensorFunction D in integral(c D grad(dof u), grad(tf u)) and the advection
+// integral(c b . grad(dof u), tf(u)) with a VectorFunction b, beside the
+// symmetric terms. One warp per element; at each point lane 0 forms
+//   M = w det (c_gg I + A_sym + c_full D)   (the unknown's gradient map),
+//   v = w det c_adv b,  m = w det c_mass,
+// the lanes map the unknown's gradients (U_j = M G_j, a_j = v . G_j + m phi_j)
+// and each lane owns entries (i, j) of the full n x n matrix:
+//   Ke[i][j] += G_i . U_j + phi_i a_j
+// (BilinearTerm::evaluate's Hermitian product with real test functions,
+// src/term/BilinearTerm.cpp:314-326: the test side is conj(field), the
+// unknown side carries the coefficient).
+struct FullWarpSmem {
+  double X[kMaxNodes * 3];
+  double J0[9], J[9], Jinv[9];
+  double det0, det;
+  double2 M[9], v[3], m, s;
+  double G[3][kMaxDofs];
+  double phi[kMaxDofs];
+  double U[2][3][kMaxDofs];
+  double a[2][kMaxDofs];
+};
+
+template <int MAXENT, bool CPLX>
+__global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
+    k_element_full_fp64(const PlanDev p, const DevTerms *__restrict__ terms, double *__restrict__ ke, double2 *__restrict__ be) {
+  __shared__ FullWarpSmem smem[kWarpsPerBlockElem];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int n = p.nb;
+  const int nEnt = n * n;
+  FullWarpSmem &S = smem[warp];
+  const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlockElem;
+  for (int64_t e = (int64_t)blockIdx.x * kWarpsPerBlockElem + warp; e < p.E; e += stride) {
+    const int o = p.orient ? p.orient[e] : 0;
+    for (int t = lane; t < p.nn * 3; t += 32) S.X[t] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + t / 3] + t % 3];
+    __syncwarp();
+    double accR[MAXENT], accI[MAXENT];
+#pragma unroll
+    for (int k = 0; k < MAXENT; ++k) {
+      accR[k] = 0.0;
+      accI[k] = 0.0;
+    }
+    double2 bacc[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+    const int nG = terms->nMod > 1 ? terms->nMod : 1;
+    for (int gq = 0; gq < nG * p.nq; ++gq) {
+      const int g = gq / p.nq, q = gq - g * p.nq;
+      if (lane == 0) {
+        double xq[3];
+        pointGeometry(p, terms, g, q, S.X, S.J0, S.det0, S.J, S.det, S.Jinv, xq);
+        const double *phq = p.bval + ((size_t)o * p.nq + q) * p.nb;
+        double2 cgg = make_double2(0.0, 0.0), cm = make_double2(0.0, 0.0), f = make_double2(0.0, 0.0);
+        for (int t = 0; t < terms->n; ++t) {
+          const DevTerm &T = terms->t[t];
+          if (T.mod != g) continue;
+          if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb)));
+          else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb)));
+          else if (T.kind == FG_TERM_SOURCE) f = cadd(f, evalExpr(T.coef, e, xq, phq, p.nb));
+        }
+        const double wd = p.w[q] * S.det;
+        double2 A6[6];
+        diffusionTensor(terms, g, e, xq, cgg, A6, phq, p.nb);  // c_gg I (+ the symmetric tensor term)
+        const int sym[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+        double2 M[9];
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c) M[3 * r + c] = A6[sym[r][c]];
+        if (terms->tensorFullTerm >= 0 && terms->t[terms->tensorFullTerm].mod == g) {
+          const DevTerm &T = terms->t[terms->tensorFullTerm];
+          const double2 fc = cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb));
+          for (int k = 0; k < 9; ++k) M[k] = cadd(M[k], cmul(fc, evalExpr(terms->tensorFull[k], e, xq, phq, p.nb)));
+        }
+        double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+        if (terms->advectTerm >= 0 && terms->t[terms->advectTerm].mod == g) {
+          const DevTerm &T = terms->t[terms->advectTerm];
+          const double2 fc = cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb));
+          for (int k = 0; k < 3; ++k) v[k] = cmul(fc, evalExpr(terms->advect[k], e, xq, phq, p.nb));
+        }
+        for (int k = 0; k < 9; ++k) S.M[k] = make_double2(wd * M[k].x, wd * M[k].y);
+        for (int k = 0; k < 3; ++k) S.v[k] = make_double2(wd * v[k].x, wd * v[k].y);
+        S.m = make_double2(wd * cm.x, wd * cm.y);
+        S.s = make_double2(wd * f.x, wd * f.y);
+      }
+      __syncwarp();
+      const size_t base = ((size_t)o * p.nq + q) * p.nb;
+      for (int i = lane; i < n; i += 32) {
+        const double g0 = p.bgrad[3 * (base + i)], g1 = p.bgrad[3 * (base + i) + 1], g2 = p.bgrad[3 * (base + i) + 2];
+        const double ph = p.bval[base + i];
+        double G[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          G[r] = S.Jinv[r] * g0 + S.Jinv[3 + r] * g1 + S.Jinv[6 + r] * g2;
+          S.G[r][i] = G[r];
+        }
+        S.phi[i] = ph;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          S.U[0][r][i] = S.M[3 * r].x * G[0] + S.M[3 * r + 1].x * G[1] + S.M[3 * r + 2].x * G[2];
+          if (CPLX) S.U[1][r][i] = S.M[3 * r].y * G[0] + S.M[3 * r + 1].y * G[1] + S.M[3 * r + 2].y * G[2];
+        }
+        S.a[0][i] = S.v[0].x * G[0] + S.v[1].x * G[1] + S.v[2].x * G[2] + S.m.x * ph;
+        if (CPLX) S.a[1][i] = S.v[0].y * G[0] + S.v[1].y * G[1] + S.v[2].y * G[2] + S.m.y * ph;
+        const int slot = i >> 5;
+        bacc[slot].x += S.s.x * ph;
+        bacc[slot].y += S.s.y * ph;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int m = 0; m < MAXENT; ++m) {
+        const int k = lane + 32 * m;
+        if (k < nEnt) {
+          const int i = k / n, j = k - i * n;
+          accR[m] += S.G[0][i] * S.U[0][0][j] + S.G[1][i] * S.U[0][1][j] + S.G[2][i] * S.U[0][2][j] + S.phi[i] * S.a[0][j];
+          if (CPLX)
+            accI[m] += S.G[0][i] * S.U[1][0][j] + S.G[1][i] * S.U[1][1][j] + S.G[2][i] * S.U[1][2][j] + S.phi[i] * S.a[1][j];
+        }
+      }
+      __syncwarp();
+    }
+    const int ncomp = CPLX ? 2 : 1;
+    double *K = ke + (size_t)e * ncomp * nEnt;
+#pragma unroll
+    for (int m = 0; m < MAXENT; ++m) {
+      const int k = lane + 32 * m;
+      if (k < nEnt) {
+        K[k] = accR[m];
+        if (CPLX) K[nEnt + k] = accI[m];
+      }
+    }
+    if (be)
+      for (int i = lane; i < n; i += 32) be[(size_t)e * n + i] = bacc[i >> 5];
+    __syncwarp();
+  }
+}
+
 // Compound (3-component) field with the isotropic Tensor4 term
 // integral(C * grad(dof(u)), grad(tf(u))) and the mass term: the Tensor4
 // evaluator of the reference (src/term/evaluator/EquationEvaluator.h:1267-1276,
@@ -435,6 +569,31 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
 
 static int launchElementKernels(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s) {
   const PlanDev &p = plan->d;
+  if (terms.nonSym) {
+    const int perLane = (p.nb * p.nb + 31) / 32;
+    int64_t blocks = std::min<int64_t>((p.E + kWarpsPerBlockElem - 1) / kWarpsPerBlockElem, (int64_t)smCount() * 64);
+    if (blocks < 1) blocks = 1;
+    const bool cplx = terms.complexKe != 0;
+    double2 *be2 = (double2 *)be;
+    ProfScope prof("k_element_full_fp64", s);
+#define FG_LAUNCH_FULL(M)                                                                                             \
+  do {                                                                                                                \
+    if (cplx) k_element_full_fp64<M, true><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, dterms, ke, be2);  \
+    else k_element_full_fp64<M, false><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, dterms, ke, be2);     \
+  } while (0)
+    if (perLane <= 2) FG_LAUNCH_FULL(2);
+    else if (perLane <= 8) FG_LAUNCH_FULL(8);
+    else if (perLane <= 13) FG_LAUNCH_FULL(13);
+    else if (perLane <= 39) FG_LAUNCH_FULL(39);
+    else {
+      setLastError("FP64 full element kernel: more than 35 basis functions per element");
+      return FG_ERR_UNSUPPORTED;
+    }
+#undef FG_LAUNCH_FULL
+    countLaunch();
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+  }
   if (p.E > 0 && factoredFp64Applies(plan, terms)) {
     int st = launchFactoredFp64(plan, terms, dterms, ke, s);
     if (st) return st;

@@ -170,7 +170,7 @@ static int prepareFactored(fg_plan *plan) {
 bool factoredFp64Applies(const fg_plan *plan, const DevTerms &terms) {
   const PlanDev &p = plan->d;
   if (plan->fp64Method != FG_FP64_FACTORED) return false;
-  if (!p.affine || p.mult != 1 || terms.hasElastic || terms.hasJacMod || terms.tensorTerm >= 0 ||
+  if (!p.affine || p.mult != 1 || terms.hasElastic || terms.hasJacMod || terms.nonSym || terms.tensorTerm >= 0 ||
       terms.tensorMassTerm >= 0)
     return false;
   for (int t = 0; t < terms.n; ++t)

@@ -423,8 +423,8 @@ extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const 
     if (b->source[q] && (st = ensureDevice((void **)&pl->be, &pl->beBytes, (size_t)pl->d.E * pl->d.n * 16))) return fail(st);
     if (b->mixed) {
       for (int t = 0; t < dt.n; ++t)
-        if ((dt.t[t].kind != FG_TERM_SOURCE && dt.t[t].coef.cls == kExprPoint) || dt.tensorPoint) {
-          setLastError("mixed path: bilinear coefficients must be constant per element");
+        if ((dt.t[t].kind != FG_TERM_SOURCE && dt.t[t].coef.cls == kExprPoint) || dt.tensorPoint || dt.nonSym) {
+          setLastError("mixed path: bilinear coefficients must be constant per element, in symmetric terms");
           return fail(FG_ERR_UNSUPPORTED);
         }
       if ((st = prepareMixed(pl, dt.complexKe ? 2 : 1, 1))) return fail(st);

@@ -563,7 +563,7 @@ static int prepareFused(fg_plan *plan) {
 
 // whether a mixed call of these terms runs fused
 bool fusedApplies(fg_plan *plan, const DevTerms &dt) {
-  if (!plan->mixedFused || dt.complexKe || dt.hasElastic || dt.hasJacMod || plan->d.nFixed > 0) return false;
+  if (!plan->mixedFused || dt.complexKe || dt.hasElastic || dt.hasJacMod || dt.nonSym || plan->d.nFixed > 0) return false;
   if (dt.tensorMassTerm >= 0) return false;
   if (prepareFused(plan) != FG_OK) {
     cudaGetLastError();

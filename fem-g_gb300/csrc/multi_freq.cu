@@ -395,7 +395,7 @@ int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t
       if (m->terms[g].complexKe) ncomp = 2;
       for (int t = 0; t < m->terms[g].n; ++t)
         if ((m->terms[g].t[t].kind != FG_TERM_SOURCE && m->terms[g].t[t].coef.cls == kExprPoint) || m->terms[g].hasJacMod ||
-            m->terms[g].tensorPoint) {
+            m->terms[g].tensorPoint || m->terms[g].nonSym) {
           setLastError("mixed path: bilinear coefficients must be constant per element, without Jacobian modificators");
           return FG_ERR_UNSUPPORTED;
         }

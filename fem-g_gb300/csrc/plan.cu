@@ -674,14 +674,21 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
   out->nMod = 0;
   out->tensorTerm = -1;
   out->tensorMassTerm = -1;
+  out->tensorFullTerm = -1;
+  out->advectTerm = -1;
   for (int t = 0; t < nTerms; ++t) {
     const fg_term_desc &src = terms[t];
     DevTerm &dt = out->t[t];
     dt.kind = src.kind;
     dt.dt = src.dt;
-    if (src.kind < FG_TERM_GRAD_GRAD || src.kind > FG_TERM_MASS_TENSOR) {
+    if (src.kind < FG_TERM_GRAD_GRAD || src.kind > FG_TERM_ADVECTION) {
       setLastError("unknown term kind");
       return FG_ERR_ARG;
+    }
+    if ((src.kind == FG_TERM_GRAD_GRAD_TENSOR_FULL || src.kind == FG_TERM_ADVECTION) &&
+        (plan->d.mult != 1 || plan->d.form != FG_FORM_0)) {
+      setLastError("the full-tensor and advection terms need a scalar H1 field");
+      return FG_ERR_UNSUPPORTED;
     }
     if (src.kind == FG_TERM_ELASTIC && plan->d.mult != 3) {
       setLastError("the elastic (Tensor4) term needs a 3-component compound field");
@@ -736,6 +743,22 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
         if (st) return st;
         if (D[k].cls == kExprPoint) out->tensorPoint = 1;
       }
+    }
+    if (src.kind == FG_TERM_GRAD_GRAD_TENSOR_FULL || src.kind == FG_TERM_ADVECTION) {
+      const bool full = src.kind == FG_TERM_GRAD_GRAD_TENSOR_FULL;
+      int32_t &slot = full ? out->tensorFullTerm : out->advectTerm;
+      if (slot >= 0 || !src.tensor) {
+        setLastError(src.tensor ? "at most one full-tensor and one advection term per assembly"
+                                : "full-tensor or advection term without its tensor / vector");
+        return FG_ERR_ARG;
+      }
+      slot = t;
+      DevExpr *D = full ? out->tensorFull : out->advect;
+      for (int k = 0; k < (full ? 9 : 3); ++k) {
+        st = devExpr(plan, src.tensor[k], &D[k], &cplx, arrays, used);
+        if (st) return st;
+      }
+      out->nonSym = 1;
     }
     // the term's Jacobian modificator: terms with equal ones share a group
     const fg_jacmod &jm = src.jacmod;

@@ -194,7 +194,12 @@ enum {
   FG_TERM_GRAD_GRAD_TENSOR = 4, /* integral(c * D * grad(dof(u)), grad(tf(u))), D a symmetric 3x3 tensor of
                                    coefficient programs (TensorFunction * grad, EquationEvaluator tensor-left);
                                    scalar H1 fields; on HCurl fields the curls: integral(c * D * curl, curl) */
-  FG_TERM_MASS_TENSOR = 5        /* integral(c * D * dof(u), tf(u)) for HCurl fields (D symmetric, as above) */
+  FG_TERM_MASS_TENSOR = 5,       /* integral(c * D * dof(u), tf(u)) for HCurl fields (D symmetric, as above) */
+  FG_TERM_GRAD_GRAD_TENSOR_FULL = 6, /* integral(c * D * grad(dof(u)), grad(tf(u))) with a general (not symmetric)
+                                        3x3 TensorFunction D: tensor[9], row-major D_00 D_01 ... D_22; scalar H1 fields;
+                                        the element matrix is not symmetric (FP64 paths only) */
+  FG_TERM_ADVECTION = 7              /* integral(c * b * grad(dof(u)), tf(u)) with a VectorFunction b: tensor[3],
+                                        b_x b_y b_z; scalar H1 fields; not symmetric (FP64 paths only) */
 };
 enum { FG_DT_NONE = 0, FG_DT_1 = 1, FG_DT_2 = 2 }; /* dof, dt_dof, dt2_dof */
 
@@ -230,7 +235,8 @@ typedef struct {
   fg_expr coef; /* c, f, or lambda for FG_TERM_ELASTIC */
   fg_expr coef2; /* mu for FG_TERM_ELASTIC */
   fg_jacmod jacmod; /* all zero: none */
-  const fg_expr *tensor; /* FG_TERM_GRAD_GRAD_TENSOR, FG_TERM_MASS_TENSOR: [6] programs of D_xx, D_yy, D_zz, D_xy, D_xz, D_yz */
+  const fg_expr *tensor; /* FG_TERM_GRAD_GRAD_TENSOR, FG_TERM_MASS_TENSOR: [6] programs of D_xx, D_yy, D_zz, D_xy, D_xz, D_yz;
+                            FG_TERM_GRAD_GRAD_TENSOR_FULL: [9] of D row-major; FG_TERM_ADVECTION: [3] of b */
 } fg_term_desc;
 
 /* ------------------------------------------------------------- plan / run */

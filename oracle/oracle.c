@@ -30,7 +30,16 @@ typedef double complex cplx;
 /* ---------------------------------------------------------------- types */
 
 enum { AT_UNDEFINED = 0, AT_FIXED = 1, AT_UNKNOWN = 2, AT_UNKNOWN_BUBBLE = 3, AT_UNKNOWN_GLOBAL = 4 };
-enum { TERM_GRAD_GRAD = 0, TERM_MASS = 1, TERM_ELASTIC = 2, TERM_SOURCE = 3, TERM_GRAD_GRAD_TENSOR = 4, TERM_MASS_TENSOR = 5 };
+enum {
+  TERM_GRAD_GRAD = 0,
+  TERM_MASS = 1,
+  TERM_ELASTIC = 2,
+  TERM_SOURCE = 3,
+  TERM_GRAD_GRAD_TENSOR = 4,
+  TERM_MASS_TENSOR = 5,
+  TERM_GRAD_GRAD_TENSOR_FULL = 6,
+  TERM_ADVECTION = 7
+};
 enum { OP_CONST = 0, OP_X, OP_Y, OP_Z, OP_ELEM, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_HEAVISIDE, OP_FIELD,
        OP_SQRT, OP_EXP, OP_LN, OP_LOG10, OP_POW, OP_SIN, OP_COS, OP_TAN, OP_SINH, OP_COSH, OP_TANH, OP_ASIN, OP_ACOS,
        OP_ATAN, OP_ASINH, OP_ACOSH, OP_ATANH, OP_ABS, OP_CONJ, OP_REAL, OP_IMAG, OP_CBRT, OP_ATAN2 };
@@ -55,7 +64,8 @@ typedef struct {
   int32_t kind, dt;
   or_expr coef, coef2;
   or_jacmod jacmod;
-  const or_expr *tensor; /* TERM_GRAD_GRAD_TENSOR, TERM_MASS_TENSOR: D_xx, D_yy, D_zz, D_xy, D_xz, D_yz */
+  const or_expr *tensor; /* TERM_GRAD_GRAD_TENSOR, TERM_MASS_TENSOR: D_xx, D_yy, D_zz, D_xy, D_xz, D_yz;
+                            TERM_GRAD_GRAD_TENSOR_FULL: D row-major [9]; TERM_ADVECTION: b [3] */
 } or_term;
 
 typedef struct {
@@ -431,6 +441,29 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
             for (int r = 0; r < 3; ++r)
               for (int t = 0; t < 3; ++t) s += D[r][t] * G[t * nb + jj] * G[r * nb + ii];
             target[jj + ii * n] += wd * s;
+          }
+      } else if (T->kind == TERM_GRAD_GRAD_TENSOR_FULL) {
+        /* a general TensorFunction: the unknown's field is c D G_j (row-major D) */
+        cplx D[3][3];
+        for (int k = 0; k < 9; ++k) D[k / 3][k % 3] = c * eval_expr(&T->tensor[k], e, xq, ph, nb);
+        or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
+        for (int ii = 0; ii < n; ++ii)
+          for (int jj = 0; jj < n; ++jj) {
+            cplx s = 0.0;
+            for (int r = 0; r < 3; ++r)
+              for (int t = 0; t < 3; ++t) s += D[r][t] * G[t * nb + jj] * G[r * nb + ii];
+            target[jj + ii * n] += wd * s;
+          }
+      } else if (T->kind == TERM_ADVECTION) {
+        /* VectorFunction b times grad(dof u), tested against tf(u): (c b . G_j) conj(phi_i) */
+        cplx bv[3];
+        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, ph, nb);
+        or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
+        const double *bf = b->bval + ((size_t)o * nq + q) * nb;
+        for (int ii = 0; ii < n; ++ii)
+          for (int jj = 0; jj < n; ++jj) {
+            cplx s = bv[0] * G[jj] + bv[1] * G[nb + jj] + bv[2] * G[2 * nb + jj];
+            target[jj + ii * n] += wd * s * conj(bf[ii]);
           }
       } else if (T->kind == TERM_GRAD_GRAD) {
         or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);

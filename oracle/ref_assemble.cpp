@@ -24,7 +24,9 @@
 // scalar (Helmholtz-type) problem, each "<term> <count>" followed by count
 // lines "<op> <arg> <re> <im>" in the bytecode of include/fem_g_gb300.h:
 // term "grad" (integral(g grad(dof u), grad(tf u))), "mass"
-// (integral(m dof(u), tf(u))) or "source" (integral(f, tf(u))). The programs
+// (integral(m dof(u), tf(u))), "source" (integral(f, tf(u))), "dfull_0" ..
+// "dfull_8" (integral(D grad(dof u), grad(tf u)) with the general tensor D,
+// row-major) or "adv_0" .. "adv_2" (integral(b . grad(dof u), tf(u))). The programs
 // become the reference's own expression trees (x(), y(), z(), constants,
 // + - * /, heaviside and the scalar operators of scalarUnaryOperators.h).
 #include <algorithm>
@@ -52,6 +54,7 @@
 #include "scalarUnaryOperators.h"
 #include "tensor4NovenaryOperators.h"
 #include "tensorNovenaryOperators.h"
+#include "vectorTernaryOperators.h"
 
 #include "../fem-g_gb300/host/mesh.h"
 #include "../include/fem_g_gb300_host.h"
@@ -304,7 +307,20 @@ int main(int argc, char **argv) {
                                             lagrange ? field::FunctionSpaceTypeForm0::Lagrange
                                                      : field::FunctionSpaceTypeForm0::HierarchicalH1,
                                             lagrange ? c.mesh_order : c.order);
+      if (c.dirichlet) u.addConstraint(domain::Domain("gammaDir"), T(c.dirichlet_value, 0.0));
       problem::Formulation<T> formulation("coefficients", matrixOptions);
+      if (progs.count("dfull_0")) {  // a general TensorFunction, row-major programs dfull_0 .. dfull_8
+        std::vector<function::ScalarFunction<T>> d;
+        for (int k = 0; k < 9; ++k) d.push_back(fromProgram(progs["dfull_" + std::to_string(k)]));
+        formulation.integral(function::tensor<T>(d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8]) *
+                                 equation::grad(equation::dof(u)),
+                             equation::grad(equation::tf(u)), omega, gauss);
+      }
+      if (progs.count("adv_0"))  // a VectorFunction times grad(dof u), tested against tf(u)
+        formulation.integral(function::vector<T>(fromProgram(progs["adv_0"]), fromProgram(progs["adv_1"]),
+                                                 fromProgram(progs["adv_2"])) *
+                                 equation::grad(equation::dof(u)),
+                             equation::tf(u), omega, gauss);
       if (progs.count("grad"))
         formulation.integral(fromProgram(progs["grad"]) * equation::grad(equation::dof(u)), equation::grad(equation::tf(u)),
                              omega, gauss);
