@@ -45,11 +45,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "element matrices/s and CSR nnz/s: mixed vs FP64 GPU at <=1e-6 rel error, 1 GB300"
 
-# DRAM bytes (read + write) per CSR nonzero of one k_gather launch on the 3D
-# P3 Helmholtz meshes, from an ncu capture of the 30^3 x 6 mesh (162,000 tets,
-# 35,811,451 nonzeros: 555.2 MB read + 550.5 MB written); the per-launch
-# traffic of other sizes of that family is this figure times their nonzeros
-GATHER_TRAFFIC_PER_NNZ_P3 = (555.207680e6 + 550.488064e6) / 35811451
+# DRAM bytes (read + write) per CSR nonzero of one reduction launch on the 3D
+# P3 Helmholtz meshes, from ncu captures of the 30^3 x 6 mesh (162,000 tets,
+# 35,811,451 nonzeros); the per-launch traffic of other sizes of that family
+# is this figure times their nonzeros. k_gather: 555.2 MB read + 550.5 MB
+# written.
+GATHER_TRAFFIC_PER_NNZ_P3 = {"k_gather": (555.207680e6 + 550.488064e6) / 35811451}
 
 
 def load_femg():
@@ -185,9 +186,14 @@ def profile_run(femg, torch, fn):
 
 def roofline(prof, alg_bytes, pk, pk_kind, traffic=None, traffic_src=None, steps=1):
     """Roofline of the dominant kernel: the algorithmic bytes its launches
-    carry per step over their summed device time per step."""
+    carry per step over their summed device time per step. alg_bytes is the
+    fused-minimum byte count of the whole step, or {kernel: bytes} where
+    kernels cover different problems (the per-class reductions of a batch):
+    the fused-minimum bytes of the problems that kernel's launches process."""
     dom, (dcount, dms) = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 0.0))
     per_step_ms = dms / max(steps, 1)
+    if isinstance(alg_bytes, dict):
+        alg_bytes = alg_bytes.get(dom, 0)
     achieved = alg_bytes / (per_step_ms / 1000.0) / 1e9 if per_step_ms > 0 else 0.0
     return {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
             "traffic": traffic, "traffic_source": traffic_src, "kernel": dom,
@@ -284,8 +290,17 @@ def bench_batch(args, femg, torch):
     ptrs = None
     torch.cuda.empty_cache()
     pk, pk_kind = peaks()
-    alg = sum(fused_bytes(p.info()["E"], p.info()["n"], p.prob.nnz, int(p.prob.sys.n_rows), coef=0) for p in plans)
-    roof = roofline(res["prof"], alg, pk, pk_kind)
+    algq = [fused_bytes(p.info()["E"], p.info()["n"], p.prob.nnz, int(p.prob.sys.n_rows), coef=0) for p in plans]
+    alg = sum(algq)
+    # the reduction kernels by class (element DOFs n): vector-load or scalar
+    v4n = {c["n"] for c in res["mixed"]["tuning"]["gather"] if c.get("vector_loads")}
+    alg_by = {k: alg for k in res["prof"] if not k.startswith("k_gather")}
+    alg_by["k_gather_batch_v4"] = sum(a for p, a in zip(plans, algq) if p.info()["n"] in v4n)
+    alg_by["k_gather_batch"] = sum(a for p, a in zip(plans, algq) if p.info()["n"] not in v4n)
+    roof = roofline(res["prof"], alg_by, pk, pk_kind)
+    step_gbs = alg / (res["mixed"]["ms"] / 1000.0) / 1e9
+    roof["step"] = {"achieved": step_gbs, "frac": step_gbs / pk["hbm_gbs"], "algorithmic_bytes": alg,
+                    "note": "fused-minimum bytes of all problems over the whole step"}
     cpu = None
     if not args.no_cpu:
         # the oracle per order on the largest problem of that order, a bounded
@@ -387,6 +402,9 @@ def bench_multi_freq(args, femg, torch):
     # pair and map once, F complex values per nonzero
     alg = E * (4 * 3 * 8 + 4 * 4 + 32 + n * n * 4) + F * nnz * 16
     roof = roofline(res["prof"], alg, pk, pk_kind)
+    step_gbs = alg / (res["mixed"] / 1000.0) / 1e9
+    roof["step"] = {"achieved": step_gbs, "frac": step_gbs / pk["hbm_gbs"],
+                    "note": "the same fused-minimum bytes over the whole step (all kernels)"}
     cpu = None
     if not args.no_cpu:
         a = prob.arrays()
@@ -722,13 +740,16 @@ def bench_headline(args, femg, torch, ws, rank, local, dist):
     avg_ms = dms / max(dcount, 1)
     achieved = alg_bytes / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
     traffic, traffic_src = None, None
-    if dom == "k_gather" and args.workload in ("c2", "c3") and head == "mixed":
-        traffic = GATHER_TRAFFIC_PER_NNZ_P3 * nnz
-        traffic_src = "ncu dram bytes of k_gather on the 30^3 x 6 P3 mesh, scaled by nonzeros"
+    if dom in GATHER_TRAFFIC_PER_NNZ_P3 and args.workload in ("c2", "c3") and head == "mixed":
+        traffic = GATHER_TRAFFIC_PER_NNZ_P3[dom] * nnz
+        traffic_src = "ncu dram bytes of %s on the 30^3 x 6 P3 mesh, scaled by nonzeros" % dom
+    step_gbs = alg_bytes / (ms_head / 1000.0) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src, "kernel": dom,
             "kernel_avg_ms": avg_ms, "algorithmic_bytes": alg_bytes, "peak_source": pk_kind,
-            "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in (prof or {}).items()}}
+            "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in (prof or {}).items()},
+            "step": {"achieved": step_gbs, "frac": step_gbs / pk["hbm_gbs"],
+                     "note": "the same fused-minimum bytes over the whole step (all kernels)"}}
 
     if rank == 0:
         cpu = None

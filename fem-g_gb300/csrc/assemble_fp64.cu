@@ -183,24 +183,32 @@ struct FullWarpSmem {
   double J0[9], J[9], Jinv[9];
   double det0, det;
   double2 M[9], v[3], m, s;
-  double G[3][kMaxDofs];
-  double phi[kMaxDofs];
-  double U[2][3][kMaxDofs];
-  double a[2][kMaxDofs];
+  double G[3][kMaxDofs];     // test functions: physical gradients
+  double phi[kMaxDofs];      // and values
+  double U[2][3][kMaxDofs];  // unknown functions: M G_j (real, imaginary parts)
+  double a[2][kMaxDofs];     // and v . G_j + m phi_j
 };
 
+// Full (non-symmetric) element matrices: Ke[i][j] = sum_q G_i . (M G_j) +
+// phi_i (v . G_j + m phi_j) with the test function i (rows) and the unknown
+// function j (columns), M the scaled diffusion tensor (isotropic, symmetric
+// and general parts), v the advection vector, m the mass coefficient. A
+// two-field plan takes the test functions from the test field's tables and
+// the unknown functions from the unknown field's (BilinearTerm with
+// _field[0] != _field[1], src/term/BilinearTerm.cpp:304-343): Ke is n x nc.
 template <int MAXENT, bool CPLX>
 __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
     k_element_full_fp64(const PlanDev p, const DevTerms *__restrict__ terms, double *__restrict__ ke, double2 *__restrict__ be) {
   __shared__ FullWarpSmem smem[kWarpsPerBlockElem];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  const int n = p.nb;
-  const int nEnt = n * n;
+  const int n = p.nb, nU = p.nbU;
+  const int nEnt = n * nU;
   FullWarpSmem &S = smem[warp];
   const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlockElem;
   for (int64_t e = (int64_t)blockIdx.x * kWarpsPerBlockElem + warp; e < p.E; e += stride) {
     const int o = p.orient ? p.orient[e] : 0;
+    const int oU = p.orientU ? p.orientU[e] : 0;
     for (int t = lane; t < p.nn * 3; t += 32) S.X[t] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + t / 3] + t % 3];
     __syncwarp();
     double accR[MAXENT], accI[MAXENT];
@@ -253,30 +261,34 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
       for (int i = lane; i < n; i += 32) {
         const double g0 = p.bgrad[3 * (base + i)], g1 = p.bgrad[3 * (base + i) + 1], g2 = p.bgrad[3 * (base + i) + 2];
         const double ph = p.bval[base + i];
-        double G[3];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          G[r] = S.Jinv[r] * g0 + S.Jinv[3 + r] * g1 + S.Jinv[6 + r] * g2;
-          S.G[r][i] = G[r];
-        }
+        for (int r = 0; r < 3; ++r) S.G[r][i] = S.Jinv[r] * g0 + S.Jinv[3 + r] * g1 + S.Jinv[6 + r] * g2;
         S.phi[i] = ph;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          S.U[0][r][i] = S.M[3 * r].x * G[0] + S.M[3 * r + 1].x * G[1] + S.M[3 * r + 2].x * G[2];
-          if (CPLX) S.U[1][r][i] = S.M[3 * r].y * G[0] + S.M[3 * r + 1].y * G[1] + S.M[3 * r + 2].y * G[2];
-        }
-        S.a[0][i] = S.v[0].x * G[0] + S.v[1].x * G[1] + S.v[2].x * G[2] + S.m.x * ph;
-        if (CPLX) S.a[1][i] = S.v[0].y * G[0] + S.v[1].y * G[1] + S.v[2].y * G[2] + S.m.y * ph;
         const int slot = i >> 5;
         bacc[slot].x += S.s.x * ph;
         bacc[slot].y += S.s.y * ph;
+      }
+      const size_t baseU = ((size_t)oU * p.nq + q) * nU;
+      for (int j = lane; j < nU; j += 32) {
+        const double g0 = p.bgradU[3 * (baseU + j)], g1 = p.bgradU[3 * (baseU + j) + 1], g2 = p.bgradU[3 * (baseU + j) + 2];
+        const double ph = p.bvalU[baseU + j];
+        double G[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) G[r] = S.Jinv[r] * g0 + S.Jinv[3 + r] * g1 + S.Jinv[6 + r] * g2;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          S.U[0][r][j] = S.M[3 * r].x * G[0] + S.M[3 * r + 1].x * G[1] + S.M[3 * r + 2].x * G[2];
+          if (CPLX) S.U[1][r][j] = S.M[3 * r].y * G[0] + S.M[3 * r + 1].y * G[1] + S.M[3 * r + 2].y * G[2];
+        }
+        S.a[0][j] = S.v[0].x * G[0] + S.v[1].x * G[1] + S.v[2].x * G[2] + S.m.x * ph;
+        if (CPLX) S.a[1][j] = S.v[0].y * G[0] + S.v[1].y * G[1] + S.v[2].y * G[2] + S.m.y * ph;
       }
       __syncwarp();
 #pragma unroll
       for (int m = 0; m < MAXENT; ++m) {
         const int k = lane + 32 * m;
         if (k < nEnt) {
-          const int i = k / n, j = k - i * n;
+          const int i = k / nU, j = k - i * nU;
           accR[m] += S.G[0][i] * S.U[0][0][j] + S.G[1][i] * S.U[0][1][j] + S.G[2][i] * S.U[0][2][j] + S.phi[i] * S.a[0][j];
           if (CPLX)
             accI[m] += S.G[0][i] * S.U[1][0][j] + S.G[1][i] * S.U[1][1][j] + S.G[2][i] * S.U[1][2][j] + S.phi[i] * S.a[1][j];
@@ -570,7 +582,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
 static int launchElementKernels(fg_plan *plan, const DevTerms &terms, const DevTerms *dterms, double *ke, double *be, cudaStream_t s) {
   const PlanDev &p = plan->d;
   if (terms.nonSym) {
-    const int perLane = (p.nb * p.nb + 31) / 32;
+    const int perLane = (p.nb * p.nbU + 31) / 32;
     int64_t blocks = std::min<int64_t>((p.E + kWarpsPerBlockElem - 1) / kWarpsPerBlockElem, (int64_t)smCount() * 64);
     if (blocks < 1) blocks = 1;
     const bool cplx = terms.complexKe != 0;
@@ -756,13 +768,14 @@ extern "C" int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_
   const DevTerms *dterms = nullptr;
   int st = resolveTerms(plan, terms, n_terms, frequency, &dt, &dterms, s);
   if (st) return st;
+  if ((st = coupledLiftCheck(plan, rhs))) return st;
   const double *uD = nullptr;
   if ((st = uploadDirichlet(plan, dirichlet, &uD, s))) return st;
   Outputs o;
   if ((st = prepareOutputs(plan, csr_values, rhs, &o))) return st;
   const PlanDev &p = plan->d;
   const int ncomp = dt.complexKe ? 2 : 1;
-  if ((st = ensureDevice((void **)&plan->ke, &plan->keBytes, (size_t)p.E * ncomp * p.n * p.n * sizeof(double)))) return st;
+  if ((st = ensureDevice((void **)&plan->ke, &plan->keBytes, (size_t)p.E * ncomp * p.n * p.nc * sizeof(double)))) return st;
   double *be = nullptr;
   if (dt.hasSource && rhs) {
     if ((st = ensureDevice((void **)&plan->be, &plan->beBytes, (size_t)p.E * p.n * 16))) return st;
@@ -771,6 +784,6 @@ extern "C" int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_
   if (p.E > 0) {
     if ((st = launchElementFp64(plan, dt, dterms, plan->ke, be, s))) return st;
   }
-  if ((st = gatherToOutputs(plan, plan->ke, dt.complexKe, 0, keFull(plan->d.n), be, uD, o, csr_values, s))) return st;
+  if ((st = gatherToOutputs(plan, plan->ke, dt.complexKe, 0, keRect(p.n, p.nc), be, uD, o, csr_values, s))) return st;
   return finishOutputs(plan, o, csr_values, rhs, s);
 }

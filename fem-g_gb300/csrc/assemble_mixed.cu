@@ -1148,6 +1148,10 @@ extern "C" int fg_assemble_mixed(fg_plan *plan, const fg_term_desc *terms, int32
     setLastError("mixed path: Jacobian modificators make the geometry point-dependent; use the FP64 path");
     return FG_ERR_UNSUPPORTED;
   }
+  if (plan->d.coupled) {
+    setLastError("mixed path: two-field plans run on the FP64 path");
+    return FG_ERR_UNSUPPORTED;
+  }
   if (dt.nonSym) {
     setLastError("mixed path: the full-tensor and advection terms run on the FP64 path");
     return FG_ERR_UNSUPPORTED;

@@ -62,6 +62,7 @@ extern "C" int fg_assemble_fp64_static(fg_plan *plan, const double *dirichlet, d
     return FG_ERR_ARG;
   }
   const PlanDev &p = plan->d;
+  if (int st0 = coupledLiftCheck(plan, rhs)) return st0;
   const double *uD = nullptr;
   if (p.nFixed > 0) {
     if (!dirichlet || !isDevicePointer(dirichlet)) {
@@ -72,10 +73,10 @@ extern "C" int fg_assemble_fp64_static(fg_plan *plan, const double *dirichlet, d
   }
   const DevTerms &dt = plan->bound;
   const int ncomp = dt.complexKe ? 2 : 1;
-  // [E][ncomp][n][n] element matrices, then [E][n] complex element vectors at
+  // [E][ncomp][n][nc] element matrices, then [E][n] complex element vectors at
   // the next 256-byte boundary. Every entry is written by the element kernels
   // before the gather reads it, so no part of the array is cleared.
-  const size_t keBytes = (size_t)p.E * ncomp * p.n * p.n * sizeof(double);
+  const size_t keBytes = (size_t)p.E * ncomp * p.n * p.nc * sizeof(double);
   const bool withBe = dt.hasSource && rhs;
   const size_t beOff = (keBytes + 255) / 256 * 256;
   const size_t need = withBe ? beOff + (size_t)p.E * p.n * 16 : keBytes;
@@ -93,5 +94,5 @@ extern "C" int fg_assemble_fp64_static(fg_plan *plan, const double *dirichlet, d
   if (p.E > 0) {
     if ((st = launchElementFp64(plan, dt, plan->boundDev, ke, be, s))) return st;
   }
-  return launchGather(plan, ke, dt.complexKe, 0, keFull(p.n), be, uD, csr_values, rhs, s);
+  return launchGather(plan, ke, dt.complexKe, 0, keRect(p.n, p.nc), be, uD, csr_values, rhs, s);
 }

@@ -98,6 +98,9 @@ struct fg_batch {
   int nCta = 0, maxK3 = 0;
   size_t smem = 0;
   std::vector<GemmClass> gemmClasses;
+  // contraction cost of one tile of problem q (CTA-milliseconds), measured
+  // per class by the tuner; empty: the analytic estimate
+  std::vector<double> tileCost;
   int *err = nullptr;
   int *errHost = nullptr;
   cudaEvent_t errEvent = nullptr;
@@ -185,17 +188,25 @@ int runAll(fg_batch *b, cudaStream_t s) {
   return FG_OK;
 }
 
-// contraction schedule over the tiles of all problems (current mmaN per problem)
+// contraction schedule over the tiles of all problems (current mmaN per
+// problem): contiguous tile ranges per CTA of equal total cost. The cost of a
+// tile is its class's measured time per tile once the tuner has timed every
+// class on its own (a tile of 16 columns costs about a sixteenth of one of
+// 1232, not the 47th that its MMA work suggests: the A load and the fixed
+// per-tile steps weigh more in narrow tiles), else the analytic estimate.
 int buildGemmSchedule(fg_batch *b, const std::vector<int> *only, int4 **tiles, int32_t **ctaStart, int *nCta,
                       std::vector<int4> *hostTiles) {
   hostTiles->clear();
   std::vector<double> cost;
+  const bool measured = !only && (int)b->tileCost.size() == b->n;
   for (int q = 0; q < b->n; ++q) {
     if (only && std::find(only->begin(), only->end(), q) == only->end()) continue;
     std::vector<int4> t = mixedTiles(b->plans[q], q, b->gemmHost[q].rowsPerElem);
+    const double full = measured ? b->tileCost[q] : (double)b->gemmHost[q].Npad * b->gemmHost[q].K3 + 256.0;
     for (const int4 &x : t) {
       hostTiles->push_back(x);
-      cost.push_back((double)b->gemmHost[q].Npad * b->gemmHost[q].K3 + 256.0);
+      // a partial tile drains fewer rows; its MMAs and loads cost the same
+      cost.push_back(measured ? full * (0.5 + 0.5 * x.w / 128.0) : full);  // 128-row tiles
     }
   }
   *nCta = std::max(1, std::min(smCount(), (int)hostTiles->size()));
@@ -257,12 +268,14 @@ int tune(fg_batch *b, cudaStream_t s) {
       if (st) return st;
       gc.mmaN = bestW;
       for (int q : gc.probs) b->gemmHost[q].mmaN = bestW;
+      if (b->tileCost.size() != (size_t)b->n) b->tileCost.assign(b->n, 0.0);
+      for (int q : gc.probs) b->tileCost[q] = ht.empty() ? 0.0 : (double)best * nc / (double)ht.size();
       gj += std::string(ci ? ", " : "") + "{\"npad\": " + std::to_string(gc.Npad) + ", \"k3\": " + std::to_string(gc.K3) +
             ", \"mma_n\": " + std::to_string(bestW) + ", \"ms\": " + std::to_string(best) + "}";
     }
     if ((st = uploadGemmProblems(b))) return st;
     if ((st = buildGemmSchedule(b, nullptr, &b->tiles, &b->ctaStart, &b->nCta, &b->tilesHost))) return st;
-    js = "{\"contract\": [" + gj + "], \"gather\": [";
+    js = "{\"contract\": [" + gj + "], \"contract_schedule\": \"measured per-class tile costs\", \"gather\": [";
   }
   if ((st = runElements(b, s))) return st;
   for (size_t ci = 0; ci < b->classes.size(); ++ci) {
@@ -370,6 +383,11 @@ extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const 
     setLastError("fg_batch_create: 1..4096 plans required");
     return FG_ERR_ARG;
   }
+  for (int32_t q = 0; q < n_problems; ++q)
+    if (plans[q] && plans[q]->d.coupled) {
+      setLastError("fg_batch_create: two-field plans are assembled with fg_assemble_fp64");
+      return FG_ERR_UNSUPPORTED;
+    }
   for (int32_t q = 0; q < n_problems; ++q)
     if (plans[q] && plans[q]->accumulate) {
       setLastError("fg_batch_create: a plan accumulates into shared outputs; batches overwrite theirs");

@@ -143,6 +143,17 @@ struct PlanDev {
   int32_t maxRowLen;
   int *jmErr;             // set by the FP64 element kernels: an integration point outside a shell
   const double2 *lscale;  // [E][n] linked DOF coefficient (1 for other DOFs), or null without linked DOFs
+  // The columns: the unknown field's DOFs. A plan of one field has them equal
+  // to the rows (nc = n, the U tables alias the ones above); a two-field plan
+  // (fg_plan_create_coupled) has the test field's DOFs as rows and the
+  // unknown field's as columns, element matrices [E][n][nc].
+  int32_t coupled;        // 1: two-field plan
+  int32_t nc, nbU, nOrientU;
+  const double *bvalU;    // [nOrientU][nq][nbU]
+  const double *bgradU;   // [nOrientU][nq][nbU][3]
+  const int32_t *orientU; // [E] or null
+  const uint32_t *edofU;  // [E][nc]: column index, or fixed index for fixed DOFs
+  const uint8_t *etypeU;  // [E][nc]: FG_AT_*
 };
 
 }  // namespace femg
@@ -179,6 +190,7 @@ struct fg_plan {
   femg::DevTerms *boundDev = nullptr;  // device copy of the bound terms
   femg::DevTerms *termsDev = nullptr;  // device copy of the last per-call terms
   bool hasBound = false;
+  bool fixedColumns = false;  // a two-field plan with fixed unknown DOFs (lifting into the test rows)
   // mixed-precision state (reference tensors per orientation), see assemble_mixed.cu
   void *mixed = nullptr;
   // multi-frequency state (term groups, element matrices), see multi_freq.cu
@@ -220,11 +232,19 @@ struct KeLayout {
   int32_t kind, ld;
 };
 inline KeLayout keFull(int n) { return KeLayout{kKeFull, n * n}; }
+// full layout of a two-field plan: n rows of nc entries
+inline KeLayout keRect(int n, int nc) { return KeLayout{kKeFull, n * nc}; }
+// offset of entry (ii, jj); n: entries per row in the full layout (the
+// columns nc), the basis count times 3 in the compound one
 __device__ __forceinline__ int keOffset(const KeLayout &lay, int n, int ii, int jj) {
   if (lay.kind == kKeFull) return ii * n + jj;
   const int nb = n / 3, i = ii / 3, a = ii - 3 * i, j = jj / 3, b = jj - 3 * j;
   return ((a * 3 + b) * nb + i) * nb + j;
 }
+// FG_ERR_UNSUPPORTED (with the message set) when a two-field plan would lift
+// fixed unknown DOFs into `rhs` through a block of n != nc: the reference's
+// addValuesDC reads values[j * nc + i] there, outside the element matrix
+int coupledLiftCheck(const fg_plan *plan, const double *rhs);
 // gather of element matrices/vectors into CSR values and RHS
 int launchGather(fg_plan *plan, const double *ke, int keComplex, int keIsFloat, KeLayout lay, const double *be,
                  const double *dirichletDev, double *values, double *rhs, cudaStream_t s);

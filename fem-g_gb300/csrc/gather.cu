@@ -28,7 +28,7 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
   constexpr int SS = KCPLX ? 2 : 1;
   // offset of entry (test ii, unknown jj) inside one component of an element
   // matrix in the layout lay (compound blocks: ii = i*3 + a, jj = j*3 + b)
-  auto keOff = [&](int ii, int jj) -> int { return keOffset(lay, p.n, ii, jj); };
+  auto keOff = [&](int ii, int jj) -> int { return keOffset(lay, p.nc, ii, jj); };
   extern __shared__ __align__(16) unsigned char smraw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / L, lt = lane % L;
@@ -36,7 +36,7 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
   const SlotT *slot = (const SlotT *)p.slot;
   const SlotT kFixed = (SlotT)(sizeof(SlotT) == 1 ? 0xFF : kSlotFixed);
   const SlotT kIgnore = (SlotT)(sizeof(SlotT) == 1 ? 0xFE : kSlotIgnore);
-  const int n = p.n;
+  const int n = p.n, nc = p.nc;  // element rows (test DOFs), columns (unknown DOFs)
   const size_t nn2 = (size_t)lay.ld;  // entries per component
   // visit records [v0, v1) of this launch
   const int64_t nRows = v1;
@@ -76,7 +76,7 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
 #pragma unroll
       for (int jj = 0; jj < J; ++jj) {
         const int j = lt + L * jj;
-        const bool ok = act && j < n;
+        const bool ok = act && j < nc;
         const int o = keOff(i, j);
         s_[jj] = ok ? S[j] : kIgnore;
         r_[jj] = ok ? K[o] : (KT)0;
@@ -119,12 +119,13 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
           atomicAdd(&A[(int)s * SS], ar);
           if (KCPLX) atomicAdd(&A[(int)s * SS + 1], ai);
         } else {
+          // (a two-field plan with fixed columns has as many columns as rows)
           const KT *Kt = ke + (size_t)e * SS * nn2;
           const int j = lt + L * jj;
           const int o = keOff(j, i);
           double2 v = make_double2((double)Kt[o], KCPLX ? (double)Kt[nn2 + o] : 0.0);
           if (linked) v = cmul(cI, v);
-          dc = cadd(dc, cmul(v, uD[p.edof[e * n + j]]));
+          dc = cadd(dc, cmul(v, uD[p.edofU[e * nc + j]]));
         }
       }
       __syncwarp();
@@ -220,7 +221,7 @@ __device__ __forceinline__ void gatherRowsV4(const PlanDev &p, const float *__re
           const uint32_t e = flat / (uint32_t)n, i = flat - e * (uint32_t)n;
           const int j = 4 * lt + c;
           const double kt = (double)ke[(size_t)e * nn2 + (size_t)j * n + i];
-          const double2 u = uD[p.edof[(size_t)e * n + j]];
+          const double2 u = uD[p.edofU[(size_t)e * n + j]];
           dc.x += kt * u.x;
           dc.y += kt * u.y;
         }
@@ -297,7 +298,8 @@ __global__ void __launch_bounds__(256) k_gather_batch(const GatherJob *__restric
 // k_gather_v4 where it applies: real FP32 element matrices in full layout,
 // n a multiple of 4 (at most 32 columns), one-byte slots, no linked DOFs
 static bool gatherV4Applies(const PlanDev &p, int keComplex, int keIsFloat, KeLayout lay) {
-  return keIsFloat && !keComplex && lay.kind == kKeFull && p.n % 4 == 0 && p.n <= 32 && p.slotBytes == 1 && !p.lscale;
+  return keIsFloat && !keComplex && lay.kind == kKeFull && p.n % 4 == 0 && p.n <= 32 && p.slotBytes == 1 && !p.lscale &&
+         !p.coupled;
 }
 
 static int launchV4(const PlanDev &p, const float *ke, const double2 *be, const double2 *uD, double2 *values, double2 *rhs,
@@ -330,7 +332,7 @@ template <typename SlotT, bool KCPLX, typename KT>
 static int launchTyped(const PlanDev &p, const void *ke, const double2 *be, const double2 *uD, double2 *values, double2 *rhs,
                        KeLayout lay, int64_t v0, int64_t v1, bool acc, cudaStream_t s) {
   using AT = KT;  // FP32 element matrices accumulate in FP32, FP64 ones in FP64
-  const GatherShape shape = gatherShape(p.n, p.maxRowLen, KCPLX ? 1 : 0, sizeof(KT) == 4 ? 1 : 0, 0, 0);
+  const GatherShape shape = gatherShape(p.nc, p.maxRowLen, KCPLX ? 1 : 0, sizeof(KT) == 4 ? 1 : 0, 0, 0);
   const int L = shape.L, J = shape.J;
   const int R = 32 / L;
   const size_t rowBytes = (size_t)std::max(p.maxRowLen, 1) * (KCPLX ? 2 : 1) * sizeof(AT);
@@ -528,6 +530,7 @@ int launchGatherBatch(const GatherJob *jobsDev, int nJobs, int64_t blocks, int s
     FG_CUDA(cudaGetLastError());
     return FG_OK;
   }
+  ProfScope prof("k_gather_batch", s);
   if (slotBytes == 1) {
     if (keIsFloat)
       return kcplx ? launchBatchTyped<uint8_t, true, float>(jobsDev, nJobs, blocks, g, s) : launchBatchTyped<uint8_t, false, float>(jobsDev, nJobs, blocks, g, s);

@@ -284,6 +284,10 @@ int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t
               const std::function<int(const int *, int, double2 *, double2 *)> &coefOf) {
   MultiState *m = multiState(plan);
   const PlanDev &p = plan->d;
+  if (p.coupled) {
+    setLastError("several frequencies / separate matrices: two-field plans are assembled with fg_assemble_fp64");
+    return FG_ERR_UNSUPPORTED;
+  }
   if (plan->accumulate) {
     setLastError("several frequencies / separate matrices: the plan accumulates; assemble one frequency at a time");
     return FG_ERR_UNSUPPORTED;

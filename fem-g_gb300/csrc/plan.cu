@@ -123,8 +123,11 @@ static int upload(fg_plan *plan, const T *host, size_t count, const T **dev) {
 
 static bool isRow(int t) { return t == FG_AT_UNKNOWN || t == FG_AT_UNKNOWN_BUBBLE || t == FG_AT_UNKNOWN_GLOBAL; }
 
+// uspace, uidx, utype: the unknown field of a two-field plan (columns), or
+// null for a plan of one field
 static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_space_desc *space, const fg_system_desc *sys,
-                      fg_plan *plan) {
+                      fg_plan *plan, const fg_space_desc *uspace = nullptr, const uint64_t *uidx = nullptr,
+                      const int32_t *utype = nullptr) {
   PlanDev &d = plan->d;
   std::memset(&d, 0, sizeof(d));  // every table absent until uploaded
   if (mesh->dim != 2 && mesh->dim != 3) {
@@ -166,6 +169,27 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   }
   d.n = n;
   d.nOrient = space->n_orientations;
+  const bool coupled = uspace != nullptr;
+  int nc = n;
+  if (coupled) {
+    nc = uspace->n_basis * uspace->multiplicity;
+    if (space->form != FG_FORM_0 || uspace->form != FG_FORM_0 || space->multiplicity != 1 || uspace->multiplicity != 1) {
+      setLastError("fg_plan_create_coupled: scalar H1 fields (FG_FORM_0, one component) on both sides");
+      return FG_ERR_UNSUPPORTED;
+    }
+    if (uspace->n_basis <= 0 || nc > kMaxDofs || uspace->n_orientations <= 0 || !uspace->basis_val || !uspace->basis_grad) {
+      setLastError("fg_plan_create_coupled: unknown space: element DOFs must be in [1, 64], with basis tables");
+      return FG_ERR_ARG;
+    }
+    if (sys->n_linked) {
+      setLastError("fg_plan_create_coupled: linked DOFs are not supported in two-field plans");
+      return FG_ERR_UNSUPPORTED;
+    }
+  }
+  d.coupled = coupled ? 1 : 0;
+  d.nc = nc;
+  d.nbU = coupled ? uspace->n_basis : space->n_basis;
+  d.nOrientU = coupled ? uspace->n_orientations : space->n_orientations;
   d.affine = (nn == mesh->dim + 1) ? 1 : 0;
   // first-order simplex with the standard basis: dN_0 = -1, dN_k = e_(k-1)
   d.p1geom = d.affine;
@@ -224,13 +248,14 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
     }
     d.affine = curved ? 0 : 1;
   }
-  if (space->n_orientations > 1) {
-    if (!space->elem_orientation) {
+  for (const fg_space_desc *sp : {space, uspace}) {
+    if (!sp || sp->n_orientations <= 1) continue;
+    if (!sp->elem_orientation) {
       setLastError("fg_plan_create: elem_orientation required with several orientations");
       return FG_ERR_ARG;
     }
     for (int64_t e = 0; e < E; ++e)
-      if (space->elem_orientation[e] < 0 || space->elem_orientation[e] >= space->n_orientations) {
+      if (sp->elem_orientation[e] < 0 || sp->elem_orientation[e] >= sp->n_orientations) {
         setLastError("fg_plan_create: orientation index out of range");
         return FG_ERR_INDEX;
       }
@@ -270,6 +295,30 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
     setLastError("fg_plan_create: element DOF index/type out of range");
     return FG_ERR_INDEX;
   }
+  // the columns: the unknown field's DOFs (a two-field plan), else the rows'
+  std::vector<uint32_t> edofU;
+  std::vector<uint8_t> etypeU;
+  if (coupled) {
+    edofU.resize((size_t)E * nc);
+    etypeU.resize((size_t)E * nc);
+#pragma omp parallel for reduction(+ : bad)
+    for (int64_t i = 0; i < E * nc; ++i) {
+      const int t = utype[i];
+      const uint64_t v = uidx[i];
+      if (t < 0 || t > FG_AT_LINKED_BUBBLE || t == FG_AT_LINKED || t == FG_AT_LINKED_BUBBLE) ++bad;
+      else if (isRow(t) && v >= sys->n_rows) ++bad;
+      else if (t == FG_AT_FIXED && v >= sys->n_fixed) ++bad;
+      edofU[(size_t)i] = (uint32_t)v;
+      etypeU[(size_t)i] = (uint8_t)t;
+    }
+    if (bad) {
+      setLastError("fg_plan_create_coupled: unknown DOF index/type out of range (linked DOFs are not supported)");
+      return FG_ERR_INDEX;
+    }
+    plan->fixedColumns = std::find(etypeU.begin(), etypeU.end(), (uint8_t)FG_AT_FIXED) != etypeU.end();
+  }
+  const std::vector<uint32_t> &cdof = coupled ? edofU : edof;
+  const std::vector<uint8_t> &ctype = coupled ? etypeU : etype;
 
   // row -> (element, local test index) lists, element order
   std::vector<uint64_t> rowPtr(sys->n_rows + 1, 0);
@@ -355,7 +404,7 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   d.maxRowLen = (int32_t)maxLen;
   const bool narrow = maxLen < 0xFE;
   d.slotBytes = narrow ? 1 : 2;
-  const int nS = n;
+  const int nS = nc;
   d.slotLd = nS;
   const size_t nSlots = (size_t)E * n * nS;
   std::vector<uint8_t> slot8;
@@ -369,15 +418,15 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
       const uint64_t I = edof[ki];
       const uint64_t *b = sys->aj + sys->ai[I];
       const uint64_t *en2 = sys->aj + sys->ai[I + 1];
-      for (int j = 0; j < n; ++j) {
-        const size_t kj = (size_t)e * n + j;
-        const int t = etype[kj];
+      for (int j = 0; j < nc; ++j) {
+        const size_t kj = (size_t)e * nc + j;
+        const int t = ctype[kj];
         uint16_t s;
         if (t == FG_AT_FIXED) s = kSlotFixed;
         else if (!isRow(t)) s = kSlotIgnore;
-        else if (sys->upper && edof[kj] < I) s = kSlotIgnore;  // below the diagonal: not stored
+        else if (sys->upper && cdof[kj] < I) s = kSlotIgnore;  // below the diagonal: not stored
         else {
-          const uint64_t J = edof[kj];
+          const uint64_t J = cdof[kj];
           const uint64_t *p = std::lower_bound(b, en2, J);
           if (p != en2 && (*p == J || sys->upper)) {
             // Upper storage: an aliased bubble row whose first bubble has a
@@ -416,6 +465,22 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
     if ((st = upload(plan, space->elem_orientation, (size_t)E, &d.orient))) return st;
   if ((st = upload(plan, edof.data(), edof.size(), &d.edof))) return st;
   if ((st = upload(plan, etype.data(), etype.size(), &d.etype))) return st;
+  if (coupled) {
+    if ((st = upload(plan, edofU.data(), edofU.size(), &d.edofU))) return st;
+    if ((st = upload(plan, etypeU.data(), etypeU.size(), &d.etypeU))) return st;
+    if ((st = upload(plan, uspace->basis_val, (size_t)uspace->n_orientations * rule->nq * uspace->n_basis, &d.bvalU))) return st;
+    if ((st = upload(plan, uspace->basis_grad, (size_t)uspace->n_orientations * rule->nq * uspace->n_basis * 3, &d.bgradU)))
+      return st;
+    d.orientU = nullptr;
+    if (uspace->n_orientations > 1)
+      if ((st = upload(plan, uspace->elem_orientation, (size_t)E, &d.orientU))) return st;
+  } else {
+    d.edofU = d.edof;
+    d.etypeU = d.etype;
+    d.bvalU = d.bval;
+    d.bgradU = d.bgrad;
+    d.orientU = d.orient;
+  }
   if ((st = upload(plan, sys->ai, (size_t)sys->n_rows + 1, &d.ai))) return st;
   if ((st = upload(plan, rowPtr.data(), rowPtr.size(), &d.rowPtr))) return st;
   if ((st = upload(plan, rowElem.data(), rowElem.size(), &d.rowElem))) return st;
@@ -452,6 +517,14 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   d.jmErr = const_cast<int *>(err);
   FG_CUDA(cudaMallocHost(&plan->jmErrHost, sizeof(int)));
   return FG_OK;
+}
+
+int coupledLiftCheck(const fg_plan *plan, const double *rhs) {
+  if (!plan->d.coupled || !plan->fixedColumns || !rhs || plan->d.n == plan->d.nc) return FG_OK;
+  setLastError("two-field plan: fixed unknown DOFs lift through VectorFactory::addValuesDC, which reads values[j * n_unknown + i]; "
+               "with " + std::to_string(plan->d.n) + " test and " + std::to_string(plan->d.nc) +
+               " unknown DOFs per element that entry lies outside the element matrix (pass rhs = NULL for the values alone)");
+  return FG_ERR_UNSUPPORTED;
 }
 
 int uploadDirichlet(fg_plan *plan, const double *dirichlet, const double **out, cudaStream_t s) {
@@ -608,6 +681,10 @@ static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complex
       setLastError("field values (FG_OP_FIELD) need an H1 bucket");
       return FG_ERR_UNSUPPORTED;
     }
+    if (field && plan->d.coupled) {
+      setLastError("field values (FG_OP_FIELD) are not supported in two-field plans");
+      return FG_ERR_UNSUPPORTED;
+    }
     const size_t bytes = (size_t)plan->E * 16 * (field ? (size_t)plan->d.nb : 1);
     if (isDevicePointer(ex.elem_values[a])) {
       out->arr[a] = (const double2 *)ex.elem_values[a];
@@ -690,6 +767,13 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
       setLastError("the full-tensor and advection terms need a scalar H1 field");
       return FG_ERR_UNSUPPORTED;
     }
+    if (plan->d.coupled && src.kind != FG_TERM_GRAD_GRAD && src.kind != FG_TERM_MASS &&
+        src.kind != FG_TERM_GRAD_GRAD_TENSOR_FULL && src.kind != FG_TERM_ADVECTION) {
+      setLastError(src.kind == FG_TERM_SOURCE
+                       ? "two-field plan: linear terms go to the test field's own plan"
+                       : "two-field plan: grad-grad, mass, full-tensor and advection terms only");
+      return FG_ERR_UNSUPPORTED;
+    }
     if (src.kind == FG_TERM_ELASTIC && plan->d.mult != 3) {
       setLastError("the elastic (Tensor4) term needs a 3-component compound field");
       return FG_ERR_UNSUPPORTED;
@@ -760,6 +844,8 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
       }
       out->nonSym = 1;
     }
+    // two-field plans: the full element-matrix kernel (FP64 path only)
+    if (plan->d.coupled) out->nonSym = 1;
     // the term's Jacobian modificator: terms with equal ones share a group
     const fg_jacmod &jm = src.jacmod;
     if (jm.kind < FG_JACMOD_NONE || jm.kind > FG_JACMOD_SPHERICAL_SHELL) {
@@ -852,6 +938,40 @@ int fg_plan_create(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_
     st = createPlan(mesh, rule, space, sys, plan);
   } catch (const std::bad_alloc &) {
     setLastError("fg_plan_create: host out of memory");
+    st = FG_ERR_OOM;
+  }
+  if (st != FG_OK) {
+    fg_plan_destroy(plan);
+    return st;
+  }
+  *out = plan;
+  return FG_OK;
+}
+
+int fg_plan_create_coupled(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_space_desc *space,
+                           const fg_system_desc *sys, const fg_space_desc *unknown_space, const uint64_t *unknown_dof_idx,
+                           const int32_t *unknown_dof_type, fg_plan **out) {
+  if (!out) return FG_ERR_ARG;
+  *out = nullptr;
+  if (!mesh || !rule || !space || !sys || !unknown_space || !unknown_dof_idx || !unknown_dof_type || !mesh->node_xyz ||
+      !mesh->elem_nodes || !rule->weights || !rule->geo_val || !rule->geo_grad || !space->basis_val || !space->basis_grad ||
+      !sys->ai || !sys->elem_dof_idx || !sys->elem_dof_type || (!sys->aj && sys->ai[sys->n_rows] != 0)) {
+    setLastError("fg_plan_create_coupled: null descriptor field");
+    return FG_ERR_ARG;
+  }
+  int dev = 0;
+  if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) {
+    cudaGetLastError();
+    setLastError("fg_plan_create_coupled: no CUDA device");
+    return FG_ERR_NO_DEVICE;
+  }
+  fg_plan *plan = new (std::nothrow) fg_plan;
+  if (!plan) return FG_ERR_OOM;
+  int st;
+  try {
+    st = createPlan(mesh, rule, space, sys, plan, unknown_space, unknown_dof_idx, unknown_dof_type);
+  } catch (const std::bad_alloc &) {
+    setLastError("fg_plan_create_coupled: host out of memory");
     st = FG_ERR_OOM;
   }
   if (st != FG_OK) {

@@ -18,9 +18,11 @@ HOST_LIB_PATH = os.path.join(HERE, "_build", "libfemg_host.so")
 FG_OK, FG_ERR_ARG, FG_ERR_OOM, FG_ERR_CUDA, FG_ERR_INDEX, FG_ERR_TIMEOUT, FG_ERR_UNSUPPORTED, FG_ERR_NO_DEVICE = range(8)
 (FG_TERM_GRAD_GRAD, FG_TERM_MASS, FG_TERM_ELASTIC, FG_TERM_SOURCE, FG_TERM_GRAD_GRAD_TENSOR, FG_TERM_MASS_TENSOR,
  FG_TERM_GRAD_GRAD_TENSOR_FULL, FG_TERM_ADVECTION) = range(8)
-FG_PROBLEM_HELMHOLTZ, FG_PROBLEM_NAVIER, FG_PROBLEM_MAXWELL = range(3)
+FG_PROBLEM_HELMHOLTZ, FG_PROBLEM_NAVIER, FG_PROBLEM_MAXWELL, FG_PROBLEM_COUPLED = range(4)
 FG_SPACE_LAGRANGE, FG_SPACE_HIERARCHICAL_H1, FG_SPACE_HCURL = range(3)
 FG_FORM_0, FG_FORM_1 = range(2)
+(FG_AT_UNDEFINED, FG_AT_FIXED, FG_AT_UNKNOWN, FG_AT_UNKNOWN_BUBBLE, FG_AT_UNKNOWN_GLOBAL, FG_AT_LINKED,
+ FG_AT_LINKED_BUBBLE) = range(7)
 FG_DT_NONE, FG_DT_1, FG_DT_2 = range(3)
 FG_JACMOD_NONE, FG_JACMOD_AXISYMMETRY, FG_JACMOD_AXISYMMETRY_SHELL, FG_JACMOD_POLAR_SHELL, FG_JACMOD_CYLINDRICAL_SHELL, \
     FG_JACMOD_SPHERICAL_SHELL = range(6)
@@ -90,7 +92,7 @@ class ProblemConfig(C.Structure):
                 ("space", C.c_int32), ("order", C.c_int32), ("gauss", C.c_int32), ("jitter", C.c_double),
                 ("seed", C.c_uint64), ("k", C.c_double), ("coef_mode", C.c_int32), ("dirichlet", C.c_int32),
                 ("dirichlet_value", C.c_double), ("source", C.c_int32), ("omega", C.c_double),
-                ("lame_sigma", C.c_double), ("upper", C.c_int32)]
+                ("lame_sigma", C.c_double), ("upper", C.c_int32), ("order2", C.c_int32)]
 
 
 _lib = None
@@ -124,6 +126,8 @@ def _bind(L):
     P = C.c_void_p
     sig = {
         "fg_plan_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(RuleDesc), C.POINTER(SpaceDesc), C.POINTER(SystemDesc), C.POINTER(P)]),
+        "fg_plan_create_coupled": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(RuleDesc), C.POINTER(SpaceDesc), C.POINTER(SystemDesc),
+                                             C.POINTER(SpaceDesc), P, P, C.POINTER(P)]),
         "fg_plan_destroy": (None, [P]),
         "fg_plan_info": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
         "fg_plan_bind_terms": (C.c_int, [P, C.POINTER(TermDesc), C.c_int32, C.c_double]),
@@ -159,6 +163,12 @@ def _bind(L):
         "fg_problem_bbox": (C.c_int, [P, P]),
         "fg_problem_reserve_log": (C.c_int64, [P, P, P, C.c_int64]),
         "fg_problem_pre_seconds": (C.c_double, [P]),
+        "fg_problem_n_fields": (C.c_int32, [P]),
+        "fg_problem_field": (C.c_int, [P, C.c_int32, C.POINTER(SpaceDesc), C.POINTER(C.POINTER(C.c_uint64)),
+                                       C.POINTER(C.POINTER(C.c_int32))]),
+        "fg_problem_n_blocks": (C.c_int32, [P]),
+        "fg_problem_block": (C.c_int, [P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.POINTER(TermDesc)),
+                                       C.POINTER(C.c_int32)]),
         "fg_problem_assemble": (C.c_int, [P, C.c_int32, P, P, P]),
     }
     for name, (res, args) in sig.items():
@@ -173,11 +183,12 @@ def _bind(L):
 def exported_symbols():
     """Names bound above (the C ABI of both headers)."""
     return [
-        "fg_plan_create", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_plan_set_fp64_method", "fg_plan_set_accumulate", "fg_plan_set_mixed_fused", "fg_plan_fused_info", "fg_assemble_fp64", "fg_assemble_mixed",
+        "fg_plan_create", "fg_plan_create_coupled", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_plan_set_fp64_method", "fg_plan_set_accumulate", "fg_plan_set_mixed_fused", "fg_plan_fused_info", "fg_assemble_fp64", "fg_assemble_mixed",
         "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_assemble_separate", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_pattern_build", "fg_hilbert_order", "fg_hilbert_numbering", "fg_profile_enable",
         "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
         "fg_problem_raw_dofs", "fg_problem_created_dofs", "fg_problem_reserve_log", "fg_problem_bbox", "fg_problem_pre_seconds", "fg_problem_assemble",
+        "fg_problem_n_fields", "fg_problem_field", "fg_problem_n_blocks", "fg_problem_block",
     ]
 
 
@@ -207,9 +218,10 @@ def _arr(ptr, count, dtype):
 
 
 def config(kind=FG_PROBLEM_HELMHOLTZ, dim=2, m=4, mesh_order=2, space=FG_SPACE_LAGRANGE, order=1, gauss=4, jitter=0.2,
-           seed=1, k=10.0, coef_mode=0, dirichlet=0, dirichlet_value=0.0, source=0, omega=1.0, lame_sigma=0.5, upper=0):
+           seed=1, k=10.0, coef_mode=0, dirichlet=0, dirichlet_value=0.0, source=0, omega=1.0, lame_sigma=0.5, upper=0,
+           order2=0):
     return ProblemConfig(kind, dim, m, mesh_order, space, order, gauss, jitter, seed, k, coef_mode, dirichlet,
-                         dirichlet_value, source, omega, lame_sigma, upper)
+                         dirichlet_value, source, omega, lame_sigma, upper, order2)
 
 
 # The benchmark workloads (seeded synthetic inputs with the shapes of the
@@ -366,15 +378,77 @@ class Problem:
     def plan(self):
         return Plan(self)
 
+    # --- several fields (FG_PROBLEM_COUPLED)
+    def n_fields(self):
+        return self._L.fg_problem_n_fields(self.ptr)
+
+    def field(self, k):
+        """(SpaceDesc, element DOF index [E][n], element DOF type [E][n]) of field k"""
+        sp = SpaceDesc()
+        ip, tp = C.POINTER(C.c_uint64)(), C.POINTER(C.c_int32)()
+        check(self._L.fg_problem_field(self.ptr, k, C.byref(sp), C.byref(ip), C.byref(tp)), self._L)
+        n = sp.n_basis * sp.multiplicity
+        E = self.mesh.n_elements
+        return sp, _arr(ip, n * E, np.uint64).reshape(E, n), _arr(tp, n * E, np.int32).reshape(E, n)
+
+    def field_arrays(self, k):
+        """arrays() with the space and element DOF map of field k"""
+        a = self.arrays()
+        sp, idx, typ = self.field(k)
+        nq, no, nb, E = self.rule.nq, sp.n_orientations, sp.n_basis, self.mesh.n_elements
+        a.update(nb=nb, mult=sp.multiplicity, n_orient=no, form=sp.form,
+                 bval=_arr(sp.basis_val, no * nq * nb, np.float64).reshape(no, nq, nb),
+                 bgrad=_arr(sp.basis_grad, no * nq * nb * 3, np.float64).reshape(no, nq, nb, 3),
+                 orient=(_arr(sp.elem_orientation, E, np.int32) if no > 1 else np.zeros(E, np.int32)),
+                 edof=idx, etype=typ)
+        return a
+
+    def blocks(self):
+        """[(test field, unknown field, terms pointer, term count)]"""
+        out = []
+        for b in range(self._L.fg_problem_n_blocks(self.ptr)):
+            t, u = C.c_int32(), C.c_int32()
+            tp, nt = C.POINTER(TermDesc)(), C.c_int32()
+            check(self._L.fg_problem_block(self.ptr, b, C.byref(t), C.byref(u), C.byref(tp), C.byref(nt)), self._L)
+            out.append((t.value, u.value, tp, nt.value))
+        return out
+
+    def block_plan(self, test, unknown):
+        """A plan for the block (test field, unknown field): fg_plan_create
+        for test == unknown, fg_plan_create_coupled otherwise; accumulating
+        when the problem has several blocks."""
+        return Plan(self, test=test, unknown=unknown)
+
 
 class Plan:
-    """fg_plan over a Problem's descriptors (through the C ABI)."""
+    """fg_plan over a Problem's descriptors (through the C ABI). test,
+    unknown: the fields of a block of a multi-field problem (None: the
+    problem's first block)."""
 
-    def __init__(self, prob):
+    def __init__(self, prob, test=None, unknown=None):
         L = lib()
         self.prob = prob
         self.ptr = C.c_void_p()
-        check(L.fg_plan_create(C.byref(prob.mesh), C.byref(prob.rule), C.byref(prob.space), C.byref(prob.sys), C.byref(self.ptr)))
+        if test is None:
+            check(L.fg_plan_create(C.byref(prob.mesh), C.byref(prob.rule), C.byref(prob.space), C.byref(prob.sys),
+                                   C.byref(self.ptr)))
+            return
+        spT, idxT, typT = prob.field(test)
+        sys = SystemDesc()
+        C.memmove(C.byref(sys), C.byref(prob.sys), C.sizeof(SystemDesc))
+        self._keep = (spT, idxT, typT)
+        sys.elem_dof_idx = idxT.ctypes.data_as(C.POINTER(C.c_uint64))
+        sys.elem_dof_type = typT.ctypes.data_as(C.POINTER(C.c_int32))
+        self.sys = sys
+        if test == unknown:
+            check(L.fg_plan_create(C.byref(prob.mesh), C.byref(prob.rule), C.byref(spT), C.byref(sys), C.byref(self.ptr)))
+        else:
+            spU, idxU, typU = prob.field(unknown)
+            self._keep = self._keep + (spU, idxU, typU)
+            check(L.fg_plan_create_coupled(C.byref(prob.mesh), C.byref(prob.rule), C.byref(spT), C.byref(sys), C.byref(spU),
+                                           idxU.ctypes.data, typU.ctypes.data, C.byref(self.ptr)))
+        if len(prob.blocks()) > 1:
+            self.set_accumulate(True)
 
     def close(self):
         if self.ptr:

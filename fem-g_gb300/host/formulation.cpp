@@ -392,6 +392,12 @@ Operand operator*(const TensorFunction &D, Operand o) {
   return o;
 }
 
+Operand operator*(const VectorFunction &b, Operand o) {
+  o.vec = true;
+  o.b = b;
+  return o;
+}
+
 // ----------------------------------------------------------- Formulation
 
 void Formulation::integral(const Operand &unknown, const Operand &test, const Domain &d, const std::string &gauss) {
@@ -424,87 +430,164 @@ void Formulation::fillIndices(const Field &f, const ElementBlock &blk, std::vect
     }
 }
 
+fg_term_desc Formulation::describe(const BTerm &t) {
+  fg_term_desc d;
+  std::memset(&d, 0, sizeof(d));
+  if (!t.test.coef.isConstant() || t.test.coef.constantValue() != cplx(1.0, 0.0))
+    throw std::invalid_argument("coefficients on the test function are not supported");
+  d.dt = t.unknown.dt;
+  if (t.unknown.vec) {
+    // b . grad(dof(u)) tested against tf(v): the advection term
+    if (!t.unknown.grad || t.test.grad) throw std::invalid_argument("a vector function multiplies grad(dof(u)), tested by tf(v)");
+    const VectorFunction &b = t.unknown.b;
+    d.kind = FG_TERM_ADVECTION;
+    d.coef = t.unknown.coef.toExpr();
+    tensorExprs.push_back({b.x.toExpr(), b.y.toExpr(), b.z.toExpr()});
+    d.tensor = tensorExprs.back().data();
+    return d;
+  }
+  if (t.unknown.grad != t.test.grad) throw std::invalid_argument("mixed value/gradient terms are not supported");
+  if (t.unknown.tensor4) {
+    if (!t.unknown.grad) throw std::invalid_argument("Tensor4 needs gradients");
+    d.kind = FG_TERM_ELASTIC;
+    d.coef = (t.unknown.coef * t.unknown.C.lambda).toExpr();
+    d.coef2 = (t.unknown.coef * t.unknown.C.mu).toExpr();
+  } else if (t.unknown.tensor2) {
+    // D * grad (H1), D * curl (HCurl) or D * dof (HCurl values)
+    if (!t.unknown.grad && t.unknown.field->fs.form() != 1)
+      throw std::invalid_argument("a tensor function multiplies gradients, curls or HCurl values");
+    const TensorFunction &D = t.unknown.D;
+    d.kind = t.unknown.grad ? FG_TERM_GRAD_GRAD_TENSOR : FG_TERM_MASS_TENSOR;
+    d.coef = t.unknown.coef.toExpr();
+    tensorExprs.push_back({D.xx.toExpr(), D.yy.toExpr(), D.zz.toExpr(), D.xy.toExpr(), D.xz.toExpr(), D.yz.toExpr()});
+    d.tensor = tensorExprs.back().data();
+  } else {
+    d.kind = t.unknown.grad ? FG_TERM_GRAD_GRAD : FG_TERM_MASS;
+    d.coef = t.unknown.coef.toExpr();
+  }
+  return d;
+}
+
 void Formulation::pre(const Mesh &m) {
   auto t0 = std::chrono::steady_clock::now();
   mesh = &m;
   if (bterms_.empty()) throw std::invalid_argument("no bilinear term");
-  field = bterms_[0].unknown.field;
+  // the unknown fields: Formulation::_addField on each bilinear term's
+  // unknown field (src/problem/Formulation.cpp:149-159, :219-300)
+  fields.clear();
   for (auto &t : bterms_)
-    if (t.unknown.field != field || t.test.field != field) throw std::invalid_argument("one field per formulation in this mirror");
-  for (auto &t : lterms_)
-    if (t.test.field != field) throw std::invalid_argument("one field per formulation in this mirror");
-  Field &f = *field;
+    if (std::find(fields.begin(), fields.end(), t.unknown.field) == fields.end()) fields.push_back(t.unknown.field);
+  if (fields.size() > 2)
+    throw std::invalid_argument(
+        "at most two fields: the reference numbers the DOFs of its fields in the iteration order of an unordered_set of "
+        "field pointers (DofsManager::_fields), which with three or more depends on the fields' addresses");
+  auto fieldIndex = [&](const Field *f) -> int {
+    for (size_t k = 0; k < fields.size(); ++k)
+      if (fields[k] == f) return (int)k;
+    throw std::invalid_argument("a test field that is the unknown of no bilinear term has no DOFs");
+  };
+  for (auto &t : bterms_) fieldIndex(t.test.field);
+  for (auto &t : lterms_) fieldIndex(t.test.field);
+  field = fields[0];
+  for (Field *fp : fields)
+    if (fields.size() > 1 && (fp->multiplicity != 1 || fp->fs.form() != 0))
+      throw std::invalid_argument("several fields: scalar H1 fields only in this mirror");
 
-  // ---- DofsFactory::generate: fixed DOFs, then unknown DOFs
-  const int maxDim = f.domain.maxDim();
+  // ---- DofsFactory::generate (src/dofs/DofsFactory.cpp:725-839): the fixed
+  // DOFs of every field, then the unknown DOFs of every field, numbered by
+  // counters shared across the fields; maxDim over all fields' domains
+  int maxDim = 0;
+  for (Field *fp : fields) maxDim = std::max(maxDim, fp->domain.maxDim());
   nFixed = nUnknown = nBubble = 0;
-  f.dofs = DofDictionary();
-  f.fixedValues.clear();
   reserveLog.clear();
+  created.clear();
+  for (Field *fp : fields) {
+    fp->dofs = DofDictionary();
+    fp->fixedValues.clear();
+  }
+  std::vector<cplx> fixedAll;
+  // DofsManager::addField order (a field enters on each of its constraints,
+  // and every field once its unknown DOFs are made)
+  std::vector<Field *> registered;
+  auto registerField = [&](Field *f) {
+    if (std::find(registered.begin(), registered.end(), f) == registered.end()) registered.push_back(f);
+  };
   std::vector<int> typeKeys, info;
   std::vector<uint64_t> entityKeys;
   std::vector<double> coord;
-  for (auto &c : f.constraints) {
-    if (!f.fs.orientationFree() || f.multiplicity != 1)
-      throw std::invalid_argument("constraints need a Lagrange / order-1 scalar field in this mirror");
-    for (auto &de : c.domain.entities) {
-      const Entity *ent = m.find(de.first, de.second);
-      if (!ent) continue;
-      for (auto &blk : ent->blocks) {
-        f.fs.getKeys(m, blk, true, typeKeys, entityKeys, coord, nullptr);
-        reserveLog.push_back({f.dofs.size(), f.dofs.size() + typeKeys.size()});
-        f.dofs.reserve(f.dofs.size() + typeKeys.size());
-        for (size_t j = 0; j < typeKeys.size(); ++j) {
-          Dof d;
-          d.numType = (uint64_t)typeKeys[j] + kDofFieldOffset * f.tag;
-          d.entity = entityKeys[j];
-          d.assembleType = kAtFixed;
-          for (int k = 0; k < 3; ++k) d.xyz[k] = (float)coord[3 * j + k];
-          d.numDof = nFixed + 1;
-          if (f.dofs.insert(d)) {
-            ++nFixed;
-            f.fixedValues.push_back(c.value);
+  for (Field *fp : fields) {
+    Field &f = *fp;
+    for (auto &c : f.constraints) {
+      if (!f.fs.orientationFree() || f.multiplicity != 1)
+        throw std::invalid_argument("constraints need a Lagrange / order-1 scalar field in this mirror");
+      for (auto &de : c.domain.entities) {
+        const Entity *ent = m.find(de.first, de.second);
+        if (!ent) continue;
+        for (auto &blk : ent->blocks) {
+          f.fs.getKeys(m, blk, true, typeKeys, entityKeys, coord, nullptr);
+          reserveLog.push_back({f.dofs.size(), f.dofs.size() + typeKeys.size()});
+          f.dofs.reserve(f.dofs.size() + typeKeys.size());
+          for (size_t j = 0; j < typeKeys.size(); ++j) {
+            Dof d;
+            d.numType = (uint64_t)typeKeys[j] + kDofFieldOffset * f.tag;
+            d.entity = entityKeys[j];
+            d.assembleType = kAtFixed;
+            for (int k = 0; k < 3; ++k) d.xyz[k] = (float)coord[3 * j + k];
+            d.numDof = nFixed + 1;
+            if (f.dofs.insert(d)) {
+              ++nFixed;
+              f.fixedValues.push_back(c.value);
+              fixedAll.push_back(c.value);
+              created.push_back(d);
+            }
           }
         }
       }
+      registerField(fp);
     }
   }
-  for (auto &de : f.domain.entities) {
-    const Entity *ent = m.find(de.first, de.second);
-    if (!ent) continue;
-    for (auto &blk : ent->blocks) {
-      const bool top = de.first == maxDim;
-      f.fs.getKeys(m, blk, true, typeKeys, entityKeys, coord, top ? &info : nullptr);
-      reserveLog.push_back({f.dofs.size(), f.dofs.size() + typeKeys.size() * f.multiplicity});
-      f.dofs.reserve(f.dofs.size() + typeKeys.size() * f.multiplicity);
-      for (size_t j = 0; j < typeKeys.size(); ++j)
-        for (int k = 0; k < f.multiplicity; ++k) {
-          const bool bubble = top && info[j] == maxDim;
-          Dof d;
-          d.numType = (uint64_t)typeKeys[j] + kDofFieldOffset * (f.tag + k);
-          d.entity = entityKeys[j];
-          d.assembleType = bubble ? kAtUnknownBubble : kAtUnknown;
-          for (int c = 0; c < 3; ++c) d.xyz[c] = (float)coord[3 * j + c];
-          d.numDof = nUnknown + 1;
-          if (f.dofs.insert(d)) {
-            ++nUnknown;
-            if (bubble) ++nBubble;
+  for (Field *fp : fields) {
+    Field &f = *fp;
+    for (auto &de : f.domain.entities) {
+      const Entity *ent = m.find(de.first, de.second);
+      if (!ent) continue;
+      for (auto &blk : ent->blocks) {
+        const bool top = de.first == maxDim;
+        f.fs.getKeys(m, blk, true, typeKeys, entityKeys, coord, top ? &info : nullptr);
+        reserveLog.push_back({f.dofs.size(), f.dofs.size() + typeKeys.size() * f.multiplicity});
+        f.dofs.reserve(f.dofs.size() + typeKeys.size() * f.multiplicity);
+        for (size_t j = 0; j < typeKeys.size(); ++j)
+          for (int k = 0; k < f.multiplicity; ++k) {
+            const bool bubble = top && info[j] == maxDim;
+            Dof d;
+            d.numType = (uint64_t)typeKeys[j] + kDofFieldOffset * (f.tag + k);
+            d.entity = entityKeys[j];
+            d.assembleType = bubble ? kAtUnknownBubble : kAtUnknown;
+            for (int c = 0; c < 3; ++c) d.xyz[c] = (float)coord[3 * j + c];
+            d.numDof = nUnknown + 1;
+            if (f.dofs.insert(d)) {
+              ++nUnknown;
+              if (bubble) ++nBubble;
+              created.push_back(d);
+            }
           }
-        }
+      }
     }
+    registerField(fp);
   }
-  created = f.dofs.pool;
 
-  // ---- DofsManager::reorderWithHilbert(true)
+  // ---- DofsManager::reorderWithHilbert(true) over the fields of
+  // DofsManager::_fields, a std::unordered_set of field pointers
+  // (src/dofs/DofsManager.h:47, DofsManager.cpp:137-151): with one or two
+  // elements libstdc++ keeps them in one bucket chain (even addresses, two
+  // buckets) and iterates the later insertion first
   if (m.dim == 2 || m.dim == 3) {
-    std::vector<DofDictionary *> fields = {&f.dofs};
-    reorderWithHilbert(m.dim, m.bbox, fields, nUnknown, nBubble);
+    std::vector<DofDictionary *> dicts;
+    for (auto it = registered.rbegin(); it != registered.rend(); ++it) dicts.push_back(&(*it)->dofs);
+    reorderWithHilbert(m.dim, m.bbox, dicts, nUnknown, nBubble);
   }
 
-  // ---- pattern over the entities carrying bilinear terms
-  PatternBuilder pb;
-  pb.init(nUnknown);
-  pb.symmetric = symmetric_;
+  // ---- the element bucket (one) and every field's element DOF map on it
   bucket = nullptr;
   for (auto &ent : m.entities) {
     bool have = false;
@@ -513,15 +596,30 @@ void Formulation::pre(const Mesh &m) {
     for (auto &blk : ent.blocks) {
       if (bucket) throw std::invalid_argument("this mirror assembles a single element bucket");
       bucket = &blk;
-      fillIndices(f, blk, elemDofIdx, elemDofType);
-      const int n = (int)(elemDofIdx.size() / blk.size());
-      pb.addElements(blk.size(), n, n, elemDofIdx.data(), elemDofType.data(), elemDofIdx.data(), elemDofType.data());
     }
   }
   if (!bucket) throw std::invalid_argument("no element carries a bilinear term");
+  fieldBuckets.assign(fields.size(), FieldBucket());
+  for (size_t k = 0; k < fields.size(); ++k)
+    fillIndices(*fields[k], *bucket, fieldBuckets[k].elemDofIdx, fieldBuckets[k].elemDofType);
+
+  // ---- pattern: MatrixFactory::addPattern per bilinear term
+  // (src/term/Pattern.cpp:69): rows the test field's DOFs, columns the
+  // unknown field's
+  PatternBuilder pb;
+  pb.init(nUnknown);
+  pb.symmetric = symmetric_;
+  const int64_t E = (int64_t)bucket->size();
+  for (auto &t : bterms_) {
+    const FieldBucket &ft = fieldBuckets[(size_t)fieldIndex(t.test.field)];
+    const FieldBucket &fu = fieldBuckets[(size_t)fieldIndex(t.unknown.field)];
+    const int nt = (int)(ft.elemDofIdx.size() / std::max<int64_t>(E, 1));
+    const int nu = (int)(fu.elemDofIdx.size() / std::max<int64_t>(E, 1));
+    pb.addElements(E, nt, nu, ft.elemDofIdx.data(), ft.elemDofType.data(), fu.elemDofIdx.data(), fu.elemDofType.data());
+  }
   pb.finalize(ai, aj);
 
-  // ---- element bucket data (Assembler::assemblyInitialization)
+  // ---- bucket data (Assembler::assemblyInitialization)
   std::string gauss = bterms_[0].gauss;
   for (auto &t : bterms_)
     if (t.gauss != gauss) throw std::invalid_argument("one integration type per formulation in this mirror");
@@ -532,46 +630,31 @@ void Formulation::pre(const Mesh &m) {
   geoVal.assign((size_t)rule.nq * nn, 0.0);
   geoGrad.assign((size_t)rule.nq * nn * 3, 0.0);
   for (int q = 0; q < rule.nq; ++q) lagrangeBasis(bucket->type, &rule.points[3 * q], &geoVal[(size_t)q * nn], &geoGrad[(size_t)q * nn * 3]);
-  int no1 = 1, no2 = 1;
-  std::vector<int32_t> o2;
-  nBasis = f.fs.basisFunctions(false, m, *bucket, rule, basisVal, orient, no1);
-  f.fs.basisFunctions(true, m, *bucket, rule, basisGrad, o2, no2);
-  nOrient = no1;
+  for (size_t k = 0; k < fields.size(); ++k) {
+    FieldBucket &fb = fieldBuckets[k];
+    int no2 = 1;
+    std::vector<int32_t> o2;
+    fb.nBasis = fields[k]->fs.basisFunctions(false, m, *bucket, rule, fb.basisVal, fb.orient, fb.nOrient);
+    fields[k]->fs.basisFunctions(true, m, *bucket, rule, fb.basisGrad, o2, no2);
+  }
   dirichlet.assign(2 * nFixed, 0.0);
   for (uint64_t i = 0; i < nFixed; ++i) {
-    dirichlet[2 * i] = f.fixedValues[i].real();
-    dirichlet[2 * i + 1] = f.fixedValues[i].imag();
+    dirichlet[2 * i] = fixedAll[i].real();
+    dirichlet[2 * i + 1] = fixedAll[i].imag();
   }
 
-  // ---- terms for the C ABI
-  termDescs.clear();
+  // ---- terms for the C ABI, by (test field, unknown field)
+  blocks.clear();
   tensorExprs.clear();
+  auto blockOf = [&](int test, int unknown) -> Block & {
+    for (auto &b : blocks)
+      if (b.test == test && b.unknown == unknown) return b;
+    blocks.push_back(Block{test, unknown, {}});
+    return blocks.back();
+  };
   for (auto &t : bterms_) {
-    fg_term_desc d;
-    std::memset(&d, 0, sizeof(d));
-    if (!t.test.coef.isConstant() || t.test.coef.constantValue() != cplx(1.0, 0.0))
-      throw std::invalid_argument("coefficients on the test function are not supported");
-    if (t.unknown.grad != t.test.grad) throw std::invalid_argument("mixed value/gradient terms are not supported");
-    d.dt = t.unknown.dt;
-    if (t.unknown.tensor4) {
-      if (!t.unknown.grad) throw std::invalid_argument("Tensor4 needs gradients");
-      d.kind = FG_TERM_ELASTIC;
-      d.coef = (t.unknown.coef * t.unknown.C.lambda).toExpr();
-      d.coef2 = (t.unknown.coef * t.unknown.C.mu).toExpr();
-    } else if (t.unknown.tensor2) {
-      // D * grad (H1), D * curl (HCurl) or D * dof (HCurl values)
-      if (!t.unknown.grad && t.unknown.field->fs.form() != 1)
-        throw std::invalid_argument("a tensor function multiplies gradients, curls or HCurl values");
-      const TensorFunction &D = t.unknown.D;
-      d.kind = t.unknown.grad ? FG_TERM_GRAD_GRAD_TENSOR : FG_TERM_MASS_TENSOR;
-      d.coef = t.unknown.coef.toExpr();
-      tensorExprs.push_back({D.xx.toExpr(), D.yy.toExpr(), D.zz.toExpr(), D.xy.toExpr(), D.xz.toExpr(), D.yz.toExpr()});
-      d.tensor = tensorExprs.back().data();
-    } else {
-      d.kind = t.unknown.grad ? FG_TERM_GRAD_GRAD : FG_TERM_MASS;
-      d.coef = t.unknown.coef.toExpr();
-    }
-    termDescs.push_back(d);
+    const fg_term_desc d = describe(t);
+    blockOf(fieldIndex(t.test.field), fieldIndex(t.unknown.field)).terms.push_back(d);
   }
   for (auto &t : lterms_) {
     fg_term_desc d;
@@ -579,9 +662,22 @@ void Formulation::pre(const Mesh &m) {
     if (t.test.grad) throw std::invalid_argument("gradient test functions in linear terms are not supported");
     d.kind = FG_TERM_SOURCE;
     d.coef = t.f.toExpr();
-    termDescs.push_back(d);
+    const int k = fieldIndex(t.test.field);
+    blockOf(k, k).terms.push_back(d);
   }
+  termDescs = blocks[0].terms;
   preSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void Formulation::spaceDesc(int k, fg_space_desc *sd) const {
+  const FieldBucket &fb = fieldBuckets[(size_t)k];
+  sd->n_basis = fb.nBasis;
+  sd->multiplicity = fields[(size_t)k]->multiplicity;
+  sd->n_orientations = fb.nOrient;
+  sd->basis_val = fb.basisVal.data();
+  sd->basis_grad = fb.basisGrad.data();
+  sd->elem_orientation = fb.nOrient > 1 ? fb.orient.data() : nullptr;
+  sd->form = fields[(size_t)k]->fs.form();
 }
 
 void Formulation::descs(fg_mesh_desc *md, fg_rule_desc *rd, fg_space_desc *sd, fg_system_desc *sys) const {
@@ -595,18 +691,13 @@ void Formulation::descs(fg_mesh_desc *md, fg_rule_desc *rd, fg_space_desc *sd, f
   rd->weights = rule.weights.data();
   rd->geo_val = geoVal.data();
   rd->geo_grad = geoGrad.data();
-  sd->n_basis = nBasis;
-  sd->multiplicity = field->multiplicity;
-  sd->n_orientations = nOrient;
-  sd->basis_val = basisVal.data();
-  sd->basis_grad = basisGrad.data();
-  sd->elem_orientation = nOrient > 1 ? orient.data() : nullptr;
-  sd->form = field->fs.form();
+  const int rows = blocks.empty() ? 0 : blocks[0].test;
+  spaceDesc(rows, sd);
   sys->n_rows = nUnknown;
   sys->ai = ai.data();
   sys->aj = aj.data();
-  sys->elem_dof_idx = elemDofIdx.data();
-  sys->elem_dof_type = elemDofType.data();
+  sys->elem_dof_idx = fieldBuckets[(size_t)rows].elemDofIdx.data();
+  sys->elem_dof_type = fieldBuckets[(size_t)rows].elemDofType.data();
   sys->n_fixed = nFixed;
   sys->upper = symmetric_ ? 1 : 0;
   sys->n_linked = 0;

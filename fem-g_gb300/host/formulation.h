@@ -153,6 +153,13 @@ class Field {
   std::vector<cplx> fixedValues;  // by fixed numDof - 1
 };
 
+// Vector of coefficient functions (the reference's VectorFunction,
+// src/function/VectorFunction.h) multiplying the gradient of the unknown in
+// integral(b * grad(dof(u)), tf(v)): the advection term
+struct VectorFunction {
+  Function x = Function(0.0), y = Function(0.0), z = Function(0.0);
+};
+
 struct Operand {
   Field *field = nullptr;
   bool grad = false;
@@ -163,6 +170,8 @@ struct Operand {
   Tensor4Isotropic C;
   bool tensor2 = false;  // D * grad(...) with a TensorFunction D
   TensorFunction D;
+  bool vec = false;      // b * grad(dof(u)) with a VectorFunction b
+  VectorFunction b;
 };
 Operand dof(Field &f);
 Operand tf(Field &f);
@@ -173,6 +182,7 @@ Operand curl(Operand o);  // the derivative of an HCurl field
 Operand operator*(const Function &c, Operand o);
 Operand operator*(const Tensor4Isotropic &C, Operand o);
 Operand operator*(const TensorFunction &D, Operand o);
+Operand operator*(const VectorFunction &b, Operand o);
 
 class Formulation {
  public:
@@ -191,25 +201,42 @@ class Formulation {
   // results of pre()
   uint64_t nUnknown = 0, nBubble = 0, nFixed = 0;
   std::vector<uint64_t> ai, aj;
+  // the unknown fields in the reference's registration order
+  // (Formulation::_addField, src/problem/Formulation.cpp:149-159: the unknown
+  // field of each bilinear term, by first appearance); field = fields[0]
+  std::vector<Field *> fields;
   Field *field = nullptr;
   const Mesh *mesh = nullptr;
   const ElementBlock *bucket = nullptr;
   QuadRule rule;
   std::vector<double> geoVal, geoGrad;    // [nq][nn], [nq][nn][3]
-  std::vector<double> basisVal, basisGrad;
-  std::vector<int32_t> orient;
-  int nBasis = 0, nOrient = 1;
-  std::vector<uint64_t> elemDofIdx;
-  std::vector<int32_t> elemDofType;
-  std::vector<double> dirichlet;          // [nFixed][2]
-  std::vector<fg_term_desc> termDescs;    // C ABI terms
-  std::deque<std::array<fg_expr, 6>> tensorExprs;  // entries of the tensor terms' D (stable addresses)
+  // per field: its basis on the bucket and its element DOF map (fillIndices)
+  struct FieldBucket {
+    std::vector<double> basisVal, basisGrad;
+    std::vector<int32_t> orient;
+    int nBasis = 0, nOrient = 1;
+    std::vector<uint64_t> elemDofIdx;
+    std::vector<int32_t> elemDofType;
+  };
+  std::vector<FieldBucket> fieldBuckets;
+  std::vector<double> dirichlet;          // [nFixed][2], every field's fixed DOFs
+  // the terms by (test field, unknown field), in order of first appearance;
+  // linear terms join the block (k, k) of their test field k
+  struct Block {
+    int test = 0, unknown = 0;
+    std::vector<fg_term_desc> terms;
+  };
+  std::vector<Block> blocks;
+  std::vector<fg_term_desc> termDescs;    // the terms of blocks[0] (the whole formulation with one field)
+  std::deque<std::array<fg_expr, 9>> tensorExprs;  // entries of the tensor / vector terms (stable addresses)
   // reserve calls on the DOF dictionary: (DOFs created before the call, argument)
   std::vector<std::pair<uint64_t, uint64_t>> reserveLog;
   double preSeconds = 0.0;
 
-  // C ABI descriptors over the data above
+  // C ABI descriptors over the data above (field 0 / the rows of blocks[0])
   void descs(fg_mesh_desc *m, fg_rule_desc *r, fg_space_desc *s, fg_system_desc *sys) const;
+  // the space of field k on the bucket
+  void spaceDesc(int k, fg_space_desc *s) const;
 
   // created DOFs in creation order (before numbering), for numbering checks
   std::vector<Dof> created;
@@ -231,6 +258,7 @@ class Formulation {
   std::vector<BTerm> bterms_;
   std::vector<LTerm> lterms_;
   void fillIndices(const Field &f, const ElementBlock &blk, std::vector<uint64_t> &idx, std::vector<int32_t> &type) const;
+  fg_term_desc describe(const BTerm &t);
 };
 
 }  // namespace femg

@@ -2,10 +2,18 @@
 // and the assembly through the C ABI of include/fem_g_gb300.h.
 #include "problem_internal.h"
 
+namespace femg {
+void setLastError(const std::string &msg);
+}
+
 extern "C" {
 
 int fg_problem_assemble(fg_problem *p, int32_t precision, double *csr_values, double *rhs, void *stream) {
   if (!p) return FG_ERR_ARG;
+  if (p->form->blocks.size() != 1) {
+    femg::setLastError("fg_problem_assemble: a problem of several fields assembles block by block (fg_problem_block)");
+    return FG_ERR_UNSUPPORTED;
+  }
   fg_mesh_desc m;
   fg_rule_desc r;
   fg_space_desc s;

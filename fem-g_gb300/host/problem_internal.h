@@ -8,7 +8,7 @@
 struct fg_problem {
   fg_problem_config cfg;
   femg::Mesh mesh;
-  std::unique_ptr<femg::Field> u;
+  std::unique_ptr<femg::Field> u, v;  // v: the second field of FG_PROBLEM_COUPLED
   std::unique_ptr<femg::Formulation> form;
   // GPU plan of fg_problem_assemble, created on first use; destroyed through
   // the hook set with it (the host-only library never creates one)

@@ -36,6 +36,37 @@ static void buildProblem(fg_problem *p) {
                                                     : SpaceType::HierarchicalH1;
   if ((c.kind == FG_PROBLEM_MAXWELL) != (st == SpaceType::HCurl))
     throw std::invalid_argument("the Maxwell problem takes the HCurl space, and only it does");
+  if (c.kind == FG_PROBLEM_COUPLED) {
+    // two scalar fields (tags 0 and 1, the reference's field counter),
+    // coupled both ways
+    p->u.reset(new Field("u", omega, st, c.order, 1, 0));
+    p->v.reset(new Field("v", omega, st, c.order2 > 0 ? c.order2 : c.order, 1, 1));
+    Field &u = *p->u, &v = *p->v;
+    p->form.reset(new Formulation("coupled"));
+    p->form->setSymmetric(c.upper != 0);
+    Formulation &f = *p->form;
+    const std::string gauss = "Gauss" + std::to_string(c.gauss);
+    if (c.dirichlet) {
+      if (c.dim != 2) throw std::invalid_argument("Dirichlet boundary only on the 2D square");
+      u.addConstraint(Domain(p->mesh, "gammaDir"), cplx(c.dirichlet_value, 0.0));
+    }
+    Function x = Function::x(), y = Function::y();
+    f.integral(grad(dof(u)), grad(tf(u)), omega, gauss);
+    f.integral(Function(-c.k * c.k) * dof(u), tf(u), omega, gauss);
+    f.integral(grad(dof(v)), grad(tf(v)), omega, gauss);
+    f.integral(Function(2.0) * dof(v), tf(v), omega, gauss);
+    f.integral((Function(0.5) + x) * dof(u), tf(v), omega, gauss);
+    VectorFunction b{Function(1.0), Function(cplx(-0.5, 0.2)), Function(0.25)};
+    f.integral(b * grad(dof(u)), tf(v), omega, gauss);
+    f.integral(Function(0.3) * grad(dof(v)), grad(tf(u)), omega, gauss);
+    if (c.source) {
+      Function fsrc = heaviside(Function(0.01) - (x - Function(0.5)) * (x - Function(0.5)) - (y - Function(0.5)) * (y - Function(0.5)));
+      f.integral(-fsrc, tf(u), omega, gauss);
+      f.integral(Function(1.0) + x * y, tf(v), omega, gauss);
+    }
+    f.pre(p->mesh);
+    return;
+  }
   const int mult = c.kind == FG_PROBLEM_NAVIER ? 3 : 1;
   p->u.reset(new Field("u", omega, st, c.order, mult, 0));
   Field &u = *p->u;
@@ -142,22 +173,53 @@ int fg_problem_descs(const fg_problem *p, fg_mesh_desc *mesh, fg_rule_desc *rule
   return FG_OK;
 }
 
-int64_t fg_problem_n_dofs(const fg_problem *p) { return p ? (int64_t)p->u->dofs.size() : -1; }
+int64_t fg_problem_n_dofs(const fg_problem *p) {
+  if (!p) return -1;
+  int64_t n = 0;
+  for (const Field *f : p->form->fields) n += (int64_t)f->dofs.size();
+  return n;
+}
 
 int fg_problem_raw_dofs(const fg_problem *p, uint64_t *num_type, uint64_t *entity, uint64_t *num_dof, int32_t *assemble_type, float *xyz) {
   if (!p) return FG_ERR_ARG;
-  const auto &dd = p->u->dofs;
   size_t i = 0;
-  for (uint32_t id : dd.table.order()) {
-    const Dof &d = dd.pool[id];
-    if (num_type) num_type[i] = d.numType;
-    if (entity) entity[i] = d.entity;
-    if (num_dof) num_dof[i] = d.numDof;
-    if (assemble_type) assemble_type[i] = d.assembleType;
-    if (xyz)
-      for (int c = 0; c < 3; ++c) xyz[3 * i + c] = d.xyz[c];
-    ++i;
+  for (const Field *f : p->form->fields) {
+    const auto &dd = f->dofs;
+    for (uint32_t id : dd.table.order()) {
+      const Dof &d = dd.pool[id];
+      if (num_type) num_type[i] = d.numType;
+      if (entity) entity[i] = d.entity;
+      if (num_dof) num_dof[i] = d.numDof;
+      if (assemble_type) assemble_type[i] = d.assembleType;
+      if (xyz)
+        for (int c = 0; c < 3; ++c) xyz[3 * i + c] = d.xyz[c];
+      ++i;
+    }
   }
+  return FG_OK;
+}
+
+int32_t fg_problem_n_fields(const fg_problem *p) { return p ? (int32_t)p->form->fields.size() : -1; }
+
+int fg_problem_field(const fg_problem *p, int32_t k, fg_space_desc *space, const uint64_t **elem_dof_idx,
+                     const int32_t **elem_dof_type) {
+  if (!p || k < 0 || k >= (int32_t)p->form->fields.size()) return FG_ERR_ARG;
+  if (space) p->form->spaceDesc(k, space);
+  if (elem_dof_idx) *elem_dof_idx = p->form->fieldBuckets[(size_t)k].elemDofIdx.data();
+  if (elem_dof_type) *elem_dof_type = p->form->fieldBuckets[(size_t)k].elemDofType.data();
+  return FG_OK;
+}
+
+int32_t fg_problem_n_blocks(const fg_problem *p) { return p ? (int32_t)p->form->blocks.size() : -1; }
+
+int fg_problem_block(const fg_problem *p, int32_t b, int32_t *test_field, int32_t *unknown_field, const fg_term_desc **terms,
+                     int32_t *n_terms) {
+  if (!p || b < 0 || b >= (int32_t)p->form->blocks.size()) return FG_ERR_ARG;
+  const auto &bl = p->form->blocks[(size_t)b];
+  if (test_field) *test_field = bl.test;
+  if (unknown_field) *unknown_field = bl.unknown;
+  if (terms) *terms = bl.terms.data();
+  if (n_terms) *n_terms = (int32_t)bl.terms.size();
   return FG_OK;
 }
 

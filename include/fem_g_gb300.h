@@ -248,6 +248,29 @@ typedef struct fg_plan fg_plan;
  * the element->nonzero map used by the deterministic CSR reduction. */
 int fg_plan_create(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_space_desc *space,
                    const fg_system_desc *sys, fg_plan **out);
+/* Plan for the terms of one bucket whose unknown field differs from their
+ * test field (a BilinearTerm with _field[0] != _field[1],
+ * src/term/BilinearTerm.cpp:156-273, scattered by MatrixFactory::addValues
+ * with the test field's indices as rows and the unknown field's as columns,
+ * src/term/Assembler.cpp:256). `space` and sys->elem_dof_idx / elem_dof_type
+ * describe the TEST field (the rows); `unknown_space` and unknown_dof_idx /
+ * unknown_dof_type ([n_elements][unknown n_basis], numDof - 1 and FG_AT_*)
+ * the unknown field (the columns); ai/aj is the formulation's shared pattern.
+ * Both fields scalar H1 (FG_FORM_0, multiplicity 1) on the same elements and
+ * rule; no linked DOFs. Terms: FG_TERM_GRAD_GRAD, FG_TERM_MASS,
+ * FG_TERM_GRAD_GRAD_TENSOR_FULL and FG_TERM_ADVECTION (with dt factors), no
+ * field-value coefficients; linear terms go to the test field's own plan.
+ * Assembled by fg_assemble_fp64 / fg_assemble_fp64_static into element
+ * matrices of n_test x n_unknown. Set fg_plan_set_accumulate(plan, 1) so that
+ * the block adds into the rows the test field's own plan writes. Fixed
+ * unknown DOFs lift into the right-hand side through the entry that
+ * VectorFactory::addValuesDC reads, values[j * n_unknown + i]
+ * (src/system/VectorFactory.cpp:184): the transposed entry when both fields
+ * have as many DOFs per element; with different counts that read falls
+ * outside the element matrix, and such a call returns FG_ERR_UNSUPPORTED. */
+int fg_plan_create_coupled(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_space_desc *space,
+                           const fg_system_desc *sys, const fg_space_desc *unknown_space,
+                           const uint64_t *unknown_dof_idx, const int32_t *unknown_dof_type, fg_plan **out);
 void fg_plan_destroy(fg_plan *plan);
 /* plan statistics: nnz, elements, element DOFs, quadrature points, orientations */
 int fg_plan_info(const fg_plan *plan, int64_t *nnz, int64_t *n_elements, int32_t *n_dofs, int32_t *nq, int32_t *n_orient);

@@ -22,7 +22,12 @@ extern "C" {
 enum {
   FG_PROBLEM_HELMHOLTZ = 0, /* -div grad u - k^2 c u = f, scalar */
   FG_PROBLEM_NAVIER = 1,    /* time-harmonic elastodynamics, 3-component field */
-  FG_PROBLEM_MAXWELL = 2    /* curl curl E - k^2 c E, lowest-order HCurl (edge) field */
+  FG_PROBLEM_MAXWELL = 2,   /* curl curl E - k^2 c E, lowest-order HCurl (edge) field */
+  FG_PROBLEM_COUPLED = 3    /* two scalar fields u, v (orders order, order2) coupled both ways:
+                               grad u.grad tu - k^2 u tu + grad v.grad tv + 2 v tv
+                               + (0.5 + x) u tv + (b . grad u) tv + 0.3 grad v.grad tu,
+                               b = (1, -0.5 + 0.2i, 0.25); source: -f tu + (1 + x y) tv;
+                               dirichlet: u fixed on the boundary curves (2D) */
 };
 enum { FG_SPACE_LAGRANGE = 0, FG_SPACE_HIERARCHICAL_H1 = 1, FG_SPACE_HCURL = 2 /* lowest order (edge functions) */ };
 enum {
@@ -49,6 +54,7 @@ typedef struct {
                         term is integral(dt2_dof(u), tf(u)) and the frequency is the assemble call's */
   double lame_sigma; /* Navier: lambda, mu lognormal(median 1, sigma) per element */
   int32_t upper;     /* 1: symmetric (upper-triangle) storage of the system matrix */
+  int32_t order2;    /* FG_PROBLEM_COUPLED: hierarchical order of the field v (0: order) */
 } fg_problem_config;
 
 typedef struct fg_problem fg_problem;
@@ -62,8 +68,23 @@ int fg_problem_descs(const fg_problem *p, fg_mesh_desc *mesh, fg_rule_desc *rule
                      fg_system_desc *sys, const fg_term_desc **terms, int32_t *n_terms,
                      const double **dirichlet);
 
-/* The field's DOF dictionary in its iteration order, as RawDof
- * (src/dofs/Dof.h:44-50): numType, entity, numDof, assembleType, coordinates. */
+/* Multi-field problems (FG_PROBLEM_COUPLED): the unknown fields in the
+ * formulation's registration order (Formulation::_addField, the unknown of
+ * each bilinear term by first appearance), each field's space on the bucket
+ * and element DOF map (fillIndices); the terms by block (test field, unknown
+ * field), linear terms in the block (k, k) of their test field k. A block
+ * with test != unknown is assembled by a plan of fg_plan_create_coupled.
+ * fg_problem_descs describes block 0 (the whole problem with one field). */
+int32_t fg_problem_n_fields(const fg_problem *p);
+int fg_problem_field(const fg_problem *p, int32_t k, fg_space_desc *space, const uint64_t **elem_dof_idx,
+                     const int32_t **elem_dof_type);
+int32_t fg_problem_n_blocks(const fg_problem *p);
+int fg_problem_block(const fg_problem *p, int32_t b, int32_t *test_field, int32_t *unknown_field,
+                     const fg_term_desc **terms, int32_t *n_terms);
+
+/* The fields' DOF dictionaries, field after field, each in its iteration
+ * order, as RawDof (src/dofs/Dof.h:44-50): numType, entity, numDof,
+ * assembleType, coordinates. */
 int64_t fg_problem_n_dofs(const fg_problem *p);
 int fg_problem_raw_dofs(const fg_problem *p, uint64_t *num_type, uint64_t *entity, uint64_t *num_dof,
                         int32_t *assemble_type, float *xyz);
@@ -82,7 +103,9 @@ int fg_problem_bbox(const fg_problem *p, double *bbox);
 double fg_problem_pre_seconds(const fg_problem *p);
 
 /* GpuFormulation::assemble: plan (cached in the problem) + assemble through
- * the C ABI; precision 0 = FP64, 1 = mixed. values [nnz][2], rhs [n_rows][2]. */
+ * the C ABI; precision 0 = FP64, 1 = mixed. values [nnz][2], rhs [n_rows][2].
+ * Problems of one field (a multi-field problem's blocks go through their own
+ * plans: FG_ERR_UNSUPPORTED). */
 int fg_problem_assemble(fg_problem *p, int32_t precision, double *csr_values, double *rhs, void *stream);
 
 #ifdef __cplusplus

@@ -656,6 +656,158 @@ int or_assemble(const or_bucket *b, const or_term *terms, int nterms, double fre
   return or_jacmod_err ? 2 : err;
 }
 
+/* ------------------------------------------------ two-field terms */
+
+/* Element matrix of a term whose unknown and test fields differ
+ * (BilinearTerm::assemblyInitialization with _field[0] != _field[1],
+ * src/term/BilinearTerm.cpp:156-273: the rule of the unknown field's space,
+ * both fields' basis functions at its points; evaluate, :304-343, with
+ * expressionLhs from the unknown field's evaluator and expressionRhs from the
+ * test field's). Scalar H1 fields (Form0, one component) on both sides.
+ * Ae[i * nU + j] = A_e(j, i): i the test DOF, j the unknown DOF, the
+ * column-major layout of the reference's nU x nT A_e. */
+static void or_element_coupled(const or_bucket *bt, const or_bucket *bu, const or_term *terms, int nterms, double freq,
+                               int64_t e, cplx *Ae, cplx *tmp, double *GT, double *GU) {
+  const int nT = bt->nb, nU = bu->nb, nq = bt->nq;
+  const int oT = bt->orient ? bt->orient[e] : 0, oU = bu->orient ? bu->orient[e] : 0;
+  int frequencyModule = 0;
+  for (int t = 0; t < nterms; ++t)
+    if (terms[t].dt) frequencyModule = 1;
+  for (int k = 0; k < nT * nU; ++k) Ae[k] = 0.0;
+  for (int t = 0; t < nterms; ++t) {
+    const or_term *T = &terms[t];
+    if (T->kind == TERM_SOURCE) continue;
+    cplx *target = (frequencyModule && T->dt) ? tmp : Ae;
+    if (target == tmp)
+      for (int k = 0; k < nT * nU; ++k) tmp[k] = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      double J[9], xq[3];
+      double det = or_jacobian(bt, e, q, J, xq);
+      if (or_jacmod_apply(&T->jacmod, xq, J, &det)) or_jacmod_err = 1;
+      const double wd = bt->w[q] * det;
+      const double *phT = bt->bval + ((size_t)oT * nq + q) * nT;
+      const double *phU = bu->bval + ((size_t)oU * nq + q) * nU;
+      /* field nodes read the unknown field's values (the coefficient's field
+       * is evaluated with the unknown's element DOFs) */
+      const cplx c = eval_expr(&T->coef, e, xq, phU, nU);
+      or_form1(J, bt->bgrad + ((size_t)oT * nq + q) * nT * 3, nT, GT);
+      or_form1(J, bu->bgrad + ((size_t)oU * nq + q) * nU * 3, nU, GU);
+      if (T->kind == TERM_MASS) {
+        for (int i = 0; i < nT; ++i)
+          for (int j = 0; j < nU; ++j) target[j + i * nU] += wd * (c * phU[j]) * conj(phT[i]);
+      } else if (T->kind == TERM_GRAD_GRAD) {
+        for (int i = 0; i < nT; ++i)
+          for (int j = 0; j < nU; ++j) {
+            cplx s = 0.0;
+            for (int r = 0; r < 3; ++r) s += (c * GU[r * nU + j]) * conj(GT[r * nT + i]);
+            target[j + i * nU] += wd * s;
+          }
+      } else if (T->kind == TERM_GRAD_GRAD_TENSOR_FULL) {
+        cplx D[3][3];
+        for (int k = 0; k < 9; ++k) D[k / 3][k % 3] = c * eval_expr(&T->tensor[k], e, xq, phU, nU);
+        for (int i = 0; i < nT; ++i)
+          for (int j = 0; j < nU; ++j) {
+            cplx s = 0.0;
+            for (int r = 0; r < 3; ++r)
+              for (int u = 0; u < 3; ++u) s += D[r][u] * GU[u * nU + j] * GT[r * nT + i];
+            target[j + i * nU] += wd * s;
+          }
+      } else if (T->kind == TERM_ADVECTION) {
+        cplx bv[3];
+        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, phU, nU);
+        for (int i = 0; i < nT; ++i)
+          for (int j = 0; j < nU; ++j) {
+            cplx s = bv[0] * GU[j] + bv[1] * GU[nU + j] + bv[2] * GU[2 * nU + j];
+            target[j + i * nU] += wd * s * conj(phT[i]);
+          }
+      }
+    }
+    if (target == tmp) {
+      cplx factor = T->dt == 2 ? -freq * freq : -I * freq;
+      for (int k = 0; k < nT * nU; ++k) Ae[k] += factor * tmp[k];
+    }
+  }
+}
+
+/* Assembly of two-field terms into the shared CSR (Assembler::_assembleBilinear,
+ * src/term/Assembler.cpp:157-359, with the test field's indices as rows and
+ * the unknown field's as columns): MatrixFactory::addValues(nT, nU, test,
+ * unknown, values) adds values[i * nU + j] at (row of test DOF i, column of
+ * unknown DOF j) (src/system/MatrixFactory.cpp:233-307); for fixed unknown
+ * DOFs VectorFactory::addValuesDC(nT, nU, ...) adds values[j * nU + i] *
+ * valuesDC (src/system/VectorFactory.cpp:178-210), the transposed entry when
+ * nT == nU. With nT != nU that read leaves the nT x nU element matrix, so no
+ * value is defined: such a call returns 4 and adds nothing. Scalar H1 fields;
+ * Unknown and Fixed DOFs (linked DOFs: returns 5). values [nnz][2] and rhs
+ * [n_rows][2] are accumulated. */
+int or_assemble_coupled(const or_bucket *bt, const or_bucket *bu, const or_term *terms, int nterms, double freq,
+                        const uint64_t *ai, const uint64_t *aj, const uint64_t *edofT, const int32_t *etypeT,
+                        const uint64_t *edofU, const int32_t *etypeU, const double *dirichlet, double *values, double *rhs) {
+  const int nT = bt->nb, nU = bu->nb;
+  if (bt->form != 0 || bu->form != 0 || bt->mult != 1 || bu->mult != 1) return 6;
+  for (int64_t k = 0; k < bt->E * nT; ++k)
+    if (etypeT[k] == AT_LINKED || etypeT[k] == AT_LINKED_BUBBLE) return 5;
+  int anyFixed = 0;
+  for (int64_t k = 0; k < bu->E * nU; ++k) {
+    if (etypeU[k] == AT_LINKED || etypeU[k] == AT_LINKED_BUBBLE) return 5;
+    if (etypeU[k] == AT_FIXED) anyFixed = 1;
+  }
+  if (anyFixed && rhs && nT != nU) return 4;
+  int err = 0;
+  or_jacmod_err = 0;
+#pragma omp parallel
+  {
+    cplx *Ae = malloc(sizeof(cplx) * nT * nU), *tmp = malloc(sizeof(cplx) * nT * nU);
+    double *GT = malloc(sizeof(double) * 3 * nT), *GU = malloc(sizeof(double) * 3 * nU);
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < bt->E; ++e) {
+      or_element_coupled(bt, bu, terms, nterms, freq, e, Ae, tmp, GT, GU);
+      const uint64_t *it = edofT + (size_t)e * nT, *iu = edofU + (size_t)e * nU;
+      const int32_t *tt = etypeT + (size_t)e * nT, *tu = etypeU + (size_t)e * nU;
+      int haveDC = 0;
+      for (int i = 0; i < nT; ++i) {
+        if (tt[i] == AT_FIXED) {
+          haveDC = 1;
+          continue;
+        }
+        if (tt[i] != AT_UNKNOWN && tt[i] != AT_UNKNOWN_BUBBLE && tt[i] != AT_UNKNOWN_GLOBAL) continue;
+        const uint64_t row = it[i];
+        for (int j = 0; j < nU; ++j) {
+          if (tu[j] == AT_FIXED) {
+            haveDC = 1;
+            continue;
+          }
+          if (tu[j] != AT_UNKNOWN && tu[j] != AT_UNKNOWN_BUBBLE && tu[j] != AT_UNKNOWN_GLOBAL) continue;
+          const uint64_t col = iu[j];
+          if (bt->upper && col < row) continue;
+          const uint64_t pos = lower_bound_u64(aj, ai[row], ai[row + 1], col);
+          if (pos == ai[row + 1] || (aj[pos] != col && !bt->upper)) {
+#pragma omp atomic write
+            err = 1;
+            continue;
+          }
+          atomic_add_c(values + 2 * pos, Ae[i * nU + j]);
+        }
+      }
+      if (haveDC && rhs) {
+        for (int i = 0; i < nT; ++i) {
+          if (tt[i] != AT_UNKNOWN && tt[i] != AT_UNKNOWN_BUBBLE && tt[i] != AT_UNKNOWN_GLOBAL) continue;
+          for (int j = 0; j < nU; ++j)
+            if (tu[j] == AT_FIXED) {
+              cplx uD = dirichlet[2 * iu[j]] + I * dirichlet[2 * iu[j] + 1];
+              atomic_add_c(rhs + 2 * it[i], Ae[j * nU + i] * uD);
+            }
+        }
+      }
+    }
+    free(Ae);
+    free(tmp);
+    free(GT);
+    free(GU);
+  }
+  return or_jacmod_err ? 2 : err;
+}
+
 /* --------------------------------------------------------------- pattern */
 
 /* MatrixFactory::addPattern (src/system/MatrixFactory.cpp:459-539) for a

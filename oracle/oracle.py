@@ -31,6 +31,8 @@ def lib():
         P = C.c_void_p
         L.or_element_matrices.argtypes = [C.POINTER(Bucket), P, C.c_int, C.c_double, P, P]
         L.or_assemble.argtypes = [C.POINTER(Bucket), P, C.c_int, C.c_double, P, P, P, P, P, P, P]
+        L.or_assemble_coupled.argtypes = [C.POINTER(Bucket), C.POINTER(Bucket), P, C.c_int, C.c_double, P, P, P, P, P, P, P,
+                                          P, P]
         L.or_pattern.argtypes = [C.c_int64, C.c_int, P, P, C.c_uint64, P, C.POINTER(P), C.c_int, P]
         L.or_free.argtypes = [P]
         L.or_hilbert_keys.argtypes = [C.c_int, C.c_int64, P, P, P, P]
@@ -122,6 +124,57 @@ def assemble(a, terms_ptr, n_terms, freq=0.0, with_rhs=True):
         raise ValueError("oracle: linked bubble DOFs are not restated")
     if err:
         raise RuntimeError("oracle: an element DOF pair is missing from the pattern")
+    return values, rhs
+
+
+def assemble_coupled(at, au, terms_ptr, n_terms, freq=0.0, with_rhs=True, values=None, rhs=None):
+    """Adds the block of two-field terms (test field: arrays at, the rows;
+    unknown field: au, the columns; femg.Problem.field_arrays) into CSR
+    values [nnz] and rhs [n_rows] (zeros when not given), as the reference's
+    assemble does; returns them."""
+    bt, bu = bucket(at), bucket(au)
+    ai = np.ascontiguousarray(at["ai"], np.uint64)
+    aj = np.ascontiguousarray(at["aj"], np.uint64)
+    et = np.ascontiguousarray(at["edof"], np.uint64)
+    tt = np.ascontiguousarray(at["etype"], np.int32)
+    eu = np.ascontiguousarray(au["edof"], np.uint64)
+    tu = np.ascontiguousarray(au["etype"], np.int32)
+    dirichlet = np.ascontiguousarray(at["dirichlet"], np.complex128)
+    if values is None:
+        values = np.zeros(int(ai[-1]), np.complex128)
+    if rhs is None and with_rhs:
+        rhs = np.zeros(int(at["n_rows"]), np.complex128)
+    err = lib().or_assemble_coupled(C.byref(bt), C.byref(bu), C.cast(terms_ptr, C.c_void_p), n_terms, freq, ai.ctypes.data,
+                                    aj.ctypes.data, et.ctypes.data, tt.ctypes.data, eu.ctypes.data, tu.ctypes.data,
+                                    dirichlet.ctypes.data if dirichlet.size else None, values.ctypes.data,
+                                    rhs.ctypes.data if with_rhs else None)
+    if err == 4:
+        raise ValueError("oracle: lifting through a block of different test and unknown DOF counts has no defined value")
+    if err == 5:
+        raise ValueError("oracle: linked DOFs in two-field terms are not restated")
+    if err == 6:
+        raise ValueError("oracle: two-field terms of scalar H1 fields only")
+    if err == 2:
+        raise ValueError("oracle: an integration point lies outside a Jacobian modificator's shell")
+    if err:
+        raise RuntimeError("oracle: an element DOF pair is missing from the pattern")
+    return values, rhs
+
+
+def assemble_blocks(prob, freq=0.0, with_rhs=True):
+    """The whole system of a multi-field femg.Problem: every block's terms
+    into one CSR value array and right-hand side."""
+    values = np.zeros(prob.nnz, np.complex128)
+    rhs = np.zeros(int(prob.sys.n_rows), np.complex128) if with_rhs else None
+    for test, unknown, tp, nt in prob.blocks():
+        at = prob.field_arrays(test)
+        if test == unknown:
+            v, b = assemble(at, tp, nt, freq, with_rhs)
+            values += v
+            if with_rhs:
+                rhs += b
+        else:
+            assemble_coupled(at, prob.field_arrays(unknown), tp, nt, freq, with_rhs, values, rhs)
     return values, rhs
 
 

@@ -18,7 +18,7 @@
 //
 // usage: ref_assemble <out-file> <threads> <repeats> <kind> <dim> <m> <mesh_order> <space> <order> <gauss>
 //                     <jitter> <seed> <k> <coef_mode> <dirichlet> <dirichlet_value> <source> <omega>
-//                     <lame_sigma> <upper> [<coefficient programs>]
+//                     <lame_sigma> <upper> <order2> [<coefficient programs>]
 // (the fields of fg_problem_config in include/fem_g_gb300_host.h, in order).
 // The optional last argument names a file of coefficient programs for the
 // scalar (Helmholtz-type) problem, each "<term> <count>" followed by count
@@ -203,8 +203,11 @@ void dumpField(F &u, Writer &w) {
   w.arr(at.data(), at.size());
 }
 
-template <class FORM, class F>
-void run(FORM &formulation, F &u, int repeats, Writer &w) {
+// pre(), assemble() (repeats times), then the outputs: the CSR pattern and
+// values, the right-hand side, the number of fields and each field's DOF
+// dictionary, the timings
+template <class FORM, class... F>
+void run(FORM &formulation, int repeats, Writer &w, F &...fields) {
   using clock = std::chrono::steady_clock;
   const auto t0 = clock::now();
   formulation.pre();
@@ -232,7 +235,8 @@ void run(FORM &formulation, F &u, int repeats, Writer &w) {
   std::vector<T> rhs(n);
   for (uint64_t i = 0; i < n && i < b.size(); ++i) rhs[i] = b[i];
   w.arr(rhs.data(), n);
-  dumpField(u, w);
+  w.u64(sizeof...(fields));
+  (dumpField(fields, w), ...);
   w.f64(preSeconds);
   w.f64(median(times));
   w.u64(times.size());
@@ -241,7 +245,7 @@ void run(FORM &formulation, F &u, int repeats, Writer &w) {
 }  // namespace
 
 int main(int argc, char **argv) {
-  if (argc != 21 && argc != 22) {
+  if (argc != 22 && argc != 23) {
     std::fprintf(stderr, "usage: ref_assemble <out> <threads> <repeats> <fg_problem_config fields...>\n");
     return 2;
   }
@@ -268,6 +272,7 @@ int main(int argc, char **argv) {
   c.omega = std::atof(argv[a++]);
   c.lame_sigma = std::atof(argv[a++]);
   c.upper = std::atoi(argv[a++]);
+  c.order2 = std::atoi(argv[a++]);
 
   char arg0[] = "ref_assemble";
   char *gargv[] = {arg0, nullptr};
@@ -299,9 +304,9 @@ int main(int argc, char **argv) {
     // option, the reference's -forceSymmetric switch
     common::Options::instance()->forceSymmetric = c.upper != 0;
     const std::string matrixOptions = c.upper ? "Symmetric" : "";
-    if (c.kind == FG_PROBLEM_HELMHOLTZ && argc == 22) {
+    if (c.kind == FG_PROBLEM_HELMHOLTZ && argc == 23) {
       // the terms from the coefficient programs
-      auto progs = readPrograms(argv[21]);
+      auto progs = readPrograms(argv[22]);
       const bool lagrange = c.space == FG_SPACE_LAGRANGE;
       field::Field<T, field::Form::Form0> u("u", omega,
                                             lagrange ? field::FunctionSpaceTypeForm0::Lagrange
@@ -327,7 +332,7 @@ int main(int argc, char **argv) {
       if (progs.count("mass"))
         formulation.integral(fromProgram(progs["mass"]) * equation::dof(u), equation::tf(u), omega, gauss);
       if (progs.count("source")) formulation.integral(fromProgram(progs["source"]), equation::tf(u), omega, gauss);
-      run(formulation, u, repeats, w);
+      run(formulation, repeats, w, u);
     } else if (c.kind == FG_PROBLEM_HELMHOLTZ) {
       const bool lagrange = c.space == FG_SPACE_LAGRANGE;
       field::Field<T, field::Form::Form0> u("u", omega,
@@ -352,7 +357,35 @@ int main(int argc, char **argv) {
         function::ScalarFunction<T> fsrc = function::heaviside<T>(0.01 - (x - 0.5) * (x - 0.5) - (y - 0.5) * (y - 0.5));
         formulation.integral(-fsrc, equation::tf(u), omega, gauss);
       }
-      run(formulation, u, repeats, w);
+      run(formulation, repeats, w, u);
+    } else if (c.kind == FG_PROBLEM_COUPLED) {
+      // two scalar fields, coupled both ways (the problem of fg_problem_config)
+      const bool lagrange = c.space == FG_SPACE_LAGRANGE;
+      const auto type = lagrange ? field::FunctionSpaceTypeForm0::Lagrange : field::FunctionSpaceTypeForm0::HierarchicalH1;
+      const int orderU = lagrange ? c.mesh_order : c.order;
+      const int orderV = lagrange ? c.mesh_order : (c.order2 > 0 ? c.order2 : c.order);
+      field::Field<T, field::Form::Form0> u("u", omega, type, orderU);
+      field::Field<T, field::Form::Form0> v("v", omega, type, orderV);
+      if (c.dirichlet) u.addConstraint(domain::Domain("gammaDir"), T(c.dirichlet_value, 0.0));
+      problem::Formulation<T> formulation("coupled", matrixOptions);
+      function::ScalarFunction<T> x = function::x<T>(), y = function::y<T>();
+      formulation.integral(equation::grad(equation::dof(u)), equation::grad(equation::tf(u)), omega, gauss);
+      formulation.integral(function::ScalarFunction<T>(T(-c.k * c.k, 0.0)) * equation::dof(u), equation::tf(u), omega, gauss);
+      formulation.integral(equation::grad(equation::dof(v)), equation::grad(equation::tf(v)), omega, gauss);
+      formulation.integral(function::ScalarFunction<T>(T(2.0, 0.0)) * equation::dof(v), equation::tf(v), omega, gauss);
+      formulation.integral((0.5 + x) * equation::dof(u), equation::tf(v), omega, gauss);
+      formulation.integral(function::vector<T>(function::ScalarFunction<T>(T(1.0, 0.0)), function::ScalarFunction<T>(T(-0.5, 0.2)),
+                                               function::ScalarFunction<T>(T(0.25, 0.0))) *
+                               equation::grad(equation::dof(u)),
+                           equation::tf(v), omega, gauss);
+      formulation.integral(function::ScalarFunction<T>(T(0.3, 0.0)) * equation::grad(equation::dof(v)), equation::grad(equation::tf(u)),
+                           omega, gauss);
+      if (c.source) {
+        function::ScalarFunction<T> fsrc = function::heaviside<T>(0.01 - (x - 0.5) * (x - 0.5) - (y - 0.5) * (y - 0.5));
+        formulation.integral(-fsrc, equation::tf(u), omega, gauss);
+        formulation.integral(1.0 + x * y, equation::tf(v), omega, gauss);
+      }
+      run(formulation, repeats, w, u, v);
     } else if (c.kind == FG_PROBLEM_MAXWELL) {
       field::Field<T, field::Form::Form1> u("u", omega, field::FunctionSpaceTypeForm1::HierarchicalHCurl, 0);
       problem::Formulation<T> formulation("maxwell", matrixOptions);
@@ -366,7 +399,7 @@ int main(int argc, char **argv) {
         for (int64_t e = 0; e < E; ++e) ce[(size_t)e] = T(-c.k * c.k * (1.0 + 0.3 * rng.normal()), 0.0);
         formulation.integral(elementArray(std::move(ce)) * equation::dof(u), equation::tf(u), omega, gauss);
       }
-      run(formulation, u, repeats, w);
+      run(formulation, repeats, w, u);
     } else if (c.kind == FG_PROBLEM_NAVIER) {
       field::CompoundField<T, field::Form::Form0, 3> u("u", omega, field::FunctionSpaceTypeForm0::HierarchicalH1, c.order);
       problem::Formulation<T> formulation("navier", matrixOptions);
@@ -403,7 +436,7 @@ int main(int argc, char **argv) {
       } else {
         formulation.integral(equation::dt2_dof(u), equation::tf(u), omega, gauss);
       }
-      run(formulation, u, repeats, w);
+      run(formulation, repeats, w, u);
     } else {
       throw std::runtime_error("unknown problem kind");
     }

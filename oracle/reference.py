@@ -19,7 +19,7 @@ EXE = os.path.join(HERE, "_ref", "ref_assemble")
 MAGIC = 0x46454D4752454631
 
 FIELDS = ["kind", "dim", "m", "mesh_order", "space", "order", "gauss", "jitter", "seed", "k", "coef_mode", "dirichlet",
-          "dirichlet_value", "source", "omega", "lame_sigma", "upper"]
+          "dirichlet_value", "source", "omega", "lame_sigma", "upper", "order2"]
 
 
 def available():
@@ -80,11 +80,18 @@ def run(cfg, threads=0, repeats=1, timeout=3600, programs=None):
     out["aj"] = take(np.uint64, nnz)
     out["values"] = take(np.complex128, nnz)
     out["rhs"] = take(np.complex128, n)
-    nd = int(take(np.uint64, 1)[0])
-    out["dof_num_type"] = take(np.uint64, nd)
-    out["dof_entity"] = take(np.uint64, nd)
-    out["dof_num_dof"] = take(np.uint64, nd)
-    out["dof_assemble_type"] = take(np.int32, nd)
+    # every field's DOF dictionary in its iteration order, field after field
+    parts = {"dof_num_type": [], "dof_entity": [], "dof_num_dof": [], "dof_assemble_type": []}
+    nf = int(take(np.uint64, 1)[0])
+    for _ in range(nf):
+        nd = int(take(np.uint64, 1)[0])
+        parts["dof_num_type"].append(take(np.uint64, nd))
+        parts["dof_entity"].append(take(np.uint64, nd))
+        parts["dof_num_dof"].append(take(np.uint64, nd))
+        parts["dof_assemble_type"].append(take(np.int32, nd))
+    for k, v in parts.items():
+        out[k] = np.concatenate(v)
+    out["fields"] = nf
     out["pre_seconds"] = float(take(np.float64, 1)[0])
     out["assemble_seconds"] = float(take(np.float64, 1)[0])
     out["timed_runs"] = int(take(np.uint64, 1)[0])
