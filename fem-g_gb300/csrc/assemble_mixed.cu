@@ -38,6 +38,12 @@ struct MixedState {
   int built = 0;
   int ncomp = 0, groups = 0;  // layout of the current tiles and buffers
   int n = 0, nn2 = 0, Npad = 0;
+  // row stride of the FP32 element matrices: nn2, except for one-block fields
+  // whose nn2 is not a multiple of 4 (order-4 tets: 1,225), padded to a
+  // multiple of 8 floats so that every row starts on a 32-byte sector and the
+  // contraction stores whole 16-byte vectors (the padding holds the zero
+  // columns of the reference tensors)
+  int ld = 0;
   int nOrient = 0;
   int blocks = 1;            // 9 component blocks per element for a compound field
   int kp = 0, k3 = 0;        // factor columns and K' of the 3xTF32 chain
@@ -56,7 +62,7 @@ struct MixedState {
   alignas(64) CUtensorMap aMap;  // TMA view of A: [rows][k3] floats, box 4 x 128
   int mmaN = 256;               // N of one MMA instruction
   void *probDev = nullptr;      // this plan's GemmProblem on the device
-  float *ke = nullptr;       // [E][groups][ncomp][n][n] fp32 (layout: mixedLayout)
+  float *ke = nullptr;       // [E][groups][ncomp][ld] fp32 (layout: mixedLayout)
   size_t keBytes = 0;
   int *err = nullptr;        // device error word (wait timeouts)
   int *errHost = nullptr;    // pinned copy of err
@@ -66,7 +72,7 @@ struct MixedState {
 
 // The layout of m->ke for the reduction
 static KeLayout mixedLayout(const MixedState *m) {
-  return KeLayout{m->blocks == 9 ? kKeBlocks3 : kKeFull, m->n * m->n};
+  return KeLayout{m->blocks == 9 ? kKeBlocks3 : kKeFull, m->blocks == 9 ? m->n * m->n : m->ld};
 }
 
 // Reports (once) a device wait timeout recorded by an earlier launch: when
@@ -448,9 +454,11 @@ __device__ inline void loadB(const GemmProblem &g, float *Bs, int o, int tid, ui
 __device__ inline void drainColumns(const GemmProblem &g, uint32_t tmemRow, float *out, bool live, int c0, int c1, float *stage,
                                     int colOff) {
   const int lane = threadIdx.x & 31;
-  const bool vec = (g.nn2 & 3) == 0;
+  const bool vec = (g.ld & 3) == 0;
   out += colOff;
-  const int nn2 = g.nn2 - colOff;  // columns left in the element row
+  // columns left in the element row, its padding included (the reference
+  // tensors' zero columns land there)
+  const int nn2 = g.ld - colOff;
   int c = c0;
   for (; c + 32 <= c1; c += 32) {
     float v[32];
@@ -598,7 +606,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
     const bool live = r < nrows;
     const int grow = row0 + r;
     const int64_t e = live ? gs.perm[grow / gs.rowsPerElem] : 0;
-    float *out = gs.ke + ((size_t)e * gs.rowsPerElem + (grow % gs.rowsPerElem)) * gs.nn2;
+    float *out = gs.ke + ((size_t)e * gs.rowsPerElem + (grow % gs.rowsPerElem)) * gs.ld;
     const uint32_t tmemRow = tmem + ((uint32_t)(quad * 32) << 16);
     float *stage = Stage + warp * (32 * 36);
     for (int n0 = 0; n0 < gs.Npad && !failed; n0 += tmemCols) {
@@ -927,6 +935,7 @@ GemmProblem mixedGemmProblem(fg_plan *plan) {
   g.ke = m->ke;
   g.Npad = m->Npad;
   g.nn2 = m->nn2;
+  g.ld = m->ld;
   g.rowsPerElem = m->rowsPerElem;
   g.K3 = m->k3;
   g.mmaN = std::min(m->mmaN, std::min(m->Npad, 256));
@@ -955,6 +964,7 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
     m->n = p.n;
     m->nn2 = p.nb * p.nb;  // one (block of the) element matrix per GEMM row
     m->Npad = (m->nn2 + 15) / 16 * 16;
+    m->ld = (m->blocks == 1 && m->nn2 % 4 != 0) ? (m->nn2 + 7) / 8 * 8 : m->nn2;
     m->nOrient = p.nOrient;
     if (gemmSmem(m->Npad, m->k3) > 220 * 1024) {
       setLastError("mixed path: element matrix too large for the shared-memory B tile");
@@ -1017,7 +1027,7 @@ int prepareMixed(fg_plan *plan, int ncomp, int groups) {
   int st = ensureDevice((void **)&m->A, &m->Abytes, (size_t)m->rows * m->k3 * 4);
   if (st) return st;
   if ((st = encodeRowsMap(&m->aMap, m->A, m->k3, m->rows))) return st;
-  st = ensureDevice((void **)&m->ke, &m->keBytes, (size_t)m->rows * m->nn2 * 4);
+  st = ensureDevice((void **)&m->ke, &m->keBytes, (size_t)m->rows * m->ld * 4);
   if (st) return st;
   m->ncomp = ncomp;
   m->groups = groups;

@@ -64,6 +64,7 @@ constexpr int kMaxDofs = 64;         // element DOFs (basis x multiplicity) hand
 constexpr int kMaxNodes = 10;        // geometric nodes per element
 constexpr int kMaxTerms = 6;
 constexpr int kOutChunks = 8;        // row ranges of the gather for overlapped host copies
+constexpr uint64_t kVisitWindow = 4096;  // rows per window of the gather's count-grouped visiting order
 constexpr uint16_t kSlotFixed = 0xFFFF;   // column is a fixed DOF (Dirichlet lifting)
 constexpr uint16_t kSlotIgnore = 0xFFFE;  // column does not assemble (undefined type)
 
@@ -301,10 +302,10 @@ struct GemmProblem {
   const float *A;       // [rows][K3] split factor rows
   const float *B;       // [nOrient][Npad * K3] core-matrix images
   const int32_t *perm;  // rank -> element
-  float *ke;            // [E][rowsPerElem][nn2]
+  float *ke;            // [E][rowsPerElem][ld]
   int Npad, nn2, rowsPerElem, K3;
   int mmaN;             // N of one MMA instruction (16..256, multiple of 16)
-  int pad_;
+  int ld;               // element-matrix row stride (floats): nn2, or nn2 padded to a multiple of 8
 };
 
 // One plan of a batched factor-row launch (mixed path)
