@@ -52,6 +52,11 @@ METRIC = "element matrices/s and CSR nnz/s: mixed vs FP64 GPU at <=1e-6 rel erro
 # written.
 GATHER_TRAFFIC_PER_NNZ_P3 = {"k_gather": (555.207680e6 + 550.488064e6) / 35811451}
 
+# FP64-pipe activity of the plain FP64 element kernel (k_element_fp64<8, 0>,
+# the quadrature loop) in an ncu capture on the 30^3 x 6 P3 mesh: the loop is
+# bound by GB300's FP64 pipe
+ELEMENT_FP64_PIPE_ACTIVE_P3 = 0.910
+
 
 def load_femg():
     import __graft_entry__ as g
@@ -565,19 +570,35 @@ def main():
         return
     line = bench_headline(args, femg, torch, ws, rank, local, dist)
     # the batched (c4) and multi-frequency (c5) workloads of the target, one
-    # GPU each, after the headline's buffers are released
+    # GPU each, after the headline's buffers are released. Each runs in a child
+    # process of its own: the batch alone holds about 120 GB of host memory
+    # (64 problems' patterns, and 78 GB of host outputs for its end-to-end
+    # figure), which a process that ran the headline before does not give
+    # back to the system in full.
     if rank == 0 and ws == 1 and args.workload == "c3":
         torch.cuda.empty_cache()
         if not args.no_c4:
-            line["c4"] = bench_batch(args, femg, torch)
-            torch.cuda.empty_cache()
+            line["c4"] = run_child(args, "c4")
         if not args.no_c5:
-            line["c5mf"] = bench_multi_freq(args, femg, torch)
-            torch.cuda.empty_cache()
+            line["c5mf"] = run_child(args, "c5mf")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+def run_child(args, workload):
+    """bench.py --workload <workload> in a child process: its JSON line."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--workload", workload, "--steps", str(args.steps), "--warmup",
+           str(args.warmup), "--cpu-seconds", str(args.cpu_seconds), "--c4-n", str(args.c4_n), "--c4-m-lo",
+           str(args.c4_m_lo), "--c4-m-hi", str(args.c4_m_hi), "--n-freq", str(args.n_freq), "--c5-m", str(args.c5_m)]
+    if args.no_cpu:
+        cmd.append("--no-cpu")
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    if r.returncode != 0 or not lines:
+        return {"error": "bench.py --workload %s exited %d: %s" % (workload, r.returncode, (r.stderr or "")[-500:])}
+    return json.loads(lines[-1])
 
 
 def bench_headline(args, femg, torch, ws, rank, local, dist):
@@ -757,7 +778,8 @@ def bench_headline(args, femg, torch, ws, rank, local, dist):
             a = prob.arrays()
             rate, S, dt, cores = cpu_rate(prob, a, args.cpu_seconds)
             cpu = {"value": rate, "unit": "element matrices/s", "cores": cores, "kind": "port",
-                   "sample": "first %d of %d elements, %.1f s, oracle restatement of Formulation::assemble" % (S, E, dt)}
+                   "sample": "first %d of %d elements, %.1f s, oracle restatement of Formulation::assemble" % (S, E, dt),
+                   "quadrature_points": plan.info()["nq"]}
         value = replica_value(E, ms_head, ws)
         line = {"metric": METRIC, "value": value, "unit": "element matrices/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_head, "higher_is_better": True, "scaling": "weak",
@@ -768,7 +790,13 @@ def bench_headline(args, femg, torch, ws, rank, local, dist):
                            "parallelism": "replicas" if ws > 1 else "single"},
                 "nnz_per_s": ws * nnz / (ms_head / 1000.0),
                 "fp64": {"value": ws * E / (ms_fp64 / 1000.0), "ms_per_step": ms_fp64, "nnz_per_s": ws * nnz / (ms_fp64 / 1000.0),
-                         "method": "plain: quadrature loop of BilinearTerm::evaluate in FP64"},
+                         "method": "plain: quadrature loop of BilinearTerm::evaluate in FP64",
+                         "quadrature_points": plan.info()["nq"],
+                         "fp64_pipe_active": (ELEMENT_FP64_PIPE_ACTIVE_P3 if args.workload in ("c2", "c3") else None),
+                         "note": ("the quadrature loop's work is proportional to the points of the rule; the stand-in "
+                                  "Gauss%d rule has %d points (Grundmann-Moeller), a published degree-6 tetrahedral rule "
+                                  "(Keast) has 24" % (cfg.gauss, plan.info()["nq"]) if cfg.dim == 3 and cfg.gauss == 6 else
+                                  "the quadrature loop's work is proportional to the points of the rule")},
                 "fp64_factored": {"value": ws * E / (ms_fp64_fact / 1000.0), "ms_per_step": ms_fp64_fact,
                                   "method": "exact factorization of the affine element matrices, FP64 on the CUDA cores"},
                 "speedup_mixed_vs_fp64_factored": ms_fp64_fact / ms_head,
