@@ -225,19 +225,45 @@ def build_problems(femg, cfgs, workers=4):
 def bench_batch(args, femg, torch):
     """Batched workload: 64 3D Helmholtz problems, m ~ U{m_lo..m_hi}, orders
     U{1..4}, k ~ U[5, 40], Gauss(2p), one seed; one step = one fg_batch_run
-    (graph replay) over all problems, outputs resident in HBM."""
+    (graph replay) over all problems, outputs resident in HBM. The host
+    problems (their CSR patterns: 8 bytes per nonzero, 39 GB here) are
+    released before the end-to-end run allocates its host outputs (16 bytes
+    per nonzero)."""
     cfgs = femg.config_c4(n=args.c4_n, m_lo=args.c4_m_lo, m_hi=args.c4_m_hi)
     w0 = time.perf_counter()
-    probs = build_problems(femg, cfgs)
+    probs = build_problems(femg, cfgs, workers=2)
     pre_wall = time.perf_counter() - w0
     pre_s = sum(p.pre_seconds() for p in probs)
     plans = [p.plan() for p in probs]
-    E = sum(p.info()["E"] for p in plans)
-    nnz = sum(p.nnz for p in probs)
-    rows = sum(int(p.sys.n_rows) for p in probs)
+    infos = [p.info() for p in plans]
+    nnzs = [p.nnz for p in probs]
+    rowsq = [int(p.sys.n_rows) for p in probs]
+    E = sum(i["E"] for i in infos)
+    nnz = sum(nnzs)
+    rows = sum(rowsq)
+    algq = [fused_bytes(i["E"], i["n"], z, r, coef=0) for i, z, r in zip(infos, nnzs, rowsq)]
+    alg = sum(algq)
+    # CPU baseline: the oracle per order on the largest problem of that order,
+    # a bounded sample each; the batch rate is the element-weighted harmonic mean
+    cpu = None
+    if not args.no_cpu:
+        by_order = {}
+        for q, p in enumerate(probs):
+            o = int(p.cfg.order)
+            if o not in by_order or p.E > probs[by_order[o]].E:
+                by_order[o] = q
+        rates, samples, cores = {}, [], 1
+        for o, q in sorted(by_order.items()):
+            p = probs[q]
+            r, S, dt, cores = cpu_rate(p, p.arrays(), args.cpu_seconds / max(len(by_order), 1))
+            rates[o] = r
+            samples.append("order %d: first %d of %d elements, %.1f s" % (o, S, p.E, dt))
+        t_all = sum(i["E"] / rates[int(c.order)] for i, c in zip(infos, cfgs))
+        cpu = {"value": E / t_all, "unit": "element matrices/s", "cores": cores, "kind": "port",
+               "sample": "; ".join(samples) + "; batch rate = all elements / sum over problems of elements / rate of its order"}
     stream = torch.cuda.current_stream()
     sptr = C.c_void_p(stream.cuda_stream)
-    outs = [torch.empty(2 * p.nnz, dtype=torch.float64, device="cuda") for p in probs]
+    outs = [torch.empty(2 * z, dtype=torch.float64, device="cuda") for z in nnzs]
     ptrs = [o.data_ptr() for o in outs]
     res = {}
     clocks = ClockSampler(torch.cuda.current_device())
@@ -258,32 +284,17 @@ def bench_batch(args, femg, torch):
         res[prec] = {"ms": ms, "first_run_s": first_s, "tuning": json.loads(b.tuning()), "launches_per_step": int(launches)}
         if prec == "mixed":
             res["prof"] = profile_run(femg, torch, lambda: b.run(values=ptrs, stream=sptr))
-            # end to end (before the FP64 comparison below grows the plans'
-            # FP64 scratch): the batch's CSR values into host memory, as the
-            # reference's module arrays hold them (ordinary pageable memory);
-            # the batch stages them on the device
-            hv = [np.empty(p.nnz, np.complex128) for p in probs]
-            hptrs = [h.ctypes.data for h in hv]
-            b.run(values=hptrs, stream=sptr)  # warm-up: first touch of the host pages
-            e2e_steps = 2
-            e0 = time.perf_counter()
-            for _ in range(e2e_steps):
-                b.run(values=hptrs, stream=sptr)
-            torch.cuda.synchronize()
-            res["e2e_ms"] = 1000.0 * (time.perf_counter() - e0) / e2e_steps
-            del hv, hptrs
         b.close()
         if prec == "mixed":
             # relative Frobenius error of every problem's CSR against the FP64 path
-            tmp = torch.empty(2 * max(p.nnz for p in probs), dtype=torch.float64, device="cuda")
+            tmp = torch.empty(2 * max(nnzs), dtype=torch.float64, device="cuda")
             d2 = r2 = 0.0
             worst = 0.0
-            for p, o in zip(plans, outs):
-                n2 = 2 * p.prob.nnz
+            for p, o, z in zip(plans, outs, nnzs):
                 p.assemble("fp64", values=tmp.data_ptr(), rhs=False, stream=sptr)
                 torch.cuda.synchronize()
-                dd = torch.linalg.vector_norm(o - tmp[:n2]).item() ** 2
-                rr = torch.linalg.vector_norm(tmp[:n2]).item() ** 2
+                dd = torch.linalg.vector_norm(o - tmp[:2 * z]).item() ** 2
+                rr = torch.linalg.vector_norm(tmp[:2 * z]).item() ** 2
                 d2 += dd
                 r2 += rr
                 worst = max(worst, (dd / rr) ** 0.5 if rr > 0 else 0.0)
@@ -294,50 +305,51 @@ def bench_batch(args, femg, torch):
     outs.clear()
     ptrs = None
     torch.cuda.empty_cache()
+    # end to end: the batch's CSR values into host memory, as the reference's
+    # module arrays hold them (ordinary pageable memory); the batch stages
+    # them on the device. Its plans keep their device tables; the host
+    # problems go first.
+    for p in plans:
+        p.set_fp64_method(femg.FG_FP64_QUADRATURE)
+    be = femg.Batch(plans, mixed=True)
+    for p in probs:
+        p.close()
+    hv = [np.empty(z, np.complex128) for z in nnzs]
+    hptrs = [h.ctypes.data for h in hv]
+    be.run(values=hptrs, stream=sptr)  # tunes, and first touch of the host pages
+    e2e_steps = 2
+    e0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        be.run(values=hptrs, stream=sptr)
+    torch.cuda.synchronize()
+    e2e_ms = 1000.0 * (time.perf_counter() - e0) / e2e_steps
+    del hv, hptrs
+    be.close()
     pk, pk_kind = peaks()
-    algq = [fused_bytes(p.info()["E"], p.info()["n"], p.prob.nnz, int(p.prob.sys.n_rows), coef=0) for p in plans]
-    alg = sum(algq)
     # the reduction kernels by class (element DOFs n): vector-load or scalar
     v4n = {c["n"] for c in res["mixed"]["tuning"]["gather"] if c.get("vector_loads")}
     alg_by = {k: alg for k in res["prof"] if not k.startswith("k_gather")}
-    alg_by["k_gather_batch_v4"] = sum(a for p, a in zip(plans, algq) if p.info()["n"] in v4n)
-    alg_by["k_gather_batch"] = sum(a for p, a in zip(plans, algq) if p.info()["n"] not in v4n)
+    alg_by["k_gather_batch_v4"] = sum(a for i, a in zip(infos, algq) if i["n"] in v4n)
+    alg_by["k_gather_batch"] = sum(a for i, a in zip(infos, algq) if i["n"] not in v4n)
     roof = roofline(res["prof"], alg_by, pk, pk_kind)
     step_gbs = alg / (res["mixed"]["ms"] / 1000.0) / 1e9
     roof["step"] = {"achieved": step_gbs, "frac": step_gbs / pk["hbm_gbs"], "algorithmic_bytes": alg,
                     "note": "fused-minimum bytes of all problems over the whole step"}
-    cpu = None
-    if not args.no_cpu:
-        # the oracle per order on the largest problem of that order, a bounded
-        # sample each; the batch rate is the element-weighted harmonic mean
-        by_order = {}
-        for p in probs:
-            o = int(p.cfg.order)
-            if o not in by_order or p.E > by_order[o].E:
-                by_order[o] = p
-        rates, samples = {}, []
-        for o, p in sorted(by_order.items()):
-            r, S, dt, cores = cpu_rate(p, p.arrays(), args.cpu_seconds / max(len(by_order), 1))
-            rates[o] = r
-            samples.append("order %d: first %d of %d elements, %.1f s" % (o, S, p.E, dt))
-        t_all = sum(p.E / rates[int(p.cfg.order)] for p in probs)
-        cpu = {"value": E / t_all, "unit": "element matrices/s", "cores": cores, "kind": "port",
-               "sample": "; ".join(samples) + "; batch rate = all elements / sum over problems of elements / rate of its order"}
     orders = {}
     for c in cfgs:
         orders[str(c.order)] = orders.get(str(c.order), 0) + 1
     for p in plans:
         p.close()
-    for p in probs:
-        p.close()
     return {"metric": METRIC, "value": E / (res["mixed"]["ms"] / 1000.0), "unit": "element matrices/s",
             "ms_per_step": res["mixed"]["ms"], "steps": args.steps, "warmup": args.warmup,
             "config": {"workload": "helmholtz3d_batch%d_m%d-%d_p1-4_k5-40_gauss2p" % (args.c4_n, args.c4_m_lo, args.c4_m_hi),
-                       "problems": len(probs), "elements": E, "nnz": nnz, "unknowns": rows, "orders": orders,
+                       "problems": len(cfgs), "elements": E, "nnz": nnz, "unknowns": rows, "orders": orders,
                        "l2": "CSR outputs larger than L2, no flush"},
             "nnz_per_s": nnz / (res["mixed"]["ms"] / 1000.0),
             "fp64": {"value": E / (res["fp64"]["ms"] / 1000.0), "ms_per_step": res["fp64"]["ms"],
-                     "method": "plain: quadrature loop of BilinearTerm::evaluate in FP64"},
+                     "method": "plain: quadrature loop of BilinearTerm::evaluate in FP64",
+                     "quadrature_points": {str(c["n"]): c["nq"] for c in res["mixed"]["tuning"]["gather"]},
+                     "note": "quadrature points per class (element DOFs: points) of the stand-in Gauss(2p) rules"},
             "fp64_factored": {"value": E / (res["fp64_factored"]["ms"] / 1000.0), "ms_per_step": res["fp64_factored"]["ms"],
                               "method": "exact factorization of the affine element matrices, FP64 on the CUDA cores"},
             "speedup_mixed_vs_fp64": res["fp64"]["ms"] / res["mixed"]["ms"],
@@ -346,7 +358,7 @@ def bench_batch(args, femg, torch):
             "first_run_s": {k: res[k]["first_run_s"] for k in ("mixed", "fp64", "fp64_factored")},
             "tuning": {"mixed": res["mixed"]["tuning"], "fp64": res["fp64"]["tuning"]},
             "gpu_launches": res["mixed"]["launches_per_step"] * args.steps,
-            "e2e": {"value": E / (res["e2e_ms"] / 1000.0), "unit": "element matrices/s", "ms_per_step": res["e2e_ms"],
+            "e2e": {"value": E / (e2e_ms / 1000.0), "unit": "element matrices/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": 0, "d2h_bytes_per_step": nnz * 16,
                     "note": "fg_batch_run into pageable host arrays; the coefficients are constants (no input arrays)"},
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk,

@@ -18,6 +18,7 @@
 // matrices leave TMEM as FP32 and are reduced into the FP64 CSR by the same
 // deterministic gather as the FP64 path.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -405,6 +406,7 @@ struct GemmSched {
   const int32_t *ctaStart;
   int *err;
   int tma;           // A tiles by TMA through aMap (one problem), else by cp.async
+  long long mmaWaitCycles;  // bound of the wait for an MMA chain (fg_set_wait_limit)
 };
 
 
@@ -629,7 +631,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
         aPending |= 1u << (buf ^ 1);
       }
       __syncwarp();
-      const bool ok = mbarWait(mbar, phase);
+      const bool ok = mbarWaitFor(mbar, phase, sc.mmaWaitCycles);
       failed = __syncthreads_or(ok ? 0 : 1) != 0;  // block-uniform
       if (failed) {
         if (tid == 0) atomicExch(sc.err, 1);
@@ -889,6 +891,12 @@ std::vector<int32_t> partitionTiles(const std::vector<double> &cost, int nCta) {
   return start;
 }
 
+// Bound of the contraction's wait for each MMA chain, in SM cycles
+// (fg_set_wait_limit). After it runs out the kernel records a timeout, waits
+// once more with the fixed bound for the chain it issued, frees its TMEM and
+// returns.
+static std::atomic<long long> g_mmaWaitCycles{kWaitCycles};
+
 // One contraction launch over the tiles of one or many problems
 int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ctaStartDev, int nCta, int *err, int maxK3,
                    size_t smem, cudaStream_t s, int tmemCols, const void *aMap) {
@@ -904,6 +912,7 @@ int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ct
   sc.tiles = tilesDev;
   sc.ctaStart = ctaStartDev;
   sc.err = err;
+  sc.mmaWaitCycles = g_mmaWaitCycles.load();
   ProfScope prof("k_contract_tf32x3", s);
   k_contract_tf32x3<<<std::max(1, nCta), kThreadsGemm, smem, s>>>(sc, maxK3, tmemCols);
   countLaunch();
@@ -1123,6 +1132,17 @@ int mixedRecordError(fg_plan *plan, cudaStream_t s) {
 }  // namespace femg
 
 using namespace femg;
+
+extern "C" int fg_set_wait_limit(double seconds) {
+  if (!(seconds >= 0.0) || seconds > 60.0) {
+    femg::setLastError("fg_set_wait_limit: seconds must be in [0, 60]");
+    return FG_ERR_ARG;
+  }
+  // clock64 counts SM cycles: at most 2.07 GHz on GB300, so the bound lasts at
+  // least `seconds` of wall time
+  g_mmaWaitCycles.store((long long)(seconds * 2.07e9));
+  return FG_OK;
+}
 
 extern "C" void mixedDestroy(fg_plan *plan) {
   MixedState *m = (MixedState *)plan->mixed;

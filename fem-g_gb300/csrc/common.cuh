@@ -64,7 +64,6 @@ constexpr int kMaxDofs = 64;         // element DOFs (basis x multiplicity) hand
 constexpr int kMaxNodes = 10;        // geometric nodes per element
 constexpr int kMaxTerms = 6;
 constexpr int kOutChunks = 8;        // row ranges of the gather for overlapped host copies
-constexpr uint64_t kVisitWindow = 4096;  // rows per window of the gather's count-grouped visiting order
 constexpr uint16_t kSlotFixed = 0xFFFF;   // column is a fixed DOF (Dirichlet lifting)
 constexpr uint16_t kSlotIgnore = 0xFFFE;  // column does not assemble (undefined type)
 

@@ -254,16 +254,15 @@ __device__ __forceinline__ void gatherRowsV4(const PlanDev &p, const float *__re
   }
 }
 
-// 5 blocks of 8 warps per SM (48 registers): the loads of 40 warps in flight
 template <bool ACC>
-__global__ void __launch_bounds__(256, 5)
+__global__ void __launch_bounds__(256)
     k_gather_v4(const PlanDev p, const float *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
                 double2 *__restrict__ values, double2 *__restrict__ rhs, int L, int64_t v0, int64_t v1) {
   gatherRowsV4<ACC>(p, ke, be, uD, values, rhs, L, blockIdx.x, gridDim.x, v0, v1);
 }
 
 // Many plans of one class in one launch (k_gather_batch with the vector loads)
-__global__ void __launch_bounds__(256, 5) k_gather_batch_v4(const GatherJob *__restrict__ jobs, int nJobs, int L) {
+__global__ void __launch_bounds__(256) k_gather_batch_v4(const GatherJob *__restrict__ jobs, int nJobs, int L) {
   int lo = 0, hi = nJobs - 1;
   while (lo < hi) {  // last job whose blockStart <= blockIdx.x
     const int mid = (lo + hi + 1) >> 1;
@@ -275,10 +274,8 @@ __global__ void __launch_bounds__(256, 5) k_gather_batch_v4(const GatherJob *__r
                       Jb.nBlocks, 0, (int64_t)Jb.p.nRows);
 }
 
-// Real FP32 element matrices (the mixed path): at least 4 blocks of 8 warps
-// per SM (64 registers); the other instantiations keep their register count
 template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J, bool ACC>
-__global__ void __launch_bounds__(256, (!KCPLX && sizeof(KT) == 4) ? 4 : 1)
+__global__ void __launch_bounds__(256)
     k_gather(const PlanDev p, const KT *__restrict__ ke, const double2 *__restrict__ be, const double2 *__restrict__ uD,
              double2 *__restrict__ values, double2 *__restrict__ rhs, int rowsPerBlock, KeLayout lay, int64_t v0, int64_t v1) {
   gatherRows<SlotT, KCPLX, KT, AT, L, J, ACC>(p, ke, be, uD, values, rhs, rowsPerBlock, lay, blockIdx.x, gridDim.x, v0, v1);
@@ -286,7 +283,7 @@ __global__ void __launch_bounds__(256, (!KCPLX && sizeof(KT) == 4) ? 4 : 1)
 
 // Many plans in one launch: job q owns blocks [blockStart, blockStart + nBlocks)
 template <typename SlotT, bool KCPLX, typename KT, typename AT, int L, int J>
-__global__ void __launch_bounds__(256, (!KCPLX && sizeof(KT) == 4) ? 4 : 1) k_gather_batch(const GatherJob *__restrict__ jobs, int nJobs, int rowsPerBlock) {
+__global__ void __launch_bounds__(256) k_gather_batch(const GatherJob *__restrict__ jobs, int nJobs, int rowsPerBlock) {
   int lo = 0, hi = nJobs - 1;
   while (lo < hi) {  // last job whose blockStart <= blockIdx.x
     const int mid = (lo + hi + 1) >> 1;

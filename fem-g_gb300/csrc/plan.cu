@@ -335,16 +335,12 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
       }
   }
 
-  // gather visiting orders: within windows of kVisitWindow consecutive rows,
-  // rows grouped by contribution count (stable), so that the sub-warps of a
-  // warp run loops of equal length while the rows in flight stay close in the
-  // Hilbert numbering, and the element rows they read (every local row of an
-  // element comes from a nearby DOF) meet in L2 instead of being fetched once
-  // per count class. Over all rows (rowOrder, for device outputs), and within
-  // kOutChunks consecutive row ranges (rowOrderRanged, for host outputs: the
-  // visit indices of a range are its rows' indices, so the CSR slice of a
-  // range is complete once its part of the order has run, and can be copied
-  // out while the next range reduces)
+  // gather visiting orders, rows grouped by contribution count (stable):
+  // over all rows (rowOrder, for device outputs), and within kOutChunks
+  // consecutive row ranges (rowOrderRanged, for host outputs: the visit
+  // indices of a range are its rows' indices, so the CSR slice of a range is
+  // complete once its part of the order has run, and can be copied out while
+  // the next range reduces)
   std::vector<uint32_t> rowOrder(sys->n_rows), rowOrderRanged;
   const int nChunks = sys->n_rows >= (uint64_t)kOutChunks * 4096 ? kOutChunks : 1;
   {
@@ -360,13 +356,10 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
       for (uint64_t k = 0; k <= maxCnt; ++k) bucket[k + 1] += bucket[k];
       for (uint64_t r = ra; r < rb; ++r) order[bucket[rowPtr[r + 1] - rowPtr[r]]++] = (uint32_t)r;
     };
-    auto windowed = [&](uint64_t ra, uint64_t rb, std::vector<uint32_t> &order) {
-      for (uint64_t w = ra; w < rb; w += kVisitWindow) countSort(w, std::min<uint64_t>(rb, w + kVisitWindow), order);
-    };
-    windowed(0, sys->n_rows, rowOrder);
+    countSort(0, sys->n_rows, rowOrder);
     if (nChunks > 1) {
       rowOrderRanged.resize(sys->n_rows);
-      for (int c = 0; c < nChunks; ++c) windowed(plan->outChunkRow[(size_t)c], plan->outChunkRow[(size_t)c + 1], rowOrderRanged);
+      for (int c = 0; c < nChunks; ++c) countSort(plan->outChunkRow[(size_t)c], plan->outChunkRow[(size_t)c + 1], rowOrderRanged);
     }
   }
   if (sys->n_rows >= (uint64_t(1) << 32) || d.nnz >= (uint64_t(1) << 32) || rowElem.size() >= (uint64_t(1) << 32)) {

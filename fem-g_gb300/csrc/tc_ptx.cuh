@@ -108,6 +108,14 @@ __device__ inline bool mbarWait(uint64_t *mbar, uint32_t parity) {
     if (clock64() - t0 > kWaitCycles) return false;
   return true;
 }
+// the same with a caller-given bound in SM cycles; 0 gives up at once
+__device__ inline bool mbarWaitFor(uint64_t *mbar, uint32_t parity, long long cycles) {
+  if (cycles <= 0) return false;
+  const long long t0 = clock64();
+  while (!mbarTryWait(mbar, parity))
+    if (clock64() - t0 > cycles) return false;
+  return true;
+}
 // TMA: the arrival that announces `bytes` of transaction on the barrier,
 // and a 2D tiled load of box {4 floats, 128 rows} at (x, y) completing on it
 __device__ inline void mbarExpectTx(uint64_t *mbar, uint32_t bytes) {

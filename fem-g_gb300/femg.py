@@ -144,6 +144,7 @@ def _bind(L):
         "fg_plan_set_fp64_method": (C.c_int, [P, C.c_int32]),
         "fg_plan_set_accumulate": (C.c_int, [P, C.c_int32]),
         "fg_plan_set_mixed_fused": (C.c_int, [P, C.c_int32]),
+        "fg_set_wait_limit": (C.c_int, [C.c_double]),
         "fg_plan_fused_info": (C.c_int, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "fg_hilbert_order": (C.c_int, [C.c_int32, C.c_uint64, P, P, P, P]),
         "fg_hilbert_numbering": (C.c_int, [C.c_int32, P, C.c_uint64, P, P, P]),
@@ -183,7 +184,7 @@ def _bind(L):
 def exported_symbols():
     """Names bound above (the C ABI of both headers)."""
     return [
-        "fg_plan_create", "fg_plan_create_coupled", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_plan_set_fp64_method", "fg_plan_set_accumulate", "fg_plan_set_mixed_fused", "fg_plan_fused_info", "fg_assemble_fp64", "fg_assemble_mixed",
+        "fg_plan_create", "fg_plan_create_coupled", "fg_plan_destroy", "fg_plan_info", "fg_plan_bind_terms", "fg_plan_set_fp64_method", "fg_plan_set_accumulate", "fg_plan_set_mixed_fused", "fg_plan_fused_info", "fg_set_wait_limit", "fg_assemble_fp64", "fg_assemble_mixed",
         "fg_assemble_fp64_static", "fg_assemble_multi_freq", "fg_assemble_separate", "fg_batch_create", "fg_batch_run", "fg_batch_destroy", "fg_batch_tuning", "fg_pattern_build", "fg_hilbert_order", "fg_hilbert_numbering", "fg_profile_enable",
         "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",

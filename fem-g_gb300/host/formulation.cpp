@@ -31,7 +31,7 @@ bool Domain::have(int dim, int tag) const {
 
 int FunctionSpace::keysPerElement(int elementType) const {
   if (type == SpaceType::Lagrange) return elementNodes(elementType);
-  if (type == SpaceType::HCurl) return whitneyCount(elementDim(elementType));
+  if (type == SpaceType::HCurl) return hcurlCount(elementDim(elementType), order);
   const int dim = elementDim(elementType);
   if (dim == 1) return 2 + (order - 1);
   return hierarchicalCount(dim, order);
@@ -66,16 +66,48 @@ void FunctionSpace::getKeys(const Mesh &mesh, const ElementBlock &blk, bool with
       }
     return;
   }
-  if (type == SpaceType::HCurl) {  // one key per edge: (1, edge tag) at the edge midpoint
+  if (type == SpaceType::HCurl) {
+    // per edge (1 + k, edge tag) at the edge midpoint, k < 1 + order; order 1
+    // adds per face (3 + k, face tag) at the face centroid, k < 2 (in 2D the
+    // element's own interior functions: (3 + k, element tag) at its centroid)
+    const int perEdge = order == 0 ? 1 : 2;
     for (int64_t e = 0; e < E; ++e) {
       const int64_t *v = &blk.nodes[(size_t)(e * nn)];
       for (auto &ed : simplexEdges(dim)) {
         double mid[3];
         for (int c = 0; c < 3; ++c) mid[c] = 0.5 * (mesh.xyz[3 * v[ed[0]] + c] + mesh.xyz[3 * v[ed[1]] + c]);
-        typeKeys.push_back(1);
-        entityKeys.push_back((uint64_t)mesh.edgeTagOf(v[ed[0]], v[ed[1]]));
-        pushCoord(mid);
-        if (infoDim) infoDim->push_back(1);
+        const int64_t tag = mesh.edgeTagOf(v[ed[0]], v[ed[1]]);
+        for (int k = 0; k < perEdge; ++k) {
+          typeKeys.push_back(1 + k);
+          entityKeys.push_back((uint64_t)tag);
+          pushCoord(mid);
+          if (infoDim) infoDim->push_back(1);
+        }
+      }
+      if (order == 0) continue;
+      if (dim == 2) {
+        double cen[3] = {0, 0, 0};
+        for (int a = 0; a < nv; ++a)
+          for (int c = 0; c < 3; ++c) cen[c] += mesh.xyz[3 * v[a] + c] / nv;
+        for (int k = 0; k < 2; ++k) {
+          typeKeys.push_back(3 + k);
+          entityKeys.push_back((uint64_t)blk.tags[(size_t)e]);
+          pushCoord(cen);
+          if (infoDim) infoDim->push_back(2);
+        }
+      } else {
+        for (auto &fc : simplexFaces(3)) {
+          const int64_t tag = mesh.faceTagOf(v[fc[0]], v[fc[1]], v[fc[2]]);
+          double fcen[3];
+          for (int c = 0; c < 3; ++c)
+            fcen[c] = (mesh.xyz[3 * v[fc[0]] + c] + mesh.xyz[3 * v[fc[1]] + c] + mesh.xyz[3 * v[fc[2]] + c]) / 3.0;
+          for (int k = 0; k < 2; ++k) {
+            typeKeys.push_back(3 + k);
+            entityKeys.push_back((uint64_t)tag);
+            pushCoord(fcen);
+            if (infoDim) infoDim->push_back(2);
+          }
+        }
       }
     }
     return;
@@ -153,7 +185,7 @@ int FunctionSpace::basisFunctions(bool derivative, const Mesh &mesh, const Eleme
   }
   const int dim = elementDim(blk.type);
   const bool hcurl = type == SpaceType::HCurl;
-  const int n = hcurl ? whitneyCount(dim) : hierarchicalCount(dim, order);
+  const int n = hcurl ? hcurlCount(dim, order) : hierarchicalCount(dim, order);
   const int nn = blk.nodesPerElement;
   const int nv = elementVertices(blk.type);
   // raw orientation per element, then the dense numbering of first
@@ -163,7 +195,7 @@ int FunctionSpace::basisFunctions(bool derivative, const Mesh &mesh, const Eleme
   for (int64_t e = 0; e < E; ++e) {
     int64_t tags[4];
     for (int a = 0; a < nv; ++a) tags[a] = blk.nodes[(size_t)(e * nn + a)] + 1;
-    const int code = orientationFree() ? 0 : (hcurl ? whitneyOrientation(dim, tags) : hierarchicalOrientation(dim, tags));
+    const int code = orientationFree() ? 0 : (hcurl ? hcurlOrientation(dim, order, tags) : hierarchicalOrientation(dim, tags));
     auto it = denseOf.find(code);
     if (it == denseOf.end()) {
       it = denseOf.emplace(code, (int)unique.size()).first;
@@ -176,7 +208,7 @@ int FunctionSpace::basisFunctions(bool derivative, const Mesh &mesh, const Eleme
   for (int o = 0; o < nOrient; ++o)
     for (int q = 0; q < rule.nq; ++q) {
       if (hcurl) {  // values [n][3], curls [n][3]
-        whitneyBasis(dim, unique[o], &rule.points[3 * q], val.data(), grad.data());
+        hcurlBasis(dim, order, unique[o], &rule.points[3 * q], val.data(), grad.data());
         for (int i = 0; i < n; ++i)
           for (int c = 0; c < 3; ++c) table.push_back(derivative ? grad[3 * i + c] : val[3 * i + c]);
         continue;

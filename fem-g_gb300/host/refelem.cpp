@@ -236,6 +236,74 @@ void whitneyBasis(int dim, int code, const double *uvw, double *val, double *cur
   }
 }
 
+int hcurlCount(int dim, int p) {
+  if (p == 0) return whitneyCount(dim);
+  if (p != 1) throw std::invalid_argument("hierarchical HCurl: orders 0 and 1");
+  return 2 * (int)simplexEdges(dim).size() + 2 * (dim == 3 ? 4 : 1);
+}
+
+int hcurlOrientation(int dim, int p, const int64_t *tags) {
+  return p == 0 ? whitneyOrientation(dim, tags) : hierarchicalOrientation(dim, tags);
+}
+
+void hcurlBasis(int dim, int p, int code, const double *uvw, double *val, double *curl) {
+  if (p == 0) {
+    whitneyBasis(dim, code, uvw, val, curl);
+    return;
+  }
+  VG lam[4];
+  barycentric(dim, uvw, lam);
+  auto cross = [](const double *x, const double *y, double *z) {
+    z[0] = x[1] * y[2] - x[2] * y[1];
+    z[1] = x[2] * y[0] - x[0] * y[2];
+    z[2] = x[0] * y[1] - x[1] * y[0];
+  };
+  int idx = 0;
+  // w_ab and its curl 2 grad(lambda_a) x grad(lambda_b)
+  auto whitney = [&](int a, int b, double *w, double *cw) {
+    for (int c = 0; c < 3; ++c) w[c] = lam[a].v * lam[b].g[c] - lam[b].v * lam[a].g[c];
+    cross(lam[a].g, lam[b].g, cw);
+    for (int c = 0; c < 3; ++c) cw[c] *= 2.0;
+  };
+  const auto &edges = simplexEdges(dim);
+  for (size_t e = 0; e < edges.size(); ++e) {
+    int a = edges[e][0], b = edges[e][1];
+    if ((code >> e) & 1) std::swap(a, b);
+    whitney(a, b, &val[3 * idx], &curl[3 * idx]);
+    ++idx;
+    for (int c = 0; c < 3; ++c) {
+      val[3 * idx + c] = lam[a].v * lam[b].g[c] + lam[b].v * lam[a].g[c];
+      curl[3 * idx + c] = 0.0;
+    }
+    ++idx;
+  }
+  // lambda_c w_ab
+  auto faceFn = [&](int a, int b, int c) {
+    double w[3], cw[3], gx[3];
+    whitney(a, b, w, cw);
+    cross(lam[c].g, w, gx);
+    for (int k = 0; k < 3; ++k) {
+      val[3 * idx + k] = lam[c].v * w[k];
+      curl[3 * idx + k] = gx[k] + lam[c].v * cw[k];
+    }
+    ++idx;
+  };
+  if (dim == 2) {
+    faceFn(0, 1, 2);
+    faceFn(1, 2, 0);
+    return;
+  }
+  int digits = code >> edges.size();
+  const auto &faces = simplexFaces(3);
+  for (size_t f = 0; f < faces.size(); ++f) {
+    const int *s = kPerm3[digits % 6];
+    digits /= 6;
+    const int s0 = faces[f][s[0]], s1 = faces[f][s[1]], s2 = faces[f][s[2]];
+    faceFn(s0, s1, s2);
+    faceFn(s1, s2, s0);
+  }
+}
+
 void hierarchicalBasis(int dim, int p, int code, const double *uvw, double *val, double *grad) {
   VG lam[4];
   barycentric(dim, uvw, lam);

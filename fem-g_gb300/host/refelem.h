@@ -1,5 +1,5 @@
 // Reference-element data: quadrature rules, geometric (Lagrange) basis, the
-// hierarchical H1 basis with orientations and the lowest-order HCurl basis.
+// hierarchical H1 basis with orientations and the hierarchical HCurl basis of orders 0 and 1.
 //
 // In the reference these come from gmsh:
 //  - quadrature: gmsh::model::mesh::getIntegrationPoints(type, "GaussN") via
@@ -55,6 +55,24 @@ int whitneyCount(int dim);
 int whitneyOrientation(int dim, const int64_t *vertexTags);
 // values [n][3] and curls [n][3] for an orientation code
 void whitneyBasis(int dim, int orientationCode, const double *uvw, double *val, double *curl);
+
+// Hierarchical HCurl of order p = 0 or 1 (the reference's
+// FunctionSpaceHierarchicalHCurl, gmsh "HcurlLegendre<p>"): order 0 is
+// whitneyBasis; order 1 spans the first-kind Nedelec space of degree 2 with,
+// per edge (a, b) directed from the lower global tag to the higher,
+//   w_ab and grad(lambda_a lambda_b)  (curl 0),
+// and per face with vertices s0 < s1 < s2 in global tag order (3D; the
+// triangle's own vertex order in 2D, where they are interior bubbles)
+//   lambda_s2 w_s0s1 and lambda_s0 w_s1s2,
+//   curl(lambda_c w_ab) = grad(lambda_c) x w_ab + 2 lambda_c grad(lambda_a) x grad(lambda_b).
+// The face functions vanish tangentially on every edge, so the basis is
+// conforming (tangential continuity) across elements. Orientation codes:
+// whitneyOrientation for p = 0, hierarchicalOrientation for p = 1.
+int hcurlCount(int dim, int p);
+int hcurlOrientation(int dim, int p, const int64_t *vertexTags);
+// values [n][3] and curls [n][3]; functions ordered edge by edge (w, grad),
+// then face by face (two each)
+void hcurlBasis(int dim, int p, int orientationCode, const double *uvw, double *val, double *curl);
 
 // Legendre polynomial P_k and derivative
 void legendre(int k, double x, double &p, double &dp);

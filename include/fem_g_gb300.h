@@ -272,6 +272,14 @@ int fg_plan_create_coupled(const fg_mesh_desc *mesh, const fg_rule_desc *rule, c
                            const fg_system_desc *sys, const fg_space_desc *unknown_space,
                            const uint64_t *unknown_dof_idx, const int32_t *unknown_dof_type, fg_plan **out);
 void fg_plan_destroy(fg_plan *plan);
+/* Bound on the tensor-core contraction's wait for each chain of MMAs, in
+ * seconds (default about 2; process-wide, read at each launch, and at capture
+ * time by batch graphs). When a wait runs out, the kernel records a timeout,
+ * waits once more (bounded) for the MMAs it issued to retire, frees its TMEM
+ * and returns; the call (host outputs) or the next call on the plan (device
+ * outputs) returns FG_ERR_TIMEOUT and the device stays usable. 0 makes the
+ * first wait give up at once, which tests that path. */
+int fg_set_wait_limit(double seconds);
 /* plan statistics: nnz, elements, element DOFs, quadrature points, orientations */
 int fg_plan_info(const fg_plan *plan, int64_t *nnz, int64_t *n_elements, int32_t *n_dofs, int32_t *nq, int32_t *n_orient);
 

@@ -5,7 +5,7 @@
 // reference's Formulation::pre() and assemble() reach, over one in-memory
 // model installed by oracleShimSetMesh(): this project's synthetic simplex
 // meshes (fem-g_gb300/host/mesh.cpp), its quadrature rules, geometric
-// Lagrange basis, hierarchical H1 and lowest-order HCurl bases and DOF keys
+// Lagrange basis, hierarchical H1 and hierarchical HCurl (orders 0, 1) bases and DOF keys
 // (fem-g_gb300/host/refelem.cpp, formulation.cpp). These are the same tables
 // the GPU path's host mirror hands to the C ABI, so the reference's own DOF
 // creation, numbering, pattern, element integration and scatter run on
@@ -101,10 +101,13 @@ femg::FunctionSpace parseSpace(const std::string &name, bool *derivative) {
   } else if (name.rfind("H1Legendre", 0) == 0) {
     fs.type = femg::SpaceType::HierarchicalH1;
     fs.order = num("H1Legendre");
-  } else if (name == "HcurlLegendre0" || name == "CurlHcurlLegendre0") {
+  } else if (name.rfind("CurlHcurlLegendre", 0) == 0) {
     fs.type = femg::SpaceType::HCurl;
-    fs.order = 0;
-    *derivative = name[0] == 'C';
+    fs.order = num("CurlHcurlLegendre");
+    *derivative = true;
+  } else if (name.rfind("HcurlLegendre", 0) == 0) {
+    fs.type = femg::SpaceType::HCurl;
+    fs.order = num("HcurlLegendre");
   } else {
     throw std::runtime_error("gmsh stand-in: function space " + name + " is not available");
   }
@@ -117,7 +120,7 @@ int orientationOf(const femg::FunctionSpace &fs, const femg::ElementBlock &blk, 
   const int nv = femg::elementVertices(blk.type);
   int64_t tags[4];
   for (int a = 0; a < nv; ++a) tags[a] = blk.nodes[(size_t)(e * blk.nodesPerElement + a)] + 1;
-  return fs.type == femg::SpaceType::HCurl ? femg::whitneyOrientation(dim, tags) : femg::hierarchicalOrientation(dim, tags);
+  return fs.type == femg::SpaceType::HCurl ? femg::hcurlOrientation(dim, fs.order, tags) : femg::hierarchicalOrientation(dim, tags);
 }
 
 // reference coordinates of the geometric nodes (vertices, then the edge
@@ -430,7 +433,7 @@ int getNumberOfOrientations(const int elementType, const std::string &functionSp
   const int dim = femg::elementDim(elementType);
   int n = 1;
   for (size_t k = 0; k < femg::simplexEdges(dim).size(); ++k) n *= 2;  // edge reversal bits
-  if (dim == 3 && fs.type != femg::SpaceType::HCurl)
+  if (dim == 3 && !(fs.type == femg::SpaceType::HCurl && fs.order == 0))
     for (int f = 0; f < 4; ++f) n *= 6;  // face permutations
   return n;
 }
@@ -462,12 +465,12 @@ void getBasisFunctions(const int elementType, const std::vector<double> &localCo
     return;
   }
   if (fs.type == femg::SpaceType::HCurl) {
-    const int n = femg::whitneyCount(dim);
+    const int n = femg::hcurlCount(dim, fs.order);
     numComponents = 3;
     std::vector<double> val(3 * n), curl(3 * n);
     for (int code : orient)
       for (int q = 0; q < nq; ++q) {
-        femg::whitneyBasis(dim, code, &localCoord[3 * q], val.data(), curl.data());
+        femg::hcurlBasis(dim, fs.order, code, &localCoord[3 * q], val.data(), curl.data());
         for (int i = 0; i < n; ++i)
           for (int c = 0; c < 3; ++c) basisFunctions.push_back(derivative ? curl[3 * i + c] : val[3 * i + c]);
       }

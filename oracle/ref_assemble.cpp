@@ -387,7 +387,7 @@ int main(int argc, char **argv) {
       }
       run(formulation, repeats, w, u, v);
     } else if (c.kind == FG_PROBLEM_MAXWELL) {
-      field::Field<T, field::Form::Form1> u("u", omega, field::FunctionSpaceTypeForm1::HierarchicalHCurl, 0);
+      field::Field<T, field::Form::Form1> u("u", omega, field::FunctionSpaceTypeForm1::HierarchicalHCurl, c.order);
       problem::Formulation<T> formulation("maxwell", matrixOptions);
       formulation.integral(equation::curl(equation::dof(u)), equation::curl(equation::tf(u)), omega, gauss);
       if (c.coef_mode == FG_COEF_MODE_CONSTANT) {

@@ -56,3 +56,27 @@ def test_batch_with_hcurl_and_h1(femg, oracle, cuda):
             ref, _ = oracle.assemble(p.arrays(), t, nt)
             assert rel(v, ref) <= tol
         batch.close()
+
+
+# order 1 (HcurlLegendre1): 8 functions per triangle, 20 per tet
+ORDER1 = {"tri_m6": (2, 6, 1), "tet_m3": (3, 3, 0), "tet_m8_percell": (3, 8, 1)}
+
+
+@pytest.mark.parametrize("case", list(ORDER1))
+@pytest.mark.parametrize("precision", ["fp64", "fp64_factored", "mixed"])
+def test_maxwell_order1_matches_oracle(femg, oracle, cuda, case, precision):
+    from test_hcurl_order1 import maxwell1
+    dim, m, mode = ORDER1[case]
+    prob = femg.Problem(maxwell1(femg, dim, m, coef_mode=mode))
+    a = prob.arrays()
+    t, nt = prob.terms()
+    ref_v, _ = oracle.assemble(a, t, nt)
+    plan = prob.plan()
+    if precision == "mixed":
+        v, _, rep = plan.assemble("mixed", report=True)
+        assert rep["global_"] <= 1e-6
+    else:
+        if precision == "fp64_factored":
+            plan.set_fp64_method(femg.FG_FP64_FACTORED)
+        v, _ = plan.assemble("fp64")
+    assert rel(v, ref_v) <= (1e-6 if precision == "mixed" else 1e-12)
