@@ -407,6 +407,11 @@ struct GemmSched {
   int *err;
   int tma;           // A tiles by TMA through aMap (one problem), else by cp.async
   long long mmaWaitCycles;  // bound of the wait for an MMA chain (fg_set_wait_limit)
+  // dynamic schedule (batches): CTAs take `chunk` consecutive tiles at a time
+  // from the counter `next` (zeroed before the launch) until nTiles; null:
+  // the static ranges of ctaStart
+  int *next;
+  int nTiles, chunk;
 };
 
 
@@ -559,9 +564,23 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
   uint32_t aParity = 0, aPending = 0;  // per A buffer: completion parity, load in flight
   uint32_t bParity = 0, bPending = 0;  // the B image: completion parity, load in flight
   bool failed = false;
-  const int t0 = sc.ctaStart[blockIdx.x], t1 = sc.ctaStart[blockIdx.x + 1];
-  if (t0 < t1) {
-    const int4 T = sc.tiles[t0];
+  // the tiles of this CTA: [t, ce) is the current chunk. Static: one chunk,
+  // the CTA's range. Dynamic: chunks taken from the counter; the next one is
+  // taken while the current chunk's last tile runs (sGrab, written by thread
+  // 0 and read by all after the barrier that follows in the same tile).
+  __shared__ int sGrab;
+  int t, ce;
+  if (sc.next) {
+    if (tid == 0) sGrab = atomicAdd(sc.next, sc.chunk);
+    __syncthreads();
+    t = sGrab;
+    ce = min(t + sc.chunk, sc.nTiles);
+  } else {
+    t = sc.ctaStart[blockIdx.x];
+    ce = sc.ctaStart[blockIdx.x + 1];
+  }
+  if (t < ce) {
+    const int4 T = sc.tiles[t];
     if (tid == 0) gs = sc.probs[T.x];
     __syncthreads();
     loadB(gs, Bs, T.y, tid, bBar);
@@ -569,9 +588,10 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
     issueATile(sc, gs, As0, T.z, T.w, tid, &aBar[0]);
     aPending |= 1u;
   }
-  for (int t = t0, it = 0; t < t1 && !failed; ++t, ++it) {
+  for (int it = 0; t < ce && !failed; ++it) {
     const int buf = it & 1;
     const int4 T = sc.tiles[t];
+    if (sc.next && t + 1 == ce && tid == 0) sGrab = atomicAdd(sc.next, sc.chunk);
     const int o = T.y, row0 = T.z, nrows = T.w;
     const uint32_t aAddr = smemAddr(As0 + buf * kBM * gs.K3);
     const uint32_t bLbo = (uint32_t)gs.Npad * 16u;  // K-adjacent core matrices of B
@@ -599,11 +619,22 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
     }
     fenceProxyAsync();  // cp.async A tiles (generic proxy) before the MMAs read them
     __syncthreads();
-    // prefetch the next tile's A when it shares this B image
-    const int tn = t + 1;
+    // the next tile (in this chunk, or the first of the next one taken), and
+    // the prefetch of its A when it shares this B image
+    int tn, ceN;
+    if (t + 1 < ce) {
+      tn = t + 1;
+      ceN = ce;
+    } else if (sc.next) {
+      tn = sGrab;
+      ceN = min(tn + sc.chunk, sc.nTiles);
+    } else {
+      tn = ceN = 0;
+    }
+    const bool hasNext = tn < ceN;
     int4 Tn = make_int4(-1, -1, 0, 0);
-    if (tn < t1) Tn = sc.tiles[tn];
-    const bool nextSameB = tn < t1 && Tn.x == T.x && Tn.y == o;
+    if (hasNext) Tn = sc.tiles[tn];
+    const bool nextSameB = hasNext && Tn.x == T.x && Tn.y == o;
     const int r = quad * 32 + lane;
     const bool live = r < nrows;
     const int grow = row0 + r;
@@ -647,7 +678,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
       tcFenceBefore();
       __syncthreads();
     }
-    if (!failed && tn < t1 && !nextSameB) {
+    if (!failed && hasNext && !nextSameB) {
       // problem or orientation change: the MMAs are done with Bs, reload it and the next A
       if (tid == 0 && Tn.x != T.x) gs = sc.probs[Tn.x];
       __syncthreads();
@@ -656,6 +687,8 @@ __global__ void __launch_bounds__(kThreadsGemm, 2)
       issueATile(sc, gs, As0 + (buf ^ 1) * kBM * gs.K3, Tn.z, Tn.w, tid, &aBar[buf ^ 1]);
       aPending |= 1u << (buf ^ 1);
     }
+    t = tn;
+    ce = ceN;
   }
   cpAsyncWaitAll();
   if (failed) {
@@ -899,7 +932,7 @@ static std::atomic<long long> g_mmaWaitCycles{kWaitCycles};
 
 // One contraction launch over the tiles of one or many problems
 int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ctaStartDev, int nCta, int *err, int maxK3,
-                   size_t smem, cudaStream_t s, int tmemCols, const void *aMap) {
+                   size_t smem, cudaStream_t s, int tmemCols, const void *aMap, int *next, int nTiles, int chunk) {
   static SmemAllowance allowed;
   FG_CUDA(allowSmem(k_contract_tf32x3, smem, allowed));
   GemmSched sc;
@@ -913,6 +946,12 @@ int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ct
   sc.ctaStart = ctaStartDev;
   sc.err = err;
   sc.mmaWaitCycles = g_mmaWaitCycles.load();
+  if (next) {
+    FG_CUDA(cudaMemsetAsync(next, 0, sizeof(int), s));
+    sc.next = next;
+    sc.nTiles = nTiles;
+    sc.chunk = std::max(1, chunk);
+  }
   ProfScope prof("k_contract_tf32x3", s);
   k_contract_tf32x3<<<std::max(1, nCta), kThreadsGemm, smem, s>>>(sc, maxK3, tmemCols);
   countLaunch();

@@ -19,6 +19,7 @@
 // graph; later runs update the output pointers in the device-side job tables
 // and launch the graph.
 #include <algorithm>
+#include <numeric>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -40,6 +41,8 @@ using namespace femg;
   } while (0)
 
 namespace {
+
+constexpr int kTileChunk = 8;  // tiles per take of the dynamic contraction schedule
 
 struct GatherClass {
   int dim = 0, nn = 0, n = 0, nq = 0, slotBytes = 1, kcplx = 0;
@@ -101,6 +104,7 @@ struct fg_batch {
   // contraction cost of one tile of problem q (CTA-milliseconds), measured
   // per class by the tuner; empty: the analytic estimate
   std::vector<double> tileCost;
+  int *tileNext = nullptr;  // tile counter of the dynamic contraction schedule
   int *err = nullptr;
   int *errHost = nullptr;
   cudaEvent_t errEvent = nullptr;
@@ -169,7 +173,9 @@ int runElements(fg_batch *b, cudaStream_t s) {
         if ((st = launchRhsFp64(b->plans[q], b->termsDev[q], b->plans[q]->be, s))) return st;
     if ((st = launchFactorsBatch(b->factorJobs, b->n, b->totalElems, s))) return st;
     if (!b->tilesHost.empty())
-      if ((st = launchContract(b->gemmDev, b->tiles, b->ctaStart, b->nCta, b->err, b->maxK3, b->smem, s))) return st;
+      if ((st = launchContract(b->gemmDev, b->tiles, b->ctaStart, b->nCta, b->err, b->maxK3, b->smem, s, 512, nullptr,
+                               b->tileNext, (int)b->tilesHost.size(), kTileChunk)))
+        return st;
     return FG_OK;
   }
   for (int q = 0; q < b->n; ++q) {
@@ -199,7 +205,13 @@ int buildGemmSchedule(fg_batch *b, const std::vector<int> *only, int4 **tiles, i
   hostTiles->clear();
   std::vector<double> cost;
   const bool measured = !only && (int)b->tileCost.size() == b->n;
-  for (int q = 0; q < b->n; ++q) {
+  // the final schedule takes its tiles dynamically: the costliest first, so
+  // that the cheap ones even out the end
+  std::vector<int> order(b->n);
+  std::iota(order.begin(), order.end(), 0);
+  if (measured)
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->tileCost[x] > b->tileCost[y]; });
+  for (int q : order) {
     if (only && std::find(only->begin(), only->end(), q) == only->end()) continue;
     std::vector<int4> t = mixedTiles(b->plans[q], q, b->gemmHost[q].rowsPerElem);
     const double full = measured ? b->tileCost[q] : (double)b->gemmHost[q].Npad * b->gemmHost[q].K3 + 256.0;
@@ -368,6 +380,7 @@ extern "C" void fg_batch_destroy(fg_batch *b) {
   cudaFree(b->gemmDev);
   cudaFree(b->tiles);
   cudaFree(b->ctaStart);
+  cudaFree(b->tileNext);
   cudaFree(b->err);
   if (b->errHost) cudaFreeHost(b->errHost);
   if (b->errEvent) cudaEventDestroy(b->errEvent);
@@ -531,6 +544,7 @@ extern "C" int fg_batch_create(fg_plan *const *plans, const fg_term_desc *const 
     if ((st = uploadGemmProblems(b))) return fail(st);
     if ((st = buildGemmSchedule(b, nullptr, &b->tiles, &b->ctaStart, &b->nCta, &b->tilesHost))) return fail(st);
     if (cudaMalloc(&b->err, sizeof(int)) != cudaSuccess) return fail(FG_ERR_OOM);
+    if (cudaMalloc(&b->tileNext, sizeof(int)) != cudaSuccess) return fail(FG_ERR_OOM);
     FG_CUDA_RET(cudaMemset(b->err, 0, sizeof(int)), fail);
     if (cudaMallocHost(&b->errHost, sizeof(int)) != cudaSuccess) return fail(FG_ERR_OOM);
     *b->errHost = 0;

@@ -337,8 +337,12 @@ std::vector<int4> mixedTiles(fg_plan *plan, int prob, int rowsPerElem);
 int gemmCtasPerSm(int Npad, int k3);
 size_t gemmSmem(int Npad, int k3, int ctasPerSm = 1);
 std::vector<int32_t> partitionTiles(const std::vector<double> &cost, int nCta);
+// next: the tile counter of a dynamic schedule (chunks of `chunk` tiles out
+// of nTiles; zeroed on the stream before the launch), or null for the
+// static ranges of ctaStartDev
 int launchContract(const void *probsDev, const int4 *tilesDev, const int32_t *ctaStartDev, int nCta, int *err, int maxK3,
-                   size_t smem, cudaStream_t s, int tmemCols = 512, const void *aMap = nullptr);
+                   size_t smem, cudaStream_t s, int tmemCols = 512, const void *aMap = nullptr, int *next = nullptr,
+                   int nTiles = 0, int chunk = 0);
 GemmProblem mixedGemmProblem(fg_plan *plan);
 
 // ------------------------------------------------------------- device helpers

@@ -422,7 +422,7 @@ static int prepareFused(fg_plan *plan) {
   const uint64_t nRows = p.nRows;
   std::vector<uint64_t> rowPtr(nRows + 1);
   std::vector<uint32_t> rowElem;
-  std::vector<uint8_t> slot((size_t)E * n * n);
+  std::vector<uint8_t> slot((size_t)E * n * p.slotLd);
   std::vector<int32_t> orient((size_t)E, 0);
   FG_CUDA(cudaMemcpy(rowPtr.data(), p.rowPtr, rowPtr.size() * 8, cudaMemcpyDeviceToHost));
   rowElem.resize(rowPtr[nRows]);
@@ -520,7 +520,7 @@ static int prepareFused(fg_plan *plan) {
         const uint32_t pidx = pairBase[u] + (uint32_t)__builtin_popcount(need[u] & ((1u << i) - 1u));
         pairs[k2++] = (uint16_t)pidx;
         flat[pidx] = e * (uint32_t)n + i;
-        std::memcpy(slots + (size_t)pidx * n, &slot[((size_t)e * n + i) * n], (size_t)n);
+        std::memcpy(slots + (size_t)pidx * n, &slot[((size_t)e * n + i) * p.slotLd], (size_t)n);
       }
     }
     rowPair[R] = (uint16_t)k2;

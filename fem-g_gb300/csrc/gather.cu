@@ -200,7 +200,7 @@ __device__ __forceinline__ void gatherRowsV4(const PlanDev &p, const float *__re
         const uint32_t e = packed >> 6, i = packed & 63;
         f_ = e * (uint32_t)n + i;
         kv_ = *reinterpret_cast<const float4 *>(ke + (size_t)e * nn2 + (size_t)i * n + 4 * lt);
-        sv_ = *reinterpret_cast<const uint32_t *>(slot + (size_t)f_ * n + 4 * lt);
+        sv_ = *reinterpret_cast<const uint32_t *>(slot + (size_t)f_ * p.slotLd + 4 * lt);
       } else {
         kv_ = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         sv_ = 0xFEFEFEFEu;  // ignore

@@ -404,7 +404,10 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   d.maxRowLen = (int32_t)maxLen;
   const bool narrow = maxLen < 0xFE;
   d.slotBytes = narrow ? 1 : 2;
-  const int nS = nc;
+  // one-byte slot rows of 17 to 32 entries take a whole 32-byte sector each:
+  // an element row's slots then come in one sector instead of straddling two
+  // (the padding reads as "ignore")
+  const int nS = (narrow && nc > 16 && nc <= 32) ? 32 : nc;
   d.slotLd = nS;
   const size_t nSlots = (size_t)E * n * nS;
   std::vector<uint8_t> slot8;
@@ -449,6 +452,9 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
     setLastError("fg_plan_create: an element DOF pair is missing from the CSR pattern");
     return FG_ERR_INDEX;
   }
+  if (nS > nc)
+    for (size_t r = 0; r < (size_t)E * n; ++r)
+      std::fill(slot8.begin() + (int64_t)(r * nS + nc), slot8.begin() + (int64_t)((r + 1) * nS), (uint8_t)0xFE);
 
   int st;
   if ((st = upload(plan, mesh->node_xyz, (size_t)mesh->n_nodes * 3, &d.xyz))) return st;

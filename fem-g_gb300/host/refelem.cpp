@@ -135,6 +135,42 @@ void legendre(int k, double x, double &p, double &dp) {
     dp = k * (x * p1 - p0) / (x * x - 1.0);
 }
 
+// The 24-point rule of degree 6 on the tetrahedron with three orbits of
+// (a, a, a, 1 - 3a) and one of (a, a, b, 1 - 2a - b) in barycentric
+// coordinates, all weights positive and all points inside (P. Keast, Comput.
+// Methods Appl. Mech. Eng. 55, 1986, rule 6). The parameters below solve its
+// moment equations (exact for every monomial of degree <= 6) to 25 digits;
+// fem-g_gb300/host/tet_rule6.py recomputes them. Weights are for the
+// reference tetrahedron of volume 1/6.
+static QuadRule keastTet6() {
+  static const double s31[3][2] = {{0.04067395853461135311557945, 0.001679535175886773824668873},
+                                   {0.2146028712591520292888392, 0.006653791709694582016615105},
+                                   {0.3223378901422755103439945, 0.009226196923942453682525546}};
+  const double a = 0.06366100187501752529923553, b = 0.6030056647916491413674311, w211 = 0.008035714285714285714285714;
+  QuadRule r;
+  auto add = [&](const double lam[4], double w) {  // reference coordinates (lambda_1, lambda_2, lambda_3)
+    r.points.insert(r.points.end(), {lam[1], lam[2], lam[3]});
+    r.weights.push_back(w);
+  };
+  for (auto &o : s31)
+    for (int k = 0; k < 4; ++k) {
+      double lam[4] = {o[0], o[0], o[0], o[0]};
+      lam[k] = 1.0 - 3.0 * o[0];
+      add(lam, o[1]);
+    }
+  const double c = 1.0 - 2.0 * a - b;
+  for (int i = 0; i < 4; ++i)      // position of b
+    for (int j = 0; j < 4; ++j) {  // position of c
+      if (j == i) continue;
+      double lam[4] = {a, a, a, a};
+      lam[i] = b;
+      lam[j] = c;
+      add(lam, w211);
+    }
+  r.nq = (int)r.weights.size();
+  return r;
+}
+
 QuadRule gaussRule(const std::string &integrationType, int elementType) {
   if (integrationType.rfind("Gauss", 0) != 0) throw std::invalid_argument("unsupported integration type " + integrationType);
   const int N = std::stoi(integrationType.substr(5));
@@ -147,6 +183,7 @@ QuadRule gaussRule(const std::string &integrationType, int elementType) {
     return r;
   }
   if (dim == 1) return gaussLegendreLine(std::max(1, (N + 2) / 2));
+  if (dim == 3 && N == 6) return keastTet6();
   const int s = N <= 1 ? 0 : (N - 1 + 1) / 2;  // smallest s with 2s+1 >= N
   return grundmannMoller(dim, s);
 }

@@ -12,7 +12,9 @@
 // mathematics:
 //  - "GaussN" on a simplex is the Grundmann-Moller rule of odd degree
 //    2*ceil((N-1)/2)+1 >= N (A. Grundmann, H.M. Moller, SIAM J. Numer. Anal. 15,
-//    1978); on a line it is the Gauss-Legendre rule with ceil((N+1)/2) points;
+//    1978), except "Gauss6" on the tetrahedron: the 24-point degree-6 rule of
+//    Keast (1986), the point count of the published tetrahedral tables; on a
+//    line it is the Gauss-Legendre rule with ceil((N+1)/2) points;
 //  - the hierarchical basis is a Legendre-kernel family: vertex functions
 //    lambda_v, edge functions lambda_a lambda_b P_k(lambda_b - lambda_a), face
 //    and interior bubbles built the same way; edges and faces are oriented by
