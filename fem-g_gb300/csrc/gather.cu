@@ -165,7 +165,9 @@ __device__ __forceinline__ void gatherRows(const PlanDev &p, const KT *__restric
 // an element row comes in with one 16-byte load per lane and its slots with
 // one 4-byte load (against 2 n / L scalar loads per lane in k_gather). Same
 // visiting order, same per-entry order (entries separated by __syncwarp),
-// same results.
+// same results. The next row's visit record is loaded while the current row
+// runs, and a row's list entries L at a time, one per lane, so that the loads
+// of an element row depend on a shuffle instead of a list load.
 // The rows of visit records [v0, v1) handled by block blk of nblk.
 template <bool ACC>
 __device__ __forceinline__ void gatherRowsV4(const PlanDev &p, const float *__restrict__ ke, const double2 *__restrict__ be,
@@ -180,12 +182,17 @@ __device__ __forceinline__ void gatherRowsV4(const PlanDev &p, const float *__re
   const int n = p.n, nn2 = n * n;
   const uint8_t *slot = (const uint8_t *)p.slot;
   const int64_t stride = nblk * wpb * R;
+  const int64_t first = v0 + (blk * wpb + warp) * R + sub;
+  uint4 vNext = (laneLive && first < v1) ? p.visit[first] : make_uint4(0, 0, 0, 0);
   for (int64_t base = v0 + (blk * wpb + warp) * R; base < v1; base += stride) {
     const int64_t idx = base + sub;
     const bool live = laneLive && idx < v1;
-    const uint4 v = live ? p.visit[idx] : make_uint4(0, 0, 0, 0);
+    const uint4 v = vNext;  // this row's record, fetched one row ahead
+    vNext = (laneLive && idx + stride < v1) ? p.visit[idx + stride] : make_uint4(0, 0, 0, 0);
     const int len = live ? (int)(v.w & 0xFFFFu) : 0;
     const int cnt = live ? (int)(v.w >> 16) : 0;
+    // the row's (element, local row) list, L entries at a time in the lanes
+    uint32_t myPacked = (lt < cnt) ? p.visitElem[v.z + lt] : 0u;
     for (int s = lt; s < len; s += L) A[s] = 0.0f;
     int maxCnt = cnt;
 #pragma unroll
@@ -194,9 +201,9 @@ __device__ __forceinline__ void gatherRowsV4(const PlanDev &p, const float *__re
     double2 dc = make_double2(0.0, 0.0), bsum = make_double2(0.0, 0.0);
     float4 kv, kvN;
     uint32_t sv, svN, flat = 0, flatN = 0;
-    auto fetch = [&](int k, float4 &kv_, uint32_t &sv_, uint32_t &f_) {
+    const int srcBase = laneLive ? sub * L : 0;
+    auto fetch = [&](int k, uint32_t packed, float4 &kv_, uint32_t &sv_, uint32_t &f_) {
       if (k < cnt) {
-        const uint32_t packed = p.visitElem[v.z + k];
         const uint32_t e = packed >> 6, i = packed & 63;
         f_ = e * (uint32_t)n + i;
         kv_ = *reinterpret_cast<const float4 *>(ke + (size_t)e * nn2 + (size_t)i * n + 4 * lt);
@@ -207,9 +214,12 @@ __device__ __forceinline__ void gatherRowsV4(const PlanDev &p, const float *__re
         f_ = 0;
       }
     };
-    if (maxCnt > 0) fetch(0, kv, sv, flat);
+    if (maxCnt > 0) fetch(0, __shfl_sync(0xffffffffu, myPacked, srcBase), kv, sv, flat);
     for (int k = 0; k < maxCnt; ++k) {
-      if (k + 1 < maxCnt) fetch(k + 1, kvN, svN, flatN);
+      if (k + 1 < maxCnt) {
+        if ((k + 1) % L == 0) myPacked = (k + 1 + lt < cnt) ? p.visitElem[v.z + k + 1 + lt] : 0u;
+        fetch(k + 1, __shfl_sync(0xffffffffu, myPacked, srcBase + (k + 1) % L), kvN, svN, flatN);
+      }
       const float vals[4] = {kv.x, kv.y, kv.z, kv.w};
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
