@@ -49,9 +49,9 @@ METRIC = "element matrices/s and CSR nnz/s: mixed vs FP64 GPU at <=1e-6 rel erro
 # P3 Helmholtz meshes, from ncu captures of the 30^3 x 6 mesh (162,000 tets,
 # 35,811,451 nonzeros); the per-launch traffic of other sizes of that family
 # is this figure times their nonzeros. k_gather: 555.2 MB read + 550.5 MB
-# written; k_gather_v4: 573.9 MB read + 549.2 MB written.
+# written; k_gather_v4: 566.2 MB read + 548.5 MB written.
 GATHER_TRAFFIC_PER_NNZ_P3 = {"k_gather": (555.207680e6 + 550.488064e6) / 35811451,
-                             "k_gather_v4": (573.856768e6 + 549.239040e6) / 35811451}
+                             "k_gather_v4": (566.168064e6 + 548.542976e6) / 35811451}
 
 # FP64-pipe activity of the plain FP64 element kernel (k_element_fp64<8, 0>,
 # the quadrature loop) in an ncu capture on the 30^3 x 6 P3 mesh: the loop is

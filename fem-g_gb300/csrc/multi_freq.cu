@@ -32,6 +32,7 @@ struct MultiIn {
   int realFactor[kMaxGroups];    // the factors of group g are real for every output
   int imagFactor[kMaxGroups];    // ... purely imaginary for every output
   int G, F, R;
+  int anyCplx;                   // some group has an imaginary part: two accumulators per group and slot, else one
   KeLayout lay;                  // element-matrix layout (ld entries per component)
   const double2 *coef;           // [F][G] factors of the value arrays
   const double2 *rcoef;          // [R][G] factors of the liftings in the right-hand sides
@@ -58,7 +59,10 @@ __global__ void __launch_bounds__(256)
   const size_t cfBytes = ((size_t)F * G * 2 * sizeof(AT) + 15) / 16 * 16;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / L, lt = lane % L;
-  const int perSlot = 2 * G;
+  // accumulators per slot: (re, im) per group when some group is complex,
+  // else one real sum per group
+  const int perSlot = in.anyCplx ? 2 * G : G;
+  const int gStep = in.anyCplx ? 2 : 1;
   AT *A = reinterpret_cast<AT *>(smraw + cfBytes) + (size_t)(warp * R + sub) * p.maxRowLen * perSlot;
   const SlotT *slot = (const SlotT *)p.slot;
   const SlotT kFixed = (SlotT)(sizeof(SlotT) == 1 ? 0xFF : kSlotFixed);
@@ -106,8 +110,8 @@ __global__ void __launch_bounds__(256)
               const KT *K = (const KT *)in.ke[g] + e * in.stride[g];
               // distinct slots per lane within an element row; rows are
               // separated by the __syncwarp below, so the adds are ordered
-              atomicAdd(&A[(int)s * perSlot + 2 * g], (AT)K[o]);
-              if (in.cplx[g]) atomicAdd(&A[(int)s * perSlot + 2 * g + 1], (AT)K[nn2 + o]);
+              atomicAdd(&A[(int)s * perSlot + gStep * g], (AT)K[o]);
+              if (in.cplx[g]) atomicAdd(&A[(int)s * perSlot + gStep * g + 1], (AT)K[nn2 + o]);
             }
           } else {
             // lifting with the transposed entry (VectorFactory::addValuesDC)
@@ -129,8 +133,8 @@ __global__ void __launch_bounds__(256)
       AT ar[kMaxGroups], ai[kMaxGroups];
 #pragma unroll
       for (int g = 0; g < kMaxGroups; ++g) {
-        ar[g] = g < G ? A[s * perSlot + 2 * g] : (AT)0;
-        ai[g] = g < G ? A[s * perSlot + 2 * g + 1] : (AT)0;
+        ar[g] = g < G ? A[s * perSlot + gStep * g] : (AT)0;
+        ai[g] = (g < G && in.cplx[g]) ? A[s * perSlot + gStep * g + 1] : (AT)0;
       }
       for (int f = 0; f < F; ++f) {
         AT re = (AT)0, im = (AT)0;
@@ -191,7 +195,7 @@ static int launchMultiTyped(const PlanDev &p, const MultiIn &in, cudaStream_t s)
   const int J = 3;
   const int R = 32 / L;
   const size_t cfBytes = ((size_t)in.F * in.G * 2 * sizeof(KT) + 15) / 16 * 16;
-  const size_t rowBytes = (size_t)std::max(p.maxRowLen, 1) * 2 * in.G * sizeof(KT);
+  const size_t rowBytes = (size_t)std::max(p.maxRowLen, 1) * (in.anyCplx ? 2 : 1) * in.G * sizeof(KT);
   int wpb = 8;
   while (wpb > 1 && cfBytes + rowBytes * R * wpb > 200 * 1024) wpb >>= 1;
   const size_t smem = cfBytes + rowBytes * R * wpb;
@@ -424,6 +428,8 @@ int runGroups(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t
     }
     isFloat = true;
   }
+  in.anyCplx = 0;
+  for (int g = 0; g < G; ++g) in.anyCplx |= in.cplx[g] ? 1 : 0;
   if ((st = launchGatherMulti(plan, in, isFloat, s))) return st;
   if (mixed)
     if ((st = mixedRecordError(plan, s))) return st;
