@@ -183,6 +183,7 @@ struct FullWarpSmem {
   double J0[9], J[9], Jinv[9];
   double det0, det;
   double2 M[9], v[3], m, s;
+  double2 vb[3], sg[3];      // w det c b (vector times dof, tested against gradients), w det f (vector source)
   double G[3][kMaxDofs];     // test functions: physical gradients
   double phi[kMaxDofs];      // and values
   double U[2][3][kMaxDofs];  // unknown functions: M G_j (real, imaginary parts)
@@ -251,8 +252,22 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
           const double2 fc = cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb));
           for (int k = 0; k < 3; ++k) v[k] = cmul(fc, evalExpr(terms->advect[k], e, xq, phq, p.nb));
         }
+        double2 vb[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+        if (terms->vecGradTerm >= 0 && terms->t[terms->vecGradTerm].mod == g) {
+          const DevTerm &T = terms->t[terms->vecGradTerm];
+          const double2 fc = cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb));
+          for (int k = 0; k < 3; ++k) vb[k] = cmul(fc, evalExpr(terms->vecGrad[k], e, xq, phq, p.nb));
+        }
+        double2 sg[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+        if (terms->srcGradTerm >= 0 && terms->t[terms->srcGradTerm].mod == g) {
+          const DevTerm &T = terms->t[terms->srcGradTerm];
+          const double2 fc = evalExpr(T.coef, e, xq, phq, p.nb);
+          for (int k = 0; k < 3; ++k) sg[k] = cmul(fc, evalExpr(terms->srcGrad[k], e, xq, phq, p.nb));
+        }
         for (int k = 0; k < 9; ++k) S.M[k] = make_double2(wd * M[k].x, wd * M[k].y);
         for (int k = 0; k < 3; ++k) S.v[k] = make_double2(wd * v[k].x, wd * v[k].y);
+        for (int k = 0; k < 3; ++k) S.vb[k] = make_double2(wd * vb[k].x, wd * vb[k].y);
+        for (int k = 0; k < 3; ++k) S.sg[k] = make_double2(wd * sg[k].x, wd * sg[k].y);
         S.m = make_double2(wd * cm.x, wd * cm.y);
         S.s = make_double2(wd * f.x, wd * f.y);
       }
@@ -265,8 +280,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         for (int r = 0; r < 3; ++r) S.G[r][i] = S.Jinv[r] * g0 + S.Jinv[3 + r] * g1 + S.Jinv[6 + r] * g2;
         S.phi[i] = ph;
         const int slot = i >> 5;
-        bacc[slot].x += S.s.x * ph;
-        bacc[slot].y += S.s.y * ph;
+        bacc[slot].x += S.s.x * ph + S.sg[0].x * S.G[0][i] + S.sg[1].x * S.G[1][i] + S.sg[2].x * S.G[2][i];
+        bacc[slot].y += S.s.y * ph + S.sg[0].y * S.G[0][i] + S.sg[1].y * S.G[1][i] + S.sg[2].y * S.G[2][i];
       }
       const size_t baseU = ((size_t)oU * p.nq + q) * nU;
       for (int j = lane; j < nU; j += 32) {
@@ -275,10 +290,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         double G[3];
 #pragma unroll
         for (int r = 0; r < 3; ++r) G[r] = S.Jinv[r] * g0 + S.Jinv[3 + r] * g1 + S.Jinv[6 + r] * g2;
+        // U_j = M G_j + vb phi_j: the unknown's vector field, tested against G_i
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-          S.U[0][r][j] = S.M[3 * r].x * G[0] + S.M[3 * r + 1].x * G[1] + S.M[3 * r + 2].x * G[2];
-          if (CPLX) S.U[1][r][j] = S.M[3 * r].y * G[0] + S.M[3 * r + 1].y * G[1] + S.M[3 * r + 2].y * G[2];
+          S.U[0][r][j] = S.M[3 * r].x * G[0] + S.M[3 * r + 1].x * G[1] + S.M[3 * r + 2].x * G[2] + S.vb[r].x * ph;
+          if (CPLX) S.U[1][r][j] = S.M[3 * r].y * G[0] + S.M[3 * r + 1].y * G[1] + S.M[3 * r + 2].y * G[2] + S.vb[r].y * ph;
         }
         S.a[0][j] = S.v[0].x * G[0] + S.v[1].x * G[1] + S.v[2].x * G[2] + S.m.x * ph;
         if (CPLX) S.a[1][j] = S.v[0].y * G[0] + S.v[1].y * G[1] + S.v[2].y * G[2] + S.m.y * ph;

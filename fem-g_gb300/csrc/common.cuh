@@ -107,12 +107,16 @@ struct DevTerms {
   DevExpr tensor[6];   // entries (00, 11, 22, 01, 02, 12) of the grad-grad (curl-curl) term's symmetric tensor
   DevExpr tensorMass[6];  // the same for the mass term's tensor
   // terms with non-symmetric element matrices (scalar H1, FP64 paths)
-  int32_t nonSym;          // a full-tensor or advection term is present
+  int32_t nonSym;          // a full-tensor, advection or vector term is present
   int32_t tensorFullTerm;  // index of the FG_TERM_GRAD_GRAD_TENSOR_FULL term, -1 when none
   int32_t advectTerm;      // index of the FG_TERM_ADVECTION term, -1 when none
+  int32_t vecGradTerm;     // index of the FG_TERM_VECTOR_GRAD_TEST term, -1 when none
+  int32_t srcGradTerm;     // index of the FG_TERM_SOURCE_GRAD term, -1 when none
   int32_t pad2_;
   DevExpr tensorFull[9];   // its D, row-major
   DevExpr advect[3];       // the advection vector b
+  DevExpr vecGrad[3];      // b of integral(b dof(u), grad(tf(u)))
+  DevExpr srcGrad[3];      // f of integral(f, grad(tf(u)))
 };
 
 // Device-resident data of one element bucket

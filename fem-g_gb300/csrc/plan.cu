@@ -759,25 +759,27 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
   out->tensorMassTerm = -1;
   out->tensorFullTerm = -1;
   out->advectTerm = -1;
+  out->vecGradTerm = -1;
+  out->srcGradTerm = -1;
   for (int t = 0; t < nTerms; ++t) {
     const fg_term_desc &src = terms[t];
     DevTerm &dt = out->t[t];
     dt.kind = src.kind;
     dt.dt = src.dt;
-    if (src.kind < FG_TERM_GRAD_GRAD || src.kind > FG_TERM_ADVECTION) {
+    if (src.kind < FG_TERM_GRAD_GRAD || src.kind > FG_TERM_SOURCE_GRAD) {
       setLastError("unknown term kind");
       return FG_ERR_ARG;
     }
-    if ((src.kind == FG_TERM_GRAD_GRAD_TENSOR_FULL || src.kind == FG_TERM_ADVECTION) &&
-        (plan->d.mult != 1 || plan->d.form != FG_FORM_0)) {
-      setLastError("the full-tensor and advection terms need a scalar H1 field");
+    const bool vectorKind = src.kind == FG_TERM_ADVECTION || src.kind == FG_TERM_VECTOR_GRAD_TEST || src.kind == FG_TERM_SOURCE_GRAD;
+    if ((src.kind == FG_TERM_GRAD_GRAD_TENSOR_FULL || vectorKind) && (plan->d.mult != 1 || plan->d.form != FG_FORM_0)) {
+      setLastError("the full-tensor, advection and vector terms need a scalar H1 field");
       return FG_ERR_UNSUPPORTED;
     }
     if (plan->d.coupled && src.kind != FG_TERM_GRAD_GRAD && src.kind != FG_TERM_MASS &&
-        src.kind != FG_TERM_GRAD_GRAD_TENSOR_FULL && src.kind != FG_TERM_ADVECTION) {
-      setLastError(src.kind == FG_TERM_SOURCE
+        src.kind != FG_TERM_GRAD_GRAD_TENSOR_FULL && src.kind != FG_TERM_ADVECTION && src.kind != FG_TERM_VECTOR_GRAD_TEST) {
+      setLastError(src.kind == FG_TERM_SOURCE || src.kind == FG_TERM_SOURCE_GRAD
                        ? "two-field plan: linear terms go to the test field's own plan"
-                       : "two-field plan: grad-grad, mass, full-tensor and advection terms only");
+                       : "two-field plan: grad-grad, mass, full-tensor, advection and vector terms only");
       return FG_ERR_UNSUPPORTED;
     }
     if (src.kind == FG_TERM_ELASTIC && plan->d.mult != 3) {
@@ -806,19 +808,20 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
       dt.factor = make_double2(0.0, -frequency);
       cplx = true;
     } else dt.factor = make_double2(1.0, 0.0);
-    if (src.dt != FG_DT_NONE && src.kind == FG_TERM_SOURCE) {
+    if (src.dt != FG_DT_NONE && (src.kind == FG_TERM_SOURCE || src.kind == FG_TERM_SOURCE_GRAD)) {
       setLastError("a linear term cannot carry a time derivative");
       return FG_ERR_ARG;
     }
     bool sourceComplex = false;  // the right-hand side is always complex
-    int st = devExpr(plan, src.coef, &dt.coef, src.kind == FG_TERM_SOURCE ? &sourceComplex : &cplx, arrays, used);
+    const bool linear = src.kind == FG_TERM_SOURCE || src.kind == FG_TERM_SOURCE_GRAD;
+    int st = devExpr(plan, src.coef, &dt.coef, linear ? &sourceComplex : &cplx, arrays, used);
     if (st) return st;
     if (src.kind == FG_TERM_ELASTIC) {
       st = devExpr(plan, src.coef2, &dt.coef2, &cplx, arrays, used);
       if (st) return st;
       out->hasElastic = 1;
     }
-    if (src.kind == FG_TERM_SOURCE) out->hasSource = 1;
+    if (linear) out->hasSource = 1;
     if (src.kind == FG_TERM_GRAD_GRAD_TENSOR || src.kind == FG_TERM_MASS_TENSOR) {
       const bool gg = src.kind == FG_TERM_GRAD_GRAD_TENSOR;
       int32_t &slot = gg ? out->tensorTerm : out->tensorMassTerm;
@@ -846,6 +849,21 @@ int uploadTerms(fg_plan *plan, const fg_term_desc *terms, int32_t nTerms, double
       DevExpr *D = full ? out->tensorFull : out->advect;
       for (int k = 0; k < (full ? 9 : 3); ++k) {
         st = devExpr(plan, src.tensor[k], &D[k], &cplx, arrays, used);
+        if (st) return st;
+      }
+      out->nonSym = 1;
+    }
+    if (src.kind == FG_TERM_VECTOR_GRAD_TEST || src.kind == FG_TERM_SOURCE_GRAD) {
+      const bool lin = src.kind == FG_TERM_SOURCE_GRAD;
+      int32_t &slot = lin ? out->srcGradTerm : out->vecGradTerm;
+      if (slot >= 0 || !src.tensor) {
+        setLastError(src.tensor ? "at most one vector term of each kind per assembly" : "vector term without its vector");
+        return FG_ERR_ARG;
+      }
+      slot = t;
+      DevExpr *V = lin ? out->srcGrad : out->vecGrad;
+      for (int k = 0; k < 3; ++k) {
+        st = devExpr(plan, src.tensor[k], &V[k], lin ? &sourceComplex : &cplx, arrays, used);
         if (st) return st;
       }
       out->nonSym = 1;

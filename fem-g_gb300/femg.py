@@ -17,7 +17,7 @@ HOST_LIB_PATH = os.path.join(HERE, "_build", "libfemg_host.so")
 
 FG_OK, FG_ERR_ARG, FG_ERR_OOM, FG_ERR_CUDA, FG_ERR_INDEX, FG_ERR_TIMEOUT, FG_ERR_UNSUPPORTED, FG_ERR_NO_DEVICE = range(8)
 (FG_TERM_GRAD_GRAD, FG_TERM_MASS, FG_TERM_ELASTIC, FG_TERM_SOURCE, FG_TERM_GRAD_GRAD_TENSOR, FG_TERM_MASS_TENSOR,
- FG_TERM_GRAD_GRAD_TENSOR_FULL, FG_TERM_ADVECTION) = range(8)
+ FG_TERM_GRAD_GRAD_TENSOR_FULL, FG_TERM_ADVECTION, FG_TERM_VECTOR_GRAD_TEST, FG_TERM_SOURCE_GRAD) = range(10)
 FG_PROBLEM_HELMHOLTZ, FG_PROBLEM_NAVIER, FG_PROBLEM_MAXWELL, FG_PROBLEM_COUPLED = range(4)
 FG_SPACE_LAGRANGE, FG_SPACE_HIERARCHICAL_H1, FG_SPACE_HCURL = range(3)
 FG_FORM_0, FG_FORM_1 = range(2)

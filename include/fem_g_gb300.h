@@ -198,8 +198,12 @@ enum {
   FG_TERM_GRAD_GRAD_TENSOR_FULL = 6, /* integral(c * D * grad(dof(u)), grad(tf(u))) with a general (not symmetric)
                                         3x3 TensorFunction D: tensor[9], row-major D_00 D_01 ... D_22; scalar H1 fields;
                                         the element matrix is not symmetric (FP64 paths only) */
-  FG_TERM_ADVECTION = 7              /* integral(c * b * grad(dof(u)), tf(u)) with a VectorFunction b: tensor[3],
+  FG_TERM_ADVECTION = 7,             /* integral(c * b * grad(dof(u)), tf(u)) with a VectorFunction b: tensor[3],
                                         b_x b_y b_z; scalar H1 fields; not symmetric (FP64 paths only) */
+  FG_TERM_VECTOR_GRAD_TEST = 8,      /* integral(c * b * dof(u), grad(tf(u))) with a VectorFunction b: tensor[3];
+                                        scalar H1 fields; not symmetric (FP64 paths only) */
+  FG_TERM_SOURCE_GRAD = 9            /* integral(f, grad(tf(u))) with a VectorFunction f: tensor[3], coef multiplies
+                                        it; right-hand side; scalar H1 fields (FP64 paths only) */
 };
 enum { FG_DT_NONE = 0, FG_DT_1 = 1, FG_DT_2 = 2 }; /* dof, dt_dof, dt2_dof */
 
@@ -236,7 +240,8 @@ typedef struct {
   fg_expr coef2; /* mu for FG_TERM_ELASTIC */
   fg_jacmod jacmod; /* all zero: none */
   const fg_expr *tensor; /* FG_TERM_GRAD_GRAD_TENSOR, FG_TERM_MASS_TENSOR: [6] programs of D_xx, D_yy, D_zz, D_xy, D_xz, D_yz;
-                            FG_TERM_GRAD_GRAD_TENSOR_FULL: [9] of D row-major; FG_TERM_ADVECTION: [3] of b */
+                            FG_TERM_GRAD_GRAD_TENSOR_FULL: [9] of D row-major; FG_TERM_ADVECTION,
+                            FG_TERM_VECTOR_GRAD_TEST, FG_TERM_SOURCE_GRAD: [3] of the vector */
 } fg_term_desc;
 
 /* ------------------------------------------------------------- plan / run */
@@ -258,7 +263,7 @@ int fg_plan_create(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_
  * the unknown field (the columns); ai/aj is the formulation's shared pattern.
  * Both fields scalar H1 (FG_FORM_0, multiplicity 1) on the same elements and
  * rule; no linked DOFs. Terms: FG_TERM_GRAD_GRAD, FG_TERM_MASS,
- * FG_TERM_GRAD_GRAD_TENSOR_FULL and FG_TERM_ADVECTION (with dt factors), no
+ * FG_TERM_GRAD_GRAD_TENSOR_FULL, FG_TERM_ADVECTION and FG_TERM_VECTOR_GRAD_TEST (with dt factors), no
  * field-value coefficients; linear terms go to the test field's own plan.
  * Assembled by fg_assemble_fp64 / fg_assemble_fp64_static into element
  * matrices of n_test x n_unknown. Set fg_plan_set_accumulate(plan, 1) so that

@@ -38,7 +38,9 @@ enum {
   TERM_GRAD_GRAD_TENSOR = 4,
   TERM_MASS_TENSOR = 5,
   TERM_GRAD_GRAD_TENSOR_FULL = 6,
-  TERM_ADVECTION = 7
+  TERM_ADVECTION = 7,
+  TERM_VECTOR_GRAD_TEST = 8,
+  TERM_SOURCE_GRAD = 9
 };
 enum { OP_CONST = 0, OP_X, OP_Y, OP_Z, OP_ELEM, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_HEAVISIDE, OP_FIELD,
        OP_SQRT, OP_EXP, OP_LN, OP_LOG10, OP_POW, OP_SIN, OP_COS, OP_TAN, OP_SINH, OP_COSH, OP_TANH, OP_ASIN, OP_ACOS,
@@ -65,7 +67,8 @@ typedef struct {
   or_expr coef, coef2;
   or_jacmod jacmod;
   const or_expr *tensor; /* TERM_GRAD_GRAD_TENSOR, TERM_MASS_TENSOR: D_xx, D_yy, D_zz, D_xy, D_xz, D_yz;
-                            TERM_GRAD_GRAD_TENSOR_FULL: D row-major [9]; TERM_ADVECTION: b [3] */
+                            TERM_GRAD_GRAD_TENSOR_FULL: D row-major [9]; TERM_ADVECTION, TERM_VECTOR_GRAD_TEST,
+                            TERM_SOURCE_GRAD: the vector [3] */
 } or_term;
 
 typedef struct {
@@ -362,7 +365,25 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
   for (int t = 0; t < nterms; ++t) {
     const or_term *T = &terms[t];
     cplx *target = (frequencyModule && T->dt) ? tmp : Ae;
-    if (T->kind != TERM_SOURCE && !bilinear) continue;
+    const int linear = T->kind == TERM_SOURCE || T->kind == TERM_SOURCE_GRAD;
+    if (!linear && !bilinear) continue;
+    if (T->kind == TERM_SOURCE_GRAD) {
+      /* a VectorFunction f tested against grad(tf(u)): b_e[i] += w det conj(G_i) . (c f)
+       * (LinearTerm::evaluate, src/term/LinearTerm.cpp:182-191, with FieldEvaluator<Form1>) */
+      if (!be || b->form == 1) continue;
+      for (int q = 0; q < nq; ++q) {
+        double J[9], xq[3];
+        double det = or_jacobian(b, e, q, J, xq);
+        if (or_jacmod_apply(&T->jacmod, xq, J, &det)) or_jacmod_err = 1;
+        const double *bf = b->bval + ((size_t)o * nq + q) * nb;
+        const cplx c = eval_expr(&T->coef, e, xq, bf, nb);
+        cplx fv[3];
+        for (int k = 0; k < 3; ++k) fv[k] = c * eval_expr(&T->tensor[k], e, xq, bf, nb);
+        or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
+        for (int i = 0; i < nb; ++i) be[i] += b->w[q] * det * (conj(G[i]) * fv[0] + conj(G[nb + i]) * fv[1] + conj(G[2 * nb + i]) * fv[2]);
+      }
+      continue;
+    }
     if (T->kind == TERM_SOURCE) {
       if (!be || b->form == 1) continue; /* scalar sources only (H1 test functions) */
       for (int q = 0; q < nq; ++q) {
@@ -453,6 +474,17 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
             for (int r = 0; r < 3; ++r)
               for (int t = 0; t < 3; ++t) s += D[r][t] * G[t * nb + jj] * G[r * nb + ii];
             target[jj + ii * n] += wd * s;
+          }
+      } else if (T->kind == TERM_VECTOR_GRAD_TEST) {
+        /* VectorFunction b times dof(u), tested against grad(tf(u)): (c b phi_j) . conj(G_i) */
+        cplx bv[3];
+        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, ph, nb);
+        or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
+        const double *bf = b->bval + ((size_t)o * nq + q) * nb;
+        for (int ii = 0; ii < n; ++ii)
+          for (int jj = 0; jj < n; ++jj) {
+            cplx s = bv[0] * conj(G[ii]) + bv[1] * conj(G[nb + ii]) + bv[2] * conj(G[2 * nb + ii]);
+            target[jj + ii * n] += wd * s * bf[jj];
           }
       } else if (T->kind == TERM_ADVECTION) {
         /* VectorFunction b times grad(dof u), tested against tf(u): (c b . G_j) conj(phi_i) */
@@ -567,7 +599,7 @@ int or_assemble(const or_bucket *b, const or_term *terms, int nterms, double fre
   const int n = b->nb * b->mult;
   int hasSource = 0;
   for (int t = 0; t < nterms; ++t)
-    if (terms[t].kind == TERM_SOURCE) hasSource = 1;
+    if (terms[t].kind == TERM_SOURCE || terms[t].kind == TERM_SOURCE_GRAD) hasSource = 1;
   int err = 0;
   or_jacmod_err = 0;
 #pragma omp parallel
@@ -676,7 +708,7 @@ static void or_element_coupled(const or_bucket *bt, const or_bucket *bu, const o
   for (int k = 0; k < nT * nU; ++k) Ae[k] = 0.0;
   for (int t = 0; t < nterms; ++t) {
     const or_term *T = &terms[t];
-    if (T->kind == TERM_SOURCE) continue;
+    if (T->kind == TERM_SOURCE || T->kind == TERM_SOURCE_GRAD) continue;
     cplx *target = (frequencyModule && T->dt) ? tmp : Ae;
     if (target == tmp)
       for (int k = 0; k < nT * nU; ++k) tmp[k] = 0.0;
@@ -711,6 +743,14 @@ static void or_element_coupled(const or_bucket *bt, const or_bucket *bu, const o
             for (int r = 0; r < 3; ++r)
               for (int u = 0; u < 3; ++u) s += D[r][u] * GU[u * nU + j] * GT[r * nT + i];
             target[j + i * nU] += wd * s;
+          }
+      } else if (T->kind == TERM_VECTOR_GRAD_TEST) {
+        cplx bv[3];
+        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, phU, nU);
+        for (int i = 0; i < nT; ++i)
+          for (int j = 0; j < nU; ++j) {
+            cplx s = bv[0] * GT[i] + bv[1] * GT[nT + i] + bv[2] * GT[2 * nT + i];
+            target[j + i * nU] += wd * s * phU[j];
           }
       } else if (T->kind == TERM_ADVECTION) {
         cplx bv[3];

@@ -26,7 +26,9 @@
 // term "grad" (integral(g grad(dof u), grad(tf u))), "mass"
 // (integral(m dof(u), tf(u))), "source" (integral(f, tf(u))), "dfull_0" ..
 // "dfull_8" (integral(D grad(dof u), grad(tf u)) with the general tensor D,
-// row-major) or "adv_0" .. "adv_2" (integral(b . grad(dof u), tf(u))). The programs
+// row-major), "adv_0" .. "adv_2" (integral(b . grad(dof u), tf(u))), "vdof_0" ..
+// "vdof_2" (integral(b dof(u), grad(tf u))) or "vsrc_0" .. "vsrc_2"
+// (integral(f, grad(tf u)) with a vector f). The programs
 // become the reference's own expression trees (x(), y(), z(), constants,
 // + - * /, heaviside and the scalar operators of scalarUnaryOperators.h).
 #include <algorithm>
@@ -326,6 +328,15 @@ int main(int argc, char **argv) {
                                                  fromProgram(progs["adv_2"])) *
                                  equation::grad(equation::dof(u)),
                              equation::tf(u), omega, gauss);
+      if (progs.count("vdof_0"))  // a VectorFunction times dof(u), tested against grad(tf(u))
+        formulation.integral(function::vector<T>(fromProgram(progs["vdof_0"]), fromProgram(progs["vdof_1"]),
+                                                 fromProgram(progs["vdof_2"])) *
+                                 equation::dof(u),
+                             equation::grad(equation::tf(u)), omega, gauss);
+      if (progs.count("vsrc_0"))  // a VectorFunction source tested against grad(tf(u))
+        formulation.integral(function::vector<T>(fromProgram(progs["vsrc_0"]), fromProgram(progs["vsrc_1"]),
+                                                 fromProgram(progs["vsrc_2"])),
+                             equation::grad(equation::tf(u)), omega, gauss);
       if (progs.count("grad"))
         formulation.integral(fromProgram(progs["grad"]) * equation::grad(equation::dof(u)), equation::grad(equation::tf(u)),
                              omega, gauss);

@@ -93,10 +93,20 @@ def advection_vector(F):
     return [_lin(F, 0.5, cx=1.0), _lin(F, 0.0, cy=-0.3, im=0.2), _lin(F, 0.1)]
 
 
+def vector_dof(F):
+    return [_lin(F, 0.7, cy=0.4), _lin(F, -0.2, cx=0.3, im=0.15), _lin(F, 0.35)]
+
+
+def vector_source(F):
+    return [_lin(F, 1.0, cy=-0.5), _lin(F, 0.2, cx=0.6), _lin(F, -0.4, im=0.3)]
+
+
 def nonsym_terms(F, what):
     """(TermDesc array, count, reference programs, keep-alive list) for
-    what in ("full", "advect", "both"): the non-symmetric term(s), a mass
-    term -4 dof(u) tf(u) and a source 1 + x y."""
+    what in ("full", "advect", "both", "vdof", "vsrc", "vector"): the
+    non-symmetric term(s) (general tensor diffusion, advection b . grad(u)
+    tested by v, b u tested by grad(v), a vector source tested by grad(v)),
+    a mass term -4 dof(u) tf(u) and a source 1 + x y."""
     keep = []
     one = [(F.FG_OP_CONST, 0, 1.0, 0.0)]
     mass = [(F.FG_OP_CONST, 0, -4.0, 0.0)]
@@ -114,6 +124,16 @@ def nonsym_terms(F, what):
         kinds.append((F.FG_TERM_ADVECTION, b))
         for k in range(3):
             programs["adv_%d" % k] = b[k]
+    if what in ("vdof", "vector"):
+        b = vector_dof(F)
+        kinds.append((F.FG_TERM_VECTOR_GRAD_TEST, b))
+        for k in range(3):
+            programs["vdof_%d" % k] = b[k]
+    if what in ("vsrc", "vector"):
+        f = vector_source(F)
+        kinds.append((F.FG_TERM_SOURCE_GRAD, f))
+        for k in range(3):
+            programs["vsrc_%d" % k] = f[k]
     arr = (F.TermDesc * (len(kinds) + 2))()
     for t in arr:
         C.memset(C.byref(t), 0, C.sizeof(F.TermDesc))

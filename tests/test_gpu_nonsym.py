@@ -17,7 +17,7 @@ def rel(a, b):
     return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
 
 
-@pytest.mark.parametrize("what", ["full", "advect", "both"])
+@pytest.mark.parametrize("what", ["full", "advect", "both", "vdof", "vsrc", "vector"])
 @pytest.mark.parametrize("geom", ["tri_p2_dirichlet1", "tri_h1_p3", "tet_h1_p2"])
 def test_gpu_nonsymmetric_matches_oracle(femg, oracle, cuda, geom, what):
     prob = femg.Problem(nonsym_configs(femg)[geom])

@@ -1,7 +1,9 @@
 """Terms with non-symmetric element matrices in the oracle, against the
 reference's own assembly (oracle/_ref/ref_assemble with coefficient
-programs): a general TensorFunction D in integral(D grad(dof u), grad(tf u))
-and the advection integral(b . grad(dof u), tf(u)) with a VectorFunction b,
+programs): a general TensorFunction D in integral(D grad(dof u), grad(tf u)),
+the advection integral(b . grad(dof u), tf(u)) with a VectorFunction b, its
+transpose integral(b dof(u), grad(tf u)) and a vector source
+integral(f, grad(tf u)),
 with a Dirichlet boundary of value 1, so that the lifting's transposed read
 of the element matrix (addValuesDC, src/system/VectorFactory.cpp:184) shows
 in the right-hand side. CSR values and right-hand side to 1e-13."""
@@ -20,7 +22,7 @@ def rel(a, b):
 
 
 @pytest.mark.skipif(not reference.available(), reason="reference program not built (no reference tree)")
-@pytest.mark.parametrize("what", ["full", "advect", "both"])
+@pytest.mark.parametrize("what", ["full", "advect", "both", "vdof", "vsrc", "vector"])
 @pytest.mark.parametrize("geom", ["tri_p2_dirichlet1", "tri_h1_p3", "tet_h1_p2"])
 def test_nonsymmetric_terms_match_reference(femg, oracle, geom, what):
     cfg = nonsym_configs(femg)[geom]
@@ -38,4 +40,5 @@ def test_nonsymmetric_terms_match_reference(femg, oracle, geom, what):
     rows = np.repeat(np.arange(n), np.diff(ai))
     A = {(int(r), int(c)): val for r, c, val in zip(rows, aj, v)}
     asym = max(abs(A[(r, c)] - A.get((c, r), 0)) for (r, c) in A)
-    assert asym > 1e-3
+    if what != "vsrc":  # a vector source alone leaves the (mass) matrix symmetric
+        assert asym > 1e-3
