@@ -6,6 +6,9 @@
 // bubble or Unknown global) holds the sorted, unique unknown DOFs of every
 // element that has I; Fixed DOFs take no column; within one element the
 // bubble rows after the first alias the first one (their pattern is its).
+// Linked DOFs are rows and columns of their masters; a linked bubble's
+// master is a bubble row of another element, whose bubble rows then share
+// one pattern with the linked element's.
 //
 // No global sort: per element the row counts and the bubble aliases, per row
 // its list of (element, local row) entries, then a warp per row gathers the
@@ -24,22 +27,26 @@ constexpr uint32_t kPatNone = 0xFFFFFFFFu;
 
 __device__ __forceinline__ bool patRow(uint8_t t) { return t == FG_AT_UNKNOWN || t == FG_AT_UNKNOWN_BUBBLE || t == FG_AT_UNKNOWN_GLOBAL; }
 
-// row counts and bubble aliases, thread per element
+// Row counts and bubble aliases, thread per element. preAliased: the
+// aliases came from the host (linked bubbles: the bubble rows of a master
+// element and of the element linked to it share one list), and an element's
+// first bubble entry counts on the list's row.
 __global__ void k_pat_count(const uint32_t *__restrict__ edof, const uint8_t *__restrict__ etype, int64_t E, int n,
-                            uint32_t *__restrict__ cnt, uint32_t *__restrict__ alias) {
+                            uint32_t *__restrict__ cnt, uint32_t *__restrict__ alias, bool preAliased) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
   uint32_t first = kPatNone;
   for (int i = 0; i < n; ++i) {
     const uint8_t t = etype[e * n + i];
     if (!patRow(t)) continue;
-    const uint32_t I = edof[e * n + i];
+    uint32_t I = edof[e * n + i];
     if (t == FG_AT_UNKNOWN_BUBBLE) {
       if (first != kPatNone) {
-        alias[I] = first;
+        if (!preAliased) alias[I] = first;
         continue;
       }
       first = I;
+      if (preAliased && alias[I] != kPatNone) I = alias[I];
     }
     atomicAdd(&cnt[I], 1u);
   }
@@ -47,18 +54,20 @@ __global__ void k_pat_count(const uint32_t *__restrict__ edof, const uint8_t *__
 
 // (element, local row) entries of every row, in any order
 __global__ void k_pat_fill(const uint32_t *__restrict__ edof, const uint8_t *__restrict__ etype, int64_t E, int n,
-                           const uint64_t *__restrict__ rowStart, uint32_t *__restrict__ fill, uint32_t *__restrict__ rowElem) {
+                           const uint64_t *__restrict__ rowStart, uint32_t *__restrict__ fill, uint32_t *__restrict__ rowElem,
+                           const uint32_t *__restrict__ alias, bool preAliased) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
   bool seenBubble = false;
   for (int i = 0; i < n; ++i) {
     const uint8_t t = etype[e * n + i];
     if (!patRow(t)) continue;
+    uint32_t I = edof[e * n + i];
     if (t == FG_AT_UNKNOWN_BUBBLE) {
       if (seenBubble) continue;
       seenBubble = true;
+      if (preAliased && alias[I] != kPatNone) I = alias[I];
     }
-    const uint32_t I = edof[e * n + i];
     rowElem[rowStart[I] + atomicAdd(&fill[I], 1u)] = (uint32_t)(e << 6) | (uint32_t)i;
   }
 }
@@ -88,8 +97,9 @@ __global__ void k_pat_rows(const uint32_t *__restrict__ edof, const uint8_t *__r
         const uint32_t pk = rowElem[s0 + k / n];
         const int64_t e = pk >> 6;
         const int j = k % n;
-        // upper storage keeps the columns at or right of the (first bubble's) row
-        if (patRow(etype[e * n + j]) && (!upper || edof[e * n + j] >= row)) v = edof[e * n + j];
+        // upper storage keeps the columns at or right of the entry's own row:
+        // the row itself, or for bubbles the row of the element's first bubble
+        if (patRow(etype[e * n + j]) && (!upper || edof[e * n + j] >= edof[e * n + (pk & 63)])) v = edof[e * n + j];
       }
       buf[k] = v;
     }
@@ -184,21 +194,20 @@ extern "C" int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *ele
   std::vector<uint32_t> ed(en);
   std::vector<uint8_t> et(en);
   int bad = 0;
+  int64_t linkedBubbles = 0;
   for (size_t k = 0; k < en; ++k) {
     int t = elem_dof_type[k];
     uint64_t v = elem_dof_idx[k];
-    if (t == FG_AT_LINKED_BUBBLE) {
-      setLastError("fg_pattern_build: linked bubble DOFs are not supported");
-      return FG_ERR_UNSUPPORTED;
-    }
-    if (t == FG_AT_LINKED) {
-      // a linked DOF is a row and a column of its master (MatrixFactory.cpp:468-470, :481-483)
+    if (t == FG_AT_LINKED || t == FG_AT_LINKED_BUBBLE) {
+      // a linked DOF is a row and a column of its master (MatrixFactory.cpp:468-470, :481-483);
+      // a linked bubble is a bubble row of its master's (:505)
       if (!linked_row || v >= n_linked) {
         ++bad;
         continue;
       }
       v = linked_row[v];
-      t = FG_AT_UNKNOWN;
+      if (t == FG_AT_LINKED_BUBBLE) ++linkedBubbles;
+      t = t == FG_AT_LINKED ? FG_AT_UNKNOWN : FG_AT_UNKNOWN_BUBBLE;
     }
     et[k] = (uint8_t)t;
     const bool row = t == FG_AT_UNKNOWN || t == FG_AT_UNKNOWN_BUBBLE || t == FG_AT_UNKNOWN_GLOBAL;
@@ -221,10 +230,43 @@ extern "C" int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *ele
   FG_CUDA(cudaMemcpy(dEt.p, et.data(), en, cudaMemcpyHostToDevice));
   FG_CUDA(cudaMemset(cnt, 0, n_rows * 4));
   FG_CUDA(cudaMemset(fill, 0, n_rows * 4));
-  FG_CUDA(cudaMemset(alias, 0xFF, n_rows * 4));
+  // With linked bubbles, the rows that share one list: the reference's
+  // element after element pointer assignment (MatrixFactory.cpp:505-535)
+  // puts every bubble row of a master element and of the element linked to
+  // it on the list of whichever bubble row was taken first; connecting the
+  // bubble rows of each element gives the same groups in any element order.
+  // Each group's list is kept on its smallest row.
+  const bool preAliased = linkedBubbles > 0;
+  if (preAliased) {
+    std::vector<uint32_t> root(n_rows);
+    for (uint64_t r = 0; r < n_rows; ++r) root[r] = (uint32_t)r;
+    auto find = [&](uint32_t r) {
+      while (root[r] != r) r = root[r] = root[root[r]];
+      return r;
+    };
+    for (int64_t e = 0; e < E; ++e) {
+      uint32_t first = kPatNone;
+      for (int i = 0; i < n; ++i) {
+        const size_t k = (size_t)e * n + i;
+        if (et[k] != FG_AT_UNKNOWN_BUBBLE) continue;
+        if (first == kPatNone) {
+          first = ed[k];
+          continue;
+        }
+        const uint32_t a = find(first), b = find(ed[k]);
+        if (a != b) root[std::max(a, b)] = std::min(a, b);
+      }
+    }
+    std::vector<uint32_t> al(n_rows, kPatNone);
+    for (uint64_t r = 0; r < n_rows; ++r)
+      if (find((uint32_t)r) != r) al[r] = find((uint32_t)r);
+    FG_CUDA(cudaMemcpy(alias, al.data(), n_rows * 4, cudaMemcpyHostToDevice));
+  } else {
+    FG_CUDA(cudaMemset(alias, 0xFF, n_rows * 4));
+  }
   const unsigned eb = (unsigned)std::max<int64_t>(1, (E + 255) / 256);
   if (E > 0) {
-    k_pat_count<<<eb, 256>>>((const uint32_t *)dEd.p, (const uint8_t *)dEt.p, E, n, cnt, alias);
+    k_pat_count<<<eb, 256>>>((const uint32_t *)dEd.p, (const uint8_t *)dEt.p, E, n, cnt, alias, preAliased);
     countLaunch();
   }
   // row starts of the entry lists (host scan)
@@ -239,7 +281,8 @@ extern "C" int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *ele
   FG_CUDA(cudaMemcpy(rowStart, h64.data(), (n_rows + 1) * 8, cudaMemcpyHostToDevice));
   if ((st = devAlloc(dElem, h64[n_rows] * 4))) return st;
   if (E > 0) {
-    k_pat_fill<<<eb, 256>>>((const uint32_t *)dEd.p, (const uint8_t *)dEt.p, E, n, rowStart, fill, (uint32_t *)dElem.p);
+    k_pat_fill<<<eb, 256>>>((const uint32_t *)dEd.p, (const uint8_t *)dEt.p, E, n, rowStart, fill, (uint32_t *)dElem.p, alias,
+                            preAliased);
     countLaunch();
   }
   // shared memory per warp: the largest candidate list, rounded to a power of two

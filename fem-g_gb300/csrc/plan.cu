@@ -262,20 +262,22 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   }
 
   // element DOF map: row/column index (or fixed index) and type. A linked
-  // DOF takes its master's row and column (MatrixFactory.cpp:241-246,
-  // :254-259), so it is stored as an Unknown DOF of that row; its coefficient
-  // goes to the scale table the reduction applies.
+  // DOF, bubble or not, takes its master's row and column
+  // (MatrixFactory.cpp:241-246, :254-259), so it is stored as an Unknown DOF
+  // of that row; its coefficient goes to the scale table the reduction
+  // applies. The reference adds a linked bubble exactly as a linked DOF
+  // (:306-309, :373-380, :409-442; VectorFactory.cpp:134, :195); the bubble
+  // kind only changes the pattern, which the caller passes in.
   std::vector<uint32_t> edof((size_t)E * n);
   std::vector<uint8_t> etype((size_t)E * n);
-  int linkedBubble = 0, linked = 0;
-#pragma omp parallel for reduction(+ : bad, linkedBubble, linked)
+  int linked = 0;
+#pragma omp parallel for reduction(+ : bad, linked)
   for (int64_t i = 0; i < E * n; ++i) {
     const int t = sys->elem_dof_type[i];
     uint64_t v = sys->elem_dof_idx[i];
     etype[(size_t)i] = (uint8_t)t;
-    if (t == FG_AT_LINKED_BUBBLE) ++linkedBubble;
-    else if (t < 0 || t > FG_AT_LINKED_BUBBLE) ++bad;
-    else if (t == FG_AT_LINKED) {
+    if (t < 0 || t > FG_AT_LINKED_BUBBLE) ++bad;
+    else if (t == FG_AT_LINKED || t == FG_AT_LINKED_BUBBLE) {
       if (!sys->linked_row || !sys->linked_value || v >= sys->n_linked || sys->linked_row[v] >= sys->n_rows) {
         ++bad;
       } else {
@@ -286,10 +288,6 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
     } else if (isRow(t) && v >= sys->n_rows) ++bad;
     else if (t == FG_AT_FIXED && v >= sys->n_fixed) ++bad;
     edof[(size_t)i] = (uint32_t)v;
-  }
-  if (linkedBubble) {
-    setLastError("fg_plan_create: linked bubble DOFs are not supported");
-    return FG_ERR_UNSUPPORTED;
   }
   if (bad) {
     setLastError("fg_plan_create: element DOF index/type out of range");
@@ -510,7 +508,7 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   if (linked) {
     std::vector<double2> ls((size_t)E * n, make_double2(1.0, 0.0));
     for (int64_t i = 0; i < E * n; ++i)
-      if (sys->elem_dof_type[i] == FG_AT_LINKED) {
+      if (sys->elem_dof_type[i] == FG_AT_LINKED || sys->elem_dof_type[i] == FG_AT_LINKED_BUBBLE) {
         const uint64_t v = sys->elem_dof_idx[i];
         ls[(size_t)i] = make_double2(sys->linked_value[2 * v], sys->linked_value[2 * v + 1]);
       }

@@ -115,13 +115,14 @@ typedef struct {
                                    or hermitian() option): the pattern holds the upper triangle and
                                    entries below the diagonal are not added
                                    (MatrixFactory::addPattern/addValues, "jIndex < iIndex") */
-  uint64_t n_linked;            /* linked DOFs (FG_AT_LINKED; elem_dof_idx holds their index below),
-                                   e.g. periodic or Bloch conditions */
+  uint64_t n_linked;            /* linked DOFs (FG_AT_LINKED and FG_AT_LINKED_BUBBLE; elem_dof_idx holds
+                                   their index below), e.g. periodic or Bloch conditions */
   const uint64_t *linked_row;   /* [n_linked] the row of each linked DOF's master (MatrixFactory _indicesLC) */
   const double *linked_value;   /* [n_linked][2] its coefficient c (_valuesLC): a linked row adds into its
                                    master's row times conj(c), a linked column into its master's column
                                    times c (MatrixFactory.cpp:233-448, VectorFactory.cpp:122-210).
-                                   FG_AT_LINKED_BUBBLE is not supported. */
+                                   A linked bubble (the interior DOF of an element linked to one of
+                                   another element) adds the same way; its master is a bubble row. */
 } fg_system_desc;
 
 /* Coefficient expression: a complex-valued program over the physical point
@@ -428,7 +429,10 @@ const char *fg_batch_tuning(const fg_batch *batch);
  * upper = 1: symmetric storage, only the columns J >= I of a row (for an
  * aliased bubble row, those of the first bubble's row). linked_row
  * ([n_linked], as in fg_system_desc): an FG_AT_LINKED DOF is a row and a
- * column of its master; NULL when there are none. */
+ * column of its master; an FG_AT_LINKED_BUBBLE DOF is a bubble row of its
+ * master's, and the bubble rows of the master element and of the linked one
+ * share one pattern (the columns of both elements; with upper = 1, each
+ * element's from its own first bubble's row); NULL when there are none. */
 int fg_pattern_build(const uint64_t *elem_dof_idx, const int32_t *elem_dof_type, int64_t n_elements, int32_t n_dofs,
                      uint64_t n_rows, uint64_t *ai, uint64_t **aj, int32_t upper, const uint64_t *linked_row,
                      uint64_t n_linked);

@@ -100,7 +100,7 @@ static int or_dof_row(const or_bucket *b, int t, uint64_t idx, uint64_t *row, cp
     *scale = 1.0;
     return 1;
   }
-  if (t == AT_LINKED && b->linked_row) {
+  if ((t == AT_LINKED || t == AT_LINKED_BUBBLE) && b->linked_row) {
     *row = b->linked_row[idx];
     *scale = b->linked_value[2 * idx] + I * b->linked_value[2 * idx + 1];
     return 1;
@@ -621,13 +621,7 @@ int or_assemble(const or_bucket *b, const or_term *terms, int nterms, double fre
         }
         uint64_t row, col;
         cplx si, sj;
-        if (!or_dof_row(b, ti, idx[i], &row, &si)) {
-          if (ti == AT_LINKED_BUBBLE) {
-#pragma omp atomic write
-            err = 3;
-          }
-          continue;
-        }
+        if (!or_dof_row(b, ti, idx[i], &row, &si)) continue;
         for (int j = 0; j < n; ++j) {
           const int tj = typ[j];
           if (tj == AT_FIXED) {
@@ -876,10 +870,12 @@ static void vec_insert_sorted(u64vec *r, uint64_t x) {
 int or_pattern(int64_t E, int n, const uint64_t *edof, const int32_t *etype, uint64_t n_rows, uint64_t *ai, uint64_t **aj_out,
                int upper, const uint64_t *linked_row) {
   for (int64_t k = 0; k < E * n; ++k)
-    if (etype[k] == AT_LINKED_BUBBLE || (etype[k] == AT_LINKED && !linked_row)) return 3; /* not restated */
+    if ((etype[k] == AT_LINKED || etype[k] == AT_LINKED_BUBBLE) && !linked_row) return 3; /* not restated */
+  /* rows[v] are the column lists; a row's pattern is the list ptr[r] points at
+   * (the reference's array of vector pointers, MatrixFactory _pattern) */
   u64vec *rows = calloc(n_rows, sizeof(u64vec));
-  int64_t *alias = malloc(n_rows * sizeof(int64_t));
-  for (uint64_t r = 0; r < n_rows; ++r) alias[r] = -1;
+  int64_t *ptr = malloc(n_rows * sizeof(int64_t));
+  for (uint64_t r = 0; r < n_rows; ++r) ptr[r] = (int64_t)r;
   for (int64_t e = 0; e < E; ++e) {
     const uint64_t *idx = edof + (size_t)e * n;
     const int32_t *typ = etype + (size_t)e * n;
@@ -888,36 +884,42 @@ int or_pattern(int64_t E, int n, const uint64_t *edof, const int32_t *etype, uin
       const int ti = typ[i];
       uint64_t Ir, Jc;
       /* a linked row is its master's row (MatrixFactory.cpp:468-470) */
-      if (ti == AT_LINKED) Ir = linked_row[idx[i]];
+      if (ti == AT_LINKED || ti == AT_LINKED_BUBBLE) Ir = linked_row[idx[i]];
       else if (ti == AT_UNKNOWN || ti == AT_UNKNOWN_GLOBAL || ti == AT_UNKNOWN_BUBBLE) Ir = idx[i];
       else continue;
-      if (ti == AT_UNKNOWN_BUBBLE) {
+      /* the element's first bubble row (unknown or linked) takes its columns
+       * into the list its row points at; the element's later bubble rows are
+       * pointed at that list (MatrixFactory.cpp:505-535). A linked bubble's
+       * master row is a bubble row of the master element, so the two
+       * elements' bubble rows end up on one list with both their columns. */
+      int64_t dst = ptr[Ir];
+      if (ti == AT_UNKNOWN_BUBBLE || ti == AT_LINKED_BUBBLE) {
         if (bubble >= 0) {
-          alias[Ir] = bubble;
+          ptr[Ir] = bubble;
           continue;
         }
-        bubble = (int64_t)Ir;
+        bubble = dst;
       }
       for (int j = 0; j < n; ++j) {
         const int tj = typ[j];
-        if (tj == AT_LINKED) Jc = linked_row[idx[j]];
+        if (tj == AT_LINKED || tj == AT_LINKED_BUBBLE) Jc = linked_row[idx[j]];
         else if (tj == AT_UNKNOWN || tj == AT_UNKNOWN_GLOBAL || tj == AT_UNKNOWN_BUBBLE) Jc = idx[j];
         else continue;
         if (upper && Jc < Ir) continue; /* upper triangular matrix (MatrixFactory.cpp:491) */
-        vec_insert_sorted(&rows[Ir], Jc);
+        vec_insert_sorted(&rows[dst], Jc);
       }
     }
   }
   ai[0] = 0;
-  for (uint64_t r = 0; r < n_rows; ++r) ai[r + 1] = ai[r] + rows[alias[r] >= 0 ? alias[r] : (int64_t)r].n;
+  for (uint64_t r = 0; r < n_rows; ++r) ai[r + 1] = ai[r] + rows[ptr[r]].n;
   uint64_t *aj = malloc((ai[n_rows] ? ai[n_rows] : 1) * sizeof(uint64_t));
   for (uint64_t r = 0; r < n_rows; ++r) {
-    const u64vec *src = &rows[alias[r] >= 0 ? alias[r] : (int64_t)r];
+    const u64vec *src = &rows[ptr[r]];
     memcpy(aj + ai[r], src->v, src->n * sizeof(uint64_t));
   }
   for (uint64_t r = 0; r < n_rows; ++r) free(rows[r].v);
   free(rows);
-  free(alias);
+  free(ptr);
   *aj_out = aj;
   return 0;
 }

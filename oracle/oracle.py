@@ -120,8 +120,6 @@ def assemble(a, terms_ptr, n_terms, freq=0.0, with_rhs=True):
                             values.ctypes.data, rhs.ctypes.data if with_rhs else None)
     if err == 2:
         raise ValueError("oracle: an integration point lies outside a Jacobian modificator's shell")
-    if err == 3:
-        raise ValueError("oracle: linked bubble DOFs are not restated")
     if err:
         raise RuntimeError("oracle: an element DOF pair is missing from the pattern")
     return values, rhs
@@ -188,7 +186,7 @@ def pattern(edof, etype, n_rows, upper=False, linked_row=None):
     st = lib().or_pattern(E, n, edof.ctypes.data, etype.ctypes.data, int(n_rows), ai.ctypes.data, C.byref(ajp), 1 if upper else 0,
                           lrow.ctypes.data if lrow is not None and lrow.size else None)
     if st:
-        raise ValueError("oracle: linked bubble DOFs are not restated")
+        raise ValueError("oracle: linked DOFs without their master rows (linked_row)")
     nnz = int(ai[-1])
     aj = np.ctypeslib.as_array(C.cast(ajp, C.POINTER(C.c_uint64)), shape=(max(nnz, 1),))[:nnz].copy()
     lib().or_free(ajp)
