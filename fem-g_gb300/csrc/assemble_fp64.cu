@@ -467,7 +467,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
 //   Ke[i][j] = sum_q w det (c_curl C_j . C_i + c_m P_j . P_i),
 // or, with tensor terms (TensorFunction * curl, TensorFunction * dof: the
 // Maxwell PML), sum_q w det (C_i . A C_j + P_i . B P_j) with A = c_curl I + c D.
-// Warp per element, lanes over the pairs i <= j; the matrix is symmetric.
+// Warp per element, lanes over the pairs i <= j (the matrix is symmetric),
+// 256 pairs at a time: the points are visited once per 256 pairs.
 struct HcurlWarpSmem {
   double X[kMaxNodes * 3];
   double J0[9], J[9], Jinv[9];
@@ -503,6 +504,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
     const int o = p.orient ? p.orient[e] : 0;
     for (int t = lane; t < p.nn * 3; t += 32) S.X[t] = p.xyz[3 * (int64_t)p.enodes[e * p.nn + t / 3] + t % 3];
     __syncwarp();
+    // the pairs in chunks of 32 MAXENT, the points once per chunk
+    for (int c0 = 0; c0 < nEnt; c0 += 32 * MAXENT) {
     double accR[MAXENT], accI[MAXENT];
 #pragma unroll
     for (int m = 0; m < MAXENT; ++m) accR[m] = accI[m] = 0.0;
@@ -561,7 +564,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
       __syncwarp();
 #pragma unroll
       for (int m = 0; m < MAXENT; ++m) {
-        const int k = lane + 32 * m;
+        const int k = c0 + lane + 32 * m;
         if (k < nEnt) {
           const int i = pairI[k], j = pairJ[k];
           if (tensor) {
@@ -584,7 +587,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
     double *K = ke + (size_t)e * ncomp * n * n;
 #pragma unroll
     for (int m = 0; m < MAXENT; ++m) {
-      const int k = lane + 32 * m;
+      const int k = c0 + lane + 32 * m;
       if (k < nEnt) {
         const int i = pairI[k], j = pairJ[k];
         K[i * n + j] = K[j * n + i] = accR[m];
@@ -592,6 +595,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
       }
     }
     __syncwarp();
+    }
   }
 }
 
@@ -647,11 +651,7 @@ static int launchElementKernels(fg_plan *plan, const DevTerms &terms, const DevT
     else k_element_hcurl_fp64<M, false><<<(unsigned)blocks, 32 * kWarpsPerBlockElem, 0, s>>>(p, dterms, ke);        \
   } while (0)
     if (perLane <= 1) FG_LAUNCH_HC(1);
-    else if (perLane <= 8) FG_LAUNCH_HC(8);
-    else {
-      setLastError("FP64 HCurl kernel: more than 22 basis functions per element");
-      return FG_ERR_UNSUPPORTED;
-    }
+    else FG_LAUNCH_HC(8);  // 256 pairs per chunk: one chunk up to 22 functions, more chunks beyond
 #undef FG_LAUNCH_HC
     (void)be;
     countLaunch();

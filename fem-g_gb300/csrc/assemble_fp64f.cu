@@ -175,7 +175,10 @@ bool factoredFp64Applies(const fg_plan *plan, const DevTerms &terms) {
     return false;
   for (int t = 0; t < terms.n; ++t)
     if (terms.t[t].kind != FG_TERM_SOURCE && terms.t[t].coef.cls == kExprPoint) return false;
-  return true;
+  // the reference tensors of a block live in shared memory (HCurl of order 2
+  // on tetrahedra, 45 functions, does not fit: the quadrature loop applies)
+  const size_t kp = p.form == FG_FORM_1 ? 12 : 7;
+  return (kp * p.n * p.n + (size_t)kFacTile * 2 * kFacMax) * sizeof(double) <= 200 * 1024;
 }
 
 bool factoredFp64Ready(const fg_plan *plan) {

@@ -171,6 +171,8 @@ def _bind(L):
         "fg_problem_block": (C.c_int, [P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.POINTER(TermDesc)),
                                        C.POINTER(C.c_int32)]),
         "fg_problem_assemble": (C.c_int, [P, C.c_int32, P, P, P]),
+        "fg_basis_eval": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int64, P, P, P]),
+        "fg_basis_orientation": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, P]),
     }
     for name, (res, args) in sig.items():
         if not hasattr(L, name):  # the host-only library has the fg_problem_* calls alone
@@ -189,8 +191,35 @@ def exported_symbols():
         "fg_profile_read", "fg_last_error", "fg_launch_count",
         "fg_host_alloc", "fg_host_free", "fg_problem_create", "fg_problem_destroy", "fg_problem_descs", "fg_problem_n_dofs",
         "fg_problem_raw_dofs", "fg_problem_created_dofs", "fg_problem_reserve_log", "fg_problem_bbox", "fg_problem_pre_seconds", "fg_problem_assemble",
-        "fg_problem_n_fields", "fg_problem_field", "fg_problem_n_blocks", "fg_problem_block",
+        "fg_problem_n_fields", "fg_problem_field", "fg_problem_n_blocks", "fg_problem_block", "fg_basis_eval",
+        "fg_basis_orientation",
     ]
+
+
+def basis_eval(space, order, dim, code, uvw):
+    """fg_basis_eval at points uvw [npts][3]: (values, derivatives) with
+    values [npts][n] (H1) or [npts][n][3] (HCurl) and derivatives [npts][n][3]
+    (gradients or curls)."""
+    uvw = np.ascontiguousarray(uvw, np.float64).reshape(-1, 3)
+    L = lib()
+    n = L.fg_basis_eval(space, order, dim, code, 0, None, None, None)
+    if n < 0:
+        check(-n)
+    shape = (len(uvw), n, 3) if space == FG_SPACE_HCURL else (len(uvw), n)
+    val, der = np.zeros(shape), np.zeros((len(uvw), n, 3))
+    r = L.fg_basis_eval(space, order, dim, code, len(uvw), uvw.ctypes.data, val.ctypes.data, der.ctypes.data)
+    if r < 0:
+        check(-r)
+    return val, der
+
+
+def basis_orientation(space, order, dim, vertex_tags):
+    """fg_basis_orientation for the global tags of an element's vertices."""
+    tags = np.ascontiguousarray(vertex_tags, np.int64)
+    r = lib().fg_basis_orientation(space, order, dim, tags.ctypes.data)
+    if r < 0:
+        check(-r)
+    return r
 
 
 def profile_enable(on=True):

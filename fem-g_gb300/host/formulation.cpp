@@ -67,12 +67,18 @@ void FunctionSpace::getKeys(const Mesh &mesh, const ElementBlock &blk, bool with
     return;
   }
   if (type == SpaceType::HCurl) {
-    // per edge (1 + k, edge tag) at the edge midpoint, k < 1 + order; order 1
-    // adds per face (3 + k, face tag) at the face centroid, k < 2 (in 2D the
-    // element's own interior functions: (3 + k, element tag) at its centroid)
-    const int perEdge = order == 0 ? 1 : 2;
+    // per edge (1 + k, edge tag) at the edge midpoint, k < perEdge; per face
+    // (1 + perEdge + k, face tag) at the face centroid, k < perFace (in 2D the
+    // element's own interior functions, with the element tag at its
+    // centroid); per tetrahedron (1 + perEdge + perFace + k, element tag) at
+    // its centroid, k < perCell
+    int perEdge = 1, perFace = 0, perCell = 0;
+    if (order > 0) hcurlEntityCounts(dim, order, perEdge, perFace, perCell);
     for (int64_t e = 0; e < E; ++e) {
       const int64_t *v = &blk.nodes[(size_t)(e * nn)];
+      double cen[3] = {0, 0, 0};
+      for (int a = 0; a < nv; ++a)
+        for (int c = 0; c < 3; ++c) cen[c] += mesh.xyz[3 * v[a] + c] / nv;
       for (auto &ed : simplexEdges(dim)) {
         double mid[3];
         for (int c = 0; c < 3; ++c) mid[c] = 0.5 * (mesh.xyz[3 * v[ed[0]] + c] + mesh.xyz[3 * v[ed[1]] + c]);
@@ -84,30 +90,33 @@ void FunctionSpace::getKeys(const Mesh &mesh, const ElementBlock &blk, bool with
           if (infoDim) infoDim->push_back(1);
         }
       }
-      if (order == 0) continue;
       if (dim == 2) {
-        double cen[3] = {0, 0, 0};
-        for (int a = 0; a < nv; ++a)
-          for (int c = 0; c < 3; ++c) cen[c] += mesh.xyz[3 * v[a] + c] / nv;
-        for (int k = 0; k < 2; ++k) {
-          typeKeys.push_back(3 + k);
+        for (int k = 0; k < perFace; ++k) {
+          typeKeys.push_back(1 + perEdge + k);
           entityKeys.push_back((uint64_t)blk.tags[(size_t)e]);
           pushCoord(cen);
           if (infoDim) infoDim->push_back(2);
         }
-      } else {
+        continue;
+      }
+      if (perFace > 0)
         for (auto &fc : simplexFaces(3)) {
           const int64_t tag = mesh.faceTagOf(v[fc[0]], v[fc[1]], v[fc[2]]);
           double fcen[3];
           for (int c = 0; c < 3; ++c)
             fcen[c] = (mesh.xyz[3 * v[fc[0]] + c] + mesh.xyz[3 * v[fc[1]] + c] + mesh.xyz[3 * v[fc[2]] + c]) / 3.0;
-          for (int k = 0; k < 2; ++k) {
-            typeKeys.push_back(3 + k);
+          for (int k = 0; k < perFace; ++k) {
+            typeKeys.push_back(1 + perEdge + k);
             entityKeys.push_back((uint64_t)tag);
             pushCoord(fcen);
             if (infoDim) infoDim->push_back(2);
           }
         }
+      for (int k = 0; k < perCell; ++k) {
+        typeKeys.push_back(1 + perEdge + perFace + k);
+        entityKeys.push_back((uint64_t)blk.tags[(size_t)e]);
+        pushCoord(cen);
+        if (infoDim) infoDim->push_back(3);
       }
     }
     return;

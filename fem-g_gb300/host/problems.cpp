@@ -254,4 +254,32 @@ int fg_problem_bbox(const fg_problem *p, double *bbox) {
 
 double fg_problem_pre_seconds(const fg_problem *p) { return p ? p->form->preSeconds : -1.0; }
 
+int fg_basis_eval(int32_t space, int32_t order, int32_t dim, int32_t code, int64_t npts, const double *uvw, double *val,
+                  double *deriv) {
+  if ((space != FG_SPACE_HIERARCHICAL_H1 && space != FG_SPACE_HCURL) || (dim != 2 && dim != 3) || npts < 0 ||
+      (npts > 0 && !uvw) || order < (space == FG_SPACE_HCURL ? 0 : 1) || order > 12 || code < 0) {
+    setLastError("fg_basis_eval: invalid arguments");
+    return -FG_ERR_ARG;
+  }
+  const bool hc = space == FG_SPACE_HCURL;
+  const int n = hc ? hcurlCount(dim, order) : hierarchicalCount(dim, order);
+  const int vn = hc ? 3 * n : n;
+  std::vector<double> v(vn), d(3 * n);
+  for (int64_t q = 0; q < npts; ++q) {
+    if (hc) hcurlBasis(dim, order, code, &uvw[3 * q], v.data(), d.data());
+    else hierarchicalBasis(dim, order, code, &uvw[3 * q], v.data(), d.data());
+    if (val) std::memcpy(val + (size_t)q * vn, v.data(), vn * sizeof(double));
+    if (deriv) std::memcpy(deriv + (size_t)q * 3 * n, d.data(), 3 * n * sizeof(double));
+  }
+  return n;
+}
+
+int fg_basis_orientation(int32_t space, int32_t order, int32_t dim, const int64_t *vertex_tags) {
+  if ((space != FG_SPACE_HIERARCHICAL_H1 && space != FG_SPACE_HCURL) || (dim != 2 && dim != 3) || !vertex_tags) {
+    setLastError("fg_basis_orientation: invalid arguments");
+    return -FG_ERR_ARG;
+  }
+  return space == FG_SPACE_HCURL ? hcurlOrientation(dim, order, vertex_tags) : hierarchicalOrientation(dim, vertex_tags);
+}
+
 }  // extern "C"

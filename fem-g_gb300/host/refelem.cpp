@@ -273,10 +273,18 @@ void whitneyBasis(int dim, int code, const double *uvw, double *val, double *cur
   }
 }
 
+void hcurlEntityCounts(int dim, int p, int &perEdge, int &perFace, int &perCell) {
+  if (p < 0 || (dim != 2 && dim != 3)) throw std::invalid_argument("hierarchical HCurl: order >= 0 on triangles and tetrahedra");
+  perEdge = p + 1;
+  perFace = p * (p + 1);
+  perCell = dim == 3 ? (p - 1) * p * (p + 1) / 2 : 0;
+}
+
 int hcurlCount(int dim, int p) {
   if (p == 0) return whitneyCount(dim);
-  if (p != 1) throw std::invalid_argument("hierarchical HCurl: orders 0 and 1");
-  return 2 * (int)simplexEdges(dim).size() + 2 * (dim == 3 ? 4 : 1);
+  int pe, pf, pc;
+  hcurlEntityCounts(dim, p, pe, pf, pc);
+  return (int)simplexEdges(dim).size() * pe + (dim == 3 ? 4 : 1) * pf + pc;
 }
 
 int hcurlOrientation(int dim, int p, const int64_t *tags) {
@@ -302,32 +310,54 @@ void hcurlBasis(int dim, int p, int code, const double *uvw, double *val, double
     cross(lam[a].g, lam[b].g, cw);
     for (int c = 0; c < 3; ++c) cw[c] *= 2.0;
   };
+  // s w_ab for a scalar s (value and gradient)
+  auto scaled = [&](const VG &sc, int a, int b) {
+    double w[3], cw[3], gx[3];
+    whitney(a, b, w, cw);
+    cross(sc.g, w, gx);
+    for (int k = 0; k < 3; ++k) {
+      val[3 * idx + k] = sc.v * w[k];
+      curl[3 * idx + k] = gx[k] + sc.v * cw[k];
+    }
+    ++idx;
+  };
   const auto &edges = simplexEdges(dim);
   for (size_t e = 0; e < edges.size(); ++e) {
     int a = edges[e][0], b = edges[e][1];
     if ((code >> e) & 1) std::swap(a, b);
     whitney(a, b, &val[3 * idx], &curl[3 * idx]);
     ++idx;
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < 3; ++c) {  // grad(lambda_a lambda_b)
       val[3 * idx + c] = lam[a].v * lam[b].g[c] + lam[b].v * lam[a].g[c];
       curl[3 * idx + c] = 0.0;
     }
     ++idx;
-  }
-  // lambda_c w_ab
-  auto faceFn = [&](int a, int b, int c) {
-    double w[3], cw[3], gx[3];
-    whitney(a, b, w, cw);
-    cross(lam[c].g, w, gx);
-    for (int k = 0; k < 3; ++k) {
-      val[3 * idx + k] = lam[c].v * w[k];
-      curl[3 * idx + k] = gx[k] + lam[c].v * cw[k];
+    const VG ab = mul(lam[a], lam[b]);
+    for (int k = 1; k <= p - 1; ++k) {
+      const VG f = mul(ab, leg(k, lam[a], lam[b]));
+      for (int c = 0; c < 3; ++c) {
+        val[3 * idx + c] = f.g[c];
+        curl[3 * idx + c] = 0.0;
+      }
+      ++idx;
     }
-    ++idx;
+  }
+  auto faceFns = [&](int s0, int s1, int s2) {
+    for (int d = 0; d <= p - 1; ++d)
+      for (int i = d; i >= 0; --i) {
+        const int j = d - i;
+        if (d == 0) {  // q = 1
+          scaled(lam[s2], s0, s1);
+          scaled(lam[s0], s1, s2);
+          continue;
+        }
+        const VG q = mul(leg(i, lam[s0], lam[s1]), leg(j, lam[s1], lam[s2]));
+        scaled(mul(lam[s2], q), s0, s1);
+        scaled(mul(lam[s0], q), s1, s2);
+      }
   };
   if (dim == 2) {
-    faceFn(0, 1, 2);
-    faceFn(1, 2, 0);
+    faceFns(0, 1, 2);
     return;
   }
   int digits = code >> edges.size();
@@ -335,10 +365,18 @@ void hcurlBasis(int dim, int p, int code, const double *uvw, double *val, double
   for (size_t f = 0; f < faces.size(); ++f) {
     const int *s = kPerm3[digits % 6];
     digits /= 6;
-    const int s0 = faces[f][s[0]], s1 = faces[f][s[1]], s2 = faces[f][s[2]];
-    faceFn(s0, s1, s2);
-    faceFn(s1, s2, s0);
+    faceFns(faces[f][s[0]], faces[f][s[1]], faces[f][s[2]]);
   }
+  const VG l23 = mul(lam[2], lam[3]), l03 = mul(lam[0], lam[3]), l01 = mul(lam[0], lam[1]);
+  for (int d = 0; d <= p - 2; ++d)
+    for (int i = d; i >= 0; --i)
+      for (int j = d - i; j >= 0; --j) {
+        const int k = d - i - j;
+        const VG q = mul(leg(i, lam[0], lam[1]), mul(leg(j, lam[1], lam[2]), leg(k, lam[2], lam[3])));
+        scaled(mul(l23, q), 0, 1);
+        scaled(mul(l03, q), 1, 2);
+        scaled(mul(l01, q), 2, 3);
+      }
 }
 
 void hierarchicalBasis(int dim, int p, int code, const double *uvw, double *val, double *grad) {

@@ -1,5 +1,5 @@
 // Reference-element data: quadrature rules, geometric (Lagrange) basis, the
-// hierarchical H1 basis with orientations and the hierarchical HCurl basis of orders 0 and 1.
+// hierarchical H1 basis with orientations and the hierarchical HCurl basis of any order.
 //
 // In the reference these come from gmsh:
 //  - quadrature: gmsh::model::mesh::getIntegrationPoints(type, "GaussN") via
@@ -58,22 +58,38 @@ int whitneyOrientation(int dim, const int64_t *vertexTags);
 // values [n][3] and curls [n][3] for an orientation code
 void whitneyBasis(int dim, int orientationCode, const double *uvw, double *val, double *curl);
 
-// Hierarchical HCurl of order p = 0 or 1 (the reference's
-// FunctionSpaceHierarchicalHCurl, gmsh "HcurlLegendre<p>"): order 0 is
-// whitneyBasis; order 1 spans the first-kind Nedelec space of degree 2 with,
-// per edge (a, b) directed from the lower global tag to the higher,
-//   w_ab and grad(lambda_a lambda_b)  (curl 0),
-// and per face with vertices s0 < s1 < s2 in global tag order (3D; the
-// triangle's own vertex order in 2D, where they are interior bubbles)
-//   lambda_s2 w_s0s1 and lambda_s0 w_s1s2,
-//   curl(lambda_c w_ab) = grad(lambda_c) x w_ab + 2 lambda_c grad(lambda_a) x grad(lambda_b).
-// The face functions vanish tangentially on every edge, so the basis is
-// conforming (tangential continuity) across elements. Orientation codes:
-// whitneyOrientation for p = 0, hierarchicalOrientation for p = 1.
+// Hierarchical HCurl of order p (the reference's FunctionSpaceHierarchicalHCurl,
+// gmsh "HcurlLegendre<p>"): order 0 is whitneyBasis; order p spans the
+// first-kind Nedelec space of degree p + 1 (all vector polynomials of degree
+// p plus the degree-(p+1) fields q with x . q = 0), of dimension (p+1)(p+3)
+// on a triangle and (p+1)(p+3)(p+4)/2 on a tetrahedron, with
+//  - per edge (a, b) directed from the lower global tag to the higher
+//    (p + 1 functions): w_ab, then grad(lambda_a lambda_b P_k(lambda_b - lambda_a))
+//    for k = 0 .. p-1 (curl 0; the gradients of the H1 edge functions of
+//    degree up to p + 1);
+//  - per face with vertices s0 < s1 < s2 in global tag order (3D; the
+//    triangle's own vertex order in 2D, where they are interior bubbles),
+//    for the face polynomials q = P_i(l_s1 - l_s0) P_j(l_s2 - l_s1), i + j = d,
+//    d = 0 .. p-1 (i from d down to 0), the pair
+//      lambda_s2 w_s0s1 q and lambda_s0 w_s1s2 q      (p(p+1) functions);
+//  - per tetrahedron (p >= 2), for q = P_i(l1 - l0) P_j(l2 - l1) P_k(l3 - l2),
+//    i + j + k = d, d = 0 .. p-2, the triple
+//      lambda_2 lambda_3 w_01 q, lambda_0 lambda_3 w_12 q, lambda_0 lambda_1 w_23 q
+//    ((p-1)p(p+1)/2 functions),
+// with curl(s w_ab) = grad(s) x w_ab + 2 s grad(lambda_a) x grad(lambda_b).
+// A face function vanishes tangentially on the face's edges and on the other
+// faces, an interior function on every face, and a face's functions depend
+// on its global vertex order only, so the basis is conforming (tangential
+// continuity) across elements; each order's functions come first within
+// their edge, face or element, so order p - 1 is a part of order p.
+// Orientation codes: whitneyOrientation for p = 0, hierarchicalOrientation
+// for p >= 1.
 int hcurlCount(int dim, int p);
 int hcurlOrientation(int dim, int p, const int64_t *vertexTags);
-// values [n][3] and curls [n][3]; functions ordered edge by edge (w, grad),
-// then face by face (two each)
+// Functions per edge, per face and per element interior (3D) of order p
+void hcurlEntityCounts(int dim, int p, int &perEdge, int &perFace, int &perCell);
+// values [n][3] and curls [n][3]; functions ordered edge by edge, then face
+// by face, then the interior ones
 void hcurlBasis(int dim, int p, int orientationCode, const double *uvw, double *val, double *curl);
 
 // Legendre polynomial P_k and derivative

@@ -22,14 +22,14 @@ extern "C" {
 enum {
   FG_PROBLEM_HELMHOLTZ = 0, /* -div grad u - k^2 c u = f, scalar */
   FG_PROBLEM_NAVIER = 1,    /* time-harmonic elastodynamics, 3-component field */
-  FG_PROBLEM_MAXWELL = 2,   /* curl curl E - k^2 c E, lowest-order HCurl (edge) field */
+  FG_PROBLEM_MAXWELL = 2,   /* curl curl E - k^2 c E, hierarchical HCurl field of order `order` */
   FG_PROBLEM_COUPLED = 3    /* two scalar fields u, v (orders order, order2) coupled both ways:
                                grad u.grad tu - k^2 u tu + grad v.grad tv + 2 v tv
                                + (0.5 + x) u tv + (b . grad u) tv + 0.3 grad v.grad tu,
                                b = (1, -0.5 + 0.2i, 0.25); source: -f tu + (1 + x y) tv;
                                dirichlet: u fixed on the boundary curves (2D) */
 };
-enum { FG_SPACE_LAGRANGE = 0, FG_SPACE_HIERARCHICAL_H1 = 1, FG_SPACE_HCURL = 2 /* lowest order (edge functions) */ };
+enum { FG_SPACE_LAGRANGE = 0, FG_SPACE_HIERARCHICAL_H1 = 1, FG_SPACE_HCURL = 2 /* hierarchical HCurl; order 0: edge functions */ };
 enum {
   FG_COEF_MODE_CONSTANT = 0,   /* mass coefficient -k^2 */
   FG_COEF_MODE_PER_ELEMENT = 1 /* mass coefficient -k^2 (1 + 0.3 xi_e), xi_e ~ N(0,1) per element */
@@ -107,6 +107,22 @@ double fg_problem_pre_seconds(const fg_problem *p);
  * Problems of one field (a multi-field problem's blocks go through their own
  * plans: FG_ERR_UNSUPPORTED). */
 int fg_problem_assemble(fg_problem *p, int32_t precision, double *csr_values, double *rhs, void *stream);
+
+/* The reference-element basis of the mirror's hierarchical spaces, as gmsh's
+ * getBasisFunctions gives it for one orientation (the function spaces'
+ * getBasisFunctions, src/field/FunctionSpaceHierarchicalH1.cpp:83-109,
+ * FunctionSpaceHierarchicalHCurl.cpp:81-120): space FG_SPACE_HIERARCHICAL_H1
+ * or FG_SPACE_HCURL, order, dim 2 (triangle) or 3 (tetrahedron), orientation
+ * code from fg_basis_orientation, npts points uvw [npts][3] in reference
+ * coordinates. val: [npts][n] (H1) or [npts][n][3] (HCurl); deriv:
+ * [npts][n][3], gradients (H1) or curls (HCurl); either may be NULL.
+ * Returns n, the functions per element, or -FG_ERR_ARG. */
+int fg_basis_eval(int32_t space, int32_t order, int32_t dim, int32_t code, int64_t npts, const double *uvw, double *val,
+                  double *deriv);
+/* The orientation code of an element with these global vertex tags
+ * ([dim + 1]): edge reversal bits, and in 3D the face permutations (not for
+ * HCurl order 0), or -FG_ERR_ARG. */
+int fg_basis_orientation(int32_t space, int32_t order, int32_t dim, const int64_t *vertex_tags);
 
 #ifdef __cplusplus
 }

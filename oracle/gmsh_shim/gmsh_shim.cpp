@@ -5,7 +5,7 @@
 // reference's Formulation::pre() and assemble() reach, over one in-memory
 // model installed by oracleShimSetMesh(): this project's synthetic simplex
 // meshes (fem-g_gb300/host/mesh.cpp), its quadrature rules, geometric
-// Lagrange basis, hierarchical H1 and hierarchical HCurl (orders 0, 1) bases and DOF keys
+// Lagrange basis, hierarchical H1 and hierarchical HCurl bases and DOF keys
 // (fem-g_gb300/host/refelem.cpp, formulation.cpp). These are the same tables
 // the GPU path's host mirror hands to the C ABI, so the reference's own DOF
 // creation, numbering, pattern, element integration and scatter run on

@@ -80,3 +80,36 @@ def test_maxwell_order1_matches_oracle(femg, oracle, cuda, case, precision):
             plan.set_fp64_method(femg.FG_FP64_FACTORED)
         v, _ = plan.assemble("fp64")
     assert rel(v, ref_v) <= (1e-6 if precision == "mixed" else 1e-12)
+
+
+# higher orders (HcurlLegendre<p>): (p+1)(p+3) functions per triangle, (p+1)(p+3)(p+4)/2 per tet;
+# the tensor-core path takes element matrices up to 24 x 24 (its B tile), FP64 up to 64 x 64
+HIGH = {"tri_p2": (2, 6, 2, 1), "tri_p3": (2, 4, 3, 0), "tri_p5": (2, 3, 5, 1), "tet_p2": (3, 3, 2, 1),
+        "tet_p2_m6": (3, 6, 2, 0)}
+
+
+@pytest.mark.parametrize("case", list(HIGH))
+@pytest.mark.parametrize("precision", ["fp64", "fp64_factored", "mixed"])
+def test_maxwell_high_order_matches_oracle(femg, oracle, cuda, case, precision):
+    from test_hcurl_high_order import maxwell as maxwell_p
+    dim, m, p, mode = HIGH[case]
+    prob = femg.Problem(maxwell_p(femg, dim, m, p, coef_mode=mode))
+    a = prob.arrays()
+    t, nt = prob.terms()
+    ref_v, _ = oracle.assemble(a, t, nt)
+    plan = prob.plan()
+    if precision == "mixed":
+        if a["nb"] > 24:
+            with pytest.raises(femg.FgError) as err:
+                plan.assemble("mixed")
+            assert err.value.status == femg.FG_ERR_UNSUPPORTED
+            return
+        v, _, rep = plan.assemble("mixed", report=True)
+        assert rep["global_"] <= 1e-6
+    else:
+        if precision == "fp64_factored":
+            plan.set_fp64_method(femg.FG_FP64_FACTORED)
+        v, _ = plan.assemble("fp64")
+        v2, _ = plan.assemble("fp64")
+        assert np.array_equal(v.view(np.uint64), v2.view(np.uint64))
+    assert rel(v, ref_v) <= (1e-6 if precision == "mixed" else 1e-12)
