@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         for (int t = 0; t < terms->n; ++t) {
           const DevTerm &T = terms->t[t];
           if (T.mod != g) continue;
-          const double2 v = evalExpr(T.coef, e, xq, phq, p.nb);
+          const double2 v = evalExpr(T.coef, e, xq, phq, p.nb, q, p.nq);
           if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, v));
           else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, v));
           else if (T.kind == FG_TERM_SOURCE) f = cadd(f, v);
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         S.s = make_double2(wd * f.x, wd * f.y);
         if (terms->tensorTerm >= 0) {
           double2 A[6];
-          diffusionTensor(terms, g, e, xq, cgg, A, phq, p.nb);
+          diffusionTensor(terms, g, e, xq, cgg, A, phq, p.nb, q, p.nq);
           for (int k = 0; k < 6; ++k) S.Aw[k] = make_double2(wd * A[k].x, wd * A[k].y);
         }
       }
@@ -230,39 +230,39 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         for (int t = 0; t < terms->n; ++t) {
           const DevTerm &T = terms->t[t];
           if (T.mod != g) continue;
-          if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb)));
-          else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb)));
-          else if (T.kind == FG_TERM_SOURCE) f = cadd(f, evalExpr(T.coef, e, xq, phq, p.nb));
+          if (T.kind == FG_TERM_GRAD_GRAD) cgg = cadd(cgg, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb, q, p.nq)));
+          else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb, q, p.nq)));
+          else if (T.kind == FG_TERM_SOURCE) f = cadd(f, evalExpr(T.coef, e, xq, phq, p.nb, q, p.nq));
         }
         const double wd = p.w[q] * S.det;
         double2 A6[6];
-        diffusionTensor(terms, g, e, xq, cgg, A6, phq, p.nb);  // c_gg I (+ the symmetric tensor term)
+        diffusionTensor(terms, g, e, xq, cgg, A6, phq, p.nb, q, p.nq);  // c_gg I (+ the symmetric tensor term)
         const int sym[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
         double2 M[9];
         for (int r = 0; r < 3; ++r)
           for (int c = 0; c < 3; ++c) M[3 * r + c] = A6[sym[r][c]];
         if (terms->tensorFullTerm >= 0 && terms->t[terms->tensorFullTerm].mod == g) {
           const DevTerm &T = terms->t[terms->tensorFullTerm];
-          const double2 fc = cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb));
-          for (int k = 0; k < 9; ++k) M[k] = cadd(M[k], cmul(fc, evalExpr(terms->tensorFull[k], e, xq, phq, p.nb)));
+          const double2 fc = cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb, q, p.nq));
+          for (int k = 0; k < 9; ++k) M[k] = cadd(M[k], cmul(fc, evalExpr(terms->tensorFull[k], e, xq, phq, p.nb, q, p.nq)));
         }
         double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
         if (terms->advectTerm >= 0 && terms->t[terms->advectTerm].mod == g) {
           const DevTerm &T = terms->t[terms->advectTerm];
-          const double2 fc = cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb));
-          for (int k = 0; k < 3; ++k) v[k] = cmul(fc, evalExpr(terms->advect[k], e, xq, phq, p.nb));
+          const double2 fc = cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb, q, p.nq));
+          for (int k = 0; k < 3; ++k) v[k] = cmul(fc, evalExpr(terms->advect[k], e, xq, phq, p.nb, q, p.nq));
         }
         double2 vb[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
         if (terms->vecGradTerm >= 0 && terms->t[terms->vecGradTerm].mod == g) {
           const DevTerm &T = terms->t[terms->vecGradTerm];
-          const double2 fc = cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb));
-          for (int k = 0; k < 3; ++k) vb[k] = cmul(fc, evalExpr(terms->vecGrad[k], e, xq, phq, p.nb));
+          const double2 fc = cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb, q, p.nq));
+          for (int k = 0; k < 3; ++k) vb[k] = cmul(fc, evalExpr(terms->vecGrad[k], e, xq, phq, p.nb, q, p.nq));
         }
         double2 sg[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
         if (terms->srcGradTerm >= 0 && terms->t[terms->srcGradTerm].mod == g) {
           const DevTerm &T = terms->t[terms->srcGradTerm];
-          const double2 fc = evalExpr(T.coef, e, xq, phq, p.nb);
-          for (int k = 0; k < 3; ++k) sg[k] = cmul(fc, evalExpr(terms->srcGrad[k], e, xq, phq, p.nb));
+          const double2 fc = evalExpr(T.coef, e, xq, phq, p.nb, q, p.nq);
+          for (int k = 0; k < 3; ++k) sg[k] = cmul(fc, evalExpr(terms->srcGrad[k], e, xq, phq, p.nb, q, p.nq));
         }
         for (int k = 0; k < 9; ++k) S.M[k] = make_double2(wd * M[k].x, wd * M[k].y);
         for (int k = 0; k < 3; ++k) S.v[k] = make_double2(wd * v[k].x, wd * v[k].y);
@@ -391,10 +391,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
           const DevTerm &T = terms->t[t];
           if (T.mod != g) continue;
           if (T.kind == FG_TERM_ELASTIC) {
-            lam = cadd(lam, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb)));
-            mu = cadd(mu, cmul(T.factor, evalExpr(T.coef2, e, xq, phq, p.nb)));
+            lam = cadd(lam, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb, q, p.nq)));
+            mu = cadd(mu, cmul(T.factor, evalExpr(T.coef2, e, xq, phq, p.nb, q, p.nq)));
           } else if (T.kind == FG_TERM_MASS) {
-            cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb)));
+            cm = cadd(cm, cmul(T.factor, evalExpr(T.coef, e, xq, phq, p.nb, q, p.nq)));
           }
         }
         const double wd = p.w[q] * S.det;
@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         for (int t = 0; t < terms->n; ++t) {
           const DevTerm &T = terms->t[t];
           if (T.mod != g) continue;
-          const double2 v = evalExpr(T.coef, e, xq);
+          const double2 v = evalExpr(T.coef, e, xq, nullptr, 0, q, p.nq);
           if (T.kind == FG_TERM_GRAD_GRAD) cc = cadd(cc, cmul(T.factor, v));
           else if (T.kind == FG_TERM_MASS) cm = cadd(cm, cmul(T.factor, v));
         }
@@ -528,8 +528,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockElem)
         S.b = make_double2(wd * cm.x, wd * cm.y);
         if (tensor) {
           double2 A[6], B[6];
-          coefTensor(terms, terms->tensorTerm, terms->tensor, g, e, xq, cc, A);
-          coefTensor(terms, terms->tensorMassTerm, terms->tensorMass, g, e, xq, cm, B);
+          coefTensor(terms, terms->tensorTerm, terms->tensor, g, e, xq, cc, A, nullptr, 0, q, p.nq);
+          coefTensor(terms, terms->tensorMassTerm, terms->tensorMass, g, e, xq, cm, B, nullptr, 0, q, p.nq);
           for (int k = 0; k < 6; ++k) {
             S.Aw[k] = make_double2(wd * A[k].x, wd * A[k].y);
             S.Bw[k] = make_double2(wd * B[k].x, wd * B[k].y);

@@ -728,7 +728,7 @@ __global__ void k_rhs_fp64(const PlanDev p, const DevTerms *__restrict__ terms, 
       double2 f = make_double2(0.0, 0.0);
       for (int t = 0; t < terms->n; ++t)
         if (terms->t[t].kind == FG_TERM_SOURCE)
-          f = cadd(f, evalExpr(terms->t[t].coef, e, xq, p.bval + ((size_t)o * p.nq + q) * p.nb, p.nb));
+          f = cadd(f, evalExpr(terms->t[t].coef, e, xq, p.bval + ((size_t)o * p.nq + q) * p.nb, p.nb, q, p.nq));
       s = make_double2(p.w[q] * det * f.x, p.w[q] * det * f.y);
     }
     s.x = __shfl_sync(0xffffffffu, s.x, 0);

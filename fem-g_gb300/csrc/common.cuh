@@ -498,8 +498,10 @@ __device__ inline double2 cUnary(int op, int arg, double2 z) {
 // Evaluate a coefficient expression at element e and physical point x; phi:
 // the scalar basis values at the point (nb of them) for field nodes, null
 // where the expression is evaluated once per element (field nodes make an
-// expression point-dependent, which those paths refuse)
-__device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x, const double *phi = nullptr, int nb = 0) {
+// expression point-dependent, which those paths refuse); q and nq: the
+// point's index in the rule and the rule's size, for point tables
+__device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x, const double *phi = nullptr, int nb = 0,
+                                   int q = 0, int nq = 1) {
   if (ex.cls == kExprConst) return ex.cval;
   double2 st[16];
   int sp = 0;
@@ -511,6 +513,7 @@ __device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x
       case FG_OP_Y: st[sp++] = make_double2(x[1], 0.0); break;
       case FG_OP_Z: st[sp++] = make_double2(x[2], 0.0); break;
       case FG_OP_ELEM: st[sp++] = ex.arr[in.arg][e]; break;
+      case FG_OP_POINT: st[sp++] = ex.arr[in.arg][e * nq + q]; break;
       case FG_OP_FIELD: {
         const double2 *u = ex.arr[in.arg] + (size_t)e * nb;
         double2 s = make_double2(0.0, 0.0);
@@ -555,18 +558,18 @@ __device__ inline double2 evalExpr(const DevExpr &ex, int64_t e, const double *x
 // kind and D the entries (00, 11, 22, 01, 02, 12) of tensor term `term`
 // (none when term < 0).
 __device__ inline void coefTensor(const DevTerms *terms, int term, const DevExpr *D, int g, int64_t e, const double *x, double2 c0,
-                                  double2 *A, const double *phi = nullptr, int nb = 0) {
+                                  double2 *A, const double *phi = nullptr, int nb = 0, int q = 0, int nq = 1) {
   for (int k = 0; k < 6; ++k) A[k] = k < 3 ? c0 : make_double2(0.0, 0.0);
   if (term < 0) return;
   const DevTerm &T = terms->t[term];
   if (T.mod != g) return;
-  const double2 fc = cmul(T.factor, evalExpr(T.coef, e, x, phi, nb));
-  for (int k = 0; k < 6; ++k) A[k] = cadd(A[k], cmul(fc, evalExpr(D[k], e, x, phi, nb)));
+  const double2 fc = cmul(T.factor, evalExpr(T.coef, e, x, phi, nb, q, nq));
+  for (int k = 0; k < 6; ++k) A[k] = cadd(A[k], cmul(fc, evalExpr(D[k], e, x, phi, nb, q, nq)));
 }
 // the grad-grad (diffusion) tensor
 __device__ inline void diffusionTensor(const DevTerms *terms, int g, int64_t e, const double *x, double2 cgg, double2 *A,
-                                       const double *phi = nullptr, int nb = 0) {
-  coefTensor(terms, terms->tensorTerm, terms->tensor, g, e, x, cgg, A, phi, nb);
+                                       const double *phi = nullptr, int nb = 0, int q = 0, int nq = 1) {
+  coefTensor(terms, terms->tensorTerm, terms->tensor, g, e, x, cgg, A, phi, nb, q, nq);
 }
 // F(a, b) = sum_rs Q[3a + r] A(r, s) Q[3b + s] for the six pairs (a, b), of
 // the real (comp 0) or imaginary (comp 1) part of the symmetric A

@@ -552,7 +552,8 @@ int uploadDirichlet(fg_plan *plan, const double *dirichlet, const double **out, 
 static int classify(const fg_expr &ex) {
   int cls = kExprConst;
   for (int k = 0; k < ex.n_code; ++k) {
-    if (ex.code[k].op == FG_OP_X || ex.code[k].op == FG_OP_Y || ex.code[k].op == FG_OP_Z || ex.code[k].op == FG_OP_FIELD)
+    if (ex.code[k].op == FG_OP_X || ex.code[k].op == FG_OP_Y || ex.code[k].op == FG_OP_Z || ex.code[k].op == FG_OP_FIELD ||
+        ex.code[k].op == FG_OP_POINT)
       return kExprPoint;
     if (ex.code[k].op == FG_OP_ELEM) cls = kExprElem;
   }
@@ -627,8 +628,8 @@ static int validateExpr(const fg_expr &ex) {
   int depth = 0;
   for (int k = 0; k < ex.n_code; ++k) {
     const int op = ex.code[k].op;
-    if (op <= FG_OP_ELEM || op == FG_OP_FIELD) {
-      if ((op == FG_OP_ELEM || op == FG_OP_FIELD) &&
+    if (op <= FG_OP_ELEM || op == FG_OP_FIELD || op == FG_OP_POINT) {
+      if ((op == FG_OP_ELEM || op == FG_OP_FIELD || op == FG_OP_POINT) &&
           (ex.code[k].arg < 0 || ex.code[k].arg >= ex.n_arrays || !ex.elem_values[ex.code[k].arg]))
         return 1;
       if (++depth > 16) return 1;
@@ -646,7 +647,8 @@ static int validateExpr(const fg_expr &ex) {
 }
 
 // arrays: the device copies of per-element coefficient arrays ([E] complex
-// each, or [E][nb] for the field values of FG_OP_FIELD); the first `used` are
+// each, [E][nb] for the field values of FG_OP_FIELD, [E][nq] for the point
+// tables of FG_OP_POINT); the first `used` are
 // this upload's, later ones are reused from the previous upload instead of
 // freed and allocated again (a buffer too small for its new array is replaced).
 static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complexOut, std::vector<void *> &arrays, size_t &used) {
@@ -672,13 +674,14 @@ static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complex
     if (v.imag() != 0.0) *complexOut = true;
   }
   for (int a = 0; a < ex.n_arrays; ++a) {
-    bool elem = false, field = false;
+    bool elem = false, field = false, point = false;
     for (int k = 0; k < ex.n_code; ++k) {
       elem = elem || (ex.code[k].op == FG_OP_ELEM && ex.code[k].arg == a);
       field = field || (ex.code[k].op == FG_OP_FIELD && ex.code[k].arg == a);
+      point = point || (ex.code[k].op == FG_OP_POINT && ex.code[k].arg == a);
     }
-    if (elem && field) {
-      setLastError("a coefficient array is used both per element and as field values");
+    if ((int)elem + (int)field + (int)point > 1) {
+      setLastError("a coefficient array is used in two ways (per element, per point, field values)");
       return FG_ERR_ARG;
     }
     if (field && plan->d.form != FG_FORM_0) {
@@ -689,7 +692,7 @@ static int devExpr(fg_plan *plan, const fg_expr &ex, DevExpr *out, bool *complex
       setLastError("field values (FG_OP_FIELD) are not supported in two-field plans");
       return FG_ERR_UNSUPPORTED;
     }
-    const size_t bytes = (size_t)plan->E * 16 * (field ? (size_t)plan->d.nb : 1);
+    const size_t bytes = (size_t)plan->E * 16 * (field ? (size_t)plan->d.nb : point ? (size_t)plan->d.nq : 1);
     if (isDevicePointer(ex.elem_values[a])) {
       out->arr[a] = (const double2 *)ex.elem_values[a];
       *complexOut = true;  // cannot scan device data cheaply: assume complex

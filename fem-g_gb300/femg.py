@@ -30,7 +30,7 @@ FG_FP64_QUADRATURE, FG_FP64_FACTORED = range(2)
 (FG_OP_CONST, FG_OP_X, FG_OP_Y, FG_OP_Z, FG_OP_ELEM, FG_OP_ADD, FG_OP_SUB, FG_OP_MUL, FG_OP_DIV, FG_OP_NEG,
  FG_OP_HEAVISIDE, FG_OP_FIELD, FG_OP_SQRT, FG_OP_EXP, FG_OP_LN, FG_OP_LOG10, FG_OP_POW, FG_OP_SIN, FG_OP_COS, FG_OP_TAN,
  FG_OP_SINH, FG_OP_COSH, FG_OP_TANH, FG_OP_ASIN, FG_OP_ACOS, FG_OP_ATAN, FG_OP_ASINH, FG_OP_ACOSH, FG_OP_ATANH, FG_OP_ABS,
- FG_OP_CONJ, FG_OP_REAL, FG_OP_IMAG, FG_OP_CBRT, FG_OP_ATAN2) = range(35)
+ FG_OP_CONJ, FG_OP_REAL, FG_OP_IMAG, FG_OP_CBRT, FG_OP_ATAN2, FG_OP_POINT) = range(36)
 FG_EXPR_MAX_CODE = 32
 FG_EXPR_MAX_ARRAYS = 4
 

@@ -169,7 +169,11 @@ enum {
   FG_OP_REAL = 31,
   FG_OP_IMAG = 32,
   FG_OP_CBRT = 33,  /* a^(1/3): real cube root for a > 0, principal complex root otherwise */
-  FG_OP_ATAN2 = 34  /* binary: atan2(Re a, Re b) of the two topmost (scalarBinaryOperators.h:21, real arguments) */
+  FG_OP_ATAN2 = 34, /* binary: atan2(Re a, Re b) of the two topmost (scalarBinaryOperators.h:21, real arguments) */
+  FG_OP_POINT = 35  /* push elem_values[arg][element * nq + q]: the coefficient at every integration point of the
+                       bucket, element-major ([n_elements * nq][2] complex), e.g. a Function the caller evaluates with
+                       the reference's own evaluator (EquationEvaluator::initialize, EquationEvaluator.h:155-168)
+                       instead of describing it; point-dependent, so FP64 paths only */
 };
 typedef struct {
   int32_t op;

@@ -44,7 +44,7 @@ enum {
 };
 enum { OP_CONST = 0, OP_X, OP_Y, OP_Z, OP_ELEM, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_HEAVISIDE, OP_FIELD,
        OP_SQRT, OP_EXP, OP_LN, OP_LOG10, OP_POW, OP_SIN, OP_COS, OP_TAN, OP_SINH, OP_COSH, OP_TANH, OP_ASIN, OP_ACOS,
-       OP_ATAN, OP_ASINH, OP_ACOSH, OP_ATANH, OP_ABS, OP_CONJ, OP_REAL, OP_IMAG, OP_CBRT, OP_ATAN2 };
+       OP_ATAN, OP_ASINH, OP_ACOSH, OP_ATANH, OP_ABS, OP_CONJ, OP_REAL, OP_IMAG, OP_CBRT, OP_ATAN2, OP_POINT };
 
 /* same memory layout as fg_instr / fg_expr / fg_term_desc of the C ABI, so
  * the tests can pass the product's term descriptors unchanged */
@@ -174,7 +174,7 @@ static cplx or_unary(int op, int arg, cplx z) {
   return z;
 }
 
-static cplx eval_expr(const or_expr *ex, int64_t e, const double *x, const double *phi, int nb) {
+static cplx eval_expr(const or_expr *ex, int64_t e, const double *x, const double *phi, int nb, int q, int nq) {
   cplx st[16];
   int sp = 0;
   for (int k = 0; k < ex->n_code; ++k) {
@@ -185,6 +185,12 @@ static cplx eval_expr(const or_expr *ex, int64_t e, const double *x, const doubl
       case OP_Y: st[sp++] = x[1]; break;
       case OP_Z: st[sp++] = x[2]; break;
       case OP_ELEM: st[sp++] = ex->elem_values[in->arg][2 * e] + I * ex->elem_values[in->arg][2 * e + 1]; break;
+      /* the coefficient at point q of element e, from a table the caller filled */
+      case OP_POINT: {
+        const double *v = ex->elem_values[in->arg] + 2 * ((size_t)e * nq + q);
+        st[sp++] = v[0] + I * v[1];
+        break;
+      }
       case OP_FIELD: {
         const double *u = ex->elem_values[in->arg] + 2 * (size_t)e * nb;
         cplx s = 0.0;
@@ -376,9 +382,9 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
         double det = or_jacobian(b, e, q, J, xq);
         if (or_jacmod_apply(&T->jacmod, xq, J, &det)) or_jacmod_err = 1;
         const double *bf = b->bval + ((size_t)o * nq + q) * nb;
-        const cplx c = eval_expr(&T->coef, e, xq, bf, nb);
+        const cplx c = eval_expr(&T->coef, e, xq, bf, nb, q, nq);
         cplx fv[3];
-        for (int k = 0; k < 3; ++k) fv[k] = c * eval_expr(&T->tensor[k], e, xq, bf, nb);
+        for (int k = 0; k < 3; ++k) fv[k] = c * eval_expr(&T->tensor[k], e, xq, bf, nb, q, nq);
         or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
         for (int i = 0; i < nb; ++i) be[i] += b->w[q] * det * (conj(G[i]) * fv[0] + conj(G[nb + i]) * fv[1] + conj(G[2 * nb + i]) * fv[2]);
       }
@@ -391,7 +397,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
         double det = or_jacobian(b, e, q, J, xq);
         if (or_jacmod_apply(&T->jacmod, xq, J, &det)) or_jacmod_err = 1;
         const double *bf = b->bval + ((size_t)o * nq + q) * nb;
-        cplx f = eval_expr(&T->coef, e, xq, bf, nb);
+        cplx f = eval_expr(&T->coef, e, xq, bf, nb, q, nq);
         for (int i = 0; i < nb; ++i)
           for (int c = 0; c < mult; ++c) be[i * mult + c] += b->w[q] * det * conj(bf[i]) * f;
       }
@@ -405,7 +411,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
       if (or_jacmod_apply(&T->jacmod, xq, J, &det)) or_jacmod_err = 1;
       const double wd = b->w[q] * det;
       const double *ph = b->form == 0 ? b->bval + ((size_t)o * nq + q) * nb : NULL;
-      cplx c = eval_expr(&T->coef, e, xq, ph, nb);
+      cplx c = eval_expr(&T->coef, e, xq, ph, nb, q, nq);
       if (T->kind == TERM_MASS && b->form == 1) {
         /* FieldEvaluator<Form1>: J^-T applied to the vector values */
         or_form1(J, b->bval + ((size_t)o * nq + q) * nb * 3, nb, G);
@@ -444,7 +450,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
         static const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
         cplx D[3][3];
         for (int k = 0; k < 6; ++k) {
-          const cplx d = c * eval_expr(&T->tensor[k], e, xq, ph, nb);
+          const cplx d = c * eval_expr(&T->tensor[k], e, xq, ph, nb, q, nq);
           D[ab[k][0]][ab[k][1]] = D[ab[k][1]][ab[k][0]] = d;
         }
         if (b->form == 1 && T->kind == TERM_GRAD_GRAD_TENSOR) {
@@ -466,7 +472,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
       } else if (T->kind == TERM_GRAD_GRAD_TENSOR_FULL) {
         /* a general TensorFunction: the unknown's field is c D G_j (row-major D) */
         cplx D[3][3];
-        for (int k = 0; k < 9; ++k) D[k / 3][k % 3] = c * eval_expr(&T->tensor[k], e, xq, ph, nb);
+        for (int k = 0; k < 9; ++k) D[k / 3][k % 3] = c * eval_expr(&T->tensor[k], e, xq, ph, nb, q, nq);
         or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
         for (int ii = 0; ii < n; ++ii)
           for (int jj = 0; jj < n; ++jj) {
@@ -478,7 +484,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
       } else if (T->kind == TERM_VECTOR_GRAD_TEST) {
         /* VectorFunction b times dof(u), tested against grad(tf(u)): (c b phi_j) . conj(G_i) */
         cplx bv[3];
-        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, ph, nb);
+        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, ph, nb, q, nq);
         or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
         const double *bf = b->bval + ((size_t)o * nq + q) * nb;
         for (int ii = 0; ii < n; ++ii)
@@ -489,7 +495,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
       } else if (T->kind == TERM_ADVECTION) {
         /* VectorFunction b times grad(dof u), tested against tf(u): (c b . G_j) conj(phi_i) */
         cplx bv[3];
-        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, ph, nb);
+        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, ph, nb, q, nq);
         or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
         const double *bf = b->bval + ((size_t)o * nq + q) * nb;
         for (int ii = 0; ii < n; ++ii)
@@ -511,7 +517,7 @@ static void or_element(const or_bucket *b, const or_term *terms, int nterms, dou
         /* (C : grad u) : grad v with grad u_{a,k} = d u_a / d x_k: for unknown
          * DOF (j, beta) the field is the 3x3 matrix D with D[beta][k] = G[k][j];
          * C : D = lambda tr(D) I + mu (D + D^T) */
-        cplx lam = c, mu = eval_expr(&T->coef2, e, xq, ph, nb);
+        cplx lam = c, mu = eval_expr(&T->coef2, e, xq, ph, nb, q, nq);
         or_form1(J, b->bgrad + ((size_t)o * nq + q) * nb * 3, nb, G);
         for (int ii = 0; ii < n; ++ii)
           for (int jj = 0; jj < n; ++jj) {
@@ -715,7 +721,7 @@ static void or_element_coupled(const or_bucket *bt, const or_bucket *bu, const o
       const double *phU = bu->bval + ((size_t)oU * nq + q) * nU;
       /* field nodes read the unknown field's values (the coefficient's field
        * is evaluated with the unknown's element DOFs) */
-      const cplx c = eval_expr(&T->coef, e, xq, phU, nU);
+      const cplx c = eval_expr(&T->coef, e, xq, phU, nU, q, nq);
       or_form1(J, bt->bgrad + ((size_t)oT * nq + q) * nT * 3, nT, GT);
       or_form1(J, bu->bgrad + ((size_t)oU * nq + q) * nU * 3, nU, GU);
       if (T->kind == TERM_MASS) {
@@ -730,7 +736,7 @@ static void or_element_coupled(const or_bucket *bt, const or_bucket *bu, const o
           }
       } else if (T->kind == TERM_GRAD_GRAD_TENSOR_FULL) {
         cplx D[3][3];
-        for (int k = 0; k < 9; ++k) D[k / 3][k % 3] = c * eval_expr(&T->tensor[k], e, xq, phU, nU);
+        for (int k = 0; k < 9; ++k) D[k / 3][k % 3] = c * eval_expr(&T->tensor[k], e, xq, phU, nU, q, nq);
         for (int i = 0; i < nT; ++i)
           for (int j = 0; j < nU; ++j) {
             cplx s = 0.0;
@@ -740,7 +746,7 @@ static void or_element_coupled(const or_bucket *bt, const or_bucket *bu, const o
           }
       } else if (T->kind == TERM_VECTOR_GRAD_TEST) {
         cplx bv[3];
-        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, phU, nU);
+        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, phU, nU, q, nq);
         for (int i = 0; i < nT; ++i)
           for (int j = 0; j < nU; ++j) {
             cplx s = bv[0] * GT[i] + bv[1] * GT[nT + i] + bv[2] * GT[2 * nT + i];
@@ -748,7 +754,7 @@ static void or_element_coupled(const or_bucket *bt, const or_bucket *bu, const o
           }
       } else if (T->kind == TERM_ADVECTION) {
         cplx bv[3];
-        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, phU, nU);
+        for (int k = 0; k < 3; ++k) bv[k] = c * eval_expr(&T->tensor[k], e, xq, phU, nU, q, nq);
         for (int i = 0; i < nT; ++i)
           for (int j = 0; j < nU; ++j) {
             cplx s = bv[0] * GU[j] + bv[1] * GU[nU + j] + bv[2] * GU[2 * nU + j];
