@@ -1,0 +1,426 @@
+// GpuFormulation<T>: GmshFEM's Formulation<T> with assemble() on the GB300
+// path, the reference-side binding of the C ABI (include/fem_g_gb300.h).
+//
+// A maintainer adds this header to GmshFEM (it includes GmshFEM's own
+// headers and links libfemg.so); a user program changes only the type of its
+// formulation. pre() stays the reference's (DOF dictionary, Hilbert
+// numbering, CSR pattern: Formulation::pre, src/problem/Formulation.cpp:
+// 897-1039). assemble() replaces Formulation::assemble
+// (src/problem/Formulation.cpp:1152-1215) and its _assembleDim loop
+// (:1418-1493): one plan per (entity, element type) bucket of the terms,
+// built from the same sources the reference's Assembler reads,
+//  - the mesh: gmsh::model::mesh::getElementsByType / getNodesByElementType;
+//  - the rule: FunctionSpaceInterface::getGaussInfo (GetGaussInfo,
+//    src/field/FunctionSpaceInterface.cpp:470-481) and the geometric
+//    Lagrange basis of gmsh::model::mesh::getBasisFunctions;
+//  - the space: FunctionSpaceInterface::getBasisFunctions with the dense
+//    orientations (src/field/FunctionSpaceHierarchicalH1.cpp:83-109);
+//  - the DOF map: FunctionSpaceInterface::getKeys and FieldInterface::
+//    getIndices (src/field/FieldInterface.cpp:959-976), the pattern through
+//    getLHS (MatrixCRSFast, a friend of MatrixFactory), the Dirichlet values
+//    through FieldInterface::getFixedValues (s_setDirichletConditions,
+//    Formulation.cpp:1041-1054);
+//  - the terms: recorded where integral() is called. The reference keeps a
+//    term's equations inside the term, out of reach, so the subclass hides
+//    integral() with a template that forwards to the reference's overloads
+//    and keeps a copy of the equations (EquationInterface::copy). Their
+//    coefficients are not described but evaluated by the reference's own
+//    evaluators at the bucket's integration points
+//    (EquationEvaluatorInterface::initialize and operator(),
+//    src/term/evaluator/EquationEvaluator.h:86-103; Function::evaluate for
+//    sources), and passed as constants, per-element arrays (FG_OP_ELEM) or
+//    point tables (FG_OP_POINT), whichever the values are.
+// Terms this binding does not map (vector or tensor coefficients, HCurl and
+// compound fields, time derivatives, Jacobian modificators, linked DOFs,
+// coefficients on the test function) make assemble() fail with the
+// reference's convention: an error message and zero A and b
+// (Formulation.cpp:1200-1209). They are assembled by GPU plans through the
+// C ABI directly (term kinds FG_TERM_*), or by Formulation<T> itself.
+#ifndef FEMG_GPU_FORMULATION_H
+#define FEMG_GPU_FORMULATION_H
+
+#include <complex>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "Equation.h"
+#include "EquationEvaluator.h"
+#include "FieldInterface.h"
+#include "Formulation.h"
+#include "FunctionSpaceInterface.h"
+#include "MatrixCRSFast.h"
+#include "MatrixFactory.h"
+#include "MatrixModule.h"
+#include "Message.h"
+#include "OmpInterface.h"
+#include "UnknownField.h"
+#include "VectorFactory.h"
+#include "fem_g_gb300.h"
+#include "gmsh.h"
+#include "numa.h"
+
+namespace gmshfem::problem {
+
+template <class T>
+class GpuFormulation : public Formulation<T> {
+  static_assert(std::is_same<T, std::complex<double>>::value, "the GB300 path assembles complex<double> systems");
+  using PointVec = std::vector<double, numa::allocator<double>>;
+
+  // One side of a term: an equation (the unknown's or the test function's)
+  // or the source function of a linear term
+  struct Side {
+    virtual ~Side() = default;
+    virtual field::FieldInterface<T> *field() const { return nullptr; }
+    virtual field::Form form() const { return field::Form::Form0; }
+    virtual bool derivative() const { return false; }
+    virtual bool dt() const { return false; }
+    // the coefficient at the points (x, y, z) [n][3] of the bucket, element-major
+    virtual void values(const PointVec &points, const std::vector<double> &gauss, int elementType,
+                        const std::pair<int, int> &entity, std::vector<T> &out) const = 0;
+  };
+
+  // c * (dof or tf, gradient or value) with a scalar coefficient c: the
+  // reference's EquationLhs<T, Degree0, F, ScalarProduct>, whose evaluator
+  // scales a field by c (EquationEvaluator.h:107-131), so a 1 x 1 field of 1
+  // gives c at each point
+  template <field::Form F>
+  struct EquationSide final : Side {
+    using Eq = equation::EquationLhs<T, Degree::Degree0, F, equation::Product::ScalarProduct>;
+    std::unique_ptr<Eq> eq;
+    explicit EquationSide(const Eq &e) : eq(e.copy()) {}
+    field::FieldInterface<T> *field() const override { return eq->getField(); }
+    field::Form form() const override { return eq->form(); }
+    bool derivative() const override { return eq->isDerivative(); }
+    bool dt() const override {
+      const auto *u = eq->getUnknownField();
+      return u && u->type() != equation::UnknownFieldType::NotDt;
+    }
+    void values(const PointVec &points, const std::vector<double> &gauss, int elementType, const std::pair<int, int> &entity,
+                std::vector<T> &out) const override {
+      std::unique_ptr<term::evaluator::EquationEvaluatorInterface<T, F>> ev(eq->getEquationEvaluator());
+      ev->initialize(points, gauss, elementType, entity);
+      const size_t n = ev->isConstant(entity) ? 1 : points.size() / 3;
+      out.resize(n);
+      Eigen::MatrixX<T> value(1, 1);
+      const Eigen::MatrixX<double> one = Eigen::MatrixX<double>::Ones(1, 1);
+      for (size_t k = 0; k < n; ++k) {
+        (*ev)(value, one, (unsigned int)k);
+        out[k] = value(0, 0);
+      }
+      ev->clear();
+    }
+  };
+
+  // the source function f of integral(f, tf(u)), a scalar Function
+  struct FunctionSide final : Side {
+    function::Function<T, Degree::Degree0> f;
+    explicit FunctionSide(const function::Function<T, Degree::Degree0> &g) : f(g) {}
+    void values(const PointVec &points, const std::vector<double> &gauss, int elementType, const std::pair<int, int> &entity,
+                std::vector<T> &out) const override {
+      if (f.isConstant(entity)) {
+        T c;
+        f.evaluate(c, 0., 0., 0., entity);
+        out.assign(1, c);
+        return;
+      }
+      std::vector<T, numa::allocator<T>> v;
+#pragma omp parallel num_threads(omp::getMaxThreads())
+      f.evaluate(v, points, gauss, elementType, entity);
+      out.assign(v.begin(), v.end());
+    }
+  };
+
+  struct Recorded {
+    std::unique_ptr<Side> lhs, rhs;  // lhs: the unknown's side or the source; rhs: the test function's
+    bool bilinear = false;
+    std::vector<std::pair<int, int>> entities;
+    bool jacobianModificators = false;
+    std::string integrationType;
+    std::string unsupported;  // why the term cannot take the GPU path
+  };
+  std::vector<Recorded> _recorded;
+
+  template <Degree DC, field::Form F, equation::Product P>
+  static std::unique_ptr<Side> side(const equation::EquationLhs<T, DC, F, P> &e) {
+    if constexpr (DC == Degree::Degree0 && P == equation::Product::ScalarProduct) return std::make_unique<EquationSide<F>>(e);
+    else return nullptr;
+  }
+  // dof(u), tf(u), grad(...): the equation made from an unknown field owns and
+  // deletes it (Equation.cpp:19-34), and the reference's integral() makes
+  // one from the object the user passed, so the side is made from a copy
+  template <field::Form F>
+  static std::unique_ptr<Side> side(const equation::UnknownField<T, F> &u) {
+    const equation::UnknownField<T, F> *own = u.copy();
+    return side(static_cast<equation::EquationLhs<T, Degree::Degree0, F, equation::Product::ScalarProduct>>(*own));
+  }
+  // a scalar source function (ScalarFunction and the other Function<T, Degree0> types), or a form not mapped
+  template <class O>
+  static std::unique_ptr<Side> side(const O &o) {
+    if constexpr (std::is_base_of<function::Function<T, Degree::Degree0>, O>::value) return std::make_unique<FunctionSide>(o);
+    else return nullptr;
+  }
+
+ public:
+  using Formulation<T>::Formulation;
+  ~GpuFormulation() override { releasePlans(); }
+
+  // integral() of the reference, and the record of the term for assemble()
+  template <class L, class R>
+  unsigned int integral(const L &lhs, const R &rhs, const domain::GeometricObject &domain, const std::string &integrationType,
+                        const term::ProductType productType = term::ProductType::Hermitian) {
+    // the sides are copied first: the reference's integral() takes over the
+    // unknown-field objects that dof() and tf() made
+    Recorded r;
+    r.lhs = side(lhs);
+    r.rhs = side(rhs);
+    const unsigned int tag = Formulation<T>::integral(lhs, rhs, domain, integrationType, productType);
+    r.integrationType = integrationType;
+    for (auto it = domain.cbegin(); it != domain.cend(); ++it) {
+      r.entities.push_back(*it);
+      r.jacobianModificators = r.jacobianModificators || domain.haveJacobiansModificators(*it);
+    }
+    if (!r.lhs || !r.rhs) r.unsupported = "a vector or tensor coefficient, or a term of another form";
+    else {
+      r.bilinear = r.lhs->field() != nullptr;
+      if (!r.rhs->field()) r.unsupported = "no test function";
+      else if (r.jacobianModificators) r.unsupported = "Jacobian modificators";
+      else if (r.bilinear && r.lhs->dt()) r.unsupported = "a time derivative of the unknown";
+      else if (r.bilinear && r.lhs->field() != r.rhs->field()) r.unsupported = "two fields";
+      else if (r.rhs->field()->form() != field::Form::Form0 || r.rhs->field()->multiplicity() != 1)
+        r.unsupported = "a field that is not a scalar H1 field";
+      else if (r.bilinear && r.lhs->derivative() != r.rhs->derivative()) r.unsupported = "a gradient against a value";
+      else if (productType != term::ProductType::Hermitian) r.unsupported = "a product other than the hermitian one";
+    }
+    _recorded.push_back(std::move(r));
+    return tag;
+  }
+
+  common::Timer pre(const DofsSort::Algorithm algo = common::Options::instance()->dofsSortAlgorithm) override {
+    releasePlans();
+    return Formulation<T>::pre(algo);  // numbering and pattern stay the reference's
+  }
+
+  common::Timer assemble(const bool separate = false,
+                         const ElementsSort::Algorithm algo = common::Options::instance()->elementsSortAlgorithm) override {
+    common::Timer time;
+    time.tick();
+    try {
+      if (separate) throw std::runtime_error("separate matrices: use fg_assemble_separate through the C ABI");
+      assembleOnGpu();
+    } catch (const std::exception &e) {
+      msg::error << "Unable to assemble the system" << msg::endl;
+      msg::error << e.what() << msg::endl;
+      this->_A->setToZero();
+      for (auto &bi : this->_multiB) bi.setToZero();
+    }
+    (void)algo;
+    time.tock();
+    return time;
+  }
+
+ private:
+  struct Bucket {
+    std::pair<int, int> entity;
+    int elementType;
+    std::string integrationType;
+    field::FieldInterface<T> *field;
+    std::vector<const Recorded *> terms;
+  };
+  std::map<std::string, fg_plan *> _plans;
+
+  void releasePlans() {
+    for (auto &kv : _plans) fg_plan_destroy(kv.second);
+    _plans.clear();
+  }
+
+  static void check(int status) {
+    if (status != FG_OK) throw std::runtime_error(fg_last_error());
+  }
+
+  void assembleOnGpu() {
+    const unsigned long long nRows = this->_dofs.nbrUnknownDofs();
+    if (this->numRHS() != this->_multiB.size()) {
+      this->_multiB.clear();
+      this->_multiB.resize(this->numRHS());
+    }
+    for (auto &bi : this->_multiB) bi.init(nRows);
+    if (this->_A->getModule() == nullptr) this->_A->setModule(new system::AModule<T>(this->_A));
+    if (this->_dofs.nbrLinkedDofs() != 0) throw std::runtime_error("linked DOFs: not mapped by this binding");
+    for (const auto &r : _recorded)
+      if (!r.unsupported.empty()) throw std::runtime_error("a term takes no GPU path here: " + r.unsupported);
+    if (nRows == 0) return;
+    // Dirichlet values (s_setDirichletConditions)
+    std::vector<T> valuesDC(this->_dofs.nbrFixedDofs());
+    for (auto &uf : this->_unknownFields) uf.second->getFixedValues(valuesDC);
+    // the pattern of pre()
+    algebra::MatrixCRSFast<T> A;
+    this->getLHS(A);
+    const unsigned long long nnz = A.ai()[nRows];
+    std::vector<uint64_t> ai(A.ai(), A.ai() + nRows + 1), aj(A.aj(), A.aj() + nnz);
+    const bool upper = this->_A->getOptions().symmetric() || this->_A->getOptions().hermitian();
+    // buckets: (entity, element type, rule, field)
+    std::map<std::string, Bucket> buckets;
+    for (const auto &r : _recorded)
+      for (const auto &ent : r.entities) {
+        std::vector<int> types;
+        gmsh::model::mesh::getElementTypes(types, ent.first, ent.second);
+        for (int type : types) {
+          const std::string key = std::to_string(ent.first) + "/" + std::to_string(ent.second) + "/" + std::to_string(type) + "/" +
+                                  r.integrationType + "/" + std::to_string(r.rhs->field()->tag());
+          Bucket &b = buckets[key];
+          b.entity = ent;
+          b.elementType = type;
+          b.integrationType = r.integrationType;
+          b.field = r.rhs->field();
+          b.terms.push_back(&r);
+        }
+      }
+    T *values = const_cast<T *>(this->_A->getModule()->getMatrix());  // MatrixModule.cpp:167-171
+    std::vector<T> rhs(nRows, T(0.0)), v(nnz), b(nRows);
+    for (unsigned long long k = 0; k < nnz; ++k) values[k] = T(0.0);
+    for (auto &kv : buckets) {
+      assembleBucket(kv.first, kv.second, ai, aj, upper, valuesDC, v, b);
+      for (unsigned long long k = 0; k < nnz; ++k) values[k] += v[k];
+      for (unsigned long long k = 0; k < nRows; ++k) rhs[k] += b[k];
+    }
+    for (unsigned long long k = 0; k < nRows; ++k)
+      if (rhs[k] != T(0.0)) this->_multiB[this->_currentRHS].addValue(k, rhs[k]);
+  }
+
+  void assembleBucket(const std::string &key, const Bucket &bk, const std::vector<uint64_t> &ai, const std::vector<uint64_t> &aj,
+                      bool upper, const std::vector<T> &valuesDC, std::vector<T> &v, std::vector<T> &b) {
+    const auto &ent = bk.entity;
+    const int type = bk.elementType;
+    field::FunctionSpaceInterface<double> *fs = bk.field->getFunctionSpace();
+    // mesh: the elements' nodes, one coordinate triple per element node
+    std::vector<std::size_t> elementTags, nodeTags, nodeTags2;
+    std::vector<double> coord, param;
+    gmsh::model::mesh::getElementsByType(type, elementTags, nodeTags, ent.second);
+    gmsh::model::mesh::getNodesByElementType(type, nodeTags2, coord, param, ent.second, false);
+    const int64_t E = (int64_t)elementTags.size();
+    if (E == 0) {
+      std::fill(v.begin(), v.end(), T(0.0));
+      std::fill(b.begin(), b.end(), T(0.0));
+      return;
+    }
+    const int nn = (int)(nodeTags.size() / (size_t)E);
+    std::vector<int64_t> elemNodes((size_t)E * nn);
+    for (size_t k = 0; k < elemNodes.size(); ++k) elemNodes[k] = (int64_t)k;
+    // rule and geometric basis
+    std::vector<double> weights, gauss;
+    fs->getGaussInfo(bk.integrationType, type, weights, gauss);
+    const int nq = (int)weights.size();
+    int nc = 0, no = 0;
+    std::vector<double> geoVal, geoGrad;
+    gmsh::model::mesh::getBasisFunctions(type, gauss, "Lagrange", nc, geoVal, no);
+    gmsh::model::mesh::getBasisFunctions(type, gauss, "GradLagrange", nc, geoGrad, no);
+    // the function space: basis per dense orientation and each element's
+    std::vector<double> bval, bgrad;
+    std::vector<int> orient, orient2;
+    const int nb = (int)fs->getBasisFunctions(false, bval, orient, gauss, type, ent);
+    fs->getBasisFunctions(true, bgrad, orient2, gauss, type, ent);
+    int nOrient = 1;
+    for (int o : orient) nOrient = std::max(nOrient, o + 1);
+    // the DOF map
+    std::vector<int> typeKeys;
+    std::vector<unsigned long long> entityKeys, numIdx;
+    std::vector<double> keyCoord;
+    std::vector<int> typeIdx;
+    fs->getKeys(false, typeKeys, entityKeys, keyCoord, type, ent);
+    numIdx.resize(typeKeys.size());
+    typeIdx.resize(typeKeys.size());
+    bk.field->getIndices(typeKeys, entityKeys, numIdx, typeIdx, 0, typeKeys.size());
+    std::vector<uint64_t> edof(numIdx.begin(), numIdx.end());
+    std::vector<int32_t> etype(typeIdx.begin(), typeIdx.end());
+    // the points of the coefficients (the reference's Assembler takes them from getJacobians)
+    std::vector<double> jac, det, pts;
+    gmsh::model::mesh::getJacobians(type, gauss, jac, det, pts, ent.second);
+    const PointVec points(pts.begin(), pts.end());
+
+    fg_plan *&plan = _plans[key];
+    if (!plan) {
+      fg_mesh_desc mesh{ent.first, nn, (int64_t)(coord.size() / 3), coord.data(), E, elemNodes.data()};
+      fg_rule_desc rule{nq, weights.data(), geoVal.data(), geoGrad.data()};
+      std::vector<int32_t> dense(orient.begin(), orient.end());
+      fg_space_desc space{nb, 1, nOrient, bval.data(), bgrad.data(), nOrient > 1 ? dense.data() : nullptr, FG_FORM_0};
+      fg_system_desc sys{};
+      sys.n_rows = ai.size() - 1;
+      sys.ai = ai.data();
+      sys.aj = aj.data();
+      sys.elem_dof_idx = edof.data();
+      sys.elem_dof_type = etype.data();
+      sys.n_fixed = valuesDC.size();
+      sys.upper = upper ? 1 : 0;
+      check(fg_plan_create(&mesh, &rule, &space, &sys, &plan));
+    }
+    // the terms, with their coefficients as the reference evaluates them
+    std::vector<fg_term_desc> terms(bk.terms.size());
+    std::vector<std::vector<double>> tables;
+    tables.reserve(bk.terms.size());
+    for (size_t t = 0; t < bk.terms.size(); ++t) {
+      const Recorded &r = *bk.terms[t];
+      fg_term_desc &d = terms[t];
+      d = fg_term_desc{};
+      d.kind = !r.bilinear ? FG_TERM_SOURCE : r.lhs->derivative() ? FG_TERM_GRAD_GRAD : FG_TERM_MASS;
+      d.dt = FG_DT_NONE;
+      std::vector<T> one;
+      r.rhs->values(points, gauss, type, ent, one);
+      for (const T &c : one)
+        if (c != T(1.0)) throw std::runtime_error("a coefficient on the test function");
+      std::vector<T> c;
+      r.lhs->values(points, gauss, type, ent, c);
+      describe(c, E, nq, d.coef, tables);
+    }
+    const std::vector<double> dir = flatten(valuesDC);
+    check(fg_assemble_fp64(plan, terms.data(), (int32_t)terms.size(), this->getAngularFrequency(),
+                           dir.empty() ? nullptr : dir.data(), reinterpret_cast<double *>(v.data()),
+                           reinterpret_cast<double *>(b.data()), nullptr));
+  }
+
+  static std::vector<double> flatten(const std::vector<T> &x) {
+    std::vector<double> out(2 * x.size());
+    for (size_t k = 0; k < x.size(); ++k) {
+      out[2 * k] = x[k].real();
+      out[2 * k + 1] = x[k].imag();
+    }
+    return out;
+  }
+
+  // values [1] (constant) or [E][nq]: a constant, a per-element array when
+  // every element's points agree, a point table otherwise
+  static void describe(const std::vector<T> &c, int64_t E, int nq, fg_expr &ex, std::vector<std::vector<double>> &tables) {
+    ex.n_code = 1;
+    ex.n_arrays = 0;
+    bool same = true, perElement = c.size() == (size_t)E * nq;
+    for (size_t k = 1; k < c.size() && same; ++k) same = c[k] == c[0];
+    if (same) {
+      ex.code[0] = fg_instr{FG_OP_CONST, 0, c.empty() ? 0.0 : c[0].real(), c.empty() ? 0.0 : c[0].imag()};
+      return;
+    }
+    for (int64_t e = 0; e < E && perElement; ++e)
+      for (int q = 1; q < nq && perElement; ++q) perElement = c[(size_t)e * nq + q] == c[(size_t)e * nq];
+    std::vector<double> tab;
+    if (perElement) {
+      tab.resize(2 * (size_t)E);
+      for (int64_t e = 0; e < E; ++e) {
+        tab[2 * e] = c[(size_t)e * nq].real();
+        tab[2 * e + 1] = c[(size_t)e * nq].imag();
+      }
+    } else {
+      tab = flatten(c);
+    }
+    tables.push_back(std::move(tab));
+    ex.code[0] = fg_instr{perElement ? FG_OP_ELEM : FG_OP_POINT, 0, 0.0, 0.0};
+    ex.n_arrays = 1;
+    ex.elem_values[0] = tables.back().data();
+  }
+};
+
+}  // namespace gmshfem::problem
+
+#endif  // FEMG_GPU_FORMULATION_H

@@ -14,6 +14,11 @@
   gmsh_shim/ (with this project's meshes and reference-element tables from
   fem-g_gb300/host/), linked with ref_assemble.cpp into a program that runs
   the reference's Formulation::pre() and assemble() on one problem.
+* ``oracle/_ref/ref_dropin``: the same program built with FEMG_DROPIN, its
+  formulations being the GpuFormulation of fem-g_gb300/binding/ (compiled
+  against the reference's headers), linked with fg_record.cpp, a stand-in of
+  the C ABI that records the binding's calls and assembles them with the
+  oracle (oracle.c).
 
 The last two are built only where the reference tree is present: the
 directory ``$FEMG_REFERENCE_DIR``, by default the reference checkout of this
@@ -31,6 +36,7 @@ REF_OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD, "liboracle.so")
 REF_LIB = os.path.join(REF_OUT, "libref.so")
 REF_EXE = os.path.join(REF_OUT, "ref_assemble")
+DROPIN_EXE = os.path.join(REF_OUT, "ref_dropin")
 REFERENCE = os.environ.get("FEMG_REFERENCE_DIR", "/root/reference/fem-master")
 
 # reference source directories (include paths), as its CMakeLists.txt lists them
@@ -103,11 +109,24 @@ def build_gmshfem_ref(jobs=None):
         jobsl.append((os.path.join(host, h), os.path.join(objdir, "host_" + h + ".o"), own_flags, host_hdr))
     jobsl.append((os.path.join(HERE, "ref_assemble.cpp"), os.path.join(objdir, "ref_assemble.o"),
                   ref_flags + ["-I" + HERE], max(shim_time, host_hdr)))
+    binding = os.path.join(ROOT, "fem-g_gb300", "binding")
+    bind_time = max([host_hdr] + [os.path.getmtime(p) for p in glob.glob(os.path.join(binding, "*.h"))])
+    jobsl.append((os.path.join(HERE, "ref_assemble.cpp"), os.path.join(objdir, "ref_dropin.o"),
+                  ref_flags + ["-I" + HERE, "-I" + binding, "-I" + os.path.join(ROOT, "include"), "-DFEMG_DROPIN"],
+                  max(shim_time, bind_time)))
+    jobsl.append((os.path.join(HERE, "fg_record.cpp"), os.path.join(objdir, "fg_record.o"), own_flags, host_hdr))
     with concurrent.futures.ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
         objs = list(ex.map(lambda j: _compile_obj(*j), jobsl))
-    if os.path.exists(REF_EXE) and os.path.getmtime(REF_EXE) >= max(os.path.getmtime(o) for o in objs):
-        return REF_EXE
-    _run(["g++", "-fopenmp", "-o", REF_EXE] + objs)
+    oracle_obj = os.path.join(objdir, "oracle.o")
+    src = os.path.join(HERE, "oracle.c")
+    if not os.path.exists(oracle_obj) or os.path.getmtime(oracle_obj) < os.path.getmtime(src):
+        _run(["gcc", "-std=c11", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-c", src, "-o", oracle_obj])
+    common = [o for o in objs if not o.endswith(("ref_assemble.o", "ref_dropin.o", "fg_record.o"))]
+    for exe, own in ((REF_EXE, ["ref_assemble.o"]), (DROPIN_EXE, ["ref_dropin.o", "fg_record.o", "oracle.o"])):
+        parts = common + [os.path.join(objdir, o) for o in own]
+        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(o) for o in parts):
+            continue
+        _run(["g++", "-fopenmp", "-o", exe] + parts + ["-lm"])
     return REF_EXE
 
 

@@ -58,12 +58,27 @@
 #include "tensorNovenaryOperators.h"
 #include "vectorTernaryOperators.h"
 
+#ifdef FEMG_DROPIN
+#include "GpuFormulation.h"
+#endif
+
 #include "../fem-g_gb300/host/mesh.h"
 #include "../include/fem_g_gb300_host.h"
 #include "gmsh_shim/shim_model.h"
 
 using T = std::complex<double>;
 using namespace gmshfem;
+
+// The drop-in program (ref_dropin, built with FEMG_DROPIN) runs the same
+// problems through the GpuFormulation subclass of fem-g_gb300/binding/, whose
+// assemble() calls the C ABI (here the recording stand-in of fg_record.cpp)
+#ifdef FEMG_DROPIN
+template <class S>
+using FormulationOf = problem::GpuFormulation<S>;
+#else
+template <class S>
+using FormulationOf = problem::Formulation<S>;
+#endif
 
 namespace {
 
@@ -315,7 +330,7 @@ int main(int argc, char **argv) {
                                                      : field::FunctionSpaceTypeForm0::HierarchicalH1,
                                             lagrange ? c.mesh_order : c.order);
       if (c.dirichlet) u.addConstraint(domain::Domain("gammaDir"), T(c.dirichlet_value, 0.0));
-      problem::Formulation<T> formulation("coefficients", matrixOptions);
+      FormulationOf<T> formulation("coefficients", matrixOptions);
       if (progs.count("dfull_0")) {  // a general TensorFunction, row-major programs dfull_0 .. dfull_8
         std::vector<function::ScalarFunction<T>> d;
         for (int k = 0; k < 9; ++k) d.push_back(fromProgram(progs["dfull_" + std::to_string(k)]));
@@ -351,7 +366,7 @@ int main(int argc, char **argv) {
                                                      : field::FunctionSpaceTypeForm0::HierarchicalH1,
                                             lagrange ? c.mesh_order : c.order);
       if (c.dirichlet) u.addConstraint(domain::Domain("gammaDir"), T(c.dirichlet_value, 0.0));
-      problem::Formulation<T> formulation("helmholtz", matrixOptions);
+      FormulationOf<T> formulation("helmholtz", matrixOptions);
       formulation.integral(equation::grad(equation::dof(u)), equation::grad(equation::tf(u)), omega, gauss);
       if (c.coef_mode == FG_COEF_MODE_CONSTANT) {
         formulation.integral(function::ScalarFunction<T>(T(-c.k * c.k, 0.0)) * equation::dof(u), equation::tf(u), omega,
@@ -378,7 +393,7 @@ int main(int argc, char **argv) {
       field::Field<T, field::Form::Form0> u("u", omega, type, orderU);
       field::Field<T, field::Form::Form0> v("v", omega, type, orderV);
       if (c.dirichlet) u.addConstraint(domain::Domain("gammaDir"), T(c.dirichlet_value, 0.0));
-      problem::Formulation<T> formulation("coupled", matrixOptions);
+      FormulationOf<T> formulation("coupled", matrixOptions);
       function::ScalarFunction<T> x = function::x<T>(), y = function::y<T>();
       formulation.integral(equation::grad(equation::dof(u)), equation::grad(equation::tf(u)), omega, gauss);
       formulation.integral(function::ScalarFunction<T>(T(-c.k * c.k, 0.0)) * equation::dof(u), equation::tf(u), omega, gauss);
@@ -399,7 +414,7 @@ int main(int argc, char **argv) {
       run(formulation, repeats, w, u, v);
     } else if (c.kind == FG_PROBLEM_MAXWELL) {
       field::Field<T, field::Form::Form1> u("u", omega, field::FunctionSpaceTypeForm1::HierarchicalHCurl, c.order);
-      problem::Formulation<T> formulation("maxwell", matrixOptions);
+      FormulationOf<T> formulation("maxwell", matrixOptions);
       formulation.integral(equation::curl(equation::dof(u)), equation::curl(equation::tf(u)), omega, gauss);
       if (c.coef_mode == FG_COEF_MODE_CONSTANT) {
         formulation.integral(function::ScalarFunction<T>(T(-c.k * c.k, 0.0)) * equation::dof(u), equation::tf(u), omega,
@@ -413,7 +428,7 @@ int main(int argc, char **argv) {
       run(formulation, repeats, w, u);
     } else if (c.kind == FG_PROBLEM_NAVIER) {
       field::CompoundField<T, field::Form::Form0, 3> u("u", omega, field::FunctionSpaceTypeForm0::HierarchicalH1, c.order);
-      problem::Formulation<T> formulation("navier", matrixOptions);
+      FormulationOf<T> formulation("navier", matrixOptions);
       // lambda, mu ~ lognormal(median 1, sigma) per element, drawn in element order
       femg::Rng rng(c.seed + 2);
       std::vector<T> lam((size_t)E), mu((size_t)E);

@@ -6,7 +6,9 @@ TEST INFRASTRUCTURE ONLY.
 where the reference tree is present) on one problem in a child process and
 returns what the reference produced: its CSR pattern and values, right-hand
 side, and DOF dictionary with the numbering. ``available()`` says whether the
-program was built here.
+program was built here. ``run(cfg, dropin=True)`` runs ``ref_dropin``
+instead: the same program whose formulation is the GpuFormulation binding,
+its C ABI calls recorded (``read_record``) and assembled by the oracle.
 """
 import os
 import subprocess
@@ -16,6 +18,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 EXE = os.path.join(HERE, "_ref", "ref_assemble")
+DROPIN_EXE = os.path.join(HERE, "_ref", "ref_dropin")
 MAGIC = 0x46454D4752454631
 
 FIELDS = ["kind", "dim", "m", "mesh_order", "space", "order", "gauss", "jitter", "seed", "k", "coef_mode", "dirichlet",
@@ -43,14 +46,20 @@ def write_programs(path, programs):
                 f.write("%d %d %r %r\n" % (op, arg, float(re), float(im)))
 
 
-def run(cfg, threads=0, repeats=1, timeout=3600, programs=None):
+def dropin_available():
+    return os.path.exists(DROPIN_EXE)
+
+
+def run(cfg, threads=0, repeats=1, timeout=3600, programs=None, dropin=False):
     """Reference pre() + assemble() of the problem `cfg` (an
     fg_problem_config, from femg.config*). threads = 0: all host threads.
     repeats > 1: assemble() that many times (setSystemToZero in between) and
     report the median wall time of the repeats after the first. programs:
     coefficient programs that replace the terms of a scalar problem
-    (write_programs)."""
-    if not available():
+    (write_programs). dropin: the drop-in program; the result then also
+    holds "record", its C ABI calls (read_record)."""
+    exe = DROPIN_EXE if dropin else EXE
+    if not os.path.exists(exe):
         raise RuntimeError("the reference program is not built (oracle/build.py, needs the reference tree)")
     threads = threads or os.cpu_count() or 1
     with tempfile.TemporaryDirectory() as tmp:
@@ -60,11 +69,15 @@ def run(cfg, threads=0, repeats=1, timeout=3600, programs=None):
             extra = [os.path.join(tmp, "programs.txt")]
             write_programs(extra[0], programs)
         env = dict(os.environ, OMP_NUM_THREADS=str(threads))
-        r = subprocess.run([EXE, path, str(threads), str(repeats)] + _args(cfg) + extra, capture_output=True, text=True,
+        if dropin:
+            env["FEMG_RECORD"] = os.path.join(tmp, "record.bin")
+        r = subprocess.run([exe, path, str(threads), str(repeats)] + _args(cfg) + extra, capture_output=True, text=True,
                            timeout=timeout, env=env)
         if r.returncode != 0:
-            raise RuntimeError("ref_assemble failed (%d): %s%s" % (r.returncode, r.stdout[-2000:], r.stderr[-2000:]))
+            raise RuntimeError("%s failed (%d): %s%s" % (os.path.basename(exe), r.returncode, r.stdout[-2000:], r.stderr[-2000:]))
         raw = open(path, "rb").read()
+        record = read_record(env["FEMG_RECORD"]) if dropin and os.path.exists(env["FEMG_RECORD"]) else None
+        log = r.stdout + r.stderr
     pos = 0
 
     def take(dtype, count):
@@ -96,5 +109,71 @@ def run(cfg, threads=0, repeats=1, timeout=3600, programs=None):
     out["assemble_seconds"] = float(take(np.float64, 1)[0])
     out["timed_runs"] = int(take(np.uint64, 1)[0])
     out["threads"] = threads
+    out["log"] = log
+    if dropin:
+        out["record"] = record or []
     assert pos == len(raw)
     return out
+
+
+def read_record(path):
+    """The C ABI calls of the drop-in program (the record format of
+    fg_record.cpp): a list of dicts, one per fg_assemble_fp64 call, with the
+    arrays of oracle.assemble's bucket dictionaries and the terms as
+    (kind, dt, [(op, arg, re, im)], [arrays])."""
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"FEMGREC1"
+    pos = 8
+
+    def take(dtype, count):
+        nonlocal pos
+        a = np.frombuffer(raw, dtype=dtype, count=count, offset=pos).copy()
+        pos += a.nbytes
+        return a
+
+    def one(dtype):
+        return take(dtype, 1)[0].item()
+
+    calls = []
+    while pos < len(raw):
+        c = {}
+        c["dim"], c["nn"] = one(np.int32), one(np.int32)
+        nodes = one(np.int64)
+        c["xyz"] = take(np.float64, 3 * nodes).reshape(nodes, 3)
+        E = one(np.int64)
+        c["E"] = E
+        c["enodes"] = take(np.int64, E * c["nn"]).reshape(E, c["nn"])
+        nq = one(np.int32)
+        c["nq"] = nq
+        c["w"] = take(np.float64, nq)
+        c["geo_val"] = take(np.float64, nq * c["nn"]).reshape(nq, c["nn"])
+        c["geo_grad"] = take(np.float64, nq * c["nn"] * 3).reshape(nq, c["nn"], 3)
+        c["nb"], c["mult"], c["n_orient"], c["form"] = (one(np.int32) for _ in range(4))
+        comp = 3 if c["form"] == 1 else 1
+        c["bval"] = take(np.float64, c["n_orient"] * nq * c["nb"] * comp)
+        c["bgrad"] = take(np.float64, c["n_orient"] * nq * c["nb"] * 3)
+        c["orient"] = take(np.int32, E) if one(np.int32) else np.zeros(E, np.int32)
+        n_rows = one(np.uint64)
+        c["n_rows"] = n_rows
+        c["ai"] = take(np.uint64, n_rows + 1)
+        c["aj"] = take(np.uint64, int(c["ai"][-1]))
+        n = c["nb"] * c["mult"]
+        c["edof"] = take(np.uint64, E * n).reshape(E, n)
+        c["etype"] = take(np.int32, E * n).reshape(E, n)
+        c["n_fixed"] = one(np.uint64)
+        c["upper"] = one(np.int32)
+        c["frequency"] = one(np.float64)
+        c["dirichlet"] = take(np.complex128, c["n_fixed"])
+        terms = []
+        for _ in range(one(np.int32)):
+            kind, dt, ncode = one(np.int32), one(np.int32), one(np.int32)
+            code = []
+            for _ in range(ncode):
+                op, arg = one(np.int32), one(np.int32)
+                re, im = one(np.float64), one(np.float64)
+                code.append((op, arg, re, im))
+            arrays = [take(np.float64, one(np.uint64)) for _ in range(one(np.int32))]
+            terms.append((kind, dt, code, arrays))
+        c["terms"] = terms
+        calls.append(c)
+    return calls

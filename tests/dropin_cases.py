@@ -1,0 +1,137 @@
+"""The drop-in binding's cases (fem-g_gb300/binding/GpuFormulation.h compiled
+against the reference's headers into oracle/_ref/ref_dropin) and the replay
+of its recorded C ABI calls, shared by the CPU and GPU tests and by
+tests/golden/make_dropin.py."""
+import ctypes as C
+
+import numpy as np
+
+from coef_programs import terms as program_terms
+
+
+def cases(F):
+    """name -> (fg_problem_config, coefficient programs or None)"""
+    _, _, progs = program_terms(F, "SQRT")
+    return {
+        # the 2D P2 workload's terms: grad-grad, -k^2 mass, Dirichlet lifting, disk source
+        "c1_m8": (F.config(dim=2, m=8, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=3, k=4.0, source=1,
+                           dirichlet=1, dirichlet_value=1.0), None),
+        # 3D hierarchical P3 with a per-element mass coefficient (a user nullary operation in the reference)
+        "c3_m2": (F.config(dim=3, m=2, mesh_order=1, space=F.FG_SPACE_HIERARCHICAL_H1, order=3, gauss=6, jitter=0.15, seed=5,
+                           k=3.0, coef_mode=1, source=1), None),
+        # point-dependent complex coefficients: mass sqrt(a(x, y)), source sqrt(a) / 2
+        "sqrt_p2": (F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=3), progs),
+        # symmetric storage
+        "c1_upper": (F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=4, k=3.0, source=1,
+                              dirichlet=1, dirichlet_value=0.5, upper=1), None),
+    }
+
+
+def oracle_arrays(call):
+    """oracle.assemble's bucket dictionary of a recorded call"""
+    a = dict(call)
+    a["n_orient"] = call["n_orient"]
+    a["dirichlet"] = call["dirichlet"]
+    return a
+
+
+class Terms:
+    """fg_term_desc array of a recorded call (keeps its arrays alive)"""
+
+    def __init__(self, F, call):
+        self.keep = []
+        self.n = len(call["terms"])
+        self.arr = (F.TermDesc * max(self.n, 1))()
+        for t, (kind, dt, code, arrays) in enumerate(call["terms"]):
+            d = self.arr[t]
+            C.memset(C.byref(d), 0, C.sizeof(F.TermDesc))
+            d.kind, d.dt = kind, dt
+            d.coef.n_code = len(code)
+            for i, (op, arg, re, im) in enumerate(code):
+                d.coef.code[i].op, d.coef.code[i].arg, d.coef.code[i].re, d.coef.code[i].im = op, arg, re, im
+            d.coef.n_arrays = len(arrays)
+            for i, v in enumerate(arrays):
+                v = np.ascontiguousarray(v, np.float64)
+                self.keep.append(v)
+                d.coef.elem_values[i] = v.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class ReplayPlan:
+    """fg_plan_create from a recorded call's descriptors"""
+
+    def __init__(self, F, call):
+        self.F, self.L = F, F.lib()
+        self.keep = []
+
+        def arr(x, dt):
+            x = np.ascontiguousarray(x, dt)
+            self.keep.append(x)
+            return x
+
+        D, I64, I32, U64 = C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_uint64)
+        xyz, en = arr(call["xyz"], np.float64), arr(call["enodes"], np.int64)
+        self.mesh = F.MeshDesc(call["dim"], call["nn"], len(xyz), xyz.ctypes.data_as(D), call["E"], en.ctypes.data_as(I64))
+        w, gv, gg = arr(call["w"], np.float64), arr(call["geo_val"], np.float64), arr(call["geo_grad"], np.float64)
+        self.rule = F.RuleDesc(call["nq"], w.ctypes.data_as(D), gv.ctypes.data_as(D), gg.ctypes.data_as(D))
+        bv, bg, orient = arr(call["bval"], np.float64), arr(call["bgrad"], np.float64), arr(call["orient"], np.int32)
+        self.space = F.SpaceDesc(call["nb"], call["mult"], call["n_orient"], bv.ctypes.data_as(D), bg.ctypes.data_as(D),
+                                 orient.ctypes.data_as(I32) if call["n_orient"] > 1 else None, call["form"])
+        ai, aj = arr(call["ai"], np.uint64), arr(call["aj"], np.uint64)
+        ed, et = arr(call["edof"], np.uint64), arr(call["etype"], np.int32)
+        self.sys = F.SystemDesc(call["n_rows"], ai.ctypes.data_as(U64), aj.ctypes.data_as(U64), ed.ctypes.data_as(U64),
+                                et.ctypes.data_as(I32), call["n_fixed"], call["upper"], 0, None, None)
+        self.dir = arr(call["dirichlet"], np.complex128)
+        self.freq = call["frequency"]
+        self.nnz, self.n_rows = len(aj), int(call["n_rows"])
+        self.ptr = C.c_void_p()
+        F.check(self.L.fg_plan_create(C.byref(self.mesh), C.byref(self.rule), C.byref(self.space), C.byref(self.sys),
+                                      C.byref(self.ptr)))
+
+    def assemble(self, precision, terms):
+        v = np.zeros(self.nnz, np.complex128)
+        r = np.zeros(self.n_rows, np.complex128)
+        d = self.dir.ctypes.data if self.dir.size else None
+        if precision == "fp64":
+            self.F.check(self.L.fg_assemble_fp64(self.ptr, terms.arr, terms.n, self.freq, d, v.ctypes.data, r.ctypes.data, None))
+        else:
+            self.F.check(self.L.fg_assemble_mixed(self.ptr, terms.arr, terms.n, self.freq, d, v.ctypes.data, r.ctypes.data, None,
+                                                  None))
+        return v, r
+
+    def close(self):
+        self.L.fg_plan_destroy(self.ptr)
+
+
+FIXTURE_KEYS = ["dim", "nn", "E", "xyz", "enodes", "nq", "w", "geo_val", "geo_grad", "nb", "mult", "n_orient", "form", "bval",
+                "bgrad", "orient", "n_rows", "ai", "aj", "edof", "etype", "n_fixed", "upper", "frequency", "dirichlet"]
+
+
+def to_fixture(prefix, call, ref):
+    """flat npz entries of a recorded call and the reference's result"""
+    out = {prefix + k: np.asarray(call[k]) for k in FIXTURE_KEYS}
+    out[prefix + "n_terms"] = np.asarray(len(call["terms"]))
+    for t, (kind, dt, code, arrays) in enumerate(call["terms"]):
+        out["%sterm%d_kind" % (prefix, t)] = np.asarray([kind, dt])
+        out["%sterm%d_code" % (prefix, t)] = np.asarray(code, np.float64).reshape(-1, 4)
+        for i, v in enumerate(arrays):
+            out["%sterm%d_array%d" % (prefix, t, i)] = np.asarray(v)
+        out["%sterm%d_n_arrays" % (prefix, t)] = np.asarray(len(arrays))
+    out[prefix + "ref_values"] = ref["values"]
+    out[prefix + "ref_rhs"] = ref["rhs"]
+    return out
+
+
+def from_fixture(z, prefix):
+    """(recorded call, reference values, reference rhs) from the npz"""
+    call = {}
+    for k in FIXTURE_KEYS:
+        v = z[prefix + k]
+        call[k] = v.item() if v.ndim == 0 else v
+    terms = []
+    for t in range(int(z[prefix + "n_terms"])):
+        kind, dt = (int(x) for x in z["%sterm%d_kind" % (prefix, t)])
+        code = [(int(c[0]), int(c[1]), float(c[2]), float(c[3])) for c in z["%sterm%d_code" % (prefix, t)]]
+        arrays = [z["%sterm%d_array%d" % (prefix, t, i)] for i in range(int(z["%sterm%d_n_arrays" % (prefix, t)]))]
+        terms.append((kind, dt, code, arrays))
+    call["terms"] = terms
+    return call, z[prefix + "ref_values"], z[prefix + "ref_rhs"]

@@ -1,0 +1,76 @@
+"""The drop-in binding, fem-g_gb300/binding/GpuFormulation.h: a subclass of
+the reference's Formulation<T> compiled against the reference's own headers
+(oracle/_ref/ref_dropin; build recipe in oracle/build.py), on the CPU:
+  * with the reference tree here: the same GmshFEM program run with
+    Formulation<T> (ref_assemble) and with GpuFormulation<T> (ref_dropin, its
+    C ABI calls taken by a recording stand-in that assembles them with the
+    oracle) gives the same pattern, CSR values and right-hand side, to 1e-13;
+    the recorded terms carry the coefficients as the binding maps them
+    (constants, per-element arrays, point tables);
+  * everywhere: the calls recorded in tests/golden/dropin.npz, assembled by
+    the oracle, give the reference's values stored beside them (1e-13)."""
+import os
+
+import numpy as np
+import pytest
+
+from dropin_cases import Terms, cases, from_fixture, oracle_arrays
+from oracle import reference
+
+FIXTURE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "dropin.npz")
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+# term kinds and coefficient ops the binding records for each case
+EXPECTED = {
+    "c1_m8": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
+    "c3_m2": [("GRAD_GRAD", "CONST"), ("MASS", "ELEM"), ("SOURCE", "POINT")],
+    "sqrt_p2": [("GRAD_GRAD", "CONST"), ("MASS", "POINT"), ("SOURCE", "POINT")],
+    "c1_upper": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
+}
+
+
+@pytest.mark.skipif(not reference.dropin_available(), reason="drop-in program not built (no reference tree)")
+@pytest.mark.parametrize("name", list(EXPECTED))
+def test_dropin_matches_reference_assemble(femg, name):
+    cfg, progs = cases(femg)[name]
+    ref = reference.run(cfg, threads=2, programs=progs)
+    drop = reference.run(cfg, threads=2, programs=progs, dropin=True)
+    assert np.array_equal(ref["ai"], drop["ai"]) and np.array_equal(ref["aj"], drop["aj"])
+    for k in ("num_type", "entity", "num_dof", "assemble_type"):
+        assert np.array_equal(ref["dof_" + k], drop["dof_" + k]), k
+    assert rel(drop["values"], ref["values"]) <= 1e-13, rel(drop["values"], ref["values"])
+    assert rel(drop["rhs"], ref["rhs"]) <= 1e-13, rel(drop["rhs"], ref["rhs"])
+    calls = drop["record"]
+    assert len(calls) == 1
+    got = [(kind, code[0][0]) for kind, _, code, _ in calls[0]["terms"]]
+    want = [(getattr(femg, "FG_TERM_" + k), getattr(femg, "FG_OP_" + op)) for k, op in EXPECTED[name]]
+    assert got == want
+    assert calls[0]["upper"] == (1 if name == "c1_upper" else 0)
+
+
+@pytest.mark.skipif(not reference.dropin_available(), reason="drop-in program not built (no reference tree)")
+def test_dropin_refuses_what_it_does_not_map(femg):
+    """A vector coefficient (the advection program) is not mapped by the
+    binding: assemble() sends the error to msg::error (silent at the
+    program's verbosity 0) and leaves A and b zero, as the reference does
+    when its assembly throws; no C ABI call is made."""
+    from coef_programs import nonsym_terms
+    cfg = femg.config(dim=2, m=4, mesh_order=2, space=femg.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=3)
+    progs = nonsym_terms(femg, "advect")[2]
+    drop = reference.run(cfg, threads=2, programs=progs, dropin=True)
+    assert np.all(drop["values"] == 0) and np.all(drop["rhs"] == 0)
+    assert drop["record"] == []
+
+
+@pytest.mark.parametrize("name", list(EXPECTED))
+def test_recorded_calls_assemble_to_reference(femg, oracle, name):
+    z = np.load(FIXTURE)
+    call, ref_v, ref_b = from_fixture(z, name + "/")
+    t = Terms(femg, call)
+    v, b = oracle.assemble(oracle_arrays(call), t.arr, t.n, call["frequency"])
+    assert rel(v, ref_v) <= 1e-13 and rel(b, ref_b) <= 1e-13

@@ -1,0 +1,41 @@
+"""The drop-in binding's C ABI calls on the GPU: the calls that
+fem-g_gb300/binding/GpuFormulation.h (compiled against the reference's
+headers) made for the cases of tests/dropin_cases.py, recorded in
+tests/golden/dropin.npz, replayed through libfemg.so (fg_plan_create,
+fg_assemble_fp64, fg_assemble_mixed) and set against the reference's own
+Formulation::assemble on the same problems: FP64 to 1e-12, mixed to 1e-6
+(point-dependent bilinear coefficients take the FP64 path only)."""
+import os
+
+import numpy as np
+import pytest
+
+from dropin_cases import ReplayPlan, Terms, from_fixture
+from test_dropin import EXPECTED, FIXTURE
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.mark.parametrize("name", list(EXPECTED))
+def test_dropin_calls_match_reference(femg, cuda, name):
+    assert os.path.exists(FIXTURE)
+    call, ref_v, ref_b = from_fixture(np.load(FIXTURE), name + "/")
+    t = Terms(femg, call)
+    plan = ReplayPlan(femg, call)
+    v, b = plan.assemble("fp64", t)
+    assert rel(v, ref_v) <= 1e-12 and rel(b, ref_b) <= 1e-12
+    v2, _ = plan.assemble("fp64", t)
+    assert np.array_equal(v.view(np.uint64), v2.view(np.uint64))
+    if ("MASS", "POINT") in EXPECTED[name]:
+        with pytest.raises(femg.FgError) as err:
+            plan.assemble("mixed", t)
+        assert err.value.status == femg.FG_ERR_UNSUPPORTED
+    else:
+        vm, bm = plan.assemble("mixed", t)
+        assert rel(vm, ref_v) <= 1e-6 and rel(bm, ref_b) <= 1e-6
+    plan.close()
