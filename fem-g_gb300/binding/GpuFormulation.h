@@ -30,9 +30,9 @@
 //    src/term/evaluator/EquationEvaluator.h:86-103; Function::evaluate for
 //    sources), and passed as constants, per-element arrays (FG_OP_ELEM) or
 //    point tables (FG_OP_POINT), whichever the values are.
-// Terms this binding does not map (vector or tensor coefficients, HCurl and
-// compound fields, time derivatives, Jacobian modificators, linked DOFs,
-// coefficients on the test function) make assemble() fail with the
+// Terms this binding does not map (vector or tensor coefficients, compound
+// fields, time derivatives, Jacobian modificators, linked DOFs, coefficients
+// on the test function) make assemble() fail with the
 // reference's convention: an error message and zero A and b
 // (Formulation.cpp:1200-1209). They are assembled by GPU plans through the
 // C ABI directly (term kinds FG_TERM_*), or by Formulation<T> itself.
@@ -191,8 +191,10 @@ class GpuFormulation : public Formulation<T> {
       else if (r.jacobianModificators) r.unsupported = "Jacobian modificators";
       else if (r.bilinear && r.lhs->dt()) r.unsupported = "a time derivative of the unknown";
       else if (r.bilinear && r.lhs->field() != r.rhs->field()) r.unsupported = "two fields";
-      else if (r.rhs->field()->form() != field::Form::Form0 || r.rhs->field()->multiplicity() != 1)
-        r.unsupported = "a field that is not a scalar H1 field";
+      else if ((r.rhs->field()->form() != field::Form::Form0 && r.rhs->field()->form() != field::Form::Form1) ||
+               r.rhs->field()->multiplicity() != 1)
+        r.unsupported = "a field that is neither a scalar H1 nor an HCurl field";
+      else if (!r.bilinear && r.rhs->field()->form() != field::Form::Form0) r.unsupported = "a source on an HCurl field";
       else if (r.bilinear && r.lhs->derivative() != r.rhs->derivative()) r.unsupported = "a gradient against a value";
       else if (productType != term::ProductType::Hermitian) r.unsupported = "a product other than the hermitian one";
     }
@@ -347,7 +349,9 @@ class GpuFormulation : public Formulation<T> {
       fg_mesh_desc mesh{ent.first, nn, (int64_t)(coord.size() / 3), coord.data(), E, elemNodes.data()};
       fg_rule_desc rule{nq, weights.data(), geoVal.data(), geoGrad.data()};
       std::vector<int32_t> dense(orient.begin(), orient.end());
-      fg_space_desc space{nb, 1, nOrient, bval.data(), bgrad.data(), nOrient > 1 ? dense.data() : nullptr, FG_FORM_0};
+      // H1: values and gradients; HCurl: values [..][3] and curls, the derivative terms being curl-curl
+      const int32_t form = bk.field->form() == field::Form::Form1 ? FG_FORM_1 : FG_FORM_0;
+      fg_space_desc space{nb, 1, nOrient, bval.data(), bgrad.data(), nOrient > 1 ? dense.data() : nullptr, form};
       fg_system_desc sys{};
       sys.n_rows = ai.size() - 1;
       sys.ai = ai.data();

@@ -21,6 +21,9 @@ def cases(F):
                            k=3.0, coef_mode=1, source=1), None),
         # point-dependent complex coefficients: mass sqrt(a(x, y)), source sqrt(a) / 2
         "sqrt_p2": (F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=3), progs),
+        # HCurl order 1 (curl-curl and a per-element permittivity) on tets
+        "maxwell_p1": (F.config(kind=F.FG_PROBLEM_MAXWELL, dim=3, m=2, mesh_order=1, space=F.FG_SPACE_HCURL, order=1, gauss=4,
+                                jitter=0.15, seed=7, k=3.0, coef_mode=1), None),
         # symmetric storage
         "c1_upper": (F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=4, k=3.0, source=1,
                               dirichlet=1, dirichlet_value=0.5, upper=1), None),

@@ -30,6 +30,7 @@ EXPECTED = {
     "c1_m8": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "c3_m2": [("GRAD_GRAD", "CONST"), ("MASS", "ELEM"), ("SOURCE", "POINT")],
     "sqrt_p2": [("GRAD_GRAD", "CONST"), ("MASS", "POINT"), ("SOURCE", "POINT")],
+    "maxwell_p1": [("GRAD_GRAD", "CONST"), ("MASS", "ELEM")],
     "c1_upper": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
 }
 
