@@ -30,9 +30,9 @@
 //    src/term/evaluator/EquationEvaluator.h:86-103; Function::evaluate for
 //    sources), and passed as constants, per-element arrays (FG_OP_ELEM) or
 //    point tables (FG_OP_POINT), whichever the values are.
-// Terms this binding does not map (vector or tensor coefficients, compound
-// fields, time derivatives, Jacobian modificators, linked DOFs, coefficients
-// on the test function) make assemble() fail with the
+// Terms this binding does not map (Tensor4 coefficients and vector
+// products, compound fields, two-field terms, time derivatives, Jacobian
+// modificators, linked DOFs, coefficients on the test function) make assemble() fail with the
 // reference's convention: an error message and zero A and b
 // (Formulation.cpp:1200-1209). They are assembled by GPU plans through the
 // C ABI directly (term kinds FG_TERM_*), or by Formulation<T> itself.
@@ -79,18 +79,23 @@ class GpuFormulation : public Formulation<T> {
     virtual field::Form form() const { return field::Form::Form0; }
     virtual bool derivative() const { return false; }
     virtual bool dt() const { return false; }
-    // the coefficient at the points (x, y, z) [n][3] of the bucket, element-major
+    // the coefficient's components: 1 (scalar), 3 (vector) or 9 (tensor, row-major)
+    virtual int components() const { return 1; }
+    // the coefficient at the points (x, y, z) [n][3] of the bucket, element-major:
+    // [1][components] when it is constant, else [n][components]
     virtual void values(const PointVec &points, const std::vector<double> &gauss, int elementType,
                         const std::pair<int, int> &entity, std::vector<T> &out) const = 0;
   };
 
-  // c * (dof or tf, gradient or value) with a scalar coefficient c: the
-  // reference's EquationLhs<T, Degree0, F, ScalarProduct>, whose evaluator
-  // scales a field by c (EquationEvaluator.h:107-131), so a 1 x 1 field of 1
-  // gives c at each point
-  template <field::Form F>
+  // c * (dof or tf, gradient or value): the reference's EquationLhs<T, DC, F,
+  // ScalarProduct> with a coefficient c of degree DC. Its evaluator applies c
+  // to a field (EquationEvaluator.h:107-131, :198-325): a scalar c scales it,
+  // a vector b gives b^T field (F a vector form: b . grad) or b field (F =
+  // Form0: b times a value), a tensor D gives D field. So a unit field (1 x 1,
+  // or the 3 x 3 identity) gives the coefficient itself at each point.
+  template <Degree DC, field::Form F>
   struct EquationSide final : Side {
-    using Eq = equation::EquationLhs<T, Degree::Degree0, F, equation::Product::ScalarProduct>;
+    using Eq = equation::EquationLhs<T, DC, F, equation::Product::ScalarProduct>;
     std::unique_ptr<Eq> eq;
     explicit EquationSide(const Eq &e) : eq(e.copy()) {}
     field::FieldInterface<T> *field() const override { return eq->getField(); }
@@ -100,38 +105,49 @@ class GpuFormulation : public Formulation<T> {
       const auto *u = eq->getUnknownField();
       return u && u->type() != equation::UnknownFieldType::NotDt;
     }
+    int components() const override { return DC == Degree::Degree0 ? 1 : DC == Degree::Degree1 ? 3 : 9; }
     void values(const PointVec &points, const std::vector<double> &gauss, int elementType, const std::pair<int, int> &entity,
                 std::vector<T> &out) const override {
       std::unique_ptr<term::evaluator::EquationEvaluatorInterface<T, F>> ev(eq->getEquationEvaluator());
       ev->initialize(points, gauss, elementType, entity);
       const size_t n = ev->isConstant(entity) ? 1 : points.size() / 3;
-      out.resize(n);
-      Eigen::MatrixX<T> value(1, 1);
-      const Eigen::MatrixX<double> one = Eigen::MatrixX<double>::Ones(1, 1);
+      const int nc = components();
+      const bool unit3 = DC == Degree::Degree2 || (DC == Degree::Degree1 && F != field::Form::Form0);
+      Eigen::MatrixX<double> unit = Eigen::MatrixX<double>::Ones(1, 1);
+      if (unit3) unit = Eigen::MatrixX<double>::Identity(3, 3);
+      const int rows = DC == Degree::Degree0 ? 1 : DC == Degree::Degree1 ? (F == field::Form::Form0 ? 3 : 1) : 3;
+      Eigen::MatrixX<T> value(rows, unit.cols());
+      out.resize(n * nc);
       for (size_t k = 0; k < n; ++k) {
-        (*ev)(value, one, (unsigned int)k);
-        out[k] = value(0, 0);
+        (*ev)(value, unit, (unsigned int)k);
+        for (int c = 0; c < nc; ++c) out[k * nc + c] = nc == 9 ? value(c / 3, c % 3) : rows == 1 ? value(0, c) : value(c, 0);
       }
       ev->clear();
     }
   };
 
-  // the source function f of integral(f, tf(u)), a scalar Function
+  // the source function f of integral(f, tf(u)) (scalar) or integral(f, grad(tf(u))) (vector)
+  template <Degree D>
   struct FunctionSide final : Side {
-    function::Function<T, Degree::Degree0> f;
-    explicit FunctionSide(const function::Function<T, Degree::Degree0> &g) : f(g) {}
+    function::Function<T, D> f;
+    explicit FunctionSide(const function::Function<T, D> &g) : f(g) {}
+    int components() const override { return D == Degree::Degree0 ? 1 : 3; }
     void values(const PointVec &points, const std::vector<double> &gauss, int elementType, const std::pair<int, int> &entity,
                 std::vector<T> &out) const override {
-      if (f.isConstant(entity)) {
-        T c;
-        f.evaluate(c, 0., 0., 0., entity);
-        out.assign(1, c);
-        return;
-      }
-      std::vector<T, numa::allocator<T>> v;
+      using V = typename MathObject<T, D>::Object;
+      std::vector<V, numa::allocator<V>> v(1);
+      if (f.isConstant(entity)) f.evaluate(v[0], 0., 0., 0., entity);
+      else {
 #pragma omp parallel num_threads(omp::getMaxThreads())
-      f.evaluate(v, points, gauss, elementType, entity);
-      out.assign(v.begin(), v.end());
+        f.evaluate(v, points, gauss, elementType, entity);
+      }
+      const int nc = components();
+      out.resize(v.size() * nc);
+      for (size_t k = 0; k < v.size(); ++k) {
+        if constexpr (D == Degree::Degree0) out[k] = v[k];
+        else
+          for (int c = 0; c < 3; ++c) out[k * 3 + c] = v[k](c);
+      }
     }
   };
 
@@ -142,12 +158,34 @@ class GpuFormulation : public Formulation<T> {
     bool jacobianModificators = false;
     std::string integrationType;
     std::string unsupported;  // why the term cannot take the GPU path
+    int kind = -1;            // FG_TERM_*
   };
+
+  // The term kind of a recorded term: scalar coefficients on grad-grad (or
+  // curl-curl) and mass; on scalar H1 fields also a vector b with
+  // (b . grad dof, tf) and (b dof, grad tf), a tensor D with (D grad dof,
+  // grad tf), and sources f (tf) and vector f (grad tf)
+  static int kindOf(const Recorded &r) {
+    const int nc = r.lhs->components();
+    const bool h1 = r.rhs->field()->form() == field::Form::Form0;
+    const bool gl = r.lhs->derivative(), gr = r.rhs->derivative();
+    if (!r.bilinear) {
+      if (nc == 1 && !gr) return FG_TERM_SOURCE;
+      if (nc == 3 && gr && h1) return FG_TERM_SOURCE_GRAD;
+      return -1;
+    }
+    if (nc == 1) return gl == gr ? (gl ? FG_TERM_GRAD_GRAD : FG_TERM_MASS) : -1;
+    if (!h1) return -1;
+    if (nc == 3 && gl && !gr) return FG_TERM_ADVECTION;
+    if (nc == 3 && !gl && gr) return FG_TERM_VECTOR_GRAD_TEST;
+    if (nc == 9 && gl && gr) return FG_TERM_GRAD_GRAD_TENSOR_FULL;
+    return -1;
+  }
   std::vector<Recorded> _recorded;
 
   template <Degree DC, field::Form F, equation::Product P>
   static std::unique_ptr<Side> side(const equation::EquationLhs<T, DC, F, P> &e) {
-    if constexpr (DC == Degree::Degree0 && P == equation::Product::ScalarProduct) return std::make_unique<EquationSide<F>>(e);
+    if constexpr (P == equation::Product::ScalarProduct && DC != Degree::Degree4) return std::make_unique<EquationSide<DC, F>>(e);
     else return nullptr;
   }
   // dof(u), tf(u), grad(...): the equation made from an unknown field owns and
@@ -158,10 +196,13 @@ class GpuFormulation : public Formulation<T> {
     const equation::UnknownField<T, F> *own = u.copy();
     return side(static_cast<equation::EquationLhs<T, Degree::Degree0, F, equation::Product::ScalarProduct>>(*own));
   }
-  // a scalar source function (ScalarFunction and the other Function<T, Degree0> types), or a form not mapped
+  // a scalar or vector source function (ScalarFunction, VectorFunction and the other Function types), or a form not mapped
   template <class O>
   static std::unique_ptr<Side> side(const O &o) {
-    if constexpr (std::is_base_of<function::Function<T, Degree::Degree0>, O>::value) return std::make_unique<FunctionSide>(o);
+    if constexpr (std::is_base_of<function::Function<T, Degree::Degree0>, O>::value)
+      return std::make_unique<FunctionSide<Degree::Degree0>>(o);
+    else if constexpr (std::is_base_of<function::Function<T, Degree::Degree1>, O>::value)
+      return std::make_unique<FunctionSide<Degree::Degree1>>(o);
     else return nullptr;
   }
 
@@ -184,7 +225,7 @@ class GpuFormulation : public Formulation<T> {
       r.entities.push_back(*it);
       r.jacobianModificators = r.jacobianModificators || domain.haveJacobiansModificators(*it);
     }
-    if (!r.lhs || !r.rhs) r.unsupported = "a vector or tensor coefficient, or a term of another form";
+    if (!r.lhs || !r.rhs) r.unsupported = "a coefficient or product of another form (Tensor4, vector products)";
     else {
       r.bilinear = r.lhs->field() != nullptr;
       if (!r.rhs->field()) r.unsupported = "no test function";
@@ -195,8 +236,10 @@ class GpuFormulation : public Formulation<T> {
                r.rhs->field()->multiplicity() != 1)
         r.unsupported = "a field that is neither a scalar H1 nor an HCurl field";
       else if (!r.bilinear && r.rhs->field()->form() != field::Form::Form0) r.unsupported = "a source on an HCurl field";
-      else if (r.bilinear && r.lhs->derivative() != r.rhs->derivative()) r.unsupported = "a gradient against a value";
       else if (productType != term::ProductType::Hermitian) r.unsupported = "a product other than the hermitian one";
+      else if (r.rhs->components() != 1) r.unsupported = "a coefficient on the test function";
+      else r.kind = kindOf(r);
+      if (r.unsupported.empty() && r.kind < 0) r.unsupported = "a coefficient of this degree on these operators";
     }
     _recorded.push_back(std::move(r));
     return tag;
@@ -364,13 +407,13 @@ class GpuFormulation : public Formulation<T> {
     }
     // the terms, with their coefficients as the reference evaluates them
     std::vector<fg_term_desc> terms(bk.terms.size());
-    std::vector<std::vector<double>> tables;
-    tables.reserve(bk.terms.size());
+    std::vector<std::vector<double>> tables;  // coefficient arrays (moving a vector keeps its data)
+    std::vector<std::vector<fg_expr>> tensors(bk.terms.size());
     for (size_t t = 0; t < bk.terms.size(); ++t) {
       const Recorded &r = *bk.terms[t];
       fg_term_desc &d = terms[t];
       d = fg_term_desc{};
-      d.kind = !r.bilinear ? FG_TERM_SOURCE : r.lhs->derivative() ? FG_TERM_GRAD_GRAD : FG_TERM_MASS;
+      d.kind = r.kind;
       d.dt = FG_DT_NONE;
       std::vector<T> one;
       r.rhs->values(points, gauss, type, ent, one);
@@ -378,7 +421,22 @@ class GpuFormulation : public Formulation<T> {
         if (c != T(1.0)) throw std::runtime_error("a coefficient on the test function");
       std::vector<T> c;
       r.lhs->values(points, gauss, type, ent, c);
-      describe(c, E, nq, d.coef, tables);
+      const int nc = r.lhs->components();
+      if (nc == 1) {
+        describe(c, E, nq, d.coef, tables);
+        continue;
+      }
+      // a vector or tensor: coefficient 1 times one program per component
+      d.coef.n_code = 1;
+      d.coef.code[0] = fg_instr{FG_OP_CONST, 0, 1.0, 0.0};
+      tensors[t].resize(nc);
+      for (int k = 0; k < nc; ++k) {
+        std::vector<T> ck(c.size() / nc);
+        for (size_t i = 0; i < ck.size(); ++i) ck[i] = c[i * nc + k];
+        tensors[t][k] = fg_expr{};
+        describe(ck, E, nq, tensors[t][k], tables);
+      }
+      d.tensor = tensors[t].data();
     }
     const std::vector<double> dir = flatten(valuesDC);
     check(fg_assemble_fp64(plan, terms.data(), (int32_t)terms.size(), this->getAngularFrequency(),

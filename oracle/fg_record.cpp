@@ -14,8 +14,9 @@
 //   space  i32 nb, mult, n_orient, form; f64 val[..], grad[..]; i32 has_orient; i32 orient[E] if has_orient
 //   system u64 n_rows; u64 ai[n_rows + 1], aj[nnz], edof[E][n]; i32 etype[E][n]; u64 n_fixed; i32 upper
 //   call   f64 frequency; f64 dirichlet[n_fixed][2]
-//   terms  i32 n; per term i32 kind, dt; i32 n_code; per instruction i32 op, arg; f64 re, im;
-//          i32 n_arrays; per array u64 count; f64 values[count]
+//   terms  i32 n; per term i32 kind, dt, then its coefficient program and i32 n_tensor programs
+//          (the vector or tensor of the kind), each program as i32 n_code; per instruction
+//          i32 op, arg; f64 re, im; i32 n_arrays; per array u64 count; f64 values[count]
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -68,6 +69,38 @@ void put(FILE *f, const V *p, size_t n) {
 template <class V>
 void put1(FILE *f, V v) {
   put(f, &v, 1);
+}
+
+// programs of a term's vector or tensor
+int tensorPrograms(int kind) {
+  switch (kind) {
+    case FG_TERM_GRAD_GRAD_TENSOR:
+    case FG_TERM_MASS_TENSOR: return 6;
+    case FG_TERM_GRAD_GRAD_TENSOR_FULL: return 9;
+    case FG_TERM_ADVECTION:
+    case FG_TERM_VECTOR_GRAD_TEST:
+    case FG_TERM_SOURCE_GRAD: return 3;
+  }
+  return 0;
+}
+
+void putExpr(FILE *f, const fg_expr &ex, int64_t E, int nq, int nb) {
+  put1<int32_t>(f, ex.n_code);
+  for (int k = 0; k < ex.n_code; ++k) {
+    put1<int32_t>(f, ex.code[k].op);
+    put1<int32_t>(f, ex.code[k].arg);
+    put1<double>(f, ex.code[k].re);
+    put1<double>(f, ex.code[k].im);
+  }
+  put1<int32_t>(f, ex.n_arrays);
+  for (int a = 0; a < ex.n_arrays; ++a) {
+    uint64_t count = 2 * (uint64_t)E;
+    for (int k = 0; k < ex.n_code; ++k)
+      if (ex.code[k].arg == a && ex.code[k].op == FG_OP_POINT) count = 2 * (uint64_t)E * nq;
+      else if (ex.code[k].arg == a && ex.code[k].op == FG_OP_FIELD) count = 2 * (uint64_t)E * nb;
+    put1<uint64_t>(f, count);
+    put(f, ex.elem_values[a], count);
+  }
 }
 
 }  // namespace
@@ -168,29 +201,16 @@ int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, 
     put1<int32_t>(f, n_terms);
     for (int t = 0; t < n_terms; ++t) {
       const fg_term_desc &d = terms[t];
-      if (d.tensor || d.coef2.n_code) {
+      if (d.coef2.n_code || (tensorPrograms(d.kind) && !d.tensor)) {
         std::fclose(f);
-        g_error = "recording stand-in: tensor and two-coefficient terms are not recorded";
+        g_error = "recording stand-in: two-coefficient terms are not recorded";
         return FG_ERR_UNSUPPORTED;
       }
       put1<int32_t>(f, d.kind);
       put1<int32_t>(f, d.dt);
-      put1<int32_t>(f, d.coef.n_code);
-      for (int k = 0; k < d.coef.n_code; ++k) {
-        put1<int32_t>(f, d.coef.code[k].op);
-        put1<int32_t>(f, d.coef.code[k].arg);
-        put1<double>(f, d.coef.code[k].re);
-        put1<double>(f, d.coef.code[k].im);
-      }
-      put1<int32_t>(f, d.coef.n_arrays);
-      for (int a = 0; a < d.coef.n_arrays; ++a) {
-        uint64_t count = 2 * (uint64_t)r.E;
-        for (int k = 0; k < d.coef.n_code; ++k)
-          if (d.coef.code[k].arg == a && d.coef.code[k].op == FG_OP_POINT) count = 2 * (uint64_t)r.E * r.nq;
-          else if (d.coef.code[k].arg == a && d.coef.code[k].op == FG_OP_FIELD) count = 2 * (uint64_t)r.E * r.nb;
-        put1<uint64_t>(f, count);
-        put(f, d.coef.elem_values[a], count);
-      }
+      putExpr(f, d.coef, r.E, r.nq, r.nb);
+      put1<int32_t>(f, tensorPrograms(d.kind));
+      for (int k = 0; k < tensorPrograms(d.kind); ++k) putExpr(f, d.tensor[k], r.E, r.nq, r.nb);
     }
     std::fclose(f);
   }

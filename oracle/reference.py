@@ -120,7 +120,8 @@ def read_record(path):
     """The C ABI calls of the drop-in program (the record format of
     fg_record.cpp): a list of dicts, one per fg_assemble_fp64 call, with the
     arrays of oracle.assemble's bucket dictionaries and the terms as
-    (kind, dt, [(op, arg, re, im)], [arrays])."""
+    (kind, dt, [(op, arg, re, im)], [arrays], [(code, arrays)] of the
+    term's vector or tensor programs)."""
     raw = open(path, "rb").read()
     assert raw[:8] == b"FEMGREC1"
     pos = 8
@@ -164,16 +165,21 @@ def read_record(path):
         c["upper"] = one(np.int32)
         c["frequency"] = one(np.float64)
         c["dirichlet"] = take(np.complex128, c["n_fixed"])
-        terms = []
-        for _ in range(one(np.int32)):
-            kind, dt, ncode = one(np.int32), one(np.int32), one(np.int32)
+        def program():
             code = []
-            for _ in range(ncode):
+            for _ in range(one(np.int32)):
                 op, arg = one(np.int32), one(np.int32)
                 re, im = one(np.float64), one(np.float64)
                 code.append((op, arg, re, im))
             arrays = [take(np.float64, one(np.uint64)) for _ in range(one(np.int32))]
-            terms.append((kind, dt, code, arrays))
+            return code, arrays
+
+        terms = []
+        for _ in range(one(np.int32)):
+            kind, dt = one(np.int32), one(np.int32)
+            code, arrays = program()
+            tensor = [program() for _ in range(one(np.int32))]
+            terms.append((kind, dt, code, arrays, tensor))
         c["terms"] = terms
         calls.append(c)
     return calls

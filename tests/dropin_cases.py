@@ -6,6 +6,7 @@ import ctypes as C
 
 import numpy as np
 
+from coef_programs import nonsym_terms
 from coef_programs import terms as program_terms
 
 
@@ -24,6 +25,12 @@ def cases(F):
         # HCurl order 1 (curl-curl and a per-element permittivity) on tets
         "maxwell_p1": (F.config(kind=F.FG_PROBLEM_MAXWELL, dim=3, m=2, mesh_order=1, space=F.FG_SPACE_HCURL, order=1, gauss=4,
                                 jitter=0.15, seed=7, k=3.0, coef_mode=1), None),
+        # a general tensor diffusion and an advection (point-dependent, partly complex)
+        "full_advect": (F.config(dim=2, m=5, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=6),
+                        nonsym_terms(F, "both")[2]),
+        # b dof(u) tested by grad(v) and a vector source tested by grad(v)
+        "vector_terms": (F.config(dim=2, m=5, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=7),
+                         nonsym_terms(F, "vector")[2]),
         # symmetric storage
         "c1_upper": (F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=4, k=3.0, source=1,
                               dirichlet=1, dirichlet_value=0.5, upper=1), None),
@@ -45,18 +52,28 @@ class Terms:
         self.keep = []
         self.n = len(call["terms"])
         self.arr = (F.TermDesc * max(self.n, 1))()
-        for t, (kind, dt, code, arrays) in enumerate(call["terms"]):
-            d = self.arr[t]
-            C.memset(C.byref(d), 0, C.sizeof(F.TermDesc))
-            d.kind, d.dt = kind, dt
-            d.coef.n_code = len(code)
+
+        def fill(ex, code, arrays):
+            ex.n_code = len(code)
             for i, (op, arg, re, im) in enumerate(code):
-                d.coef.code[i].op, d.coef.code[i].arg, d.coef.code[i].re, d.coef.code[i].im = op, arg, re, im
-            d.coef.n_arrays = len(arrays)
+                ex.code[i].op, ex.code[i].arg, ex.code[i].re, ex.code[i].im = op, arg, re, im
+            ex.n_arrays = len(arrays)
             for i, v in enumerate(arrays):
                 v = np.ascontiguousarray(v, np.float64)
                 self.keep.append(v)
-                d.coef.elem_values[i] = v.ctypes.data_as(C.POINTER(C.c_double))
+                ex.elem_values[i] = v.ctypes.data_as(C.POINTER(C.c_double))
+
+        for t, (kind, dt, code, arrays, tensor) in enumerate(call["terms"]):
+            d = self.arr[t]
+            C.memset(C.byref(d), 0, C.sizeof(F.TermDesc))
+            d.kind, d.dt = kind, dt
+            fill(d.coef, code, arrays)
+            if tensor:
+                ex = (F.Expr * len(tensor))()
+                for k, (c, a) in enumerate(tensor):
+                    fill(ex[k], c, a)
+                self.keep.append(ex)
+                d.tensor = C.cast(ex, C.POINTER(F.Expr))
 
 
 class ReplayPlan:
@@ -113,12 +130,19 @@ def to_fixture(prefix, call, ref):
     """flat npz entries of a recorded call and the reference's result"""
     out = {prefix + k: np.asarray(call[k]) for k in FIXTURE_KEYS}
     out[prefix + "n_terms"] = np.asarray(len(call["terms"]))
-    for t, (kind, dt, code, arrays) in enumerate(call["terms"]):
-        out["%sterm%d_kind" % (prefix, t)] = np.asarray([kind, dt])
-        out["%sterm%d_code" % (prefix, t)] = np.asarray(code, np.float64).reshape(-1, 4)
+
+    def put(key, code, arrays):
+        out[key + "_code"] = np.asarray(code, np.float64).reshape(-1, 4)
         for i, v in enumerate(arrays):
-            out["%sterm%d_array%d" % (prefix, t, i)] = np.asarray(v)
-        out["%sterm%d_n_arrays" % (prefix, t)] = np.asarray(len(arrays))
+            out["%s_array%d" % (key, i)] = np.asarray(v)
+        out[key + "_n_arrays"] = np.asarray(len(arrays))
+
+    for t, (kind, dt, code, arrays, tensor) in enumerate(call["terms"]):
+        key = "%sterm%d" % (prefix, t)
+        out[key + "_kind"] = np.asarray([kind, dt, len(tensor)])
+        put(key, code, arrays)
+        for k, (c, a) in enumerate(tensor):
+            put("%s_tensor%d" % (key, k), c, a)
     out[prefix + "ref_values"] = ref["values"]
     out[prefix + "ref_rhs"] = ref["rhs"]
     return out
@@ -130,11 +154,15 @@ def from_fixture(z, prefix):
     for k in FIXTURE_KEYS:
         v = z[prefix + k]
         call[k] = v.item() if v.ndim == 0 else v
+    def get(key):
+        code = [(int(c[0]), int(c[1]), float(c[2]), float(c[3])) for c in z[key + "_code"]]
+        return code, [z["%s_array%d" % (key, i)] for i in range(int(z[key + "_n_arrays"]))]
+
     terms = []
     for t in range(int(z[prefix + "n_terms"])):
-        kind, dt = (int(x) for x in z["%sterm%d_kind" % (prefix, t)])
-        code = [(int(c[0]), int(c[1]), float(c[2]), float(c[3])) for c in z["%sterm%d_code" % (prefix, t)]]
-        arrays = [z["%sterm%d_array%d" % (prefix, t, i)] for i in range(int(z["%sterm%d_n_arrays" % (prefix, t)]))]
-        terms.append((kind, dt, code, arrays))
+        key = "%sterm%d" % (prefix, t)
+        kind, dt, nt = (int(x) for x in z[key + "_kind"])
+        code, arrays = get(key)
+        terms.append((kind, dt, code, arrays, [get("%s_tensor%d" % (key, k)) for k in range(nt)]))
     call["terms"] = terms
     return call, z[prefix + "ref_values"], z[prefix + "ref_rhs"]

@@ -31,6 +31,8 @@ EXPECTED = {
     "c3_m2": [("GRAD_GRAD", "CONST"), ("MASS", "ELEM"), ("SOURCE", "POINT")],
     "sqrt_p2": [("GRAD_GRAD", "CONST"), ("MASS", "POINT"), ("SOURCE", "POINT")],
     "maxwell_p1": [("GRAD_GRAD", "CONST"), ("MASS", "ELEM")],
+    "full_advect": [("GRAD_GRAD_TENSOR_FULL", "CONST"), ("ADVECTION", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
+    "vector_terms": [("VECTOR_GRAD_TEST", "CONST"), ("SOURCE_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "c1_upper": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
 }
 
@@ -48,7 +50,7 @@ def test_dropin_matches_reference_assemble(femg, name):
     assert rel(drop["rhs"], ref["rhs"]) <= 1e-13, rel(drop["rhs"], ref["rhs"])
     calls = drop["record"]
     assert len(calls) == 1
-    got = [(kind, code[0][0]) for kind, _, code, _ in calls[0]["terms"]]
+    got = [(kind, code[0][0]) for kind, _, code, _, _ in calls[0]["terms"]]
     want = [(getattr(femg, "FG_TERM_" + k), getattr(femg, "FG_OP_" + op)) for k, op in EXPECTED[name]]
     assert got == want
     assert calls[0]["upper"] == (1 if name == "c1_upper" else 0)
@@ -56,14 +58,13 @@ def test_dropin_matches_reference_assemble(femg, name):
 
 @pytest.mark.skipif(not reference.dropin_available(), reason="drop-in program not built (no reference tree)")
 def test_dropin_refuses_what_it_does_not_map(femg):
-    """A vector coefficient (the advection program) is not mapped by the
-    binding: assemble() sends the error to msg::error (silent at the
-    program's verbosity 0) and leaves A and b zero, as the reference does
-    when its assembly throws; no C ABI call is made."""
-    from coef_programs import nonsym_terms
-    cfg = femg.config(dim=2, m=4, mesh_order=2, space=femg.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=3)
-    progs = nonsym_terms(femg, "advect")[2]
-    drop = reference.run(cfg, threads=2, programs=progs, dropin=True)
+    """A compound field with a Tensor4 coefficient (the Navier problem) is not
+    mapped by the binding: assemble() sends the error to msg::error (silent
+    at the program's verbosity 0) and leaves A and b zero, as the reference
+    does when its assembly throws; no C ABI call is made."""
+    cfg = femg.config(kind=femg.FG_PROBLEM_NAVIER, dim=3, m=1, mesh_order=1, space=femg.FG_SPACE_HIERARCHICAL_H1, order=2,
+                      gauss=4, jitter=0.1, seed=2, omega=2.0, lame_sigma=0.3)
+    drop = reference.run(cfg, threads=2, dropin=True)
     assert np.all(drop["values"] == 0) and np.all(drop["rhs"] == 0)
     assert drop["record"] == []
 
