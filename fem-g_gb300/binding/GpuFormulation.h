@@ -31,8 +31,9 @@
 //    sources), and passed as constants, per-element arrays (FG_OP_ELEM) or
 //    point tables (FG_OP_POINT), whichever the values are.
 // Terms this binding does not map (Tensor4 coefficients and vector
-// products, compound fields, two-field terms, time derivatives, Jacobian
-// modificators, linked DOFs, coefficients on the test function) make assemble() fail with the
+// products, compound fields, two-field terms of HCurl fields, time
+// derivatives, Jacobian modificators, linked DOFs, coefficients on the test
+// function) make assemble() fail with the
 // reference's convention: an error message and zero A and b
 // (Formulation.cpp:1200-1209). They are assembled by GPU plans through the
 // C ABI directly (term kinds FG_TERM_*), or by Formulation<T> itself.
@@ -231,7 +232,10 @@ class GpuFormulation : public Formulation<T> {
       if (!r.rhs->field()) r.unsupported = "no test function";
       else if (r.jacobianModificators) r.unsupported = "Jacobian modificators";
       else if (r.bilinear && r.lhs->dt()) r.unsupported = "a time derivative of the unknown";
-      else if (r.bilinear && r.lhs->field() != r.rhs->field()) r.unsupported = "two fields";
+      else if (r.bilinear && r.lhs->field() != r.rhs->field() &&
+               (r.lhs->field()->form() != field::Form::Form0 || r.rhs->field()->form() != field::Form::Form0 ||
+                r.lhs->field()->multiplicity() != 1 || r.rhs->field()->multiplicity() != 1))
+        r.unsupported = "two fields that are not both scalar H1 fields";
       else if ((r.rhs->field()->form() != field::Form::Form0 && r.rhs->field()->form() != field::Form::Form1) ||
                r.rhs->field()->multiplicity() != 1)
         r.unsupported = "a field that is neither a scalar H1 nor an HCurl field";
@@ -273,7 +277,8 @@ class GpuFormulation : public Formulation<T> {
     std::pair<int, int> entity;
     int elementType;
     std::string integrationType;
-    field::FieldInterface<T> *field;
+    field::FieldInterface<T> *field;    // the test field: the rows
+    field::FieldInterface<T> *unknown;  // the unknown field: the columns (the test field's for linear terms)
     std::vector<const Recorded *> terms;
   };
   std::map<std::string, fg_plan *> _plans;
@@ -315,13 +320,16 @@ class GpuFormulation : public Formulation<T> {
         std::vector<int> types;
         gmsh::model::mesh::getElementTypes(types, ent.first, ent.second);
         for (int type : types) {
+          field::FieldInterface<T> *unknown = r.bilinear ? r.lhs->field() : r.rhs->field();
           const std::string key = std::to_string(ent.first) + "/" + std::to_string(ent.second) + "/" + std::to_string(type) + "/" +
-                                  r.integrationType + "/" + std::to_string(r.rhs->field()->tag());
+                                  r.integrationType + "/" + std::to_string(r.rhs->field()->tag()) + "/" +
+                                  std::to_string(unknown->tag());
           Bucket &b = buckets[key];
           b.entity = ent;
           b.elementType = type;
           b.integrationType = r.integrationType;
           b.field = r.rhs->field();
+          b.unknown = unknown;
           b.terms.push_back(&r);
         }
       }
@@ -335,6 +343,42 @@ class GpuFormulation : public Formulation<T> {
     }
     for (unsigned long long k = 0; k < nRows; ++k)
       if (rhs[k] != T(0.0)) this->_multiB[this->_currentRHS].addValue(k, rhs[k]);
+  }
+
+  // A field's basis tables on a bucket, per dense orientation, and its DOF map
+  struct SpaceTables {
+    int nb = 0, nOrient = 1;
+    int32_t form = FG_FORM_0;
+    std::vector<double> bval, bgrad;
+    std::vector<int32_t> orient;
+    std::vector<uint64_t> edof;
+    std::vector<int32_t> etype;
+    fg_space_desc desc() const {
+      return fg_space_desc{nb, 1, nOrient, bval.data(), bgrad.data(), nOrient > 1 ? orient.data() : nullptr, form};
+    }
+  };
+
+  static SpaceTables spaceOf(field::FieldInterface<T> *f, const std::vector<double> &gauss, int type,
+                             const std::pair<int, int> &ent) {
+    SpaceTables st;
+    field::FunctionSpaceInterface<double> *fs = f->getFunctionSpace();
+    std::vector<int> orient, orient2;
+    st.nb = (int)fs->getBasisFunctions(false, st.bval, orient, gauss, type, ent);
+    fs->getBasisFunctions(true, st.bgrad, orient2, gauss, type, ent);
+    for (int o : orient) st.nOrient = std::max(st.nOrient, o + 1);
+    st.orient.assign(orient.begin(), orient.end());
+    // H1: values and gradients; HCurl: values [..][3] and curls, the derivative terms being curl-curl
+    st.form = f->form() == field::Form::Form1 ? FG_FORM_1 : FG_FORM_0;
+    std::vector<int> typeKeys, typeIdx;
+    std::vector<unsigned long long> entityKeys, numIdx;
+    std::vector<double> keyCoord;
+    fs->getKeys(false, typeKeys, entityKeys, keyCoord, type, ent);
+    numIdx.resize(typeKeys.size());
+    typeIdx.resize(typeKeys.size());
+    f->getIndices(typeKeys, entityKeys, numIdx, typeIdx, 0, typeKeys.size());
+    st.edof.assign(numIdx.begin(), numIdx.end());
+    st.etype.assign(typeIdx.begin(), typeIdx.end());
+    return st;
   }
 
   void assembleBucket(const std::string &key, const Bucket &bk, const std::vector<uint64_t> &ai, const std::vector<uint64_t> &aj,
@@ -364,24 +408,10 @@ class GpuFormulation : public Formulation<T> {
     std::vector<double> geoVal, geoGrad;
     gmsh::model::mesh::getBasisFunctions(type, gauss, "Lagrange", nc, geoVal, no);
     gmsh::model::mesh::getBasisFunctions(type, gauss, "GradLagrange", nc, geoGrad, no);
-    // the function space: basis per dense orientation and each element's
-    std::vector<double> bval, bgrad;
-    std::vector<int> orient, orient2;
-    const int nb = (int)fs->getBasisFunctions(false, bval, orient, gauss, type, ent);
-    fs->getBasisFunctions(true, bgrad, orient2, gauss, type, ent);
-    int nOrient = 1;
-    for (int o : orient) nOrient = std::max(nOrient, o + 1);
-    // the DOF map
-    std::vector<int> typeKeys;
-    std::vector<unsigned long long> entityKeys, numIdx;
-    std::vector<double> keyCoord;
-    std::vector<int> typeIdx;
-    fs->getKeys(false, typeKeys, entityKeys, keyCoord, type, ent);
-    numIdx.resize(typeKeys.size());
-    typeIdx.resize(typeKeys.size());
-    bk.field->getIndices(typeKeys, entityKeys, numIdx, typeIdx, 0, typeKeys.size());
-    std::vector<uint64_t> edof(numIdx.begin(), numIdx.end());
-    std::vector<int32_t> etype(typeIdx.begin(), typeIdx.end());
+    // the test field's space and DOF map, and the unknown field's when it differs
+    const SpaceTables test = spaceOf(bk.field, gauss, type, ent);
+    SpaceTables unknown;
+    if (bk.unknown != bk.field) unknown = spaceOf(bk.unknown, gauss, type, ent);
     // the points of the coefficients (the reference's Assembler takes them from getJacobians)
     std::vector<double> jac, det, pts;
     gmsh::model::mesh::getJacobians(type, gauss, jac, det, pts, ent.second);
@@ -391,19 +421,21 @@ class GpuFormulation : public Formulation<T> {
     if (!plan) {
       fg_mesh_desc mesh{ent.first, nn, (int64_t)(coord.size() / 3), coord.data(), E, elemNodes.data()};
       fg_rule_desc rule{nq, weights.data(), geoVal.data(), geoGrad.data()};
-      std::vector<int32_t> dense(orient.begin(), orient.end());
-      // H1: values and gradients; HCurl: values [..][3] and curls, the derivative terms being curl-curl
-      const int32_t form = bk.field->form() == field::Form::Form1 ? FG_FORM_1 : FG_FORM_0;
-      fg_space_desc space{nb, 1, nOrient, bval.data(), bgrad.data(), nOrient > 1 ? dense.data() : nullptr, form};
+      const fg_space_desc space = test.desc();
       fg_system_desc sys{};
       sys.n_rows = ai.size() - 1;
       sys.ai = ai.data();
       sys.aj = aj.data();
-      sys.elem_dof_idx = edof.data();
-      sys.elem_dof_type = etype.data();
+      sys.elem_dof_idx = test.edof.data();
+      sys.elem_dof_type = test.etype.data();
       sys.n_fixed = valuesDC.size();
       sys.upper = upper ? 1 : 0;
-      check(fg_plan_create(&mesh, &rule, &space, &sys, &plan));
+      if (bk.unknown == bk.field) {
+        check(fg_plan_create(&mesh, &rule, &space, &sys, &plan));
+      } else {  // rows from the test field, columns from the unknown field
+        const fg_space_desc uspace = unknown.desc();
+        check(fg_plan_create_coupled(&mesh, &rule, &space, &sys, &uspace, unknown.edof.data(), unknown.etype.data(), &plan));
+      }
     }
     // the terms, with their coefficients as the reference evaluates them
     std::vector<fg_term_desc> terms(bk.terms.size());

@@ -2,7 +2,8 @@
 // INFRASTRUCTURE ONLY. Linked into the drop-in program (ref_dropin: the
 // reference's library and a GmshFEM program whose formulation is the
 // GpuFormulation of fem-g_gb300/binding/), it takes the calls the binding
-// makes (fg_plan_create, fg_assemble_fp64, fg_plan_destroy, fg_last_error),
+// makes (fg_plan_create, fg_plan_create_coupled, fg_assemble_fp64,
+// fg_plan_destroy, fg_last_error),
 // computes each assembly with the oracle's restatement (or_assemble) so that
 // the program's output can be set against the reference's own assemble(),
 // and appends every call's descriptors to the file named by FEMG_RECORD, for
@@ -13,6 +14,9 @@
 //   rule   i32 nq; f64 w[nq], geo_val[nq][nn], geo_grad[nq][nn][3]
 //   space  i32 nb, mult, n_orient, form; f64 val[..], grad[..]; i32 has_orient; i32 orient[E] if has_orient
 //   system u64 n_rows; u64 ai[n_rows + 1], aj[nnz], edof[E][n]; i32 etype[E][n]; u64 n_fixed; i32 upper
+//   column i32 coupled; if coupled (fg_plan_create_coupled) the unknown field's space and DOF map:
+//          i32 nb, n_orient, form; f64 val[..], grad[..]; i32 has_orient; i32 orient[E] if has_orient;
+//          u64 edof[E][nb]; i32 etype[E][nb]
 //   call   f64 frequency; f64 dirichlet[n_fixed][2]
 //   terms  i32 n; per term i32 kind, dt, then its coefficient program and i32 n_tensor programs
 //          (the vector or tensor of the kind), each program as i32 n_code; per instruction
@@ -46,6 +50,9 @@ typedef struct {
 } or_bucket;
 int or_assemble(const or_bucket *b, const fg_term_desc *terms, int nterms, double freq, const uint64_t *ai, const uint64_t *aj,
                 const uint64_t *edof, const int32_t *etype, const double *dirichlet, double *values, double *rhs);
+int or_assemble_coupled(const or_bucket *bt, const or_bucket *bu, const fg_term_desc *terms, int nterms, double freq,
+                        const uint64_t *ai, const uint64_t *aj, const uint64_t *edofT, const int32_t *etypeT,
+                        const uint64_t *edofU, const int32_t *etypeU, const double *dirichlet, double *values, double *rhs);
 }
 
 namespace {
@@ -60,6 +67,12 @@ struct Recorded {
   std::vector<int32_t> orient, etype;
   std::vector<uint64_t> ai, aj, edof;
   uint64_t nRows, nFixed;
+  // the unknown field of a two-field plan
+  bool coupled = false;
+  int32_t nbU = 0, nOrientU = 1, formU = 0;
+  std::vector<double> bvalU, bgradU;
+  std::vector<int32_t> orientU, etypeU;
+  std::vector<uint64_t> edofU;
 };
 
 template <class V>
@@ -152,6 +165,28 @@ int fg_plan_create(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_
   return FG_OK;
 }
 
+int fg_plan_create_coupled(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const fg_space_desc *space, const fg_system_desc *sys,
+                           const fg_space_desc *uspace, const uint64_t *uidx, const int32_t *utype, fg_plan **out) {
+  if (!uspace || !uidx || !utype) {
+    g_error = "fg_plan_create_coupled: invalid arguments";
+    return FG_ERR_ARG;
+  }
+  const int st = fg_plan_create(mesh, rule, space, sys, out);
+  if (st) return st;
+  Recorded &r = (*out)->r;
+  r.coupled = true;
+  r.nbU = uspace->n_basis;
+  r.nOrientU = uspace->n_orientations;
+  r.formU = uspace->form;
+  const size_t per = (size_t)r.nOrientU * r.nq * r.nbU;
+  r.bvalU.assign(uspace->basis_val, uspace->basis_val + per * (r.formU == FG_FORM_1 ? 3 : 1));
+  r.bgradU.assign(uspace->basis_grad, uspace->basis_grad + per * 3);
+  if (uspace->elem_orientation) r.orientU.assign(uspace->elem_orientation, uspace->elem_orientation + r.E);
+  r.edofU.assign(uidx, uidx + (size_t)r.E * r.nbU);
+  r.etypeU.assign(utype, utype + (size_t)r.E * r.nbU);
+  return FG_OK;
+}
+
 void fg_plan_destroy(fg_plan *plan) { delete plan; }
 
 const char *fg_last_error(void) { return g_error.c_str(); }
@@ -196,6 +231,18 @@ int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, 
     put(f, r.etype.data(), r.etype.size());
     put1<uint64_t>(f, r.nFixed);
     put1<int32_t>(f, r.upper);
+    put1<int32_t>(f, r.coupled ? 1 : 0);
+    if (r.coupled) {
+      put1<int32_t>(f, r.nbU);
+      put1<int32_t>(f, r.nOrientU);
+      put1<int32_t>(f, r.formU);
+      put(f, r.bvalU.data(), r.bvalU.size());
+      put(f, r.bgradU.data(), r.bgradU.size());
+      put1<int32_t>(f, r.orientU.empty() ? 0 : 1);
+      put(f, r.orientU.data(), r.orientU.size());
+      put(f, r.edofU.data(), r.edofU.size());
+      put(f, r.etypeU.data(), r.etypeU.size());
+    }
     put1<double>(f, frequency);
     put(f, dirichlet, r.nFixed ? 2 * r.nFixed : 0);
     put1<int32_t>(f, n_terms);
@@ -233,8 +280,20 @@ int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, 
   b.upper = r.upper;
   std::memset(csr_values, 0, r.ai[r.nRows] * 16);
   if (rhs) std::memset(rhs, 0, r.nRows * 16);
-  const int err = or_assemble(&b, terms, n_terms, frequency, r.ai.data(), r.aj.data(), r.edof.data(), r.etype.data(), dirichlet,
-                              csr_values, rhs);
+  int err = 0;
+  if (r.coupled) {
+    or_bucket bu = b;
+    bu.nb = r.nbU;
+    bu.bval = r.bvalU.data();
+    bu.bgrad = r.bgradU.data();
+    bu.orient = r.orientU.empty() ? nullptr : r.orientU.data();
+    bu.form = r.formU;
+    err = or_assemble_coupled(&b, &bu, terms, n_terms, frequency, r.ai.data(), r.aj.data(), r.edof.data(), r.etype.data(),
+                              r.edofU.data(), r.etypeU.data(), dirichlet, csr_values, rhs);
+  } else {
+    err = or_assemble(&b, terms, n_terms, frequency, r.ai.data(), r.aj.data(), r.edof.data(), r.etype.data(), dirichlet,
+                      csr_values, rhs);
+  }
   if (err) {
     g_error = "oracle assembly failed with status " + std::to_string(err);
     return FG_ERR_ARG;

@@ -163,6 +163,16 @@ def read_record(path):
         c["etype"] = take(np.int32, E * n).reshape(E, n)
         c["n_fixed"] = one(np.uint64)
         c["upper"] = one(np.int32)
+        c["coupled"] = one(np.int32)
+        if c["coupled"]:
+            nbu, nou, formu = one(np.int32), one(np.int32), one(np.int32)
+            u = {"nb": nbu, "n_orient": nou, "form": formu}
+            u["bval"] = take(np.float64, nou * nq * nbu * (3 if formu == 1 else 1))
+            u["bgrad"] = take(np.float64, nou * nq * nbu * 3)
+            u["orient"] = take(np.int32, E) if one(np.int32) else np.zeros(E, np.int32)
+            u["edof"] = take(np.uint64, E * nbu).reshape(E, nbu)
+            u["etype"] = take(np.int32, E * nbu).reshape(E, nbu)
+            c["unknown"] = u
         c["frequency"] = one(np.float64)
         c["dirichlet"] = take(np.complex128, c["n_fixed"])
         def program():

@@ -31,6 +31,9 @@ def cases(F):
         # b dof(u) tested by grad(v) and a vector source tested by grad(v)
         "vector_terms": (F.config(dim=2, m=5, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=7),
                          nonsym_terms(F, "vector")[2]),
+        # two scalar fields coupled both ways (four blocks, two of them two-field plans), Dirichlet on u
+        "coupled_p2": (F.config(kind=F.FG_PROBLEM_COUPLED, dim=2, m=5, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4,
+                                jitter=0.2, seed=3, k=2.0, source=1, dirichlet=1, dirichlet_value=0.5), None),
         # symmetric storage
         "c1_upper": (F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=4, k=3.0, source=1,
                               dirichlet=1, dirichlet_value=0.5, upper=1), None),
@@ -43,6 +46,20 @@ def oracle_arrays(call):
     a["n_orient"] = call["n_orient"]
     a["dirichlet"] = call["dirichlet"]
     return a
+
+
+def oracle_unknown_arrays(call):
+    """the unknown field's bucket dictionary of a two-field call"""
+    a = oracle_arrays(call)
+    a.update(call["unknown"])
+    return a
+
+
+def oracle_assemble(oracle, call, terms):
+    """the oracle's assembly of one recorded call"""
+    if call.get("unknown") is not None:
+        return oracle.assemble_coupled(oracle_arrays(call), oracle_unknown_arrays(call), terms.arr, terms.n, call["frequency"])
+    return oracle.assemble(oracle_arrays(call), terms.arr, terms.n, call["frequency"])
 
 
 class Terms:
@@ -104,8 +121,17 @@ class ReplayPlan:
         self.freq = call["frequency"]
         self.nnz, self.n_rows = len(aj), int(call["n_rows"])
         self.ptr = C.c_void_p()
-        F.check(self.L.fg_plan_create(C.byref(self.mesh), C.byref(self.rule), C.byref(self.space), C.byref(self.sys),
-                                      C.byref(self.ptr)))
+        u = call.get("unknown")
+        if u is None:
+            F.check(self.L.fg_plan_create(C.byref(self.mesh), C.byref(self.rule), C.byref(self.space), C.byref(self.sys),
+                                          C.byref(self.ptr)))
+            return
+        ubv, ubg, uor = arr(u["bval"], np.float64), arr(u["bgrad"], np.float64), arr(u["orient"], np.int32)
+        self.uspace = F.SpaceDesc(u["nb"], 1, u["n_orient"], ubv.ctypes.data_as(D), ubg.ctypes.data_as(D),
+                                  uor.ctypes.data_as(I32) if u["n_orient"] > 1 else None, u["form"])
+        ued, uet = arr(u["edof"], np.uint64), arr(u["etype"], np.int32)
+        F.check(self.L.fg_plan_create_coupled(C.byref(self.mesh), C.byref(self.rule), C.byref(self.space), C.byref(self.sys),
+                                              C.byref(self.uspace), ued.ctypes.data, uet.ctypes.data, C.byref(self.ptr)))
 
     def assemble(self, precision, terms):
         v = np.zeros(self.nnz, np.complex128)
@@ -126,9 +152,24 @@ FIXTURE_KEYS = ["dim", "nn", "E", "xyz", "enodes", "nq", "w", "geo_val", "geo_gr
                 "bgrad", "orient", "n_rows", "ai", "aj", "edof", "etype", "n_fixed", "upper", "frequency", "dirichlet"]
 
 
-def to_fixture(prefix, call, ref):
-    """flat npz entries of a recorded call and the reference's result"""
+UNKNOWN_KEYS = ["nb", "n_orient", "form", "bval", "bgrad", "orient", "edof", "etype"]
+
+
+def to_fixture(prefix, calls, ref):
+    """flat npz entries of a case's recorded calls and the reference's result"""
+    out = {prefix + "n_calls": np.asarray(len(calls)), prefix + "ref_values": ref["values"], prefix + "ref_rhs": ref["rhs"]}
+    for k, call in enumerate(calls):
+        out.update(_call_to_fixture("%s%d/" % (prefix, k), call))
+    return out
+
+
+def _call_to_fixture(prefix, call):
     out = {prefix + k: np.asarray(call[k]) for k in FIXTURE_KEYS}
+    u = call.get("unknown")
+    out[prefix + "coupled"] = np.asarray(0 if u is None else 1)
+    if u is not None:
+        for k in UNKNOWN_KEYS:
+            out[prefix + "u_" + k] = np.asarray(u[k])
     out[prefix + "n_terms"] = np.asarray(len(call["terms"]))
 
     def put(key, code, arrays):
@@ -143,13 +184,16 @@ def to_fixture(prefix, call, ref):
         put(key, code, arrays)
         for k, (c, a) in enumerate(tensor):
             put("%s_tensor%d" % (key, k), c, a)
-    out[prefix + "ref_values"] = ref["values"]
-    out[prefix + "ref_rhs"] = ref["rhs"]
     return out
 
 
 def from_fixture(z, prefix):
-    """(recorded call, reference values, reference rhs) from the npz"""
+    """(recorded calls, reference values, reference rhs) of a case from the npz"""
+    calls = [_call_from_fixture(z, "%s%d/" % (prefix, k)) for k in range(int(z[prefix + "n_calls"]))]
+    return calls, z[prefix + "ref_values"], z[prefix + "ref_rhs"]
+
+
+def _call_from_fixture(z, prefix):
     call = {}
     for k in FIXTURE_KEYS:
         v = z[prefix + k]
@@ -165,4 +209,8 @@ def from_fixture(z, prefix):
         code, arrays = get(key)
         terms.append((kind, dt, code, arrays, [get("%s_tensor%d" % (key, k)) for k in range(nt)]))
     call["terms"] = terms
-    return call, z[prefix + "ref_values"], z[prefix + "ref_rhs"]
+    call["unknown"] = None
+    if int(z[prefix + "coupled"]):
+        call["unknown"] = {k: (z[prefix + "u_" + k].item() if z[prefix + "u_" + k].ndim == 0 else z[prefix + "u_" + k])
+                           for k in UNKNOWN_KEYS}
+    return call

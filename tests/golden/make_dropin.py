@@ -31,8 +31,8 @@ def main():
     for name, (cfg, progs) in cases(femg).items():
         ref = reference.run(cfg, threads=2, programs=progs)
         drop = reference.run(cfg, threads=2, programs=progs, dropin=True)
-        assert len(drop["record"]) == 1, name  # one bucket
-        out.update(to_fixture(name + "/", drop["record"][0], ref))
+        assert len(drop["record"]) >= 1, name
+        out.update(to_fixture(name + "/", drop["record"], ref))
         names.append(name)
     out["cases"] = np.array(names)
     path = os.path.join(ROOT, "tests", "golden", "dropin.npz")

@@ -14,7 +14,7 @@ import os
 import numpy as np
 import pytest
 
-from dropin_cases import Terms, cases, from_fixture, oracle_arrays
+from dropin_cases import Terms, cases, from_fixture, oracle_assemble
 from oracle import reference
 
 FIXTURE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "dropin.npz")
@@ -34,7 +34,15 @@ EXPECTED = {
     "full_advect": [("GRAD_GRAD_TENSOR_FULL", "CONST"), ("ADVECTION", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "vector_terms": [("VECTOR_GRAD_TEST", "CONST"), ("SOURCE_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "c1_upper": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
+    # one call per (test field, unknown field) block: u-u, u-v, v-u, v-v
+    "coupled_p2": [[("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", None)], [("GRAD_GRAD", "CONST")],
+                   [("MASS", "POINT"), ("ADVECTION", "CONST")], [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")]],
 }
+
+
+def expected_calls(name):
+    e = EXPECTED[name]
+    return e if isinstance(e[0], list) else [e]
 
 
 @pytest.mark.skipif(not reference.dropin_available(), reason="drop-in program not built (no reference tree)")
@@ -49,11 +57,13 @@ def test_dropin_matches_reference_assemble(femg, name):
     assert rel(drop["values"], ref["values"]) <= 1e-13, rel(drop["values"], ref["values"])
     assert rel(drop["rhs"], ref["rhs"]) <= 1e-13, rel(drop["rhs"], ref["rhs"])
     calls = drop["record"]
-    assert len(calls) == 1
-    got = [(kind, code[0][0]) for kind, _, code, _, _ in calls[0]["terms"]]
-    want = [(getattr(femg, "FG_TERM_" + k), getattr(femg, "FG_OP_" + op)) for k, op in EXPECTED[name]]
-    assert got == want
-    assert calls[0]["upper"] == (1 if name == "c1_upper" else 0)
+    want = expected_calls(name)
+    assert len(calls) == len(want)
+    for call, w in zip(calls, want):
+        got = [(kind, code[0][0] if op is not None else None) for (kind, _, code, _, _), (_, op) in zip(call["terms"], w)]
+        assert got == [(getattr(femg, "FG_TERM_" + k), getattr(femg, "FG_OP_" + op) if op else None) for k, op in w]
+        assert call["upper"] == (1 if name == "c1_upper" else 0)
+    assert sum(c.get("unknown") is not None for c in calls) == (2 if name == "coupled_p2" else 0)
 
 
 @pytest.mark.skipif(not reference.dropin_available(), reason="drop-in program not built (no reference tree)")
@@ -72,7 +82,9 @@ def test_dropin_refuses_what_it_does_not_map(femg):
 @pytest.mark.parametrize("name", list(EXPECTED))
 def test_recorded_calls_assemble_to_reference(femg, oracle, name):
     z = np.load(FIXTURE)
-    call, ref_v, ref_b = from_fixture(z, name + "/")
-    t = Terms(femg, call)
-    v, b = oracle.assemble(oracle_arrays(call), t.arr, t.n, call["frequency"])
+    calls, ref_v, ref_b = from_fixture(z, name + "/")
+    v, b = 0.0, 0.0
+    for call in calls:
+        vk, bk = oracle_assemble(oracle, call, Terms(femg, call))
+        v, b = v + vk, b + bk
     assert rel(v, ref_v) <= 1e-13 and rel(b, ref_b) <= 1e-13

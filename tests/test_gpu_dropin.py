@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from dropin_cases import ReplayPlan, Terms, from_fixture
-from test_dropin import EXPECTED, FIXTURE
+from test_dropin import EXPECTED, FIXTURE, expected_calls
 
 pytestmark = pytest.mark.gpu
 
@@ -25,19 +25,27 @@ def rel(a, b):
 @pytest.mark.parametrize("name", list(EXPECTED))
 def test_dropin_calls_match_reference(femg, cuda, name):
     assert os.path.exists(FIXTURE)
-    call, ref_v, ref_b = from_fixture(np.load(FIXTURE), name + "/")
-    t = Terms(femg, call)
-    plan = ReplayPlan(femg, call)
-    v, b = plan.assemble("fp64", t)
-    assert rel(v, ref_v) <= 1e-12 and rel(b, ref_b) <= 1e-12
-    v2, _ = plan.assemble("fp64", t)
-    assert np.array_equal(v.view(np.uint64), v2.view(np.uint64))
+    calls, ref_v, ref_b = from_fixture(np.load(FIXTURE), name + "/")
     fp64_only = {"GRAD_GRAD_TENSOR_FULL", "ADVECTION", "VECTOR_GRAD_TEST", "SOURCE_GRAD"}
-    if ("MASS", "POINT") in EXPECTED[name] or any(k in fp64_only for k, _ in EXPECTED[name]):
-        with pytest.raises(femg.FgError) as err:
-            plan.assemble("mixed", t)
-        assert err.value.status == femg.FG_ERR_UNSUPPORTED
-    else:
-        vm, bm = plan.assemble("mixed", t)
+    v, b, vm, bm, mixed = 0.0, 0.0, 0.0, 0.0, True
+    for call, want in zip(calls, expected_calls(name)):
+        t = Terms(femg, call)
+        plan = ReplayPlan(femg, call)
+        vk, bk = plan.assemble("fp64", t)
+        v2, _ = plan.assemble("fp64", t)
+        assert np.array_equal(vk.view(np.uint64), v2.view(np.uint64))
+        v, b = v + vk, b + bk
+        # two-field plans take the FP64 path only; so do point-dependent
+        # bilinear coefficients and the non-symmetric terms
+        if call["unknown"] is not None or ("MASS", "POINT") in want or any(k in fp64_only for k, _ in want):
+            with pytest.raises(femg.FgError) as err:
+                plan.assemble("mixed", t)
+            assert err.value.status == femg.FG_ERR_UNSUPPORTED
+            mixed = False
+        else:
+            vmk, bmk = plan.assemble("mixed", t)
+            vm, bm = vm + vmk, bm + bmk
+        plan.close()
+    assert rel(v, ref_v) <= 1e-12 and rel(b, ref_b) <= 1e-12
+    if mixed:
         assert rel(vm, ref_v) <= 1e-6 and rel(bm, ref_b) <= 1e-6
-    plan.close()
