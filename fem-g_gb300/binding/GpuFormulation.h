@@ -31,8 +31,8 @@
 //    sources), and passed as constants, per-element arrays (FG_OP_ELEM) or
 //    point tables (FG_OP_POINT), whichever the values are.
 // Terms this binding does not map (Tensor4 coefficients and vector
-// products, compound fields, two-field terms of HCurl fields, time
-// derivatives, Jacobian modificators, linked DOFs, coefficients on the test
+// products, compound fields, two-field terms of HCurl fields, Jacobian
+// modificators, linked DOFs, coefficients or time derivatives on the test
 // function) make assemble() fail with the
 // reference's convention: an error message and zero A and b
 // (Formulation.cpp:1200-1209). They are assembled by GPU plans through the
@@ -79,7 +79,7 @@ class GpuFormulation : public Formulation<T> {
     virtual field::FieldInterface<T> *field() const { return nullptr; }
     virtual field::Form form() const { return field::Form::Form0; }
     virtual bool derivative() const { return false; }
-    virtual bool dt() const { return false; }
+    virtual int dt() const { return FG_DT_NONE; }  // FG_DT_*: the unknown's time derivative
     // the coefficient's components: 1 (scalar), 3 (vector) or 9 (tensor, row-major)
     virtual int components() const { return 1; }
     // the coefficient at the points (x, y, z) [n][3] of the bucket, element-major:
@@ -102,9 +102,11 @@ class GpuFormulation : public Formulation<T> {
     field::FieldInterface<T> *field() const override { return eq->getField(); }
     field::Form form() const override { return eq->form(); }
     bool derivative() const override { return eq->isDerivative(); }
-    bool dt() const override {
+    int dt() const override {
       const auto *u = eq->getUnknownField();
-      return u && u->type() != equation::UnknownFieldType::NotDt;
+      if (!u) return FG_DT_NONE;
+      if (u->type() == equation::UnknownFieldType::Dt) return FG_DT_1;
+      return u->type() == equation::UnknownFieldType::DtDt ? FG_DT_2 : FG_DT_NONE;  // NotDt, or Tf for tf()
     }
     int components() const override { return DC == Degree::Degree0 ? 1 : DC == Degree::Degree1 ? 3 : 9; }
     void values(const PointVec &points, const std::vector<double> &gauss, int elementType, const std::pair<int, int> &entity,
@@ -231,7 +233,7 @@ class GpuFormulation : public Formulation<T> {
       r.bilinear = r.lhs->field() != nullptr;
       if (!r.rhs->field()) r.unsupported = "no test function";
       else if (r.jacobianModificators) r.unsupported = "Jacobian modificators";
-      else if (r.bilinear && r.lhs->dt()) r.unsupported = "a time derivative of the unknown";
+      else if (r.rhs->dt() != FG_DT_NONE) r.unsupported = "a time derivative of the test function";
       else if (r.bilinear && r.lhs->field() != r.rhs->field() &&
                (r.lhs->field()->form() != field::Form::Form0 || r.rhs->field()->form() != field::Form::Form0 ||
                 r.lhs->field()->multiplicity() != 1 || r.rhs->field()->multiplicity() != 1))
@@ -299,7 +301,19 @@ class GpuFormulation : public Formulation<T> {
       this->_multiB.resize(this->numRHS());
     }
     for (auto &bi : this->_multiB) bi.init(nRows);
-    if (this->_A->getModule() == nullptr) this->_A->setModule(new system::AModule<T>(this->_A));
+    // the module of s_setModule (Formulation.cpp:1096-1149): with time
+    // derivatives the AFrequency one, whose single matrix is K + i w C - w^2 M
+    if (this->_A->getModule() == nullptr) {
+      bool dt = false;
+      for (const auto &r : _recorded) dt = dt || (r.bilinear && r.lhs && r.lhs->dt() != FG_DT_NONE);
+      if (dt) {
+        auto *m = new system::AFrequencyModule<T>(this->_A);
+        m->setFrequency(this->_frequency);
+        this->_A->setModule(m);
+      } else {
+        this->_A->setModule(new system::AModule<T>(this->_A));
+      }
+    }
     if (this->_dofs.nbrLinkedDofs() != 0) throw std::runtime_error("linked DOFs: not mapped by this binding");
     for (const auto &r : _recorded)
       if (!r.unsupported.empty()) throw std::runtime_error("a term takes no GPU path here: " + r.unsupported);
@@ -446,7 +460,7 @@ class GpuFormulation : public Formulation<T> {
       fg_term_desc &d = terms[t];
       d = fg_term_desc{};
       d.kind = r.kind;
-      d.dt = FG_DT_NONE;
+      d.dt = r.bilinear ? r.lhs->dt() : FG_DT_NONE;
       std::vector<T> one;
       r.rhs->values(points, gauss, type, ent, one);
       for (const T &c : one)

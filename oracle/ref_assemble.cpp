@@ -24,7 +24,9 @@
 // scalar (Helmholtz-type) problem, each "<term> <count>" followed by count
 // lines "<op> <arg> <re> <im>" in the bytecode of include/fem_g_gb300.h:
 // term "grad" (integral(g grad(dof u), grad(tf u))), "mass"
-// (integral(m dof(u), tf(u))), "source" (integral(f, tf(u))), "dfull_0" ..
+// (integral(m dof(u), tf(u))), "source" (integral(f, tf(u))), "damping" and
+// "inertia" (integral(c dt_dof(u), tf(u)) and integral(c dt2_dof(u), tf(u)),
+// at the angular frequency omega of the configuration), "dfull_0" ..
 // "dfull_8" (integral(D grad(dof u), grad(tf u)) with the general tensor D,
 // row-major), "adv_0" .. "adv_2" (integral(b . grad(dof u), tf(u))), "vdof_0" ..
 // "vdof_2" (integral(b dof(u), grad(tf u))) or "vsrc_0" .. "vsrc_2"
@@ -358,6 +360,12 @@ int main(int argc, char **argv) {
       if (progs.count("mass"))
         formulation.integral(fromProgram(progs["mass"]) * equation::dof(u), equation::tf(u), omega, gauss);
       if (progs.count("source")) formulation.integral(fromProgram(progs["source"]), equation::tf(u), omega, gauss);
+      // time derivatives of the unknown, assembled at the angular frequency omega by the AFrequency module
+      if (progs.count("damping"))
+        formulation.integral(fromProgram(progs["damping"]) * equation::dt_dof(u), equation::tf(u), omega, gauss);
+      if (progs.count("inertia"))
+        formulation.integral(fromProgram(progs["inertia"]) * equation::dt2_dof(u), equation::tf(u), omega, gauss);
+      if (progs.count("damping") || progs.count("inertia")) formulation.setAngularFrequency(c.omega);
       run(formulation, repeats, w, u);
     } else if (c.kind == FG_PROBLEM_HELMHOLTZ) {
       const bool lagrange = c.space == FG_SPACE_LAGRANGE;

@@ -10,10 +10,24 @@ from coef_programs import nonsym_terms
 from coef_programs import terms as program_terms
 
 
+def dt_programs(F):
+    """grad-grad, mass and source, plus a point-dependent damping term
+    c dt_dof(u) and an inertia term 2 dt2_dof(u)"""
+    from coef_programs import argument
+    one = [(F.FG_OP_CONST, 0, 1.0, 0.0)]
+    src = [(F.FG_OP_CONST, 0, 1.0, 0.0), (F.FG_OP_X, 0, 0, 0), (F.FG_OP_Y, 0, 0, 0), (F.FG_OP_MUL, 0, 0, 0),
+           (F.FG_OP_ADD, 0, 0, 0)]
+    return {"grad": one, "mass": [(F.FG_OP_CONST, 0, -1.5, 0.0)], "source": src, "damping": argument(F),
+            "inertia": [(F.FG_OP_CONST, 0, 2.0, 0.0)]}
+
+
 def cases(F):
     """name -> (fg_problem_config, coefficient programs or None)"""
     _, _, progs = program_terms(F, "SQRT")
     return {
+        # time derivatives of the unknown at an angular frequency (the AFrequency module)
+        "dt_terms": (F.config(dim=2, m=5, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=8, omega=1.7),
+                     dt_programs(F)),
         # the 2D P2 workload's terms: grad-grad, -k^2 mass, Dirichlet lifting, disk source
         "c1_m8": (F.config(dim=2, m=8, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=3, k=4.0, source=1,
                            dirichlet=1, dirichlet_value=1.0), None),

@@ -34,6 +34,7 @@ EXPECTED = {
     "full_advect": [("GRAD_GRAD_TENSOR_FULL", "CONST"), ("ADVECTION", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "vector_terms": [("VECTOR_GRAD_TEST", "CONST"), ("SOURCE_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "c1_upper": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
+    "dt_terms": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT"), ("MASS", "POINT"), ("MASS", "CONST")],
     # one call per (test field, unknown field) block: u-u, u-v, v-u, v-v
     "coupled_p2": [[("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", None)], [("GRAD_GRAD", "CONST")],
                    [("MASS", "POINT"), ("ADVECTION", "CONST")], [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")]],
@@ -64,6 +65,9 @@ def test_dropin_matches_reference_assemble(femg, name):
         assert got == [(getattr(femg, "FG_TERM_" + k), getattr(femg, "FG_OP_" + op) if op else None) for k, op in w]
         assert call["upper"] == (1 if name == "c1_upper" else 0)
     assert sum(c.get("unknown") is not None for c in calls) == (2 if name == "coupled_p2" else 0)
+    if name == "dt_terms":  # damping dt, inertia dt2, at the formulation's frequency
+        assert [t[1] for t in calls[0]["terms"]] == [0, 0, 0, femg.FG_DT_1, femg.FG_DT_2]
+        assert calls[0]["frequency"] == cfg.omega
 
 
 @pytest.mark.skipif(not reference.dropin_available(), reason="drop-in program not built (no reference tree)")
