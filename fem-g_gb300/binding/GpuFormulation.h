@@ -251,6 +251,12 @@ class GpuFormulation : public Formulation<T> {
     return tag;
   }
 
+  void removeTerms() override {
+    releasePlans();
+    _recorded.clear();
+    Formulation<T>::removeTerms();
+  }
+
   common::Timer pre(const DofsSort::Algorithm algo = common::Options::instance()->dofsSortAlgorithm) override {
     releasePlans();
     return Formulation<T>::pre(algo);  // numbering and pattern stay the reference's
