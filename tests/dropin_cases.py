@@ -48,6 +48,9 @@ def cases(F):
         # two scalar fields coupled both ways (four blocks, two of them two-field plans), Dirichlet on u
         "coupled_p2": (F.config(kind=F.FG_PROBLEM_COUPLED, dim=2, m=5, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4,
                                 jitter=0.2, seed=3, k=2.0, source=1, dirichlet=1, dirichlet_value=0.5), None),
+        # HCurl order 2 on tets: 45 functions per element (the FP64 path)
+        "maxwell_p2": (F.config(kind=F.FG_PROBLEM_MAXWELL, dim=3, m=1, mesh_order=1, space=F.FG_SPACE_HCURL, order=2, gauss=6,
+                                jitter=0.15, seed=9, k=2.0, coef_mode=0), None),
         # symmetric storage
         "c1_upper": (F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=4, k=3.0, source=1,
                               dirichlet=1, dirichlet_value=0.5, upper=1), None),

@@ -31,6 +31,7 @@ EXPECTED = {
     "c3_m2": [("GRAD_GRAD", "CONST"), ("MASS", "ELEM"), ("SOURCE", "POINT")],
     "sqrt_p2": [("GRAD_GRAD", "CONST"), ("MASS", "POINT"), ("SOURCE", "POINT")],
     "maxwell_p1": [("GRAD_GRAD", "CONST"), ("MASS", "ELEM")],
+    "maxwell_p2": [("GRAD_GRAD", "CONST"), ("MASS", "CONST")],
     "full_advect": [("GRAD_GRAD_TENSOR_FULL", "CONST"), ("ADVECTION", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "vector_terms": [("VECTOR_GRAD_TEST", "CONST"), ("SOURCE_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "c1_upper": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
