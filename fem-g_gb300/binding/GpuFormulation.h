@@ -333,7 +333,7 @@ class GpuFormulation : public Formulation<T> {
     const unsigned long long nnz = A.ai()[nRows];
     std::vector<uint64_t> ai(A.ai(), A.ai() + nRows + 1), aj(A.aj(), A.aj() + nnz);
     const bool upper = this->_A->getOptions().symmetric() || this->_A->getOptions().hermitian();
-    // buckets: (entity, element type, rule, field)
+    // buckets: (entity, element type, rule, test field, unknown field)
     std::map<std::string, Bucket> buckets;
     for (const auto &r : _recorded)
       for (const auto &ent : r.entities) {
@@ -354,12 +354,17 @@ class GpuFormulation : public Formulation<T> {
         }
       }
     T *values = const_cast<T *>(this->_A->getModule()->getMatrix());  // MatrixModule.cpp:167-171
-    std::vector<T> rhs(nRows, T(0.0)), v(nnz), b(nRows);
-    for (unsigned long long k = 0; k < nnz; ++k) values[k] = T(0.0);
-    for (auto &kv : buckets) {
-      assembleBucket(kv.first, kv.second, ai, aj, upper, valuesDC, v, b);
-      for (unsigned long long k = 0; k < nnz; ++k) values[k] += v[k];
-      for (unsigned long long k = 0; k < nRows; ++k) rhs[k] += b[k];
+    std::vector<T> rhs(nRows, T(0.0));
+    if (buckets.size() == 1) {  // one plan: its call writes the module array itself
+      assembleBucket(buckets.begin()->first, buckets.begin()->second, ai, aj, upper, valuesDC, values, rhs.data());
+    } else {  // several: each call into scratch, summed here
+      std::vector<T> v(nnz), b(nRows);
+      for (unsigned long long k = 0; k < nnz; ++k) values[k] = T(0.0);
+      for (auto &kv : buckets) {
+        assembleBucket(kv.first, kv.second, ai, aj, upper, valuesDC, v.data(), b.data());
+        for (unsigned long long k = 0; k < nnz; ++k) values[k] += v[k];
+        for (unsigned long long k = 0; k < nRows; ++k) rhs[k] += b[k];
+      }
     }
     for (unsigned long long k = 0; k < nRows; ++k)
       if (rhs[k] != T(0.0)) this->_multiB[this->_currentRHS].addValue(k, rhs[k]);
@@ -401,8 +406,9 @@ class GpuFormulation : public Formulation<T> {
     return st;
   }
 
+  // the bucket's values [nnz] and right-hand side [n_rows] (overwritten)
   void assembleBucket(const std::string &key, const Bucket &bk, const std::vector<uint64_t> &ai, const std::vector<uint64_t> &aj,
-                      bool upper, const std::vector<T> &valuesDC, std::vector<T> &v, std::vector<T> &b) {
+                      bool upper, const std::vector<T> &valuesDC, T *v, T *b) {
     const auto &ent = bk.entity;
     const int type = bk.elementType;
     field::FunctionSpaceInterface<double> *fs = bk.field->getFunctionSpace();
@@ -413,8 +419,8 @@ class GpuFormulation : public Formulation<T> {
     gmsh::model::mesh::getNodesByElementType(type, nodeTags2, coord, param, ent.second, false);
     const int64_t E = (int64_t)elementTags.size();
     if (E == 0) {
-      std::fill(v.begin(), v.end(), T(0.0));
-      std::fill(b.begin(), b.end(), T(0.0));
+      std::fill(v, v + aj.size(), T(0.0));
+      std::fill(b, b + (ai.size() - 1), T(0.0));
       return;
     }
     const int nn = (int)(nodeTags.size() / (size_t)E);
@@ -492,8 +498,8 @@ class GpuFormulation : public Formulation<T> {
     }
     const std::vector<double> dir = flatten(valuesDC);
     check(fg_assemble_fp64(plan, terms.data(), (int32_t)terms.size(), this->getAngularFrequency(),
-                           dir.empty() ? nullptr : dir.data(), reinterpret_cast<double *>(v.data()),
-                           reinterpret_cast<double *>(b.data()), nullptr));
+                           dir.empty() ? nullptr : dir.data(), reinterpret_cast<double *>(v), reinterpret_cast<double *>(b),
+                           nullptr));
   }
 
   static std::vector<double> flatten(const std::vector<T> &x) {
