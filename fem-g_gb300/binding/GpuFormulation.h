@@ -30,8 +30,9 @@
 //    src/term/evaluator/EquationEvaluator.h:86-103; Function::evaluate for
 //    sources), and passed as constants, per-element arrays (FG_OP_ELEM) or
 //    point tables (FG_OP_POINT), whichever the values are.
-// Terms this binding does not map (Tensor4 coefficients and vector
-// products, compound fields, two-field terms of HCurl fields, Jacobian
+// Terms this binding does not map (Tensor4 coefficients that are not
+// isotropic, vector products, compound-field terms other than mass and the
+// elastic Tensor4, two-field terms of HCurl or compound fields, Jacobian
 // modificators, linked DOFs, coefficients or time derivatives on the test
 // function) make assemble() fail with the
 // reference's convention: an error message and zero A and b
@@ -40,6 +41,8 @@
 #ifndef FEMG_GPU_FORMULATION_H
 #define FEMG_GPU_FORMULATION_H
 
+#include <algorithm>
+#include <cmath>
 #include <complex>
 #include <map>
 #include <memory>
@@ -129,6 +132,46 @@ class GpuFormulation : public Formulation<T> {
     }
   };
 
+  // c * (dof or tf, gradient or value) of a compound field of three
+  // components (a vector H1 field): the reference's EquationLhsCompound<T, DC,
+  // F, ScalarProduct, 3>. A scalar c scales the field
+  // (EquationEvaluator.h:832-895); a Tensor4 C maps a gradient u_kl to C_ijkl
+  // u_kl (:1222-1290), so the nine unit gradients give its 81 entries,
+  // C_ijkl at (i + 3 j, k + 3 l)... in the evaluator's column order
+  // (column m is the unit gradient with k = m % 3, l = m / 3).
+  template <Degree DC, field::Form F>
+  struct CompoundSide final : Side {
+    using Eq = equation::EquationLhsCompound<T, DC, F, equation::Product::ScalarProduct, 3>;
+    std::unique_ptr<Eq> eq;
+    explicit CompoundSide(const Eq &e) : eq(e.copy()) {}
+    field::FieldInterface<T> *field() const override { return eq->getField(); }
+    field::Form form() const override { return eq->form(); }
+    bool derivative() const override { return eq->isDerivative(); }
+    int dt() const override {
+      const auto *u = eq->getUnknownField();
+      if (!u) return FG_DT_NONE;
+      if (u->type() == equation::UnknownFieldType::Dt) return FG_DT_1;
+      return u->type() == equation::UnknownFieldType::DtDt ? FG_DT_2 : FG_DT_NONE;
+    }
+    int components() const override { return DC == Degree::Degree0 ? 1 : 81; }
+    void values(const PointVec &points, const std::vector<double> &gauss, int elementType, const std::pair<int, int> &entity,
+                std::vector<T> &out) const override {
+      std::unique_ptr<term::evaluator::EquationEvaluatorInterface<T, F>> ev(eq->getEquationEvaluator());
+      ev->initialize(points, gauss, elementType, entity);
+      const size_t n = ev->isConstant(entity) ? 1 : points.size() / 3;
+      const int nc = components();
+      Eigen::MatrixX<double> unit = Eigen::MatrixX<double>::Ones(1, 1);
+      if (nc == 81) unit = Eigen::MatrixX<double>::Identity(9, 9);
+      Eigen::MatrixX<T> value(nc == 81 ? 9 : 1, unit.cols());
+      out.resize(n * nc);
+      for (size_t k = 0; k < n; ++k) {
+        (*ev)(value, unit, (unsigned int)k);
+        for (int c = 0; c < nc; ++c) out[k * nc + c] = nc == 81 ? value(c / 9, c % 9) : value(0, 0);
+      }
+      ev->clear();
+    }
+  };
+
   // the source function f of integral(f, tf(u)) (scalar) or integral(f, grad(tf(u))) (vector)
   template <Degree D>
   struct FunctionSide final : Side {
@@ -170,6 +213,11 @@ class GpuFormulation : public Formulation<T> {
   // grad tf), and sources f (tf) and vector f (grad tf)
   static int kindOf(const Recorded &r) {
     const int nc = r.lhs->components();
+    if (r.rhs->field()->multiplicity() == 3) {  // compound: mass, and an isotropic Tensor4 on the gradients
+      if (nc == 1 && !r.lhs->derivative() && !r.rhs->derivative()) return FG_TERM_MASS;
+      if (nc == 81 && r.lhs->derivative() && r.rhs->derivative()) return FG_TERM_ELASTIC;
+      return -1;
+    }
     const bool h1 = r.rhs->field()->form() == field::Form::Form0;
     const bool gl = r.lhs->derivative(), gr = r.rhs->derivative();
     if (!r.bilinear) {
@@ -190,6 +238,17 @@ class GpuFormulation : public Formulation<T> {
   static std::unique_ptr<Side> side(const equation::EquationLhs<T, DC, F, P> &e) {
     if constexpr (P == equation::Product::ScalarProduct && DC != Degree::Degree4) return std::make_unique<EquationSide<DC, F>>(e);
     else return nullptr;
+  }
+  template <Degree DC, field::Form F, equation::Product P, unsigned int N>
+  static std::unique_ptr<Side> side(const equation::EquationLhsCompound<T, DC, F, P, N> &e) {
+    if constexpr (N == 3 && P == equation::Product::ScalarProduct && (DC == Degree::Degree0 || DC == Degree::Degree4))
+      return std::make_unique<CompoundSide<DC, F>>(e);
+    else return nullptr;
+  }
+  template <field::Form F, unsigned int N>
+  static std::unique_ptr<Side> side(const equation::UnknownCompoundField<T, F, N> &u) {
+    const equation::UnknownCompoundField<T, F, N> *own = u.copy();
+    return side(static_cast<equation::EquationLhsCompound<T, Degree::Degree0, F, equation::Product::ScalarProduct, N>>(*own));
   }
   // dof(u), tf(u), grad(...): the equation made from an unknown field owns and
   // deletes it (Equation.cpp:19-34), and the reference's integral() makes
@@ -238,9 +297,11 @@ class GpuFormulation : public Formulation<T> {
                (r.lhs->field()->form() != field::Form::Form0 || r.rhs->field()->form() != field::Form::Form0 ||
                 r.lhs->field()->multiplicity() != 1 || r.rhs->field()->multiplicity() != 1))
         r.unsupported = "two fields that are not both scalar H1 fields";
-      else if ((r.rhs->field()->form() != field::Form::Form0 && r.rhs->field()->form() != field::Form::Form1) ||
-               r.rhs->field()->multiplicity() != 1)
-        r.unsupported = "a field that is neither a scalar H1 nor an HCurl field";
+      else if (!(r.rhs->field()->form() == field::Form::Form0 &&
+                 (r.rhs->field()->multiplicity() == 1 || r.rhs->field()->multiplicity() == 3)) &&
+               !(r.rhs->field()->form() == field::Form::Form1 && r.rhs->field()->multiplicity() == 1))
+        r.unsupported = "a field that is not a scalar or three-component H1 field or an HCurl field";
+      else if (!r.bilinear && r.rhs->field()->multiplicity() != 1) r.unsupported = "a source on a compound field";
       else if (!r.bilinear && r.rhs->field()->form() != field::Form::Form0) r.unsupported = "a source on an HCurl field";
       else if (productType != term::ProductType::Hermitian) r.unsupported = "a product other than the hermitian one";
       else if (r.rhs->components() != 1) r.unsupported = "a coefficient on the test function";
@@ -372,14 +433,14 @@ class GpuFormulation : public Formulation<T> {
 
   // A field's basis tables on a bucket, per dense orientation, and its DOF map
   struct SpaceTables {
-    int nb = 0, nOrient = 1;
+    int nb = 0, nOrient = 1, mult = 1;
     int32_t form = FG_FORM_0;
     std::vector<double> bval, bgrad;
     std::vector<int32_t> orient;
-    std::vector<uint64_t> edof;
+    std::vector<uint64_t> edof;  // [E][nb * mult], DOF = basis * mult + component
     std::vector<int32_t> etype;
     fg_space_desc desc() const {
-      return fg_space_desc{nb, 1, nOrient, bval.data(), bgrad.data(), nOrient > 1 ? orient.data() : nullptr, form};
+      return fg_space_desc{nb, mult, nOrient, bval.data(), bgrad.data(), nOrient > 1 ? orient.data() : nullptr, form};
     }
   };
 
@@ -394,12 +455,13 @@ class GpuFormulation : public Formulation<T> {
     st.orient.assign(orient.begin(), orient.end());
     // H1: values and gradients; HCurl: values [..][3] and curls, the derivative terms being curl-curl
     st.form = f->form() == field::Form::Form1 ? FG_FORM_1 : FG_FORM_0;
+    st.mult = (int)f->multiplicity();
     std::vector<int> typeKeys, typeIdx;
     std::vector<unsigned long long> entityKeys, numIdx;
     std::vector<double> keyCoord;
     fs->getKeys(false, typeKeys, entityKeys, keyCoord, type, ent);
-    numIdx.resize(typeKeys.size());
-    typeIdx.resize(typeKeys.size());
+    numIdx.resize(typeKeys.size() * st.mult);
+    typeIdx.resize(typeKeys.size() * st.mult);
     f->getIndices(typeKeys, entityKeys, numIdx, typeIdx, 0, typeKeys.size());
     st.edof.assign(numIdx.begin(), numIdx.end());
     st.etype.assign(typeIdx.begin(), typeIdx.end());
@@ -482,6 +544,28 @@ class GpuFormulation : public Formulation<T> {
       const int nc = r.lhs->components();
       if (nc == 1) {
         describe(c, E, nq, d.coef, tables);
+        continue;
+      }
+      if (nc == 81) {  // isotropic C = lambda d_ij d_kl + mu (d_ik d_jl + d_il d_jk): lambda, mu
+        std::vector<T> lam(c.size() / 81), mu(c.size() / 81);
+        for (size_t k = 0; k < lam.size(); ++k) {
+          const T *C = &c[k * 81];
+          lam[k] = C[0 * 9 + 4];  // C_0011
+          mu[k] = C[3 * 9 + 3];   // C_0101
+          double scale = 0.0;
+          for (int x = 0; x < 81; ++x) scale = std::max(scale, std::abs(C[x]));
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+              for (int kk = 0; kk < 3; ++kk)
+                for (int l = 0; l < 3; ++l) {
+                  const T want = (i == j && kk == l ? lam[k] : T(0.0)) + ((i == kk && j == l) ? mu[k] : T(0.0)) +
+                                 ((i == l && j == kk) ? mu[k] : T(0.0));
+                  if (std::abs(C[(i + 3 * j) * 9 + kk + 3 * l] - want) > 1e-12 * scale)
+                    throw std::runtime_error("a Tensor4 coefficient that is not isotropic");
+                }
+        }
+        describe(lam, E, nq, d.coef, tables);
+        describe(mu, E, nq, d.coef2, tables);
         continue;
       }
       // a vector or tensor: coefficient 1 times one program per component

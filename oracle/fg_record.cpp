@@ -18,7 +18,8 @@
 //          i32 nb, n_orient, form; f64 val[..], grad[..]; i32 has_orient; i32 orient[E] if has_orient;
 //          u64 edof[E][nb]; i32 etype[E][nb]
 //   call   f64 frequency; f64 dirichlet[n_fixed][2]
-//   terms  i32 n; per term i32 kind, dt, then its coefficient program and i32 n_tensor programs
+//   terms  i32 n; per term i32 kind, dt, then its coefficient programs coef and coef2 (mu of the
+//          elastic term; n_code 0 otherwise) and i32 n_tensor programs
 //          (the vector or tensor of the kind), each program as i32 n_code; per instruction
 //          i32 op, arg; f64 re, im; i32 n_arrays; per array u64 count; f64 values[count]
 #include <cstdint>
@@ -248,14 +249,15 @@ int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, 
     put1<int32_t>(f, n_terms);
     for (int t = 0; t < n_terms; ++t) {
       const fg_term_desc &d = terms[t];
-      if (d.coef2.n_code || (tensorPrograms(d.kind) && !d.tensor)) {
+      if (tensorPrograms(d.kind) && !d.tensor) {
         std::fclose(f);
-        g_error = "recording stand-in: two-coefficient terms are not recorded";
-        return FG_ERR_UNSUPPORTED;
+        g_error = "recording stand-in: a tensor term without its programs";
+        return FG_ERR_ARG;
       }
       put1<int32_t>(f, d.kind);
       put1<int32_t>(f, d.dt);
       putExpr(f, d.coef, r.E, r.nq, r.nb);
+      putExpr(f, d.coef2, r.E, r.nq, r.nb);
       put1<int32_t>(f, tensorPrograms(d.kind));
       for (int k = 0; k < tensorPrograms(d.kind); ++k) putExpr(f, d.tensor[k], r.E, r.nq, r.nb);
     }

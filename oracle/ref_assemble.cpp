@@ -26,7 +26,8 @@
 // term "grad" (integral(g grad(dof u), grad(tf u))), "mass"
 // (integral(m dof(u), tf(u))), "source" (integral(f, tf(u))), "damping" and
 // "inertia" (integral(c dt_dof(u), tf(u)) and integral(c dt2_dof(u), tf(u)),
-// at the angular frequency omega of the configuration), "dfull_0" ..
+// at the angular frequency omega of the configuration), "mass_tf"
+// (integral(dof(u), m tf(u)), the coefficient on the test side), "dfull_0" ..
 // "dfull_8" (integral(D grad(dof u), grad(tf u)) with the general tensor D,
 // row-major), "adv_0" .. "adv_2" (integral(b . grad(dof u), tf(u))), "vdof_0" ..
 // "vdof_2" (integral(b dof(u), grad(tf u))) or "vsrc_0" .. "vsrc_2"
@@ -366,6 +367,9 @@ int main(int argc, char **argv) {
       if (progs.count("inertia"))
         formulation.integral(fromProgram(progs["inertia"]) * equation::dt2_dof(u), equation::tf(u), omega, gauss);
       if (progs.count("damping") || progs.count("inertia")) formulation.setAngularFrequency(c.omega);
+      // a coefficient on the test function's side
+      if (progs.count("mass_tf"))
+        formulation.integral(equation::dof(u), fromProgram(progs["mass_tf"]) * equation::tf(u), omega, gauss);
       run(formulation, repeats, w, u);
     } else if (c.kind == FG_PROBLEM_HELMHOLTZ) {
       const bool lagrange = c.space == FG_SPACE_LAGRANGE;

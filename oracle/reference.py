@@ -121,7 +121,8 @@ def read_record(path):
     fg_record.cpp): a list of dicts, one per fg_assemble_fp64 call, with the
     arrays of oracle.assemble's bucket dictionaries and the terms as
     (kind, dt, [(op, arg, re, im)], [arrays], [(code, arrays)] of the
-    term's vector or tensor programs)."""
+    term's vector or tensor programs, (code, arrays) of its second
+    coefficient))."""
     raw = open(path, "rb").read()
     assert raw[:8] == b"FEMGREC1"
     pos = 8
@@ -188,8 +189,9 @@ def read_record(path):
         for _ in range(one(np.int32)):
             kind, dt = one(np.int32), one(np.int32)
             code, arrays = program()
+            code2, arrays2 = program()
             tensor = [program() for _ in range(one(np.int32))]
-            terms.append((kind, dt, code, arrays, tensor))
+            terms.append((kind, dt, code, arrays, tensor, (code2, arrays2)))
         c["terms"] = terms
         calls.append(c)
     return calls

@@ -51,6 +51,12 @@ def cases(F):
         # HCurl order 2 on tets: 45 functions per element (the FP64 path)
         "maxwell_p2": (F.config(kind=F.FG_PROBLEM_MAXWELL, dim=3, m=1, mesh_order=1, space=F.FG_SPACE_HCURL, order=2, gauss=6,
                                 jitter=0.15, seed=9, k=2.0, coef_mode=0), None),
+        # a three-component field: isotropic elasticity with per-element Lame parameters and an inertia term
+        "navier_p2": (F.config(kind=F.FG_PROBLEM_NAVIER, dim=3, m=2, mesh_order=1, space=F.FG_SPACE_HIERARCHICAL_H1, order=2,
+                               gauss=4, jitter=0.1, seed=2, omega=0.0, lame_sigma=0.3), None),
+        # the same with the frequency in the mass coefficient (-omega^2 rho dof(u))
+        "navier_p2_omega": (F.config(kind=F.FG_PROBLEM_NAVIER, dim=3, m=1, mesh_order=1, space=F.FG_SPACE_HIERARCHICAL_H1,
+                                     order=2, gauss=4, jitter=0.1, seed=3, omega=2.5, lame_sigma=0.3), None),
         # symmetric storage
         "c1_upper": (F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=4, k=3.0, source=1,
                               dirichlet=1, dirichlet_value=0.5, upper=1), None),
@@ -97,11 +103,12 @@ class Terms:
                 self.keep.append(v)
                 ex.elem_values[i] = v.ctypes.data_as(C.POINTER(C.c_double))
 
-        for t, (kind, dt, code, arrays, tensor) in enumerate(call["terms"]):
+        for t, (kind, dt, code, arrays, tensor, (code2, arrays2)) in enumerate(call["terms"]):
             d = self.arr[t]
             C.memset(C.byref(d), 0, C.sizeof(F.TermDesc))
             d.kind, d.dt = kind, dt
             fill(d.coef, code, arrays)
+            fill(d.coef2, code2, arrays2)
             if tensor:
                 ex = (F.Expr * len(tensor))()
                 for k, (c, a) in enumerate(tensor):
@@ -195,10 +202,11 @@ def _call_to_fixture(prefix, call):
             out["%s_array%d" % (key, i)] = np.asarray(v)
         out[key + "_n_arrays"] = np.asarray(len(arrays))
 
-    for t, (kind, dt, code, arrays, tensor) in enumerate(call["terms"]):
+    for t, (kind, dt, code, arrays, tensor, (code2, arrays2)) in enumerate(call["terms"]):
         key = "%sterm%d" % (prefix, t)
         out[key + "_kind"] = np.asarray([kind, dt, len(tensor)])
         put(key, code, arrays)
+        put(key + "_coef2", code2, arrays2)
         for k, (c, a) in enumerate(tensor):
             put("%s_tensor%d" % (key, k), c, a)
     return out
@@ -224,7 +232,7 @@ def _call_from_fixture(z, prefix):
         key = "%sterm%d" % (prefix, t)
         kind, dt, nt = (int(x) for x in z[key + "_kind"])
         code, arrays = get(key)
-        terms.append((kind, dt, code, arrays, [get("%s_tensor%d" % (key, k)) for k in range(nt)]))
+        terms.append((kind, dt, code, arrays, [get("%s_tensor%d" % (key, k)) for k in range(nt)], get(key + "_coef2")))
     call["terms"] = terms
     call["unknown"] = None
     if int(z[prefix + "coupled"]):

@@ -35,6 +35,8 @@ EXPECTED = {
     "full_advect": [("GRAD_GRAD_TENSOR_FULL", "CONST"), ("ADVECTION", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "vector_terms": [("VECTOR_GRAD_TEST", "CONST"), ("SOURCE_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "c1_upper": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
+    "navier_p2": [("ELASTIC", "ELEM"), ("MASS", "CONST")],
+    "navier_p2_omega": [("ELASTIC", "ELEM"), ("MASS", "CONST")],
     "dt_terms": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT"), ("MASS", "POINT"), ("MASS", "CONST")],
     # one call per (test field, unknown field) block: u-u, u-v, v-u, v-v
     "coupled_p2": [[("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", None)], [("GRAD_GRAD", "CONST")],
@@ -62,7 +64,7 @@ def test_dropin_matches_reference_assemble(femg, name):
     want = expected_calls(name)
     assert len(calls) == len(want)
     for call, w in zip(calls, want):
-        got = [(kind, code[0][0] if op is not None else None) for (kind, _, code, _, _), (_, op) in zip(call["terms"], w)]
+        got = [(kind, code[0][0] if op is not None else None) for (kind, _, code, _, _, _), (_, op) in zip(call["terms"], w)]
         assert got == [(getattr(femg, "FG_TERM_" + k), getattr(femg, "FG_OP_" + op) if op else None) for k, op in w]
         assert call["upper"] == (1 if name == "c1_upper" else 0)
     assert sum(c.get("unknown") is not None for c in calls) == (2 if name == "coupled_p2" else 0)
@@ -73,13 +75,15 @@ def test_dropin_matches_reference_assemble(femg, name):
 
 @pytest.mark.skipif(not reference.dropin_available(), reason="drop-in program not built (no reference tree)")
 def test_dropin_refuses_what_it_does_not_map(femg):
-    """A compound field with a Tensor4 coefficient (the Navier problem) is not
-    mapped by the binding: assemble() sends the error to msg::error (silent
-    at the program's verbosity 0) and leaves A and b zero, as the reference
-    does when its assembly throws; no C ABI call is made."""
-    cfg = femg.config(kind=femg.FG_PROBLEM_NAVIER, dim=3, m=1, mesh_order=1, space=femg.FG_SPACE_HIERARCHICAL_H1, order=2,
-                      gauss=4, jitter=0.1, seed=2, omega=2.0, lame_sigma=0.3)
-    drop = reference.run(cfg, threads=2, dropin=True)
+    """A coefficient on the test function's side (integral(dof(u), m tf(u)))
+    is not mapped by the binding: assemble() sends the error to msg::error
+    (silent at the program's verbosity 0) and leaves A and b zero, as the
+    reference does when its assembly throws; no C ABI call is made."""
+    cfg = femg.config(dim=2, m=3, mesh_order=2, space=femg.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=3)
+    progs = {"grad": [(femg.FG_OP_CONST, 0, 1.0, 0.0)], "mass_tf": [(femg.FG_OP_CONST, 0, 2.0, 0.5)]}
+    ref = reference.run(cfg, threads=2, programs=progs)
+    assert np.abs(ref["values"]).max() > 0
+    drop = reference.run(cfg, threads=2, programs=progs, dropin=True)
     assert np.all(drop["values"] == 0) and np.all(drop["rhs"] == 0)
     assert drop["record"] == []
 
