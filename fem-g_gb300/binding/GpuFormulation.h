@@ -30,7 +30,8 @@
 //    src/term/evaluator/EquationEvaluator.h:86-103; Function::evaluate for
 //    sources), and passed as constants, per-element arrays (FG_OP_ELEM) or
 //    point tables (FG_OP_POINT), whichever the values are.
-// Terms this binding does not map (Tensor4 coefficients that are not
+// assemble(separate = true) takes fg_assemble_separate into the MCK, MK or CK
+// module's matrices, as the reference does. Terms this binding does not map (Tensor4 coefficients that are not
 // isotropic, vector products, compound-field terms other than mass and the
 // elastic Tensor4, two-field terms of HCurl or compound fields, Jacobian
 // modificators, linked DOFs, coefficients or time derivatives on the test
@@ -328,8 +329,7 @@ class GpuFormulation : public Formulation<T> {
     common::Timer time;
     time.tick();
     try {
-      if (separate) throw std::runtime_error("separate matrices: use fg_assemble_separate through the C ABI");
-      assembleOnGpu();
+      assembleOnGpu(separate);
     } catch (const std::exception &e) {
       msg::error << "Unable to assemble the system" << msg::endl;
       msg::error << e.what() << msg::endl;
@@ -361,7 +361,7 @@ class GpuFormulation : public Formulation<T> {
     if (status != FG_OK) throw std::runtime_error(fg_last_error());
   }
 
-  void assembleOnGpu() {
+  void assembleOnGpu(bool separate) {
     const unsigned long long nRows = this->_dofs.nbrUnknownDofs();
     if (this->numRHS() != this->_multiB.size()) {
       this->_multiB.clear();
@@ -369,18 +369,30 @@ class GpuFormulation : public Formulation<T> {
     }
     for (auto &bi : this->_multiB) bi.init(nRows);
     // the module of s_setModule (Formulation.cpp:1096-1149): with time
-    // derivatives the AFrequency one, whose single matrix is K + i w C - w^2 M
+    // derivatives the AFrequency one, whose single matrix is K + i w C - w^2 M;
+    // separate matrices: the MCK, MK or CK one (K, C and M apart)
     if (this->_A->getModule() == nullptr) {
-      bool dt = false;
-      for (const auto &r : _recorded) dt = dt || (r.bilinear && r.lhs && r.lhs->dt() != FG_DT_NONE);
-      if (dt) {
-        auto *m = new system::AFrequencyModule<T>(this->_A);
-        m->setFrequency(this->_frequency);
-        this->_A->setModule(m);
+      bool k = false, c = false, m = false;
+      for (const auto &r : _recorded)
+        if (r.bilinear && r.lhs) {
+          const int dt = r.lhs->dt();
+          k = k || dt == FG_DT_NONE;
+          c = c || dt == FG_DT_1;
+          m = m || dt == FG_DT_2;
+        }
+      if (separate && m && c && k) this->_A->setModule(new system::MCKModule<T>(this->_A));
+      else if (separate && m && !c && k) this->_A->setModule(new system::MKModule<T>(this->_A));
+      else if (separate && !m && c && k) this->_A->setModule(new system::CKModule<T>(this->_A));
+      else if (!separate && (m || c)) {
+        auto *mod = new system::AFrequencyModule<T>(this->_A);
+        mod->setFrequency(this->_frequency);
+        this->_A->setModule(mod);
       } else {
-        this->_A->setModule(new system::AModule<T>(this->_A));
+        this->_A->setModule(new system::AModule<T>(this->_A));  // separate without M or C: the reference warns and does this
       }
     }
+    const std::string moduleName = this->_A->getModule()->name();
+    const bool split = moduleName == "MCK" || moduleName == "MK" || moduleName == "CK";
     if (this->_dofs.nbrLinkedDofs() != 0) throw std::runtime_error("linked DOFs: not mapped by this binding");
     for (const auto &r : _recorded)
       if (!r.unsupported.empty()) throw std::runtime_error("a term takes no GPU path here: " + r.unsupported);
@@ -388,9 +400,10 @@ class GpuFormulation : public Formulation<T> {
     // Dirichlet values (s_setDirichletConditions)
     std::vector<T> valuesDC(this->_dofs.nbrFixedDofs());
     for (auto &uf : this->_unknownFields) uf.second->getFixedValues(valuesDC);
-    // the pattern of pre()
+    // the pattern of pre() (any of the module's matrices carries it)
     algebra::MatrixCRSFast<T> A;
-    this->getLHS(A);
+    if (split) this->getStiffness(A);
+    else this->getLHS(A);
     const unsigned long long nnz = A.ai()[nRows];
     std::vector<uint64_t> ai(A.ai(), A.ai() + nRows + 1), aj(A.aj(), A.aj() + nnz);
     const bool upper = this->_A->getOptions().symmetric() || this->_A->getOptions().hermitian();
@@ -414,17 +427,36 @@ class GpuFormulation : public Formulation<T> {
           b.terms.push_back(&r);
         }
       }
-    T *values = const_cast<T *>(this->_A->getModule()->getMatrix());  // MatrixModule.cpp:167-171
+    // the module's arrays: one (A, AFrequency) or K, C, M (null when the module has none)
+    T *out[3] = {nullptr, nullptr, nullptr};
+    const char which[3] = {'K', 'C', 'M'};
+    if (!split) {
+      out[0] = const_cast<T *>(this->_A->getModule()->getMatrix());  // MatrixModule.cpp:167-171
+    } else {
+      for (int k = 0; k < 3; ++k) {
+        if ((k == 1 && moduleName == "MK") || (k == 2 && moduleName == "CK")) continue;
+        this->_A->getModule()->activate(which[k]);
+        out[k] = const_cast<T *>(this->_A->getModule()->getMatrix());
+      }
+    }
     std::vector<T> rhs(nRows, T(0.0));
-    if (buckets.size() == 1) {  // one plan: its call writes the module array itself
-      assembleBucket(buckets.begin()->first, buckets.begin()->second, ai, aj, upper, valuesDC, values, rhs.data());
+    if (buckets.size() == 1) {  // one plan: its call writes the module arrays themselves
+      assembleBucket(buckets.begin()->first, buckets.begin()->second, ai, aj, upper, valuesDC, split, out, rhs.data());
     } else {  // several: each call into scratch, summed here
-      std::vector<T> v(nnz), b(nRows);
-      for (unsigned long long k = 0; k < nnz; ++k) values[k] = T(0.0);
+      std::vector<T> scratch[3], b(nRows);
+      T *tmp[3] = {nullptr, nullptr, nullptr};
+      for (int k = 0; k < 3; ++k)
+        if (out[k]) {
+          scratch[k].assign(nnz, T(0.0));
+          tmp[k] = scratch[k].data();
+          for (unsigned long long x = 0; x < nnz; ++x) out[k][x] = T(0.0);
+        }
       for (auto &kv : buckets) {
-        assembleBucket(kv.first, kv.second, ai, aj, upper, valuesDC, v.data(), b.data());
-        for (unsigned long long k = 0; k < nnz; ++k) values[k] += v[k];
-        for (unsigned long long k = 0; k < nRows; ++k) rhs[k] += b[k];
+        assembleBucket(kv.first, kv.second, ai, aj, upper, valuesDC, split, tmp, b.data());
+        for (int k = 0; k < 3; ++k)
+          if (out[k])
+            for (unsigned long long x = 0; x < nnz; ++x) out[k][x] += tmp[k][x];
+        for (unsigned long long x = 0; x < nRows; ++x) rhs[x] += b[x];
       }
     }
     for (unsigned long long k = 0; k < nRows; ++k)
@@ -468,9 +500,10 @@ class GpuFormulation : public Formulation<T> {
     return st;
   }
 
-  // the bucket's values [nnz] and right-hand side [n_rows] (overwritten)
+  // the bucket's values [nnz] (v[0]; or K, C, M in v[0..2] when split) and
+  // right-hand side [n_rows], overwritten
   void assembleBucket(const std::string &key, const Bucket &bk, const std::vector<uint64_t> &ai, const std::vector<uint64_t> &aj,
-                      bool upper, const std::vector<T> &valuesDC, T *v, T *b) {
+                      bool upper, const std::vector<T> &valuesDC, bool split, T *const *v, T *b) {
     const auto &ent = bk.entity;
     const int type = bk.elementType;
     field::FunctionSpaceInterface<double> *fs = bk.field->getFunctionSpace();
@@ -481,7 +514,8 @@ class GpuFormulation : public Formulation<T> {
     gmsh::model::mesh::getNodesByElementType(type, nodeTags2, coord, param, ent.second, false);
     const int64_t E = (int64_t)elementTags.size();
     if (E == 0) {
-      std::fill(v, v + aj.size(), T(0.0));
+      for (int k = 0; k < 3; ++k)
+        if (v[k]) std::fill(v[k], v[k] + aj.size(), T(0.0));
       std::fill(b, b + (ai.size() - 1), T(0.0));
       return;
     }
@@ -581,9 +615,13 @@ class GpuFormulation : public Formulation<T> {
       d.tensor = tensors[t].data();
     }
     const std::vector<double> dir = flatten(valuesDC);
-    check(fg_assemble_fp64(plan, terms.data(), (int32_t)terms.size(), this->getAngularFrequency(),
-                           dir.empty() ? nullptr : dir.data(), reinterpret_cast<double *>(v), reinterpret_cast<double *>(b),
-                           nullptr));
+    auto d = [](T *x) { return reinterpret_cast<double *>(x); };
+    if (split)
+      check(fg_assemble_separate(plan, terms.data(), (int32_t)terms.size(), 0, dir.empty() ? nullptr : dir.data(), d(v[0]), d(v[1]),
+                                 d(v[2]), d(b), nullptr));
+    else
+      check(fg_assemble_fp64(plan, terms.data(), (int32_t)terms.size(), this->getAngularFrequency(),
+                             dir.empty() ? nullptr : dir.data(), d(v[0]), d(b), nullptr));
   }
 
   static std::vector<double> flatten(const std::vector<T> &x) {

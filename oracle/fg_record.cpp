@@ -3,13 +3,14 @@
 // reference's library and a GmshFEM program whose formulation is the
 // GpuFormulation of fem-g_gb300/binding/), it takes the calls the binding
 // makes (fg_plan_create, fg_plan_create_coupled, fg_assemble_fp64,
-// fg_plan_destroy, fg_last_error),
+// fg_assemble_separate, fg_plan_destroy, fg_last_error),
 // computes each assembly with the oracle's restatement (or_assemble) so that
 // the program's output can be set against the reference's own assemble(),
 // and appends every call's descriptors to the file named by FEMG_RECORD, for
 // the GPU tests to replay through the real library.
 //
-// Record file: "FEMGREC1", then per fg_assemble_fp64 call
+// Record file: "FEMGREC1", then per fg_assemble_fp64 / fg_assemble_separate call
+//   entry  i32 0 (fg_assemble_fp64) or 1 (fg_assemble_separate)
 //   mesh   i32 dim, nn; i64 n_nodes; f64 xyz[n_nodes][3]; i64 E; i64 elem_nodes[E][nn]
 //   rule   i32 nq; f64 w[nq], geo_val[nq][nn], geo_grad[nq][nn][3]
 //   space  i32 nb, mult, n_orient, form; f64 val[..], grad[..]; i32 has_orient; i32 orient[E] if has_orient
@@ -192,13 +193,8 @@ void fg_plan_destroy(fg_plan *plan) { delete plan; }
 
 const char *fg_last_error(void) { return g_error.c_str(); }
 
-int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency, const double *dirichlet,
-                     double *csr_values, double *rhs, void *stream) {
-  (void)stream;
-  if (!plan || (n_terms > 0 && !terms) || !csr_values) {
-    g_error = "fg_assemble_fp64: invalid arguments";
-    return FG_ERR_ARG;
-  }
+static int recordCall(const fg_plan *plan, int entry, const fg_term_desc *terms, int32_t n_terms, double frequency,
+                      const double *dirichlet) {
   const Recorded &r = plan->r;
   if (const char *path = std::getenv("FEMG_RECORD")) {
     FILE *f = std::fopen(path, "ab");
@@ -207,6 +203,7 @@ int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, 
       return FG_ERR_ARG;
     }
     if (std::ftell(f) == 0) std::fwrite("FEMGREC1", 1, 8, f);
+    put1<int32_t>(f, entry);
     put1<int32_t>(f, r.dim);
     put1<int32_t>(f, r.nn);
     put1<int64_t>(f, (int64_t)(r.xyz.size() / 3));
@@ -263,6 +260,13 @@ int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, 
     }
     std::fclose(f);
   }
+  return FG_OK;
+}
+
+// the oracle's assembly of the call into csr_values / rhs (overwritten)
+static int compute(const fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency, const double *dirichlet,
+                   double *csr_values, double *rhs) {
+  const Recorded &r = plan->r;
   or_bucket b{};
   b.dim = r.dim;
   b.nn = r.nn;
@@ -299,6 +303,49 @@ int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, 
   if (err) {
     g_error = "oracle assembly failed with status " + std::to_string(err);
     return FG_ERR_ARG;
+  }
+  return FG_OK;
+}
+
+int fg_assemble_fp64(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, double frequency, const double *dirichlet,
+                     double *csr_values, double *rhs, void *stream) {
+  (void)stream;
+  if (!plan || (n_terms > 0 && !terms) || !csr_values) {
+    g_error = "fg_assemble_fp64: invalid arguments";
+    return FG_ERR_ARG;
+  }
+  if (int st = recordCall(plan, 0, terms, n_terms, frequency, dirichlet)) return st;
+  return compute(plan, terms, n_terms, frequency, dirichlet, csr_values, rhs);
+}
+
+// K from the terms without time derivative (with the sources and the
+// lifting), C from the dt terms, M from the dt2 terms, each without the
+// frequency factor
+int fg_assemble_separate(fg_plan *plan, const fg_term_desc *terms, int32_t n_terms, int32_t mixed, const double *dirichlet,
+                         double *k_values, double *c_values, double *m_values, double *rhs, void *stream) {
+  (void)stream;
+  (void)mixed;
+  if (!plan || (n_terms > 0 && !terms)) {
+    g_error = "fg_assemble_separate: invalid arguments";
+    return FG_ERR_ARG;
+  }
+  if (int st = recordCall(plan, 1, terms, n_terms, 0.0, dirichlet)) return st;
+  double *outs[3] = {k_values, c_values, m_values};
+  for (int dt = 0; dt < 3; ++dt) {
+    std::vector<fg_term_desc> sub;
+    for (int t = 0; t < n_terms; ++t)
+      if (terms[t].dt == dt) {
+        sub.push_back(terms[t]);
+        sub.back().dt = FG_DT_NONE;
+      }
+    std::vector<double> scratch;
+    double *v = outs[dt];
+    if (!v) {
+      scratch.resize(2 * plan->r.ai[plan->r.nRows]);
+      v = scratch.data();
+    }
+    // the right-hand side (sources and the lifting) comes with K alone
+    if (int st = compute(plan, sub.data(), (int32_t)sub.size(), 0.0, dirichlet, v, dt == 0 ? rhs : nullptr)) return st;
   }
   return FG_OK;
 }

@@ -27,7 +27,8 @@
 // (integral(m dof(u), tf(u))), "source" (integral(f, tf(u))), "damping" and
 // "inertia" (integral(c dt_dof(u), tf(u)) and integral(c dt2_dof(u), tf(u)),
 // at the angular frequency omega of the configuration), "mass_tf"
-// (integral(dof(u), m tf(u)), the coefficient on the test side), "dfull_0" ..
+// (integral(dof(u), m tf(u)), the coefficient on the test side), "separate"
+// (any program: assemble(separate = true), K, C and M written apart), "dfull_0" ..
 // "dfull_8" (integral(D grad(dof u), grad(tf u)) with the general tensor D,
 // row-major), "adv_0" .. "adv_2" (integral(b . grad(dof u), tf(u))), "vdof_0" ..
 // "vdof_2" (integral(b dof(u), grad(tf u))) or "vsrc_0" .. "vsrc_2"
@@ -226,6 +227,9 @@ void dumpField(F &u, Writer &w) {
 // pre(), assemble() (repeats times), then the outputs: the CSR pattern and
 // values, the right-hand side, the number of fields and each field's DOF
 // dictionary, the timings
+// assemble(separate = true) instead of assemble() (set by the "separate" program key)
+bool g_separate = false;
+
 template <class FORM, class... F>
 void run(FORM &formulation, int repeats, Writer &w, F &...fields) {
   using clock = std::chrono::steady_clock;
@@ -236,13 +240,20 @@ void run(FORM &formulation, int repeats, Writer &w, F &...fields) {
   for (int r = 0; r < std::max(1, repeats); ++r) {
     formulation.setSystemToZero();
     const auto a0 = clock::now();
-    common::Timer timer = formulation.assemble();
+    common::Timer timer = formulation.assemble(g_separate);
     const double wall = std::chrono::duration<double>(clock::now() - a0).count();
     if (r > 0 || repeats == 1) times.push_back(wall);
     (void)timer;
   }
-  algebra::MatrixCRSFast<T> A;
-  formulation.getLHS(A);
+  // separate matrices: K in place of the system matrix, C and M after the timings
+  algebra::MatrixCRSFast<T> A, Cm, Mm;
+  if (g_separate) {
+    formulation.getStiffness(A);
+    formulation.getDamping(Cm);
+    formulation.getMass(Mm);
+  } else {
+    formulation.getLHS(A);
+  }
   algebra::Vector<T> b;
   formulation.getRHS(b);
   const uint64_t n = A.size(0);
@@ -260,6 +271,13 @@ void run(FORM &formulation, int repeats, Writer &w, F &...fields) {
   w.f64(preSeconds);
   w.f64(median(times));
   w.u64(times.size());
+  w.u64(g_separate ? 2 : 0);
+  if (g_separate)
+    for (auto *X : {&Cm, &Mm}) {  // zeros for a matrix the module does not hold
+      std::vector<T> vals(nnz, T(0.0));
+      if (X->size(0) == n && n && X->ai()[n] == nnz) std::copy(X->a(), X->a() + nnz, vals.begin());
+      w.arr(vals.data(), nnz);
+    }
 }
 
 }  // namespace
@@ -327,6 +345,7 @@ int main(int argc, char **argv) {
     if (c.kind == FG_PROBLEM_HELMHOLTZ && argc == 23) {
       // the terms from the coefficient programs
       auto progs = readPrograms(argv[22]);
+      g_separate = progs.count("separate") != 0;
       const bool lagrange = c.space == FG_SPACE_LAGRANGE;
       field::Field<T, field::Form::Form0> u("u", omega,
                                             lagrange ? field::FunctionSpaceTypeForm0::Lagrange

@@ -110,6 +110,11 @@ def run(cfg, threads=0, repeats=1, timeout=3600, programs=None, dropin=False):
     out["timed_runs"] = int(take(np.uint64, 1)[0])
     out["threads"] = threads
     out["log"] = log
+    nsep = int(take(np.uint64, 1)[0])
+    if nsep:  # assemble(separate = true): values are K, then C and M
+        out["K"] = out["values"]
+        out["C"] = take(np.complex128, nnz)
+        out["M"] = take(np.complex128, nnz)
     if dropin:
         out["record"] = record or []
     assert pos == len(raw)
@@ -139,6 +144,7 @@ def read_record(path):
     calls = []
     while pos < len(raw):
         c = {}
+        c["entry"] = one(np.int32)  # 0: fg_assemble_fp64, 1: fg_assemble_separate
         c["dim"], c["nn"] = one(np.int32), one(np.int32)
         nodes = one(np.int64)
         c["xyz"] = take(np.float64, 3 * nodes).reshape(nodes, 3)

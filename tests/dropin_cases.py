@@ -25,6 +25,9 @@ def cases(F):
     """name -> (fg_problem_config, coefficient programs or None)"""
     _, _, progs = program_terms(F, "SQRT")
     return {
+        # the same terms as separate matrices K, C, M (assemble(separate = true), the MCK module)
+        "separate_mck": (F.config(dim=2, m=4, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=9, omega=1.7),
+                         dict(dt_programs(F), separate=[(F.FG_OP_CONST, 0, 1.0, 0.0)])),
         # time derivatives of the unknown at an angular frequency (the AFrequency module)
         "dt_terms": (F.config(dim=2, m=5, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=8, omega=1.7),
                      dt_programs(F)),
@@ -83,6 +86,18 @@ def oracle_assemble(oracle, call, terms):
     if call.get("unknown") is not None:
         return oracle.assemble_coupled(oracle_arrays(call), oracle_unknown_arrays(call), terms.arr, terms.n, call["frequency"])
     return oracle.assemble(oracle_arrays(call), terms.arr, terms.n, call["frequency"])
+
+
+def oracle_separate(F, oracle, call):
+    """K, C, M and the right-hand side (with K) of a recorded
+    fg_assemble_separate call: each group of terms by its time derivative,
+    without the frequency factor"""
+    out = []
+    for dt in range(3):
+        sub = dict(call, terms=[(k, 0) + tuple(t[2:]) for t in call["terms"] for k in [t[0]] if t[1] == dt])
+        t = Terms(F, sub)
+        out.append(oracle.assemble(oracle_arrays(sub), t.arr, t.n, 0.0))
+    return out[0][0], out[1][0], out[2][0], out[0][1]
 
 
 class Terms:
@@ -168,6 +183,15 @@ class ReplayPlan:
                                                   None))
         return v, r
 
+    def assemble_separate(self, terms):
+        """fg_assemble_separate: K, C, M, rhs"""
+        k, c, m = (np.zeros(self.nnz, np.complex128) for _ in range(3))
+        r = np.zeros(self.n_rows, np.complex128)
+        d = self.dir.ctypes.data if self.dir.size else None
+        self.F.check(self.L.fg_assemble_separate(self.ptr, terms.arr, terms.n, 0, d, k.ctypes.data, c.ctypes.data, m.ctypes.data,
+                                                 r.ctypes.data, None))
+        return k, c, m, r
+
     def close(self):
         self.L.fg_plan_destroy(self.ptr)
 
@@ -182,6 +206,8 @@ UNKNOWN_KEYS = ["nb", "n_orient", "form", "bval", "bgrad", "orient", "edof", "et
 def to_fixture(prefix, calls, ref):
     """flat npz entries of a case's recorded calls and the reference's result"""
     out = {prefix + "n_calls": np.asarray(len(calls)), prefix + "ref_values": ref["values"], prefix + "ref_rhs": ref["rhs"]}
+    if "C" in ref:  # separate matrices: values are K
+        out[prefix + "ref_C"], out[prefix + "ref_M"] = ref["C"], ref["M"]
     for k, call in enumerate(calls):
         out.update(_call_to_fixture("%s%d/" % (prefix, k), call))
     return out
@@ -189,6 +215,7 @@ def to_fixture(prefix, calls, ref):
 
 def _call_to_fixture(prefix, call):
     out = {prefix + k: np.asarray(call[k]) for k in FIXTURE_KEYS}
+    out[prefix + "entry"] = np.asarray(call.get("entry", 0))
     u = call.get("unknown")
     out[prefix + "coupled"] = np.asarray(0 if u is None else 1)
     if u is not None:
@@ -213,9 +240,15 @@ def _call_to_fixture(prefix, call):
 
 
 def from_fixture(z, prefix):
-    """(recorded calls, reference values, reference rhs) of a case from the npz"""
+    """(recorded calls, reference values, reference rhs) of a case from the npz;
+    for separate matrices the values are K"""
     calls = [_call_from_fixture(z, "%s%d/" % (prefix, k)) for k in range(int(z[prefix + "n_calls"]))]
     return calls, z[prefix + "ref_values"], z[prefix + "ref_rhs"]
+
+
+def separate_refs(z, prefix):
+    """the reference's C and M of a separate-matrices case, or None"""
+    return (z[prefix + "ref_C"], z[prefix + "ref_M"]) if prefix + "ref_C" in z.files else None
 
 
 def _call_from_fixture(z, prefix):
@@ -234,6 +267,7 @@ def _call_from_fixture(z, prefix):
         code, arrays = get(key)
         terms.append((kind, dt, code, arrays, [get("%s_tensor%d" % (key, k)) for k in range(nt)], get(key + "_coef2")))
     call["terms"] = terms
+    call["entry"] = int(z[prefix + "entry"])
     call["unknown"] = None
     if int(z[prefix + "coupled"]):
         call["unknown"] = {k: (z[prefix + "u_" + k].item() if z[prefix + "u_" + k].ndim == 0 else z[prefix + "u_" + k])

@@ -14,7 +14,7 @@ import os
 import numpy as np
 import pytest
 
-from dropin_cases import Terms, cases, from_fixture, oracle_assemble
+from dropin_cases import Terms, cases, from_fixture, oracle_assemble, oracle_separate, separate_refs
 from oracle import reference
 
 FIXTURE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "dropin.npz")
@@ -38,6 +38,7 @@ EXPECTED = {
     "navier_p2": [("ELASTIC", "ELEM"), ("MASS", "CONST")],
     "navier_p2_omega": [("ELASTIC", "ELEM"), ("MASS", "CONST")],
     "dt_terms": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT"), ("MASS", "POINT"), ("MASS", "CONST")],
+    "separate_mck": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT"), ("MASS", "POINT"), ("MASS", "CONST")],
     # one call per (test field, unknown field) block: u-u, u-v, v-u, v-v
     "coupled_p2": [[("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", None)], [("GRAD_GRAD", "CONST")],
                    [("MASS", "POINT"), ("ADVECTION", "CONST")], [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")]],
@@ -60,6 +61,10 @@ def test_dropin_matches_reference_assemble(femg, name):
         assert np.array_equal(ref["dof_" + k], drop["dof_" + k]), k
     assert rel(drop["values"], ref["values"]) <= 1e-13, rel(drop["values"], ref["values"])
     assert rel(drop["rhs"], ref["rhs"]) <= 1e-13, rel(drop["rhs"], ref["rhs"])
+    assert ("C" in drop) == ("C" in ref) == (name == "separate_mck")
+    if "C" in ref:  # separate matrices: values are K, and C, M apart
+        assert rel(drop["C"], ref["C"]) <= 1e-13 and rel(drop["M"], ref["M"]) <= 1e-13
+        assert np.abs(ref["C"]).max() > 0 and np.abs(ref["M"]).max() > 0
     calls = drop["record"]
     want = expected_calls(name)
     assert len(calls) == len(want)
@@ -68,9 +73,11 @@ def test_dropin_matches_reference_assemble(femg, name):
         assert got == [(getattr(femg, "FG_TERM_" + k), getattr(femg, "FG_OP_" + op) if op else None) for k, op in w]
         assert call["upper"] == (1 if name == "c1_upper" else 0)
     assert sum(c.get("unknown") is not None for c in calls) == (2 if name == "coupled_p2" else 0)
-    if name == "dt_terms":  # damping dt, inertia dt2, at the formulation's frequency
+    if name in ("dt_terms", "separate_mck"):  # damping dt, inertia dt2
         assert [t[1] for t in calls[0]["terms"]] == [0, 0, 0, femg.FG_DT_1, femg.FG_DT_2]
-        assert calls[0]["frequency"] == cfg.omega
+        assert calls[0]["entry"] == (1 if name == "separate_mck" else 0)
+        if name == "dt_terms":  # at the formulation's frequency
+            assert calls[0]["frequency"] == cfg.omega
 
 
 @pytest.mark.skipif(not reference.dropin_available(), reason="drop-in program not built (no reference tree)")
@@ -92,6 +99,12 @@ def test_dropin_refuses_what_it_does_not_map(femg):
 def test_recorded_calls_assemble_to_reference(femg, oracle, name):
     z = np.load(FIXTURE)
     calls, ref_v, ref_b = from_fixture(z, name + "/")
+    sep = separate_refs(z, name + "/")
+    if sep is not None:
+        assert len(calls) == 1 and calls[0]["entry"] == 1
+        k, c, m, b = oracle_separate(femg, oracle, calls[0])
+        assert rel(k, ref_v) <= 1e-13 and rel(c, sep[0]) <= 1e-13 and rel(m, sep[1]) <= 1e-13 and rel(b, ref_b) <= 1e-13
+        return
     v, b = 0.0, 0.0
     for call in calls:
         vk, bk = oracle_assemble(oracle, call, Terms(femg, call))

@@ -11,7 +11,7 @@ import os
 import numpy as np
 import pytest
 
-from dropin_cases import ReplayPlan, Terms, from_fixture
+from dropin_cases import ReplayPlan, Terms, from_fixture, separate_refs
 from test_dropin import EXPECTED, FIXTURE, expected_calls
 
 pytestmark = pytest.mark.gpu
@@ -25,7 +25,16 @@ def rel(a, b):
 @pytest.mark.parametrize("name", list(EXPECTED))
 def test_dropin_calls_match_reference(femg, cuda, name):
     assert os.path.exists(FIXTURE)
-    calls, ref_v, ref_b = from_fixture(np.load(FIXTURE), name + "/")
+    z = np.load(FIXTURE)
+    calls, ref_v, ref_b = from_fixture(z, name + "/")
+    sep = separate_refs(z, name + "/")
+    if sep is not None:  # fg_assemble_separate: K, C, M apart
+        t = Terms(femg, calls[0])
+        plan = ReplayPlan(femg, calls[0])
+        k, c, m, b = plan.assemble_separate(t)
+        assert rel(k, ref_v) <= 1e-12 and rel(c, sep[0]) <= 1e-12 and rel(m, sep[1]) <= 1e-12 and rel(b, ref_b) <= 1e-12
+        plan.close()
+        return
     fp64_only = {"GRAD_GRAD_TENSOR_FULL", "ADVECTION", "VECTOR_GRAD_TEST", "SOURCE_GRAD"}
     v, b, vm, bm, mixed = 0.0, 0.0, 0.0, 0.0, True
     for call, want in zip(calls, expected_calls(name)):
