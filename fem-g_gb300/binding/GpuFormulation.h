@@ -227,7 +227,11 @@ class GpuFormulation : public Formulation<T> {
       return -1;
     }
     if (nc == 1) return gl == gr ? (gl ? FG_TERM_GRAD_GRAD : FG_TERM_MASS) : -1;
-    if (!h1) return -1;
+    if (!h1) {  // HCurl: a symmetric tensor on the curls or on the values (the PML form)
+      if (nc == 9 && gl && gr) return FG_TERM_GRAD_GRAD_TENSOR;
+      if (nc == 9 && !gl && !gr) return FG_TERM_MASS_TENSOR;
+      return -1;
+    }
     if (nc == 3 && gl && !gr) return FG_TERM_ADVECTION;
     if (nc == 3 && !gl && gr) return FG_TERM_VECTOR_GRAD_TEST;
     if (nc == 9 && gl && gr) return FG_TERM_GRAD_GRAD_TENSOR_FULL;
@@ -602,13 +606,32 @@ class GpuFormulation : public Formulation<T> {
         describe(mu, E, nq, d.coef2, tables);
         continue;
       }
-      // a vector or tensor: coefficient 1 times one program per component
+      // a vector or tensor: coefficient 1 times one program per component.
+      // A symmetric tensor goes as its six entries xx, yy, zz, xy, xz, yz
+      // (the symmetric tensor kinds, one of each per call; on H1 fields that
+      // lets the tensor-core path take it); HCurl tensors must be symmetric
       d.coef.n_code = 1;
       d.coef.code[0] = fg_instr{FG_OP_CONST, 0, 1.0, 0.0};
-      tensors[t].resize(nc);
-      for (int k = 0; k < nc; ++k) {
+      std::vector<int> comps;
+      for (int k = 0; k < nc; ++k) comps.push_back(k);
+      if (nc == 9) {
+        bool sym = true;
+        for (size_t i = 0; i + 9 <= c.size() && sym; i += 9)
+          sym = c[i + 1] == c[i + 3] && c[i + 2] == c[i + 6] && c[i + 5] == c[i + 7];
+        const int symKind = d.kind == FG_TERM_MASS_TENSOR ? FG_TERM_MASS_TENSOR : FG_TERM_GRAD_GRAD_TENSOR;
+        bool taken = false;
+        for (size_t u = 0; u < t; ++u) taken = taken || terms[u].kind == symKind;
+        if (d.kind != FG_TERM_GRAD_GRAD_TENSOR_FULL && (!sym || taken))
+          throw std::runtime_error("an HCurl tensor coefficient that is not symmetric, or two of one kind");
+        if (sym && !taken) {
+          d.kind = symKind;
+          comps = {0, 4, 8, 1, 2, 5};
+        }
+      }
+      tensors[t].resize(comps.size());
+      for (size_t k = 0; k < comps.size(); ++k) {
         std::vector<T> ck(c.size() / nc);
-        for (size_t i = 0; i < ck.size(); ++i) ck[i] = c[i * nc + k];
+        for (size_t i = 0; i < ck.size(); ++i) ck[i] = c[i * nc + comps[k]];
         tensors[t][k] = fg_expr{};
         describe(ck, E, nq, tensors[t][k], tables);
       }

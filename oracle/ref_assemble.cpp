@@ -26,6 +26,8 @@
 // term "grad" (integral(g grad(dof u), grad(tf u))), "mass"
 // (integral(m dof(u), tf(u))), "source" (integral(f, tf(u))), "damping" and
 // "inertia" (integral(c dt_dof(u), tf(u)) and integral(c dt2_dof(u), tf(u)),
+// and for the Maxwell problem "dcurl_0" .. "dcurl_8" and "dmass_0" ..
+// "dmass_8" (integral(D curl(dof E), curl(tf E)), integral(D dof(E), tf(E))),
 // at the angular frequency omega of the configuration), "mass_tf"
 // (integral(dof(u), m tf(u)), the coefficient on the test side), "separate"
 // (any program: assemble(separate = true), K, C and M written apart), "dfull_0" ..
@@ -446,6 +448,18 @@ int main(int argc, char **argv) {
     } else if (c.kind == FG_PROBLEM_MAXWELL) {
       field::Field<T, field::Form::Form1> u("u", omega, field::FunctionSpaceTypeForm1::HierarchicalHCurl, c.order);
       FormulationOf<T> formulation("maxwell", matrixOptions);
+      std::map<std::string, std::vector<Instr>> progs;
+      if (argc == 23) progs = readPrograms(argv[22]);
+      auto tensorOf = [&](const std::string &name) {  // programs name_0 .. name_8, row-major
+        std::vector<function::ScalarFunction<T>> d;
+        for (int k = 0; k < 9; ++k) d.push_back(fromProgram(progs[name + "_" + std::to_string(k)]));
+        return function::tensor<T>(d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8]);
+      };
+      // anisotropic media: TensorFunction * curl and TensorFunction * dof (the PML form)
+      if (progs.count("dcurl_0"))
+        formulation.integral(tensorOf("dcurl") * equation::curl(equation::dof(u)), equation::curl(equation::tf(u)), omega, gauss);
+      if (progs.count("dmass_0"))
+        formulation.integral(tensorOf("dmass") * equation::dof(u), equation::tf(u), omega, gauss);
       formulation.integral(equation::curl(equation::dof(u)), equation::curl(equation::tf(u)), omega, gauss);
       if (c.coef_mode == FG_COEF_MODE_CONSTANT) {
         formulation.integral(function::ScalarFunction<T>(T(-c.k * c.k, 0.0)) * equation::dof(u), equation::tf(u), omega,

@@ -21,6 +21,12 @@ def dt_programs(F):
             "inertia": [(F.FG_OP_CONST, 0, 2.0, 0.0)]}
 
 
+def tensor_programs(F, name, rows):
+    """programs name_0 .. name_8 of the constant 3 x 3 tensor `rows` (complex entries)"""
+    return {"%s_%d" % (name, 3 * i + j): [(F.FG_OP_CONST, 0, complex(rows[i][j]).real, complex(rows[i][j]).imag)]
+            for i in range(3) for j in range(3)}
+
+
 def cases(F):
     """name -> (fg_problem_config, coefficient programs or None)"""
     _, _, progs = program_terms(F, "SQRT")
@@ -40,7 +46,7 @@ def cases(F):
         # point-dependent complex coefficients: mass sqrt(a(x, y)), source sqrt(a) / 2
         "sqrt_p2": (F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=3), progs),
         # HCurl order 1 (curl-curl and a per-element permittivity) on tets
-        "maxwell_p1": (F.config(kind=F.FG_PROBLEM_MAXWELL, dim=3, m=2, mesh_order=1, space=F.FG_SPACE_HCURL, order=1, gauss=4,
+        "maxwell_p1": (F.config(kind=F.FG_PROBLEM_MAXWELL, dim=3, m=1, mesh_order=1, space=F.FG_SPACE_HCURL, order=1, gauss=4,
                                 jitter=0.15, seed=7, k=3.0, coef_mode=1), None),
         # a general tensor diffusion and an advection (point-dependent, partly complex)
         "full_advect": (F.config(dim=2, m=5, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=6),
@@ -60,6 +66,15 @@ def cases(F):
         # the same with the frequency in the mass coefficient (-omega^2 rho dof(u))
         "navier_p2_omega": (F.config(kind=F.FG_PROBLEM_NAVIER, dim=3, m=1, mesh_order=1, space=F.FG_SPACE_HIERARCHICAL_H1,
                                      order=2, gauss=4, jitter=0.1, seed=3, omega=2.5, lame_sigma=0.3), None),
+        # a symmetric tensor diffusion: the six-entry kind, which the tensor-core path takes too
+        "sym_tensor": (F.config(dim=2, m=5, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=10),
+                       dict(tensor_programs(F, "dfull", [[1.2, 0.3, 0.1], [0.3, 0.9, -0.2], [0.1, -0.2, 1.1]]),
+                            mass=[(F.FG_OP_CONST, 0, -2.0, 0.0)])),
+        # anisotropic HCurl media (the PML form): complex symmetric tensors on the curls and the values
+        "maxwell_tensor": (F.config(kind=F.FG_PROBLEM_MAXWELL, dim=3, m=1, mesh_order=1, space=F.FG_SPACE_HCURL, order=1,
+                                    gauss=4, jitter=0.15, seed=11, k=2.0, coef_mode=0),
+                           dict(tensor_programs(F, "dcurl", [[1 + 0.2j, 0.1, 0], [0.1, 0.9 - 0.1j, 0], [0, 0, 1.1]]),
+                                **tensor_programs(F, "dmass", [[-1.5 + 0.3j, 0, 0.2], [0, -1.2, 0], [0.2, 0, -1.8 - 0.4j]]))),
         # symmetric storage
         "c1_upper": (F.config(dim=2, m=6, mesh_order=2, space=F.FG_SPACE_LAGRANGE, gauss=4, jitter=0.2, seed=4, k=3.0, source=1,
                               dirichlet=1, dirichlet_value=0.5, upper=1), None),

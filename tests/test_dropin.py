@@ -35,6 +35,8 @@ EXPECTED = {
     "full_advect": [("GRAD_GRAD_TENSOR_FULL", "CONST"), ("ADVECTION", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "vector_terms": [("VECTOR_GRAD_TEST", "CONST"), ("SOURCE_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
     "c1_upper": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT")],
+    "sym_tensor": [("GRAD_GRAD_TENSOR", "CONST"), ("MASS", "CONST")],
+    "maxwell_tensor": [("GRAD_GRAD_TENSOR", "CONST"), ("MASS_TENSOR", "CONST"), ("GRAD_GRAD", "CONST"), ("MASS", "CONST")],
     "navier_p2": [("ELASTIC", "ELEM"), ("MASS", "CONST")],
     "navier_p2_omega": [("ELASTIC", "ELEM"), ("MASS", "CONST")],
     "dt_terms": [("GRAD_GRAD", "CONST"), ("MASS", "CONST"), ("SOURCE", "POINT"), ("MASS", "POINT"), ("MASS", "CONST")],
