@@ -145,6 +145,7 @@ struct PlanDev {
   int32_t slotBytes;
   int32_t slotLd;         // slot row stride (entries)
   int32_t maxRowLen;
+  int32_t plainSlots;     // 1: no element row has two columns in one slot (plain shared adds are race-free)
   int *jmErr;             // set by the FP64 element kernels: an integration point outside a shell
   const double2 *lscale;  // [E][n] linked DOF coefficient (1 for other DOFs), or null without linked DOFs
   // The columns: the unknown field's DOFs. A plan of one field has them equal

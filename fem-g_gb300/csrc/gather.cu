@@ -225,7 +225,10 @@ __device__ __forceinline__ void gatherRowsV4(const PlanDev &p, const float *__re
       for (int c = 0; c < 4; ++c) {
         const uint32_t s = (sv >> (8 * c)) & 0xFFu;
         if (s < 0xFEu) {
-          atomicAdd(&A[s], vals[c]);  // distinct slots within an element row; rows ordered by __syncwarp
+          // an element row's columns sit in distinct slots unless the plan
+          // says otherwise; successive element rows are ordered by __syncwarp
+          if (p.plainSlots) A[s] += vals[c];
+          else atomicAdd(&A[s], vals[c]);
         } else if (s == 0xFFu) {
           // Dirichlet lifting with the transposed entry (addValuesDC, VectorFactory.cpp:184)
           const uint32_t e = flat / (uint32_t)n, i = flat - e * (uint32_t)n;

@@ -411,8 +411,17 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
   std::vector<uint8_t> slot8;
   std::vector<uint16_t> slot16;
   if (narrow) slot8.assign(nSlots, 0xFF); else slot16.assign(nSlots, kSlotIgnore);
-#pragma omp parallel for schedule(dynamic, 256) reduction(+ : bad)
+  int dup = 0;  // elements with two row columns on one DOF, or slots taken from the upper-storage lower_bound
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : bad, dup)
   for (int64_t e = 0; e < E; ++e) {
+    {
+      uint32_t cols[64];
+      int m = 0;
+      for (int j = 0; j < nc; ++j)
+        if (isRow(ctype[(size_t)e * nc + j])) cols[m++] = cdof[(size_t)e * nc + j];
+      std::sort(cols, cols + m);
+      if (std::adjacent_find(cols, cols + m) != cols + m) ++dup;
+    }
     for (int i = 0; i < n; ++i) {
       const size_t ki = (size_t)e * n + i;
       if (!isRow(etype[ki])) continue;
@@ -434,6 +443,7 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
             // larger index lacks the columns between the two; the reference
             // adds those entries at the lower_bound position without checking
             // it (MatrixFactory.cpp:267-268), and so does this map.
+            if (*p != J) ++dup;
             s = (uint16_t)(p - b);
           } else {
             ++bad;
@@ -450,6 +460,7 @@ static int createPlan(const fg_mesh_desc *mesh, const fg_rule_desc *rule, const 
     setLastError("fg_plan_create: an element DOF pair is missing from the CSR pattern");
     return FG_ERR_INDEX;
   }
+  d.plainSlots = dup == 0;
   if (nS > nc)
     for (size_t r = 0; r < (size_t)E * n; ++r)
       std::fill(slot8.begin() + (int64_t)(r * nS + nc), slot8.begin() + (int64_t)((r + 1) * nS), (uint8_t)0xFE);
