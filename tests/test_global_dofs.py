@@ -58,6 +58,67 @@ def merged_system(femg, oracle, name):
     return prob, a, b, newrow
 
 
+# order-3 tetrahedra (20 DOFs per element, rows under 254 entries): the
+# vector-load reduction of the mixed path takes them, five lanes per element
+# row, lane l owning columns 4l .. 4l + 3
+PAIR_CFG = dict(dim=3, m=3, mesh_order=1, space=1, order=3, gauss=6, jitter=0.15, seed=5, k=3.0, source=1)
+# local DOF 0 (vertex 0, lane 0) and local DOF 4 (the first DOF of edge
+# (0, 1), lane 1): every element around that edge holds vertex 0, so the
+# merged row is no longer than the vertex's own
+PAIR_LOCAL = (0, 4)
+
+
+def pair_merged_system(femg, oracle, every=5):
+    """DOF pairs merged into global rows: for every `every`-th element whose
+    local DOFs PAIR_LOCAL are still free, those two DOFs become one row, so
+    that the element has two columns (and two local rows) on one CSR row and
+    one slot, held by two lanes of the vector-load reduction.
+    (problem, arrays, merged arrays, map old row -> new row)"""
+    prob = femg.Problem(femg.config(**PAIR_CFG))
+    a = prob.arrays()
+    n = int(a["n_rows"])
+    edof = a["edof"].astype(np.int64)
+    etype = a["etype"].copy()
+    rows = (etype == femg.FG_AT_UNKNOWN) | (etype == femg.FG_AT_UNKNOWN_BUBBLE)
+    target = np.arange(n)
+    used = np.zeros(n, bool)
+    for e in range(0, edof.shape[0], every):
+        a0, a1 = PAIR_LOCAL
+        if not (rows[e, a0] and rows[e, a1]):
+            continue
+        i, j = edof[e, a0], edof[e, a1]
+        if used[i] or used[j]:
+            continue
+        used[i] = used[j] = True
+        target[max(i, j)] = min(i, j)
+    keep = np.flatnonzero(target == np.arange(n))
+    newrow = np.empty(n, np.int64)
+    newrow[keep] = np.arange(len(keep))
+    newrow = newrow[target]
+    e2 = edof.copy()
+    e2[rows] = newrow[edof[rows]]
+    etype[rows & used[np.where(rows, edof, 0)]] = AT_UNKNOWN_GLOBAL
+    m = len(keep)
+    ai, aj = oracle.pattern(e2.astype(np.uint64), etype, m)
+    b = dict(a, edof=e2.astype(np.uint64), etype=etype, n_rows=m, ai=ai, aj=aj)
+    return prob, a, b, newrow
+
+
+def test_oracle_pairs_equal_lumped_system(femg, oracle):
+    prob, a, b, newrow = pair_merged_system(femg, oracle)
+    e2 = b["edof"].astype(np.int64)
+    assert (e2[:, PAIR_LOCAL[0]] == e2[:, PAIR_LOCAL[1]]).sum() >= 10  # elements with two columns on one row
+    assert np.diff(b["ai"].astype(np.int64)).max() < 254  # one-byte slots
+    t, nt = prob.terms()
+    v, r = oracle.assemble(a, t, nt)
+    vm, rm = oracle.assemble(b, t, nt)
+    n, m = int(a["n_rows"]), int(b["n_rows"])
+    P = np.zeros((n, m))
+    P[np.arange(n), newrow] = 1.0
+    assert rel(csr_dense(b["ai"], b["aj"], vm, m), P.T @ csr_dense(a["ai"], a["aj"], v, n) @ P) <= 1e-13
+    assert rel(rm, P.T @ r) <= 1e-13
+
+
 def csr_dense(ai, aj, v, n):
     A = np.zeros((n, n), np.complex128)
     r = np.repeat(np.arange(n), np.diff(ai.astype(np.int64)))
